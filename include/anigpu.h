@@ -1,0 +1,166 @@
+/* anigpu -- GB300-native element-matrix assembly, CSR scatter and Krylov solve for
+ * tetrahedral finite elements.  C ABI: plain pointers and sizes, int status codes,
+ * no exceptions across the boundary.  All array arguments are DEVICE pointers unless
+ * the parameter name ends in _host.  One CUDA stream per handle; a handle is not
+ * thread-safe, distinct handles are.
+ *
+ * Each entry point names the reference interface it replaces (AniFem++,
+ * INMOST-DEV/INMOST-FEM; paths relative to that project).
+ */
+#ifndef ANIGPU_H
+#define ANIGPU_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes.  -1/-2 keep the meaning of AssemblerT::Assemble's status
+ * (anifem++/inmost_interface/assembler.inl:306-313). */
+#define ANIGPU_OK 0
+#define ANIGPU_ERR_NONFINITE (-1)     /* a non-finite element value was produced */
+#define ANIGPU_ERR_BAD_ELEMENT (-2)   /* degenerate / broken element */
+#define ANIGPU_ERR_ARG (-3)           /* invalid argument or size */
+#define ANIGPU_ERR_UNSUPPORTED (-4)   /* operator pair, order or tensor kind not provided */
+#define ANIGPU_ERR_CUDA (-5)          /* a CUDA runtime call failed */
+#define ANIGPU_ERR_NOT_CONVERGED (-6) /* Krylov solve hit maxit or stagnated */
+#define ANIGPU_ERR_STATE (-7)         /* call order violated (e.g. assemble before setup) */
+#define ANIGPU_ERR_TIMEOUT (-8)       /* a bounded device-side wait expired */
+
+/* ---- spaces and operators: code = 10*space + op (Ani::FiniteElement / Ani::OperatorType,
+ * anifem++/fem/operators.h:25-45; FemVec<3,.> as anifem++/fem/operators.h:63-67,127-155) */
+#define ANIGPU_P0 0
+#define ANIGPU_P1 1
+#define ANIGPU_P2 2
+#define ANIGPU_P3 3
+#define ANIGPU_VEC3_P1 4
+#define ANIGPU_VEC3_P2 5
+#define ANIGPU_IDEN 1
+#define ANIGPU_GRAD 2
+#define ANIGPU_OP(space, op) (10 * (space) + (op))
+
+/* ---- coefficient tensor kinds (Ani::TensorType + DfuncTraits sparsity,
+ * anifem++/fem/diff_tensor.h:17-53).  Tensor data layouts:
+ *   NULL          no data (identity, or a column of ones when dim(OpA) == 1)
+ *   CONST_SCALAR  1 value for all tets
+ *   TET_SCALAR    nt values
+ *   TET_SYM       6 values per tet: d00 d01 d02 d11 d12 d22 (3x3 operators only)
+ *   TET_GENERAL   dimB*dimA per tet, column-major dimB x dimA (the layout the user
+ *                 functor writes, int_tet_test.cpp:218)
+ *   POINT         dimB*dimA per (tet, quadrature point), column-major, points in the order
+ *                 of anigpu_quadrature() (the PerPoint functor evaluated at
+ *                 anigpu_quadrature_points(), diff_tensor.h:488-552) */
+#define ANIGPU_TENSOR_NULL 0
+#define ANIGPU_TENSOR_CONST_SCALAR 1
+#define ANIGPU_TENSOR_TET_SCALAR 2
+#define ANIGPU_TENSOR_TET_SYM 3
+#define ANIGPU_TENSOR_TET_GENERAL 4
+#define ANIGPU_TENSOR_POINT 5
+
+/* ---- arithmetic of element matrices / CSR values */
+#define ANIGPU_F64 0
+#define ANIGPU_F32 1
+
+/* ---- Krylov methods (replacing INMOST Solver, examples/tutorials/ex1.cpp:161-163) */
+#define ANIGPU_SOLVE_JACOBI_PCG 0 /* FP64 Jacobi-preconditioned CG */
+#define ANIGPU_SOLVE_IR_CG32 1    /* FP32-SpMV Jacobi-CG inside FP64 iterative refinement */
+#define ANIGPU_SOLVE_FCG_LEARNED 2 /* flexible CG, learned preconditioner, Jacobi fallback */
+
+typedef struct anigpu_ctx* anigpu_handle;
+
+typedef struct anigpu_solve_stats {
+    int64_t iterations;       /* total inner Krylov iterations */
+    int64_t outer_iterations; /* refinement steps (IR / FCG restarts) */
+    double rel_residual;      /* final FP64 ||b - A x|| / ||b|| */
+    double seconds;           /* wall time of the solve (device events) */
+    int64_t fallback_steps;   /* FCG steps that fell back to Jacobi */
+} anigpu_solve_stats;
+
+/* ---- lifetime */
+int anigpu_create(anigpu_handle* h, int device);
+int anigpu_destroy(anigpu_handle h);
+/* run the handle's work on an existing stream (cudaStream_t), 0 = the handle's own */
+int anigpu_set_stream(anigpu_handle h, void* stream);
+const char* anigpu_last_error(anigpu_handle h);
+/* kernels launched by this handle since creation (evidence for bench reports) */
+int64_t anigpu_launch_count(anigpu_handle h);
+
+/* ---- element level: the fused batch of Ani::fem3Dtet
+ * (anifem++/fem/operations/int_tet.h:17-29, int_tet.inl:30-57,93-122; the FUSION batch of
+ * TetrasT columns becomes the whole device batch).
+ *   XY: nt*12 doubles, per tet X0 X1 X2 X3 (3 each), the TetrasT columns
+ *   D : tensor data by kind (see above), doubles
+ *   A : nt * nfB * nfA values (F64 or F32 by precision), per tet column-major nfB x nfA,
+ *       A(i_test, j_trial), exactly the DenseMatrix A of fem3Dtet
+ *   order: quadrature order 0..6 (the stack-memory fem3Dtet limit, int_tet.inl:98-99) */
+int anigpu_fem3dtet(anigpu_handle h, int opA, int opB, int tensor_kind, int order, int precision, int64_t nt,
+                    const double* XY, const double* D, void* A);
+/* quadrature rule (host arrays): p[4*np] barycentric, w[np] summing to 1; returns np or <0
+ * (replaces tetrahedron_quadrature_formulas, anifem++/fem/quadrature_formulas.cpp:526) */
+int anigpu_quadrature(int order, double* p_host, double* w_host, int cap);
+/* physical quadrature points XYG[nt][q][3] (internalFem3DtetGeomInit_XYG, core.inl:249-269) */
+int anigpu_quadrature_points(anigpu_handle h, int order, int64_t nt, const double* XY, double* XYG);
+/* element-level Dirichlet on a batch of element matrices (Ani::applyDir,
+ * anifem++/fem/operations/dc_on_dof.h:39-45): for every tet t and local DOF k with bit k of
+ * mask[t] set, applies applyDir(A_t, F_t, k, bc[t*n + k]) in ascending k.  A: F64, n x n. */
+int anigpu_apply_dir(anigpu_handle h, int64_t nt, int n, double* A, double* F, const uint32_t* mask,
+                     const double* bc);
+
+/* ---- mesh and global problem (AssemblerT, anifem++/inmost_interface/assembler.h:316-386)
+ * mesh_upload: coordinates xyz[nv*3] (f64) and tets[nt*4] (i32) -- device pointers; the
+ * library keeps its own copies, with every tet reoriented like reorderNodesOnTetrahedron
+ * (anifem++/inmost_interface/ordering.inl:9-26). */
+int anigpu_mesh_upload(anigpu_handle h, int64_t nv, const double* xyz, int64_t nt, const int32_t* tets);
+/* replace the coordinates only (moving mesh), same topology */
+int anigpu_mesh_update_coords(anigpu_handle h, const double* xyz);
+/* space: ANIGPU_P1, ANIGPU_P2 or ANIGPU_VEC3_P2.  Builds the NATURAL DOF numbering
+ * (GlobEnumeration default, global_enumerator.h:392-404: vertex DOFs by vertex id, then edge
+ * DOFs by edge id, edges ranked by (min vertex, max vertex); FemVec component-major), the
+ * topological CSR template (AssembleTemplate, assembler.inl:590-693: sorted rows, diagonal
+ * forced) and the row-gather scatter records.  All on the device. */
+int anigpu_problem_setup(anigpu_handle h, int space);
+int anigpu_problem_info(anigpu_handle h, int64_t* ndof, int64_t* nnz, int64_t* nedges);
+/* copy the template out: rowptr[ndof+1] (i64), col[nnz] (i32) -- device pointers */
+int anigpu_csr_template(anigpu_handle h, int64_t* rowptr, int32_t* col);
+/* element DOF table edofs[nt*nloc] (i32, device) */
+int anigpu_element_dofs(anigpu_handle h, int32_t* edofs);
+/* coordinates of every DOF's node: xyz[ndof*3] (f64, device).  Vertex DOFs sit at the
+ * vertex, P2 edge DOFs at the edge midpoint (DOF_coord<FEM_P2>, anifem++/fem/operators.h:750-767);
+ * vector components repeat the scalar coordinates. */
+int anigpu_dof_coords(anigpu_handle h, double* xyz);
+/* Dirichlet DOFs: mask[ndof] (u8, nonzero = Dirichlet), bc[ndof] (f64) or NULL for zero */
+int anigpu_set_dirichlet(anigpu_handle h, const uint8_t* mask, const double* bc);
+
+/* Global assembly (AssemblerT::Assemble, assembler.inl:314-487) of
+ *   A = sum_T fem3Dtet<GRAD space, GRAD space>(T, D_T)     (element matrices)
+ *   b = sum_T fem3Dtet<IDEN P0, IDEN space>(T, f_T)         (right-hand side)
+ * with applyDir on Dirichlet DOFs, into the template: vals[nnz] (F64/F32 by precision),
+ * rhs[ndof] (f64).  tensor_kind: NULL, CONST_SCALAR, TET_SCALAR, TET_SYM for scalar spaces;
+ * for ANIGPU_VEC3_P2: TET_GENERAL (9x9 per tet) or ANIGPU_TENSOR_LAME (2 per tet: lambda, mu).
+ * f: per-tet source (f64[nt]) or NULL for f = f_const.  order: quadrature order of both integrals
+ * (0..6, as fem3Dtet's `order`).  touched (u8[nnz], optional) marks
+ * every slot that received |a| > drop_val (assembler.inl:416-418); NULL skips it.
+ * Deterministic: every CSR value is summed in ascending tet order, no atomics.
+ * Returns ANIGPU_ERR_NONFINITE when a value is not finite (assembler.inl:419-423). */
+#define ANIGPU_TENSOR_LAME 7
+int anigpu_assemble(anigpu_handle h, int tensor_kind, const double* D, const double* f, double f_const, int order,
+                    int precision, void* vals, double* rhs, uint8_t* touched, double drop_val);
+/* the drop-rule pattern (assembler without template): keep touched slots and the diagonal
+ * (set_elements_on_matrix_diagonal, assembler.inl:114-135).  In-place on rowptr/col/vals;
+ * returns the new nnz through nnz_out. */
+int anigpu_csr_compact(anigpu_handle h, int64_t* rowptr, int32_t* col, void* vals, int precision,
+                       const uint8_t* touched, int64_t* nnz_out);
+
+/* ---- Krylov solve on the handle's CSR template with given values.
+ * vals: F64 (JACOBI_PCG) or the values in `precision`; b, x: f64[ndof] (x is the initial guess
+ * and the result).  Convergence: ||b - A x||_2 <= rtol * ||b||_2 in FP64. */
+int anigpu_solve(anigpu_handle h, int method, const void* vals, int precision, const double* b, double* x,
+                 double rtol, int64_t maxit, anigpu_solve_stats* stats);
+/* y = A x on the handle's template (F64 or F32 values, f64 vectors) */
+int anigpu_spmv(anigpu_handle h, const void* vals, int precision, const double* x, double* y);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ANIGPU_H */

@@ -1,0 +1,292 @@
+"""anigpu: Python host binding of the anigpu C ABI (include/anigpu.h).
+
+The classes mirror the reference's interfaces for the hot path:
+  * ``Anigpu.fem3dtet``      -- Ani::fem3Dtet over a batch of tets
+                                (anifem++/fem/operations/int_tet.h:17-29)
+  * ``Anigpu.mesh_upload`` / ``problem_setup`` / ``assemble``
+                             -- AssemblerT::PrepareProblem / Assemble
+                                (anifem++/inmost_interface/assembler.h:316-386)
+  * ``Anigpu.solve``         -- the Krylov solve that consumes the matrix
+All numerics run in libanigpu.so on the GPU.  There is no CPU fallback: importing works
+anywhere, but creating a handle raises when the library or a CUDA device is missing.
+Device buffers are torch CUDA tensors (plumbing only); the library sees raw pointers.
+"""
+import ctypes
+import os
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG_DIR, "libanigpu.so")
+
+# ---- constants (include/anigpu.h)
+OK = 0
+ERR_NONFINITE, ERR_BAD_ELEMENT, ERR_ARG, ERR_UNSUPPORTED, ERR_CUDA, ERR_NOT_CONVERGED, ERR_STATE, ERR_TIMEOUT = (
+    -1, -2, -3, -4, -5, -6, -7, -8)
+P0, P1, P2, P3, VEC3_P1, VEC3_P2 = 0, 1, 2, 3, 4, 5
+IDEN, GRAD = 1, 2
+TENSOR_NULL, TENSOR_CONST_SCALAR, TENSOR_TET_SCALAR, TENSOR_TET_SYM, TENSOR_TET_GENERAL, TENSOR_POINT = range(6)
+TENSOR_LAME = 7
+F64, F32 = 0, 1
+SOLVE_JACOBI_PCG, SOLVE_IR_CG32, SOLVE_FCG_LEARNED = 0, 1, 2
+
+# every entry point the header declares: name -> (restype, argtypes)
+_vp, _i, _i64, _d = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_double
+
+
+class SolveStats(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int64), ("outer_iterations", ctypes.c_int64),
+                ("rel_residual", ctypes.c_double), ("seconds", ctypes.c_double),
+                ("fallback_steps", ctypes.c_int64)]
+
+
+SIGNATURES = {
+    "anigpu_create": (_i, [ctypes.POINTER(_vp), _i]),
+    "anigpu_destroy": (_i, [_vp]),
+    "anigpu_set_stream": (_i, [_vp, _vp]),
+    "anigpu_last_error": (ctypes.c_char_p, [_vp]),
+    "anigpu_launch_count": (_i64, [_vp]),
+    "anigpu_fem3dtet": (_i, [_vp, _i, _i, _i, _i, _i, _i64, _vp, _vp, _vp]),
+    "anigpu_quadrature": (_i, [_i, _vp, _vp, _i]),
+    "anigpu_quadrature_points": (_i, [_vp, _i, _i64, _vp, _vp]),
+    "anigpu_apply_dir": (_i, [_vp, _i64, _i, _vp, _vp, _vp, _vp]),
+    "anigpu_mesh_upload": (_i, [_vp, _i64, _vp, _i64, _vp]),
+    "anigpu_mesh_update_coords": (_i, [_vp, _vp]),
+    "anigpu_problem_setup": (_i, [_vp, _i]),
+    "anigpu_problem_info": (_i, [_vp, ctypes.POINTER(_i64), ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
+    "anigpu_csr_template": (_i, [_vp, _vp, _vp]),
+    "anigpu_element_dofs": (_i, [_vp, _vp]),
+    "anigpu_dof_coords": (_i, [_vp, _vp]),
+    "anigpu_set_dirichlet": (_i, [_vp, _vp, _vp]),
+    "anigpu_assemble": (_i, [_vp, _i, _vp, _vp, _d, _i, _i, _vp, _vp, _vp, _d]),
+    "anigpu_csr_compact": (_i, [_vp, _vp, _vp, _vp, _i, _vp, ctypes.POINTER(_i64)]),
+    "anigpu_solve": (_i, [_vp, _i, _vp, _i, _vp, _vp, _d, _i64, ctypes.POINTER(SolveStats)]),
+    "anigpu_spmv": (_i, [_vp, _vp, _i, _vp, _vp]),
+}
+
+_LIB = None
+
+
+def load_library(path=None):
+    """Load libanigpu.so (raises OSError when it is missing: there is no fallback)."""
+    global _LIB
+    if _LIB is not None and path is None:
+        return _LIB
+    lib = ctypes.CDLL(path or LIB_PATH)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _LIB = lib
+    return lib
+
+
+def build(verbose=False, force=False):
+    from . import _build
+    return _build.build_library(verbose=verbose, force=force)
+
+
+class AnigpuError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"anigpu error {code}: {msg}")
+        self.code = code
+
+
+def op_info(code):
+    """(nf, dim) of operator code 10*space + op (Operator<OP, FEM>::Nfa / Dim)."""
+    space, op = divmod(code, 10)
+    nfs = {P0: 1, P1: 4, P2: 10, P3: 20, VEC3_P1: 4, VEC3_P2: 10}[space]
+    nc = 3 if space in (VEC3_P1, VEC3_P2) else 1
+    bd = 1 if op == IDEN else 3
+    return nfs * nc, bd * nc
+
+
+def quadrature(order):
+    """(points[np,4], weights[np]) -- tetrahedron_quadrature_formulas(order)."""
+    import numpy as np
+    lib = load_library()
+    p = np.zeros(4 * 64)
+    w = np.zeros(64)
+    n = lib.anigpu_quadrature(order, p.ctypes.data, w.ctypes.data, 64)
+    if n < 0:
+        raise AnigpuError(n, f"no quadrature rule of order {order}")
+    return p[:4 * n].reshape(n, 4).copy(), w[:n].copy()
+
+
+def _ptr(t):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+class Anigpu:
+    """One library handle: one device, one stream (the caller's torch stream by default)."""
+
+    def __init__(self, device=0, use_torch_stream=True):
+        import torch
+        if not torch.cuda.is_available():
+            raise RuntimeError("anigpu needs a CUDA device (no CPU fallback)")
+        self.torch = torch
+        self.lib = load_library()
+        self.device = device
+        h = ctypes.c_void_p()
+        self._check(self.lib.anigpu_create(ctypes.byref(h), device), None)
+        self.h = h
+        if use_torch_stream:
+            with torch.cuda.device(device):
+                self.set_stream(torch.cuda.current_stream().cuda_stream)
+        self.space = None
+
+    # -------------------------------------------------------------- plumbing
+    def _check(self, rc, h="self"):
+        if rc < 0:
+            hh = self.h if h == "self" else h
+            msg = self.lib.anigpu_last_error(hh).decode() if hh is not None else ""
+            raise AnigpuError(rc, msg)
+        return rc
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            self.lib.anigpu_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_handle):
+        self._check(self.lib.anigpu_set_stream(self.h, ctypes.c_void_p(stream_handle)))
+
+    def launch_count(self):
+        return int(self.lib.anigpu_launch_count(self.h))
+
+    def _dev(self, a, dtype):
+        """numpy array or tensor -> contiguous CUDA tensor of dtype."""
+        torch = self.torch
+        if a is None:
+            return None
+        if not isinstance(a, torch.Tensor):
+            a = torch.as_tensor(a)
+        return a.to(device=f"cuda:{self.device}", dtype=dtype).contiguous()
+
+    # -------------------------------------------------------------- element level
+    def fem3dtet(self, opA, opB, XY, D=None, kind=TENSOR_NULL, order=5, precision=F64, out=None):
+        """Element matrices of a batch of tets: A[nt, nfA, nfB] whose per-tet memory is the
+        column-major nfB x nfA DenseMatrix of fem3Dtet (so A[t].T is A(i_test, j_trial))."""
+        torch = self.torch
+        XY = self._dev(XY, torch.float64)
+        nt = XY.numel() // 12
+        nfA, _ = op_info(opA)
+        nfB, _ = op_info(opB)
+        dt = torch.float64 if precision == F64 else torch.float32
+        if out is None:
+            out = torch.empty((nt, nfA, nfB), dtype=dt, device=XY.device)
+        Dd = self._dev(D, torch.float64) if D is not None else None
+        self._check(self.lib.anigpu_fem3dtet(self.h, opA, opB, kind, order, precision, nt, _ptr(XY), _ptr(Dd),
+                                             _ptr(out)))
+        return out
+
+    def quadrature_points(self, order, XY):
+        torch = self.torch
+        XY = self._dev(XY, torch.float64)
+        nt = XY.numel() // 12
+        q = quadrature(order)[1].size
+        out = torch.empty((nt, q, 3), dtype=torch.float64, device=XY.device)
+        self._check(self.lib.anigpu_quadrature_points(self.h, order, nt, _ptr(XY), _ptr(out)))
+        return out
+
+    def apply_dir(self, A, F, mask, bc=None):
+        torch = self.torch
+        nt, n = F.shape[0], F.shape[1]
+        m = self._dev(mask, torch.int32)
+        b = self._dev(bc, torch.float64) if bc is not None else None
+        self._check(self.lib.anigpu_apply_dir(self.h, nt, n, _ptr(A), _ptr(F), _ptr(m), _ptr(b)))
+
+    # -------------------------------------------------------------- global problem
+    def mesh_upload(self, xyz, tets):
+        torch = self.torch
+        self._xyz = self._dev(xyz, torch.float64)
+        self._tets = self._dev(tets, torch.int32)
+        self.nv = self._xyz.numel() // 3
+        self.nt = self._tets.numel() // 4
+        self._check(self.lib.anigpu_mesh_upload(self.h, self.nv, _ptr(self._xyz), self.nt, _ptr(self._tets)))
+
+    def update_coords(self, xyz):
+        self._xyz = self._dev(xyz, self.torch.float64)
+        self._check(self.lib.anigpu_mesh_update_coords(self.h, _ptr(self._xyz)))
+
+    def problem_setup(self, space):
+        self._check(self.lib.anigpu_problem_setup(self.h, space))
+        self.space = space
+        nd, nz, ne = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        self._check(self.lib.anigpu_problem_info(self.h, ctypes.byref(nd), ctypes.byref(nz), ctypes.byref(ne)))
+        self.ndof, self.nnz, self.nedges = nd.value, nz.value, ne.value
+        return self.ndof, self.nnz
+
+    def csr_template(self):
+        torch = self.torch
+        rp = torch.empty(self.ndof + 1, dtype=torch.int64, device=f"cuda:{self.device}")
+        col = torch.empty(self.nnz, dtype=torch.int32, device=f"cuda:{self.device}")
+        self._check(self.lib.anigpu_csr_template(self.h, _ptr(rp), _ptr(col)))
+        return rp, col
+
+    def element_dofs(self):
+        torch = self.torch
+        nloc = 4 if self.space == P1 else 10
+        e = torch.empty((self.nt, nloc), dtype=torch.int32, device=f"cuda:{self.device}")
+        self._check(self.lib.anigpu_element_dofs(self.h, _ptr(e)))
+        return e
+
+    def dof_coords(self):
+        torch = self.torch
+        c = torch.empty((self.ndof, 3), dtype=torch.float64, device=f"cuda:{self.device}")
+        self._check(self.lib.anigpu_dof_coords(self.h, _ptr(c)))
+        return c
+
+    def set_dirichlet(self, mask=None, bc=None):
+        torch = self.torch
+        self._dmask = self._dev(mask, torch.uint8) if mask is not None else None
+        self._dbc = self._dev(bc, torch.float64) if bc is not None else None
+        self._check(self.lib.anigpu_set_dirichlet(self.h, _ptr(self._dmask), _ptr(self._dbc)))
+
+    def assemble(self, kind=TENSOR_NULL, D=None, f=None, f_const=1.0, order=2, precision=F64, vals=None, rhs=None,
+                 touched=False, drop=1e-100):
+        """AssemblerT::Assemble: returns (vals[nnz], rhs[ndof], touched[nnz] or None)."""
+        torch = self.torch
+        dev = f"cuda:{self.device}"
+        dt = torch.float64 if precision == F64 else torch.float32
+        if vals is None:
+            vals = torch.empty(self.nnz, dtype=dt, device=dev)
+        if rhs is None:
+            rhs = torch.empty(self.ndof, dtype=torch.float64, device=dev)
+        tch = torch.empty(self.nnz, dtype=torch.uint8, device=dev) if touched else None
+        Dd = self._dev(D, torch.float64) if D is not None else None
+        fd = self._dev(f, torch.float64) if f is not None else None
+        self._check(self.lib.anigpu_assemble(self.h, kind, _ptr(Dd), _ptr(fd), float(f_const), order, precision,
+                                             _ptr(vals), _ptr(rhs), _ptr(tch), float(drop)))
+        return vals, rhs, tch
+
+    def csr_compact(self, rowptr, col, vals, precision, touched):
+        n = ctypes.c_int64()
+        self._check(self.lib.anigpu_csr_compact(self.h, _ptr(rowptr), _ptr(col), _ptr(vals), precision,
+                                                _ptr(touched), ctypes.byref(n)))
+        return n.value
+
+    def spmv(self, vals, x, precision=F64):
+        torch = self.torch
+        x = self._dev(x, torch.float64)
+        y = torch.empty_like(x)
+        self._check(self.lib.anigpu_spmv(self.h, _ptr(vals), precision, _ptr(x), _ptr(y)))
+        return y
+
+    def solve(self, vals, b, method=SOLVE_JACOBI_PCG, precision=F64, x0=None, rtol=1e-10, maxit=100000,
+              check=True):
+        """Returns (x, stats).  stats: SolveStats (iterations, outer_iterations, rel_residual, seconds)."""
+        torch = self.torch
+        b = self._dev(b, torch.float64)
+        x = torch.zeros_like(b) if x0 is None else self._dev(x0, torch.float64).clone()
+        st = SolveStats()
+        rc = self.lib.anigpu_solve(self.h, method, _ptr(vals), precision, _ptr(b), _ptr(x), float(rtol), int(maxit),
+                                   ctypes.byref(st))
+        if check:
+            self._check(rc)
+        return x, st

@@ -1,0 +1,151 @@
+// Internal declarations shared by the anigpu translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/anigpu.h"
+
+#define ANIGPU_MAX_NF 30
+#define ANIGPU_MAX_DIM 9
+#define ANIGPU_MAX_Q 24
+
+// ------------------------------------------------------------------ basis tables (host)
+// Reference-element data of one scalar space at the points of one quadrature rule.
+struct ScalarBasisTable {
+    int space = -1, order = -1, q = 0, nf = 0;
+    std::vector<double> pts, wts;   // 4*q barycentric, q weights (sum 1)
+    std::vector<double> val;        // val[n*nf + i]
+    std::vector<double> grad;       // grad[(n*nf + i)*3 + d]  d/dxi_d of phi_i
+};
+bool make_scalar_basis(int space, int order, ScalarBasisTable* t);
+int scalar_space_nf(int space);
+// op code helpers (code = 10*space + op)
+bool op_info(int code, int* nf, int* dim, int* base_space, int* ncomp, int* op);
+
+// ------------------------------------------------------------------ device records
+// One scatter record per (row DOF, incident tet): the tet, the row's local index in
+// the tet, the tet's Dirichlet local DOFs and, for each local DOF j of the tet, the
+// offset of its column within the row (8 bits each).
+//   x: tet id
+//   y: bits 0-3 local index i, bits 4-13 Dirichlet mask (local j), bits 16-31 offsets j=8,9
+//   z: offsets j=0..3, w: offsets j=4..7 (8 bits each, little end first)
+struct __align__(16) ScatterRec {
+    uint32_t tet, meta, off03, off47;
+};
+
+// ------------------------------------------------------------------ context
+struct anigpu_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaStream_t own_stream = nullptr;
+    std::string err;
+    int64_t launches = 0;
+
+    // mesh
+    int64_t nv = 0, nt = 0;
+    double* xyz = nullptr;    // nv*3
+    int32_t* tets = nullptr;  // nt*4 (oriented)
+
+    // problem
+    int space = -1;      // ANIGPU_P1 / ANIGPU_P2 / ANIGPU_VEC3_P2
+    int nloc_s = 0;      // scalar local DOFs per tet (4 or 10)
+    int ncomp = 1;
+    int64_t ne = 0;      // edges
+    int64_t nds = 0;     // scalar DOFs
+    int64_t ndof = 0;    // DOFs (ncomp * nds)
+    int64_t nnz_s = 0;   // scalar template nnz
+    int64_t nnz = 0;     // template nnz
+    int32_t* tet_edges = nullptr;  // nt*6
+    int32_t* edofs = nullptr;      // nt*nloc_s (scalar DOFs)
+    int64_t* rowptr_s = nullptr;   // nds+1
+    int32_t* col_s = nullptr;      // nnz_s
+    int64_t* rowptr = nullptr;     // ndof+1 (== rowptr_s for scalar spaces)
+    int32_t* col = nullptr;        // nnz   (== col_s for scalar spaces)
+    int64_t* inc_ptr = nullptr;    // nds+1
+    ScatterRec* recs = nullptr;    // nt*nloc_s
+    int max_row_len_s = 0;
+    int max_deg = 0;               // max incident tets of a scalar DOF
+    uint8_t* dir_mask = nullptr;   // ndof
+    double* dir_bc = nullptr;      // ndof
+    bool bc_nonzero = false;
+    bool has_dirichlet = false;
+    int order_assembled = -1;
+
+    // scratch
+    void* tetdata = nullptr;       // per-tet K blocks (phase 1 output)
+    size_t tetdata_bytes = 0;
+    int* d_status = nullptr;       // device status word
+    double* d_ref_tables = nullptr; // device copy of the T tables etc.
+    size_t d_ref_tables_bytes = 0;
+
+    // solver workspace (lazily sized)
+    void* solve_ws = nullptr;
+    size_t solve_ws_bytes = 0;
+    void* learned = nullptr;       // learned preconditioner state
+
+    std::vector<void*> extra_allocs;
+    // device copies of reference-element tables, keyed by 100*space + order
+    std::vector<std::pair<int, double*>> basis_dev;
+};
+// device table for (space, order): q*nf values then q*nf*3 gradients, then q weights
+int get_basis_dev(anigpu_ctx* h, int space, int order, const double** dev, ScalarBasisTable* host);
+
+// ------------------------------------------------------------------ helpers
+int set_err(anigpu_ctx* h, int code, const std::string& msg);
+int cuda_check(anigpu_ctx* h, cudaError_t e, const char* what);
+#define ANI_CUDA(h, call)                                      \
+    do {                                                       \
+        cudaError_t _e = (call);                               \
+        if (_e != cudaSuccess) return cuda_check(h, _e, #call); \
+    } while (0)
+#define ANI_LAUNCHED(h)                                                  \
+    do {                                                                 \
+        (h)->launches++;                                                 \
+        cudaError_t _e = cudaGetLastError();                             \
+        if (_e != cudaSuccess) return cuda_check(h, _e, "kernel launch"); \
+    } while (0)
+
+template <typename T>
+int dev_alloc(anigpu_ctx* h, T** p, size_t count) {
+    if (*p) {
+        cudaFree(*p);
+        *p = nullptr;
+    }
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+    if (e != cudaSuccess) return cuda_check(h, e, "cudaMalloc");
+    return ANIGPU_OK;
+}
+inline unsigned grid_for(int64_t n, int block) {
+    int64_t g = (n + block - 1) / block;
+    if (g < 1) g = 1;
+    if (g > 2147483647LL) g = 2147483647LL;
+    return (unsigned)g;
+}
+
+// ------------------------------------------------------------------ kernel entry points (host side)
+// element level (k_element.cu)
+int launch_fem3dtet(anigpu_ctx* h, int opA, int opB, int kind, int order, int precision, int64_t nt,
+                    const double* XY, const double* D, void* A);
+int launch_quad_points(anigpu_ctx* h, int order, int64_t nt, const double* XY, double* XYG);
+int launch_apply_dir(anigpu_ctx* h, int64_t nt, int n, double* A, double* F, const uint32_t* mask, const double* bc);
+// setup (k_setup.cu)
+int setup_orient(anigpu_ctx* h);
+int setup_problem(anigpu_ctx* h, int space);
+int setup_dirichlet_bits(anigpu_ctx* h);
+int setup_dof_coords(anigpu_ctx* h, double* out);
+// exclusive scan of cnt[0..n] (cnt[n] must be 0) into ptr[0..n]; ptr[n] = total
+int scan_counts(anigpu_ctx* h, unsigned long long* cnt, int64_t n, int64_t* ptr);
+// assembly (k_assemble.cu)
+int run_assemble(anigpu_ctx* h, int kind, const double* D, const double* f, double f_const, int order,
+                 int precision, void* vals, double* rhs, uint8_t* touched, double drop_val);
+int run_compact(anigpu_ctx* h, int64_t* rowptr, int32_t* col, void* vals, int precision, const uint8_t* touched,
+                int64_t* nnz_out);
+// solve (k_solve.cu)
+int run_spmv(anigpu_ctx* h, const void* vals, int precision, const double* x, double* y);
+int run_solve(anigpu_ctx* h, int method, const void* vals, int precision, const double* b, double* x, double rtol,
+              int64_t maxit, anigpu_solve_stats* st);
+void free_solver(anigpu_ctx* h);

@@ -1,0 +1,235 @@
+// The C ABI of anigpu (declared in include/anigpu.h): handles, errors, mesh upload and
+// the thin host orchestration around the kernels.  No computation of the path happens
+// on the host; every entry point that produces numbers launches device kernels.
+#include <cstring>
+#include <new>
+
+#include "anigpu_internal.h"
+#include "learned.h"
+#include "quad_tables.h"
+
+int set_err(anigpu_ctx* h, int code, const std::string& msg) {
+    if (h) h->err = msg;
+    return code;
+}
+
+int cuda_check(anigpu_ctx* h, cudaError_t e, const char* what) {
+    return set_err(h, ANIGPU_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CHECK_H(h) \
+    if (!(h)) return ANIGPU_ERR_ARG
+
+extern "C" {
+
+int anigpu_create(anigpu_handle* out, int device) {
+    if (!out) return ANIGPU_ERR_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) return ANIGPU_ERR_CUDA;
+    if (device < 0 || device >= ndev) return ANIGPU_ERR_ARG;
+    if (cudaSetDevice(device) != cudaSuccess) return ANIGPU_ERR_CUDA;
+    anigpu_ctx* h = new (std::nothrow) anigpu_ctx();
+    if (!h) return ANIGPU_ERR_ARG;
+    h->device = device;
+    if (cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete h;
+        return ANIGPU_ERR_CUDA;
+    }
+    h->stream = h->own_stream;
+    if (cudaMalloc((void**)&h->d_status, sizeof(int)) != cudaSuccess ||
+        cudaMemset(h->d_status, 0, sizeof(int)) != cudaSuccess) {
+        cudaStreamDestroy(h->own_stream);
+        delete h;
+        return ANIGPU_ERR_CUDA;
+    }
+    *out = h;
+    return ANIGPU_OK;
+}
+
+int anigpu_destroy(anigpu_handle h) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    cudaStreamSynchronize(h->stream);
+    free_solver(h);
+    free_learned(h);
+    void* ptrs[] = {h->xyz, h->tets, h->tet_edges, h->edofs, h->inc_ptr, h->recs, h->dir_mask, h->dir_bc,
+                    h->tetdata, h->d_status, h->d_ref_tables};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (h->rowptr && h->rowptr != h->rowptr_s) cudaFree(h->rowptr);
+    if (h->col && h->col != h->col_s) cudaFree(h->col);
+    if (h->rowptr_s) cudaFree(h->rowptr_s);
+    if (h->col_s) cudaFree(h->col_s);
+    for (auto& kv : h->basis_dev) cudaFree(kv.second);
+    for (void* p : h->extra_allocs) cudaFree(p);
+    if (h->own_stream) cudaStreamDestroy(h->own_stream);
+    delete h;
+    return ANIGPU_OK;
+}
+
+int anigpu_set_stream(anigpu_handle h, void* stream) {
+    CHECK_H(h);
+    h->stream = stream ? (cudaStream_t)stream : h->own_stream;
+    return ANIGPU_OK;
+}
+
+const char* anigpu_last_error(anigpu_handle h) { return h ? h->err.c_str() : "invalid handle"; }
+
+int64_t anigpu_launch_count(anigpu_handle h) { return h ? h->launches : -1; }
+
+int anigpu_fem3dtet(anigpu_handle h, int opA, int opB, int tensor_kind, int order, int precision, int64_t nt,
+                    const double* XY, const double* D, void* A) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    return launch_fem3dtet(h, opA, opB, tensor_kind, order, precision, nt, XY, D, A);
+}
+
+int anigpu_quadrature(int order, double* p_host, double* w_host, int cap) {
+    const double *p, *w;
+    int np;
+    if (!anigpu_quad_rule(order, &p, &w, &np)) return ANIGPU_ERR_UNSUPPORTED;
+    if (np > cap) return ANIGPU_ERR_ARG;
+    if (p_host) std::memcpy(p_host, p, sizeof(double) * 4 * np);
+    if (w_host) std::memcpy(w_host, w, sizeof(double) * np);
+    return np;
+}
+
+int anigpu_quadrature_points(anigpu_handle h, int order, int64_t nt, const double* XY, double* XYG) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    return launch_quad_points(h, order, nt, XY, XYG);
+}
+
+int anigpu_apply_dir(anigpu_handle h, int64_t nt, int n, double* A, double* F, const uint32_t* mask,
+                     const double* bc) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    return launch_apply_dir(h, nt, n, A, F, mask, bc);
+}
+
+int anigpu_mesh_upload(anigpu_handle h, int64_t nv, const double* xyz, int64_t nt, const int32_t* tets) {
+    CHECK_H(h);
+    if (nv <= 0 || nt <= 0 || !xyz || !tets) return set_err(h, ANIGPU_ERR_ARG, "empty or NULL mesh");
+    if (nv >= (int64_t)INT32_MAX || nt >= ((int64_t)1 << 27))
+        return set_err(h, ANIGPU_ERR_UNSUPPORTED, "mesh too large for 32-bit vertex / 27-bit tet ids");
+    cudaSetDevice(h->device);
+    int rc = dev_alloc(h, &h->xyz, (size_t)nv * 3);
+    if (rc) return rc;
+    rc = dev_alloc(h, &h->tets, (size_t)nt * 4);
+    if (rc) return rc;
+    ANI_CUDA(h, cudaMemcpyAsync(h->xyz, xyz, sizeof(double) * 3 * nv, cudaMemcpyDefault, h->stream));
+    ANI_CUDA(h, cudaMemcpyAsync(h->tets, tets, sizeof(int32_t) * 4 * nt, cudaMemcpyDefault, h->stream));
+    h->nv = nv;
+    h->nt = nt;
+    h->space = -1;
+    return setup_orient(h);
+}
+
+int anigpu_mesh_update_coords(anigpu_handle h, const double* xyz) {
+    CHECK_H(h);
+    if (!h->xyz || !xyz) return set_err(h, ANIGPU_ERR_STATE, "no mesh");
+    cudaSetDevice(h->device);
+    ANI_CUDA(h, cudaMemcpyAsync(h->xyz, xyz, sizeof(double) * 3 * h->nv, cudaMemcpyDefault, h->stream));
+    return ANIGPU_OK;
+}
+
+int anigpu_problem_setup(anigpu_handle h, int space) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    return setup_problem(h, space);
+}
+
+int anigpu_problem_info(anigpu_handle h, int64_t* ndof, int64_t* nnz, int64_t* nedges) {
+    CHECK_H(h);
+    if (h->space < 0) return set_err(h, ANIGPU_ERR_STATE, "anigpu_problem_setup not called");
+    if (ndof) *ndof = h->ndof;
+    if (nnz) *nnz = h->nnz;
+    if (nedges) *nedges = h->ne;
+    return ANIGPU_OK;
+}
+
+int anigpu_csr_template(anigpu_handle h, int64_t* rowptr, int32_t* col) {
+    CHECK_H(h);
+    if (h->space < 0) return set_err(h, ANIGPU_ERR_STATE, "anigpu_problem_setup not called");
+    cudaSetDevice(h->device);
+    if (rowptr)
+        ANI_CUDA(h, cudaMemcpyAsync(rowptr, h->rowptr, sizeof(int64_t) * (h->ndof + 1), cudaMemcpyDefault, h->stream));
+    if (col) ANI_CUDA(h, cudaMemcpyAsync(col, h->col, sizeof(int32_t) * h->nnz, cudaMemcpyDefault, h->stream));
+    ANI_CUDA(h, cudaStreamSynchronize(h->stream));
+    return ANIGPU_OK;
+}
+
+int anigpu_element_dofs(anigpu_handle h, int32_t* edofs) {
+    CHECK_H(h);
+    if (h->space < 0) return set_err(h, ANIGPU_ERR_STATE, "anigpu_problem_setup not called");
+    if (!edofs) return set_err(h, ANIGPU_ERR_ARG, "NULL");
+    cudaSetDevice(h->device);
+    ANI_CUDA(h, cudaMemcpyAsync(edofs, h->edofs, sizeof(int32_t) * h->nt * h->nloc_s, cudaMemcpyDefault, h->stream));
+    ANI_CUDA(h, cudaStreamSynchronize(h->stream));
+    return ANIGPU_OK;
+}
+
+int anigpu_dof_coords(anigpu_handle h, double* xyz) {
+    CHECK_H(h);
+    if (h->space < 0) return set_err(h, ANIGPU_ERR_STATE, "anigpu_problem_setup not called");
+    if (!xyz) return set_err(h, ANIGPU_ERR_ARG, "NULL");
+    cudaSetDevice(h->device);
+    return setup_dof_coords(h, xyz);
+}
+
+int anigpu_set_dirichlet(anigpu_handle h, const uint8_t* mask, const double* bc) {
+    CHECK_H(h);
+    if (h->space < 0) return set_err(h, ANIGPU_ERR_STATE, "anigpu_problem_setup not called");
+    cudaSetDevice(h->device);
+    if (mask)
+        ANI_CUDA(h, cudaMemcpyAsync(h->dir_mask, mask, h->ndof, cudaMemcpyDefault, h->stream));
+    else
+        ANI_CUDA(h, cudaMemsetAsync(h->dir_mask, 0, h->ndof, h->stream));
+    if (bc)
+        ANI_CUDA(h, cudaMemcpyAsync(h->dir_bc, bc, sizeof(double) * h->ndof, cudaMemcpyDefault, h->stream));
+    else
+        ANI_CUDA(h, cudaMemsetAsync(h->dir_bc, 0, sizeof(double) * h->ndof, h->stream));
+    h->has_dirichlet = mask != nullptr;
+    h->bc_nonzero = bc != nullptr;
+    return setup_dirichlet_bits(h);
+}
+
+int anigpu_assemble(anigpu_handle h, int tensor_kind, const double* D, const double* f, double f_const, int order,
+                    int precision, void* vals, double* rhs, uint8_t* touched, double drop_val) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    int rc = run_assemble(h, tensor_kind, D, f, f_const, order, precision, vals, rhs, touched, drop_val);
+    if (rc) return rc;
+    int st = 0;
+    ANI_CUDA(h, cudaMemcpyAsync(&st, h->d_status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    ANI_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (st) {
+        ANI_CUDA(h, cudaMemsetAsync(h->d_status, 0, sizeof(int), h->stream));
+        return set_err(h, st, "non-finite value in assembly (AssemblerT status -1)");
+    }
+    return ANIGPU_OK;
+}
+
+int anigpu_csr_compact(anigpu_handle h, int64_t* rowptr, int32_t* col, void* vals, int precision,
+                       const uint8_t* touched, int64_t* nnz_out) {
+    CHECK_H(h);
+    if (!rowptr || !col || !touched || !nnz_out) return set_err(h, ANIGPU_ERR_ARG, "NULL argument");
+    cudaSetDevice(h->device);
+    return run_compact(h, rowptr, col, vals, precision, touched, nnz_out);
+}
+
+int anigpu_solve(anigpu_handle h, int method, const void* vals, int precision, const double* b, double* x,
+                 double rtol, int64_t maxit, anigpu_solve_stats* stats) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    return run_solve(h, method, vals, precision, b, x, rtol, maxit, stats);
+}
+
+int anigpu_spmv(anigpu_handle h, const void* vals, int precision, const double* x, double* y) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    return run_spmv(h, vals, precision, x, y);
+}
+
+}  // extern "C"

@@ -1,0 +1,288 @@
+// Element level: the batched fem3Dtet (every operator pair, every tensor kind), the
+// physical quadrature points and the element-level Dirichlet elimination.
+//
+// This is the quadrature-faithful path that mirrors Ani::fem3Dtet
+// (anifem++/fem/operations/int_tet.inl:93-122 -> core.inl:277-367):
+//     U = OpA(phi) at every quadrature point, V = OpB(phi),
+//     DU = w_n |T| D(x_n) U          (internal_Dfunc::applyDU, diff_tensor.h:275-994)
+//     A  = V^T DU                      (fusive_AT_mul_B, core.inl:28-60)
+// One CTA per tetrahedron (grid-stride); the reference-element tables of both spaces
+// are staged once per CTA in shared memory, U/V/DU of one quadrature point live in
+// shared memory, and each thread owns a fixed set of entries of A in registers.
+#include <cstring>
+
+#include "anigpu_internal.h"
+#include "quad_tables.h"
+
+namespace {
+
+constexpr int kThreads = 128;
+constexpr int kMaxOwned = (ANIGPU_MAX_NF * ANIGPU_MAX_NF + kThreads - 1) / kThreads;  // 8
+
+struct OpDesc {
+    int nf, dim, nfs, bd, ncomp, op;  // op: 1 IDEN, 2 GRAD
+    const double* tab;                // device basis table (vals q*nfs, grads q*nfs*3)
+};
+
+struct ElemParams {
+    OpDesc A, B;
+    int q, kind;
+    const double* w;  // device weights
+};
+
+__device__ inline void tet_geometry(const double* X, double* PSI, double* mes) {
+    // internalFem3DtetGeomInit_Tet (core.inl:217-247) with inverse3x3 (geometry.h:26-44)
+    double m[9];
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int i = 0; i < 3; ++i) m[i + 3 * c] = X[3 * (c + 1) + i] - X[i];
+#define M(I, J) m[(I) + 3 * (J)]
+    const double da = M(1, 1) * M(2, 2) - M(1, 2) * M(2, 1);
+    const double db = M(1, 2) * M(2, 0) - M(1, 0) * M(2, 2);
+    const double dc = M(1, 0) * M(2, 1) - M(1, 1) * M(2, 0);
+    const double det = M(0, 0) * da + M(0, 1) * db + M(0, 2) * dc;
+    PSI[0] = da / det;
+    PSI[1] = db / det;
+    PSI[2] = dc / det;
+#pragma unroll
+    for (int i = 1; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+            PSI[j + 3 * i] = (M((i + 1) % 3, (j + 1) % 3) * M((i + 2) % 3, (j + 2) % 3) -
+                              M((i + 1) % 3, (j + 2) % 3) * M((i + 2) % 3, (j + 1) % 3)) / det;
+#undef M
+    *mes = fabs(det) / 6.0;
+}
+
+// value of operator `o` for column `col`, row `k` at point n (block structure of FemVec,
+// operators.h:127-155: component c owns rows [c*bd,(c+1)*bd) and columns [c*nfs,(c+1)*nfs))
+template <typename Real>
+__device__ inline Real op_value(const OpDesc& o, const double* tab, int q, int n, int k, int col, const double* PSI) {
+    const int c = col / o.nfs, i = col - c * o.nfs;
+    const int kc = k / o.bd, kk = k - kc * o.bd;
+    if (kc != c) return Real(0);
+    if (o.op == ANIGPU_IDEN) return Real(tab[n * o.nfs + i]);
+    const double* g = tab + (size_t)q * o.nfs + 3 * ((size_t)n * o.nfs + i);
+    // U_k = sum_j PSI(j,k) ghat_j (poly_2.h:91-97)
+    return Real(PSI[0 + 3 * kk] * g[0] + PSI[1 + 3 * kk] * g[1] + PSI[2 + 3 * kk] * g[2]);
+}
+
+template <typename Real>
+__global__ void __launch_bounds__(kThreads) fem3dtet_kernel(ElemParams p, int64_t nt, const double* __restrict__ XY,
+                                                             const double* __restrict__ D, Real* __restrict__ A) {
+    extern __shared__ double smem[];
+    const int q = p.q;
+    const int nfA = p.A.nf, nfB = p.B.nf, dA = p.A.dim, dB = p.B.dim;
+    const size_t tabA = (size_t)q * p.A.nfs * 4, tabB = (size_t)q * p.B.nfs * 4;
+    double* sTabA = smem;
+    double* sTabB = sTabA + tabA;
+    double* sW = sTabB + tabB;
+    double* sGeo = sW + q;              // PSI[9], mes
+    double* sD = sGeo + 10;             // dB*dA
+    Real* sU = reinterpret_cast<Real*>(sD + ANIGPU_MAX_DIM * ANIGPU_MAX_DIM);
+    Real* sV = sU + dA * nfA;
+    Real* sDU = sV + dB * nfB;
+    for (size_t i = threadIdx.x; i < tabA; i += blockDim.x) sTabA[i] = p.A.tab[i];
+    for (size_t i = threadIdx.x; i < tabB; i += blockDim.x) sTabB[i] = p.B.tab[i];
+    for (int i = threadIdx.x; i < q; i += blockDim.x) sW[i] = p.w[i];
+    const int nent = nfA * nfB;
+    const int nD = dA * dB;
+    for (int64_t t = blockIdx.x; t < nt; t += gridDim.x) {
+        __syncthreads();
+        if (threadIdx.x == 0) tet_geometry(XY + 12 * t, sGeo, sGeo + 9);
+        Real acc[kMaxOwned];
+#pragma unroll
+        for (int m = 0; m < kMaxOwned; ++m) acc[m] = Real(0);
+        __syncthreads();
+        const double mes = sGeo[9];
+        for (int n = 0; n < q; ++n) {
+            // U, V and the tensor at point n
+            for (int e = threadIdx.x; e < dA * nfA; e += blockDim.x)
+                sU[e] = op_value<Real>(p.A, sTabA, q, n, e % dA, e / dA, sGeo);
+            for (int e = threadIdx.x; e < dB * nfB; e += blockDim.x)
+                sV[e] = op_value<Real>(p.B, sTabB, q, n, e % dB, e / dB, sGeo);
+            // dense D(k,j), column-major dB x dA, with applyDU semantics for NULL/SCALAR
+            for (int e = threadIdx.x; e < nD; e += blockDim.x) {
+                const int k = e % dB, j = e / dB;
+                double v;
+                switch (p.kind) {
+                    case ANIGPU_TENSOR_NULL:
+                    case ANIGPU_TENSOR_CONST_SCALAR:
+                    case ANIGPU_TENSOR_TET_SCALAR: {
+                        const double s = p.kind == ANIGPU_TENSOR_NULL
+                                             ? 1.0
+                                             : (p.kind == ANIGPU_TENSOR_CONST_SCALAR ? D[0] : D[t]);
+                        v = (dA == dB) ? (k == j ? s : 0.0) : s;  // dimA==1: column of s
+                        break;
+                    }
+                    case ANIGPU_TENSOR_TET_SYM: {
+                        const double* s6 = D + 6 * t;
+                        const int lo = k < j ? k : j, hi = k < j ? j : k;
+                        const int idx = lo == 0 ? hi : (lo == 1 ? 2 + hi : 5);
+                        v = s6[idx];
+                        break;
+                    }
+                    case ANIGPU_TENSOR_TET_GENERAL: v = D[(size_t)nD * t + e]; break;
+                    default: v = D[(size_t)nD * (n + (size_t)q * t) + e]; break;
+                }
+                sD[e] = v;
+            }
+            __syncthreads();
+            const Real wv = Real(sW[n] * mes);
+            for (int e = threadIdx.x; e < dB * nfA; e += blockDim.x) {
+                const int k = e % dB, ia = e / dB;
+                Real s = 0;
+                for (int j = 0; j < dA; ++j) s += Real(sD[k + dB * j]) * sU[j + dA * ia];
+                sDU[e] = wv * s;
+            }
+            __syncthreads();
+#pragma unroll
+            for (int m = 0; m < kMaxOwned; ++m) {
+                const int e = threadIdx.x + m * kThreads;
+                if (e < nent) {
+                    const int ib = e % nfB, ia = e / nfB;
+                    Real s = 0;
+                    for (int k = 0; k < dB; ++k) s += sV[k + dB * ib] * sDU[k + dB * ia];
+                    acc[m] += s;
+                }
+            }
+            __syncthreads();
+        }
+        Real* At = A + (size_t)nent * t;
+#pragma unroll
+        for (int m = 0; m < kMaxOwned; ++m) {
+            const int e = threadIdx.x + m * kThreads;
+            if (e < nent) At[e] = acc[m];
+        }
+    }
+}
+
+__global__ void quad_points_kernel(int64_t nt, int q, const double* __restrict__ pts, const double* __restrict__ XY,
+                                   double* __restrict__ XYG) {
+    const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (idx >= nt * q) return;
+    const int64_t t = idx / q;
+    const int n = (int)(idx - t * q);
+    const double* X = XY + 12 * t;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        double s = X[k];
+#pragma unroll
+        for (int l = 0; l < 3; ++l) s += pts[l + 1 + 4 * n] * (X[3 * (l + 1) + k] - X[k]);
+        XYG[3 * idx + k] = s;
+    }
+}
+
+// Ani::applyDir (dc_on_dof.h:39-45), ascending local k
+__global__ void apply_dir_kernel(int64_t nt, int n, double* __restrict__ A, double* __restrict__ F,
+                                 const uint32_t* __restrict__ mask, const double* __restrict__ bc) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= nt) return;
+    double* At = A + (size_t)n * n * t;
+    double* Ft = F + (size_t)n * t;
+    const uint32_t m = mask[t];
+    for (int k = 0; k < n; ++k) {
+        if (!((m >> k) & 1u)) continue;
+        const double b = bc ? bc[(size_t)n * t + k] : 0.0;
+        for (int i = 0; i < n; ++i) Ft[i] -= At[i + n * k] * b;
+        Ft[k] = b;
+        for (int i = 0; i < n; ++i) At[i + n * k] = 0.0;
+        for (int i = 0; i < n; ++i) At[k + n * i] = 0.0;
+        At[k + n * k] = 1.0;
+    }
+}
+
+}  // namespace
+
+int get_basis_dev(anigpu_ctx* h, int space, int order, const double** dev, ScalarBasisTable* host) {
+    ScalarBasisTable tab;
+    if (!make_scalar_basis(space, order, &tab)) return set_err(h, ANIGPU_ERR_UNSUPPORTED, "unsupported space/order");
+    if (host) *host = tab;
+    const int key = 100 * space + order;
+    for (auto& kv : h->basis_dev)
+        if (kv.first == key) {
+            *dev = kv.second;
+            return ANIGPU_OK;
+        }
+    std::vector<double> buf;
+    buf.insert(buf.end(), tab.val.begin(), tab.val.end());
+    buf.insert(buf.end(), tab.grad.begin(), tab.grad.end());
+    buf.insert(buf.end(), tab.wts.begin(), tab.wts.end());
+    buf.insert(buf.end(), tab.pts.begin(), tab.pts.end());
+    double* d = nullptr;
+    ANI_CUDA(h, cudaMalloc((void**)&d, buf.size() * sizeof(double)));
+    ANI_CUDA(h, cudaMemcpy(d, buf.data(), buf.size() * sizeof(double), cudaMemcpyHostToDevice));
+    h->basis_dev.push_back({key, d});
+    *dev = d;
+    return ANIGPU_OK;
+}
+
+int launch_fem3dtet(anigpu_ctx* h, int opA, int opB, int kind, int order, int precision, int64_t nt,
+                    const double* XY, const double* D, void* A) {
+    int nfA, dA, bsA, ncA, oA, nfB, dB, bsB, ncB, oB;
+    if (!op_info(opA, &nfA, &dA, &bsA, &ncA, &oA) || !op_info(opB, &nfB, &dB, &bsB, &ncB, &oB))
+        return set_err(h, ANIGPU_ERR_UNSUPPORTED, "unknown operator code");
+    if (nt < 0) return set_err(h, ANIGPU_ERR_ARG, "nt < 0");
+    if (nt == 0) return ANIGPU_OK;
+    if (kind < ANIGPU_TENSOR_NULL || kind > ANIGPU_TENSOR_POINT)
+        return set_err(h, ANIGPU_ERR_UNSUPPORTED, "tensor kind");
+    if (kind == ANIGPU_TENSOR_TET_SYM && (dA != 3 || dB != 3))
+        return set_err(h, ANIGPU_ERR_ARG, "TET_SYM needs 3x3 operators");
+    if ((kind == ANIGPU_TENSOR_NULL || kind == ANIGPU_TENSOR_CONST_SCALAR || kind == ANIGPU_TENSOR_TET_SCALAR) &&
+        dA != dB && !(nfA == 1 && dA == 1))
+        // diff_tensor.h:314-317: identity defined only for operators of the same dimension
+        return set_err(h, ANIGPU_ERR_ARG, "Identity tensor defined only for compatible operators A and B");
+    if (kind != ANIGPU_TENSOR_NULL && D == nullptr) return set_err(h, ANIGPU_ERR_ARG, "tensor data is NULL");
+    if (!XY || !A) return set_err(h, ANIGPU_ERR_ARG, "NULL coordinates or output");
+    const double *tA, *tB;
+    ScalarBasisTable hA;
+    int rc = get_basis_dev(h, bsA, order, &tA, &hA);
+    if (rc) return rc;
+    rc = get_basis_dev(h, bsB, order, &tB, nullptr);
+    if (rc) return rc;
+    ElemParams p;
+    p.A = {nfA, dA, nfA / ncA, dA / ncA, ncA, oA, tA};
+    p.B = {nfB, dB, nfB / ncB, dB / ncB, ncB, oB, tB};
+    p.q = hA.q;
+    p.kind = kind;
+    p.w = tA + (size_t)hA.q * hA.nf * 4;
+    const size_t tabs = (size_t)p.q * (p.A.nfs + p.B.nfs) * 4;
+    const size_t rsz = precision == ANIGPU_F32 ? sizeof(float) : sizeof(double);
+    const size_t smem = sizeof(double) * (tabs + p.q + 10 + ANIGPU_MAX_DIM * ANIGPU_MAX_DIM) +
+                        rsz * (size_t)(dA * nfA + dB * nfB + dB * nfA);
+    int dev_sms = 148;
+    cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, h->device);
+    const unsigned grid = (unsigned)std::min<int64_t>(nt, (int64_t)dev_sms * 16);
+    if (precision == ANIGPU_F32) {
+        ANI_CUDA(h, cudaFuncSetAttribute(fem3dtet_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        fem3dtet_kernel<float><<<grid, kThreads, smem, h->stream>>>(p, nt, XY, D, (float*)A);
+    } else if (precision == ANIGPU_F64) {
+        ANI_CUDA(h, cudaFuncSetAttribute(fem3dtet_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        fem3dtet_kernel<double><<<grid, kThreads, smem, h->stream>>>(p, nt, XY, D, (double*)A);
+    } else {
+        return set_err(h, ANIGPU_ERR_ARG, "precision");
+    }
+    ANI_LAUNCHED(h);
+    return ANIGPU_OK;
+}
+
+int launch_quad_points(anigpu_ctx* h, int order, int64_t nt, const double* XY, double* XYG) {
+    const double* tab;
+    ScalarBasisTable host;
+    int rc = get_basis_dev(h, ANIGPU_P1, order, &tab, &host);
+    if (rc) return rc;
+    if (nt <= 0) return nt < 0 ? set_err(h, ANIGPU_ERR_ARG, "nt < 0") : ANIGPU_OK;
+    const double* pts = tab + (size_t)host.q * host.nf * 4 + host.q;
+    quad_points_kernel<<<grid_for(nt * host.q, 256), 256, 0, h->stream>>>(nt, host.q, pts, XY, XYG);
+    ANI_LAUNCHED(h);
+    return ANIGPU_OK;
+}
+
+int launch_apply_dir(anigpu_ctx* h, int64_t nt, int n, double* A, double* F, const uint32_t* mask, const double* bc) {
+    if (n <= 0 || n > 32 || nt < 0 || !A || !F || !mask) return set_err(h, ANIGPU_ERR_ARG, "apply_dir arguments");
+    if (nt == 0) return ANIGPU_OK;
+    apply_dir_kernel<<<grid_for(nt, 128), 128, 0, h->stream>>>(nt, n, A, F, mask, bc);
+    ANI_LAUNCHED(h);
+    return ANIGPU_OK;
+}

@@ -1,0 +1,568 @@
+/* The oracle (test infrastructure only; see anifem_oracle.h).  Plain C restatement of
+ * the reference's element-matrix engine and global assembly rules.  Every function
+ * cites the reference lines it restates.  The quadrature rules come from the table
+ * the product also uses (generated by inmost-fem_gb300/csrc/gen_quadrature.py); the
+ * tests pin that table against the reference's own tetrahedron_quadrature_formulas
+ * and against polynomial exactness. */
+#define _POSIX_C_SOURCE 199309L
+#include "anifem_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+#include "../inmost-fem_gb300/csrc/quad_tables.h"
+
+#define MAXNF 30
+#define MAXDIM 9
+#define MAXQ 64
+
+/* ---------------------------------------------------------------- bases */
+
+/* edge (I,J) order of P2/P3 edge DOFs: poly_2.h:34,76 and poly_3.h:36,86 */
+static const int EI[6] = {0, 0, 0, 1, 1, 2}, EJ[6] = {1, 2, 3, 2, 3, 3};
+/* P3 face DOF vertex triples: poly_3.h:33 (IPF) */
+static const int FV[4][3] = {{0, 1, 2}, {1, 2, 3}, {0, 2, 3}, {0, 1, 3}};
+/* d(lambda_i)/d(xi_d): lambda_0 = 1 - xi1 - xi2 - xi3, lambda_k = xi_k (poly_2.h:68 GRAD_P1) */
+static double dl(int i, int d) { return i == 0 ? -1.0 : (i - 1 == d ? 1.0 : 0.0); }
+
+/* values and reference gradients of a scalar space at barycentric point l[4] */
+static int scalar_basis(int space, const double* l, double* val, double (*g)[3]) {
+    int d, i, e;
+    switch (space) {
+        case 0: /* P0: poly_0.h */
+            val[0] = 1;
+            for (d = 0; d < 3; ++d) g[0][d] = 0;
+            return 1;
+        case 1: /* P1: poly_1.h:12-30, :91-120 */
+            for (i = 0; i < 4; ++i) {
+                val[i] = l[i];
+                for (d = 0; d < 3; ++d) g[i][d] = dl(i, d);
+            }
+            return 4;
+        case 2: /* P2: poly_2.h:12-100 */
+            for (i = 0; i < 4; ++i) {
+                val[i] = l[i] * (2 * l[i] - 1);
+                for (d = 0; d < 3; ++d) g[i][d] = dl(i, d) * (4 * l[i] - 1);
+            }
+            for (e = 0; e < 6; ++e) {
+                double a = l[EI[e]], b = l[EJ[e]];
+                val[4 + e] = 4 * a * b;
+                for (d = 0; d < 3; ++d) g[4 + e][d] = 4 * (dl(EJ[e], d) * a + dl(EI[e], d) * b);
+            }
+            return 10;
+        case 3: /* P3: poly_3.h:12-110 */
+            for (i = 0; i < 4; ++i) {
+                double s = l[i];
+                val[i] = s * (3 * s - 1) * (3 * s - 2) / 2;
+                for (d = 0; d < 3; ++d) g[i][d] = dl(i, d) * ((13.5 * s - 9) * s + 1);
+            }
+            for (e = 0; e < 6; ++e) {
+                int I = EI[e], J = EJ[e];
+                double s1 = l[I], s2 = l[J];
+                val[4 + 2 * e] = s1 * (3 * s1 - 1) * s2 * 4.5;
+                val[4 + 2 * e + 1] = s1 * (3 * s2 - 1) * s2 * 4.5;
+                for (d = 0; d < 3; ++d) {
+                    g[4 + 2 * e][d] = (dl(I, d) * (6 * s1 - 1) * s2 + dl(J, d) * (3 * s1 - 1) * s1) * 4.5;
+                    g[4 + 2 * e + 1][d] = (dl(J, d) * (6 * s2 - 1) * s1 + dl(I, d) * (3 * s2 - 1) * s2) * 4.5;
+                }
+            }
+            for (i = 0; i < 4; ++i) {
+                int a = FV[i][0], b = FV[i][1], c = FV[i][2];
+                double s1 = l[a], s2 = l[b], s3 = l[c];
+                val[16 + i] = 27 * s1 * s2 * s3;
+                for (d = 0; d < 3; ++d)
+                    g[16 + i][d] = 27 * (dl(a, d) * s2 * s3 + s1 * dl(b, d) * s3 + s1 * s2 * dl(c, d));
+            }
+            return 20;
+    }
+    return -1;
+}
+
+static int scalar_nf(int space) {
+    static const int nf[4] = {1, 4, 10, 20};
+    return (space >= 0 && space < 4) ? nf[space] : -1;
+}
+
+int orc_op_info(int code, int* nf, int* dim) {
+    int space = code / 10, op = code % 10;
+    int vec = (space == 4 || space == 5), base = vec ? space - 3 : space;
+    int n = scalar_nf(base);
+    if (n < 0 || (op != 1 && op != 2)) return -1;
+    int dm = (op == 1) ? 1 : 3;
+    *nf = vec ? 3 * n : n;
+    *dim = vec ? 3 * dm : dm;
+    return 0;
+}
+
+/* Operator application at one point: U[k + dim*i] (operators.h:127-155 for FemVec:
+ * component c occupies rows [c*bdim, (c+1)*bdim) and columns [c*nfs, (c+1)*nfs)). */
+static void apply_op(int code, const double* l, const double* PSI, double* U) {
+    int space = code / 10, op = code % 10;
+    int vec = (space == 4 || space == 5), base = vec ? space - 3 : space;
+    double val[20], g[20][3];
+    int nfs = scalar_basis(base, l, val, g);
+    int bdim = (op == 1) ? 1 : 3;
+    int ncomp = vec ? 3 : 1;
+    int dim = bdim * ncomp, nf = nfs * ncomp;
+    memset(U, 0, sizeof(double) * dim * nf);
+    for (int c = 0; c < ncomp; ++c)
+        for (int i = 0; i < nfs; ++i) {
+            int col = c * nfs + i;
+            if (op == 1) {
+                U[c + dim * col] = val[i];
+            } else {
+                for (int k = 0; k < 3; ++k) {
+                    double s = 0; /* U_k = sum_j PSI(j,k) ghat_j  (poly_2.h:91-97) */
+                    for (int j = 0; j < 3; ++j) s += PSI[j + 3 * k] * g[i][j];
+                    U[c * 3 + k + dim * col] = s;
+                }
+            }
+        }
+}
+
+/* ---------------------------------------------------------------- geometry */
+
+/* Ani::inverse3x3 (geometry.h:26-44): col-major m, returns det */
+static double inverse3x3(const double* m, double* inv) {
+#define M(I, J) m[(I) + 3 * (J)]
+    double da = M(1, 1) * M(2, 2) - M(1, 2) * M(2, 1);
+    double db = M(1, 2) * M(2, 0) - M(1, 0) * M(2, 2);
+    double dc = M(1, 0) * M(2, 1) - M(1, 1) * M(2, 0);
+    double det = M(0, 0) * da + M(0, 1) * db + M(0, 2) * dc;
+    inv[0] = da / det;
+    inv[1] = db / det;
+    inv[2] = dc / det;
+    for (int i = 1; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            inv[j + 3 * i] = (M((i + 1) % 3, (j + 1) % 3) * M((i + 2) % 3, (j + 2) % 3) -
+                              M((i + 1) % 3, (j + 2) % 3) * M((i + 2) % 3, (j + 1) % 3)) / det;
+#undef M
+    return det;
+}
+
+/* internalFem3DtetGeomInit_Tet (core.inl:217-247): edges from X0, PSI = inv, MES = |det|/6 */
+static double tet_geom(const double* X, double* PSI, double* mes) {
+    double J[9];
+    for (int c = 0; c < 3; ++c)
+        for (int i = 0; i < 3; ++i) J[i + 3 * c] = X[3 * (c + 1) + i] - X[i];
+    double det = inverse3x3(J, PSI);
+    *mes = fabs(det) / 6;
+    return det;
+}
+
+int orc_quad_rule(int order, double* p, double* w, int cap) {
+    const double *pp, *ww;
+    int np;
+    if (!anigpu_quad_rule(order, &pp, &ww, &np)) return -1;
+    if (np > cap) return -np;
+    if (p) memcpy(p, pp, sizeof(double) * 4 * np);
+    if (w) memcpy(w, ww, sizeof(double) * np);
+    return np;
+}
+
+/* physical points: X0 + sum_l xi_l (X_l - X0) (core.inl:249-269) */
+int orc_quad_points(int order, long nt, const double* XY, double* XYG) {
+    const double *pp, *ww;
+    int q;
+    if (!anigpu_quad_rule(order, &pp, &ww, &q)) return -1;
+    for (long t = 0; t < nt; ++t) {
+        const double* X = XY + 12 * t;
+        for (int n = 0; n < q; ++n)
+            for (int k = 0; k < 3; ++k) {
+                double s = X[k];
+                for (int l = 0; l < 3; ++l) s += pp[l + 1 + 4 * n] * (X[3 * (l + 1) + k] - X[k]);
+                XYG[3 * (n + (long)q * t) + k] = s;
+            }
+    }
+    return q;
+}
+
+/* ---------------------------------------------------------------- element matrices */
+
+/* expand one tensor sample into a full col-major dimB x dimA matrix D(k,j) with the
+ * semantics of internal_Dfunc::applyDU (diff_tensor.h:275-552): NULL -> identity (or a
+ * column of ones when dimA == 1), SCALAR -> s * identity (or a column of s). */
+static void expand_tensor(int kind, const double* src, int dA, int dB, double* D) {
+    memset(D, 0, sizeof(double) * dA * dB);
+    switch (kind) {
+        case ORC_NULL:
+        case ORC_CONST_SCALAR:
+        case ORC_TET_SCALAR: {
+            double s = (kind == ORC_NULL) ? 1.0 : src[0];
+            if (dA == dB)
+                for (int i = 0; i < dA; ++i) D[i + dB * i] = s;
+            else
+                for (int k = 0; k < dB; ++k) D[k] = s; /* dimA == 1 (P0 right-hand side) */
+            break;
+        }
+        case ORC_TET_SYM: { /* d00 d01 d02 d11 d12 d22 */
+            double m[9] = {src[0], src[1], src[2], src[1], src[3], src[4], src[2], src[4], src[5]};
+            memcpy(D, m, sizeof m);
+            break;
+        }
+        default:
+            memcpy(D, src, sizeof(double) * dA * dB);
+    }
+}
+
+/* A(ib, ia) = sum_n w_n |T| sum_k V_k(ib) sum_j D(k,j) U_j(ia)
+ * (core.inl:277-367: U = OpA(apply), DU (diff_tensor.h:488-552), A = V^T DU (core.inl:28-60)) */
+int orc_fem3dtet(int codeA, int codeB, int kind, int order, long nt, const double* XY, const double* D, double* A) {
+    int nfA, dA, nfB, dB;
+    if (orc_op_info(codeA, &nfA, &dA) || orc_op_info(codeB, &nfB, &dB)) return -1;
+    if ((kind == ORC_TET_SYM) && (dA != 3 || dB != 3)) return -1;
+    if ((kind == ORC_NULL || kind == ORC_CONST_SCALAR || kind == ORC_TET_SCALAR) && dA != dB && dA != 1) return -1;
+    const double *pp, *ww;
+    int q;
+    if (!anigpu_quad_rule(order, &pp, &ww, &q)) return -1;
+    double U[MAXDIM * MAXNF], V[MAXDIM * MAXNF], Dm[MAXDIM * MAXDIM], DU[MAXDIM * MAXNF];
+    for (long t = 0; t < nt; ++t) {
+        double PSI[9], mes;
+        tet_geom(XY + 12 * t, PSI, &mes);
+        double* At = A + (size_t)t * nfA * nfB;
+        memset(At, 0, sizeof(double) * nfA * nfB);
+        for (int n = 0; n < q; ++n) {
+            const double* l = pp + 4 * n;
+            apply_op(codeA, l, PSI, U); /* l = (lambda_0..lambda_3) as tabulated (int_tet.inl:116-121) */
+            apply_op(codeB, l, PSI, V);
+            const double* src = NULL;
+            switch (kind) {
+                case ORC_CONST_SCALAR: src = D; break;
+                case ORC_TET_SCALAR: src = D + t; break;
+                case ORC_TET_SYM: src = D + 6 * t; break;
+                case ORC_TET_GENERAL: src = D + (size_t)dA * dB * t; break;
+                case ORC_POINT: src = D + (size_t)dA * dB * (n + (size_t)q * t); break;
+            }
+            expand_tensor(kind, src, dA, dB, Dm);
+            double wv = ww[n] * mes;
+            for (int ia = 0; ia < nfA; ++ia)
+                for (int k = 0; k < dB; ++k) {
+                    double s = 0;
+                    for (int j = 0; j < dA; ++j) s += Dm[k + dB * j] * U[j + dA * ia];
+                    DU[k + dB * ia] = wv * s;
+                }
+            for (int ia = 0; ia < nfA; ++ia)
+                for (int ib = 0; ib < nfB; ++ib) {
+                    double s = 0;
+                    for (int k = 0; k < dB; ++k) s += V[k + dB * ib] * DU[k + dB * ia];
+                    At[ib + nfB * ia] += s;
+                }
+        }
+    }
+    return 0;
+}
+
+/* Ani::applyDir (dc_on_dof.h:39-45) */
+void orc_apply_dir(int n, double* A, double* F, int k, double bc) {
+    for (int i = 0; i < n; ++i) F[i] -= A[i + n * k] * bc;
+    F[k] = bc;
+    for (int i = 0; i < n; ++i) A[i + n * k] = 0; /* column k */
+    for (int i = 0; i < n; ++i) A[k + n * i] = 0; /* row k */
+    A[k + n * k] = 1.0;
+}
+
+/* ---------------------------------------------------------------- mesh topology */
+
+/* reorderNodesOnTetrahedron (ordering.inl:9-26): swap local nodes 2,3 when
+ * det(X0-X3, X1-X3, X2-X3) < 0 */
+void orc_orient(const double* xyz, long nt, int32_t* tets) {
+    for (long t = 0; t < nt; ++t) {
+        int32_t* v = tets + 4 * t;
+        double m[3][3];
+        for (int j = 0; j < 3; ++j) {
+            m[0][j] = xyz[3 * v[0] + j] - xyz[3 * v[3] + j];
+            m[1][j] = xyz[3 * v[1] + j] - xyz[3 * v[3] + j];
+            m[2][j] = xyz[3 * v[2] + j] - xyz[3 * v[3] + j];
+        }
+        double det = 0;
+        det += m[0][0] * (m[1][1] * m[2][2] - m[1][2] * m[2][1]);
+        det += m[0][1] * (m[1][2] * m[2][0] - m[1][0] * m[2][2]);
+        det += m[0][2] * (m[1][0] * m[2][1] - m[1][1] * m[2][0]);
+        if (det < 0) {
+            int32_t s = v[2];
+            v[2] = v[3];
+            v[3] = s;
+        }
+    }
+}
+
+static int cmp_u64(const void* a, const void* b) {
+    uint64_t x = *(const uint64_t*)a, y = *(const uint64_t*)b;
+    return (x > y) - (x < y);
+}
+static int cmp_i32(const void* a, const void* b) {
+    int32_t x = *(const int32_t*)a, y = *(const int32_t*)b;
+    return (x > y) - (x < y);
+}
+
+/* Edge numbering: the NATURAL enumeration (global_enumerator.h:392-404) orders edge
+ * DOFs by edge id; this library defines the edge id as the rank of the edge's
+ * (min vertex, max vertex) pair in lexicographic order. */
+long orc_edges(long nv, long nt, const int32_t* tets, int32_t* tet_edges) {
+    (void)nv;
+    uint64_t* keys = (uint64_t*)malloc(sizeof(uint64_t) * 6 * (size_t)nt);
+    for (long t = 0; t < nt; ++t)
+        for (int e = 0; e < 6; ++e) {
+            uint32_t a = (uint32_t)tets[4 * t + EI[e]], b = (uint32_t)tets[4 * t + EJ[e]];
+            uint32_t lo = a < b ? a : b, hi = a < b ? b : a;
+            keys[6 * t + e] = ((uint64_t)lo << 32) | hi;
+        }
+    uint64_t* u = (uint64_t*)malloc(sizeof(uint64_t) * 6 * (size_t)nt);
+    memcpy(u, keys, sizeof(uint64_t) * 6 * (size_t)nt);
+    qsort(u, 6 * (size_t)nt, sizeof(uint64_t), cmp_u64);
+    long ne = 0;
+    for (long i = 0; i < 6 * nt; ++i)
+        if (i == 0 || u[i] != u[i - 1]) u[ne++] = u[i];
+    for (long i = 0; i < 6 * nt; ++i) {
+        long lo = 0, hi = ne - 1;
+        while (lo < hi) {
+            long mid = (lo + hi) / 2;
+            if (u[mid] < keys[i]) lo = mid + 1;
+            else hi = mid;
+        }
+        tet_edges[i] = (int32_t)lo;
+    }
+    free(keys);
+    free(u);
+    return ne;
+}
+
+/* NATURAL numbering (global_enumerator.h:392-404): vertex DOFs by vertex id, then edge
+ * DOFs by edge id; Vec3P2 is component-major (component c block of ndof_scalar). */
+long orc_element_dofs(int space, long nv, long ne, long nt, const int32_t* tets, const int32_t* tet_edges,
+                      int32_t* edofs) {
+    long nd = (space == 1) ? nv : nv + ne;
+    for (long t = 0; t < nt; ++t) {
+        int32_t loc[10];
+        for (int i = 0; i < 4; ++i) loc[i] = tets[4 * t + i];
+        if (space != 1)
+            for (int e = 0; e < 6; ++e) loc[4 + e] = (int32_t)(nv + tet_edges[6 * t + e]);
+        if (space == 1) {
+            for (int i = 0; i < 4; ++i) edofs[4 * t + i] = loc[i];
+        } else if (space == 2) {
+            for (int i = 0; i < 10; ++i) edofs[10 * t + i] = loc[i];
+        } else {
+            for (int c = 0; c < 3; ++c)
+                for (int i = 0; i < 10; ++i) edofs[30 * t + 10 * c + i] = (int32_t)(c * nd + loc[i]);
+        }
+    }
+    return (space == 5) ? 3 * nd : nd;
+}
+
+/* dof -> incident (tet) lists, tets ascending */
+static void incidence(long ndof, long nt, int nloc, const int32_t* edofs, int64_t** iptr, int32_t** itet) {
+    int64_t* p = (int64_t*)calloc((size_t)ndof + 1, sizeof(int64_t));
+    for (long t = 0; t < nt; ++t)
+        for (int i = 0; i < nloc; ++i) p[edofs[(size_t)nloc * t + i] + 1]++;
+    for (long r = 0; r < ndof; ++r) p[r + 1] += p[r];
+    int64_t* fill = (int64_t*)malloc(sizeof(int64_t) * (size_t)ndof);
+    memcpy(fill, p, sizeof(int64_t) * (size_t)ndof);
+    int32_t* it = (int32_t*)malloc(sizeof(int32_t) * (size_t)(p[ndof] > 0 ? p[ndof] : 1));
+    for (long t = 0; t < nt; ++t)
+        for (int i = 0; i < nloc; ++i) it[fill[edofs[(size_t)nloc * t + i]]++] = (int32_t)t;
+    free(fill);
+    *iptr = p;
+    *itet = it;
+}
+
+long orc_csr_template(long ndof, long nt, int nloc, const int32_t* edofs, int64_t* rowptr, int32_t* col) {
+    int64_t* ip;
+    int32_t* itet;
+    incidence(ndof, nt, nloc, edofs, &ip, &itet);
+    int32_t* buf = (int32_t*)malloc(sizeof(int32_t) * (64 * nloc + 8));
+    int cap = 64 * nloc + 8;
+    long nnz = 0;
+    rowptr[0] = 0;
+    for (long r = 0; r < ndof; ++r) {
+        long m = 0;
+        long deg = ip[r + 1] - ip[r];
+        if (deg * nloc + 1 > cap) {
+            cap = (int)(deg * nloc + 1);
+            buf = (int32_t*)realloc(buf, sizeof(int32_t) * cap);
+        }
+        buf[m++] = (int32_t)r; /* diagonal forced (assembler.inl:114-135) */
+        for (int64_t k = ip[r]; k < ip[r + 1]; ++k)
+            for (int j = 0; j < nloc; ++j) buf[m++] = edofs[(size_t)nloc * itet[k] + j];
+        qsort(buf, m, sizeof(int32_t), cmp_i32);
+        long u = 0;
+        for (long k = 0; k < m; ++k)
+            if (k == 0 || buf[k] != buf[k - 1]) buf[u++] = buf[k];
+        if (col) memcpy(col + nnz, buf, sizeof(int32_t) * u);
+        nnz += u;
+        rowptr[r + 1] = nnz;
+    }
+    free(buf);
+    free(ip);
+    free(itet);
+    return nnz;
+}
+
+static long find_slot(const int64_t* rowptr, const int32_t* col, long r, int32_t c) {
+    long lo = rowptr[r], hi = rowptr[r + 1] - 1;
+    while (lo < hi) {
+        long mid = (lo + hi) / 2;
+        if (col[mid] < c) lo = mid + 1;
+        else hi = mid;
+    }
+    return (lo <= hi && col[lo] == c) ? lo : -1;
+}
+
+int orc_scatter(long ndof, const int64_t* rowptr, const int32_t* col, long nt, int nloc, const int32_t* edofs,
+                const double* Aelem, const double* Felem, double drop, double* vals, double* rhs, uint8_t* touched) {
+    (void)ndof;
+    for (long t = 0; t < nt; ++t) {
+        const int32_t* ed = edofs + (size_t)nloc * t;
+        const double* Ae = Aelem + (size_t)nloc * nloc * t;
+        for (int i = 0; i < nloc; ++i) {
+            long r = ed[i];
+            if (Felem) {
+                if (!isfinite(Felem[(size_t)nloc * t + i])) return -1;
+                rhs[r] += Felem[(size_t)nloc * t + i];
+            }
+            for (int j = 0; j < nloc; ++j) {
+                double a = Ae[i + nloc * j]; /* element matrix column-major: A(i,j) = Ae[j*n + i] */
+                if (!isfinite(a)) return -1;
+                if (fabs(a) > drop) {
+                    long s = find_slot(rowptr, col, r, ed[j]);
+                    if (s < 0) return -2;
+                    vals[s] += a;
+                    if (touched) touched[s] = 1;
+                }
+            }
+        }
+    }
+    return 0;
+}
+
+long orc_csr_compact(long ndof, int64_t* rowptr, int32_t* col, double* vals, const uint8_t* touched) {
+    long w = 0;
+    int64_t start = rowptr[0];
+    for (long r = 0; r < ndof; ++r) {
+        int64_t end = rowptr[r + 1];
+        for (int64_t k = start; k < end; ++k)
+            if (touched[k] || col[k] == r) {
+                col[w] = col[k];
+                if (vals) vals[w] = vals[k];
+                ++w;
+            }
+        start = end;
+        rowptr[r + 1] = w;
+    }
+    return w;
+}
+
+/* ---------------------------------------------------------------- solver */
+
+void orc_spmv(long n, const int64_t* rowptr, const int32_t* col, const double* vals, const double* x, double* y) {
+    for (long r = 0; r < n; ++r) {
+        double s = 0;
+        for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k) s += vals[k] * x[col[k]];
+        y[r] = s;
+    }
+}
+
+static double dot(long n, const double* a, const double* b) {
+    double s = 0;
+    for (long i = 0; i < n; ++i) s += a[i] * b[i];
+    return s;
+}
+
+double orc_true_residual(long n, const int64_t* rowptr, const int32_t* col, const double* vals, const double* x,
+                         const double* b) {
+    double* r = (double*)malloc(sizeof(double) * n);
+    orc_spmv(n, rowptr, col, vals, x, r);
+    for (long i = 0; i < n; ++i) r[i] = b[i] - r[i];
+    double res = sqrt(dot(n, r, r)) / sqrt(dot(n, b, b));
+    free(r);
+    return res;
+}
+
+long orc_jacobi_pcg(long n, const int64_t* rowptr, const int32_t* col, const double* vals, const double* b,
+                    double* x, double rtol, long maxit, double* final_rel) {
+    double* r = (double*)malloc(sizeof(double) * n);
+    double* z = (double*)malloc(sizeof(double) * n);
+    double* p = (double*)malloc(sizeof(double) * n);
+    double* q = (double*)malloc(sizeof(double) * n);
+    double* dinv = (double*)malloc(sizeof(double) * n);
+    for (long i = 0; i < n; ++i) {
+        long s = find_slot(rowptr, col, i, (int32_t)i);
+        double d = s >= 0 ? vals[s] : 0.0;
+        dinv[i] = d != 0 ? 1.0 / d : 1.0;
+    }
+    orc_spmv(n, rowptr, col, vals, x, q);
+    for (long i = 0; i < n; ++i) r[i] = b[i] - q[i];
+    double bn = sqrt(dot(n, b, b));
+    if (bn == 0) bn = 1;
+    for (long i = 0; i < n; ++i) z[i] = dinv[i] * r[i];
+    memcpy(p, z, sizeof(double) * n);
+    double rz = dot(n, r, z);
+    long it = 0;
+    double rel = sqrt(dot(n, r, r)) / bn;
+    while (rel > rtol && it < maxit) {
+        orc_spmv(n, rowptr, col, vals, p, q);
+        double alpha = rz / dot(n, p, q);
+        for (long i = 0; i < n; ++i) {
+            x[i] += alpha * p[i];
+            r[i] -= alpha * q[i];
+        }
+        for (long i = 0; i < n; ++i) z[i] = dinv[i] * r[i];
+        double rz1 = dot(n, r, z);
+        double beta = rz1 / rz;
+        rz = rz1;
+        for (long i = 0; i < n; ++i) p[i] = z[i] + beta * p[i];
+        ++it;
+        rel = sqrt(dot(n, r, r)) / bn;
+    }
+    if (final_rel) *final_rel = rel;
+    free(r);
+    free(z);
+    free(p);
+    free(q);
+    free(dinv);
+    return rel <= rtol ? it : -1;
+}
+
+/* ---------------------------------------------------------------- CPU baseline */
+
+struct chunk {
+    long nt;
+    const double *XY, *D6;
+    int order;
+    double* A;
+};
+static void* run_chunk(void* arg) {
+    struct chunk* c = (struct chunk*)arg;
+    orc_fem3dtet(22, 22, ORC_TET_SYM, c->order, c->nt, c->XY, c->D6, c->A);
+    return NULL;
+}
+
+double orc_time_p2_sym(long nt, const double* XY, const double* D6, int order, int nthreads, double* A) {
+    struct timespec t0, t1;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    if (nthreads <= 1) {
+        orc_fem3dtet(22, 22, ORC_TET_SYM, order, nt, XY, D6, A);
+    } else {
+        pthread_t th[256];
+        struct chunk cs[256];
+        if (nthreads > 256) nthreads = 256;
+        long per = (nt + nthreads - 1) / nthreads;
+        int k = 0;
+        for (int i = 0; i < nthreads; ++i) {
+            long b = i * per, e = b + per < nt ? b + per : nt;
+            if (b >= e) break;
+            cs[k].nt = e - b;
+            cs[k].XY = XY + 12 * b;
+            cs[k].D6 = D6 + 6 * b;
+            cs[k].order = order;
+            cs[k].A = A + 100 * b;
+            pthread_create(&th[k], NULL, run_chunk, &cs[k]);
+            ++k;
+        }
+        for (int i = 0; i < k; ++i) pthread_join(th[i], NULL);
+    }
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    return (t1.tv_sec - t0.tv_sec) + 1e-9 * (t1.tv_nsec - t0.tv_nsec);
+}

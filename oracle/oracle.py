@@ -1,0 +1,239 @@
+"""ctypes binding of the oracle (test infrastructure only).
+
+    Restated  -- oracle/_build/libanifem_oracle.so: the plain-C restatement (anifem_oracle.c)
+    Reference -- oracle/_ref/libanifem_ref.so: the reference's own fem3Dtet compiled from its
+                 sources (only where the reference sources exist; absent on GPU machines)
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this module.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+RESTATE_PATH = os.path.join(HERE, "_build", "libanifem_oracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libanifem_ref.so")
+
+NULL, CONST_SCALAR, TET_SCALAR, TET_SYM, TET_GENERAL, POINT = range(6)
+
+_vp, _i, _l, _d = ctypes.c_void_p, ctypes.c_int, ctypes.c_long, ctypes.c_double
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def build_restated():
+    if not os.path.exists(RESTATE_PATH):
+        subprocess.run(["make", "-C", HERE, "restate"], check=True, capture_output=True)
+
+
+class Restated:
+    def __init__(self):
+        build_restated()
+        L = ctypes.CDLL(RESTATE_PATH)
+        L.orc_op_info.argtypes = [_i, ctypes.POINTER(_i), ctypes.POINTER(_i)]
+        L.orc_quad_rule.argtypes = [_i, _vp, _vp, _i]
+        L.orc_quad_points.argtypes = [_i, _l, _vp, _vp]
+        L.orc_fem3dtet.argtypes = [_i, _i, _i, _i, _l, _vp, _vp, _vp]
+        L.orc_apply_dir.argtypes = [_i, _vp, _vp, _i, _d]
+        L.orc_orient.argtypes = [_vp, _l, _vp]
+        L.orc_edges.argtypes = [_l, _l, _vp, _vp]
+        L.orc_edges.restype = _l
+        L.orc_element_dofs.argtypes = [_i, _l, _l, _l, _vp, _vp, _vp]
+        L.orc_element_dofs.restype = _l
+        L.orc_csr_template.argtypes = [_l, _l, _i, _vp, _vp, _vp]
+        L.orc_csr_template.restype = _l
+        L.orc_scatter.argtypes = [_l, _vp, _vp, _l, _i, _vp, _vp, _vp, _d, _vp, _vp, _vp]
+        L.orc_csr_compact.argtypes = [_l, _vp, _vp, _vp, _vp]
+        L.orc_csr_compact.restype = _l
+        L.orc_spmv.argtypes = [_l, _vp, _vp, _vp, _vp, _vp]
+        L.orc_true_residual.argtypes = [_l, _vp, _vp, _vp, _vp, _vp]
+        L.orc_true_residual.restype = _d
+        L.orc_jacobi_pcg.argtypes = [_l, _vp, _vp, _vp, _vp, _vp, _d, _l, ctypes.POINTER(_d)]
+        L.orc_jacobi_pcg.restype = _l
+        L.orc_time_p2_sym.argtypes = [_l, _vp, _vp, _i, _i, _vp]
+        L.orc_time_p2_sym.restype = _d
+        self.L = L
+
+    def op_info(self, code):
+        nf, dim = _i(), _i()
+        assert self.L.orc_op_info(code, ctypes.byref(nf), ctypes.byref(dim)) == 0
+        return nf.value, dim.value
+
+    def quadrature(self, order):
+        p = np.zeros(4 * 64)
+        w = np.zeros(64)
+        n = self.L.orc_quad_rule(order, _p(p), _p(w), 64)
+        assert n > 0
+        return p[:4 * n].reshape(n, 4).copy(), w[:n].copy()
+
+    def quad_points(self, order, XY):
+        XY = np.ascontiguousarray(XY, dtype=np.float64)
+        nt = XY.size // 12
+        q = self.quadrature(order)[1].size
+        out = np.zeros((nt, q, 3))
+        self.L.orc_quad_points(order, nt, _p(XY), _p(out))
+        return out
+
+    def fem3dtet(self, codeA, codeB, kind, order, XY, D=None):
+        """A[nt, nfA, nfB] with the memory of the column-major nfB x nfA matrix per tet."""
+        XY = np.ascontiguousarray(XY, dtype=np.float64)
+        nt = XY.size // 12
+        nfA, _ = self.op_info(codeA)
+        nfB, _ = self.op_info(codeB)
+        A = np.zeros((nt, nfA, nfB))
+        Dd = None if D is None else np.ascontiguousarray(D, dtype=np.float64)
+        rc = self.L.orc_fem3dtet(codeA, codeB, kind, order, nt, _p(XY), _p(Dd), _p(A))
+        assert rc == 0, rc
+        return A
+
+    def apply_dir(self, A, F, k, bc):
+        n = F.shape[0]
+        self.L.orc_apply_dir(n, _p(A), _p(F), k, bc)
+
+    def orient(self, xyz, tets):
+        t = np.ascontiguousarray(tets, dtype=np.int32).copy()
+        self.L.orc_orient(_p(np.ascontiguousarray(xyz, dtype=np.float64)), t.shape[0], _p(t))
+        return t
+
+    def edges(self, nv, tets):
+        tets = np.ascontiguousarray(tets, dtype=np.int32)
+        te = np.zeros((tets.shape[0], 6), dtype=np.int32)
+        ne = self.L.orc_edges(nv, tets.shape[0], _p(tets), _p(te))
+        return ne, te
+
+    def element_dofs(self, space, nv, ne, tets, tet_edges):
+        tets = np.ascontiguousarray(tets, dtype=np.int32)
+        nloc = {1: 4, 2: 10, 5: 30}[space]
+        e = np.zeros((tets.shape[0], nloc), dtype=np.int32)
+        te = np.ascontiguousarray(tet_edges, dtype=np.int32) if tet_edges is not None else np.zeros((1, 6), np.int32)
+        nd = self.L.orc_element_dofs(space, nv, ne, tets.shape[0], _p(tets), _p(te), _p(e))
+        return nd, e
+
+    def csr_template(self, ndof, edofs):
+        edofs = np.ascontiguousarray(edofs, dtype=np.int32)
+        nt, nloc = edofs.shape
+        rp = np.zeros(ndof + 1, dtype=np.int64)
+        nnz = self.L.orc_csr_template(ndof, nt, nloc, _p(edofs), _p(rp), None)
+        col = np.zeros(nnz, dtype=np.int32)
+        self.L.orc_csr_template(ndof, nt, nloc, _p(edofs), _p(rp), _p(col))
+        return rp, col
+
+    def scatter(self, rowptr, col, edofs, Aelem, Felem=None, drop=1e-100):
+        edofs = np.ascontiguousarray(edofs, dtype=np.int32)
+        nt, nloc = edofs.shape
+        n = rowptr.size - 1
+        vals = np.zeros(col.size)
+        rhs = np.zeros(n)
+        touched = np.zeros(col.size, dtype=np.uint8)
+        Ae = np.ascontiguousarray(Aelem, dtype=np.float64)
+        Fe = None if Felem is None else np.ascontiguousarray(Felem, dtype=np.float64)
+        rc = self.L.orc_scatter(n, _p(rowptr), _p(col), nt, nloc, _p(edofs), _p(Ae), _p(Fe), drop, _p(vals), _p(rhs),
+                                _p(touched))
+        return rc, vals, rhs, touched
+
+    def csr_compact(self, rowptr, col, vals, touched):
+        rp, c, v = rowptr.copy(), col.copy(), vals.copy()
+        nnz = self.L.orc_csr_compact(rp.size - 1, _p(rp), _p(c), _p(v), _p(np.ascontiguousarray(touched)))
+        return rp, c[:nnz], v[:nnz]
+
+    def spmv(self, rowptr, col, vals, x):
+        y = np.zeros(rowptr.size - 1)
+        self.L.orc_spmv(y.size, _p(rowptr), _p(col), _p(np.ascontiguousarray(vals, dtype=np.float64)),
+                        _p(np.ascontiguousarray(x, dtype=np.float64)), _p(y))
+        return y
+
+    def true_residual(self, rowptr, col, vals, x, b):
+        return self.L.orc_true_residual(rowptr.size - 1, _p(rowptr), _p(col),
+                                        _p(np.ascontiguousarray(vals, dtype=np.float64)),
+                                        _p(np.ascontiguousarray(x, dtype=np.float64)),
+                                        _p(np.ascontiguousarray(b, dtype=np.float64)))
+
+    def jacobi_pcg(self, rowptr, col, vals, b, rtol, maxit):
+        x = np.zeros(rowptr.size - 1)
+        rel = _d()
+        it = self.L.orc_jacobi_pcg(x.size, _p(rowptr), _p(col), _p(np.ascontiguousarray(vals, dtype=np.float64)),
+                                   _p(np.ascontiguousarray(b, dtype=np.float64)), _p(x), rtol, maxit,
+                                   ctypes.byref(rel))
+        return x, it, rel.value
+
+    def time_p2_sym(self, XY, D6, order, nthreads):
+        XY = np.ascontiguousarray(XY, dtype=np.float64)
+        D6 = np.ascontiguousarray(D6, dtype=np.float64)
+        nt = XY.size // 12
+        A = np.zeros((nt, 100))
+        sec = self.L.orc_time_p2_sym(nt, _p(XY), _p(D6), order, nthreads, _p(A))
+        return sec, A
+
+    # ---- the whole restated assembler for a scalar problem (P1 or P2)
+    def assemble_problem(self, xyz, tets, space, kind, D, f_const, order, dirichlet=None, f=None):
+        """orient -> numbering -> template -> element matrices + rhs -> applyDir -> scatter.
+        Returns dict(rowptr, col, vals, rhs, touched, edofs, ndof)."""
+        nv = xyz.shape[0]
+        t = self.orient(xyz, tets)
+        ne, te = self.edges(nv, t) if space == 2 else (0, None)
+        ndof, ed = self.element_dofs(space, nv, ne, t, te)
+        rp, col = self.csr_template(ndof, ed)
+        XY = np.ascontiguousarray(xyz[t].reshape(-1, 12))
+        code = 10 * space + 2
+        A = self.fem3dtet(code, code, kind, order, XY, D)  # [nt, nf, nf] (col-major per tet)
+        rhs_code = 10 * space + 1
+        if f is None:
+            F = self.fem3dtet(1, rhs_code, CONST_SCALAR, order, XY, np.array([f_const]))[:, 0, :]
+        else:
+            F = self.fem3dtet(1, rhs_code, TET_SCALAR, order, XY, np.asarray(f, dtype=np.float64))[:, 0, :]
+        F = np.ascontiguousarray(F)
+        if dirichlet is not None:
+            mask, bc = dirichlet
+            for tt in range(ed.shape[0]):
+                for k in range(ed.shape[1]):
+                    d = ed[tt, k]
+                    if mask[d]:
+                        self.apply_dir(A[tt], F[tt], k, float(bc[d]) if bc is not None else 0.0)
+        rc, vals, rhs, touched = self.scatter(rp, col, ed, A, F)
+        assert rc == 0, rc
+        return dict(rowptr=rp, col=col, vals=vals, rhs=rhs, touched=touched, edofs=ed, ndof=ndof, oriented=t,
+                    nedges=ne)
+
+
+class Reference:
+    """The reference's own fem3Dtet (only where oracle/_ref/libanifem_ref.so was built)."""
+
+    @staticmethod
+    def available():
+        return os.path.exists(REF_PATH)
+
+    def __init__(self):
+        L = ctypes.CDLL(REF_PATH)
+        L.ref_fem3dtet.argtypes = [_i, _i, _i, _i, _l, _vp, _vp, _i, _vp]
+        L.ref_quadrature.argtypes = [_i, _vp, _vp, _i]
+        L.ref_applyDir.argtypes = [_vp, _vp, _i, _i, _d]
+        L.ref_time_p2_sym.argtypes = [_l, _vp, _vp, _i, _i, _vp]
+        L.ref_time_p2_sym.restype = _d
+        self.L = L
+
+    def fem3dtet(self, codeA, codeB, kind, order, XY, D=None, fn=0, nfA=None, nfB=None):
+        XY = np.ascontiguousarray(XY, dtype=np.float64)
+        nt = XY.size // 12
+        A = np.zeros((nt, nfA, nfB))
+        Dd = None if D is None else np.ascontiguousarray(D, dtype=np.float64)
+        rc = self.L.ref_fem3dtet(codeA, codeB, kind, order, nt, _p(XY), _p(Dd), fn, _p(A))
+        assert rc == 0, rc
+        return A
+
+    def quadrature(self, order):
+        p = np.zeros(4 * 128)
+        w = np.zeros(128)
+        n = self.L.ref_quadrature(order, _p(p), _p(w), 128)
+        return p[:4 * n].reshape(n, 4).copy(), w[:n].copy()
+
+    def time_p2_sym(self, XY, D6, order, nthreads):
+        XY = np.ascontiguousarray(XY, dtype=np.float64)
+        D6 = np.ascontiguousarray(D6, dtype=np.float64)
+        nt = XY.size // 12
+        A = np.zeros((nt, 100))
+        sec = self.L.ref_time_p2_sym(nt, _p(XY), _p(D6), order, nthreads, _p(A))
+        return sec, A

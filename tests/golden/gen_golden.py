@@ -1,0 +1,130 @@
+#!/usr/bin/env python3
+"""Generate the golden fixtures of the parity tests from the reference itself.
+
+Run where the reference sources exist (they are not present on GPU machines):
+    make -C oracle ref && python tests/golden/gen_golden.py [REF_ROOT]
+
+Writes tests/golden/golden.npz with
+  * int_tet_test_*   the golden matrices of the reference's own unit tests, read as text
+                     from tests/fem/operations/int_tet_test.cpp (Operations_IntTet_OnePointTensor
+                     :229-243 and :333-346, RhsEval :455) together with their scale factors;
+  * quad_<order>     the reference's tetrahedron rules (quadrature_formulas.cpp:526);
+  * case_<name>_*    inputs and outputs of the reference's fem3Dtet (compiled from its
+                     sources by oracle/Makefile) on seeded random tets, for every operator
+                     pair and tensor kind the GPU path provides.
+"""
+import os
+import re
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+sys.path.insert(0, os.path.join(REPO, "inmost-fem_gb300"))
+
+from oracle.oracle import Reference  # noqa: E402
+from anigpu import meshgen  # noqa: E402
+
+# operator codes: 10*space + op (space 0 P0, 1 P1, 2 P2, 3 P3, 4 Vec3P1, 5 Vec3P2; op 1 IDEN, 2 GRAD)
+NF = {0: 1, 1: 4, 2: 10, 3: 20, 4: 12, 5: 30}
+DIM = {1: 1, 2: 3}
+
+
+def op_nf_dim(code):
+    space, op = divmod(code, 10)
+    nc = 3 if space in (4, 5) else 1
+    return NF[space], DIM[op] * nc
+
+
+def parse_int_tet_test(path):
+    src = open(path).read()
+    # 12 x 20 block of Operations_IntTet_OnePointTensor
+    m = re.search(r"At_exp_m\{std::array<double, 20>\s*(.*?)\};", src, re.S)
+    rows = re.findall(r"\{([^{}]*)\}", m.group(1))
+    A1 = np.array([[float(v) for v in r.replace("\n", " ").split(",") if v.strip()] for r in rows])
+    m = re.search(r"double A_exp_m1p\[\] = \{(.*?)\};", src, re.S)
+    A2 = np.array([float(v) for v in m.group(1).split(",") if v.strip()]).reshape(12, 12)
+    m = re.search(r"Bp\[30\] = \{(.*?)\}", src, re.S)
+    Bp = np.array([float(v) for v in m.group(1).split(",") if v.strip()])
+    return A1, A2, Bp
+
+
+def point_tensor(fn, X, nr, nc):
+    """The analytic per-point fields of oracle/ref_driver.cpp (eval_fn), column-major nr x nc."""
+    x, y, z = X[..., 0], X[..., 1], X[..., 2]
+    if fn == 0:
+        out = np.zeros(X.shape[:-1] + (nr * nc,))
+        cnt = 0
+        for i in range(nr):
+            for j in range(nc):
+                out[..., i + nr * j] = (i * x + j * y + (i % 2) * z) * cnt
+                cnt += 1
+        return out
+    if fn == 2:
+        m = [1 + x * x, x * y / 2, 0 * x, x * y / 2, 1 + y * y, z / 3, 0 * x, z / 3, 2 + z * z]
+        return np.stack(m, axis=-1)
+    raise ValueError(fn)
+
+
+def main():
+    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if not Reference.available():
+        raise SystemExit("build the reference oracle first: make -C oracle ref")
+    R = Reference()
+    out = {}
+    A1, A2, Bp = parse_int_tet_test(os.path.join(ref_root, "tests/fem/operations/int_tet_test.cpp"))
+    out["int_tet_test_onepoint_12x20"] = A1
+    out["int_tet_test_onepoint_coef"] = np.array(9 * 80.0)
+    out["int_tet_test_vecp1_12x12"] = A2
+    out["int_tet_test_vecp1_coef"] = np.array(9 * 160.0)
+    out["int_tet_test_rhs_Bp"] = Bp
+    # the golden tests' tets (XY1p+3 etc. in int_tet_test.cpp:191-201 and :398-403)
+    out["int_tet_test_tet_onepoint"] = np.array([0, 0, 0, 2, 1, 1, 1, 2, 1, 2, 1, 2], dtype=np.float64)
+    out["int_tet_test_tet_rhs"] = np.array([0, 0, 0, 2, 1, 1, 1, 2, 1, 2, 1, 2], dtype=np.float64)
+    for o in range(7):
+        p, w = R.quadrature(o)
+        out[f"quad_{o}_p"] = p
+        out[f"quad_{o}_w"] = w
+
+    nt = 6
+    XY = meshgen.random_tets(nt, seed=11)
+    out["tets_XY"] = XY
+    cases = []
+    scalar_tet = np.exp(meshgen.normal(21, nt))
+    sym6 = meshgen.aniso_tensors(nt, sigma=1.0, seed=22)
+    for (ca, cb) in [(12, 12), (22, 22), (32, 32), (42, 42), (52, 52), (32, 42), (11, 11), (21, 21), (31, 31),
+                     (1, 11), (1, 21), (1, 51), (12, 22), (22, 12)]:
+        nfA, dA = op_nf_dim(ca)
+        nfB, dB = op_nf_dim(cb)
+        kinds = []
+        if dA == dB or dA == 1:
+            kinds += [("null", 0, None), ("cscalar", 1, np.array([2.5])), ("tscalar", 2, scalar_tet)]
+        if dA == 3 and dB == 3:
+            kinds += [("tsym", 3, sym6)]
+        gen = (meshgen.uniform(31 + ca + cb, nt * dA * dB) - 0.5).reshape(nt, dA * dB)
+        kinds += [("tgeneral", 4, gen)]
+        for order in (2, 4, 5, 6):
+            for kname, kind, D in kinds:
+                name = f"{ca}_{cb}_{kname}_o{order}"
+                A = R.fem3dtet(ca, cb, kind, order, XY, D, nfA=nfA, nfB=nfB)
+                out[f"case_{name}_A"] = A
+                if D is not None:
+                    out[f"case_{name}_D"] = np.asarray(D, dtype=np.float64)
+                cases.append(name)
+            # per-point analytic field (fn 0 general; fn 2 symmetric 3x3)
+            fns = [0] + ([2] if (dA == 3 and dB == 3) else [])
+            for fn in fns:
+                name = f"{ca}_{cb}_point{fn}_o{order}"
+                A = R.fem3dtet(ca, cb, 5, order, XY, None, fn=fn, nfA=nfA, nfB=nfB)
+                out[f"case_{name}_A"] = A
+                cases.append(name)
+    out["case_names"] = np.array(cases)
+    path = os.path.join(HERE, "golden.npz")
+    np.savez_compressed(path, **out)
+    print(path, len(cases), "cases", os.path.getsize(path), "bytes")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,173 @@
+"""GPU parity of the global path: DOF numbering, CSR template (bit-exact), row-gather
+assembly with Dirichlet elimination, drop-rule pattern, and the Krylov solves, against the
+restated oracle on the same seeded inputs."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _problem(lib, restated, n, space, perturb, kind, order, dirichlet=True, seed=1, f=None, bc_value=None):
+    import anigpu
+    from anigpu import meshgen
+    xyz, tets = meshgen.kuhn_cube(n, perturb=perturb, seed=seed)
+    nt = tets.shape[0]
+    D = None
+    if kind == anigpu.TENSOR_TET_SYM:
+        D = meshgen.aniso_tensors(nt, 1.5, seed + 10)
+    elif kind == anigpu.TENSOR_TET_SCALAR:
+        D = np.exp(meshgen.normal(seed + 20, nt))
+    elif kind == anigpu.TENSOR_CONST_SCALAR:
+        D = np.array([1.7])
+    lib.mesh_upload(xyz, tets)
+    ndof, nnz = lib.problem_setup(space)
+    coords = lib.dof_coords().cpu().numpy()
+    mask = meshgen.boundary_mask(coords) if dirichlet else np.zeros(ndof, np.uint8)
+    bc = None
+    if bc_value is not None:
+        bc = np.where(mask == 1, bc_value(coords), 0.0)
+    lib.set_dirichlet(mask if dirichlet else None, bc)
+    ref = restated.assemble_problem(xyz, tets, space, kind, D, 1.0, order,
+                                    dirichlet=(mask, bc) if dirichlet else None, f=f)
+    return dict(xyz=xyz, tets=tets, D=D, mask=mask, ref=ref, ndof=ndof, nnz=nnz, bc=bc)
+
+
+@pytest.mark.parametrize("space,n,perturb", [(1, 4, 0.0), (1, 5, 0.2), (2, 3, 0.0), (2, 4, 0.2)])
+def test_numbering_and_template_bit_exact(lib, restated, space, n, perturb):
+    import anigpu
+    P = _problem(lib, restated, n, space, perturb, anigpu.TENSOR_NULL, 2)
+    ref = P["ref"]
+    assert P["ndof"] == ref["ndof"]
+    ed = lib.element_dofs().cpu().numpy()
+    assert np.array_equal(ed, ref["edofs"])
+    rp, col = lib.csr_template()
+    assert np.array_equal(rp.cpu().numpy(), ref["rowptr"])
+    assert np.array_equal(col.cpu().numpy(), ref["col"])
+
+
+@pytest.mark.parametrize("space,kind,order", [(1, 0, 2), (1, 2, 2), (2, 3, 4), (2, 1, 4), (2, 3, 2), (2, 0, 5)])
+def test_assembly_f64_matches_oracle(lib, restated, space, kind, order):
+    import anigpu
+    P = _problem(lib, restated, 4, space, 0.2, kind, order)
+    vals, rhs, touched = lib.assemble(kind, P["D"], None, 1.0, order, anigpu.F64, touched=True)
+    ref = P["ref"]
+    v = vals.cpu().numpy()
+    scale = np.abs(ref["vals"]).max()
+    assert np.abs(v - ref["vals"]).max() <= 1e-12 * scale
+    assert np.abs(rhs.cpu().numpy() - ref["rhs"]).max() <= 1e-12 * max(np.abs(ref["rhs"]).max(), 1e-300)
+    assert np.array_equal(touched.cpu().numpy(), ref["touched"])
+
+
+def test_assembly_f32_error(lib, restated):
+    import anigpu
+    P = _problem(lib, restated, 5, 2, 0.2, anigpu.TENSOR_TET_SYM, 4)
+    vals, rhs, _ = lib.assemble(anigpu.TENSOR_TET_SYM, P["D"], None, 1.0, 4, anigpu.F32)
+    ref = P["ref"]
+    rp = ref["rowptr"]
+    v = vals.double().cpu().numpy()
+    # per-row relative error against the FP64 oracle
+    rows = np.repeat(np.arange(rp.size - 1), np.diff(rp))
+    rown = np.sqrt(np.bincount(rows, ref["vals"] ** 2))
+    err = np.sqrt(np.bincount(rows, (v - ref["vals"]) ** 2)) / np.maximum(rown, 1e-300)
+    print("FP32 assembly: max/median per-row relative error", err.max(), np.median(err))
+    assert err.max() <= 5e-5
+
+
+def test_assembly_nonhomogeneous_dirichlet(lib, restated):
+    import anigpu
+    P = _problem(lib, restated, 4, 2, 0.15, anigpu.TENSOR_TET_SCALAR, 4,
+                 bc_value=lambda c: 1.0 + c[:, 0] - 2 * c[:, 2])
+    vals, rhs, _ = lib.assemble(anigpu.TENSOR_TET_SCALAR, P["D"], None, 1.0, 4, anigpu.F64)
+    ref = P["ref"]
+    assert np.abs(vals.cpu().numpy() - ref["vals"]).max() <= 1e-12 * np.abs(ref["vals"]).max()
+    assert np.abs(rhs.cpu().numpy() - ref["rhs"]).max() <= 1e-12 * np.abs(ref["rhs"]).max()
+
+
+def test_per_tet_source(lib, restated):
+    import anigpu
+    from anigpu import meshgen
+    f = meshgen.normal(99, 6 * 4 ** 3)
+    P = _problem(lib, restated, 4, 1, 0.1, anigpu.TENSOR_NULL, 2, f=f)
+    vals, rhs, _ = lib.assemble(anigpu.TENSOR_NULL, None, f, 0.0, 2, anigpu.F64)
+    assert np.abs(rhs.cpu().numpy() - P["ref"]["rhs"]).max() <= 1e-12 * np.abs(P["ref"]["rhs"]).max()
+
+
+def test_drop_rule_pattern(lib, restated):
+    """The assembler without a template keeps only |a| > drop entries plus the diagonal
+    (assembler.inl:114-135,416-418); Dirichlet rows/columns create exact zeros."""
+    import anigpu
+    P = _problem(lib, restated, 5, 1, 0.0, anigpu.TENSOR_NULL, 2)
+    vals, rhs, touched = lib.assemble(anigpu.TENSOR_NULL, None, None, 1.0, 2, anigpu.F64, touched=True)
+    rp, col = lib.csr_template()
+    nnz = lib.csr_compact(rp, col, vals, anigpu.F64, touched)
+    ref = P["ref"]
+    rp_o, col_o, v_o = restated.csr_compact(ref["rowptr"], ref["col"], ref["vals"], ref["touched"])
+    assert nnz == col_o.size < P["nnz"]
+    assert np.array_equal(rp.cpu().numpy(), rp_o)
+    assert np.array_equal(col[:nnz].cpu().numpy(), col_o)
+    assert np.abs(vals[:nnz].cpu().numpy() - v_o).max() <= 1e-12 * np.abs(v_o).max()
+
+
+def test_assembly_is_deterministic(lib, restated):
+    import anigpu
+    P = _problem(lib, restated, 6, 2, 0.2, anigpu.TENSOR_TET_SYM, 4, dirichlet=True)
+    a1, r1, _ = lib.assemble(anigpu.TENSOR_TET_SYM, P["D"], None, 1.0, 4, anigpu.F32)
+    a2, r2, _ = lib.assemble(anigpu.TENSOR_TET_SYM, P["D"], None, 1.0, 4, anigpu.F32)
+    assert bool((a1 == a2).all()) and bool((r1 == r2).all())
+
+
+def test_nonfinite_tensor_reports_status(lib, restated):
+    import anigpu
+    P = _problem(lib, restated, 3, 2, 0.0, anigpu.TENSOR_TET_SCALAR, 4, dirichlet=False)
+    D = P["D"].copy()
+    D[5] = np.nan  # injected on the host
+    with pytest.raises(anigpu.AnigpuError) as e:
+        lib.assemble(anigpu.TENSOR_TET_SCALAR, D, None, 1.0, 4, anigpu.F64)
+    assert e.value.code == anigpu.ERR_NONFINITE
+    # the handle stays usable
+    vals, rhs, _ = lib.assemble(anigpu.TENSOR_TET_SCALAR, P["D"], None, 1.0, 4, anigpu.F64)
+    assert np.isfinite(vals.cpu().numpy()).all()
+
+
+def test_config1_end_to_end(lib, restated):
+    """Config 1: P1 Poisson on 16^3 x 6 Kuhn tets, identity tensor, order 2, f = 1,
+    homogeneous Dirichlet, Jacobi-PCG to 1e-10."""
+    import anigpu
+    P = _problem(lib, restated, 16, 1, 0.0, anigpu.TENSOR_NULL, 2)
+    vals, rhs, _ = lib.assemble(anigpu.TENSOR_NULL, None, None, 1.0, 2, anigpu.F64)
+    ref = P["ref"]
+    assert np.abs(vals.cpu().numpy() - ref["vals"]).max() <= 1e-12 * np.abs(ref["vals"]).max()
+    x, st = lib.solve(vals, rhs, anigpu.SOLVE_JACOBI_PCG, anigpu.F64, rtol=1e-10, maxit=20000)
+    xh = x.cpu().numpy()
+    tr = restated.true_residual(ref["rowptr"], ref["col"], ref["vals"], xh, ref["rhs"])
+    assert tr <= 1e-10 and st.rel_residual <= 1e-10
+    xo, it_o, rel_o = restated.jacobi_pcg(ref["rowptr"], ref["col"], ref["vals"], ref["rhs"], 1e-10, 20000)
+    assert abs(st.iterations - it_o) <= 2
+    assert np.abs(xh - xo).max() <= 1e-8 * np.abs(xo).max()
+
+
+def test_ir_cg32_reaches_fp64_tolerance(lib, restated):
+    import anigpu
+    P = _problem(lib, restated, 8, 2, 0.2, anigpu.TENSOR_TET_SYM, 4)
+    vals32, rhs, _ = lib.assemble(anigpu.TENSOR_TET_SYM, P["D"], None, 1.0, 4, anigpu.F32)
+    x, st = lib.solve(vals32, rhs, anigpu.SOLVE_IR_CG32, anigpu.F32, rtol=1e-8, maxit=200000)
+    assert st.rel_residual <= 1e-8 and st.outer_iterations >= 1
+    ref = P["ref"]
+    # FP64 true residual against the FP32-assembled matrix (the system that is solved)
+    v32 = vals32.double().cpu().numpy()
+    assert restated.true_residual(ref["rowptr"], ref["col"], v32, x.cpu().numpy(), ref["rhs"]) <= 1e-8
+    # and against the FP64 oracle matrix: bounded by the FP32 assembly error
+    tr64 = restated.true_residual(ref["rowptr"], ref["col"], ref["vals"], x.cpu().numpy(), ref["rhs"])
+    print("IR-CG32 residual vs FP64 oracle matrix:", tr64)
+    assert tr64 <= 1e-4
+
+
+def test_spmv_matches_oracle(lib, restated):
+    import anigpu
+    P = _problem(lib, restated, 5, 2, 0.2, anigpu.TENSOR_TET_SYM, 4)
+    vals, rhs, _ = lib.assemble(anigpu.TENSOR_TET_SYM, P["D"], None, 1.0, 4, anigpu.F64)
+    xx = np.sin(np.arange(P["ndof"]) * 0.37)
+    y = lib.spmv(vals, xx).cpu().numpy()
+    ref = P["ref"]
+    yo = restated.spmv(ref["rowptr"], ref["col"], ref["vals"], xx)
+    assert np.abs(y - yo).max() <= 1e-12 * np.abs(yo).max()

@@ -1,0 +1,113 @@
+"""GPU parity of the batched fem3Dtet (anigpu_fem3dtet) against the reference's own
+fem3Dtet outputs (tests/golden/golden.npz) and the reference's golden matrices."""
+import numpy as np
+import pytest
+
+from helpers import KIND_CODE, op_nf_dim, parse_case, point_tensor, ref_tol, rel_err_per_tet
+
+pytestmark = pytest.mark.gpu
+
+
+def _run_case(lib, golden, name, precision):
+    import anigpu
+    XY = golden["tets_XY"]
+    ca, cb, kind, order = parse_case(name)
+    nfA, dA = op_nf_dim(ca)
+    nfB, dB = op_nf_dim(cb)
+    if kind.startswith("point"):
+        fn = int(kind[5:])
+        q = lib.quadrature_points(order, XY).cpu().numpy()
+        D = point_tensor(fn, q, dB, dA)
+        A = lib.fem3dtet(ca, cb, XY, D, anigpu.TENSOR_POINT, order, precision)
+    else:
+        D = golden[f"case_{name}_D"] if f"case_{name}_D" in golden.files else None
+        A = lib.fem3dtet(ca, cb, XY, D, KIND_CODE[kind], order, precision)
+    return A.double().cpu().numpy()
+
+
+def test_fem3dtet_f64_matches_reference(lib, golden):
+    import anigpu
+    worst = 0.0
+    for name in golden["case_names"]:
+        name = str(name)
+        A = _run_case(lib, golden, name, anigpu.F64)
+        err = rel_err_per_tet(A, golden[f"case_{name}_A"])
+        worst = max(worst, err)
+        assert err <= 1e-12, (name, err)
+    print("worst FP64 relative error per tet:", worst)
+
+
+def test_fem3dtet_f32_error_bound(lib, golden):
+    import anigpu
+    worst = 0.0
+    for name in golden["case_names"]:
+        name = str(name)
+        A = _run_case(lib, golden, name, anigpu.F32)
+        err = rel_err_per_tet(A, golden[f"case_{name}_A"])
+        worst = max(worst, err)
+        assert err <= 2e-5, (name, err)
+    print("worst FP32 relative error per tet:", worst)
+
+
+def test_golden_matrices_on_gpu(lib, golden):
+    import anigpu
+    XY = golden["int_tet_test_tet_onepoint"].reshape(1, 12)
+    exp = golden["int_tet_test_onepoint_12x20"] / golden["int_tet_test_onepoint_coef"]
+    for order in (5, 6):
+        q = lib.quadrature_points(order, XY).cpu().numpy()
+        D = point_tensor(0, q, 9, 3)
+        A = lib.fem3dtet(32, 42, XY, D, anigpu.TENSOR_POINT, order).cpu().numpy()[0].T
+        assert np.linalg.norm(A - exp) <= ref_tol(A)
+    exp = golden["int_tet_test_vecp1_12x12"] / golden["int_tet_test_vecp1_coef"]
+    for kind, D in ((anigpu.TENSOR_NULL, None), (anigpu.TENSOR_CONST_SCALAR, np.array([1.0])),
+                    (anigpu.TENSOR_TET_GENERAL, np.eye(9).reshape(1, 81))):
+        A = lib.fem3dtet(42, 42, XY, D, kind, 5).cpu().numpy()[0].T
+        assert np.linalg.norm(A - exp) <= ref_tol(A)
+    Bp = golden["int_tet_test_rhs_Bp"]
+    XYr = golden["int_tet_test_tet_rhs"].reshape(1, 12)
+    for k in (1, 2):
+        A = lib.fem3dtet(1, 51, XYr, np.array([40.0 * k]), anigpu.TENSOR_CONST_SCALAR, 2).cpu().numpy()[0, 0]
+        assert np.linalg.norm(A - k * Bp) <= ref_tol(A)
+
+
+def test_fem3dtet_large_batch_vs_oracle(lib, restated):
+    """A batch larger than the grid (grid-stride loop) against the restated oracle."""
+    import anigpu
+    from anigpu import meshgen
+    XY = meshgen.random_tets(5000, seed=77)
+    D6 = meshgen.aniso_tensors(5000, 1.5, 78)
+    A = lib.fem3dtet(22, 22, XY, D6, anigpu.TENSOR_TET_SYM, 4).cpu().numpy()
+    Ao = restated.fem3dtet(22, 22, 3, 4, XY, D6)
+    assert rel_err_per_tet(A, Ao) <= 1e-12
+
+
+def test_apply_dir_on_gpu(lib, restated):
+    import torch
+    rng = np.random.default_rng(3)
+    nt, n = 7, 10
+    A = rng.standard_normal((nt, n, n))
+    F = rng.standard_normal((nt, n))
+    mask = rng.integers(0, 1 << n, nt).astype(np.int32)
+    bc = rng.standard_normal((nt, n))
+    Ad = torch.tensor(A, device="cuda")
+    Fd = torch.tensor(F, device="cuda")
+    lib.apply_dir(Ad, Fd, mask, bc)
+    torch.cuda.synchronize()
+    for t in range(nt):
+        a, f = A[t].copy(), F[t].copy()
+        for k in range(n):
+            if (mask[t] >> k) & 1:
+                restated.apply_dir(a, f, k, bc[t, k])
+        assert np.array_equal(Ad[t].cpu().numpy(), a)
+        assert np.allclose(Fd[t].cpu().numpy(), f, rtol=0, atol=1e-14)
+
+
+def test_errors_are_reported(lib):
+    import anigpu
+    XY = np.zeros((1, 12))
+    with pytest.raises(anigpu.AnigpuError) as e:
+        lib.fem3dtet(22, 22, XY, None, anigpu.TENSOR_NULL, 9)  # order above 6
+    assert e.value.code == anigpu.ERR_UNSUPPORTED
+    with pytest.raises(anigpu.AnigpuError) as e:
+        lib.fem3dtet(22, 51, XY, None, anigpu.TENSOR_NULL, 2)  # identity of incompatible dims
+    assert e.value.code == anigpu.ERR_ARG
