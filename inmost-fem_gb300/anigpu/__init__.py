@@ -112,6 +112,16 @@ def quadrature(order):
     return p[:4 * n].reshape(n, 4).copy(), w[:n].copy()
 
 
+def _streamed(fn):
+    import functools
+
+    @functools.wraps(fn)
+    def wrap(self, *a, **k):
+        with self.on_stream():
+            return fn(self, *a, **k)
+    return wrap
+
+
 def _ptr(t):
     return None if t is None else ctypes.c_void_p(t.data_ptr())
 
@@ -119,7 +129,7 @@ def _ptr(t):
 class Anigpu:
     """One library handle: one device, one stream (the caller's torch stream by default)."""
 
-    def __init__(self, device=0, use_torch_stream=True):
+    def __init__(self, device=0):
         import torch
         if not torch.cuda.is_available():
             raise RuntimeError("anigpu needs a CUDA device (no CPU fallback)")
@@ -129,10 +139,29 @@ class Anigpu:
         h = ctypes.c_void_p()
         self._check(self.lib.anigpu_create(ctypes.byref(h), device), None)
         self.h = h
-        if use_torch_stream:
-            with torch.cuda.device(device):
-                self.set_stream(torch.cuda.current_stream().cuda_stream)
+        # one stream for the torch plumbing and the library kernels of this handle
+        self.stream = torch.cuda.Stream(device=device)
+        self.set_stream(self.stream.cuda_stream)
         self.space = None
+
+    class _OnStream:
+        def __init__(self, outer):
+            self.o = outer
+
+        def __enter__(self):
+            t = self.o.torch
+            self.caller = t.cuda.current_stream(self.o.device)
+            self.o.stream.wait_stream(self.caller)
+            self.ctx = t.cuda.stream(self.o.stream)
+            self.ctx.__enter__()
+
+        def __exit__(self, *a):
+            self.ctx.__exit__(*a)
+            self.caller.wait_stream(self.o.stream)
+
+    def on_stream(self):
+        """Context in which torch work and library calls share the handle's stream."""
+        return Anigpu._OnStream(self)
 
     # -------------------------------------------------------------- plumbing
     def _check(self, rc, h="self"):
@@ -169,6 +198,7 @@ class Anigpu:
         return a.to(device=f"cuda:{self.device}", dtype=dtype).contiguous()
 
     # -------------------------------------------------------------- element level
+    @_streamed
     def fem3dtet(self, opA, opB, XY, D=None, kind=TENSOR_NULL, order=5, precision=F64, out=None):
         """Element matrices of a batch of tets: A[nt, nfA, nfB] whose per-tet memory is the
         column-major nfB x nfA DenseMatrix of fem3Dtet (so A[t].T is A(i_test, j_trial))."""
@@ -185,6 +215,7 @@ class Anigpu:
                                              _ptr(out)))
         return out
 
+    @_streamed
     def quadrature_points(self, order, XY):
         torch = self.torch
         XY = self._dev(XY, torch.float64)
@@ -194,6 +225,7 @@ class Anigpu:
         self._check(self.lib.anigpu_quadrature_points(self.h, order, nt, _ptr(XY), _ptr(out)))
         return out
 
+    @_streamed
     def apply_dir(self, A, F, mask, bc=None):
         torch = self.torch
         nt, n = F.shape[0], F.shape[1]
@@ -202,6 +234,7 @@ class Anigpu:
         self._check(self.lib.anigpu_apply_dir(self.h, nt, n, _ptr(A), _ptr(F), _ptr(m), _ptr(b)))
 
     # -------------------------------------------------------------- global problem
+    @_streamed
     def mesh_upload(self, xyz, tets):
         torch = self.torch
         self._xyz = self._dev(xyz, torch.float64)
@@ -210,10 +243,12 @@ class Anigpu:
         self.nt = self._tets.numel() // 4
         self._check(self.lib.anigpu_mesh_upload(self.h, self.nv, _ptr(self._xyz), self.nt, _ptr(self._tets)))
 
+    @_streamed
     def update_coords(self, xyz):
         self._xyz = self._dev(xyz, self.torch.float64)
         self._check(self.lib.anigpu_mesh_update_coords(self.h, _ptr(self._xyz)))
 
+    @_streamed
     def problem_setup(self, space):
         self._check(self.lib.anigpu_problem_setup(self.h, space))
         self.space = space
@@ -222,6 +257,7 @@ class Anigpu:
         self.ndof, self.nnz, self.nedges = nd.value, nz.value, ne.value
         return self.ndof, self.nnz
 
+    @_streamed
     def csr_template(self):
         torch = self.torch
         rp = torch.empty(self.ndof + 1, dtype=torch.int64, device=f"cuda:{self.device}")
@@ -229,6 +265,7 @@ class Anigpu:
         self._check(self.lib.anigpu_csr_template(self.h, _ptr(rp), _ptr(col)))
         return rp, col
 
+    @_streamed
     def element_dofs(self):
         torch = self.torch
         nloc = 4 if self.space == P1 else 10
@@ -236,18 +273,21 @@ class Anigpu:
         self._check(self.lib.anigpu_element_dofs(self.h, _ptr(e)))
         return e
 
+    @_streamed
     def dof_coords(self):
         torch = self.torch
         c = torch.empty((self.ndof, 3), dtype=torch.float64, device=f"cuda:{self.device}")
         self._check(self.lib.anigpu_dof_coords(self.h, _ptr(c)))
         return c
 
+    @_streamed
     def set_dirichlet(self, mask=None, bc=None):
         torch = self.torch
         self._dmask = self._dev(mask, torch.uint8) if mask is not None else None
         self._dbc = self._dev(bc, torch.float64) if bc is not None else None
         self._check(self.lib.anigpu_set_dirichlet(self.h, _ptr(self._dmask), _ptr(self._dbc)))
 
+    @_streamed
     def assemble(self, kind=TENSOR_NULL, D=None, f=None, f_const=1.0, order=2, precision=F64, vals=None, rhs=None,
                  touched=False, drop=1e-100):
         """AssemblerT::Assemble: returns (vals[nnz], rhs[ndof], touched[nnz] or None)."""
@@ -265,12 +305,14 @@ class Anigpu:
                                              _ptr(vals), _ptr(rhs), _ptr(tch), float(drop)))
         return vals, rhs, tch
 
+    @_streamed
     def csr_compact(self, rowptr, col, vals, precision, touched):
         n = ctypes.c_int64()
         self._check(self.lib.anigpu_csr_compact(self.h, _ptr(rowptr), _ptr(col), _ptr(vals), precision,
                                                 _ptr(touched), ctypes.byref(n)))
         return n.value
 
+    @_streamed
     def spmv(self, vals, x, precision=F64):
         torch = self.torch
         x = self._dev(x, torch.float64)
@@ -278,6 +320,7 @@ class Anigpu:
         self._check(self.lib.anigpu_spmv(self.h, _ptr(vals), precision, _ptr(x), _ptr(y)))
         return y
 
+    @_streamed
     def solve(self, vals, b, method=SOLVE_JACOBI_PCG, precision=F64, x0=None, rtol=1e-10, maxit=100000,
               check=True):
         """Returns (x, stats).  stats: SolveStats (iterations, outer_iterations, rel_residual, seconds)."""
