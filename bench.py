@@ -1,0 +1,358 @@
+#!/usr/bin/env python3
+"""Benchmark of the anigpu hot path on the P2 anisotropic-diffusion workload.
+
+Workload (one "step"): global assembly of the P2 GRAD.GRAD stiffness matrix and the
+right-hand side of  -div(D grad u) = 1  on a 64^3 x 6 perturbed Kuhn mesh
+(1,572,864 tets, 2,146,689 DOFs), per-tet SPD tensors D = R diag(exp g) R^T with
+g ~ N(0, 1.5^2), quadrature order 4, homogeneous Dirichlet on the boundary, FP32 element
+matrices with FP32 accumulation (FP64 geometry on badly shaped tets), written into the
+CSR template.  Metric: tets assembled per second.  After the timed steps the same run
+measures time-to-tolerance (FP64 true residual 1e-8) of the solvers on that system.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--n 64]
+
+--impl reference times the reference's CPU element-matrix loop over a bounded sample of
+the same tets on all host cores (the oracle port of fem3Dtet, since the reference sources
+are not present on GPU machines), and prints the same JSON line with "impl": "reference".
+With N > 1 (torchrun) every rank runs an independent replica of the workload (the path
+needs no exchange between GPUs) and rank 0 prints the aggregate.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+for _p in (REPO, os.path.join(REPO, "inmost-fem_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "P2 tets assembled/s (%HBM roofline); time to 1e-8 residual, FCG vs Jacobi-PCG"
+UNIT = "tets/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=64, help="cubes per axis (64 -> 1,572,864 tets)")
+    ap.add_argument("--no-solve", action="store_true")
+    ap.add_argument("--cpu-sample", type=int, default=0, help="tets in the CPU-baseline sample (0 = auto)")
+    return ap.parse_args()
+
+
+def workload(n, seed=2024):
+    from anigpu import meshgen
+    xyz, tets = meshgen.kuhn_cube(n, perturb=0.2, seed=seed)
+    D6 = meshgen.aniso_tensors(tets.shape[0], 1.5, seed + 1)
+    return xyz, tets, D6
+
+
+def peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as fh:
+            p = json.load(fh)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax = max(smax, float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        dist.init_process_group(backend=backend)
+        pg = dist
+    return world, rank, local, pg
+
+
+def cpu_baseline(xyz, tets, D6, sample, threads):
+    """The reference's element-matrix loop (oracle port of fem3Dtet, P2 GRAD.GRAD,
+    per-tet symmetric tensor, order 4) on `sample` tets over `threads` host threads."""
+    from oracle.oracle import Restated
+    from anigpu import meshgen
+    orc = Restated()
+    XY = meshgen.tet_coords(xyz, tets[:sample])
+    sec, _ = orc.time_p2_sym(XY, D6[:sample], 4, threads)
+    return sample / sec, sec
+
+
+def run_reference(args):
+    world, rank, local, pg = dist_setup(args)
+    if rank != 0:
+        return
+    n = args.n
+    xyz, tets, D6 = workload(n)
+    threads = os.cpu_count() or 1
+    sample = args.cpu_sample or tets.shape[0]
+    vals = []
+    for _ in range(args.warmup):
+        cpu_baseline(xyz, tets, D6, min(sample, 20000), threads)
+    secs = []
+    for _ in range(args.steps):
+        v, s = cpu_baseline(xyz, tets, D6, sample, threads)
+        vals.append(v)
+        secs.append(s)
+    value = statistics.median(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median(secs),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"P2 element matrices of {6 * n ** 3} tets (sample of {sample} per step), "
+                               f"perturbed Kuhn {n}^3, anisotropic per-tet tensor, order 4",
+                   "parallelism": f"{threads} host threads"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{sample} tets per step, fem3Dtet P2 GRAD.GRAD loop, {threads} threads"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    world, rank, local, pg = dist_setup(args)
+    torch.cuda.set_device(local)
+    import anigpu
+    from anigpu import meshgen
+    n = args.n
+    xyz, tets, D6 = workload(n)
+    nt, nv = tets.shape[0], xyz.shape[0]
+    lib = anigpu.Anigpu(local)
+    dev = f"cuda:{local}"
+    t0 = time.time()
+    lib.mesh_upload(xyz, tets)
+    ndof, nnz = lib.problem_setup(anigpu.P2)
+    mask = meshgen.boundary_mask(lib.dof_coords().cpu().numpy())
+    lib.set_dirichlet(mask)
+    torch.cuda.synchronize()
+    setup_s = time.time() - t0
+    D_dev = torch.tensor(D6, device=dev)
+    vals32 = torch.empty(nnz, dtype=torch.float32, device=dev)
+    rhs = torch.empty(ndof, dtype=torch.float64, device=dev)
+    stream = lib.stream
+
+    def step():
+        lib.assemble(anigpu.TENSOR_TET_SYM, D_dev, None, 1.0, 4, anigpu.F32, vals32, rhs)
+
+    lib.set_timing(True)
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    if pg:
+        pg.barrier()
+    launches0 = lib.launch_count()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    phase_ms = []
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        for k in range(args.steps):
+            ev[k][0].record(stream)
+            step()
+            ev[k][1].record(stream)
+            phase_ms.append(lib.last_timing())
+        torch.cuda.synchronize()
+    launches = lib.launch_count() - launches0
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    ms = float(np.mean(step_ms))
+    if pg:
+        t = torch.tensor([ms], device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * nt / (ms * 1e-3)
+    phases = np.array(phase_ms)  # [steps, 2]: prepare, rows
+    prep_ms, rows_ms = float(phases[:, 0].mean()), float(phases[:, 1].mean())
+    # algorithmic bytes of one assembly (inputs read once, outputs written once)
+    b_alg = nt * 16 + nv * 24 + nt * 48 + nnz * 4 + ndof * 8
+    peak, peak_kind = peaks()
+    ach = b_alg / ((prep_ms + rows_ms) * 1e-3) / 1e9
+    traffic = None
+    tfile = os.path.join(REPO, "profiles", "assembly_traffic.json")
+    if os.path.exists(tfile):
+        try:
+            with open(tfile) as fh:
+                traffic = json.load(fh).get("bytes_per_assembly_n%d" % n)
+        except Exception:
+            traffic = None
+
+    # end to end through the public API with host buffers: H2D of the step's inputs
+    # (coordinates and tensors, pinned), assembly, D2H of the matrix values and rhs
+    xyz_h = torch.tensor(xyz).pin_memory()
+    D_h = torch.tensor(D6).pin_memory()
+    vals_h = torch.empty(nnz, dtype=torch.float32).pin_memory()
+    rhs_h = torch.empty(ndof, dtype=torch.float64).pin_memory()
+    xyz_d = torch.empty_like(xyz_h, device=dev)
+    D_d2 = torch.empty_like(D_h, device=dev)
+    h2d = xyz_h.numel() * 8 + D_h.numel() * 8
+    d2h = nnz * 4 + ndof * 8
+
+    def e2e_step():
+        with torch.cuda.stream(stream):
+            xyz_d.copy_(xyz_h, non_blocking=True)
+            D_d2.copy_(D_h, non_blocking=True)
+        lib.update_coords(xyz_d)
+        lib.assemble(anigpu.TENSOR_TET_SYM, D_d2, None, 1.0, 4, anigpu.F32, vals32, rhs)
+        with torch.cuda.stream(stream):
+            vals_h.copy_(vals32, non_blocking=True)
+            rhs_h.copy_(rhs, non_blocking=True)
+
+    for _ in range(3):
+        e2e_step()
+    torch.cuda.synchronize()
+    ee = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for k in range(args.steps):
+        ee[k][0].record(stream)
+        e2e_step()
+        ee[k][1].record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = float(np.mean([a.elapsed_time(b) for a, b in ee]))
+    if pg:
+        t = torch.tensor([e2e_ms], device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+
+    # FP64 plain path (parity arithmetic) for comparison
+    vals64 = torch.empty(nnz, dtype=torch.float64, device=dev)
+    rhs64 = torch.empty(ndof, dtype=torch.float64, device=dev)
+    lib.assemble(anigpu.TENSOR_TET_SYM, D_dev, None, 1.0, 4, anigpu.F64, vals64, rhs64)
+    f64_ms = []
+    for _ in range(3):
+        lib.assemble(anigpu.TENSOR_TET_SYM, D_dev, None, 1.0, 4, anigpu.F64, vals64, rhs64)
+        f64_ms.append(sum(lib.last_timing()))
+    f64_ms = float(np.mean(f64_ms))
+    lib.set_timing(False)
+
+    solve = None
+    if not args.no_solve:
+        solve = {}
+        x, st = lib.solve(vals64, rhs64, anigpu.SOLVE_JACOBI_PCG, anigpu.F64, rtol=1e-8, maxit=200000, check=False)
+        solve["jacobi_pcg_f64"] = {"seconds": st.seconds, "iterations": st.iterations,
+                                   "rel_residual_f64": st.rel_residual}
+        x, st = lib.solve(vals32, rhs, anigpu.SOLVE_IR_CG32, anigpu.F32, rtol=1e-8, maxit=200000, check=False)
+        # error of the mixed solution against the FP64-assembled system
+        r64 = rhs64 - lib.spmv(vals64, x, anigpu.F64)
+        solve["ir_cg32"] = {"seconds": st.seconds, "iterations": st.iterations, "outer": st.outer_iterations,
+                            "rel_residual_f64": st.rel_residual,
+                            "rel_residual_vs_f64_matrix": float(r64.norm() / rhs64.norm())}
+        try:
+            x, st = lib.solve(vals32, rhs, anigpu.SOLVE_FCG_LEARNED, anigpu.F32, rtol=1e-8, maxit=200000,
+                              check=True)
+            solve["fcg_learned"] = {"seconds": st.seconds, "iterations": st.iterations,
+                                    "rel_residual_f64": st.rel_residual, "fallback_steps": st.fallback_steps}
+        except anigpu.AnigpuError as e:
+            solve["fcg_learned"] = {"unavailable": str(e)}
+
+    if rank != 0:
+        return
+    cpu = None
+    if world == 1:
+        threads = os.cpu_count() or 1
+        sample = args.cpu_sample or nt
+        v, sec = cpu_baseline(xyz, tets, D6, sample, threads)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"fem3Dtet P2 GRAD.GRAD element matrices of the first {sample} tets "
+                         f"({sec:.1f} s), oracle port on {threads} host threads"}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"P2 anisotropic diffusion, {n}^3x6 perturbed Kuhn tets ({nt} tets, {ndof} DOFs, "
+                               f"{nnz} nnz), order 4, FP32 element matrices into the CSR template, "
+                               f"homogeneous Dirichlet",
+                   "l2": "working set (inputs, scatter records, CSR values) larger than L2; no flush",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                     "traffic": traffic, "peak_kind": peak_kind,
+                     "kernel": "assembly = tet_prepare + row_gather (2 launches)",
+                     "algorithmic_bytes": b_alg, "ms": {"tet_prepare": prep_ms, "row_gather": rows_ms}},
+        "e2e": {"value": world * nt / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+        "cpu_baseline": cpu,
+        "f64_assembly": {"ms": f64_ms, "value": nt / (f64_ms * 1e-3), "unit": UNIT},
+        "setup_s": setup_s,
+        "solve": solve,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+    if int(os.environ.get("WORLD_SIZE", "1")) > 1:
+        import torch.distributed as dist
+        if dist.is_initialized():
+            dist.barrier()
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

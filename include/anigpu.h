@@ -86,6 +86,13 @@ const char* anigpu_last_error(anigpu_handle h);
 /* kernels launched by this handle since creation (evidence for bench reports) */
 int64_t anigpu_launch_count(anigpu_handle h);
 
+/* per-phase device timings (CUDA events on the handle's stream), the counterpart of the
+ * reference's OPTIMIZER_TIMERS_FEM3DTET phase timers (anifem++/fem/operations/core.inl:1-9)
+ * and WITH_ASSEMBLER_TIMERS (assembler.h:234-247).  When enabled, anigpu_assemble records
+ * [tet prepare, row gather] in milliseconds; anigpu_last_timing copies them out. */
+int anigpu_set_timing(anigpu_handle h, int enable);
+int anigpu_last_timing(anigpu_handle h, double* ms_host, int cap);
+
 /* ---- element level: the fused batch of Ani::fem3Dtet
  * (anifem++/fem/operations/int_tet.h:17-29, int_tet.inl:30-57,93-122; the FUSION batch of
  * TetrasT columns becomes the whole device batch).

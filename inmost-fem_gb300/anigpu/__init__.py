@@ -44,6 +44,8 @@ SIGNATURES = {
     "anigpu_set_stream": (_i, [_vp, _vp]),
     "anigpu_last_error": (ctypes.c_char_p, [_vp]),
     "anigpu_launch_count": (_i64, [_vp]),
+    "anigpu_set_timing": (_i, [_vp, _i]),
+    "anigpu_last_timing": (_i, [_vp, _vp, _i]),
     "anigpu_fem3dtet": (_i, [_vp, _i, _i, _i, _i, _i, _i64, _vp, _vp, _vp]),
     "anigpu_quadrature": (_i, [_i, _vp, _vp, _i]),
     "anigpu_quadrature_points": (_i, [_vp, _i, _i64, _vp, _vp]),
@@ -184,6 +186,16 @@ class Anigpu:
 
     def set_stream(self, stream_handle):
         self._check(self.lib.anigpu_set_stream(self.h, ctypes.c_void_p(stream_handle)))
+
+    def set_timing(self, enable=True):
+        self._check(self.lib.anigpu_set_timing(self.h, 1 if enable else 0))
+
+    def last_timing(self):
+        """Per-phase device milliseconds of the last timed call."""
+        import numpy as np
+        ms = np.zeros(8)
+        n = self._check(self.lib.anigpu_last_timing(self.h, ms.ctypes.data, 8))
+        return ms[:n].tolist()
 
     def launch_count(self):
         return int(self.lib.anigpu_launch_count(self.h))

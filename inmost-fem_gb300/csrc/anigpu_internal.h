@@ -86,6 +86,11 @@ struct anigpu_ctx {
     size_t solve_ws_bytes = 0;
     void* learned = nullptr;       // learned preconditioner state
 
+    // per-phase timing (anigpu_set_timing)
+    bool timing = false;
+    cudaEvent_t tev[9] = {};
+    int ntev = 0;  // events recorded in the last timed call
+
     std::vector<void*> extra_allocs;
     // device copies of reference-element tables, keyed by 100*space + order
     std::vector<std::pair<int, double*>> basis_dev;
@@ -94,6 +99,13 @@ struct anigpu_ctx {
 int get_basis_dev(anigpu_ctx* h, int space, int order, const double** dev, ScalarBasisTable* host);
 
 // ------------------------------------------------------------------ helpers
+// record timing event k (k = 0 starts the call) when timing is enabled
+inline void time_mark(anigpu_ctx* h, int k) {
+    if (!h->timing || k >= 9) return;
+    if (!h->tev[k]) cudaEventCreate(&h->tev[k]);
+    cudaEventRecord(h->tev[k], h->stream);
+    h->ntev = k + 1;
+}
 int set_err(anigpu_ctx* h, int code, const std::string& msg);
 int cuda_check(anigpu_ctx* h, cudaError_t e, const char* what);
 #define ANI_CUDA(h, call)                                      \

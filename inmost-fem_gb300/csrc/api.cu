@@ -17,8 +17,11 @@ int cuda_check(anigpu_ctx* h, cudaError_t e, const char* what) {
     return set_err(h, ANIGPU_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-#define CHECK_H(h) \
-    if (!(h)) return ANIGPU_ERR_ARG
+// entry check; also clears a sticky error left by other code in this thread so that the
+// launch checks below report this library's own launches only
+#define CHECK_H(h)                   \
+    if (!(h)) return ANIGPU_ERR_ARG; \
+    (void)cudaGetLastError()
 
 extern "C" {
 
@@ -63,6 +66,8 @@ int anigpu_destroy(anigpu_handle h) {
     if (h->col_s) cudaFree(h->col_s);
     for (auto& kv : h->basis_dev) cudaFree(kv.second);
     for (void* p : h->extra_allocs) cudaFree(p);
+    for (auto& e : h->tev)
+        if (e) cudaEventDestroy(e);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
     delete h;
     return ANIGPU_OK;
@@ -77,6 +82,26 @@ int anigpu_set_stream(anigpu_handle h, void* stream) {
 const char* anigpu_last_error(anigpu_handle h) { return h ? h->err.c_str() : "invalid handle"; }
 
 int64_t anigpu_launch_count(anigpu_handle h) { return h ? h->launches : -1; }
+
+int anigpu_set_timing(anigpu_handle h, int enable) {
+    CHECK_H(h);
+    h->timing = enable != 0;
+    h->ntev = 0;
+    return ANIGPU_OK;
+}
+
+int anigpu_last_timing(anigpu_handle h, double* ms_host, int cap) {
+    CHECK_H(h);
+    if (!h->timing || h->ntev < 2) return 0;
+    ANI_CUDA(h, cudaEventSynchronize(h->tev[h->ntev - 1]));
+    int n = 0;
+    for (int k = 1; k < h->ntev && n < cap; ++k, ++n) {
+        float ms = 0;
+        ANI_CUDA(h, cudaEventElapsedTime(&ms, h->tev[k - 1], h->tev[k]));
+        ms_host[n] = ms;
+    }
+    return n;
+}
 
 int anigpu_fem3dtet(anigpu_handle h, int opA, int opB, int tensor_kind, int order, int precision, int64_t nt,
                     const double* XY, const double* D, void* A) {

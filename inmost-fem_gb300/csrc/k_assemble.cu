@@ -442,6 +442,7 @@ int run_assemble(anigpu_ctx* h, int kind, const double* D, const double* f, doub
         ANI_CUDA(h, cudaMalloc(&h->tetdata, need));
         h->tetdata_bytes = need;
     }
+    time_mark(h, 0);
     if (precision == ANIGPU_F32)
         tet_prepare_kernel<float><<<grid_for(h->nt, 256), 256, 0, h->stream>>>(h->nt, h->xyz, h->tets, kind, D, f,
                                                                               f_const, (float*)h->tetdata, h->d_status);
@@ -449,6 +450,7 @@ int run_assemble(anigpu_ctx* h, int kind, const double* D, const double* f, doub
         tet_prepare_kernel<double><<<grid_for(h->nt, 256), 256, 0, h->stream>>>(
             h->nt, h->xyz, h->tets, kind, D, f, f_const, (double*)h->tetdata, h->d_status);
     ANI_LAUNCHED(h);
+    time_mark(h, 1);
     RowParams p;
     p.nrows = h->nds;
     p.inc_ptr = h->inc_ptr;
@@ -467,6 +469,7 @@ int run_assemble(anigpu_ctx* h, int kind, const double* D, const double* f, doub
         rc = precision == ANIGPU_F32 ? launch_rows<float, 4>(h, p, tables, vals, rhs, touched)
                                      : launch_rows<double, 4>(h, p, tables, vals, rhs, touched);
     }
+    time_mark(h, 2);
     return rc;
 }
 

@@ -380,6 +380,17 @@ int setup_problem(anigpu_ctx* h, int space) {
     if (h->nt <= 0) return set_err(h, ANIGPU_ERR_STATE, "no mesh uploaded");
     cudaStream_t s = h->stream;
     const int64_t nv = h->nv, nt = h->nt;
+    // drop the aliases of a previous scalar setup before the scalar arrays are reallocated
+    if (h->rowptr == h->rowptr_s) h->rowptr = nullptr;
+    if (h->col == h->col_s) h->col = nullptr;
+    if (h->rowptr) {
+        cudaFree(h->rowptr);
+        h->rowptr = nullptr;
+    }
+    if (h->col) {
+        cudaFree(h->col);
+        h->col = nullptr;
+    }
     h->space = space;
     h->nloc_s = space == ANIGPU_P1 ? 4 : 10;
     h->ncomp = space == ANIGPU_VEC3_P2 ? 3 : 1;
@@ -517,14 +528,10 @@ int setup_problem(anigpu_ctx* h, int space) {
 
     // full template
     if (h->ncomp == 1) {
-        if (h->rowptr && h->rowptr != h->rowptr_s) cudaFree(h->rowptr);
-        if (h->col && h->col != h->col_s) cudaFree(h->col);
         h->rowptr = h->rowptr_s;
         h->col = h->col_s;
         h->nnz = h->nnz_s;
     } else {
-        if (h->rowptr == h->rowptr_s) h->rowptr = nullptr;
-        if (h->col == h->col_s) h->col = nullptr;
         h->nnz = 9 * h->nnz_s;
         RC(dev_alloc(h, &h->rowptr, (size_t)h->ndof + 1));
         RC(dev_alloc(h, &h->col, (size_t)h->nnz));

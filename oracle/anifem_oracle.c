@@ -208,6 +208,48 @@ static void expand_tensor(int kind, const double* src, int dA, int dB, double* D
     }
 }
 
+/* GRAD.GRAD of one scalar space with a per-tet symmetric tensor: the same steps as the
+ * reference's template path for one tet (core.inl:277-367): U = PSI^T ghat at every point
+ * (poly_2.h:52-100), DU = w |T| D U (diff_tensor.h:275-310), A = U^T DU (core.inl:28-60). */
+static void gradgrad_sym(int space, int order, long nt, const double* XY, const double* D6, double* A) {
+    const double *pp, *ww;
+    int q;
+    anigpu_quad_rule(order, &pp, &ww, &q);
+    int nf = scalar_nf(space);
+    double val[20], g[20][3];
+    double U[MAXQ * 3 * 20], DU[MAXQ * 3 * 20];
+    double G[MAXQ][20][3];
+    for (long t = 0; t < nt; ++t) {
+        double PSI[9], mes;
+        tet_geom(XY + 12 * t, PSI, &mes);
+        const double* s = D6 + 6 * t;
+        const double Dm[9] = {s[0], s[1], s[2], s[1], s[3], s[4], s[2], s[4], s[5]};
+        for (int n = 0; n < q; ++n) scalar_basis(space, pp + 4 * n, val, G[n]);
+        for (int i = 0; i < nf; ++i)
+            for (int n = 0; n < q; ++n)
+                for (int k = 0; k < 3; ++k)
+                    U[k + 3 * (n + q * i)] = PSI[0 + 3 * k] * G[n][i][0] + PSI[1 + 3 * k] * G[n][i][1] + PSI[2 + 3 * k] * G[n][i][2];
+        for (int i = 0; i < nf; ++i)
+            for (int n = 0; n < q; ++n) {
+                const double wv = ww[n] * mes;
+                const double* u = U + 3 * (n + q * i);
+                for (int k = 0; k < 3; ++k)
+                    DU[k + 3 * (n + q * i)] = wv * (Dm[k + 0] * u[0] + Dm[k + 3] * u[1] + Dm[k + 6] * u[2]);
+            }
+        double* At = A + (size_t)t * nf * nf;
+        const int nr = 3 * q;
+        for (int ia = 0; ia < nf; ++ia)
+            for (int ib = 0; ib < nf; ++ib) {
+                double acc = 0;
+                const double* v = U + nr * ib;
+                const double* du = DU + nr * ia;
+                for (int j = 0; j < nr; ++j) acc += v[j] * du[j];
+                At[ib + nf * ia] = acc;
+            }
+    }
+    (void)g;
+}
+
 /* A(ib, ia) = sum_n w_n |T| sum_k V_k(ib) sum_j D(k,j) U_j(ia)
  * (core.inl:277-367: U = OpA(apply), DU (diff_tensor.h:488-552), A = V^T DU (core.inl:28-60)) */
 int orc_fem3dtet(int codeA, int codeB, int kind, int order, long nt, const double* XY, const double* D, double* A) {
@@ -535,7 +577,7 @@ struct chunk {
 };
 static void* run_chunk(void* arg) {
     struct chunk* c = (struct chunk*)arg;
-    orc_fem3dtet(22, 22, ORC_TET_SYM, c->order, c->nt, c->XY, c->D6, c->A);
+    gradgrad_sym(2, c->order, c->nt, c->XY, c->D6, c->A);
     return NULL;
 }
 
@@ -543,7 +585,7 @@ double orc_time_p2_sym(long nt, const double* XY, const double* D6, int order, i
     struct timespec t0, t1;
     clock_gettime(CLOCK_MONOTONIC, &t0);
     if (nthreads <= 1) {
-        orc_fem3dtet(22, 22, ORC_TET_SYM, order, nt, XY, D6, A);
+        gradgrad_sym(2, order, nt, XY, D6, A);
     } else {
         pthread_t th[256];
         struct chunk cs[256];

@@ -109,5 +109,5 @@ def test_errors_are_reported(lib):
         lib.fem3dtet(22, 22, XY, None, anigpu.TENSOR_NULL, 9)  # order above 6
     assert e.value.code == anigpu.ERR_UNSUPPORTED
     with pytest.raises(anigpu.AnigpuError) as e:
-        lib.fem3dtet(22, 51, XY, None, anigpu.TENSOR_NULL, 2)  # identity of incompatible dims
+        lib.fem3dtet(22, 21, XY, None, anigpu.TENSOR_NULL, 2)  # identity of incompatible dims (3 vs 1)
     assert e.value.code == anigpu.ERR_ARG
