@@ -47,6 +47,7 @@ struct anigpu_ctx {
     // mesh
     int64_t nv = 0, nt = 0;
     double* xyz = nullptr;    // nv*3
+    float2* xyz2 = nullptr;   // nv*3 (hi, lo) float pairs with hi + lo == xyz to ~2^-48 (FP32 geometry)
     int32_t* tets = nullptr;  // nt*4 (oriented)
 
     // problem
@@ -149,6 +150,8 @@ int setup_orient(anigpu_ctx* h);
 int setup_problem(anigpu_ctx* h, int space);
 int setup_dirichlet_bits(anigpu_ctx* h);
 int setup_dof_coords(anigpu_ctx* h, double* out);
+// refresh the (hi, lo) float copy of the coordinates after an upload or update
+int setup_coords_split(anigpu_ctx* h);
 // exclusive scan of cnt[0..n] (cnt[n] must be 0) into ptr[0..n]; ptr[n] = total
 int scan_counts(anigpu_ctx* h, unsigned long long* cnt, int64_t n, int64_t* ptr);
 // assembly (k_assemble.cu)

@@ -56,7 +56,7 @@ int anigpu_destroy(anigpu_handle h) {
     cudaStreamSynchronize(h->stream);
     free_solver(h);
     free_learned(h);
-    void* ptrs[] = {h->xyz, h->tets, h->tet_edges, h->edofs, h->inc_ptr, h->recs, h->dir_mask, h->dir_bc,
+    void* ptrs[] = {h->xyz, h->xyz2, h->tets, h->tet_edges, h->edofs, h->inc_ptr, h->recs, h->dir_mask, h->dir_bc,
                     h->tetdata, h->d_status, h->d_ref_tables};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -148,6 +148,12 @@ int anigpu_mesh_upload(anigpu_handle h, int64_t nv, const double* xyz, int64_t n
     h->nv = nv;
     h->nt = nt;
     h->space = -1;
+    if (h->xyz2) {
+        cudaFree(h->xyz2);
+        h->xyz2 = nullptr;
+    }
+    rc = setup_coords_split(h);
+    if (rc) return rc;
     return setup_orient(h);
 }
 
@@ -156,7 +162,7 @@ int anigpu_mesh_update_coords(anigpu_handle h, const double* xyz) {
     if (!h->xyz || !xyz) return set_err(h, ANIGPU_ERR_STATE, "no mesh");
     cudaSetDevice(h->device);
     ANI_CUDA(h, cudaMemcpyAsync(h->xyz, xyz, sizeof(double) * 3 * h->nv, cudaMemcpyDefault, h->stream));
-    return ANIGPU_OK;
+    return setup_coords_split(h);
 }
 
 int anigpu_problem_setup(anigpu_handle h, int space) {

@@ -23,25 +23,63 @@ namespace {
 constexpr int kChunk = 16;  // incidences staged per group per step
 
 // ---------------------------------------------------------------- phase 1
-// K = |T| PSI D PSI^T (k00 k11 k22 k01 k02 k12), then f*|T| and 0: 8 values per tet.
-template <typename Real>
-__global__ void tet_prepare_kernel(int64_t nt, const double* __restrict__ xyz, const int32_t* __restrict__ tets,
-                                   int kind, const double* __restrict__ D, const double* __restrict__ f,
-                                   double f_const, Real* __restrict__ out, int* __restrict__ status) {
-    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (t >= nt) return;
-    const int4 v = reinterpret_cast<const int4*>(tets)[t];
-    double X0[3], e[9];
+// FP64 -> FP32 with round-to-nearest-even in integer arithmetic.  GB300 runs FP64 (and
+// the F64->F32 conversion) at a small fraction of its FP32 rate, so the FP32 path keeps
+// every FP64 instruction off its common path; zero, subnormal and out-of-range inputs go
+// through the hardware conversion.
+__device__ __forceinline__ float d2f_rn(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
+    if (e <= 0 || e >= 255) return (b << 1) == 0 ? __uint_as_float(hi & 0x80000000u) : __double2float_rn(x);
+    const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const unsigned rest = lo & 0x1fffffffu;
+    unsigned f = (hi & 0x80000000u) | ((unsigned)e << 23) | m;
+    if (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) f += 1u;
+    return __uint_as_float(f);
+}
+
+// K = |T| PSI D PSI^T (k00 k11 k22 k01 k02 k12), then f|T| and 0: 8 values per tet.
+// PSI(a,a') = PSI[a + 3a'] (inverse3x3, geometry.h:26-44; core.inl:217-247).
+template <typename R>
+__device__ __forceinline__ void k_from_psi(const R* PSI, const R* d, R mes, R* K) {
+    const R Dm[9] = {d[0], d[1], d[2], d[1], d[3], d[4], d[2], d[4], d[5]};
+    R M[9];
 #pragma unroll
-    for (int k = 0; k < 3; ++k) X0[k] = xyz[3 * (int64_t)v.x + k];
+    for (int a = 0; a < 3; ++a)
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        e[k + 0] = xyz[3 * (int64_t)v.y + k] - X0[k];  // column 0: X1 - X0 (core.inl:230-236)
-        e[k + 3] = xyz[3 * (int64_t)v.z + k] - X0[k];
-        e[k + 6] = xyz[3 * (int64_t)v.w + k] - X0[k];
-    }
-    // symmetric tensor d00 d01 d02 d11 d12 d22
-    double d[6];
+        for (int b = 0; b < 3; ++b) M[a + 3 * b] = PSI[a] * Dm[3 * b] + PSI[a + 3] * Dm[1 + 3 * b] + PSI[a + 6] * Dm[2 + 3 * b];
+    auto kab = [&](int a, int b) { return mes * (M[a] * PSI[b] + M[a + 3] * PSI[b + 3] + M[a + 6] * PSI[b + 6]); };
+    K[0] = kab(0, 0);
+    K[1] = kab(1, 1);
+    K[2] = kab(2, 2);
+    K[3] = kab(0, 1);
+    K[4] = kab(0, 2);
+    K[5] = kab(1, 2);
+}
+
+template <typename R>
+__device__ __forceinline__ R inverse3(const R* m, R* inv) {
+#define M(I, J) m[(I) + 3 * (J)]
+    const R da = M(1, 1) * M(2, 2) - M(1, 2) * M(2, 1);
+    const R db = M(1, 2) * M(2, 0) - M(1, 0) * M(2, 2);
+    const R dc = M(1, 0) * M(2, 1) - M(1, 1) * M(2, 0);
+    const R det = M(0, 0) * da + M(0, 1) * db + M(0, 2) * dc;
+    const R r = R(1) / det;
+    inv[0] = da * r;
+    inv[1] = db * r;
+    inv[2] = dc * r;
+#pragma unroll
+    for (int i = 1; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+            inv[j + 3 * i] = (M((i + 1) % 3, (j + 1) % 3) * M((i + 2) % 3, (j + 2) % 3) -
+                              M((i + 1) % 3, (j + 2) % 3) * M((i + 2) % 3, (j + 1) % 3)) * r;
+#undef M
+    return det;
+}
+
+__device__ __forceinline__ void load_sym(int kind, const double* __restrict__ D, int64_t t, double* d) {
     switch (kind) {
         case ANIGPU_TENSOR_NULL: d[0] = d[3] = d[5] = 1; d[1] = d[2] = d[4] = 0; break;
         case ANIGPU_TENSOR_CONST_SCALAR: d[0] = d[3] = d[5] = D[0]; d[1] = d[2] = d[4] = 0; break;
@@ -50,129 +88,113 @@ __global__ void tet_prepare_kernel(int64_t nt, const double* __restrict__ xyz, c
 #pragma unroll
             for (int k = 0; k < 6; ++k) d[k] = D[6 * t + k];
     }
-    const double fv = f ? f[t] : f_const;
-    Real K[8];
-    bool bad = false;
-    // cofactor inverse (inverse3x3, geometry.h:26-44).  The FP32 path inverts in FP32 unless
-    // the tet is badly shaped (|det| small against the edge lengths), then in FP64.
-    bool use64 = sizeof(Real) == 8;
-    float ef[9], PSIf[9];
-    float detf = 0.f;
-    if (!use64) {
+}
+
+// FP64 path (parity arithmetic): everything in FP64, as the reference.
+__global__ void tet_prepare_f64_kernel(int64_t nt, const double* __restrict__ xyz, const int32_t* __restrict__ tets,
+                                       int kind, const double* __restrict__ D, const double* __restrict__ f,
+                                       double f_const, double* __restrict__ out, int* __restrict__ status) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= nt) return;
+    const int4 v = reinterpret_cast<const int4*>(tets)[t];
+    double e[9];
 #pragma unroll
-        for (int k = 0; k < 9; ++k) ef[k] = (float)e[k];
-#define M(I, J) ef[(I) + 3 * (J)]
-        const float da = M(1, 1) * M(2, 2) - M(1, 2) * M(2, 1);
-        const float db = M(1, 2) * M(2, 0) - M(1, 0) * M(2, 2);
-        const float dc = M(1, 0) * M(2, 1) - M(1, 1) * M(2, 0);
-        detf = M(0, 0) * da + M(0, 1) * db + M(0, 2) * dc;
-        const float l0 = sqrtf(M(0, 0) * M(0, 0) + M(1, 0) * M(1, 0) + M(2, 0) * M(2, 0));
-        const float l1 = sqrtf(M(0, 1) * M(0, 1) + M(1, 1) * M(1, 1) + M(2, 1) * M(2, 1));
-        const float l2 = sqrtf(M(0, 2) * M(0, 2) + M(1, 2) * M(1, 2) + M(2, 2) * M(2, 2));
-        if (!(fabsf(detf) > 0.05f * l0 * l1 * l2)) {
-            use64 = true;
-        } else {
-            const float inv = 1.0f / detf;
-            PSIf[0] = da * inv;
-            PSIf[1] = db * inv;
-            PSIf[2] = dc * inv;
-#pragma unroll
-            for (int i = 1; i < 3; ++i)
-#pragma unroll
-                for (int j = 0; j < 3; ++j)
-                    PSIf[j + 3 * i] = (M((i + 1) % 3, (j + 1) % 3) * M((i + 2) % 3, (j + 2) % 3) -
-                                       M((i + 1) % 3, (j + 2) % 3) * M((i + 2) % 3, (j + 1) % 3)) * inv;
-        }
-#undef M
+    for (int k = 0; k < 3; ++k) {
+        const double x0 = xyz[3 * (int64_t)v.x + k];
+        e[k + 0] = xyz[3 * (int64_t)v.y + k] - x0;  // columns X1-X0, X2-X0, X3-X0 (core.inl:230-236)
+        e[k + 3] = xyz[3 * (int64_t)v.z + k] - x0;
+        e[k + 6] = xyz[3 * (int64_t)v.w + k] - x0;
     }
-    if (use64) {
-        double PSI[9];
-#define M(I, J) e[(I) + 3 * (J)]
-        const double da = M(1, 1) * M(2, 2) - M(1, 2) * M(2, 1);
-        const double db = M(1, 2) * M(2, 0) - M(1, 0) * M(2, 2);
-        const double dc = M(1, 0) * M(2, 1) - M(1, 1) * M(2, 0);
-        const double det = M(0, 0) * da + M(0, 1) * db + M(0, 2) * dc;
-        PSI[0] = da / det;
-        PSI[1] = db / det;
-        PSI[2] = dc / det;
+    double d[6], PSI[9], K[8];
+    load_sym(kind, D, t, d);
+    const double det = inverse3(e, PSI);
+    const double mes = fabs(det) / 6.0;
+    k_from_psi(PSI, d, mes, K);
+    K[6] = (f ? f[t] : f_const) * mes;
+    K[7] = 0;
+    bool bad = !(det != 0.0);
 #pragma unroll
-        for (int i = 1; i < 3; ++i)
-#pragma unroll
-            for (int j = 0; j < 3; ++j)
-                PSI[j + 3 * i] = (M((i + 1) % 3, (j + 1) % 3) * M((i + 2) % 3, (j + 2) % 3) -
-                                  M((i + 1) % 3, (j + 2) % 3) * M((i + 2) % 3, (j + 1) % 3)) / det;
-#undef M
-        const double mes = fabs(det) / 6.0;
-        // M = PSI * D, K = mes * M * PSI^T ; PSI(a,a') = PSI[a + 3a']
-        double Dm[9] = {d[0], d[1], d[2], d[1], d[3], d[4], d[2], d[4], d[5]};
-        double Mm[9];
-#pragma unroll
-        for (int a = 0; a < 3; ++a)
-#pragma unroll
-            for (int b = 0; b < 3; ++b) {
-                double s = 0;
-#pragma unroll
-                for (int c = 0; c < 3; ++c) s += PSI[a + 3 * c] * Dm[c + 3 * b];
-                Mm[a + 3 * b] = s;
-            }
-        auto kab = [&](int a, int b) {
-            double s = 0;
-#pragma unroll
-            for (int c = 0; c < 3; ++c) s += Mm[a + 3 * c] * PSI[b + 3 * c];
-            return mes * s;
-        };
-        K[0] = (Real)kab(0, 0);
-        K[1] = (Real)kab(1, 1);
-        K[2] = (Real)kab(2, 2);
-        K[3] = (Real)kab(0, 1);
-        K[4] = (Real)kab(0, 2);
-        K[5] = (Real)kab(1, 2);
-        K[6] = (Real)(fv * mes);
-        K[7] = (Real)0;
-        bad = !isfinite(det) || det == 0.0;
-    } else {
-        const float mes = fabsf(detf) / 6.0f;
-        const float Dm[9] = {(float)d[0], (float)d[1], (float)d[2], (float)d[1], (float)d[3],
-                             (float)d[4], (float)d[2], (float)d[4], (float)d[5]};
-        float Mm[9];
-#pragma unroll
-        for (int a = 0; a < 3; ++a)
-#pragma unroll
-            for (int b = 0; b < 3; ++b) {
-                float s = 0;
-#pragma unroll
-                for (int c = 0; c < 3; ++c) s += PSIf[a + 3 * c] * Dm[c + 3 * b];
-                Mm[a + 3 * b] = s;
-            }
-        auto kab = [&](int a, int b) {
-            float s = 0;
-#pragma unroll
-            for (int c = 0; c < 3; ++c) s += Mm[a + 3 * c] * PSIf[b + 3 * c];
-            return mes * s;
-        };
-        K[0] = (Real)kab(0, 0);
-        K[1] = (Real)kab(1, 1);
-        K[2] = (Real)kab(2, 2);
-        K[3] = (Real)kab(0, 1);
-        K[4] = (Real)kab(0, 2);
-        K[5] = (Real)kab(1, 2);
-        K[6] = (Real)((float)fv * mes);
-        K[7] = (Real)0;
-    }
-#pragma unroll
-    for (int k = 0; k < 7; ++k) bad |= !isfinite((double)K[k]);
+    for (int k = 0; k < 7; ++k) bad |= !isfinite(K[k]);
     if (bad) atomicExch(status, ANIGPU_ERR_NONFINITE);
-    if (sizeof(Real) == 4) {
-        float4* o = reinterpret_cast<float4*>(out + 8 * t);
-        o[0] = make_float4((float)K[0], (float)K[1], (float)K[2], (float)K[3]);
-        o[1] = make_float4((float)K[4], (float)K[5], (float)K[6], (float)K[7]);
-    } else {
-        double2* o = reinterpret_cast<double2*>(out + 8 * t);
-        o[0] = make_double2((double)K[0], (double)K[1]);
-        o[1] = make_double2((double)K[2], (double)K[3]);
-        o[2] = make_double2((double)K[4], (double)K[5]);
-        o[3] = make_double2((double)K[6], (double)K[7]);
+    double2* o = reinterpret_cast<double2*>(out + 8 * t);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) o[q] = make_double2(K[2 * q], K[2 * q + 1]);
+}
+
+// FP32 path: FP32 geometry from the (hi, lo) coordinate pairs; the edge vectors carry one
+// FP32 rounding.  A tet whose |det| is small against its edge lengths (badly shaped,
+// |det| <= 0.05 |e1||e2||e3|) is redone in FP64 from the FP64 coordinates.
+__global__ void tet_prepare_f32_kernel(int64_t nt, const double* __restrict__ xyz, const float2* __restrict__ xyz2,
+                                       const int32_t* __restrict__ tets, int kind, const double* __restrict__ D,
+                                       const double* __restrict__ f, double f_const, float* __restrict__ out,
+                                       int* __restrict__ status) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= nt) return;
+    const int4 v = reinterpret_cast<const int4*>(tets)[t];
+    float e[9];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float2 x0 = xyz2[3 * (int64_t)v.x + k];
+        const float2 x1 = xyz2[3 * (int64_t)v.y + k];
+        const float2 x2 = xyz2[3 * (int64_t)v.z + k];
+        const float2 x3 = xyz2[3 * (int64_t)v.w + k];
+        e[k + 0] = (x1.x - x0.x) + (x1.y - x0.y);
+        e[k + 3] = (x2.x - x0.x) + (x2.y - x0.y);
+        e[k + 6] = (x3.x - x0.x) + (x3.y - x0.y);
     }
+    float d[6];
+    if (kind == ANIGPU_TENSOR_TET_SYM) {
+        const double2* Dp = reinterpret_cast<const double2*>(D + 6 * t);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const double2 w = Dp[q];
+            d[2 * q] = d2f_rn(w.x);
+            d[2 * q + 1] = d2f_rn(w.y);
+        }
+    } else {
+        const float s = kind == ANIGPU_TENSOR_NULL ? 1.f : d2f_rn(kind == ANIGPU_TENSOR_CONST_SCALAR ? D[0] : D[t]);
+        d[0] = d[3] = d[5] = s;
+        d[1] = d[2] = d[4] = 0.f;
+    }
+    const float fv = d2f_rn(f ? f[t] : f_const);
+    float PSI[9], K[8];
+    const float det = inverse3(e, PSI);
+    const float l0 = e[0] * e[0] + e[1] * e[1] + e[2] * e[2];
+    const float l1 = e[3] * e[3] + e[4] * e[4] + e[5] * e[5];
+    const float l2 = e[6] * e[6] + e[7] * e[7] + e[8] * e[8];
+    float mes;
+    if (det * det > 0.0025f * l0 * l1 * l2) {
+        mes = fabsf(det) * (1.0f / 6.0f);
+        k_from_psi(PSI, d, mes, K);
+    } else {
+        // badly shaped (or degenerate) tet: Jacobian and inverse in FP64
+        double ed[9], P64[9], dd[6];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const double x0 = xyz[3 * (int64_t)v.x + k];
+            ed[k + 0] = xyz[3 * (int64_t)v.y + k] - x0;
+            ed[k + 3] = xyz[3 * (int64_t)v.z + k] - x0;
+            ed[k + 6] = xyz[3 * (int64_t)v.w + k] - x0;
+        }
+        load_sym(kind, D, t, dd);
+        const double det64 = inverse3(ed, P64);
+        const double mes64 = fabs(det64) / 6.0;
+        double K64[6];
+        k_from_psi(P64, dd, mes64, K64);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) K[k] = (float)K64[k];
+        mes = (float)mes64;
+        if (!(det64 != 0.0)) atomicExch(status, ANIGPU_ERR_NONFINITE);
+    }
+    K[6] = fv * mes;
+    K[7] = 0.f;
+    bool bad = false;
+#pragma unroll
+    for (int k = 0; k < 7; ++k) bad |= !isfinite(K[k]);
+    if (bad) atomicExch(status, ANIGPU_ERR_NONFINITE);
+    float4* o = reinterpret_cast<float4*>(out + 8 * t);
+    o[0] = make_float4(K[0], K[1], K[2], K[3]);
+    o[1] = make_float4(K[4], K[5], K[6], K[7]);
 }
 
 // ---------------------------------------------------------------- phase 2
@@ -184,150 +206,184 @@ struct RowParams {
     const uint8_t* dir_mask;
     const double* dir_bc;
     const int32_t* edofs;
-    int bc_nonzero;
     int cap;  // row buffer capacity (>= longest row)
     double drop;
 };
 
-__device__ inline uint32_t rec_off(const ScatterRec& r, int j) {
+__device__ __forceinline__ uint32_t rec_off(const ScatterRec& r, int j) {
     const uint32_t w = j < 4 ? r.off03 : (j < 8 ? r.off47 : (r.meta >> 16));
     return (w >> (8 * (j & 3))) & 0xffu;
 }
 
-template <typename Real, int NLOC>
+template <typename Real>
+struct KVec;
+template <>
+struct KVec<float> {
+    float4 a, b;
+    __device__ __forceinline__ void load(const float* p) {
+        a = reinterpret_cast<const float4*>(p)[0];
+        b = reinterpret_cast<const float4*>(p)[1];
+    }
+    __device__ __forceinline__ float k(int i) const {
+        return i == 0 ? a.x : i == 1 ? a.y : i == 2 ? a.z : i == 3 ? a.w : i == 4 ? b.x : i == 5 ? b.y : b.z;
+    }
+    __device__ __forceinline__ void zero() { a = b = make_float4(0.f, 0.f, 0.f, 0.f); }
+};
+template <>
+struct KVec<double> {
+    double2 a, b, c, d;
+    __device__ __forceinline__ void load(const double* p) {
+        const double2* q = reinterpret_cast<const double2*>(p);
+        a = q[0];
+        b = q[1];
+        c = q[2];
+        d = q[3];
+    }
+    __device__ __forceinline__ double k(int i) const {
+        return i == 0 ? a.x : i == 1 ? a.y : i == 2 ? b.x : i == 3 ? b.y : i == 4 ? c.x : i == 5 ? c.y : d.x;
+    }
+    __device__ __forceinline__ void zero() { a = b = c = d = make_double2(0.0, 0.0); }
+};
+
+// Row gather.  A group of NLOC lanes owns one CSR row; lane j computes A_t(i, j) of each
+// incident tet t (i = the row's local index in t) and adds it into a shared-memory copy of
+// the row at the offset held by the scatter record.  Incidences are walked in ascending
+// tet order with the record and the per-tet block of the next incidences prefetched.
+template <typename Real, int NLOC, bool DIR, bool BCNZ, bool TOUCH>
 __global__ void __launch_bounds__(128) row_gather_kernel(RowParams p, const Real* __restrict__ tables,
                                                          const Real* __restrict__ tetK, Real* __restrict__ vals,
                                                          double* __restrict__ rhs, uint8_t* __restrict__ touched_out,
                                                          int* __restrict__ status) {
     constexpr int G = 32 / NLOC;
+    constexpr int TAB = NLOC * NLOC * 8 + NLOC;  // Tsym[i][j][8] then m[i]
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int g = lane / NLOC, lj = lane - g * NLOC;
     const bool in_group = g < G;
-    // tables: Tsym[6][NLOC][NLOC], m[NLOC]
     Real* sT = reinterpret_cast<Real*>(smem_raw);
-    constexpr int ntab = 6 * NLOC * NLOC + NLOC;
-    for (int k = threadIdx.x; k < ntab; k += blockDim.x) sT[k] = tables[k];
-    const Real* sM = sT + 6 * NLOC * NLOC;
-    // per-group regions
-    const size_t tab_bytes = ((sizeof(Real) * ntab + 15) / 16) * 16;
-    const size_t grp_bytes = ((kChunk * sizeof(ScatterRec) + kChunk * 8 * sizeof(Real) +
-                               p.cap * sizeof(Real) + NLOC * sizeof(Real) + p.cap + 15) / 16) * 16;
+    for (int k = threadIdx.x; k < TAB; k += blockDim.x) sT[k] = tables[k];
+    const Real* sM = sT + NLOC * NLOC * 8;
+    const size_t tab_bytes = ((sizeof(Real) * TAB + 15) / 16) * 16;
+    const size_t grp_bytes = ((p.cap * sizeof(Real) + (TOUCH ? p.cap : 0) + (BCNZ ? NLOC * sizeof(Real) : 0) + 15) / 16) * 16;
     unsigned char* gbase = smem_raw + tab_bytes + grp_bytes * (size_t)(warp * G + (in_group ? g : 0));
-    ScatterRec* sRec = reinterpret_cast<ScatterRec*>(gbase);
-    Real* sK = reinterpret_cast<Real*>(gbase + kChunk * sizeof(ScatterRec));
-    Real* sRow = sK + kChunk * 8;
-    Real* sA = sRow + p.cap;
-    uint8_t* sTouch = reinterpret_cast<uint8_t*>(sA + NLOC);
+    Real* sRow = reinterpret_cast<Real*>(gbase);
+    uint8_t* sTouch = reinterpret_cast<uint8_t*>(sRow + p.cap);
+    Real* sA = reinterpret_cast<Real*>(gbase + p.cap * sizeof(Real) + (TOUCH ? p.cap : 0));
     __syncthreads();
 
     const int64_t row = ((int64_t)blockIdx.x * (blockDim.x >> 5) + warp) * G + g;
     const bool valid = in_group && row < p.nrows;
-    int64_t ib = 0, ie = 0, rb = 0;
-    int len = 0;
+    int64_t ib = 0, rb = 0;
+    int len = 0, deg = 0;
     bool isdir = false;
-    double bcr = 0;
     if (valid) {
         ib = p.inc_ptr[row];
-        ie = p.inc_ptr[row + 1];
+        deg = (int)(p.inc_ptr[row + 1] - ib);
         rb = p.rowptr[row];
         len = (int)(p.rowptr[row + 1] - rb);
-        isdir = p.dir_mask[row] != 0;
-        bcr = p.dir_bc[row];
+        if (DIR) isdir = p.dir_mask[row] != 0;
         for (int s = lj; s < len; s += NLOC) {
             sRow[s] = Real(0);
-            sTouch[s] = 0;
+            if (TOUCH) sTouch[s] = 0;
         }
     }
-    Real racc = 0;  // right-hand side (lane lj == 0)
-    double racc64 = 0;
+    int maxdeg = deg;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) maxdeg = max(maxdeg, __shfl_xor_sync(0xffffffffu, maxdeg, o));
+    const Real drop = Real(p.drop);
+    Real racc = Real(0);
+    int ndir = 0;
+    // software pipeline: r0/K0 current, r1 next record (its K is loaded one step ahead)
+    ScatterRec r0 = {0u, 0u, 0u, 0u}, r1 = {0u, 0u, 0u, 0u};
+    KVec<Real> K0, K1;
+    K0.zero();
+    K1.zero();
+    if (deg > 0) {
+        r0 = p.recs[ib];
+        K0.load(tetK + 8 * (int64_t)r0.tet);
+    }
+    if (deg > 1) r1 = p.recs[ib + 1];
     __syncwarp();
-    const int ninc = valid ? (int)(ie - ib) : 0;
-    int maxinc = ninc;
-#pragma unroll
-    for (int o = 16; o; o >>= 1) maxinc = max(maxinc, __shfl_xor_sync(0xffffffffu, maxinc, o));
-    for (int c0 = 0; c0 < maxinc; c0 += kChunk) {
-        // stage records and per-tet K of this chunk
-        const int nch = min(kChunk, ninc - c0);
-        for (int s = lj; s < nch; s += NLOC) {
-            const ScatterRec r = p.recs[ib + c0 + s];
-            sRec[s] = r;
-            const Real* kp = tetK + 8 * (int64_t)r.tet;
+    for (int k = 0; k < maxdeg; ++k) {
+        ScatterRec r2 = {0u, 0u, 0u, 0u};
+        if (k + 1 < deg) K1.load(tetK + 8 * (int64_t)r1.tet);
+        if (k + 2 < deg) r2 = p.recs[ib + k + 2];
+        if (k < deg) {
+            const int i = r0.meta & 15;
+            const Real* T = sT + (i * NLOC + lj) * 8;
+            Real a;
             if (sizeof(Real) == 4) {
-                const float4* k4 = reinterpret_cast<const float4*>(kp);
-                reinterpret_cast<float4*>(sK + 8 * s)[0] = k4[0];
-                reinterpret_cast<float4*>(sK + 8 * s)[1] = k4[1];
+                const float4 t0 = reinterpret_cast<const float4*>(T)[0];
+                const float4 t1 = reinterpret_cast<const float4*>(T)[1];
+                a = K0.k(0) * Real(t0.x);
+                a = fma(K0.k(1), Real(t0.y), a);
+                a = fma(K0.k(2), Real(t0.z), a);
+                a = fma(K0.k(3), Real(t0.w), a);
+                a = fma(K0.k(4), Real(t1.x), a);
+                a = fma(K0.k(5), Real(t1.y), a);
             } else {
-                const double2* k2 = reinterpret_cast<const double2*>(kp);
+                a = K0.k(0) * T[0];
 #pragma unroll
-                for (int q = 0; q < 4; ++q) reinterpret_cast<double2*>(sK + 8 * s)[q] = k2[q];
+                for (int q = 1; q < 6; ++q) a = fma(K0.k(q), T[q], a);
             }
-        }
-        __syncwarp();
-        for (int s = 0; s < kChunk; ++s) {
-            const bool act = s < nch;
-            ScatterRec r = {0u, 0u, 0u, 0u};
-            Real a = Real(0);
-            if (act) {
-                r = sRec[s];
-                const int i = r.meta & 15;
-                const Real* Kt = sK + 8 * s;
-                if (isdir) {
-                    // applyDir on the row DOF: the element row becomes e_i, F(i) = bc
-                    if (lj == i) {
-                        const uint32_t off = rec_off(r, i);
-                        sRow[off] += Real(1);
-                        sTouch[off] = 1;
-                    }
-                    if (lj == 0) racc64 += bcr;
+            const uint32_t off = rec_off(r0, lj);
+            bool add = fabs(a) > drop;
+            if (DIR) {
+                const bool colDir = (r0.meta >> (4 + lj)) & 1u;
+                if (isdir) {  // applyDir on the row DOF: the element row becomes e_i
+                    a = Real(1);
+                    add = (lj == i);
                 } else {
-                    const Real* T = sT + i * NLOC + lj;
-                    a = Kt[0] * T[0 * NLOC * NLOC];
-                    a = fma(Kt[1], T[1 * NLOC * NLOC], a);
-                    a = fma(Kt[2], T[2 * NLOC * NLOC], a);
-                    a = fma(Kt[3], T[3 * NLOC * NLOC], a);
-                    a = fma(Kt[4], T[4 * NLOC * NLOC], a);
-                    a = fma(Kt[5], T[5 * NLOC * NLOC], a);
-                    if (!isfinite((double)a)) atomicExch(status, ANIGPU_ERR_NONFINITE);
-                    const uint32_t dm = (r.meta >> 4) & 0x3ffu;
-                    const bool colDir = (dm >> lj) & 1u;
-                    if (!colDir && fabs((double)a) > p.drop) {
-                        const uint32_t off = rec_off(r, lj);
-                        sRow[off] += a;
-                        sTouch[off] = 1;
+                    add = add && !colDir;
+                }
+            }
+            if (BCNZ) sA[lj] = a;
+            if (add) {
+                sRow[off] += a;
+                if (TOUCH) sTouch[off] = 1;
+            }
+            if (lj == 0) {
+                if (isdir) {
+                    ++ndir;
+                } else {
+                    // right-hand side fem3Dtet<IDEN P0, IDEN space>, then applyDir on
+                    // Dirichlet columns in ascending local order (dc_on_dof.h:39-45)
+                    Real F = K0.k(6) * sM[i];
+                    if (BCNZ) {
+                        const uint32_t dm = (r0.meta >> 4) & 0x3ffu;
+                        for (int j = 0; j < NLOC; ++j)
+                            if ((dm >> j) & 1u) F -= sA[j] * Real(p.dir_bc[p.edofs[(int64_t)r0.tet * NLOC + j]]);
                     }
+                    racc += F;
                 }
             }
-            if (p.bc_nonzero) {
-                if (act && !isdir) sA[lj] = a;
-                __syncwarp();
-            }
-            if (act && !isdir && lj == 0) {
-                // right-hand side: fem3Dtet<IDEN P0, IDEN space> then applyDir on Dirichlet
-                // columns in ascending local order (dc_on_dof.h:39-45)
-                const int i = r.meta & 15;
-                const uint32_t dm = (r.meta >> 4) & 0x3ffu;
-                Real F = sK[8 * s + 6] * sM[i];
-                if (p.bc_nonzero && dm) {
-                    for (int j = 0; j < NLOC; ++j)
-                        if ((dm >> j) & 1u) F -= sA[j] * Real(p.dir_bc[p.edofs[(int64_t)r.tet * NLOC + j]]);
-                }
-                racc += F;
-            }
-            __syncwarp();
         }
         __syncwarp();
+        r0 = r1;
+        K0 = K1;
+        r1 = r2;
     }
     if (valid) {
+        bool bad = false;
         for (int s = lj; s < len; s += NLOC) {
-            vals[rb + s] = sRow[s];
-            if (touched_out) touched_out[rb + s] = sTouch[s];
+            const Real v = sRow[s];
+            bad |= !isfinite(v);
+            vals[rb + s] = v;
+            if (TOUCH) touched_out[rb + s] = sTouch[s];
         }
         if (lj == 0) {
-            const double F = isdir ? racc64 : (double)racc;
-            if (!isfinite(F)) atomicExch(status, ANIGPU_ERR_NONFINITE);
+            double F;
+            if (isdir) {
+                const double bcr = p.dir_bc[row];
+                F = 0;
+                for (int q = 0; q < ndir; ++q) F += bcr;  // sum of bc over the incident tets
+            } else {
+                F = (double)racc;
+            }
+            bad |= !isfinite(F);
             rhs[row] = F;
         }
+        if (bad) atomicExch(status, ANIGPU_ERR_NONFINITE);
     }
 }
 
@@ -369,7 +425,8 @@ static int get_row_tables(anigpu_ctx* h, int space, int order, int precision, co
     ScalarBasisTable tb;
     if (!make_scalar_basis(space, order, &tb)) return set_err(h, ANIGPU_ERR_UNSUPPORTED, "unsupported space/order");
     const int nf = tb.nf, q = tb.q;
-    std::vector<double> T(6 * nf * nf + nf, 0.0);
+    // Tsym[i][j][k] (k = 00 11 22 01 02 12, padded to 8) then m[i]
+    std::vector<double> T((size_t)nf * nf * 8 + nf, 0.0);
     const int A[6] = {0, 1, 2, 0, 0, 1}, B[6] = {0, 1, 2, 1, 2, 2};
     for (int k = 0; k < 6; ++k)
         for (int i = 0; i < nf; ++i)
@@ -382,12 +439,12 @@ static int get_row_tables(anigpu_ctx* h, int space, int order, int precision, co
                     if (A[k] != B[k]) v += gi[B[k]] * gj[A[k]];
                     s += tb.wts[n] * v;
                 }
-                T[(size_t)k * nf * nf + i * nf + j] = s;
+                T[((size_t)i * nf + j) * 8 + k] = s;
             }
     for (int i = 0; i < nf; ++i) {
         double s = 0;
         for (int n = 0; n < q; ++n) s += tb.wts[n] * tb.val[(size_t)n * nf + i];
-        T[6 * nf * nf + i] = s;
+        T[(size_t)nf * nf * 8 + i] = s;
     }
     void* d = nullptr;
     if (precision == ANIGPU_F32) {
@@ -403,22 +460,40 @@ static int get_row_tables(anigpu_ctx* h, int space, int order, int precision, co
     return ANIGPU_OK;
 }
 
-template <typename Real, int NLOC>
-static int launch_rows(anigpu_ctx* h, const RowParams& p, const void* tables, void* vals, double* rhs,
-                       uint8_t* touched) {
+template <typename Real, int NLOC, bool DIR, bool BCNZ, bool TOUCH>
+static int launch_rows_t(anigpu_ctx* h, const RowParams& p, const void* tables, void* vals, double* rhs,
+                         uint8_t* touched) {
     constexpr int G = 32 / NLOC;
     const int warps = 4;
-    const size_t tab_bytes = ((sizeof(Real) * (6 * NLOC * NLOC + NLOC) + 15) / 16) * 16;
-    const size_t grp_bytes = ((kChunk * sizeof(ScatterRec) + kChunk * 8 * sizeof(Real) + p.cap * sizeof(Real) +
-                               NLOC * sizeof(Real) + p.cap + 15) / 16) * 16;
+    const size_t tab_bytes = ((sizeof(Real) * (NLOC * NLOC * 8 + NLOC) + 15) / 16) * 16;
+    const size_t grp_bytes =
+        ((p.cap * sizeof(Real) + (TOUCH ? p.cap : 0) + (BCNZ ? NLOC * sizeof(Real) : 0) + 15) / 16) * 16;
     const size_t smem = tab_bytes + grp_bytes * warps * G;
-    auto kern = row_gather_kernel<Real, NLOC>;
+    auto kern = row_gather_kernel<Real, NLOC, DIR, BCNZ, TOUCH>;
     ANI_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int64_t rows_per_block = (int64_t)warps * G;
     kern<<<grid_for(p.nrows, (int)rows_per_block), 32 * warps, smem, h->stream>>>(
         p, (const Real*)tables, (const Real*)h->tetdata, (Real*)vals, rhs, touched, h->d_status);
     ANI_LAUNCHED(h);
     return ANIGPU_OK;
+}
+
+template <typename Real, int NLOC>
+static int launch_rows(anigpu_ctx* h, const RowParams& p, const void* tables, void* vals, double* rhs,
+                       uint8_t* touched) {
+    const bool dir = h->has_dirichlet, bcnz = h->bc_nonzero, tch = touched != nullptr;
+#define LR(D, B, T) return launch_rows_t<Real, NLOC, D, B, T>(h, p, tables, vals, rhs, touched)
+    if (!dir) {
+        if (tch) LR(false, false, true);
+        LR(false, false, false);
+    }
+    if (bcnz) {
+        if (tch) LR(true, true, true);
+        LR(true, true, false);
+    }
+    if (tch) LR(true, false, true);
+    LR(true, false, false);
+#undef LR
 }
 
 int run_assemble(anigpu_ctx* h, int kind, const double* D, const double* f, double f_const, int order,
@@ -444,10 +519,10 @@ int run_assemble(anigpu_ctx* h, int kind, const double* D, const double* f, doub
     }
     time_mark(h, 0);
     if (precision == ANIGPU_F32)
-        tet_prepare_kernel<float><<<grid_for(h->nt, 256), 256, 0, h->stream>>>(h->nt, h->xyz, h->tets, kind, D, f,
-                                                                              f_const, (float*)h->tetdata, h->d_status);
+        tet_prepare_f32_kernel<<<grid_for(h->nt, 256), 256, 0, h->stream>>>(
+            h->nt, h->xyz, h->xyz2, h->tets, kind, D, f, f_const, (float*)h->tetdata, h->d_status);
     else
-        tet_prepare_kernel<double><<<grid_for(h->nt, 256), 256, 0, h->stream>>>(
+        tet_prepare_f64_kernel<<<grid_for(h->nt, 256), 256, 0, h->stream>>>(
             h->nt, h->xyz, h->tets, kind, D, f, f_const, (double*)h->tetdata, h->d_status);
     ANI_LAUNCHED(h);
     time_mark(h, 1);
@@ -459,7 +534,6 @@ int run_assemble(anigpu_ctx* h, int kind, const double* D, const double* f, doub
     p.dir_mask = h->dir_mask;
     p.dir_bc = h->dir_bc;
     p.edofs = h->edofs;
-    p.bc_nonzero = h->bc_nonzero ? 1 : 0;
     p.cap = ((h->max_row_len_s + 15) / 16) * 16;
     p.drop = drop_val;
     if (h->nloc_s == 10) {

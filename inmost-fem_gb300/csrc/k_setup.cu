@@ -573,6 +573,27 @@ __global__ void dof_coords_kernel(int64_t nt, int nloc, int64_t nds, int ncomp, 
 }
 }  // namespace
 
+namespace {
+__global__ void split_coords_kernel(int64_t n, const double* __restrict__ x, float2* __restrict__ out) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double v = x[i];
+    const float hi = __double2float_rn(v);
+    const float lo = __double2float_rn(v - (double)hi);
+    out[i] = make_float2(hi, lo);
+}
+}  // namespace
+
+int setup_coords_split(anigpu_ctx* h) {
+    if (!h->xyz2) {
+        int rc = dev_alloc(h, &h->xyz2, (size_t)h->nv * 3);
+        if (rc) return rc;
+    }
+    split_coords_kernel<<<grid_for(h->nv * 3, 256), 256, 0, h->stream>>>(h->nv * 3, h->xyz, h->xyz2);
+    ANI_LAUNCHED(h);
+    return ANIGPU_OK;
+}
+
 int setup_dof_coords(anigpu_ctx* h, double* out) {
     const int64_t n = h->nt * h->nloc_s;
     dof_coords_kernel<<<grid_for(n, 256), 256, 0, h->stream>>>(h->nt, h->nloc_s, h->nds, h->ncomp, h->xyz, h->tets,
