@@ -245,34 +245,47 @@ struct KVec<double> {
     __device__ __forceinline__ void zero() { a = b = c = d = make_double2(0.0, 0.0); }
 };
 
-// Row gather.  A group of NLOC lanes owns one CSR row; lane j computes A_t(i, j) of each
-// incident tet t (i = the row's local index in t) and adds it into a shared-memory copy of
-// the row at the offset held by the scatter record.  Incidences are walked in ascending
-// tet order with the record and the per-tet block of the next incidences prefetched.
+// Row gather.  One lane owns one CSR row.  It walks the row's incident tets in ascending
+// tet order (the order of the reference's serial cell loop), computes the tet's element
+// row A_t(i, 0..NLOC-1) = sum_k K_t[k] Tsym[i][j][k] in registers and adds it into its own
+// copy of the row in shared memory, laid out lane-interleaved (slot s of lane l at
+// s*32 + l) so that every shared-memory access of the warp is bank-conflict free.  The
+// record and the per-tet block of the next incidence are prefetched.  At the end the warp
+// writes its 32 rows cooperatively (each row contiguous, coalesced).  No atomics: every
+// CSR value is produced by exactly one lane with a fixed summation order.
+template <typename Real, int NLOC>
+struct RowTab {
+    // per-i stride padded so that lanes holding different i read distinct banks
+    static constexpr int TS = NLOC * 8 + (16 / (int)sizeof(Real));
+    static constexpr int SIZE = NLOC * TS + NLOC;  // then m[i]
+};
+
 template <typename Real, int NLOC, bool DIR, bool BCNZ, bool TOUCH>
-__global__ void __launch_bounds__(128) row_gather_kernel(RowParams p, const Real* __restrict__ tables,
-                                                         const Real* __restrict__ tetK, Real* __restrict__ vals,
-                                                         double* __restrict__ rhs, uint8_t* __restrict__ touched_out,
-                                                         int* __restrict__ status) {
-    constexpr int G = 32 / NLOC;
-    constexpr int TAB = NLOC * NLOC * 8 + NLOC;  // Tsym[i][j][8] then m[i]
+__global__ void __launch_bounds__(64) row_gather_kernel(RowParams p, const Real* __restrict__ tables,
+                                                        const Real* __restrict__ tetK, Real* __restrict__ vals,
+                                                        double* __restrict__ rhs, uint8_t* __restrict__ touched_out,
+                                                        int* __restrict__ status) {
+    using Tab = RowTab<Real, NLOC>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int g = lane / NLOC, lj = lane - g * NLOC;
-    const bool in_group = g < G;
+    const int nwarps = blockDim.x >> 5;
     Real* sT = reinterpret_cast<Real*>(smem_raw);
-    for (int k = threadIdx.x; k < TAB; k += blockDim.x) sT[k] = tables[k];
-    const Real* sM = sT + NLOC * NLOC * 8;
-    const size_t tab_bytes = ((sizeof(Real) * TAB + 15) / 16) * 16;
-    const size_t grp_bytes = ((p.cap * sizeof(Real) + (TOUCH ? p.cap : 0) + (BCNZ ? NLOC * sizeof(Real) : 0) + 15) / 16) * 16;
-    unsigned char* gbase = smem_raw + tab_bytes + grp_bytes * (size_t)(warp * G + (in_group ? g : 0));
-    Real* sRow = reinterpret_cast<Real*>(gbase);
-    uint8_t* sTouch = reinterpret_cast<uint8_t*>(sRow + p.cap);
-    Real* sA = reinterpret_cast<Real*>(gbase + p.cap * sizeof(Real) + (TOUCH ? p.cap : 0));
+    // host layout [i][j][8] -> padded stride TS per i
+    for (int k = threadIdx.x; k < NLOC * NLOC * 8; k += blockDim.x) {
+        const int i = k / (NLOC * 8), rem = k - i * NLOC * 8;
+        sT[i * Tab::TS + rem] = tables[k];
+    }
+    for (int k = threadIdx.x; k < NLOC; k += blockDim.x) sT[NLOC * Tab::TS + k] = tables[NLOC * NLOC * 8 + k];
+    const Real* sM = sT + NLOC * Tab::TS;
+    const size_t tab_bytes = ((sizeof(Real) * Tab::SIZE + 15) / 16) * 16;
+    const size_t warp_bytes = (size_t)p.cap * 32 * (sizeof(Real) + (TOUCH ? 1 : 0));
+    Real* sRow = reinterpret_cast<Real*>(smem_raw + tab_bytes + warp_bytes * warp);
+    uint8_t* sTouch = reinterpret_cast<uint8_t*>(sRow + (size_t)p.cap * 32);
     __syncthreads();
 
-    const int64_t row = ((int64_t)blockIdx.x * (blockDim.x >> 5) + warp) * G + g;
-    const bool valid = in_group && row < p.nrows;
+    const int64_t row0 = ((int64_t)blockIdx.x * nwarps + warp) * 32;
+    const int64_t row = row0 + lane;
+    const bool valid = row < p.nrows;
     int64_t ib = 0, rb = 0;
     int len = 0, deg = 0;
     bool isdir = false;
@@ -282,18 +295,13 @@ __global__ void __launch_bounds__(128) row_gather_kernel(RowParams p, const Real
         rb = p.rowptr[row];
         len = (int)(p.rowptr[row + 1] - rb);
         if (DIR) isdir = p.dir_mask[row] != 0;
-        for (int s = lj; s < len; s += NLOC) {
-            sRow[s] = Real(0);
-            if (TOUCH) sTouch[s] = 0;
-        }
     }
-    int maxdeg = deg;
-#pragma unroll
-    for (int o = 16; o; o >>= 1) maxdeg = max(maxdeg, __shfl_xor_sync(0xffffffffu, maxdeg, o));
+    for (int s = 0; s < len; ++s) {
+        sRow[s * 32 + lane] = Real(0);
+        if (TOUCH) sTouch[s * 32 + lane] = 0;
+    }
     const Real drop = Real(p.drop);
     Real racc = Real(0);
-    int ndir = 0;
-    // software pipeline: r0/K0 current, r1 next record (its K is loaded one step ahead)
     ScatterRec r0 = {0u, 0u, 0u, 0u}, r1 = {0u, 0u, 0u, 0u};
     KVec<Real> K0, K1;
     K0.zero();
@@ -303,88 +311,87 @@ __global__ void __launch_bounds__(128) row_gather_kernel(RowParams p, const Real
         K0.load(tetK + 8 * (int64_t)r0.tet);
     }
     if (deg > 1) r1 = p.recs[ib + 1];
-    __syncwarp();
-    for (int k = 0; k < maxdeg; ++k) {
+    for (int k = 0; k < deg; ++k) {
         ScatterRec r2 = {0u, 0u, 0u, 0u};
         if (k + 1 < deg) K1.load(tetK + 8 * (int64_t)r1.tet);
         if (k + 2 < deg) r2 = p.recs[ib + k + 2];
-        if (k < deg) {
-            const int i = r0.meta & 15;
-            const Real* T = sT + (i * NLOC + lj) * 8;
-            Real a;
-            if (sizeof(Real) == 4) {
-                const float4 t0 = reinterpret_cast<const float4*>(T)[0];
-                const float4 t1 = reinterpret_cast<const float4*>(T)[1];
-                a = K0.k(0) * Real(t0.x);
-                a = fma(K0.k(1), Real(t0.y), a);
-                a = fma(K0.k(2), Real(t0.z), a);
-                a = fma(K0.k(3), Real(t0.w), a);
-                a = fma(K0.k(4), Real(t1.x), a);
-                a = fma(K0.k(5), Real(t1.y), a);
-            } else {
-                a = K0.k(0) * T[0];
+        const int i = r0.meta & 15;
+        if (DIR && isdir) {
+            // applyDir on the row DOF: the element row becomes e_i, F(i) = bc
+            const uint32_t off = rec_off(r0, i);
+            sRow[off * 32 + lane] += Real(1);
+            if (TOUCH) sTouch[off * 32 + lane] = 1;
+        } else {
+            const Real* T = sT + i * Tab::TS;
+            const uint32_t dm = DIR ? (r0.meta >> 4) & 0x3ffu : 0u;
+            Real F = K0.k(6) * sM[i];
+            const Real k0 = K0.k(0), k1 = K0.k(1), k2 = K0.k(2), k3 = K0.k(3), k4 = K0.k(4), k5 = K0.k(5);
 #pragma unroll
-                for (int q = 1; q < 6; ++q) a = fma(K0.k(q), T[q], a);
-            }
-            const uint32_t off = rec_off(r0, lj);
-            bool add = fabs(a) > drop;
-            if (DIR) {
-                const bool colDir = (r0.meta >> (4 + lj)) & 1u;
-                if (isdir) {  // applyDir on the row DOF: the element row becomes e_i
-                    a = Real(1);
-                    add = (lj == i);
+            for (int j = 0; j < NLOC; ++j) {
+                Real a;
+                if (sizeof(Real) == 4) {
+                    const float4 t0 = reinterpret_cast<const float4*>(T + j * 8)[0];
+                    const float4 t1 = reinterpret_cast<const float4*>(T + j * 8)[1];
+                    a = k0 * Real(t0.x);
+                    a = fma(k1, Real(t0.y), a);
+                    a = fma(k2, Real(t0.z), a);
+                    a = fma(k3, Real(t0.w), a);
+                    a = fma(k4, Real(t1.x), a);
+                    a = fma(k5, Real(t1.y), a);
                 } else {
-                    add = add && !colDir;
+                    const double2 t0 = reinterpret_cast<const double2*>(T + j * 8)[0];
+                    const double2 t1 = reinterpret_cast<const double2*>(T + j * 8)[1];
+                    const double2 t2 = reinterpret_cast<const double2*>(T + j * 8)[2];
+                    a = k0 * Real(t0.x);
+                    a = fma(k1, Real(t0.y), a);
+                    a = fma(k2, Real(t1.x), a);
+                    a = fma(k3, Real(t1.y), a);
+                    a = fma(k4, Real(t2.x), a);
+                    a = fma(k5, Real(t2.y), a);
                 }
-            }
-            if (BCNZ) sA[lj] = a;
-            if (add) {
-                sRow[off] += a;
-                if (TOUCH) sTouch[off] = 1;
-            }
-            if (lj == 0) {
-                if (isdir) {
-                    ++ndir;
-                } else {
-                    // right-hand side fem3Dtet<IDEN P0, IDEN space>, then applyDir on
-                    // Dirichlet columns in ascending local order (dc_on_dof.h:39-45)
-                    Real F = K0.k(6) * sM[i];
-                    if (BCNZ) {
-                        const uint32_t dm = (r0.meta >> 4) & 0x3ffu;
-                        for (int j = 0; j < NLOC; ++j)
-                            if ((dm >> j) & 1u) F -= sA[j] * Real(p.dir_bc[p.edofs[(int64_t)r0.tet * NLOC + j]]);
-                    }
-                    racc += F;
+                const uint32_t off = rec_off(r0, j);
+                const bool colDir = DIR && ((dm >> j) & 1u);
+                if (!colDir && fabs(a) > drop) {
+                    sRow[off * 32 + lane] += a;
+                    if (TOUCH) sTouch[off * 32 + lane] = 1;
                 }
+                if (BCNZ && colDir)  // applyDir on Dirichlet column j, ascending j (dc_on_dof.h:39-45)
+                    F -= a * Real(p.dir_bc[p.edofs[(int64_t)r0.tet * NLOC + j]]);
             }
+            racc += F;
         }
-        __syncwarp();
         r0 = r1;
         K0 = K1;
         r1 = r2;
     }
+    bool bad = false;
     if (valid) {
-        bool bad = false;
-        for (int s = lj; s < len; s += NLOC) {
-            const Real v = sRow[s];
-            bad |= !isfinite(v);
-            vals[rb + s] = v;
-            if (TOUCH) touched_out[rb + s] = sTouch[s];
+        double F;
+        if (DIR && isdir) {
+            const double bcr = p.dir_bc[row];
+            F = 0;
+            for (int q = 0; q < deg; ++q) F += bcr;  // sum of bc over the incident tets
+        } else {
+            F = (double)racc;
         }
-        if (lj == 0) {
-            double F;
-            if (isdir) {
-                const double bcr = p.dir_bc[row];
-                F = 0;
-                for (int q = 0; q < ndir; ++q) F += bcr;  // sum of bc over the incident tets
-            } else {
-                F = (double)racc;
-            }
-            bad |= !isfinite(F);
-            rhs[row] = F;
-        }
-        if (bad) atomicExch(status, ANIGPU_ERR_NONFINITE);
+        bad |= !isfinite(F);
+        rhs[row] = F;
     }
+    __syncwarp();
+    // cooperative write-out: row by row, all lanes, contiguous stores
+    const int64_t rem_rows = p.nrows - row0;
+    const int nrow = rem_rows < 32 ? (int)rem_rows : 32;
+    for (int w = 0; w < nrow; ++w) {
+        const int64_t rbw = __shfl_sync(0xffffffffu, rb, w);
+        const int lenw = __shfl_sync(0xffffffffu, len, w);
+        for (int s = lane; s < lenw; s += 32) {
+            const Real v = sRow[s * 32 + w];
+            bad |= !isfinite(v);
+            vals[rbw + s] = v;
+            if (TOUCH) touched_out[rbw + s] = sTouch[s * 32 + w];
+        }
+    }
+    if (bad) atomicExch(status, ANIGPU_ERR_NONFINITE);
 }
 
 // ---------------------------------------------------------------- CSR compaction
@@ -463,16 +470,13 @@ static int get_row_tables(anigpu_ctx* h, int space, int order, int precision, co
 template <typename Real, int NLOC, bool DIR, bool BCNZ, bool TOUCH>
 static int launch_rows_t(anigpu_ctx* h, const RowParams& p, const void* tables, void* vals, double* rhs,
                          uint8_t* touched) {
-    constexpr int G = 32 / NLOC;
-    const int warps = 4;
-    const size_t tab_bytes = ((sizeof(Real) * (NLOC * NLOC * 8 + NLOC) + 15) / 16) * 16;
-    const size_t grp_bytes =
-        ((p.cap * sizeof(Real) + (TOUCH ? p.cap : 0) + (BCNZ ? NLOC * sizeof(Real) : 0) + 15) / 16) * 16;
-    const size_t smem = tab_bytes + grp_bytes * warps * G;
+    const int warps = 2;
+    const size_t tab_bytes = ((sizeof(Real) * RowTab<Real, NLOC>::SIZE + 15) / 16) * 16;
+    const size_t warp_bytes = (size_t)p.cap * 32 * (sizeof(Real) + (TOUCH ? 1 : 0));
+    const size_t smem = tab_bytes + warp_bytes * warps;
     auto kern = row_gather_kernel<Real, NLOC, DIR, BCNZ, TOUCH>;
     ANI_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const int64_t rows_per_block = (int64_t)warps * G;
-    kern<<<grid_for(p.nrows, (int)rows_per_block), 32 * warps, smem, h->stream>>>(
+    kern<<<grid_for(p.nrows, 32 * warps), 32 * warps, smem, h->stream>>>(
         p, (const Real*)tables, (const Real*)h->tetdata, (Real*)vals, rhs, touched, h->d_status);
     ANI_LAUNCHED(h);
     return ANIGPU_OK;
@@ -534,7 +538,7 @@ int run_assemble(anigpu_ctx* h, int kind, const double* D, const double* f, doub
     p.dir_mask = h->dir_mask;
     p.dir_bc = h->dir_bc;
     p.edofs = h->edofs;
-    p.cap = ((h->max_row_len_s + 15) / 16) * 16;
+    p.cap = h->max_row_len_s;
     p.drop = drop_val;
     if (h->nloc_s == 10) {
         rc = precision == ANIGPU_F32 ? launch_rows<float, 10>(h, p, tables, vals, rhs, touched)
