@@ -68,6 +68,8 @@ struct anigpu_ctx {
     int64_t* inc_ptr = nullptr;    // nds+1
     ScatterRec* recs = nullptr;    // nt*nloc_s
     int max_row_len_s = 0;
+    int64_t row_range[3] = {0, 0, 0};  // scalar rows [vertex DOFs | edge DOFs]
+    int row_range_cap[2] = {0, 0};     // longest row of each range
     int max_deg = 0;               // max incident tets of a scalar DOF
     uint8_t* dir_mask = nullptr;   // ndof
     double* dir_bc = nullptr;      // ndof

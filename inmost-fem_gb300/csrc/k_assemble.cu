@@ -199,7 +199,8 @@ __global__ void tet_prepare_f32_kernel(int64_t nt, const double* __restrict__ xy
 
 // ---------------------------------------------------------------- phase 2
 struct RowParams {
-    int64_t nrows;
+    int64_t row_begin;  // first row of this launch
+    int64_t nrows;      // one past the last row of this launch
     const int64_t* inc_ptr;
     const ScatterRec* recs;
     const int64_t* rowptr;
@@ -248,11 +249,15 @@ struct KVec<double> {
 // Row gather.  One lane owns one CSR row.  It walks the row's incident tets in ascending
 // tet order (the order of the reference's serial cell loop), computes the tet's element
 // row A_t(i, 0..NLOC-1) = sum_k K_t[k] Tsym[i][j][k] in registers and adds it into its own
-// copy of the row in shared memory, laid out lane-interleaved (slot s of lane l at
-// s*32 + l) so that every shared-memory access of the warp is bank-conflict free.  The
+// copy of the row in shared memory, lane-interleaved and rotated (see rot()).  The
 // record and the per-tet block of the next incidence are prefetched.  At the end the warp
 // writes its 32 rows cooperatively (each row contiguous, coalesced).  No atomics: every
 // CSR value is produced by exactly one lane with a fixed summation order.
+// slot s of lane l lives at s*32 + ((s + l) & 31): every lane touching its own slot and
+// the transposed read of one row by the whole warp are both free of bank conflicts when
+// the lanes' slots are equal (structured meshes), and at most a few-way otherwise.
+__device__ __forceinline__ int rot(int s, int l) { return s * 32 + ((s + l) & 31); }
+
 template <typename Real, int NLOC>
 struct RowTab {
     // per-i stride padded so that lanes holding different i read distinct banks
@@ -283,7 +288,7 @@ __global__ void __launch_bounds__(64) row_gather_kernel(RowParams p, const Real*
     uint8_t* sTouch = reinterpret_cast<uint8_t*>(sRow + (size_t)p.cap * 32);
     __syncthreads();
 
-    const int64_t row0 = ((int64_t)blockIdx.x * nwarps + warp) * 32;
+    const int64_t row0 = p.row_begin + ((int64_t)blockIdx.x * nwarps + warp) * 32;
     const int64_t row = row0 + lane;
     const bool valid = row < p.nrows;
     int64_t ib = 0, rb = 0;
@@ -297,8 +302,8 @@ __global__ void __launch_bounds__(64) row_gather_kernel(RowParams p, const Real*
         if (DIR) isdir = p.dir_mask[row] != 0;
     }
     for (int s = 0; s < len; ++s) {
-        sRow[s * 32 + lane] = Real(0);
-        if (TOUCH) sTouch[s * 32 + lane] = 0;
+        sRow[rot(s, lane)] = Real(0);
+        if (TOUCH) sTouch[rot(s, lane)] = 0;
     }
     const Real drop = Real(p.drop);
     Real racc = Real(0);
@@ -319,8 +324,8 @@ __global__ void __launch_bounds__(64) row_gather_kernel(RowParams p, const Real*
         if (DIR && isdir) {
             // applyDir on the row DOF: the element row becomes e_i, F(i) = bc
             const uint32_t off = rec_off(r0, i);
-            sRow[off * 32 + lane] += Real(1);
-            if (TOUCH) sTouch[off * 32 + lane] = 1;
+            sRow[rot(off, lane)] += Real(1);
+            if (TOUCH) sTouch[rot(off, lane)] = 1;
         } else {
             const Real* T = sT + i * Tab::TS;
             const uint32_t dm = DIR ? (r0.meta >> 4) & 0x3ffu : 0u;
@@ -351,9 +356,13 @@ __global__ void __launch_bounds__(64) row_gather_kernel(RowParams p, const Real*
                 }
                 const uint32_t off = rec_off(r0, j);
                 const bool colDir = DIR && ((dm >> j) & 1u);
-                if (!colDir && fabs(a) > drop) {
-                    sRow[off * 32 + lane] += a;
-                    if (TOUCH) sTouch[off * 32 + lane] = 1;
+                // the drop rule (|a| > drop_val, assembler.inl:416-418); without a touched map and
+                // with a drop value below the smallest FP32 subnormal it only skips exact zeros,
+                // which cannot change a sum, so the FP32 template path omits the test
+                const bool keep = (!TOUCH && sizeof(Real) == 4 && drop == Real(0)) ? true : (fabs(a) > drop);
+                if (!colDir && keep) {
+                    sRow[rot(off, lane)] += a;
+                    if (TOUCH) sTouch[rot(off, lane)] = 1;
                 }
                 if (BCNZ && colDir)  // applyDir on Dirichlet column j, ascending j (dc_on_dof.h:39-45)
                     F -= a * Real(p.dir_bc[p.edofs[(int64_t)r0.tet * NLOC + j]]);
@@ -385,10 +394,10 @@ __global__ void __launch_bounds__(64) row_gather_kernel(RowParams p, const Real*
         const int64_t rbw = __shfl_sync(0xffffffffu, rb, w);
         const int lenw = __shfl_sync(0xffffffffu, len, w);
         for (int s = lane; s < lenw; s += 32) {
-            const Real v = sRow[s * 32 + w];
+            const Real v = sRow[rot(s, w)];
             bad |= !isfinite(v);
             vals[rbw + s] = v;
-            if (TOUCH) touched_out[rbw + s] = sTouch[s * 32 + w];
+            if (TOUCH) touched_out[rbw + s] = sTouch[rot(s, w)];
         }
     }
     if (bad) atomicExch(status, ANIGPU_ERR_NONFINITE);
@@ -476,7 +485,7 @@ static int launch_rows_t(anigpu_ctx* h, const RowParams& p, const void* tables, 
     const size_t smem = tab_bytes + warp_bytes * warps;
     auto kern = row_gather_kernel<Real, NLOC, DIR, BCNZ, TOUCH>;
     ANI_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kern<<<grid_for(p.nrows, 32 * warps), 32 * warps, smem, h->stream>>>(
+    kern<<<grid_for(p.nrows - p.row_begin, 32 * warps), 32 * warps, smem, h->stream>>>(
         p, (const Real*)tables, (const Real*)h->tetdata, (Real*)vals, rhs, touched, h->d_status);
     ANI_LAUNCHED(h);
     return ANIGPU_OK;
@@ -531,21 +540,28 @@ int run_assemble(anigpu_ctx* h, int kind, const double* D, const double* f, doub
     ANI_LAUNCHED(h);
     time_mark(h, 1);
     RowParams p;
-    p.nrows = h->nds;
     p.inc_ptr = h->inc_ptr;
     p.recs = h->recs;
     p.rowptr = h->rowptr_s;
     p.dir_mask = h->dir_mask;
     p.dir_bc = h->dir_bc;
     p.edofs = h->edofs;
-    p.cap = h->max_row_len_s;
     p.drop = drop_val;
-    if (h->nloc_s == 10) {
-        rc = precision == ANIGPU_F32 ? launch_rows<float, 10>(h, p, tables, vals, rhs, touched)
-                                     : launch_rows<double, 10>(h, p, tables, vals, rhs, touched);
-    } else {
-        rc = precision == ANIGPU_F32 ? launch_rows<float, 4>(h, p, tables, vals, rhs, touched)
-                                     : launch_rows<double, 4>(h, p, tables, vals, rhs, touched);
+    // one launch per row range (vertex rows, edge rows) so that the shared-memory row
+    // buffer fits the longest row of that range
+    for (int rg = 0; rg < 2; ++rg) {
+        p.row_begin = h->row_range[rg];
+        p.nrows = h->row_range[rg + 1];
+        p.cap = h->row_range_cap[rg];
+        if (p.nrows <= p.row_begin) continue;
+        if (h->nloc_s == 10) {
+            rc = precision == ANIGPU_F32 ? launch_rows<float, 10>(h, p, tables, vals, rhs, touched)
+                                         : launch_rows<double, 10>(h, p, tables, vals, rhs, touched);
+        } else {
+            rc = precision == ANIGPU_F32 ? launch_rows<float, 4>(h, p, tables, vals, rhs, touched)
+                                         : launch_rows<double, 4>(h, p, tables, vals, rhs, touched);
+        }
+        if (rc) return rc;
     }
     time_mark(h, 2);
     return rc;

@@ -507,6 +507,16 @@ int setup_problem(anigpu_ctx* h, int space) {
         unsigned long long maxlen = 0;
         RC(max_count(h, dcnt, nds, &maxlen));
         h->max_row_len_s = (int)maxlen;
+        // row ranges: vertex rows [0, nv) and (P2) edge rows [nv, nds), each with its longest row
+        h->row_range[0] = 0;
+        h->row_range[1] = space == ANIGPU_P1 ? nds : nv;
+        h->row_range[2] = nds;
+        for (int rg = 0; rg < 2; ++rg) {
+            const int64_t b = h->row_range[rg], e = h->row_range[rg + 1];
+            unsigned long long m = 0;
+            if (e > b) RC(max_count(h, dcnt + b, e - b, &m));
+            h->row_range_cap[rg] = (int)m;
+        }
         if (maxlen > 256) return set_err(h, ANIGPU_ERR_UNSUPPORTED, "scalar row longer than 256 entries");
         RC(dev_alloc(h, &h->rowptr_s, (size_t)nds + 1));
         RC(scan_counts(h, dcnt, nds, h->rowptr_s));
