@@ -331,41 +331,52 @@ __global__ void __launch_bounds__(64) row_gather_kernel(RowParams p, const Real*
             const uint32_t dm = DIR ? (r0.meta >> 4) & 0x3ffu : 0u;
             Real F = K0.k(6) * sM[i];
             const Real k0 = K0.k(0), k1 = K0.k(1), k2 = K0.k(2), k3 = K0.k(3), k4 = K0.k(4), k5 = K0.k(5);
+            Real a[NLOC];
+            int addr[NLOC];
+            bool add[NLOC];
 #pragma unroll
             for (int j = 0; j < NLOC; ++j) {
-                Real a;
                 if (sizeof(Real) == 4) {
                     const float4 t0 = reinterpret_cast<const float4*>(T + j * 8)[0];
                     const float4 t1 = reinterpret_cast<const float4*>(T + j * 8)[1];
-                    a = k0 * Real(t0.x);
-                    a = fma(k1, Real(t0.y), a);
-                    a = fma(k2, Real(t0.z), a);
-                    a = fma(k3, Real(t0.w), a);
-                    a = fma(k4, Real(t1.x), a);
-                    a = fma(k5, Real(t1.y), a);
+                    Real v = k0 * Real(t0.x);
+                    v = fma(k1, Real(t0.y), v);
+                    v = fma(k2, Real(t0.z), v);
+                    v = fma(k3, Real(t0.w), v);
+                    v = fma(k4, Real(t1.x), v);
+                    a[j] = fma(k5, Real(t1.y), v);
                 } else {
                     const double2 t0 = reinterpret_cast<const double2*>(T + j * 8)[0];
                     const double2 t1 = reinterpret_cast<const double2*>(T + j * 8)[1];
                     const double2 t2 = reinterpret_cast<const double2*>(T + j * 8)[2];
-                    a = k0 * Real(t0.x);
-                    a = fma(k1, Real(t0.y), a);
-                    a = fma(k2, Real(t1.x), a);
-                    a = fma(k3, Real(t1.y), a);
-                    a = fma(k4, Real(t2.x), a);
-                    a = fma(k5, Real(t2.y), a);
+                    Real v = k0 * Real(t0.x);
+                    v = fma(k1, Real(t0.y), v);
+                    v = fma(k2, Real(t1.x), v);
+                    v = fma(k3, Real(t1.y), v);
+                    v = fma(k4, Real(t2.x), v);
+                    a[j] = fma(k5, Real(t2.y), v);
                 }
-                const uint32_t off = rec_off(r0, j);
+                addr[j] = rot((int)rec_off(r0, j), lane);
                 const bool colDir = DIR && ((dm >> j) & 1u);
-                // the drop rule (|a| > drop_val, assembler.inl:416-418); without a touched map and
-                // with a drop value below the smallest FP32 subnormal it only skips exact zeros,
-                // which cannot change a sum, so the FP32 template path omits the test
-                const bool keep = (!TOUCH && sizeof(Real) == 4 && drop == Real(0)) ? true : (fabs(a) > drop);
-                if (!colDir && keep) {
-                    sRow[rot(off, lane)] += a;
-                    if (TOUCH) sTouch[rot(off, lane)] = 1;
-                }
+                // the drop rule (|a| > drop_val, assembler.inl:416-418); without a touched map
+                // and with a drop value below the smallest FP32 subnormal it only skips exact
+                // zeros, which cannot change a sum, so the FP32 template path omits the test
+                const bool keep = (!TOUCH && sizeof(Real) == 4 && drop == Real(0)) ? true : (fabs(a[j]) > drop);
+                add[j] = !colDir && keep;
                 if (BCNZ && colDir)  // applyDir on Dirichlet column j, ascending j (dc_on_dof.h:39-45)
-                    F -= a * Real(p.dir_bc[p.edofs[(int64_t)r0.tet * NLOC + j]]);
+                    F -= a[j] * Real(p.dir_bc[p.edofs[(int64_t)r0.tet * NLOC + j]]);
+            }
+            // the NLOC slots of one element row are distinct columns: independent updates
+            Real cur[NLOC];
+#pragma unroll
+            for (int j = 0; j < NLOC; ++j) cur[j] = sRow[addr[j]];
+#pragma unroll
+            for (int j = 0; j < NLOC; ++j)
+                if (add[j]) sRow[addr[j]] = cur[j] + a[j];
+            if (TOUCH) {
+#pragma unroll
+                for (int j = 0; j < NLOC; ++j)
+                    if (add[j]) sTouch[addr[j]] = 1;
             }
             racc += F;
         }
