@@ -41,6 +41,8 @@ struct anigpu_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t own_stream = nullptr;
+    cudaStream_t side_stream = nullptr;  // second stream for concurrent launches inside one call
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     std::string err;
     int64_t launches = 0;
 

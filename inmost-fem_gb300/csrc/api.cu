@@ -40,6 +40,13 @@ int anigpu_create(anigpu_handle* out, int device) {
         return ANIGPU_ERR_CUDA;
     }
     h->stream = h->own_stream;
+    if (cudaStreamCreateWithFlags(&h->side_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->join_ev, cudaEventDisableTiming) != cudaSuccess) {
+        cudaStreamDestroy(h->own_stream);
+        delete h;
+        return ANIGPU_ERR_CUDA;
+    }
     if (cudaMalloc((void**)&h->d_status, sizeof(int)) != cudaSuccess ||
         cudaMemset(h->d_status, 0, sizeof(int)) != cudaSuccess) {
         cudaStreamDestroy(h->own_stream);
@@ -68,6 +75,9 @@ int anigpu_destroy(anigpu_handle h) {
     for (void* p : h->extra_allocs) cudaFree(p);
     for (auto& e : h->tev)
         if (e) cudaEventDestroy(e);
+    if (h->fork_ev) cudaEventDestroy(h->fork_ev);
+    if (h->join_ev) cudaEventDestroy(h->join_ev);
+    if (h->side_stream) cudaStreamDestroy(h->side_stream);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
     delete h;
     return ANIGPU_OK;

@@ -253,10 +253,11 @@ struct KVec<double> {
 // record and the per-tet block of the next incidence are prefetched.  At the end the warp
 // writes its 32 rows cooperatively (each row contiguous, coalesced).  No atomics: every
 // CSR value is produced by exactly one lane with a fixed summation order.
-// slot s of lane l lives at s*32 + ((s + l) & 31): every lane touching its own slot and
-// the transposed read of one row by the whole warp are both free of bank conflicts when
-// the lanes' slots are equal (structured meshes), and at most a few-way otherwise.
-__device__ __forceinline__ int rot(int s, int l) { return s * 32 + ((s + l) & 31); }
+// slot s of lane l lives at s*33 + l (rows padded to 33 words): every lane touching its
+// own slot and the transposed read of one row by the whole warp are both free of bank
+// conflicts when the lanes' slots are equal (structured meshes), and at most a few-way
+// otherwise.
+__device__ __forceinline__ int rot(int s, int l) { return s * 33 + l; }
 
 template <typename Real, int NLOC>
 struct RowTab {
@@ -265,7 +266,7 @@ struct RowTab {
     static constexpr int SIZE = NLOC * TS + NLOC;  // then m[i]
 };
 
-template <typename Real, int NLOC, bool DIR, bool BCNZ, bool TOUCH>
+template <typename Real, int NLOC, bool DIR, bool BCNZ, bool TOUCH, bool DROPCHK>
 __global__ void __launch_bounds__(64) row_gather_kernel(RowParams p, const Real* __restrict__ tables,
                                                         const Real* __restrict__ tetK, Real* __restrict__ vals,
                                                         double* __restrict__ rhs, uint8_t* __restrict__ touched_out,
@@ -283,9 +284,9 @@ __global__ void __launch_bounds__(64) row_gather_kernel(RowParams p, const Real*
     for (int k = threadIdx.x; k < NLOC; k += blockDim.x) sT[NLOC * Tab::TS + k] = tables[NLOC * NLOC * 8 + k];
     const Real* sM = sT + NLOC * Tab::TS;
     const size_t tab_bytes = ((sizeof(Real) * Tab::SIZE + 15) / 16) * 16;
-    const size_t warp_bytes = (size_t)p.cap * 32 * (sizeof(Real) + (TOUCH ? 1 : 0));
+    const size_t warp_bytes = (size_t)p.cap * 33 * (sizeof(Real) + (TOUCH ? 1 : 0));
     Real* sRow = reinterpret_cast<Real*>(smem_raw + tab_bytes + warp_bytes * warp);
-    uint8_t* sTouch = reinterpret_cast<uint8_t*>(sRow + (size_t)p.cap * 32);
+    uint8_t* sTouch = reinterpret_cast<uint8_t*>(sRow + (size_t)p.cap * 33);
     __syncthreads();
 
     const int64_t row0 = p.row_begin + ((int64_t)blockIdx.x * nwarps + warp) * 32;
@@ -358,11 +359,10 @@ __global__ void __launch_bounds__(64) row_gather_kernel(RowParams p, const Real*
                 }
                 addr[j] = rot((int)rec_off(r0, j), lane);
                 const bool colDir = DIR && ((dm >> j) & 1u);
-                // the drop rule (|a| > drop_val, assembler.inl:416-418); without a touched map
-                // and with a drop value below the smallest FP32 subnormal it only skips exact
-                // zeros, which cannot change a sum, so the FP32 template path omits the test
-                const bool keep = (!TOUCH && sizeof(Real) == 4 && drop == Real(0)) ? true : (fabs(a[j]) > drop);
-                add[j] = !colDir && keep;
+                // the drop rule |a| > drop_val (assembler.inl:416-418).  Without a touched map
+                // and with a drop value that rounds to zero in FP32 the rule only skips exact
+                // zeros, which cannot change a sum: that variant is compiled without the test.
+                add[j] = !colDir && (!DROPCHK || fabs(a[j]) > drop);
                 if (BCNZ && colDir)  // applyDir on Dirichlet column j, ascending j (dc_on_dof.h:39-45)
                     F -= a[j] * Real(p.dir_bc[p.edofs[(int64_t)r0.tet * NLOC + j]]);
             }
@@ -487,16 +487,16 @@ static int get_row_tables(anigpu_ctx* h, int space, int order, int precision, co
     return ANIGPU_OK;
 }
 
-template <typename Real, int NLOC, bool DIR, bool BCNZ, bool TOUCH>
+template <typename Real, int NLOC, bool DIR, bool BCNZ, bool TOUCH, bool DROPCHK>
 static int launch_rows_t(anigpu_ctx* h, const RowParams& p, const void* tables, void* vals, double* rhs,
-                         uint8_t* touched) {
+                         uint8_t* touched, cudaStream_t st) {
     const int warps = 2;
     const size_t tab_bytes = ((sizeof(Real) * RowTab<Real, NLOC>::SIZE + 15) / 16) * 16;
-    const size_t warp_bytes = (size_t)p.cap * 32 * (sizeof(Real) + (TOUCH ? 1 : 0));
+    const size_t warp_bytes = (size_t)p.cap * 33 * (sizeof(Real) + (TOUCH ? 1 : 0));
     const size_t smem = tab_bytes + warp_bytes * warps;
-    auto kern = row_gather_kernel<Real, NLOC, DIR, BCNZ, TOUCH>;
+    auto kern = row_gather_kernel<Real, NLOC, DIR, BCNZ, TOUCH, DROPCHK>;
     ANI_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kern<<<grid_for(p.nrows - p.row_begin, 32 * warps), 32 * warps, smem, h->stream>>>(
+    kern<<<grid_for(p.nrows - p.row_begin, 32 * warps), 32 * warps, smem, st>>>(
         p, (const Real*)tables, (const Real*)h->tetdata, (Real*)vals, rhs, touched, h->d_status);
     ANI_LAUNCHED(h);
     return ANIGPU_OK;
@@ -504,19 +504,24 @@ static int launch_rows_t(anigpu_ctx* h, const RowParams& p, const void* tables, 
 
 template <typename Real, int NLOC>
 static int launch_rows(anigpu_ctx* h, const RowParams& p, const void* tables, void* vals, double* rhs,
-                       uint8_t* touched) {
+                       uint8_t* touched, cudaStream_t st) {
     const bool dir = h->has_dirichlet, bcnz = h->bc_nonzero, tch = touched != nullptr;
-#define LR(D, B, T) return launch_rows_t<Real, NLOC, D, B, T>(h, p, tables, vals, rhs, touched)
-    if (!dir) {
-        if (tch) LR(false, false, true);
-        LR(false, false, false);
+    // FP32 template assembly with a drop value that is zero in FP32 needs no drop test
+    const bool dchk = tch || sizeof(Real) == 8 || (float)p.drop != 0.0f;
+#define LR(D, B, T, C) return launch_rows_t<Real, NLOC, D, B, T, C>(h, p, tables, vals, rhs, touched, st)
+    if (tch) {
+        if (!dir) LR(false, false, true, true);
+        if (bcnz) LR(true, true, true, true);
+        LR(true, false, true, true);
     }
-    if (bcnz) {
-        if (tch) LR(true, true, true);
-        LR(true, true, false);
+    if (dchk) {
+        if (!dir) LR(false, false, false, true);
+        if (bcnz) LR(true, true, false, true);
+        LR(true, false, false, true);
     }
-    if (tch) LR(true, false, true);
-    LR(true, false, false);
+    if (!dir) LR(false, false, false, false);
+    if (bcnz) LR(true, true, false, false);
+    LR(true, false, false, false);
 #undef LR
 }
 
@@ -559,20 +564,31 @@ int run_assemble(anigpu_ctx* h, int kind, const double* D, const double* f, doub
     p.edofs = h->edofs;
     p.drop = drop_val;
     // one launch per row range (vertex rows, edge rows) so that the shared-memory row
-    // buffer fits the longest row of that range
+    // buffer fits the longest row of that range; the two run concurrently (the vertex
+    // range on a side stream) so that the tail of one overlaps the other
+    cudaStream_t side = h->side_stream ? h->side_stream : h->stream;
+    if (side != h->stream) {
+        ANI_CUDA(h, cudaEventRecord(h->fork_ev, h->stream));
+        ANI_CUDA(h, cudaStreamWaitEvent(side, h->fork_ev, 0));
+    }
     for (int rg = 0; rg < 2; ++rg) {
         p.row_begin = h->row_range[rg];
         p.nrows = h->row_range[rg + 1];
         p.cap = h->row_range_cap[rg];
         if (p.nrows <= p.row_begin) continue;
+        cudaStream_t st = rg == 0 ? side : h->stream;
         if (h->nloc_s == 10) {
-            rc = precision == ANIGPU_F32 ? launch_rows<float, 10>(h, p, tables, vals, rhs, touched)
-                                         : launch_rows<double, 10>(h, p, tables, vals, rhs, touched);
+            rc = precision == ANIGPU_F32 ? launch_rows<float, 10>(h, p, tables, vals, rhs, touched, st)
+                                         : launch_rows<double, 10>(h, p, tables, vals, rhs, touched, st);
         } else {
-            rc = precision == ANIGPU_F32 ? launch_rows<float, 4>(h, p, tables, vals, rhs, touched)
-                                         : launch_rows<double, 4>(h, p, tables, vals, rhs, touched);
+            rc = precision == ANIGPU_F32 ? launch_rows<float, 4>(h, p, tables, vals, rhs, touched, st)
+                                         : launch_rows<double, 4>(h, p, tables, vals, rhs, touched, st);
         }
         if (rc) return rc;
+    }
+    if (side != h->stream) {
+        ANI_CUDA(h, cudaEventRecord(h->join_ev, side));
+        ANI_CUDA(h, cudaStreamWaitEvent(h->stream, h->join_ev, 0));
     }
     time_mark(h, 2);
     return rc;
