@@ -284,7 +284,7 @@ __global__ void __launch_bounds__(64) row_gather_kernel(RowParams p, const Real*
     for (int k = threadIdx.x; k < NLOC; k += blockDim.x) sT[NLOC * Tab::TS + k] = tables[NLOC * NLOC * 8 + k];
     const Real* sM = sT + NLOC * Tab::TS;
     const size_t tab_bytes = ((sizeof(Real) * Tab::SIZE + 15) / 16) * 16;
-    const size_t warp_bytes = (size_t)p.cap * 33 * (sizeof(Real) + (TOUCH ? 1 : 0));
+    const size_t warp_bytes = (((size_t)p.cap * 33 * (sizeof(Real) + (TOUCH ? 1 : 0))) + 15) / 16 * 16;
     Real* sRow = reinterpret_cast<Real*>(smem_raw + tab_bytes + warp_bytes * warp);
     uint8_t* sTouch = reinterpret_cast<uint8_t*>(sRow + (size_t)p.cap * 33);
     __syncthreads();
@@ -492,7 +492,7 @@ static int launch_rows_t(anigpu_ctx* h, const RowParams& p, const void* tables, 
                          uint8_t* touched, cudaStream_t st) {
     const int warps = 2;
     const size_t tab_bytes = ((sizeof(Real) * RowTab<Real, NLOC>::SIZE + 15) / 16) * 16;
-    const size_t warp_bytes = (size_t)p.cap * 33 * (sizeof(Real) + (TOUCH ? 1 : 0));
+    const size_t warp_bytes = (((size_t)p.cap * 33 * (sizeof(Real) + (TOUCH ? 1 : 0))) + 15) / 16 * 16;
     const size_t smem = tab_bytes + warp_bytes * warps;
     auto kern = row_gather_kernel<Real, NLOC, DIR, BCNZ, TOUCH, DROPCHK>;
     ANI_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

@@ -90,7 +90,9 @@ __global__ void __launch_bounds__(kBlock) spmv_dot_kernel(int64_t n, const int64
     __shared__ double sh[33];
     if (sc->done) return;
     const int64_t rows_per_block = kBlock / W;
-    double acc = 0;
+    // per-thread partial in the vector type (a few rows per thread), block sum in FP64:
+    // the FP32 solve keeps FP64 instructions off its per-row path
+    T acc = 0;
     for (int64_t base = blockIdx.x * rows_per_block; base < n; base += (int64_t)gridDim.x * rows_per_block) {
         const int64_t row = base + threadIdx.x / W;
         const int lane = threadIdx.x & (W - 1);
@@ -103,10 +105,10 @@ __global__ void __launch_bounds__(kBlock) spmv_dot_kernel(int64_t n, const int64
         for (int o = W / 2; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, W);
         if (row < n && lane == 0) {
             q[row] = s;
-            acc += (double)s * (double)p[row];
+            acc += s * p[row];
         }
     }
-    const double tot = block_reduce_sum(acc, sh);
+    const double tot = block_reduce_sum((double)acc, sh);
     if (threadIdx.x == 0) part[blockIdx.x] = tot;
 }
 
@@ -124,19 +126,20 @@ __global__ void __launch_bounds__(kBlock) update_kernel(int64_t n, int parity, X
     const double rz = sc->rz[parity];
     const double alpha = rz / pq;
     const T a = (T)alpha;
-    double arz = 0, arr = 0;
+    const X ax = (X)alpha;
+    T arz = 0, arr = 0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        x[i] += (X)(alpha * (double)p[i]);
+        x[i] += ax * (X)p[i];
         const T ri = r[i] - a * q[i];
         r[i] = ri;
         const T zi = dinv[i] * ri;
         z[i] = zi;
-        arz += (double)ri * (double)zi;
-        arr += (double)ri * (double)ri;
+        arz += ri * zi;
+        arr += ri * ri;
     }
-    const double trz = block_reduce_sum(arz, sh);
+    const double trz = block_reduce_sum((double)arz, sh);
     __syncthreads();
-    const double trr = block_reduce_sum(arr, sh);
+    const double trr = block_reduce_sum((double)arr, sh);
     if (threadIdx.x == 0) {
         part_rz[blockIdx.x] = trz;
         part_rr[blockIdx.x] = trr;
