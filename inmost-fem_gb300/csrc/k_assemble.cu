@@ -284,10 +284,17 @@ __global__ void __launch_bounds__(64) row_gather_kernel(RowParams p, const Real*
     for (int k = threadIdx.x; k < NLOC; k += blockDim.x) sT[NLOC * Tab::TS + k] = tables[NLOC * NLOC * 8 + k];
     const Real* sM = sT + NLOC * Tab::TS;
     const size_t tab_bytes = ((sizeof(Real) * Tab::SIZE + 15) / 16) * 16;
-    const size_t warp_bytes = (((size_t)p.cap * 33 * (sizeof(Real) + (TOUCH ? 1 : 0))) + 15) / 16 * 16;
-    Real* sRow = reinterpret_cast<Real*>(smem_raw + tab_bytes + warp_bytes * warp);
-    uint8_t* sTouch = reinterpret_cast<uint8_t*>(sRow + (size_t)p.cap * 33);
-    __syncthreads();
+    // per warp: row metadata (32 x {row start, length}), the rows, the touched map
+    const size_t meta_bytes = 32 * 16;
+    const size_t row_bytes = (((size_t)p.cap * 33 * sizeof(Real)) + 15) / 16 * 16;
+    const size_t touch_bytes = TOUCH ? (((size_t)p.cap * 33) + 15) / 16 * 16 : 0;
+    unsigned char* wbase = smem_raw + tab_bytes + (meta_bytes + row_bytes + touch_bytes) * warp;
+    longlong2* sMeta = reinterpret_cast<longlong2*>(wbase);
+    Real* sRow = reinterpret_cast<Real*>(wbase + meta_bytes);
+    uint8_t* sTouch = reinterpret_cast<uint8_t*>(wbase + meta_bytes + row_bytes);
+    // zero this warp's rows (and touched map), 16 bytes per store
+    for (size_t k = lane; k < (row_bytes + touch_bytes) / 16; k += 32)
+        reinterpret_cast<int4*>(sRow)[k] = make_int4(0, 0, 0, 0);
 
     const int64_t row0 = p.row_begin + ((int64_t)blockIdx.x * nwarps + warp) * 32;
     const int64_t row = row0 + lane;
@@ -302,84 +309,84 @@ __global__ void __launch_bounds__(64) row_gather_kernel(RowParams p, const Real*
         len = (int)(p.rowptr[row + 1] - rb);
         if (DIR) isdir = p.dir_mask[row] != 0;
     }
-    for (int s = 0; s < len; ++s) {
-        sRow[rot(s, lane)] = Real(0);
-        if (TOUCH) sTouch[rot(s, lane)] = 0;
-    }
+    sMeta[lane] = make_longlong2(rb, len);
+    __syncthreads();
+    Real* myRow = sRow + lane;  // slot s at myRow[s * 33]
+    uint8_t* myTouch = sTouch + lane;
     const Real drop = Real(p.drop);
     Real racc = Real(0);
+    // software pipeline over the incidences: r0/K0 current, r1 next; indices are clamped
+    // to the last incidence so that the loop body has no branches
     ScatterRec r0 = {0u, 0u, 0u, 0u}, r1 = {0u, 0u, 0u, 0u};
     KVec<Real> K0, K1;
     K0.zero();
-    K1.zero();
     if (deg > 0) {
         r0 = p.recs[ib];
         K0.load(tetK + 8 * (int64_t)r0.tet);
+        r1 = p.recs[ib + (deg > 1 ? 1 : 0)];
     }
-    if (deg > 1) r1 = p.recs[ib + 1];
+    const int last = deg - 1;
     for (int k = 0; k < deg; ++k) {
-        ScatterRec r2 = {0u, 0u, 0u, 0u};
-        if (k + 1 < deg) K1.load(tetK + 8 * (int64_t)r1.tet);
-        if (k + 2 < deg) r2 = p.recs[ib + k + 2];
+        K1.load(tetK + 8 * (int64_t)r1.tet);
+        const ScatterRec r2 = p.recs[ib + min(k + 2, last)];
         const int i = r0.meta & 15;
-        if (DIR && isdir) {
-            // applyDir on the row DOF: the element row becomes e_i, F(i) = bc
-            const uint32_t off = rec_off(r0, i);
-            sRow[rot(off, lane)] += Real(1);
-            if (TOUCH) sTouch[rot(off, lane)] = 1;
-        } else {
-            const Real* T = sT + i * Tab::TS;
-            const uint32_t dm = DIR ? (r0.meta >> 4) & 0x3ffu : 0u;
-            Real F = K0.k(6) * sM[i];
-            const Real k0 = K0.k(0), k1 = K0.k(1), k2 = K0.k(2), k3 = K0.k(3), k4 = K0.k(4), k5 = K0.k(5);
-            Real a[NLOC];
-            int addr[NLOC];
-            bool add[NLOC];
+        const Real* T = sT + i * Tab::TS;
+        const uint32_t dm = DIR ? (r0.meta >> 4) & 0x3ffu : 0u;
+        const Real k0 = K0.k(0), k1 = K0.k(1), k2 = K0.k(2), k3 = K0.k(3), k4 = K0.k(4), k5 = K0.k(5);
+        Real F = K0.k(6) * sM[i];
+        Real a[NLOC];
+        int addr[NLOC];
+        uint32_t addbits = 0;
 #pragma unroll
-            for (int j = 0; j < NLOC; ++j) {
-                if (sizeof(Real) == 4) {
-                    const float4 t0 = reinterpret_cast<const float4*>(T + j * 8)[0];
-                    const float4 t1 = reinterpret_cast<const float4*>(T + j * 8)[1];
-                    Real v = k0 * Real(t0.x);
-                    v = fma(k1, Real(t0.y), v);
-                    v = fma(k2, Real(t0.z), v);
-                    v = fma(k3, Real(t0.w), v);
-                    v = fma(k4, Real(t1.x), v);
-                    a[j] = fma(k5, Real(t1.y), v);
-                } else {
-                    const double2 t0 = reinterpret_cast<const double2*>(T + j * 8)[0];
-                    const double2 t1 = reinterpret_cast<const double2*>(T + j * 8)[1];
-                    const double2 t2 = reinterpret_cast<const double2*>(T + j * 8)[2];
-                    Real v = k0 * Real(t0.x);
-                    v = fma(k1, Real(t0.y), v);
-                    v = fma(k2, Real(t1.x), v);
-                    v = fma(k3, Real(t1.y), v);
-                    v = fma(k4, Real(t2.x), v);
-                    a[j] = fma(k5, Real(t2.y), v);
-                }
-                addr[j] = rot((int)rec_off(r0, j), lane);
-                const bool colDir = DIR && ((dm >> j) & 1u);
-                // the drop rule |a| > drop_val (assembler.inl:416-418).  Without a touched map
-                // and with a drop value that rounds to zero in FP32 the rule only skips exact
-                // zeros, which cannot change a sum: that variant is compiled without the test.
-                add[j] = !colDir && (!DROPCHK || fabs(a[j]) > drop);
-                if (BCNZ && colDir)  // applyDir on Dirichlet column j, ascending j (dc_on_dof.h:39-45)
-                    F -= a[j] * Real(p.dir_bc[p.edofs[(int64_t)r0.tet * NLOC + j]]);
+        for (int j = 0; j < NLOC; ++j) {
+            Real v;
+            if (sizeof(Real) == 4) {
+                const float4 t0 = reinterpret_cast<const float4*>(T + j * 8)[0];
+                const float4 t1 = reinterpret_cast<const float4*>(T + j * 8)[1];
+                v = k0 * Real(t0.x);
+                v = fma(k1, Real(t0.y), v);
+                v = fma(k2, Real(t0.z), v);
+                v = fma(k3, Real(t0.w), v);
+                v = fma(k4, Real(t1.x), v);
+                v = fma(k5, Real(t1.y), v);
+            } else {
+                const double2 t0 = reinterpret_cast<const double2*>(T + j * 8)[0];
+                const double2 t1 = reinterpret_cast<const double2*>(T + j * 8)[1];
+                const double2 t2 = reinterpret_cast<const double2*>(T + j * 8)[2];
+                v = k0 * Real(t0.x);
+                v = fma(k1, Real(t0.y), v);
+                v = fma(k2, Real(t1.x), v);
+                v = fma(k3, Real(t1.y), v);
+                v = fma(k4, Real(t2.x), v);
+                v = fma(k5, Real(t2.y), v);
             }
-            // the NLOC slots of one element row are distinct columns: independent updates
-            Real cur[NLOC];
+            const bool colDir = DIR && ((dm >> j) & 1u);
+            if (BCNZ && colDir)  // applyDir on Dirichlet column j, ascending j (dc_on_dof.h:39-45)
+                F -= v * Real(p.dir_bc[p.edofs[(int64_t)r0.tet * NLOC + j]]);
+            // the drop rule |a| > drop_val (assembler.inl:416-418).  Without a touched map and
+            // with a drop value that rounds to zero in FP32 the rule only skips exact zeros,
+            // which cannot change a sum: that variant is compiled without the test.
+            bool add = !colDir && (!DROPCHK || fabs(v) > drop);
+            if (DIR) {  // a Dirichlet row: applyDir makes the element row e_i
+                add = isdir ? (j == i) : add;
+                v = isdir ? Real(1) : v;
+            }
+            a[j] = add ? v : Real(0);
+            if (TOUCH) addbits |= (add ? 1u : 0u) << j;
+            addr[j] = (int)rec_off(r0, j) * 33;
+        }
+        // the NLOC slots of one element row are distinct columns: independent updates
+        Real cur[NLOC];
 #pragma unroll
-            for (int j = 0; j < NLOC; ++j) cur[j] = sRow[addr[j]];
+        for (int j = 0; j < NLOC; ++j) cur[j] = myRow[addr[j]];
+#pragma unroll
+        for (int j = 0; j < NLOC; ++j) myRow[addr[j]] = cur[j] + a[j];
+        if (TOUCH) {
 #pragma unroll
             for (int j = 0; j < NLOC; ++j)
-                if (add[j]) sRow[addr[j]] = cur[j] + a[j];
-            if (TOUCH) {
-#pragma unroll
-                for (int j = 0; j < NLOC; ++j)
-                    if (add[j]) sTouch[addr[j]] = 1;
-            }
-            racc += F;
+                myTouch[addr[j]] |= (uint8_t)((addbits >> j) & 1u);
         }
+        racc += (DIR && isdir) ? Real(0) : F;
         r0 = r1;
         K0 = K1;
         r1 = r2;
@@ -402,13 +409,13 @@ __global__ void __launch_bounds__(64) row_gather_kernel(RowParams p, const Real*
     const int64_t rem_rows = p.nrows - row0;
     const int nrow = rem_rows < 32 ? (int)rem_rows : 32;
     for (int w = 0; w < nrow; ++w) {
-        const int64_t rbw = __shfl_sync(0xffffffffu, rb, w);
-        const int lenw = __shfl_sync(0xffffffffu, len, w);
-        for (int s = lane; s < lenw; s += 32) {
-            const Real v = sRow[rot(s, w)];
+        const longlong2 m = sMeta[w];
+        const Real* src = sRow + w;
+        for (int s = lane; s < (int)m.y; s += 32) {
+            const Real v = src[s * 33];
             bad |= !isfinite(v);
-            vals[rbw + s] = v;
-            if (TOUCH) touched_out[rbw + s] = sTouch[rot(s, w)];
+            vals[m.x + s] = v;
+            if (TOUCH) touched_out[m.x + s] = sTouch[s * 33 + w];
         }
     }
     if (bad) atomicExch(status, ANIGPU_ERR_NONFINITE);
@@ -492,8 +499,9 @@ static int launch_rows_t(anigpu_ctx* h, const RowParams& p, const void* tables, 
                          uint8_t* touched, cudaStream_t st) {
     const int warps = 2;
     const size_t tab_bytes = ((sizeof(Real) * RowTab<Real, NLOC>::SIZE + 15) / 16) * 16;
-    const size_t warp_bytes = (((size_t)p.cap * 33 * (sizeof(Real) + (TOUCH ? 1 : 0))) + 15) / 16 * 16;
-    const size_t smem = tab_bytes + warp_bytes * warps;
+    const size_t row_bytes = (((size_t)p.cap * 33 * sizeof(Real)) + 15) / 16 * 16;
+    const size_t touch_bytes = TOUCH ? (((size_t)p.cap * 33) + 15) / 16 * 16 : 0;
+    const size_t smem = tab_bytes + (32 * 16 + row_bytes + touch_bytes) * warps;
     auto kern = row_gather_kernel<Real, NLOC, DIR, BCNZ, TOUCH, DROPCHK>;
     ANI_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     kern<<<grid_for(p.nrows - p.row_begin, 32 * warps), 32 * warps, smem, st>>>(
