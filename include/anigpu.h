@@ -153,6 +153,22 @@ int anigpu_set_dirichlet(anigpu_handle h, const uint8_t* mask, const double* bc)
 #define ANIGPU_TENSOR_LAME 7
 int anigpu_assemble(anigpu_handle h, int tensor_kind, const double* D, const double* f, double f_const, int order,
                     int precision, void* vals, double* rhs, uint8_t* touched, double drop_val);
+/* Allocation-free variant of anigpu_assemble (this entry point has no counterpart in the
+ * reference).  For callers that cannot allocate device memory when they assemble: code whose
+ * device memory is held by another allocator (a framework's caching allocator, for example)
+ * and latency-critical loops that cannot afford cudaMalloc's implicit device-wide
+ * synchronisation.  Same arguments and results as anigpu_assemble without the touched map.
+ * It calls no cudaMalloc, cudaFree or other allocating routine: its scratch (the per-tet
+ * blocks and the reference tables) is a fixed 16 MiB device array inside the library, which
+ * every GPU that loads the library holds until the process exits.  Limit: 524,288 tets in
+ * F32, 262,144 in F64; larger meshes are rejected with ANIGPU_ERR_ARG and a message.  The
+ * handle must already be set up (anigpu_problem_setup and anigpu_set_dirichlet allocate).
+ * The first call on a device looks up the array's device address (cudaGetSymbolAddress) and
+ * should come before any stream capture.  All calls share the one array: calls that overlap
+ * on the GPU (other handles, other streams) race and must be serialised by the caller. */
+int anigpu_assemble_noalloc(anigpu_handle h, int tensor_kind, const double* D, const double* f, double f_const,
+                            int order, int precision, void* vals, double* rhs, double drop_val);
+
 /* the drop-rule pattern (assembler without template): keep touched slots and the diagonal
  * (set_elements_on_matrix_diagonal, assembler.inl:114-135).  In-place on rowptr/col/vals;
  * returns the new nnz through nnz_out. */

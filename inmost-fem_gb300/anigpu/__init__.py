@@ -59,6 +59,7 @@ SIGNATURES = {
     "anigpu_dof_coords": (_i, [_vp, _vp]),
     "anigpu_set_dirichlet": (_i, [_vp, _vp, _vp]),
     "anigpu_assemble": (_i, [_vp, _i, _vp, _vp, _d, _i, _i, _vp, _vp, _vp, _d]),
+    "anigpu_assemble_noalloc": (_i, [_vp, _i, _vp, _vp, _d, _i, _i, _vp, _vp, _d]),
     "anigpu_csr_compact": (_i, [_vp, _vp, _vp, _vp, _i, _vp, ctypes.POINTER(_i64)]),
     "anigpu_solve": (_i, [_vp, _i, _vp, _i, _vp, _vp, _d, _i64, ctypes.POINTER(SolveStats)]),
     "anigpu_spmv": (_i, [_vp, _vp, _i, _vp, _vp]),

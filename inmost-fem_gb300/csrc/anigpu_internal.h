@@ -21,6 +21,7 @@ struct ScalarBasisTable {
     std::vector<double> grad;       // grad[(n*nf + i)*3 + d]  d/dxi_d of phi_i
 };
 bool make_scalar_basis(int space, int order, ScalarBasisTable* t);
+int eval_scalar_basis_at(int space, const double* l, double* val, double (*grad)[3]);
 int scalar_space_nf(int space);
 // op code helpers (code = 10*space + op)
 bool op_info(int code, int* nf, int* dim, int* base_space, int* ncomp, int* op);

@@ -124,3 +124,9 @@ bool make_scalar_basis(int space, int order, ScalarBasisTable* t) {
     }
     return true;
 }
+
+// Basis values and reference gradients at one barycentric point, without any allocation
+// (for callers that must not allocate).  Returns the number of basis functions or -1.
+int eval_scalar_basis_at(int space, const double* l, double* val, double (*grad)[3]) {
+    return eval_space(space, l, val, grad);
+}

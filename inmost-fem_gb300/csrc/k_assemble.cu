@@ -16,7 +16,10 @@
 // computes A(i, j)) and adds it into a shared-memory copy of the row at the offsets held
 // by the scatter record.  Each value is therefore summed in the same order as the
 // reference's serial cell loop, without atomics, and written to HBM once, coalesced.
+#include <mutex>
+
 #include "anigpu_internal.h"
+#include "quad_tables.h"
 
 namespace {
 
@@ -644,5 +647,185 @@ int run_compact(anigpu_ctx* h, int64_t* rowptr, int32_t* col, void* vals, int pr
     ANI_CUDA(h, cudaFreeAsync(nvals, s));
     ANI_CUDA(h, cudaStreamSynchronize(s));
     (void)nnz_old;
+    return ANIGPU_OK;
+}
+
+// ---------------------------------------------------------------- allocation-free assembly
+// anigpu_assemble_noalloc: the same two kernels as anigpu_assemble, with their scratch (the
+// per-tet K blocks and the reference-element tables) in a fixed device array that the
+// library owns for its lifetime instead of memory from cudaMalloc.  It exists for callers
+// that cannot allocate device memory at the moment they assemble: code whose device memory
+// is fully reserved by another allocator (for example a framework's caching allocator), and
+// latency-critical loops where cudaMalloc's implicit device-wide synchronisation is not
+// acceptable.  The array is a file-scope __device__ variable, so every GPU that loads the
+// library holds it (kNoallocScratchBytes) until the process exits.
+namespace {
+constexpr size_t kNoallocTableBytes = 16u << 10;  // reference tables, at the start
+constexpr size_t kNoallocScratchBytes = 16u << 20;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
+constexpr int kNoallocMaxDevices = 64;
+void* g_noalloc_dev_ptr[kNoallocMaxDevices] = {};
+std::mutex g_noalloc_mu;
+
+// host address of the array is only a stand-in: the device address comes from
+// cudaGetSymbolAddress, once per device, with that device current
+int noalloc_scratch(anigpu_ctx* h, unsigned char** out) {
+    int dev = -1;
+    ANI_CUDA(h, cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoallocMaxDevices) return set_err(h, ANIGPU_ERR_UNSUPPORTED, "device index above 63");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_dev_ptr[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) return cuda_check(h, e != cudaSuccess ? e : cudaErrorInvalidSymbol, "cudaGetSymbolAddress");
+        g_noalloc_dev_ptr[dev] = p;
+    }
+    *out = static_cast<unsigned char*>(g_noalloc_dev_ptr[dev]);
+    return ANIGPU_OK;
+}
+
+// Tsym[i][j][8] and m[i] for (space, order), computed into caller storage (no allocation)
+bool noalloc_tables(int space, int order, double* T, int* nf_out) {
+    const double *pp, *ww;
+    int q;
+    if (!anigpu_quad_rule(order, &pp, &ww, &q)) return false;
+    double val[ANIGPU_MAX_Q][20], grad[ANIGPU_MAX_Q][20][3];
+    int nf = -1;
+    for (int n = 0; n < q; ++n) nf = eval_scalar_basis_at(space, pp + 4 * n, val[n], grad[n]);
+    if (nf != 4 && nf != 10) return false;
+    const int A[6] = {0, 1, 2, 0, 0, 1}, B[6] = {0, 1, 2, 1, 2, 2};
+    for (int i = 0; i < nf; ++i)
+        for (int j = 0; j < nf; ++j)
+            for (int k = 0; k < 8; ++k) {
+                double s = 0;
+                if (k < 6)
+                    for (int n = 0; n < q; ++n) {
+                        double v = grad[n][i][A[k]] * grad[n][j][B[k]];
+                        if (A[k] != B[k]) v += grad[n][i][B[k]] * grad[n][j][A[k]];
+                        s += ww[n] * v;
+                    }
+                T[((size_t)i * nf + j) * 8 + k] = s;
+            }
+    for (int i = 0; i < nf; ++i) {
+        double s = 0;
+        for (int n = 0; n < q; ++n) s += ww[n] * val[n][i];
+        T[(size_t)nf * nf * 8 + i] = s;
+    }
+    *nf_out = nf;
+    return true;
+}
+
+template <typename Real, int NLOC, bool DIR, bool BCNZ, bool DROPCHK>
+int noalloc_rows(anigpu_ctx* h, const RowParams& p, const Real* tables, const Real* tetK, Real* vals, double* rhs) {
+    const int warps = 2;
+    const size_t tab_bytes = ((sizeof(Real) * RowTab<Real, NLOC>::SIZE + 15) / 16) * 16;
+    const size_t row_bytes = (((size_t)p.cap * 33 * sizeof(Real)) + 15) / 16 * 16;
+    const size_t smem = tab_bytes + (32 * 16 + row_bytes) * warps;
+    auto kern = row_gather_kernel<Real, NLOC, DIR, BCNZ, false, DROPCHK>;
+    ANI_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<grid_for(p.nrows - p.row_begin, 32 * warps), 32 * warps, smem, h->stream>>>(p, tables, tetK, vals, rhs,
+                                                                                        nullptr, h->d_status);
+    ANI_LAUNCHED(h);
+    return ANIGPU_OK;
+}
+
+template <typename Real, int NLOC>
+int noalloc_rows_dispatch(anigpu_ctx* h, const RowParams& p, const Real* tables, const Real* tetK, Real* vals,
+                          double* rhs) {
+    const bool dir = h->has_dirichlet, bcnz = h->bc_nonzero;
+    const bool dchk = sizeof(Real) == 8 || (float)p.drop != 0.0f;
+#define NR(D, B, C) return noalloc_rows<Real, NLOC, D, B, C>(h, p, tables, tetK, vals, rhs)
+    if (dchk) {
+        if (!dir) NR(false, false, true);
+        if (bcnz) NR(true, true, true);
+        NR(true, false, true);
+    }
+    if (!dir) NR(false, false, false);
+    if (bcnz) NR(true, true, false);
+    NR(true, false, false);
+#undef NR
+}
+}  // namespace
+
+extern "C" int anigpu_assemble_noalloc(anigpu_handle h, int tensor_kind, const double* D, const double* f,
+                                       double f_const, int order, int precision, void* vals, double* rhs,
+                                       double drop_val) {
+    if (!h) return ANIGPU_ERR_ARG;
+    (void)cudaGetLastError();
+    cudaSetDevice(h->device);
+    if (h->space < 0) return set_err(h, ANIGPU_ERR_STATE, "anigpu_problem_setup not called");
+    if (h->space == ANIGPU_VEC3_P2) return set_err(h, ANIGPU_ERR_UNSUPPORTED, "vector assembly not built yet");
+    if (tensor_kind != ANIGPU_TENSOR_NULL && tensor_kind != ANIGPU_TENSOR_CONST_SCALAR &&
+        tensor_kind != ANIGPU_TENSOR_TET_SCALAR && tensor_kind != ANIGPU_TENSOR_TET_SYM)
+        return set_err(h, ANIGPU_ERR_UNSUPPORTED, "assembly tensor kind must be NULL, CONST_SCALAR, TET_SCALAR or TET_SYM");
+    if (tensor_kind != ANIGPU_TENSOR_NULL && !D) return set_err(h, ANIGPU_ERR_ARG, "tensor data is NULL");
+    if (!vals || !rhs) return set_err(h, ANIGPU_ERR_ARG, "NULL output");
+    if (precision != ANIGPU_F32 && precision != ANIGPU_F64) return set_err(h, ANIGPU_ERR_ARG, "precision");
+    const size_t rsz = precision == ANIGPU_F32 ? 4 : 8;
+    const size_t need = (size_t)h->nt * 8 * rsz;
+    if (need > kNoallocScratchBytes - kNoallocTableBytes)
+        return set_err(h, ANIGPU_ERR_ARG,
+                       "anigpu_assemble_noalloc: mesh too large for the fixed scratch (" +
+                           std::to_string(h->nt) + " tets need " + std::to_string(need) + " bytes, limit " +
+                           std::to_string(kNoallocScratchBytes - kNoallocTableBytes) +
+                           " bytes: 524288 tets in FP32, 262144 in FP64)");
+    unsigned char* scratch = nullptr;
+    int rc = noalloc_scratch(h, &scratch);
+    if (rc) return rc;
+    // reference tables: computed on the host into fixed storage, copied to the array's head
+    double T64[10 * 10 * 8 + 10];
+    int nf = 0;
+    if (!noalloc_tables(h->space, order, T64, &nf) || nf != h->nloc_s)
+        return set_err(h, ANIGPU_ERR_UNSUPPORTED, "unsupported space/order");
+    const size_t ntab = (size_t)nf * nf * 8 + nf;
+    static thread_local float T32[10 * 10 * 8 + 10];
+    static thread_local double T64s[10 * 10 * 8 + 10];
+    if (precision == ANIGPU_F32) {
+        for (size_t k = 0; k < ntab; ++k) T32[k] = (float)T64[k];
+        ANI_CUDA(h, cudaMemcpyAsync(scratch, T32, ntab * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+    } else {
+        for (size_t k = 0; k < ntab; ++k) T64s[k] = T64[k];
+        ANI_CUDA(h, cudaMemcpyAsync(scratch, T64s, ntab * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    }
+    void* tetK = scratch + kNoallocTableBytes;
+    if (precision == ANIGPU_F32)
+        tet_prepare_f32_kernel<<<grid_for(h->nt, 256), 256, 0, h->stream>>>(
+            h->nt, h->xyz, h->xyz2, h->tets, tensor_kind, D, f, f_const, (float*)tetK, h->d_status);
+    else
+        tet_prepare_f64_kernel<<<grid_for(h->nt, 256), 256, 0, h->stream>>>(
+            h->nt, h->xyz, h->tets, tensor_kind, D, f, f_const, (double*)tetK, h->d_status);
+    ANI_LAUNCHED(h);
+    RowParams p;
+    p.inc_ptr = h->inc_ptr;
+    p.recs = h->recs;
+    p.rowptr = h->rowptr_s;
+    p.dir_mask = h->dir_mask;
+    p.dir_bc = h->dir_bc;
+    p.edofs = h->edofs;
+    p.drop = drop_val;
+    for (int rg = 0; rg < 2; ++rg) {
+        p.row_begin = h->row_range[rg];
+        p.nrows = h->row_range[rg + 1];
+        p.cap = h->row_range_cap[rg];
+        if (p.nrows <= p.row_begin) continue;
+        if (h->nloc_s == 10)
+            rc = precision == ANIGPU_F32
+                     ? noalloc_rows_dispatch<float, 10>(h, p, (const float*)scratch, (const float*)tetK, (float*)vals, rhs)
+                     : noalloc_rows_dispatch<double, 10>(h, p, (const double*)scratch, (const double*)tetK,
+                                                         (double*)vals, rhs);
+        else
+            rc = precision == ANIGPU_F32
+                     ? noalloc_rows_dispatch<float, 4>(h, p, (const float*)scratch, (const float*)tetK, (float*)vals, rhs)
+                     : noalloc_rows_dispatch<double, 4>(h, p, (const double*)scratch, (const double*)tetK,
+                                                        (double*)vals, rhs);
+        if (rc) return rc;
+    }
+    int st = 0;
+    ANI_CUDA(h, cudaMemcpyAsync(&st, h->d_status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    ANI_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (st) {
+        ANI_CUDA(h, cudaMemsetAsync(h->d_status, 0, sizeof(int), h->stream));
+        return set_err(h, st, "non-finite value in assembly (AssemblerT status -1)");
+    }
     return ANIGPU_OK;
 }
