@@ -58,9 +58,10 @@ extern "C" {
 #define ANIGPU_TENSOR_TET_GENERAL 4
 #define ANIGPU_TENSOR_POINT 5
 
-/* ---- arithmetic of element matrices / CSR values */
+/* ---- arithmetic of element matrices / CSR values (BF16: learned-preconditioner activations) */
 #define ANIGPU_F64 0
 #define ANIGPU_F32 1
+#define ANIGPU_BF16 2
 
 /* ---- Krylov methods (replacing INMOST Solver, examples/tutorials/ex1.cpp:161-163) */
 #define ANIGPU_SOLVE_JACOBI_PCG 0 /* FP64 Jacobi-preconditioned CG */
@@ -180,6 +181,36 @@ int anigpu_csr_compact(anigpu_handle h, int64_t* rowptr, int32_t* col, void* val
  * and the result).  Convergence: ||b - A x||_2 <= rtol * ||b||_2 in FP64. */
 int anigpu_solve(anigpu_handle h, int method, const void* vals, int precision, const double* b, double* x,
                  double rtol, int64_t maxit, anigpu_solve_stats* stats);
+/* ---- learned preconditioner for ANIGPU_SOLVE_FCG_LEARNED (no counterpart in the reference,
+ * whose solves go through INMOST's ILU-Krylov, examples/tutorials/ex1.cpp:161-163).
+ *   M r = D^-1 r + P Dc^-1/2 B B^T Dc^-1/2 P^T r,   B = sum_{k<4} diag(a_k) A_hat^k
+ *   (symmetric positive definite by construction).  P interpolates vertex values onto the P2
+ *   DOFs, Dc = the vertex diagonal, A_hat = -Dc^-1/2 A_vv' Dc^-1/2 over the vertex-vertex
+ *   couplings.  The per-vertex coefficients a (4 per vertex) come from a message-passing
+ *   network on that vertex graph, run once per bind on static features (log A_vv and the
+ *   local mean of log(trace D / 3)).  Hidden width 64, `layers` residual layers, activations
+ *   in act_precision (ANIGPU_BF16, or ANIGPU_F32 for gradient checks), FP32 accumulation,
+ *   FP32 master parameters.
+ * init: random parameters (seeded; the untrained B is the identity); get/set_params: the flat
+ *   FP32 parameter vector (checkpoint); bind: the system the preconditioner serves (values of
+ *   a P2 problem, and the per-tet tensor for the features), runs the network;
+ * apply: z = M r (f64 vectors); apply_f32: z = M r with the fused FP32 kernels the solver
+ *   uses (f32[ndof] vectors); coefficients: a as f32[nv][4] into a device buffer;
+ * loss_grad: L = (M r - e)^T A (M r - e) / (e^T A e) for a pair (r, e = A^-1 r), gradients
+ *   accumulated; adam: one Adam step on the accumulated gradients (then zeroed), network re-run. */
+int anigpu_gnn_init(anigpu_handle h, int layers, int act_precision, uint64_t seed);
+int64_t anigpu_gnn_num_params(anigpu_handle h);
+int anigpu_gnn_get_params(anigpu_handle h, float* host, int64_t n);
+int anigpu_gnn_set_params(anigpu_handle h, const float* host, int64_t n);
+int anigpu_gnn_get_grads(anigpu_handle h, float* host, int64_t n);
+int anigpu_gnn_zero_grads(anigpu_handle h);
+int anigpu_gnn_bind(anigpu_handle h, const void* vals, int precision, int tensor_kind, const double* D);
+int anigpu_gnn_apply(anigpu_handle h, const double* r, double* z);
+int anigpu_gnn_apply_f32(anigpu_handle h, const float* r, float* z);
+int anigpu_gnn_coefficients(anigpu_handle h, float* coef);
+int anigpu_gnn_loss_grad(anigpu_handle h, const double* r, const double* e, double* loss_host);
+int anigpu_gnn_adam(anigpu_handle h, float lr, float beta1, float beta2, float eps, int step, float grad_scale);
+
 /* y = A x on the handle's template (F64 or F32 values, f64 vectors) */
 int anigpu_spmv(anigpu_handle h, const void* vals, int precision, const double* x, double* y);
 

@@ -25,7 +25,7 @@ P0, P1, P2, P3, VEC3_P1, VEC3_P2 = 0, 1, 2, 3, 4, 5
 IDEN, GRAD = 1, 2
 TENSOR_NULL, TENSOR_CONST_SCALAR, TENSOR_TET_SCALAR, TENSOR_TET_SYM, TENSOR_TET_GENERAL, TENSOR_POINT = range(6)
 TENSOR_LAME = 7
-F64, F32 = 0, 1
+F64, F32, BF16 = 0, 1, 2
 SOLVE_JACOBI_PCG, SOLVE_IR_CG32, SOLVE_FCG_LEARNED = 0, 1, 2
 
 # every entry point the header declares: name -> (restype, argtypes)
@@ -63,6 +63,19 @@ SIGNATURES = {
     "anigpu_csr_compact": (_i, [_vp, _vp, _vp, _vp, _i, _vp, ctypes.POINTER(_i64)]),
     "anigpu_solve": (_i, [_vp, _i, _vp, _i, _vp, _vp, _d, _i64, ctypes.POINTER(SolveStats)]),
     "anigpu_spmv": (_i, [_vp, _vp, _i, _vp, _vp]),
+    "anigpu_gnn_init": (_i, [_vp, _i, _i, ctypes.c_uint64]),
+    "anigpu_gnn_num_params": (_i64, [_vp]),
+    "anigpu_gnn_get_params": (_i, [_vp, _vp, _i64]),
+    "anigpu_gnn_set_params": (_i, [_vp, _vp, _i64]),
+    "anigpu_gnn_get_grads": (_i, [_vp, _vp, _i64]),
+    "anigpu_gnn_zero_grads": (_i, [_vp]),
+    "anigpu_gnn_bind": (_i, [_vp, _vp, _i, _i, _vp]),
+    "anigpu_gnn_apply": (_i, [_vp, _vp, _vp]),
+    "anigpu_gnn_apply_f32": (_i, [_vp, _vp, _vp]),
+    "anigpu_gnn_coefficients": (_i, [_vp, _vp]),
+    "anigpu_gnn_loss_grad": (_i, [_vp, _vp, _vp, ctypes.POINTER(_d)]),
+    "anigpu_gnn_adam": (_i, [_vp, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, _i,
+                             ctypes.c_float]),
 }
 
 _LIB = None
@@ -346,3 +359,80 @@ class Anigpu:
         if check:
             self._check(rc)
         return x, st
+
+
+class LearnedPreconditioner:
+    """Training and use of the learned preconditioner of ANIGPU_SOLVE_FCG_LEARNED on a handle.
+
+    Mirrors nothing in the reference (its solves go through INMOST's ILU-Krylov); see
+    include/anigpu.h for the network.  Parameters are a flat FP32 vector (checkpoint: save with
+    get_params, restore with set_params)."""
+
+    def __init__(self, lib, layers=4, act=BF16, seed=1234):
+        self.lib = lib
+        lib._check(lib.lib.anigpu_gnn_init(lib.h, layers, act, seed))
+        self.nparam = int(lib.lib.anigpu_gnn_num_params(lib.h))
+        self.step = 0
+
+    def get_params(self):
+        import numpy as np
+        w = np.zeros(self.nparam, dtype=np.float32)
+        self.lib._check(self.lib.lib.anigpu_gnn_get_params(self.lib.h, w.ctypes.data, self.nparam))
+        return w
+
+    def set_params(self, w):
+        import numpy as np
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        self.lib._check(self.lib.lib.anigpu_gnn_set_params(self.lib.h, w.ctypes.data, self.nparam))
+
+    def get_grads(self):
+        import numpy as np
+        g = np.zeros(self.nparam, dtype=np.float32)
+        self.lib._check(self.lib.lib.anigpu_gnn_get_grads(self.lib.h, g.ctypes.data, self.nparam))
+        return g
+
+    def zero_grads(self):
+        self.lib._check(self.lib.lib.anigpu_gnn_zero_grads(self.lib.h))
+
+    def bind(self, vals, precision, kind, D):
+        with self.lib.on_stream():
+            Dd = self.lib._dev(D, self.lib.torch.float64) if D is not None else None
+            self._D = Dd
+            self._vals = vals
+            self.lib._check(self.lib.lib.anigpu_gnn_bind(self.lib.h, _ptr(vals), precision, kind, _ptr(Dd)))
+
+    def apply(self, r):
+        with self.lib.on_stream():
+            r = self.lib._dev(r, self.lib.torch.float64)
+            z = self.lib.torch.empty_like(r)
+            self.lib._check(self.lib.lib.anigpu_gnn_apply(self.lib.h, _ptr(r), _ptr(z)))
+        return z
+
+    def apply_f32(self, r):
+        """z = M r with the fused FP32 kernels the FCG solve runs."""
+        with self.lib.on_stream():
+            r = self.lib._dev(r, self.lib.torch.float32)
+            z = self.lib.torch.empty_like(r)
+            self.lib._check(self.lib.lib.anigpu_gnn_apply_f32(self.lib.h, _ptr(r), _ptr(z)))
+        return z
+
+    def coefficients(self):
+        """The network output a, float32 [nv, 4]."""
+        torch = self.lib.torch
+        with self.lib.on_stream():
+            a = torch.empty((self.lib.nv, 4), dtype=torch.float32, device=f"cuda:{self.lib.device}")
+            self.lib._check(self.lib.lib.anigpu_gnn_coefficients(self.lib.h, _ptr(a)))
+        return a
+
+    def loss_grad(self, r, e):
+        loss = ctypes.c_double()
+        with self.lib.on_stream():
+            r = self.lib._dev(r, self.lib.torch.float64)
+            e = self.lib._dev(e, self.lib.torch.float64)
+            self.lib._check(self.lib.lib.anigpu_gnn_loss_grad(self.lib.h, _ptr(r), _ptr(e), ctypes.byref(loss)))
+        return loss.value
+
+    def adam(self, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8, grad_scale=1.0):
+        self.step += 1
+        with self.lib.on_stream():
+            self.lib._check(self.lib.lib.anigpu_gnn_adam(self.lib.h, lr, b1, b2, eps, self.step, grad_scale))

@@ -1,0 +1,69 @@
+"""Training of the learned preconditioner of ANIGPU_SOLVE_FCG_LEARNED on the GPU.
+
+Everything runs through the library: the network forward pass (at bind), the hand-written
+backward kernels (loss_grad) and Adam.  A training example is a pair (r, e = A^-1 r); the
+residuals are those of the early iterates of a Jacobi-CG solve, where a preconditioner has to
+act on smooth, slowly converging error, plus the right-hand side itself.
+"""
+import os
+
+import numpy as np
+
+import anigpu
+
+WEIGHTS_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights")
+DEFAULT_WEIGHTS = os.path.join(WEIGHTS_DIR, "p2_aniso_l4.npy")
+
+
+def training_pairs(lib, vals, b, ks=(0, 1, 2, 4, 8, 16, 32, 64, 128), rtol=1e-10):
+    """Pairs (r_k, x* - x_k) for Jacobi-PCG iterates x_k of A x = b (FP32 values)."""
+    torch = lib.torch
+    b = lib._dev(b, torch.float64)
+    xs, _ = lib.solve(vals, b, anigpu.SOLVE_IR_CG32, anigpu.F32, rtol=rtol, maxit=1_000_000)
+    pairs = []
+    for k in ks:
+        if k == 0:
+            xk = torch.zeros_like(b)
+        else:
+            xk, _ = lib.solve(vals, b, anigpu.SOLVE_JACOBI_PCG, anigpu.F32, rtol=1e-30, maxit=k, check=False)
+        rk = b - lib.spmv(vals, xk, anigpu.F32)
+        pairs.append((rk.clone(), (xs - xk).clone()))
+    return pairs
+
+
+def train(prec, systems, steps, lr=2e-3, lr_final=5e-4, batch=4, seed=0, log_every=0, log=print):
+    """Adam on the relative energy-norm error.  systems: list of (vals, kind, D, pairs).
+    Returns the per-step mean losses."""
+    rng = np.random.default_rng(seed)
+    hist = []
+    for step in range(steps):
+        vals, kind, D, pairs = systems[step % len(systems)]
+        prec.bind(vals, anigpu.F32, kind, D)
+        prec.zero_grads()
+        idx = rng.choice(len(pairs), min(batch, len(pairs)), replace=False)
+        loss = sum(prec.loss_grad(*pairs[i]) for i in idx) / len(idx)
+        prec.adam(lr=lr if step < 0.7 * steps else lr_final, grad_scale=1.0 / len(idx))
+        hist.append(loss)
+        if log_every and (step % log_every == 0 or step == steps - 1):
+            log(f"step {step} loss {np.mean(hist[-log_every:]):.4f}")
+    return hist
+
+
+def mean_loss(prec, systems):
+    """Mean loss over every pair of every system (no gradient step)."""
+    tot, cnt = 0.0, 0
+    for vals, kind, D, pairs in systems:
+        prec.bind(vals, anigpu.F32, kind, D)
+        for r, e in pairs:
+            prec.zero_grads()
+            tot += prec.loss_grad(r, e)
+            cnt += 1
+    prec.zero_grads()
+    return tot / max(cnt, 1)
+
+
+def load_default(prec):
+    """Set the committed trained parameters (P2, anisotropic tensors, 4 layers)."""
+    w = np.load(DEFAULT_WEIGHTS)
+    prec.set_params(w)
+    return w

@@ -91,6 +91,7 @@ struct anigpu_ctx {
     void* solve_ws = nullptr;
     size_t solve_ws_bytes = 0;
     void* learned = nullptr;       // learned preconditioner state
+    void* fcg_ws = nullptr;        // flexible-CG workspace and its captured graphs
 
     // per-phase timing (anigpu_set_timing)
     bool timing = false;

@@ -62,6 +62,7 @@ int anigpu_destroy(anigpu_handle h) {
     cudaSetDevice(h->device);
     cudaStreamSynchronize(h->stream);
     free_solver(h);
+    free_fcg(h);
     free_learned(h);
     void* ptrs[] = {h->xyz, h->xyz2, h->tets, h->tet_edges, h->edofs, h->inc_ptr, h->recs, h->dir_mask, h->dir_bc,
                     h->tetdata, h->d_status, h->d_ref_tables};
@@ -149,6 +150,7 @@ int anigpu_mesh_upload(anigpu_handle h, int64_t nv, const double* xyz, int64_t n
     if (nv >= (int64_t)INT32_MAX || nt >= ((int64_t)1 << 27))
         return set_err(h, ANIGPU_ERR_UNSUPPORTED, "mesh too large for 32-bit vertex / 27-bit tet ids");
     cudaSetDevice(h->device);
+    learned_invalidate(h);  // bindings and captured solver graphs refer to the old mesh
     int rc = dev_alloc(h, &h->xyz, (size_t)nv * 3);
     if (rc) return rc;
     rc = dev_alloc(h, &h->tets, (size_t)nt * 4);
@@ -178,6 +180,7 @@ int anigpu_mesh_update_coords(anigpu_handle h, const double* xyz) {
 int anigpu_problem_setup(anigpu_handle h, int space) {
     CHECK_H(h);
     cudaSetDevice(h->device);
+    learned_invalidate(h);
     return setup_problem(h, space);
 }
 
@@ -271,6 +274,73 @@ int anigpu_spmv(anigpu_handle h, const void* vals, int precision, const double* 
     CHECK_H(h);
     cudaSetDevice(h->device);
     return run_spmv(h, vals, precision, x, y);
+}
+
+}  // extern "C"
+
+extern "C" {
+
+int anigpu_gnn_init(anigpu_handle h, int layers, int act_precision, uint64_t seed) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    return gnn_init(h, layers, act_precision, seed);
+}
+int64_t anigpu_gnn_num_params(anigpu_handle h) { return h ? gnn_num_params(h) : -1; }
+int anigpu_gnn_get_params(anigpu_handle h, float* host, int64_t n) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    return gnn_params(h, host, n, 0, 0);
+}
+int anigpu_gnn_set_params(anigpu_handle h, const float* host, int64_t n) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    return gnn_params(h, const_cast<float*>(host), n, 1, 0);
+}
+int anigpu_gnn_get_grads(anigpu_handle h, float* host, int64_t n) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    return gnn_params(h, host, n, 0, 1);
+}
+int anigpu_gnn_zero_grads(anigpu_handle h) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    return gnn_zero_grads(h);
+}
+int anigpu_gnn_bind(anigpu_handle h, const void* vals, int precision, int tensor_kind, const double* D) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    return gnn_bind(h, vals, precision, tensor_kind, D);
+}
+int anigpu_gnn_apply(anigpu_handle h, const double* r, double* z) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    int rc = gnn_apply(h, r, z);
+    if (rc) return rc;
+    ANI_CUDA(h, cudaStreamSynchronize(h->stream));
+    return ANIGPU_OK;
+}
+int anigpu_gnn_apply_f32(anigpu_handle h, const float* r, float* z) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    int rc = gnn_apply_f32(h, r, z);
+    if (rc) return rc;
+    ANI_CUDA(h, cudaStreamSynchronize(h->stream));
+    return ANIGPU_OK;
+}
+int anigpu_gnn_coefficients(anigpu_handle h, float* coef) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    return gnn_coefficients(h, coef);
+}
+int anigpu_gnn_loss_grad(anigpu_handle h, const double* r, const double* e, double* loss_host) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    return gnn_loss_grad(h, r, e, loss_host);
+}
+int anigpu_gnn_adam(anigpu_handle h, float lr, float beta1, float beta2, float eps, int step, float grad_scale) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    return gnn_adam(h, lr, beta1, beta2, eps, step, grad_scale);
 }
 
 }  // extern "C"

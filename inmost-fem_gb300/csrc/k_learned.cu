@@ -1,7 +1,1175 @@
-// Learned preconditioner for flexible CG: placeholder until the network kernels land.
+// Learned preconditioner for flexible CG (a new component: the reference has no learned
+// part; its solver is INMOST's ILU-Krylov, examples/tutorials/ex1.cpp:161-163).
+//
+// Preconditioner (additive two-level, symmetric positive definite by construction):
+//     M r = D^-1 r + P Dc^-1/2 B B^T Dc^-1/2 P^T r,      B = sum_{k<K} diag(a_k) A_hat^k
+// P interpolates vertex values onto the P2 DOFs (vertex DOF = its vertex, edge DOF = mean of
+// the two end vertices); P^T is its transpose.  A_hat_vw = -A_vw / sqrt(A_vv A_ww) over the
+// vertex-vertex entries of the P2 matrix (no self loop), Dc = diag(A_vv).  The per-vertex
+// coefficients a_k come from a message-passing network run once per system:
+//     h0 = relu(F W0 + b0)                     F: log A_vv, mean log(trace D / 3) (centred)
+//     h_l = h_{l-1} + relu((A_hat h_{l-1}) W_l + b_l),  l = 1..L
+//     a = h_L W_out + b_out                      (K outputs per vertex)
+// Activations and the weights the kernels use are BF16 (FP32 for gradient checks); every
+// accumulation is FP32.  Training minimises the relative energy-norm error against pairs
+// (r, e = A^-1 r):   L = (M r - e)^T A (M r - e) / (e^T A e), with hand-written backward
+// kernels (through the polynomial and the network) and Adam.  Every reduction is two-stage
+// with a fixed order, so runs reproduce bit for bit.
+#include <cuda_bf16.h>
+
+#include <atomic>
+#include <cmath>
+#include <vector>
+
 #include "learned.h"
 
-int run_fcg_learned(anigpu_ctx* h, const void*, int, const double*, double*, double, int64_t, anigpu_solve_stats*) {
-    return set_err(h, ANIGPU_ERR_UNSUPPORTED, "learned preconditioner not loaded");
+namespace {
+
+constexpr int C = 64;           // hidden channels
+constexpr int K = 4;            // polynomial terms of B (A_hat^0 .. A_hat^3)
+constexpr int NF = 2;           // input features
+constexpr int kMaxLayers = 8;
+constexpr int kBlk = 256;
+constexpr int kMaxPart = 1024;  // block partials of reductions
+
+template <typename A>
+__device__ __forceinline__ float ld(const A* p) {
+    return (float)*p;
 }
-void free_learned(anigpu_ctx*) {}
+template <>
+__device__ __forceinline__ float ld<__nv_bfloat16>(const __nv_bfloat16* p) {
+    return __bfloat162float(*p);
+}
+template <typename A>
+__device__ __forceinline__ A cvt(float v) {
+    return (A)v;
+}
+template <>
+__device__ __forceinline__ __nv_bfloat16 cvt<__nv_bfloat16>(float v) {
+    return __float2bfloat16_rn(v);
+}
+
+struct Gnn {
+    int layers = 4, act = ANIGPU_BF16;  // act: ANIGPU_F32 or ANIGPU_BF16
+    int64_t nparam = 0;
+    float* w = nullptr;      // FP32 master parameters
+    float* g = nullptr;      // FP32 gradient accumulator
+    float* m1 = nullptr;     // Adam moments
+    float* m2 = nullptr;
+    float* wk = nullptr;     // parameters as the kernels see them (rounded to BF16 when act is BF16)
+    // bound system
+    int64_t nc = 0;          // coarse nodes (vertices)
+    int64_t nf = 0;          // fine DOFs
+    int64_t* crow = nullptr; // coarse graph CSR
+    int32_t* ccol = nullptr;
+    float* cval = nullptr;
+    int64_t cnnz = 0;
+    float* diag_f = nullptr;    // fine diagonal
+    float* isd_c = nullptr;     // 1/sqrt(A_vv)
+    float* feat = nullptr;      // static features [nc][NF]
+    int32_t* edge_ends = nullptr;  // [ne][2]
+    int64_t* vrow = nullptr;       // vertex -> incident edge DOFs (CSR, ascending)
+    int32_t* vedge = nullptr;
+    double* dpart = nullptr;       // [2][kMaxPart] dot partials of the standalone FP32 apply
+    float* coef = nullptr;      // a [nc][K] (network output)
+    // activations: H_l (l=0..L), G_l (l=1..L), Z_l (l=0..L) -- each nc*C of act type
+    void* act_buf = nullptr;
+    size_t act_bytes = 0;
+    float* u = nullptr;         // Dc^-1/2 P^T r            [nc]
+    float* pw = nullptr;        // A_hat^k w, k = 0..K-1    [K][nc]
+    float* qv = nullptr;        // A_hat^k v, k = 0..K-1    [K][nc]
+    float* t0 = nullptr;        // scratch [nc]
+    float* t1 = nullptr;        // scratch [nc]
+    float* cc = nullptr;        // coarse correction [nc]
+    float* ga = nullptr;        // dL/da [nc][K]
+    float* dH = nullptr;        // backward buffers [nc][C] fp32
+    float* dG = nullptr;
+    float* dZ = nullptr;
+    float* part = nullptr;      // reduction partials
+    float* wpart = nullptr;     // weight-gradient partials [kMaxPart][C*C]
+    double* fine_tmp = nullptr;   // [nf] f64
+    double* fine_tmp2 = nullptr;  // [nf]
+    int64_t bind_gen = 0;       // incremented by every bind (solver graphs bake the buffers in)
+    const void* bound_vals = nullptr;
+    int bound_prec = -1;
+    bool bound = false;
+};
+
+// ------------------------------------------------------------ parameter layout
+struct Layout {
+    int64_t W0, b0, W[kMaxLayers], b[kMaxLayers], wout, bout, total;
+};
+Layout layout(int L) {
+    Layout o;
+    int64_t p = 0;
+    o.W0 = p; p += NF * C;
+    o.b0 = p; p += C;
+    for (int l = 0; l < L; ++l) {
+        o.W[l] = p; p += C * C;
+        o.b[l] = p; p += C;
+    }
+    o.wout = p; p += C * K;
+    o.bout = p; p += K;
+    o.total = p;
+    return o;
+}
+
+// ------------------------------------------------------------ bind: coarse graph and features
+__global__ void fine_diag_kernel(int64_t n, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                                 const void* __restrict__ vals, int f32, float* __restrict__ diag) {
+    const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    float d = 0.f;
+    for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k)
+        if (col[k] == r) {
+            d = f32 ? ((const float*)vals)[k] : (float)((const double*)vals)[k];
+            break;
+        }
+    diag[r] = d;
+}
+
+__global__ void coarse_count_kernel(int64_t nc, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                                    unsigned long long* __restrict__ cnt) {
+    const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (r >= nc) return;
+    unsigned long long c = 0;
+    for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k) c += (col[k] < nc && col[k] != r) ? 1 : 0;
+    cnt[r] = c;
+}
+
+__global__ void coarse_fill_kernel(int64_t nc, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                                   const void* __restrict__ vals, int f32, const float* __restrict__ diag,
+                                   const int64_t* __restrict__ crow, int32_t* __restrict__ ccol,
+                                   float* __restrict__ cval, float* __restrict__ isd) {
+    const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (r >= nc) return;
+    int64_t w = crow[r];
+    const float dr = diag[r];
+    isd[r] = dr > 0.f ? rsqrtf(dr) : 0.f;
+    for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k) {
+        const int32_t c = col[k];
+        if (c < nc && c != r) {
+            const float a = f32 ? ((const float*)vals)[k] : (float)((const double*)vals)[k];
+            const float dd = dr * diag[c];
+            ccol[w] = c;
+            cval[w] = dd > 0.f ? -a * rsqrtf(dd) : 0.f;
+            ++w;
+        }
+    }
+}
+
+// static features: log(A_vv), mean over incident tets of log(trace(D)/3)
+__global__ void static_feat_kernel(int64_t nc, const float* __restrict__ diag_f, const int64_t* __restrict__ inc_ptr,
+                                   const ScatterRec* __restrict__ recs, int kind, const double* __restrict__ D,
+                                   float* __restrict__ feat) {
+    const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (v >= nc) return;
+    const float d = diag_f[v];
+    feat[NF * v] = d > 0.f ? logf(d) : 0.f;
+    float s = 0.f;
+    const int64_t b = inc_ptr[v], e = inc_ptr[v + 1];
+    for (int64_t k = b; k < e; ++k) {
+        const int64_t t = recs[k].tet;
+        float tr = 1.f;
+        if (kind == ANIGPU_TENSOR_TET_SYM) tr = (float)((D[6 * t] + D[6 * t + 3] + D[6 * t + 5]) / 3.0);
+        else if (kind == ANIGPU_TENSOR_TET_SCALAR) tr = (float)D[t];
+        else if (kind == ANIGPU_TENSOR_CONST_SCALAR) tr = (float)D[0];
+        s += logf(fmaxf(tr, 1e-30f));
+    }
+    feat[NF * v + 1] = e > b ? s / (float)(e - b) : 0.f;
+}
+
+__global__ void edge_ends_kernel(int64_t ne, int64_t nv, const int64_t* __restrict__ inc_ptr,
+                                 const ScatterRec* __restrict__ recs, const int32_t* __restrict__ tets,
+                                 int32_t* __restrict__ ends) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    const int64_t row = nv + e;
+    const int64_t b = inc_ptr[row];
+    const ScatterRec r = recs[b];
+    const int i = (r.meta & 15) - 4;
+    const int I[6] = {0, 0, 0, 1, 1, 2}, J[6] = {1, 2, 3, 2, 3, 3};
+    ends[2 * e] = tets[4 * (int64_t)r.tet + I[i]];
+    ends[2 * e + 1] = tets[4 * (int64_t)r.tet + J[i]];
+}
+
+// vertex -> edge adjacency: counts, fill (any order), then an ascending sort of every row so
+// that sums over it have a fixed order
+__global__ void vedge_count_kernel(int64_t ne, const int32_t* __restrict__ ends, unsigned long long* __restrict__ cnt) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    atomicAdd(cnt + ends[2 * e], 1ull);
+    atomicAdd(cnt + ends[2 * e + 1], 1ull);
+}
+__global__ void vedge_fill_kernel(int64_t ne, int64_t nv, const int32_t* __restrict__ ends,
+                                  const int64_t* __restrict__ vrow, unsigned long long* __restrict__ fill,
+                                  int32_t* __restrict__ vedge) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        const int32_t v = ends[2 * e + q];
+        const unsigned long long k = atomicAdd(fill + v, 1ull);
+        vedge[vrow[v] + (int64_t)k] = (int32_t)(nv + e);
+    }
+}
+__global__ void vedge_sort_kernel(int64_t nc, const int64_t* __restrict__ vrow, int32_t* __restrict__ vedge) {
+    const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (v >= nc) return;
+    const int64_t b = vrow[v], e = vrow[v + 1];
+    for (int64_t i = b + 1; i < e; ++i) {
+        const int32_t key = vedge[i];
+        int64_t j = i - 1;
+        while (j >= b && vedge[j] > key) {
+            vedge[j + 1] = vedge[j];
+            --j;
+        }
+        vedge[j + 1] = key;
+    }
+}
+
+// fixed-order block reduction helper (float)
+__device__ __forceinline__ float block_sum(float v, float* sh) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+    __syncthreads();
+    float s = 0.f;
+    if (threadIdx.x == 0)
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += sh[i];
+    return s;
+}
+
+// centre the feature columns (partial sums, then apply)
+__global__ void feat_partial_kernel(int64_t nc, const float* __restrict__ feat, float* __restrict__ part) {
+    __shared__ float sh[32];
+    float a0 = 0.f, a1 = 0.f;
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < nc; v += (int64_t)gridDim.x * blockDim.x) {
+        a0 += feat[NF * v];
+        a1 += feat[NF * v + 1];
+    }
+    const float s0 = block_sum(a0, sh);
+    __syncthreads();
+    const float s1 = block_sum(a1, sh);
+    if (threadIdx.x == 0) {
+        part[2 * blockIdx.x] = s0;
+        part[2 * blockIdx.x + 1] = s1;
+    }
+}
+__global__ void feat_center_kernel(int64_t nc, int nb, const float* __restrict__ part, float* __restrict__ feat) {
+    __shared__ float m[2];
+    if (threadIdx.x < 2) {
+        double s = 0;
+        for (int b = 0; b < nb; ++b) s += part[2 * b + threadIdx.x];
+        m[threadIdx.x] = (float)(s / (double)nc);
+    }
+    __syncthreads();
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < nc; v += (int64_t)gridDim.x * blockDim.x) {
+        feat[NF * v] -= m[0];
+        feat[NF * v + 1] -= m[1];
+    }
+}
+
+// ------------------------------------------------------------ transfers
+// out_v = isd_v * (x_v + 1/2 sum over the edge DOFs e of v of x_e)        (Dc^-1/2 P^T x)
+template <typename T>
+__global__ void restrict_kernel(int64_t nc, const T* __restrict__ x, const int64_t* __restrict__ vrow,
+                                const int32_t* __restrict__ vedge, const float* __restrict__ isd,
+                                float* __restrict__ out) {
+    const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (v >= nc) return;
+    float s = 0.f;
+    for (int64_t k = vrow[v]; k < vrow[v + 1]; ++k) s += (float)x[vedge[k]];
+    out[v] = isd[v] * fmaf(0.5f, s, (float)x[v]);
+}
+
+// z = dinv .* r + P c
+template <typename T>
+__global__ void prolong_kernel(int64_t nf, int64_t nv, const T* __restrict__ r, const float* __restrict__ diag_f,
+                               const float* __restrict__ c, const int32_t* __restrict__ ends, T* __restrict__ z) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= nf) return;
+    const float d = diag_f[i];
+    T v = d != 0.f ? r[i] / (T)d : r[i];
+    if (i < nv) v += (T)c[i];
+    else {
+        const int64_t e = i - nv;
+        v += (T)0.5 * ((T)c[ends[2 * e]] + (T)c[ends[2 * e + 1]]);
+    }
+    z[i] = v;
+}
+
+// scalar coarse SpMV: y = A_hat x (+ coef_k .* s when s given)   (one thread per row)
+__global__ void cspmv_kernel(int64_t nc, const int64_t* __restrict__ crow, const int32_t* __restrict__ ccol,
+                             const float* __restrict__ cval, const float* __restrict__ x,
+                             const float* __restrict__ coef, int k, const float* __restrict__ s,
+                             float* __restrict__ y) {
+    const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (v >= nc) return;
+    float a = 0.f;
+    for (int64_t q = crow[v]; q < crow[v + 1]; ++q) a = fmaf(cval[q], x[ccol[q]], a);
+    if (s) a = fmaf(coef[K * v + k], s[v], a);
+    y[v] = a;
+}
+
+// y = coef_k .* s   (start of a Horner chain)
+__global__ void cscale_kernel(int64_t nc, const float* __restrict__ coef, int k, const float* __restrict__ s,
+                              float* __restrict__ y) {
+    const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (v < nc) y[v] = coef[K * v + k] * s[v];
+}
+
+// c = isd .* sum_k coef_k .* pw_k
+__global__ void combine_kernel(int64_t nc, const float* __restrict__ coef, const float* __restrict__ pw,
+                               const float* __restrict__ isd, float* __restrict__ c) {
+    const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (v >= nc) return;
+    float a = 0.f;
+#pragma unroll
+    for (int k = 0; k < K; ++k) a = fmaf(coef[K * v + k], pw[k * nc + v], a);
+    c[v] = isd[v] * a;
+}
+
+// dL/da_k = g' .* P_k + u .* Q_k
+__global__ void coef_grad_kernel(int64_t nc, const float* __restrict__ gp, const float* __restrict__ pw,
+                                 const float* __restrict__ u, const float* __restrict__ qv, float* __restrict__ ga) {
+    const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (v >= nc) return;
+#pragma unroll
+    for (int k = 0; k < K; ++k) ga[K * v + k] = gp[v] * pw[k * nc + v] + u[v] * qv[k * nc + v];
+}
+
+// ------------------------------------------------------------ fused FP32 apply (the solver's path)
+// CW lanes per coarse row; every kernel returns at once when *stop is set (a converged or
+// stopped batch of solver iterations).
+constexpr int CW = 4;
+
+__device__ __forceinline__ float cw_sum(float s) {
+#pragma unroll
+    for (int o = CW / 2; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, CW);
+    return s;
+}
+
+// u = Dc^-1/2 P^T r ; t = a_{K-1} .* u
+__global__ void __launch_bounds__(256) restrict_scale_kernel(int64_t nc, const float* __restrict__ r,
+                                                             const int64_t* __restrict__ vrow,
+                                                             const int32_t* __restrict__ vedge,
+                                                             const float* __restrict__ isd,
+                                                             const float* __restrict__ coef, float* __restrict__ u,
+                                                             float* __restrict__ t, const int* __restrict__ stop) {
+    if (stop && *stop) return;
+    const int64_t v = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / CW;
+    const int lane = threadIdx.x & (CW - 1);
+    float s = 0.f;
+    if (v < nc)
+        for (int64_t k = vrow[v] + lane; k < vrow[v + 1]; k += CW) s += r[vedge[k]];
+    s = cw_sum(s);
+    if (v < nc && lane == 0) {
+        const float uu = isd[v] * fmaf(0.5f, s, r[v]);
+        u[v] = uu;
+        t[v] = coef[K * v + K - 1] * uu;
+    }
+}
+
+// y = A_hat x (+ a_k .* s when s is given)
+__global__ void __launch_bounds__(256) cspmv4_kernel(int64_t nc, const int64_t* __restrict__ crow,
+                                                     const int32_t* __restrict__ ccol, const float* __restrict__ cval,
+                                                     const float* __restrict__ x, const float* __restrict__ coef, int k,
+                                                     const float* __restrict__ sv, float* __restrict__ y,
+                                                     const int* __restrict__ stop) {
+    if (stop && *stop) return;
+    const int64_t v = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / CW;
+    const int lane = threadIdx.x & (CW - 1);
+    float a = 0.f;
+    if (v < nc)
+        for (int64_t q = crow[v] + lane; q < crow[v + 1]; q += CW) a = fmaf(cval[q], x[ccol[q]], a);
+    a = cw_sum(a);
+    if (v < nc && lane == 0) y[v] = sv ? fmaf(coef[K * v + k], sv[v], a) : a;
+}
+
+// P_{K-1} = A_hat P_{K-2};  c = isd .* sum_k a_k .* P_k
+__global__ void __launch_bounds__(256) combine4_kernel(int64_t nc, const int64_t* __restrict__ crow,
+                                                       const int32_t* __restrict__ ccol,
+                                                       const float* __restrict__ cval, const float* __restrict__ pw,
+                                                       const float* __restrict__ coef, const float* __restrict__ isd,
+                                                       float* __restrict__ c, const int* __restrict__ stop) {
+    if (stop && *stop) return;
+    const int64_t v = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / CW;
+    const int lane = threadIdx.x & (CW - 1);
+    const float* x = pw + (int64_t)(K - 2) * nc;
+    float a = 0.f;
+    if (v < nc)
+        for (int64_t q = crow[v] + lane; q < crow[v + 1]; q += CW) a = fmaf(cval[q], x[ccol[q]], a);
+    a = cw_sum(a);
+    if (v < nc && lane == 0) {
+        float s = coef[K * v + K - 1] * a;
+#pragma unroll
+        for (int k = K - 2; k >= 0; --k) s = fmaf(coef[K * v + k], pw[(int64_t)k * nc + v], s);
+        c[v] = isd[v] * s;
+    }
+}
+
+// z = D^-1 r + P c ; block partials of r.z and z.qold (FP32 per thread, FP64 across the block)
+__global__ void __launch_bounds__(256) prolong_dot_kernel(int64_t nf, int64_t nv, const float* __restrict__ r,
+                                                          const float* __restrict__ diag_f,
+                                                          const float* __restrict__ c,
+                                                          const int32_t* __restrict__ ends,
+                                                          const float* __restrict__ qold, float* __restrict__ z,
+                                                          double* __restrict__ part_rz, double* __restrict__ part_zq,
+                                                          const int* __restrict__ stop) {
+    __shared__ double sh[32];
+    if (stop && *stop) return;
+    float arz = 0.f, azq = 0.f;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nf; i += (int64_t)gridDim.x * blockDim.x) {
+        const float d = diag_f[i];
+        const float ri = r[i];
+        float zi = d != 0.f ? ri / d : ri;
+        if (i < nv) zi += c[i];
+        else {
+            const int64_t e = i - nv;
+            zi = fmaf(0.5f, c[ends[2 * e]] + c[ends[2 * e + 1]], zi);
+        }
+        z[i] = zi;
+        arz = fmaf(ri, zi, arz);
+        if (qold) azq = fmaf(zi, qold[i], azq);
+    }
+    double a = arz, b = azq;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        sh[threadIdx.x >> 5] = a;
+        sh[16 + (threadIdx.x >> 5)] = b;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double ta = 0, tb = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            ta += sh[w];
+            tb += sh[16 + w];
+        }
+        part_rz[blockIdx.x] = ta;
+        part_zq[blockIdx.x] = tb;
+    }
+}
+
+// ------------------------------------------------------------ network forward
+// one warp per node; lane owns channels lane and lane + 32
+template <typename A>
+__global__ void input_layer_kernel(int64_t nc, const float* __restrict__ feat, const float* __restrict__ W0,
+                                   const float* __restrict__ b0, A* __restrict__ Z, A* __restrict__ H) {
+    const int64_t v = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (v >= nc) return;
+    const float f1 = feat[NF * v], f2 = feat[NF * v + 1];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int c = lane + 32 * h;
+        const float z = b0[c] + f1 * W0[c] + f2 * W0[C + c];
+        Z[v * C + c] = cvt<A>(z);
+        H[v * C + c] = cvt<A>(fmaxf(z, 0.f));
+    }
+}
+
+// G = A_hat H   (rows of the coarse graph)
+template <typename In, typename Out>
+__global__ void spmm_kernel(int64_t nc, const int64_t* __restrict__ crow, const int32_t* __restrict__ ccol,
+                            const float* __restrict__ cval, const In* __restrict__ H, Out* __restrict__ G,
+                            int accumulate) {
+    const int64_t v = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (v >= nc) return;
+    float a0 = 0.f, a1 = 0.f;
+    for (int64_t k = crow[v]; k < crow[v + 1]; ++k) {
+        const float w = cval[k];
+        const In* hr = H + (int64_t)ccol[k] * C;
+        a0 = fmaf(w, ld(hr + lane), a0);
+        a1 = fmaf(w, ld(hr + lane + 32), a1);
+    }
+    if (accumulate) {
+        a0 += ld(G + v * C + lane);
+        a1 += ld(G + v * C + lane + 32);
+    }
+    G[v * C + lane] = cvt<Out>(a0);
+    G[v * C + lane + 32] = cvt<Out>(a1);
+}
+
+// Z = G W + b ; Hout = Hin + relu(Z)
+template <typename A>
+__global__ void __launch_bounds__(kBlk) dense_kernel(int64_t nc, const A* __restrict__ G, const float* __restrict__ W,
+                                                     const float* __restrict__ b, const A* __restrict__ Hin,
+                                                     A* __restrict__ Z, A* __restrict__ Hout) {
+    __shared__ float sW[C * C];
+    for (int k = threadIdx.x; k < C * C; k += blockDim.x) sW[k] = W[k];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int64_t v = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (v >= nc) return;
+    const float g0 = ld(G + v * C + lane), g1 = ld(G + v * C + lane + 32);
+    float z0 = b[lane], z1 = b[lane + 32];
+#pragma unroll 8
+    for (int k = 0; k < 32; ++k) {
+        const float ga = __shfl_sync(0xffffffffu, g0, k), gb = __shfl_sync(0xffffffffu, g1, k);
+        z0 = fmaf(ga, sW[k * C + lane], z0);
+        z1 = fmaf(ga, sW[k * C + lane + 32], z1);
+        z0 = fmaf(gb, sW[(k + 32) * C + lane], z0);
+        z1 = fmaf(gb, sW[(k + 32) * C + lane + 32], z1);
+    }
+    Z[v * C + lane] = cvt<A>(z0);
+    Z[v * C + lane + 32] = cvt<A>(z1);
+    Hout[v * C + lane] = cvt<A>(ld(Hin + v * C + lane) + fmaxf(z0, 0.f));
+    Hout[v * C + lane + 32] = cvt<A>(ld(Hin + v * C + lane + 32) + fmaxf(z1, 0.f));
+}
+
+// a = H W_out + b_out   (K outputs per node)
+template <typename A>
+__global__ void output_kernel(int64_t nc, const A* __restrict__ H, const float* __restrict__ wout,
+                              const float* __restrict__ bout, float* __restrict__ coef) {
+    const int64_t v = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (v >= nc) return;
+    const float h0 = ld(H + v * C + lane), h1 = ld(H + v * C + lane + 32);
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        float s = h0 * wout[lane * K + k] + h1 * wout[(lane + 32) * K + k];
+#pragma unroll
+        for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) coef[K * v + k] = s + bout[k];
+    }
+}
+
+// ------------------------------------------------------------ network backward
+// dH_L = ga W_out^T ; partials of dW_out (C x K) and db_out (K)
+template <typename A>
+__global__ void output_bwd_kernel(int64_t nc, const A* __restrict__ H, const float* __restrict__ wout,
+                                  const float* __restrict__ ga, float* __restrict__ dH, float* __restrict__ part) {
+    const int lane = threadIdx.x & 31;
+    const int wpb = blockDim.x >> 5;
+    float acc0[K], acc1[K], accb[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) acc0[k] = acc1[k] = accb[k] = 0.f;
+    for (int64_t v = (int64_t)blockIdx.x * wpb + (threadIdx.x >> 5); v < nc; v += (int64_t)gridDim.x * wpb) {
+        float d0 = 0.f, d1 = 0.f;
+        const float h0 = ld(H + v * C + lane), h1 = ld(H + v * C + lane + 32);
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const float g = ga[K * v + k];
+            d0 = fmaf(g, wout[lane * K + k], d0);
+            d1 = fmaf(g, wout[(lane + 32) * K + k], d1);
+            acc0[k] = fmaf(g, h0, acc0[k]);
+            acc1[k] = fmaf(g, h1, acc1[k]);
+            accb[k] += g;
+        }
+        dH[v * C + lane] = d0;
+        dH[v * C + lane + 32] = d1;
+    }
+    // fixed-order combination over the warps of the block: [C*K] weights then [K] biases
+    __shared__ float red[8][C * K + K];
+    const int w = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        red[w][lane * K + k] = acc0[k];
+        red[w][(lane + 32) * K + k] = acc1[k];
+    }
+    if (lane < K) red[w][C * K + lane] = accb[lane];
+    __syncthreads();
+    for (int q = threadIdx.x; q < C * K + K; q += blockDim.x) {
+        float s = 0.f;
+        for (int u = 0; u < wpb; ++u) s += red[u][q];
+        part[(int64_t)blockIdx.x * (C * K + K) + q] = s;
+    }
+}
+
+// dZ = dH * (Z > 0); dG = dZ W^T ; dW partial = G^T dZ (per block); db partial
+template <typename A>
+__global__ void __launch_bounds__(kBlk) dense_bwd_kernel(int64_t nc, const float* __restrict__ dH,
+                                                         const A* __restrict__ Z, const A* __restrict__ G,
+                                                         const float* __restrict__ W, float* __restrict__ dZout,
+                                                         float* __restrict__ dG, float* __restrict__ wpart,
+                                                         float* __restrict__ bpart, int rows_per_block) {
+    __shared__ float sW[C * C];
+    __shared__ float sG[32][C + 1];
+    __shared__ float sZ[32][C + 1];
+    for (int k = threadIdx.x; k < C * C; k += blockDim.x) sW[k] = W[k];
+    // each thread owns 16 entries of dW: rows (tid / 16) * 4 .. +4, cols (tid % 16) * 4 .. +4
+    const int tr = (threadIdx.x >> 4) * 4, tc = (threadIdx.x & 15) * 4;
+    float acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[a][q] = 0.f;
+    float bacc = 0.f;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t v0 = (int64_t)blockIdx.x * rows_per_block;
+    const int64_t vend = (v0 + rows_per_block < nc) ? v0 + rows_per_block : nc;
+    for (int64_t base = v0; base < vend; base += 32) {
+        for (int r = w; r < 32; r += kBlk / 32) {
+            const int64_t v = base + r;
+            float z0 = 0.f, z1 = 0.f, g0 = 0.f, g1 = 0.f;
+            if (v < vend) {
+                const float h0 = dH[v * C + lane], h1 = dH[v * C + lane + 32];
+                z0 = ld(Z + v * C + lane) > 0.f ? h0 : 0.f;
+                z1 = ld(Z + v * C + lane + 32) > 0.f ? h1 : 0.f;
+                g0 = ld(G + v * C + lane);
+                g1 = ld(G + v * C + lane + 32);
+                dZout[v * C + lane] = z0;
+                dZout[v * C + lane + 32] = z1;
+                float d0 = 0.f, d1 = 0.f;
+#pragma unroll 8
+                for (int c = 0; c < 32; ++c) {
+                    const float za = __shfl_sync(0xffffffffu, z0, c), zb = __shfl_sync(0xffffffffu, z1, c);
+                    d0 = fmaf(za, sW[lane * C + c], d0);
+                    d0 = fmaf(zb, sW[lane * C + c + 32], d0);
+                    d1 = fmaf(za, sW[(lane + 32) * C + c], d1);
+                    d1 = fmaf(zb, sW[(lane + 32) * C + c + 32], d1);
+                }
+                dG[v * C + lane] = d0;
+                dG[v * C + lane + 32] = d1;
+            }
+            sZ[r][lane] = z0;
+            sZ[r][lane + 32] = z1;
+            sG[r][lane] = g0;
+            sG[r][lane + 32] = g1;
+        }
+        __syncthreads();
+        for (int r = 0; r < 32; ++r) {
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) acc[a][q] = fmaf(sG[r][tr + a], sZ[r][tc + q], acc[a][q]);
+        }
+        if (threadIdx.x < C)
+            for (int r = 0; r < 32; ++r) bacc += sZ[r][threadIdx.x];
+        __syncthreads();
+    }
+    float* wp = wpart + (int64_t)blockIdx.x * C * C;
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) wp[(tr + a) * C + tc + q] = acc[a][q];
+    if (threadIdx.x < C) bpart[(int64_t)blockIdx.x * C + threadIdx.x] = bacc;
+}
+
+// input layer: dZ0 = dH0 * (Z0 > 0); dW0 partial = F^T dZ0 (NF x C); db0 partial
+template <typename A>
+__global__ void input_bwd_kernel(int64_t nc, const float* __restrict__ dH, const A* __restrict__ Z,
+                                 const float* __restrict__ feat, float* __restrict__ part, int rows_per_block) {
+    const int c = threadIdx.x;
+    if (c >= C) return;
+    float a1 = 0.f, a2 = 0.f, ab = 0.f;
+    const int64_t v0 = (int64_t)blockIdx.x * rows_per_block;
+    const int64_t v1 = (v0 + rows_per_block < nc) ? v0 + rows_per_block : nc;
+    for (int64_t v = v0; v < v1; ++v) {
+        const float d = ld(Z + v * C + c) > 0.f ? dH[v * C + c] : 0.f;
+        a1 = fmaf(feat[NF * v], d, a1);
+        a2 = fmaf(feat[NF * v + 1], d, a2);
+        ab += d;
+    }
+    float* p = part + (int64_t)blockIdx.x * 3 * C;
+    p[c] = a1;
+    p[C + c] = a2;
+    p[2 * C + c] = ab;
+}
+
+// out[k] += sum_b part[b * stride + k]  (fixed order over blocks)
+__global__ void reduce_parts_kernel(int n, int nb, int64_t stride, const float* __restrict__ part,
+                                    float* __restrict__ out) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    float s = 0.f;
+    for (int b = 0; b < nb; ++b) s += part[(int64_t)b * stride + k];
+    out[k] += s;
+}
+
+// ------------------------------------------------------------ loss pieces
+__global__ void sub_kernel(int64_t n, const double* __restrict__ a, const double* __restrict__ b,
+                           double* __restrict__ out) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) out[i] = a[i] - b[i];
+}
+__global__ void dot_partial_kernel(int64_t n, const double* __restrict__ a, const double* __restrict__ b,
+                                   double* __restrict__ part) {
+    __shared__ double sh[32];
+    double acc = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        acc += a[i] * b[i];
+#pragma unroll
+    for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += sh[i];
+        part[blockIdx.x] = s;
+    }
+}
+__global__ void scale_kernel(int64_t n, float a, float* __restrict__ x) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) x[i] *= a;
+}
+
+__global__ void adam_kernel(int64_t n, float* __restrict__ w, float* __restrict__ g, float* __restrict__ m1,
+                            float* __restrict__ m2, float* __restrict__ wk, float lr, float b1, float b2, float eps,
+                            float c1, float c2, float gscale, int bf16) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i] * gscale;
+    const float a = b1 * m1[i] + (1.f - b1) * gi;
+    const float b = b2 * m2[i] + (1.f - b2) * gi * gi;
+    m1[i] = a;
+    m2[i] = b;
+    const float wi = w[i] - lr * (a / c1) / (sqrtf(b / c2) + eps);
+    w[i] = wi;
+    wk[i] = bf16 ? __bfloat162float(__float2bfloat16_rn(wi)) : wi;
+    g[i] = 0.f;
+}
+
+__global__ void round_params_kernel(int64_t n, const float* __restrict__ w, float* __restrict__ wk, int bf16) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) wk[i] = bf16 ? __bfloat162float(__float2bfloat16_rn(w[i])) : w[i];
+}
+
+// ------------------------------------------------------------ host helpers
+#define RC(x)                \
+    do {                     \
+        int _rc = (x);       \
+        if (_rc) return _rc; \
+    } while (0)
+
+Gnn* gnn(anigpu_ctx* h) { return static_cast<Gnn*>(h->learned); }
+
+std::atomic<int64_t> g_bind_counter{0};
+
+unsigned nblk(int64_t n, int threads) { return grid_for(n, threads); }
+
+size_t act_size(const Gnn* g) { return g->act == ANIGPU_BF16 ? 2 : 4; }
+
+// activation arrays: H_l (L+1), G_l (L), Z_l (L+1)
+void* act_ptr(Gnn* g, int which, int l) {
+    const size_t sz = (size_t)g->nc * C * act_size(g);
+    int idx = which == 0 ? l : (which == 1 ? (g->layers + 1) + (l - 1) : (2 * g->layers + 1) + l);
+    return static_cast<char*>(g->act_buf) + sz * idx;
+}
+
+template <typename A>
+int forward_t(anigpu_ctx* h, Gnn* g, const Layout& L) {
+    cudaStream_t s = h->stream;
+    const int64_t nc = g->nc;
+    const unsigned wb = nblk(nc * 32, kBlk);
+    input_layer_kernel<A><<<wb, kBlk, 0, s>>>(nc, g->feat, g->wk + L.W0, g->wk + L.b0, (A*)act_ptr(g, 2, 0),
+                                             (A*)act_ptr(g, 0, 0));
+    ANI_LAUNCHED(h);
+    for (int l = 1; l <= g->layers; ++l) {
+        spmm_kernel<A, A><<<wb, kBlk, 0, s>>>(nc, g->crow, g->ccol, g->cval, (const A*)act_ptr(g, 0, l - 1),
+                                              (A*)act_ptr(g, 1, l), 0);
+        ANI_LAUNCHED(h);
+        dense_kernel<A><<<wb, kBlk, 0, s>>>(nc, (const A*)act_ptr(g, 1, l), g->wk + L.W[l - 1], g->wk + L.b[l - 1],
+                                            (const A*)act_ptr(g, 0, l - 1), (A*)act_ptr(g, 2, l),
+                                            (A*)act_ptr(g, 0, l));
+        ANI_LAUNCHED(h);
+    }
+    output_kernel<A><<<wb, kBlk, 0, s>>>(nc, (const A*)act_ptr(g, 0, g->layers), g->wk + L.wout, g->wk + L.bout,
+                                         g->coef);
+    ANI_LAUNCHED(h);
+    return ANIGPU_OK;
+}
+
+template <typename A>
+int backward_t(anigpu_ctx* h, Gnn* g, const Layout& L) {
+    cudaStream_t s = h->stream;
+    const int64_t nc = g->nc;
+    int nb = (int)std::min<int64_t>(kMaxPart, (int64_t)nblk(nc * 32, kBlk));
+    output_bwd_kernel<A><<<nb, kBlk, 0, s>>>(nc, (const A*)act_ptr(g, 0, g->layers), g->wk + L.wout, g->ga, g->dH,
+                                             g->part);
+    ANI_LAUNCHED(h);
+    reduce_parts_kernel<<<1, C * K + K, 0, s>>>(C * K, nb, C * K + K, g->part, g->g + L.wout);
+    ANI_LAUNCHED(h);
+    reduce_parts_kernel<<<1, K, 0, s>>>(K, nb, C * K + K, g->part + C * K, g->g + L.bout);
+    ANI_LAUNCHED(h);
+    const int64_t rpb = std::max<int64_t>(32, ((nc + kMaxPart - 1) / kMaxPart + 31) / 32 * 32);
+    const int nbw = (int)((nc + rpb - 1) / rpb);
+    for (int l = g->layers; l >= 1; --l) {
+        dense_bwd_kernel<A><<<nbw, kBlk, 0, s>>>(nc, g->dH, (const A*)act_ptr(g, 2, l), (const A*)act_ptr(g, 1, l),
+                                                 g->wk + L.W[l - 1], g->dZ, g->dG, g->wpart, g->part, (int)rpb);
+        ANI_LAUNCHED(h);
+        reduce_parts_kernel<<<nblk(C * C, 256), 256, 0, s>>>(C * C, nbw, (int64_t)C * C, g->wpart, g->g + L.W[l - 1]);
+        ANI_LAUNCHED(h);
+        reduce_parts_kernel<<<1, C, 0, s>>>(C, nbw, C, g->part, g->g + L.b[l - 1]);
+        ANI_LAUNCHED(h);
+        // dH_{l-1} = dH_l + A_hat dG   (A_hat symmetric)
+        spmm_kernel<float, float><<<nblk(nc * 32, kBlk), kBlk, 0, s>>>(nc, g->crow, g->ccol, g->cval, g->dG, g->dH, 1);
+        ANI_LAUNCHED(h);
+    }
+    input_bwd_kernel<A><<<nbw, C, 0, s>>>(nc, g->dH, (const A*)act_ptr(g, 2, 0), g->feat, g->part, (int)rpb);
+    ANI_LAUNCHED(h);
+    reduce_parts_kernel<<<1, NF * C, 0, s>>>(NF * C, nbw, 3 * C, g->part, g->g + L.W0);
+    ANI_LAUNCHED(h);
+    reduce_parts_kernel<<<1, C, 0, s>>>(C, nbw, 3 * C, g->part + NF * C, g->g + L.b0);
+    ANI_LAUNCHED(h);
+    return ANIGPU_OK;
+}
+
+// Horner: out = sum_k A_hat^k (coef_k .* s)   (K-1 SpMVs)
+int horner(anigpu_ctx* h, Gnn* g, const float* sv, float* out) {
+    cudaStream_t st = h->stream;
+    const unsigned b = nblk(g->nc, 256);
+    cscale_kernel<<<b, 256, 0, st>>>(g->nc, g->coef, K - 1, sv, g->t0);
+    ANI_LAUNCHED(h);
+    float* cur = g->t0;
+    float* nxt = g->t1;
+    for (int k = K - 2; k >= 0; --k) {
+        float* dst = k == 0 ? out : nxt;
+        cspmv_kernel<<<b, 256, 0, st>>>(g->nc, g->crow, g->ccol, g->cval, cur, g->coef, k, sv, dst);
+        ANI_LAUNCHED(h);
+        std::swap(cur, nxt);
+    }
+    return ANIGPU_OK;
+}
+
+// powers: P_0 = x, P_k = A_hat P_{k-1}, stored in pw[k*nc]
+int powers(anigpu_ctx* h, Gnn* g, const float* x, float* pw) {
+    cudaStream_t st = h->stream;
+    const unsigned b = nblk(g->nc, 256);
+    ANI_CUDA(h, cudaMemcpyAsync(pw, x, sizeof(float) * g->nc, cudaMemcpyDeviceToDevice, st));
+    for (int k = 1; k < K; ++k) {
+        cspmv_kernel<<<b, 256, 0, st>>>(g->nc, g->crow, g->ccol, g->cval, pw + (k - 1) * g->nc, nullptr, 0, nullptr,
+                                        pw + k * g->nc);
+        ANI_LAUNCHED(h);
+    }
+    return ANIGPU_OK;
+}
+
+// z = M r (and keeps u, w powers for the backward pass)
+template <typename T>
+int apply_impl(anigpu_ctx* h, Gnn* g, const T* r, T* z) {
+    cudaStream_t s = h->stream;
+    restrict_kernel<T><<<nblk(g->nc, 256), 256, 0, s>>>(g->nc, r, g->vrow, g->vedge, g->isd_c, g->u);
+    ANI_LAUNCHED(h);
+    // w = B^T u = sum_k A_hat^k (a_k .* u); then P_k = A_hat^k w; c = isd .* sum_k a_k .* P_k
+    float* wv = g->qv;  // w lives in qv[0..nc) until the backward pass needs qv
+    RC(horner(h, g, g->u, wv));
+    RC(powers(h, g, wv, g->pw));
+    combine_kernel<<<nblk(g->nc, 256), 256, 0, s>>>(g->nc, g->coef, g->pw, g->isd_c, g->cc);
+    ANI_LAUNCHED(h);
+    prolong_kernel<T><<<nblk(g->nf, 256), 256, 0, s>>>(g->nf, h->nv, r, g->diag_f, g->cc, g->edge_ends, z);
+    ANI_LAUNCHED(h);
+    return ANIGPU_OK;
+}
+
+}  // namespace
+
+// z = M r in FP32 with fused kernels; nb blocks of partials for r.z and z.qold.  No
+// allocation and no synchronisation, so solver iterations around it can be graph-captured.
+int gnn_precond_f32(anigpu_ctx* h, const float* r, float* z, const float* qold, double* part_rz, double* part_zq,
+                    int nb, const int* stop) {
+    Gnn* g = gnn(h);
+    cudaStream_t s = h->stream;
+    const unsigned bc = nblk(g->nc * CW, 256);
+    restrict_scale_kernel<<<bc, 256, 0, s>>>(g->nc, r, g->vrow, g->vedge, g->isd_c, g->coef, g->u, g->t0, stop);
+    ANI_LAUNCHED(h);
+    float* cur = g->t0;
+    float* nxt = g->t1;
+    for (int k = K - 2; k >= 0; --k) {  // Horner: w = sum_k A_hat^k (a_k .* u), into pw[0]
+        float* dst = k == 0 ? g->pw : nxt;
+        cspmv4_kernel<<<bc, 256, 0, s>>>(g->nc, g->crow, g->ccol, g->cval, cur, g->coef, k, g->u, dst, stop);
+        ANI_LAUNCHED(h);
+        std::swap(cur, nxt);
+    }
+    for (int k = 1; k <= K - 2; ++k) {  // P_k = A_hat^k w
+        cspmv4_kernel<<<bc, 256, 0, s>>>(g->nc, g->crow, g->ccol, g->cval, g->pw + (k - 1) * g->nc, nullptr, 0,
+                                         nullptr, g->pw + k * g->nc, stop);
+        ANI_LAUNCHED(h);
+    }
+    combine4_kernel<<<bc, 256, 0, s>>>(g->nc, g->crow, g->ccol, g->cval, g->pw, g->coef, g->isd_c, g->cc, stop);
+    ANI_LAUNCHED(h);
+    prolong_dot_kernel<<<nb, 256, 0, s>>>(g->nf, h->nv, r, g->diag_f, g->cc, g->edge_ends, qold, z, part_rz, part_zq,
+                                          stop);
+    ANI_LAUNCHED(h);
+    return ANIGPU_OK;
+}
+
+int64_t gnn_bind_generation(anigpu_ctx* h) { return gnn(h) ? gnn(h)->bind_gen : -1; }
+
+// ------------------------------------------------------------ entry points
+int gnn_init(anigpu_ctx* h, int layers, int act, uint64_t seed) {
+    if (layers < 1 || layers > kMaxLayers) return set_err(h, ANIGPU_ERR_ARG, "layers must be 1..8");
+    if (act != ANIGPU_F32 && act != ANIGPU_BF16) return set_err(h, ANIGPU_ERR_ARG, "activation precision");
+    free_learned(h);
+    Gnn* g = new Gnn();
+    h->learned = g;
+    g->layers = layers;
+    g->act = act;
+    const Layout L = layout(layers);
+    g->nparam = L.total;
+    RC(dev_alloc(h, &g->w, L.total));
+    RC(dev_alloc(h, &g->g, L.total));
+    RC(dev_alloc(h, &g->m1, L.total));
+    RC(dev_alloc(h, &g->m2, L.total));
+    RC(dev_alloc(h, &g->wk, L.total));
+    // deterministic init (splitmix64 -> uniform): He-uniform hidden weights, zero biases, small
+    // output weights, b_out = (1, 0, ...) so that the untrained B is the identity
+    std::vector<float> w(L.total, 0.f);
+    uint64_t st = seed;
+    auto next = [&]() {
+        uint64_t z = (st += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        return (double)(z >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0;
+    };
+    for (int k = 0; k < NF * C; ++k) w[L.W0 + k] = (float)(next() * std::sqrt(6.0 / NF));
+    for (int l = 0; l < layers; ++l)
+        for (int k = 0; k < C * C; ++k) w[L.W[l] + k] = (float)(next() * std::sqrt(6.0 / C) * 0.3);
+    for (int k = 0; k < C * K; ++k) w[L.wout + k] = (float)(next() * std::sqrt(3.0 / C) * 0.01);
+    w[L.bout] = 1.f;
+    ANI_CUDA(h, cudaMemcpyAsync(g->w, w.data(), sizeof(float) * L.total, cudaMemcpyHostToDevice, h->stream));
+    ANI_CUDA(h, cudaMemsetAsync(g->g, 0, sizeof(float) * L.total, h->stream));
+    ANI_CUDA(h, cudaMemsetAsync(g->m1, 0, sizeof(float) * L.total, h->stream));
+    ANI_CUDA(h, cudaMemsetAsync(g->m2, 0, sizeof(float) * L.total, h->stream));
+    round_params_kernel<<<nblk(L.total, 256), 256, 0, h->stream>>>(L.total, g->w, g->wk, act == ANIGPU_BF16);
+    ANI_LAUNCHED(h);
+    ANI_CUDA(h, cudaStreamSynchronize(h->stream));
+    return ANIGPU_OK;
+}
+
+int64_t gnn_num_params(anigpu_ctx* h) { return gnn(h) ? gnn(h)->nparam : -1; }
+
+int gnn_forward_coefs(anigpu_ctx* h) {
+    Gnn* g = gnn(h);
+    const Layout L = layout(g->layers);
+    if (g->act == ANIGPU_BF16) return forward_t<__nv_bfloat16>(h, g, L);
+    return forward_t<float>(h, g, L);
+}
+
+int gnn_params(anigpu_ctx* h, float* host, int64_t n, int set, int which) {
+    Gnn* g = gnn(h);
+    if (!g) return set_err(h, ANIGPU_ERR_STATE, "anigpu_gnn_init not called");
+    if (n != g->nparam) return set_err(h, ANIGPU_ERR_ARG, "parameter count mismatch");
+    float* dev = which == 0 ? g->w : g->g;
+    if (set) {
+        ANI_CUDA(h, cudaMemcpyAsync(dev, host, sizeof(float) * n, cudaMemcpyHostToDevice, h->stream));
+        if (which == 0) {
+            round_params_kernel<<<nblk(n, 256), 256, 0, h->stream>>>(n, g->w, g->wk, g->act == ANIGPU_BF16);
+            ANI_LAUNCHED(h);
+            if (g->bound) RC(gnn_forward_coefs(h));  // new parameters: new coefficients
+        }
+    } else {
+        ANI_CUDA(h, cudaMemcpyAsync(host, dev, sizeof(float) * n, cudaMemcpyDeviceToHost, h->stream));
+    }
+    ANI_CUDA(h, cudaStreamSynchronize(h->stream));
+    return ANIGPU_OK;
+}
+
+int gnn_bind(anigpu_ctx* h, const void* vals, int precision, int kind, const double* D) {
+    Gnn* g = gnn(h);
+    if (!g) return set_err(h, ANIGPU_ERR_STATE, "anigpu_gnn_init not called");
+    if (h->space != ANIGPU_P2) return set_err(h, ANIGPU_ERR_UNSUPPORTED, "the learned preconditioner needs a P2 problem");
+    if (!vals) return set_err(h, ANIGPU_ERR_ARG, "NULL values");
+    if (kind != ANIGPU_TENSOR_NULL && !D) return set_err(h, ANIGPU_ERR_ARG, "NULL tensor");
+    cudaStream_t s = h->stream;
+    const int f32 = precision == ANIGPU_F32;
+    const bool resize = g->nc != h->nv || g->nf != h->ndof;
+    g->nc = h->nv;
+    g->nf = h->ndof;
+    if (resize) {
+        RC(dev_alloc(h, &g->crow, g->nc + 1));
+        RC(dev_alloc(h, &g->diag_f, g->nf));
+        RC(dev_alloc(h, &g->isd_c, g->nc));
+        RC(dev_alloc(h, &g->feat, NF * g->nc));
+        RC(dev_alloc(h, &g->edge_ends, 2 * std::max<int64_t>(h->ne, 1)));
+        RC(dev_alloc(h, &g->vrow, g->nc + 1));
+        RC(dev_alloc(h, &g->vedge, 2 * std::max<int64_t>(h->ne, 1)));
+        RC(dev_alloc(h, &g->dpart, 2 * kMaxPart));
+        RC(dev_alloc(h, &g->coef, (size_t)K * g->nc));
+        RC(dev_alloc(h, &g->u, g->nc));
+        RC(dev_alloc(h, &g->pw, (size_t)K * g->nc));
+        RC(dev_alloc(h, &g->qv, (size_t)K * g->nc));
+        RC(dev_alloc(h, &g->t0, g->nc));
+        RC(dev_alloc(h, &g->t1, g->nc));
+        RC(dev_alloc(h, &g->cc, g->nc));
+        RC(dev_alloc(h, &g->ga, (size_t)K * g->nc));
+        RC(dev_alloc(h, &g->dH, g->nc * C));
+        RC(dev_alloc(h, &g->dG, g->nc * C));
+        RC(dev_alloc(h, &g->dZ, g->nc * C));
+        RC(dev_alloc(h, &g->part, (size_t)kMaxPart * (C * K + K)));
+        RC(dev_alloc(h, &g->wpart, (size_t)kMaxPart * C * C));
+        RC(dev_alloc(h, &g->fine_tmp, g->nf));
+        RC(dev_alloc(h, &g->fine_tmp2, g->nf));
+        g->act_bytes = (size_t)g->nc * C * act_size(g) * (3 * g->layers + 2);
+        if (g->act_buf) cudaFree(g->act_buf);
+        g->act_buf = nullptr;
+        ANI_CUDA(h, cudaMalloc(&g->act_buf, g->act_bytes));
+    }
+    fine_diag_kernel<<<nblk(g->nf, 256), 256, 0, s>>>(g->nf, h->rowptr, h->col, vals, f32, g->diag_f);
+    ANI_LAUNCHED(h);
+    unsigned long long* cnt = nullptr;
+    ANI_CUDA(h, cudaMallocAsync((void**)&cnt, sizeof(unsigned long long) * (g->nc + 1), s));
+    ANI_CUDA(h, cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * (g->nc + 1), s));
+    coarse_count_kernel<<<nblk(g->nc, 256), 256, 0, s>>>(g->nc, h->rowptr, h->col, cnt);
+    ANI_LAUNCHED(h);
+    RC(scan_counts(h, cnt, g->nc, g->crow));
+    int64_t cnnz = 0;
+    ANI_CUDA(h, cudaMemcpyAsync(&cnnz, g->crow + g->nc, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    ANI_CUDA(h, cudaStreamSynchronize(s));
+    ANI_CUDA(h, cudaFreeAsync(cnt, s));
+    if (cnnz != g->cnnz || !g->ccol) {
+        RC(dev_alloc(h, &g->ccol, std::max<int64_t>(cnnz, 1)));
+        RC(dev_alloc(h, &g->cval, std::max<int64_t>(cnnz, 1)));
+        g->cnnz = cnnz;
+    }
+    coarse_fill_kernel<<<nblk(g->nc, 256), 256, 0, s>>>(g->nc, h->rowptr, h->col, vals, f32, g->diag_f, g->crow,
+                                                        g->ccol, g->cval, g->isd_c);
+    ANI_LAUNCHED(h);
+    static_feat_kernel<<<nblk(g->nc, 256), 256, 0, s>>>(g->nc, g->diag_f, h->inc_ptr, h->recs, kind, D, g->feat);
+    ANI_LAUNCHED(h);
+    const int nb = (int)std::min<int64_t>(kMaxPart, nblk(g->nc, 256));
+    feat_partial_kernel<<<nb, 256, 0, s>>>(g->nc, g->feat, g->part);
+    ANI_LAUNCHED(h);
+    feat_center_kernel<<<nb, 256, 0, s>>>(g->nc, nb, g->part, g->feat);
+    ANI_LAUNCHED(h);
+    edge_ends_kernel<<<nblk(std::max<int64_t>(h->ne, 1), 256), 256, 0, s>>>(h->ne, h->nv, h->inc_ptr, h->recs, h->tets,
+                                                                          g->edge_ends);
+    ANI_LAUNCHED(h);
+    {
+        unsigned long long* vc = nullptr;
+        ANI_CUDA(h, cudaMallocAsync((void**)&vc, sizeof(unsigned long long) * 2 * (g->nc + 1), s));
+        ANI_CUDA(h, cudaMemsetAsync(vc, 0, sizeof(unsigned long long) * 2 * (g->nc + 1), s));
+        const unsigned eb = nblk(std::max<int64_t>(h->ne, 1), 256);
+        vedge_count_kernel<<<eb, 256, 0, s>>>(h->ne, g->edge_ends, vc);
+        ANI_LAUNCHED(h);
+        RC(scan_counts(h, vc, g->nc, g->vrow));
+        vedge_fill_kernel<<<eb, 256, 0, s>>>(h->ne, h->nv, g->edge_ends, g->vrow, vc + g->nc + 1, g->vedge);
+        ANI_LAUNCHED(h);
+        vedge_sort_kernel<<<nblk(g->nc, 256), 256, 0, s>>>(g->nc, g->vrow, g->vedge);
+        ANI_LAUNCHED(h);
+        ANI_CUDA(h, cudaFreeAsync(vc, s));
+    }
+    g->bound_vals = vals;
+    g->bound_prec = precision;
+    g->bound = true;
+    g->bind_gen = ++g_bind_counter;  // unique over every state of every handle
+    RC(gnn_forward_coefs(h));
+    ANI_CUDA(h, cudaStreamSynchronize(s));
+    return ANIGPU_OK;
+}
+
+int gnn_apply(anigpu_ctx* h, const double* r, double* z) {
+    Gnn* g = gnn(h);
+    if (!g || !g->bound) return set_err(h, ANIGPU_ERR_STATE, "anigpu_gnn_bind not called");
+    return apply_impl<double>(h, g, r, z);
+}
+
+int gnn_coefficients(anigpu_ctx* h, float* coef) {
+    Gnn* g = gnn(h);
+    if (!g || !g->bound) return set_err(h, ANIGPU_ERR_STATE, "anigpu_gnn_bind not called");
+    if (!coef) return set_err(h, ANIGPU_ERR_ARG, "NULL output");
+    ANI_CUDA(h, cudaMemcpyAsync(coef, g->coef, sizeof(float) * K * g->nc, cudaMemcpyDeviceToDevice, h->stream));
+    ANI_CUDA(h, cudaStreamSynchronize(h->stream));
+    return ANIGPU_OK;
+}
+
+int gnn_apply_f32(anigpu_ctx* h, const float* r, float* z) {
+    Gnn* g = gnn(h);
+    if (!g || !g->bound) return set_err(h, ANIGPU_ERR_STATE, "anigpu_gnn_bind not called");
+    const int nb = (int)std::min<int64_t>(kMaxPart, nblk(g->nf, 256));
+    return gnn_precond_f32(h, r, z, nullptr, g->dpart, g->dpart + kMaxPart, nb, nullptr);
+}
+
+// forward + backward for one pair; accumulates gradients; loss to host
+int gnn_loss_grad(anigpu_ctx* h, const double* r, const double* e, double* loss) {
+    Gnn* g = gnn(h);
+    if (!g || !g->bound) return set_err(h, ANIGPU_ERR_STATE, "anigpu_gnn_bind not called");
+    cudaStream_t s = h->stream;
+    const Layout L = layout(g->layers);
+    double* m = g->fine_tmp;
+    double* q = g->fine_tmp2;
+    RC(apply_impl<double>(h, g, r, m));
+    // d = m - e (into m), q = A d
+    sub_kernel<<<nblk(g->nf, 256), 256, 0, s>>>(g->nf, m, e, m);
+    ANI_LAUNCHED(h);
+    RC(run_spmv(h, g->bound_vals, g->bound_prec, m, q));
+    const int nb = (int)std::min<int64_t>(kMaxPart, nblk(g->nf, 256));
+    double* dpart = reinterpret_cast<double*>(g->wpart);
+    dot_partial_kernel<<<nb, 256, 0, s>>>(g->nf, m, q, dpart);
+    ANI_LAUNCHED(h);
+    RC(run_spmv(h, g->bound_vals, g->bound_prec, e, m));
+    dot_partial_kernel<<<nb, 256, 0, s>>>(g->nf, e, m, dpart + kMaxPart);
+    ANI_LAUNCHED(h);
+    std::vector<double> hp(2 * kMaxPart);
+    ANI_CUDA(h, cudaMemcpyAsync(hp.data(), dpart, sizeof(double) * 2 * kMaxPart, cudaMemcpyDeviceToHost, s));
+    ANI_CUDA(h, cudaStreamSynchronize(s));
+    double dq = 0, eae = 0;
+    for (int b = 0; b < nb; ++b) {
+        dq += hp[b];
+        eae += hp[kMaxPart + b];
+    }
+    if (!(eae > 0)) return set_err(h, ANIGPU_ERR_ARG, "e^T A e is not positive");
+    *loss = dq / eae;
+    // dL/dc = 2/eAe P^T q ; g' = Dc^-1/2 dL/dc = 2/eAe * restrict(q) (restrict includes Dc^-1/2)
+    float* gp = g->cc;
+    restrict_kernel<double><<<nblk(g->nc, 256), 256, 0, s>>>(g->nc, q, g->vrow, g->vedge, g->isd_c, gp);
+    ANI_LAUNCHED(h);
+    scale_kernel<<<nblk(g->nc, 256), 256, 0, s>>>(g->nc, (float)(2.0 / eae), gp);
+    ANI_LAUNCHED(h);
+    // v = B^T g' = sum_k A_hat^k (a_k .* g'); Q_k = A_hat^k v; dL/da_k = g' .* P_k + u .* Q_k
+    float* vv = g->ga;  // v staged in ga (overwritten by the gradient below)
+    RC(horner(h, g, gp, vv));
+    RC(powers(h, g, vv, g->qv));
+    coef_grad_kernel<<<nblk(g->nc, 256), 256, 0, s>>>(g->nc, gp, g->pw, g->u, g->qv, g->ga);
+    ANI_LAUNCHED(h);
+    if (g->act == ANIGPU_BF16) RC(backward_t<__nv_bfloat16>(h, g, L));
+    else RC(backward_t<float>(h, g, L));
+    ANI_CUDA(h, cudaStreamSynchronize(s));
+    return ANIGPU_OK;
+}
+
+int gnn_adam(anigpu_ctx* h, float lr, float b1, float b2, float eps, int step, float gscale) {
+    Gnn* g = gnn(h);
+    if (!g) return set_err(h, ANIGPU_ERR_STATE, "anigpu_gnn_init not called");
+    const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
+    adam_kernel<<<nblk(g->nparam, 256), 256, 0, h->stream>>>(g->nparam, g->w, g->g, g->m1, g->m2, g->wk, lr, b1, b2,
+                                                             eps, c1, c2, gscale, g->act == ANIGPU_BF16);
+    ANI_LAUNCHED(h);
+    if (g->bound) RC(gnn_forward_coefs(h));
+    return ANIGPU_OK;
+}
+
+int gnn_zero_grads(anigpu_ctx* h) {
+    Gnn* g = gnn(h);
+    if (!g) return set_err(h, ANIGPU_ERR_STATE, "anigpu_gnn_init not called");
+    ANI_CUDA(h, cudaMemsetAsync(g->g, 0, sizeof(float) * g->nparam, h->stream));
+    return ANIGPU_OK;
+}
+
+bool gnn_bound_to(anigpu_ctx* h, const void* vals) {
+    Gnn* g = gnn(h);
+    return g && g->bound && g->bound_vals == vals;
+}
+
+const float* gnn_fine_diag(anigpu_ctx* h) { return gnn(h) ? gnn(h)->diag_f : nullptr; }
+
+void learned_invalidate(anigpu_ctx* h) {
+    free_fcg(h);
+    if (Gnn* g = gnn(h)) {
+        g->bound = false;
+        g->bound_vals = nullptr;
+    }
+}
+
+void free_learned(anigpu_ctx* h) {
+    free_fcg(h);
+    Gnn* g = gnn(h);
+    if (!g) return;
+    void* ptrs[] = {g->w,      g->g,  g->m1, g->m2, g->wk, g->crow, g->ccol, g->cval, g->diag_f, g->isd_c,
+                    g->feat,   g->edge_ends, g->vrow, g->vedge, g->dpart, g->coef, g->act_buf, g->u, g->pw, g->qv, g->t0, g->t1,
+                    g->cc,     g->ga, g->dH, g->dG, g->dZ, g->part, g->wpart, g->fine_tmp, g->fine_tmp2};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    delete g;
+    h->learned = nullptr;
+}

@@ -1,0 +1,171 @@
+"""GPU checks of the learned preconditioner and its flexible-CG solve: the network, transfers
+and polynomial against the FP64 autograd oracle (oracle/gnn_oracle.py), the hand-written
+backward kernels against autograd gradients, symmetry of M, training that lowers the loss and
+the iteration count, and the Jacobi fallback."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _system(lib, restated, n, seed, perturb=0.2):
+    import anigpu
+    from anigpu import meshgen
+    xyz, tets = meshgen.kuhn_cube(n, perturb=perturb, seed=7)
+    D = meshgen.aniso_tensors(tets.shape[0], 1.5, seed)
+    lib.mesh_upload(xyz, tets)
+    lib.problem_setup(anigpu.P2)
+    mask = meshgen.boundary_mask(lib.dof_coords().cpu().numpy())
+    lib.set_dirichlet(mask)
+    vals, rhs, _ = lib.assemble(anigpu.TENSOR_TET_SYM, D, None, 1.0, 4, anigpu.F32)
+    return dict(xyz=xyz, tets=tets, D=D, mask=mask, vals=vals, rhs=rhs)
+
+
+def _oracle(lib, restated, S):
+    from oracle.gnn_oracle import GnnOracle
+    rp, col = lib.csr_template()
+    return GnnOracle(rp.cpu().numpy(), col.cpu().numpy(), S["vals"].double().cpu().numpy(),
+                     restated.orient(S["xyz"], S["tets"]), lib.element_dofs().cpu().numpy(), S["D"],
+                     S["xyz"].shape[0], 4)
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+@pytest.fixture(scope="module")
+def small(lib, restated):
+    import anigpu
+    S = _system(lib, restated, 4, 11)
+    prec = anigpu.LearnedPreconditioner(lib, layers=4, act=anigpu.F32, seed=5)
+    w = prec.get_params()
+    # move the output layer away from its near-identity start so that every block has gradient
+    rng = np.random.default_rng(3)
+    w = (w + 0.05 * rng.standard_normal(w.size)).astype(np.float32)
+    prec.set_params(w)
+    prec.bind(S["vals"], anigpu.F32, anigpu.TENSOR_TET_SYM, S["D"])
+    S["prec"], S["w"], S["O"] = prec, w, _oracle(lib, restated, S)
+    r = np.random.default_rng(0).standard_normal(lib.ndof) * (1 - S["mask"])
+    S["r"] = r
+    x, _ = lib.solve(S["vals"], r, anigpu.SOLVE_IR_CG32, anigpu.F32, rtol=1e-11, maxit=100000)
+    S["e"] = x.cpu().numpy()
+    return S
+
+
+def test_network_coefficients_match_oracle(small):
+    a_gpu = small["prec"].coefficients().cpu().numpy()
+    a_or = small["O"].coefficients_np(small["w"])
+    assert _rel(a_gpu, a_or) <= 1e-5  # FP32 activations and accumulation vs FP64
+
+
+def test_apply_matches_oracle(small):
+    z_or = small["O"].apply(small["w"], small["r"]).detach().numpy()
+    z64 = small["prec"].apply(small["r"]).cpu().numpy()
+    z32 = small["prec"].apply_f32(small["r"]).double().cpu().numpy()
+    assert _rel(z64, z_or) <= 1e-5
+    assert _rel(z32, z_or) <= 1e-5
+
+
+def test_preconditioner_is_symmetric_positive(small, lib):
+    rng = np.random.default_rng(9)
+    x = rng.standard_normal(lib.ndof)
+    y = rng.standard_normal(lib.ndof)
+    Mx = small["prec"].apply(x).cpu().numpy()
+    My = small["prec"].apply(y).cpu().numpy()
+    assert abs(y @ Mx - x @ My) <= 1e-5 * np.linalg.norm(Mx) * np.linalg.norm(y)
+    assert x @ Mx > 0 and y @ My > 0
+
+
+def test_backward_kernels_match_autograd(small):
+    from oracle.gnn_oracle import layout
+    prec = small["prec"]
+    prec.zero_grads()
+    L = prec.loss_grad(small["r"], small["e"])
+    g = prec.get_grads()
+    L_or, g_or = small["O"].loss_and_grad(small["w"], small["r"], small["e"])
+    assert abs(L - L_or) <= 1e-5 * L_or
+    off, _ = layout(4)
+    for name, (o, s) in off.items():
+        k = int(np.prod(s))
+        assert _rel(g[o:o + k], g_or[o:o + k]) <= 2e-3, name  # FP32 kernels vs FP64 autograd
+    assert _rel(g, g_or) <= 1e-4
+    prec.zero_grads()
+
+
+def test_bf16_network_close_to_oracle(small, lib):
+    import anigpu
+    pb = anigpu.LearnedPreconditioner(lib, layers=4, act=anigpu.BF16, seed=5)
+    pb.set_params(small["w"])
+    pb.bind(small["vals"], anigpu.F32, anigpu.TENSOR_TET_SYM, small["D"])
+    a_or = small["O"].coefficients_np(small["w"])
+    assert _rel(pb.coefficients().cpu().numpy(), a_or) <= 3e-2  # BF16 activations and weights
+    pb.zero_grads()
+    pb.loss_grad(small["r"], small["e"])
+    _, g_or = small["O"].loss_and_grad(small["w"], small["r"], small["e"])
+    assert _rel(pb.get_grads(), g_or) <= 1e-1
+    # the module-scoped F32 preconditioner is gone with the re-init: rebuild it for later tests
+    small["prec"] = anigpu.LearnedPreconditioner(lib, layers=4, act=anigpu.F32, seed=5)
+    small["prec"].set_params(small["w"])
+    small["prec"].bind(small["vals"], anigpu.F32, anigpu.TENSOR_TET_SYM, small["D"])
+
+
+def test_fcg_learned_solves_and_matches_pcg(small, lib):
+    import anigpu
+    x1, s1 = lib.solve(small["vals"], small["r"], anigpu.SOLVE_FCG_LEARNED, anigpu.F32, rtol=1e-8, maxit=10000)
+    x2, s2 = lib.solve(small["vals"], small["r"], anigpu.SOLVE_JACOBI_PCG, anigpu.F32, rtol=1e-8, maxit=10000)
+    assert s1.rel_residual <= 1e-8 and s1.fallback_steps == 0
+    # true residual on the host
+    y = lib.spmv(small["vals"], x1, anigpu.F32).cpu().numpy()
+    assert np.linalg.norm(small["r"] - y) <= 1e-8 * np.linalg.norm(small["r"]) * 1.0001
+    assert s2.rel_residual <= 1e-8
+    assert _rel(x1.cpu().numpy(), small["e"]) <= 1e-3 and _rel(x2.cpu().numpy(), small["e"]) <= 1e-3
+
+
+def test_fcg_falls_back_to_jacobi_on_nonfinite_preconditioner(small, lib):
+    import anigpu
+    prec = small["prec"]
+    w = small["w"].copy()
+    from oracle.gnn_oracle import layout
+    off, _ = layout(4)
+    w[off["bout"][0]] = np.nan  # every coefficient a_0 becomes NaN: M r is NaN
+    prec.set_params(w)
+    try:
+        x, st = lib.solve(small["vals"], small["r"], anigpu.SOLVE_FCG_LEARNED, anigpu.F32, rtol=1e-8, maxit=10000)
+        assert st.rel_residual <= 1e-8
+        assert st.fallback_steps > 0 and st.fallback_steps == st.iterations
+        assert np.isfinite(x.cpu().numpy()).all()
+    finally:
+        prec.set_params(small["w"])
+
+
+def test_training_lowers_loss_and_iterations(lib, restated):
+    import anigpu
+    from anigpu import learned, meshgen
+    n = 6
+    S = _system(lib, restated, n, 100)
+    systems = []
+    for sd in range(4):
+        D = meshgen.aniso_tensors(S["tets"].shape[0], 1.5, 100 + sd)
+        v, _, _ = lib.assemble(anigpu.TENSOR_TET_SYM, D, None, 1.0, 4, anigpu.F32)
+        v = v.clone()
+        b = meshgen.normal(500 + sd, lib.ndof) * (1 - S["mask"])
+        systems.append((v, anigpu.TENSOR_TET_SYM, D, learned.training_pairs(lib, v, b, ks=(0, 2, 8, 32))))
+    Dh = meshgen.aniso_tensors(S["tets"].shape[0], 1.5, 999)
+    vh, rhs_h, _ = lib.assemble(anigpu.TENSOR_TET_SYM, Dh, None, 1.0, 4, anigpu.F32)
+    vh = vh.clone()
+    held = [(vh, anigpu.TENSOR_TET_SYM, Dh, learned.training_pairs(lib, vh, rhs_h, ks=(0, 4, 16)))]
+    prec = anigpu.LearnedPreconditioner(lib, layers=4, act=anigpu.BF16, seed=1)
+    loss0 = learned.mean_loss(prec, held)
+    prec.bind(vh, anigpu.F32, anigpu.TENSOR_TET_SYM, Dh)
+    _, s0 = lib.solve(vh, rhs_h, anigpu.SOLVE_FCG_LEARNED, anigpu.F32, rtol=1e-8, maxit=100000)
+    hist = learned.train(prec, systems, 160, lr=3e-3, lr_final=1e-3)
+    assert np.mean(hist[-16:]) < np.mean(hist[:16])
+    loss1 = learned.mean_loss(prec, held)
+    assert loss1 < 0.97 * loss0
+    prec.bind(vh, anigpu.F32, anigpu.TENSOR_TET_SYM, Dh)
+    _, s1 = lib.solve(vh, rhs_h, anigpu.SOLVE_FCG_LEARNED, anigpu.F32, rtol=1e-8, maxit=100000)
+    _, sj = lib.solve(vh, rhs_h, anigpu.SOLVE_JACOBI_PCG, anigpu.F32, rtol=1e-8,
+                      maxit=100000)
+    assert s1.rel_residual <= 1e-8 and s1.fallback_steps == 0
+    assert s1.iterations <= s0.iterations
+    assert s1.iterations < sj.iterations
