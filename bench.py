@@ -288,21 +288,42 @@ def run_ours(args):
 
     solve = None
     if not args.no_solve:
+        # each solver runs twice from x = 0; the second run is reported (the first captures graphs)
         solve = {}
-        x, st = lib.solve(vals64, rhs64, anigpu.SOLVE_JACOBI_PCG, anigpu.F64, rtol=1e-8, maxit=200000, check=False)
+        for _ in range(2):
+            x, st = lib.solve(vals64, rhs64, anigpu.SOLVE_JACOBI_PCG, anigpu.F64, rtol=1e-8, maxit=200000,
+                              check=False)
         solve["jacobi_pcg_f64"] = {"seconds": st.seconds, "iterations": st.iterations,
                                    "rel_residual_f64": st.rel_residual}
-        x, st = lib.solve(vals32, rhs, anigpu.SOLVE_IR_CG32, anigpu.F32, rtol=1e-8, maxit=200000, check=False)
+        for _ in range(2):
+            x, st = lib.solve(vals32, rhs, anigpu.SOLVE_IR_CG32, anigpu.F32, rtol=1e-8, maxit=200000, check=False)
         # error of the mixed solution against the FP64-assembled system
         r64 = rhs64 - lib.spmv(vals64, x, anigpu.F64)
         solve["ir_cg32"] = {"seconds": st.seconds, "iterations": st.iterations, "outer": st.outer_iterations,
                             "rel_residual_f64": st.rel_residual,
                             "rel_residual_vs_f64_matrix": float(r64.norm() / rhs64.norm())}
         try:
-            x, st = lib.solve(vals32, rhs, anigpu.SOLVE_FCG_LEARNED, anigpu.F32, rtol=1e-8, maxit=200000,
-                              check=True)
-            solve["fcg_learned"] = {"seconds": st.seconds, "iterations": st.iterations,
-                                    "rel_residual_f64": st.rel_residual, "fallback_steps": st.fallback_steps}
+            from anigpu import learned
+            prec = anigpu.LearnedPreconditioner(lib, layers=4, act=anigpu.BF16, seed=1)
+            trained = os.path.exists(learned.DEFAULT_WEIGHTS)
+            if trained:
+                learned.load_default(prec)
+            for _ in range(2):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                prec.bind(vals32, anigpu.F32, anigpu.TENSOR_TET_SYM, D_dev)
+                torch.cuda.synchronize()
+                bind_s = time.perf_counter() - t0
+                x, st = lib.solve(vals32, rhs, anigpu.SOLVE_FCG_LEARNED, anigpu.F32, rtol=1e-8, maxit=200000,
+                                  check=True)
+            r64 = rhs64 - lib.spmv(vals64, x, anigpu.F64)
+            tot = bind_s + st.seconds
+            solve["fcg_learned"] = {"seconds": st.seconds, "bind_seconds": bind_s, "iterations": st.iterations,
+                                    "replacements": st.outer_iterations, "fallback_steps": st.fallback_steps,
+                                    "rel_residual_f64": st.rel_residual,
+                                    "rel_residual_vs_f64_matrix": float(r64.norm() / rhs64.norm()),
+                                    "weights": "trained (anigpu/weights)" if trained else "untrained",
+                                    "speedup_vs_jacobi_pcg_f64": solve["jacobi_pcg_f64"]["seconds"] / tot}
         except anigpu.AnigpuError as e:
             solve["fcg_learned"] = {"unavailable": str(e)}
 

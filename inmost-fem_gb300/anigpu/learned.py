@@ -67,3 +67,45 @@ def load_default(prec):
     w = np.load(DEFAULT_WEIGHTS)
     prec.set_params(w)
     return w
+
+
+def main(argv=None):
+    """Train the default parameters on seeded synthetic P2 problems (perturbed Kuhn cube,
+    anisotropic per-tet tensors with log-normal eigenvalues) and save them:
+        python -m anigpu.learned --n 12 --systems 24 --steps 1500 --out weights/p2_aniso_l4.npy"""
+    import argparse
+    import time
+
+    from anigpu import meshgen
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--n", type=int, default=12)
+    ap.add_argument("--systems", type=int, default=24)
+    ap.add_argument("--steps", type=int, default=1500)
+    ap.add_argument("--lr", type=float, default=3e-3)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--out", default=DEFAULT_WEIGHTS)
+    a = ap.parse_args(argv)
+    lib = anigpu.Anigpu(0)
+    xyz, tets = meshgen.kuhn_cube(a.n, perturb=0.2, seed=7)
+    lib.mesh_upload(xyz, tets)
+    lib.problem_setup(anigpu.P2)
+    mask = meshgen.boundary_mask(lib.dof_coords().cpu().numpy())
+    lib.set_dirichlet(mask)
+    systems = []
+    for sd in range(a.systems):
+        D = meshgen.aniso_tensors(tets.shape[0], 1.5, 100 + sd)
+        v, _, _ = lib.assemble(anigpu.TENSOR_TET_SYM, D, None, 1.0, 4, anigpu.F32)
+        v = v.clone()
+        b = meshgen.normal(500 + sd, lib.ndof) * (1 - mask)
+        systems.append((v, anigpu.TENSOR_TET_SYM, D, training_pairs(lib, v, b)))
+    prec = anigpu.LearnedPreconditioner(lib, layers=4, act=anigpu.BF16, seed=a.seed)
+    t0 = time.time()
+    train(prec, systems, a.steps, lr=a.lr, lr_final=a.lr / 3, log_every=max(1, a.steps // 10))
+    print(f"trained {a.steps} steps in {time.time() - t0:.1f} s; mean loss {mean_loss(prec, systems[:4]):.4f}")
+    os.makedirs(os.path.dirname(os.path.abspath(a.out)), exist_ok=True)
+    np.save(a.out, prec.get_params())
+    print("saved", a.out)
+
+
+if __name__ == "__main__":
+    main()

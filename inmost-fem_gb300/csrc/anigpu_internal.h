@@ -27,15 +27,35 @@ int scalar_space_nf(int space);
 bool op_info(int code, int* nf, int* dim, int* base_space, int* ncomp, int* op);
 
 // ------------------------------------------------------------------ device records
-// One scatter record per (row DOF, incident tet): the tet, the row's local index in
-// the tet, the tet's Dirichlet local DOFs and, for each local DOF j of the tet, the
-// offset of its column within the row (8 bits each).
+// One scatter record per (row DOF, incident tet): the tet, the row's local index i in the
+// tet, the Dirichlet flags and the column offsets of the tet's DOFs within the row, both
+// in the canonical column order of row i (canon_local below):
 //   x: tet id
-//   y: bits 0-3 local index i, bits 4-13 Dirichlet mask (local j), bits 16-31 offsets j=8,9
-//   z: offsets j=0..3, w: offsets j=4..7 (8 bits each, little end first)
+//   y: bits 0-3 local index i, bits 4-13 Dirichlet flag of canonical column c (bit 4+c),
+//      bits 16-31 offsets of canonical columns 8, 9
+//   z: offsets of canonical columns 0..3, w: of columns 4..7 (8 bits each, little end first)
 struct __align__(16) ScatterRec {
     uint32_t tet, meta, off03, off47;
 };
+
+// Canonical column order of element row i: the local DOF of canonical column c.
+//   P1 vertex i:    i, then the other vertices ascending.
+//   P2 vertex i:    i, the other vertices o1<o2<o3, edges (i,o1) (i,o2) (i,o3), then the
+//                   opposite edges (o1,o2) (o1,o3) (o2,o3).
+//   P2 edge (a,b):  a, b, the other vertices c<d, the edge itself, (a,c) (a,d) (b,c) (b,d), (c,d).
+// Local edges are (0,1) (0,2) (0,3) (1,2) (1,3) (2,3) = local DOFs 4..9 (poly_2.h:76).
+// In this order one element row is a fixed function of the tet's Gram matrix whatever i is,
+// and the diagonal is column 0 (vertex rows) or 4 (P2 edge rows).
+__host__ __device__ inline int canon_local(int nloc, int i, int c) {
+    constexpr signed char k4[4][4] = {{0, 1, 2, 3}, {1, 0, 2, 3}, {2, 0, 1, 3}, {3, 0, 1, 2}};
+    constexpr signed char k10[10][10] = {
+        {0, 1, 2, 3, 4, 5, 6, 7, 8, 9}, {1, 0, 2, 3, 4, 7, 8, 5, 6, 9}, {2, 0, 1, 3, 5, 7, 9, 4, 6, 8},
+        {3, 0, 1, 2, 6, 8, 9, 4, 5, 7}, {0, 1, 2, 3, 4, 5, 6, 7, 8, 9}, {0, 2, 1, 3, 5, 4, 6, 7, 9, 8},
+        {0, 3, 1, 2, 6, 4, 5, 8, 9, 7}, {1, 2, 0, 3, 7, 4, 8, 5, 9, 6}, {1, 3, 0, 2, 8, 4, 7, 6, 9, 5},
+        {2, 3, 0, 1, 9, 5, 7, 6, 8, 4}};
+    return nloc == 4 ? k4[i][c] : k10[i][c];
+}
+__host__ __device__ inline int canon_diag(int nloc, int i) { return (nloc == 10 && i >= 4) ? 4 : 0; }
 
 // ------------------------------------------------------------------ context
 struct anigpu_ctx {

@@ -10,20 +10,33 @@
 //     K = |T| PSI D PSI^T (3x3 symmetric, 6 numbers per tet)
 //     Tsym^{aa} = S^{aa}, Tsym^{ab} = S^{ab} + S^{ba},  S^{ab}_ij = sum_n w_n g_i^a(n) g_j^b(n)
 // where g are the reference gradients and S is computed once on the host with the same
-// quadrature rule the caller asked for.  Phase 1 computes K (and f|T|) once per tet;
-// phase 2 is a row gather: every CSR row is owned by one group of NLOC lanes, which walks
-// the row's incident tets in ascending tet order, computes that tet's row of A (lane j
-// computes A(i, j)) and adds it into a shared-memory copy of the row at the offsets held
+// quadrature rule the caller asked for ("table" form, any quadrature order).
+//
+// When the quadrature integrates the element integrals exactly (P1: any order; P2: order
+// >= 2, whose rules are exact for the degree-2 integrands of GRAD.GRAD and of the P0 x P2
+// right-hand side) the "Gram" form is used instead: with G_pq = |T| grad(l_p)^T D grad(l_q)
+// (the 4x4 Gram matrix of the barycentric gradients) and the barycentric moments
+// E[l_p] = 1/4, E[l_p^2] = 1/10, E[l_p l_q] = 1/20, one row of the P2 element matrix in the
+// canonical column order of its row (canon_local) is a fixed combination of 4 (vertex row)
+// or 7 (edge row) entries of G, e.g. for vertex row i with others o1 < o2 < o3
+//     A(i,i) = 0.6 G_ii,  A(i,o) = -0.2 G_io,  A(i, edge(i,o)) = 0.6 G_io - 0.2 G_ii,
+//     A(i, edge(o,o')) = -0.2 (G_io + G_io')
+// so the gather needs no tables.  The values agree with the quadrature sums of fem3Dtet to
+// rounding (FP64: ~1e-15 relative).
+//
+// Phase 1 computes K or G (and f|T|) once per tet; phase 2 is a row gather: every CSR row
+// is owned by one lane, which walks the row's incident tets in ascending tet order, computes
+// that tet's row of A and adds it into a shared-memory copy of the row at the offsets held
 // by the scatter record.  Each value is therefore summed in the same order as the
 // reference's serial cell loop, without atomics, and written to HBM once, coalesced.
 #include <mutex>
+#include <type_traits>
 
 #include "anigpu_internal.h"
 #include "quad_tables.h"
 
 namespace {
 
-constexpr int kChunk = 16;  // incidences staged per group per step
 
 // ---------------------------------------------------------------- phase 1
 // FP64 -> FP32 with round-to-nearest-even in integer arithmetic.  GB300 runs FP64 (and
@@ -200,6 +213,142 @@ __global__ void tet_prepare_f32_kernel(int64_t nt, const double* __restrict__ xy
     o[1] = make_float4(K[4], K[5], K[6], K[7]);
 }
 
+// Gram form: G = |T| g^T D g for the four barycentric gradients g_0..g_3 (g_{a+1} = row a of
+// PSI, g_0 = -(g_1 + g_2 + g_3), poly_1.h), stored as G00 G11 G22 G33, then the six edges
+// G01 G02 G03 G12 G13 G23, then f|T| and 0: 12 values per tet.
+template <typename R>
+__device__ __forceinline__ void gram_from_psi(const R* PSI, const R* d, R mes, R* out) {
+    R g[4][3], Dg[4][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        g[a + 1][0] = PSI[a];
+        g[a + 1][1] = PSI[a + 3];
+        g[a + 1][2] = PSI[a + 6];
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) g[0][c] = -(g[1][c] + g[2][c] + g[3][c]);
+#pragma unroll
+    for (int p = 0; p < 4; ++p) {
+        Dg[p][0] = d[0] * g[p][0] + d[1] * g[p][1] + d[2] * g[p][2];
+        Dg[p][1] = d[1] * g[p][0] + d[3] * g[p][1] + d[4] * g[p][2];
+        Dg[p][2] = d[2] * g[p][0] + d[4] * g[p][1] + d[5] * g[p][2];
+    }
+    auto dot = [&](int p, int q) { return mes * (g[p][0] * Dg[q][0] + g[p][1] * Dg[q][1] + g[p][2] * Dg[q][2]); };
+    out[0] = dot(0, 0);
+    out[1] = dot(1, 1);
+    out[2] = dot(2, 2);
+    out[3] = dot(3, 3);
+    out[4] = dot(0, 1);
+    out[5] = dot(0, 2);
+    out[6] = dot(0, 3);
+    out[7] = dot(1, 2);
+    out[8] = dot(1, 3);
+    out[9] = dot(2, 3);
+}
+
+__global__ void tet_gram_f64_kernel(int64_t nt, const double* __restrict__ xyz, const int32_t* __restrict__ tets,
+                                    int kind, const double* __restrict__ D, const double* __restrict__ f,
+                                    double f_const, double* __restrict__ out, int* __restrict__ status) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= nt) return;
+    const int4 v = reinterpret_cast<const int4*>(tets)[t];
+    double e[9];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const double x0 = xyz[3 * (int64_t)v.x + k];
+        e[k + 0] = xyz[3 * (int64_t)v.y + k] - x0;
+        e[k + 3] = xyz[3 * (int64_t)v.z + k] - x0;
+        e[k + 6] = xyz[3 * (int64_t)v.w + k] - x0;
+    }
+    double d[6], PSI[9], G[12];
+    load_sym(kind, D, t, d);
+    const double det = inverse3(e, PSI);
+    const double mes = fabs(det) / 6.0;
+    gram_from_psi(PSI, d, mes, G);
+    G[10] = (f ? f[t] : f_const) * mes;
+    G[11] = 0;
+    bool bad = !(det != 0.0);
+#pragma unroll
+    for (int k = 0; k < 11; ++k) bad |= !isfinite(G[k]);
+    if (bad) atomicExch(status, ANIGPU_ERR_NONFINITE);
+    double2* o = reinterpret_cast<double2*>(out + 12 * t);
+#pragma unroll
+    for (int q = 0; q < 6; ++q) o[q] = make_double2(G[2 * q], G[2 * q + 1]);
+}
+
+__global__ void tet_gram_f32_kernel(int64_t nt, const double* __restrict__ xyz, const float2* __restrict__ xyz2,
+                                    const int32_t* __restrict__ tets, int kind, const double* __restrict__ D,
+                                    const double* __restrict__ f, double f_const, float* __restrict__ out,
+                                    int* __restrict__ status) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= nt) return;
+    const int4 v = reinterpret_cast<const int4*>(tets)[t];
+    float e[9];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float2 x0 = xyz2[3 * (int64_t)v.x + k];
+        const float2 x1 = xyz2[3 * (int64_t)v.y + k];
+        const float2 x2 = xyz2[3 * (int64_t)v.z + k];
+        const float2 x3 = xyz2[3 * (int64_t)v.w + k];
+        e[k + 0] = (x1.x - x0.x) + (x1.y - x0.y);
+        e[k + 3] = (x2.x - x0.x) + (x2.y - x0.y);
+        e[k + 6] = (x3.x - x0.x) + (x3.y - x0.y);
+    }
+    float d[6];
+    if (kind == ANIGPU_TENSOR_TET_SYM) {
+        const double2* Dp = reinterpret_cast<const double2*>(D + 6 * t);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const double2 w = Dp[q];
+            d[2 * q] = d2f_rn(w.x);
+            d[2 * q + 1] = d2f_rn(w.y);
+        }
+    } else {
+        const float s = kind == ANIGPU_TENSOR_NULL ? 1.f : d2f_rn(kind == ANIGPU_TENSOR_CONST_SCALAR ? D[0] : D[t]);
+        d[0] = d[3] = d[5] = s;
+        d[1] = d[2] = d[4] = 0.f;
+    }
+    const float fv = d2f_rn(f ? f[t] : f_const);
+    float PSI[9], G[12];
+    const float det = inverse3(e, PSI);
+    const float l0 = e[0] * e[0] + e[1] * e[1] + e[2] * e[2];
+    const float l1 = e[3] * e[3] + e[4] * e[4] + e[5] * e[5];
+    const float l2 = e[6] * e[6] + e[7] * e[7] + e[8] * e[8];
+    float mes;
+    if (det * det > 0.0025f * l0 * l1 * l2) {
+        mes = fabsf(det) * (1.0f / 6.0f);
+        gram_from_psi(PSI, d, mes, G);
+    } else {
+        // badly shaped (or degenerate) tet: Jacobian, inverse and Gram matrix in FP64
+        double ed[9], P64[9], dd[6], G64[10];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const double x0 = xyz[3 * (int64_t)v.x + k];
+            ed[k + 0] = xyz[3 * (int64_t)v.y + k] - x0;
+            ed[k + 3] = xyz[3 * (int64_t)v.z + k] - x0;
+            ed[k + 6] = xyz[3 * (int64_t)v.w + k] - x0;
+        }
+        load_sym(kind, D, t, dd);
+        const double det64 = inverse3(ed, P64);
+        const double mes64 = fabs(det64) / 6.0;
+        gram_from_psi(P64, dd, mes64, G64);
+#pragma unroll
+        for (int k = 0; k < 10; ++k) G[k] = (float)G64[k];
+        mes = (float)mes64;
+        if (!(det64 != 0.0)) atomicExch(status, ANIGPU_ERR_NONFINITE);
+    }
+    G[10] = fv * mes;
+    G[11] = 0.f;
+    bool bad = false;
+#pragma unroll
+    for (int k = 0; k < 11; ++k) bad |= !isfinite(G[k]);
+    if (bad) atomicExch(status, ANIGPU_ERR_NONFINITE);
+    float4* o = reinterpret_cast<float4*>(out + 12 * t);
+    o[0] = make_float4(G[0], G[1], G[2], G[3]);
+    o[1] = make_float4(G[4], G[5], G[6], G[7]);
+    o[2] = make_float4(G[8], G[9], G[10], G[11]);
+}
+
 // ---------------------------------------------------------------- phase 2
 struct RowParams {
     int64_t row_begin;  // first row of this launch
@@ -211,57 +360,110 @@ struct RowParams {
     const double* dir_bc;
     const int32_t* edofs;
     int cap;  // row buffer capacity (>= longest row)
+    int vec_ok;  // the value array is 16-byte aligned: vector stores
     double drop;
 };
 
-__device__ __forceinline__ uint32_t rec_off(const ScatterRec& r, int j) {
-    const uint32_t w = j < 4 ? r.off03 : (j < 8 ? r.off47 : (r.meta >> 16));
-    return (w >> (8 * (j & 3))) & 0xffu;
-}
 
-template <typename Real>
-struct KVec;
-template <>
-struct KVec<float> {
-    float4 a, b;
-    __device__ __forceinline__ void load(const float* p) {
-        a = reinterpret_cast<const float4*>(p)[0];
-        b = reinterpret_cast<const float4*>(p)[1];
+// per-tet block of N values (N = 8 table form, 12 Gram form), loaded with 16-byte loads
+template <typename Real, int N>
+struct KVec {
+    Real v[N];
+    __device__ __forceinline__ void load(const Real* p) {
+        if (sizeof(Real) == 4) {
+#pragma unroll
+            for (int q = 0; q < N / 4; ++q) {
+                const float4 w = reinterpret_cast<const float4*>(p)[q];
+                v[4 * q] = w.x;
+                v[4 * q + 1] = w.y;
+                v[4 * q + 2] = w.z;
+                v[4 * q + 3] = w.w;
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < N / 2; ++q) {
+                const double2 w = reinterpret_cast<const double2*>(p)[q];
+                v[2 * q] = w.x;
+                v[2 * q + 1] = w.y;
+            }
+        }
     }
-    __device__ __forceinline__ float k(int i) const {
-        return i == 0 ? a.x : i == 1 ? a.y : i == 2 ? a.z : i == 3 ? a.w : i == 4 ? b.x : i == 5 ? b.y : b.z;
+    __device__ __forceinline__ void zero() {
+#pragma unroll
+        for (int q = 0; q < N; ++q) v[q] = Real(0);
     }
-    __device__ __forceinline__ void zero() { a = b = make_float4(0.f, 0.f, 0.f, 0.f); }
 };
-template <>
-struct KVec<double> {
-    double2 a, b, c, d;
-    __device__ __forceinline__ void load(const double* p) {
-        const double2* q = reinterpret_cast<const double2*>(p);
-        a = q[0];
-        b = q[1];
-        c = q[2];
-        d = q[3];
+
+// Gram-form element rows in canonical column order (FORM 1: vertex rows, FORM 2: P2 edge
+// rows); G = K.v: G00 G11 G22 G33, G01 G02 G03 G12 G13 G23, f|T|.  Returns f|T| E[phi_i].
+template <typename Real, int NLOC, int FORM>
+__device__ __forceinline__ Real gram_row(const Real* G, int i, Real* a) {
+    const Real d0 = G[0], d1 = G[1], d2 = G[2], d3 = G[3];
+    const Real e0 = G[4], e1 = G[5], e2 = G[6], e3 = G[7], e4 = G[8], e5 = G[9];
+    if (FORM == 1) {
+        // vertex i and the others o1 < o2 < o3: G_ii, G_io1, G_io2, G_io3
+        const Real gii = i == 0 ? d0 : i == 1 ? d1 : i == 2 ? d2 : d3;
+        const Real g1 = i <= 1 ? e0 : i == 2 ? e1 : e2;
+        const Real g2 = i == 0 ? e1 : i <= 2 ? e3 : e4;
+        const Real g3 = i == 0 ? e2 : i == 1 ? e4 : e5;
+        if (NLOC == 4) {
+            a[0] = gii;
+            a[1] = g1;
+            a[2] = g2;
+            a[3] = g3;
+            return Real(0.25) * G[10];
+        } else {
+            const Real m2 = Real(-0.2), p6 = Real(0.6);
+            a[0] = p6 * gii;
+            a[1] = m2 * g1;
+            a[2] = m2 * g2;
+            a[3] = m2 * g3;
+            const Real t = m2 * gii;
+            a[4] = fma(p6, g1, t);
+            a[5] = fma(p6, g2, t);
+            a[6] = fma(p6, g3, t);
+            a[7] = m2 * (g1 + g2);
+            a[8] = m2 * (g1 + g3);
+            a[9] = m2 * (g2 + g3);
+            return Real(-0.05) * G[10];
+        }
+    } else {
+        // edge k = (a,b) with the other vertices c < d
+        const int k = i - 4;
+        const Real gaa = k <= 2 ? d0 : k <= 4 ? d1 : d2;
+        const Real gbb = k == 0 ? d1 : (k == 1 || k == 3) ? d2 : d3;
+        const Real gab = k == 0 ? e0 : k == 1 ? e1 : k == 2 ? e2 : k == 3 ? e3 : k == 4 ? e4 : e5;
+        const Real gac = (k == 0 || k == 5) ? e1 : e0;
+        const Real gad = k <= 1 ? e2 : k == 2 ? e1 : k == 3 ? e4 : e3;
+        const Real gbc = k <= 1 ? e3 : k == 2 ? e4 : k == 3 ? e1 : e2;
+        const Real gbd = (k == 0 || k == 5) ? e4 : e5;
+        const Real m2 = Real(-0.2), p6 = Real(0.6), p8 = Real(0.8), p16 = Real(1.6);
+        a[0] = fma(m2, gaa, p6 * gab);
+        a[1] = fma(m2, gbb, p6 * gab);
+        a[2] = m2 * (gac + gbc);
+        a[3] = m2 * (gad + gbd);
+        a[4] = p16 * (gaa + gbb + gab);
+        const Real sa = gaa + gab, sb = gab + gbb;
+        a[5] = fma(p8, sa + gac, p16 * gbc);
+        a[6] = fma(p8, sa + gad, p16 * gbd);
+        a[7] = fma(p8, sb + gbc, p16 * gac);
+        a[8] = fma(p8, sb + gbd, p16 * gad);
+        a[9] = p8 * ((gac + gad) + (gbc + gbd));
+        return Real(0.2) * G[10];
     }
-    __device__ __forceinline__ double k(int i) const {
-        return i == 0 ? a.x : i == 1 ? a.y : i == 2 ? b.x : i == 3 ? b.y : i == 4 ? c.x : i == 5 ? c.y : d.x;
-    }
-    __device__ __forceinline__ void zero() { a = b = c = d = make_double2(0.0, 0.0); }
-};
+}
 
 // Row gather.  One lane owns one CSR row.  It walks the row's incident tets in ascending
 // tet order (the order of the reference's serial cell loop), computes the tet's element
-// row A_t(i, 0..NLOC-1) = sum_k K_t[k] Tsym[i][j][k] in registers and adds it into its own
-// copy of the row in shared memory, lane-interleaved and rotated (see rot()).  The
-// record and the per-tet block of the next incidence are prefetched.  At the end the warp
-// writes its 32 rows cooperatively (each row contiguous, coalesced).  No atomics: every
-// CSR value is produced by exactly one lane with a fixed summation order.
-// slot s of lane l lives at s*33 + l (rows padded to 33 words): every lane touching its
-// own slot and the transposed read of one row by the whole warp are both free of bank
-// conflicts when the lanes' slots are equal (structured meshes), and at most a few-way
-// otherwise.
-__device__ __forceinline__ int rot(int s, int l) { return s * 33 + l; }
-
+// row A_t(i, .) in canonical column order in registers and adds it into the row's values in
+// shared memory at the offsets held by the scatter record.  The 32 rows of a warp are
+// consecutive, so their values are one contiguous range of the CSR value array; the warp
+// keeps that range in shared memory in CSR order (lane l's row at rowptr[row] - rowptr[row0])
+// and writes it back with one contiguous, vectorised copy.  Loads of later incidences (tet
+// ids, per-tet blocks, records) are in flight while one is computed.  A Dirichlet row does not walk
+// its incidences: applyDir makes each of its element rows e_i, so the row is zero except the
+// diagonal, which is the number of incident tets.  No atomics: every CSR value is produced by
+// exactly one lane with a fixed summation order.
 template <typename Real, int NLOC>
 struct RowTab {
     // per-i stride padded so that lanes holding different i read distinct banks
@@ -269,138 +471,196 @@ struct RowTab {
     static constexpr int SIZE = NLOC * TS + NLOC;  // then m[i]
 };
 
-template <typename Real, int NLOC, bool DIR, bool BCNZ, bool TOUCH, bool DROPCHK>
+// shared memory of one row-gather block: tables (table form), then per warp the value
+// range (32 rows of at most cap values, shifted by up to one 16-byte vector so that shared
+// and global addresses have the same alignment) and, with a touched map, its bytes
+template <typename Real, int NLOC, int FORM, bool TOUCH>
+struct RowSmem {
+    static constexpr int VEC = 16 / (int)sizeof(Real);
+    __host__ __device__ static size_t tab_bytes() { return FORM == 0 ? ((sizeof(Real) * RowTab<Real, NLOC>::SIZE + 15) / 16) * 16 : 0; }
+    __host__ __device__ static size_t chunk_bytes(int cap) { return (((size_t)32 * cap + VEC) * sizeof(Real) + 15) / 16 * 16; }
+    __host__ __device__ static size_t touch_bytes(int cap) { return TOUCH ? ((size_t)32 * cap + 16 + 15) / 16 * 16 : 0; }
+    __host__ __device__ static size_t warp_bytes(int cap) { return chunk_bytes(cap) + touch_bytes(cap); }
+    __host__ __device__ static size_t total(int cap, int warps) { return tab_bytes() + warp_bytes(cap) * warps; }
+};
+
+// prefetch depths of the row gather (per-tet blocks, records)
+#ifndef ROW_KD
+#define ROW_KD 2
+#endif
+#ifndef ROW_RD
+#define ROW_RD 4
+#endif
+
+// byte c & 3 of w, zero-extended
+__device__ __forceinline__ uint32_t byte_of(uint32_t w, int c) { return __byte_perm(w, 0u, 0x4440u + (uint32_t)(c & 3)); }
+
+// FORM 0: table form (any row kind); FORM 1: Gram form, vertex rows; FORM 2: Gram form, P2 edge rows
+template <typename Real, int NLOC, int FORM, bool DIR, bool BCNZ, bool TOUCH, bool DROPCHK>
 __global__ void __launch_bounds__(64) row_gather_kernel(RowParams p, const Real* __restrict__ tables,
                                                         const Real* __restrict__ tetK, Real* __restrict__ vals,
                                                         double* __restrict__ rhs, uint8_t* __restrict__ touched_out,
                                                         int* __restrict__ status) {
     using Tab = RowTab<Real, NLOC>;
+    using Sm = RowSmem<Real, NLOC, FORM, TOUCH>;
+    constexpr int KS = FORM == 0 ? 8 : 12;  // values per tet block
+    constexpr int VEC = Sm::VEC;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nwarps = blockDim.x >> 5;
     Real* sT = reinterpret_cast<Real*>(smem_raw);
-    // host layout [i][j][8] -> padded stride TS per i
-    for (int k = threadIdx.x; k < NLOC * NLOC * 8; k += blockDim.x) {
-        const int i = k / (NLOC * 8), rem = k - i * NLOC * 8;
-        sT[i * Tab::TS + rem] = tables[k];
+    if (FORM == 0) {
+        // host layout [i][c][8] -> padded stride TS per i
+        for (int k = threadIdx.x; k < NLOC * NLOC * 8; k += blockDim.x) {
+            const int i = k / (NLOC * 8), rem = k - i * NLOC * 8;
+            sT[i * Tab::TS + rem] = tables[k];
+        }
+        for (int k = threadIdx.x; k < NLOC; k += blockDim.x) sT[NLOC * Tab::TS + k] = tables[NLOC * NLOC * 8 + k];
+        __syncthreads();
     }
-    for (int k = threadIdx.x; k < NLOC; k += blockDim.x) sT[NLOC * Tab::TS + k] = tables[NLOC * NLOC * 8 + k];
     const Real* sM = sT + NLOC * Tab::TS;
-    const size_t tab_bytes = ((sizeof(Real) * Tab::SIZE + 15) / 16) * 16;
-    // per warp: row metadata (32 x {row start, length}), the rows, the touched map
-    const size_t meta_bytes = 32 * 16;
-    const size_t row_bytes = (((size_t)p.cap * 33 * sizeof(Real)) + 15) / 16 * 16;
-    const size_t touch_bytes = TOUCH ? (((size_t)p.cap * 33) + 15) / 16 * 16 : 0;
-    unsigned char* wbase = smem_raw + tab_bytes + (meta_bytes + row_bytes + touch_bytes) * warp;
-    longlong2* sMeta = reinterpret_cast<longlong2*>(wbase);
-    Real* sRow = reinterpret_cast<Real*>(wbase + meta_bytes);
-    uint8_t* sTouch = reinterpret_cast<uint8_t*>(wbase + meta_bytes + row_bytes);
-    // zero this warp's rows (and touched map), 16 bytes per store
-    for (size_t k = lane; k < (row_bytes + touch_bytes) / 16; k += 32)
-        reinterpret_cast<int4*>(sRow)[k] = make_int4(0, 0, 0, 0);
-
     const int64_t row0 = p.row_begin + ((int64_t)blockIdx.x * nwarps + warp) * 32;
+    if (row0 >= p.nrows) return;  // warp-uniform; no block-wide barrier follows
+    const int64_t rend = row0 + 32 < p.nrows ? row0 + 32 : p.nrows;
+    const int64_t cbase = p.rowptr[row0];
+    const int clen = (int)(p.rowptr[rend] - cbase);
+    const int shift = (int)(cbase & (VEC - 1));  // shared index s <-> global cbase + s, same alignment
+    unsigned char* wbase = smem_raw + Sm::tab_bytes() + Sm::warp_bytes(p.cap) * warp;
+    Real* sC = reinterpret_cast<Real*>(wbase) + shift;
+    uint8_t* sTouch = wbase + Sm::chunk_bytes(p.cap) + shift;
+    // zero [0, shift + clen) of this warp's range, 16 bytes per store
+    {
+        const int nvec = (shift + clen + VEC - 1) / VEC;
+        int4* z = reinterpret_cast<int4*>(wbase);
+        for (int k = lane; k < nvec; k += 32) z[k] = make_int4(0, 0, 0, 0);
+        if (TOUCH) {
+            int4* zt = reinterpret_cast<int4*>(wbase + Sm::chunk_bytes(p.cap));
+            for (int k = lane; k < (shift + clen + 15) / 16; k += 32) zt[k] = make_int4(0, 0, 0, 0);
+        }
+    }
     const int64_t row = row0 + lane;
     const bool valid = row < p.nrows;
-    int64_t ib = 0, rb = 0;
-    int len = 0, deg = 0;
+    int64_t ib = 0;
+    int deg = 0, base = 0;
     bool isdir = false;
     if (valid) {
         ib = p.inc_ptr[row];
         deg = (int)(p.inc_ptr[row + 1] - ib);
-        rb = p.rowptr[row];
-        len = (int)(p.rowptr[row + 1] - rb);
+        base = (int)(p.rowptr[row] - cbase);
         if (DIR) isdir = p.dir_mask[row] != 0;
     }
-    sMeta[lane] = make_longlong2(rb, len);
-    __syncthreads();
-    Real* myRow = sRow + lane;  // slot s at myRow[s * 33]
-    uint8_t* myTouch = sTouch + lane;
+    __syncwarp();
+    Real* myRow = sC + base;
+    uint8_t* myTouch = sTouch + base;
     const Real drop = Real(p.drop);
     Real racc = Real(0);
-    // software pipeline over the incidences: r0/K0 current, r1 next; indices are clamped
-    // to the last incidence so that the loop body has no branches
-    ScatterRec r0 = {0u, 0u, 0u, 0u}, r1 = {0u, 0u, 0u, 0u};
-    KVec<Real> K0, K1;
-    K0.zero();
-    if (deg > 0) {
-        r0 = p.recs[ib];
-        K0.load(tetK + 8 * (int64_t)r0.tet);
-        r1 = p.recs[ib + (deg > 1 ? 1 : 0)];
+    const int nloop = isdir ? 0 : deg;
+    // software pipeline over the incidences, indices clamped to the last incidence so that the
+    // loop body has no branches: per-tet blocks KD incidences ahead, records RD ahead, so that
+    // the record that addresses a block arrived RD - KD iterations before the block is requested
+    constexpr int KD = ROW_KD, RD = ROW_RD;
+    static_assert(RD > KD, "records must run ahead of the blocks they address");
+    KVec<Real, KS> Kq[KD];
+    ScatterRec Rq[RD];
+    const int last = nloop - 1;
+#pragma unroll
+    for (int j = 0; j < KD; ++j) Kq[j].zero();
+#pragma unroll
+    for (int j = 0; j < RD; ++j) Rq[j] = ScatterRec{0u, 0u, 0u, 0u};
+    if (nloop > 0) {
+#pragma unroll
+        for (int j = 0; j < RD; ++j) Rq[j] = p.recs[ib + min(j, last)];
+#pragma unroll
+        for (int j = 0; j < KD; ++j) Kq[j].load(tetK + KS * (int64_t)Rq[j].tet);
     }
-    const int last = deg - 1;
-    for (int k = 0; k < deg; ++k) {
-        K1.load(tetK + 8 * (int64_t)r1.tet);
-        const ScatterRec r2 = p.recs[ib + min(k + 2, last)];
+    for (int k = 0; k < nloop; ++k) {
+        KVec<Real, KS> Kn;
+        Kn.load(tetK + KS * (int64_t)Rq[KD].tet);
+        const ScatterRec Rn = p.recs[ib + min(k + RD, last)];
+        const ScatterRec r0 = Rq[0];
+        const KVec<Real, KS>& K0 = Kq[0];
         const int i = r0.meta & 15;
-        const Real* T = sT + i * Tab::TS;
         const uint32_t dm = DIR ? (r0.meta >> 4) & 0x3ffu : 0u;
-        const Real k0 = K0.k(0), k1 = K0.k(1), k2 = K0.k(2), k3 = K0.k(3), k4 = K0.k(4), k5 = K0.k(5);
-        Real F = K0.k(6) * sM[i];
+        Real F;
         Real a[NLOC];
-        int addr[NLOC];
-        uint32_t addbits = 0;
+        if (FORM != 0) {
+            F = gram_row<Real, NLOC, FORM>(K0.v, i, a);
+        } else {
+            const Real* T = sT + i * Tab::TS;
+            const Real k0 = K0.v[0], k1 = K0.v[1], k2 = K0.v[2], k3 = K0.v[3], k4 = K0.v[4], k5 = K0.v[5];
+            F = K0.v[6] * sM[i];
+#pragma unroll
+            for (int j = 0; j < NLOC; ++j) {
+                Real v;
+                if (sizeof(Real) == 4) {
+                    const float4 t0 = reinterpret_cast<const float4*>(T + j * 8)[0];
+                    const float4 t1 = reinterpret_cast<const float4*>(T + j * 8)[1];
+                    v = k0 * Real(t0.x);
+                    v = fma(k1, Real(t0.y), v);
+                    v = fma(k2, Real(t0.z), v);
+                    v = fma(k3, Real(t0.w), v);
+                    v = fma(k4, Real(t1.x), v);
+                    v = fma(k5, Real(t1.y), v);
+                } else {
+                    const double2 t0 = reinterpret_cast<const double2*>(T + j * 8)[0];
+                    const double2 t1 = reinterpret_cast<const double2*>(T + j * 8)[1];
+                    const double2 t2 = reinterpret_cast<const double2*>(T + j * 8)[2];
+                    v = k0 * Real(t0.x);
+                    v = fma(k1, Real(t0.y), v);
+                    v = fma(k2, Real(t1.x), v);
+                    v = fma(k3, Real(t1.y), v);
+                    v = fma(k4, Real(t2.x), v);
+                    v = fma(k5, Real(t2.y), v);
+                }
+                a[j] = v;
+            }
+        }
+        int o[NLOC];
 #pragma unroll
         for (int j = 0; j < NLOC; ++j) {
-            Real v;
-            if (sizeof(Real) == 4) {
-                const float4 t0 = reinterpret_cast<const float4*>(T + j * 8)[0];
-                const float4 t1 = reinterpret_cast<const float4*>(T + j * 8)[1];
-                v = k0 * Real(t0.x);
-                v = fma(k1, Real(t0.y), v);
-                v = fma(k2, Real(t0.z), v);
-                v = fma(k3, Real(t0.w), v);
-                v = fma(k4, Real(t1.x), v);
-                v = fma(k5, Real(t1.y), v);
-            } else {
-                const double2 t0 = reinterpret_cast<const double2*>(T + j * 8)[0];
-                const double2 t1 = reinterpret_cast<const double2*>(T + j * 8)[1];
-                const double2 t2 = reinterpret_cast<const double2*>(T + j * 8)[2];
-                v = k0 * Real(t0.x);
-                v = fma(k1, Real(t0.y), v);
-                v = fma(k2, Real(t1.x), v);
-                v = fma(k3, Real(t1.y), v);
-                v = fma(k4, Real(t2.x), v);
-                v = fma(k5, Real(t2.y), v);
-            }
+            const uint32_t w = j < 4 ? r0.off03 : (j < 8 ? r0.off47 : (r0.meta >> 16));
+            o[j] = (int)byte_of(w, j);
+            const Real v = a[j];
             const bool colDir = DIR && ((dm >> j) & 1u);
-            if (BCNZ && colDir)  // applyDir on Dirichlet column j, ascending j (dc_on_dof.h:39-45)
-                F -= v * Real(p.dir_bc[p.edofs[(int64_t)r0.tet * NLOC + j]]);
+            if (BCNZ && colDir)  // applyDir on a Dirichlet column (dc_on_dof.h:39-45), canonical order
+                F -= v * Real(p.dir_bc[p.edofs[(int64_t)r0.tet * NLOC + canon_local(NLOC, i, j)]]);
             // the drop rule |a| > drop_val (assembler.inl:416-418).  Without a touched map and
             // with a drop value that rounds to zero in FP32 the rule only skips exact zeros,
             // which cannot change a sum: that variant is compiled without the test.
-            bool add = !colDir && (!DROPCHK || fabs(v) > drop);
-            if (DIR) {  // a Dirichlet row: applyDir makes the element row e_i
-                add = isdir ? (j == i) : add;
-                v = isdir ? Real(1) : v;
-            }
+            const bool add = !colDir && (!DROPCHK || fabs(v) > drop);
             a[j] = add ? v : Real(0);
-            if (TOUCH) addbits |= (add ? 1u : 0u) << j;
-            addr[j] = (int)rec_off(r0, j) * 33;
+            if (TOUCH) myTouch[o[j]] |= (uint8_t)(add ? 1 : 0);
         }
         // the NLOC slots of one element row are distinct columns: independent updates
         Real cur[NLOC];
 #pragma unroll
-        for (int j = 0; j < NLOC; ++j) cur[j] = myRow[addr[j]];
+        for (int j = 0; j < NLOC; ++j) cur[j] = myRow[o[j]];
 #pragma unroll
-        for (int j = 0; j < NLOC; ++j) myRow[addr[j]] = cur[j] + a[j];
-        if (TOUCH) {
+        for (int j = 0; j < NLOC; ++j) myRow[o[j]] = cur[j] + a[j];
+        racc += F;
 #pragma unroll
-            for (int j = 0; j < NLOC; ++j)
-                myTouch[addr[j]] |= (uint8_t)((addbits >> j) & 1u);
-        }
-        racc += (DIR && isdir) ? Real(0) : F;
-        r0 = r1;
-        K0 = K1;
-        r1 = r2;
+        for (int j = 0; j + 1 < KD; ++j) Kq[j] = Kq[j + 1];
+        Kq[KD - 1] = Kn;
+#pragma unroll
+        for (int j = 0; j + 1 < RD; ++j) Rq[j] = Rq[j + 1];
+        Rq[RD - 1] = Rn;
     }
     bool bad = false;
     if (valid) {
         double F;
         if (DIR && isdir) {
+            // diagonal = number of incident tets (a sum of ones, exact); rhs = sum of bc over them
+            if (deg > 0) {
+                const ScatterRec rd = p.recs[ib];
+                const int dc = canon_diag(NLOC, rd.meta & 15);
+                const uint32_t w = dc < 4 ? rd.off03 : rd.off47;
+                const int od = (int)byte_of(w, dc);
+                myRow[od] = Real(deg);
+                if (TOUCH) myTouch[od] = 1;
+            }
             const double bcr = p.dir_bc[row];
             F = 0;
-            for (int q = 0; q < deg; ++q) F += bcr;  // sum of bc over the incident tets
+            for (int q = 0; q < deg; ++q) F += bcr;
         } else {
             F = (double)racc;
         }
@@ -408,19 +668,41 @@ __global__ void __launch_bounds__(64) row_gather_kernel(RowParams p, const Real*
         rhs[row] = F;
     }
     __syncwarp();
-    // cooperative write-out: row by row, all lanes, contiguous stores
-    const int64_t rem_rows = p.nrows - row0;
-    const int nrow = rem_rows < 32 ? (int)rem_rows : 32;
-    for (int w = 0; w < nrow; ++w) {
-        const longlong2 m = sMeta[w];
-        const Real* src = sRow + w;
-        for (int s = lane; s < (int)m.y; s += 32) {
-            const Real v = src[s * 33];
-            bad |= !isfinite(v);
-            vals[m.x + s] = v;
-            if (TOUCH) touched_out[m.x + s] = sTouch[s * 33 + w];
-        }
+    // contiguous write-out of the warp's value range: vectors over the aligned middle
+    Real fin = Real(0);
+    const int head = shift == 0 ? 0 : (VEC - shift < clen ? VEC - shift : clen);
+    if (lane < head) {
+        const Real v = sC[lane];
+        fin = fma(v, Real(0), fin);
+        vals[cbase + lane] = v;
     }
+    const int nbody = (clen - head) / VEC;
+    using V = typename std::conditional<sizeof(Real) == 4, float4, double2>::type;
+    const V* sv = reinterpret_cast<const V*>(sC + head);
+    V* gv = reinterpret_cast<V*>(vals + cbase + head);
+    for (int k = lane; k < (p.vec_ok ? nbody : 0); k += 32) {
+        const V v = sv[k];
+        if (sizeof(Real) == 4) {
+            const float4 f = *reinterpret_cast<const float4*>(&v);
+            fin = fma(Real(f.x), Real(0), fin);
+            fin = fma(Real(f.y), Real(0), fin);
+            fin = fma(Real(f.z), Real(0), fin);
+            fin = fma(Real(f.w), Real(0), fin);
+        } else {
+            const double2 f = *reinterpret_cast<const double2*>(&v);
+            fin = fma(Real(f.x), Real(0), fin);
+            fin = fma(Real(f.y), Real(0), fin);
+        }
+        gv[k] = v;
+    }
+    for (int k = (p.vec_ok ? head + nbody * VEC : head) + lane; k < clen; k += 32) {
+        const Real v = sC[k];
+        fin = fma(v, Real(0), fin);
+        vals[cbase + k] = v;
+    }
+    if (TOUCH)
+        for (int k = lane; k < clen; k += 32) touched_out[cbase + k] = sTouch[k];
+    bad |= !isfinite(fin);
     if (bad) atomicExch(status, ANIGPU_ERR_NONFINITE);
 }
 
@@ -451,7 +733,18 @@ __global__ void compact_fill_kernel(int64_t n, const int64_t* __restrict__ rowpt
 
 }  // namespace
 
-// host: Tsym tables and m for (space, order) in precision
+// columns of every row i of the [i][j][8] tables into the canonical order of row i
+static void to_canonical(int nf, double* T) {
+    std::vector<double> row((size_t)nf * 8);
+    for (int i = 0; i < nf; ++i) {
+        double* Ti = T + (size_t)i * nf * 8;
+        for (int c = 0; c < nf; ++c)
+            for (int k = 0; k < 8; ++k) row[(size_t)c * 8 + k] = Ti[(size_t)canon_local(nf, i, c) * 8 + k];
+        std::copy(row.begin(), row.end(), Ti);
+    }
+}
+
+// host: Tsym tables (canonical columns) and m for (space, order) in precision
 static int get_row_tables(anigpu_ctx* h, int space, int order, int precision, const void** dev) {
     const int key = 1000 * precision + 100 * space + order + 100000;
     for (auto& kv : h->basis_dev)
@@ -483,6 +776,7 @@ static int get_row_tables(anigpu_ctx* h, int space, int order, int precision, co
         for (int n = 0; n < q; ++n) s += tb.wts[n] * tb.val[(size_t)n * nf + i];
         T[(size_t)nf * nf * 8 + i] = s;
     }
+    to_canonical(nf, T.data());
     void* d = nullptr;
     if (precision == ANIGPU_F32) {
         std::vector<float> Tf(T.begin(), T.end());
@@ -497,15 +791,12 @@ static int get_row_tables(anigpu_ctx* h, int space, int order, int precision, co
     return ANIGPU_OK;
 }
 
-template <typename Real, int NLOC, bool DIR, bool BCNZ, bool TOUCH, bool DROPCHK>
+template <typename Real, int NLOC, int FORM, bool DIR, bool BCNZ, bool TOUCH, bool DROPCHK>
 static int launch_rows_t(anigpu_ctx* h, const RowParams& p, const void* tables, void* vals, double* rhs,
                          uint8_t* touched, cudaStream_t st) {
     const int warps = 2;
-    const size_t tab_bytes = ((sizeof(Real) * RowTab<Real, NLOC>::SIZE + 15) / 16) * 16;
-    const size_t row_bytes = (((size_t)p.cap * 33 * sizeof(Real)) + 15) / 16 * 16;
-    const size_t touch_bytes = TOUCH ? (((size_t)p.cap * 33) + 15) / 16 * 16 : 0;
-    const size_t smem = tab_bytes + (32 * 16 + row_bytes + touch_bytes) * warps;
-    auto kern = row_gather_kernel<Real, NLOC, DIR, BCNZ, TOUCH, DROPCHK>;
+    const size_t smem = RowSmem<Real, NLOC, FORM, TOUCH>::total(p.cap, warps);
+    auto kern = row_gather_kernel<Real, NLOC, FORM, DIR, BCNZ, TOUCH, DROPCHK>;
     ANI_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     kern<<<grid_for(p.nrows - p.row_begin, 32 * warps), 32 * warps, smem, st>>>(
         p, (const Real*)tables, (const Real*)h->tetdata, (Real*)vals, rhs, touched, h->d_status);
@@ -513,13 +804,13 @@ static int launch_rows_t(anigpu_ctx* h, const RowParams& p, const void* tables, 
     return ANIGPU_OK;
 }
 
-template <typename Real, int NLOC>
+template <typename Real, int NLOC, int FORM>
 static int launch_rows(anigpu_ctx* h, const RowParams& p, const void* tables, void* vals, double* rhs,
                        uint8_t* touched, cudaStream_t st) {
     const bool dir = h->has_dirichlet, bcnz = h->bc_nonzero, tch = touched != nullptr;
     // FP32 template assembly with a drop value that is zero in FP32 needs no drop test
     const bool dchk = tch || sizeof(Real) == 8 || (float)p.drop != 0.0f;
-#define LR(D, B, T, C) return launch_rows_t<Real, NLOC, D, B, T, C>(h, p, tables, vals, rhs, touched, st)
+#define LR(D, B, T, C) return launch_rows_t<Real, NLOC, FORM, D, B, T, C>(h, p, tables, vals, rhs, touched, st)
     if (tch) {
         if (!dir) LR(false, false, true, true);
         if (bcnz) LR(true, true, true, true);
@@ -546,11 +837,20 @@ int run_assemble(anigpu_ctx* h, int kind, const double* D, const double* f, doub
     if (kind != ANIGPU_TENSOR_NULL && !D) return set_err(h, ANIGPU_ERR_ARG, "tensor data is NULL");
     if (!vals || !rhs) return set_err(h, ANIGPU_ERR_ARG, "NULL output");
     if (precision != ANIGPU_F32 && precision != ANIGPU_F64) return set_err(h, ANIGPU_ERR_ARG, "precision");
+    // Gram form where the quadrature is exact for the element integrals, table form otherwise
+    const bool gram = h->space == ANIGPU_P1 || (h->space == ANIGPU_P2 && order >= 2);
     const void* tables = nullptr;
-    int rc = get_row_tables(h, h->space, order, precision, &tables);
-    if (rc) return rc;
+    int rc = ANIGPU_OK;
+    if (!gram) {
+        rc = get_row_tables(h, h->space, order, precision, &tables);
+        if (rc) return rc;
+    } else {
+        const double *pp, *ww;
+        int q;
+        if (!anigpu_quad_rule(order, &pp, &ww, &q)) return set_err(h, ANIGPU_ERR_UNSUPPORTED, "quadrature order");
+    }
     const size_t rsz = precision == ANIGPU_F32 ? 4 : 8;
-    const size_t need = (size_t)h->nt * 8 * rsz;
+    const size_t need = (size_t)h->nt * (gram ? 12 : 8) * rsz;
     if (h->tetdata_bytes < need) {
         if (h->tetdata) cudaFree(h->tetdata);
         h->tetdata = nullptr;
@@ -558,12 +858,20 @@ int run_assemble(anigpu_ctx* h, int kind, const double* D, const double* f, doub
         h->tetdata_bytes = need;
     }
     time_mark(h, 0);
-    if (precision == ANIGPU_F32)
+    if (gram) {
+        if (precision == ANIGPU_F32)
+            tet_gram_f32_kernel<<<grid_for(h->nt, 256), 256, 0, h->stream>>>(
+                h->nt, h->xyz, h->xyz2, h->tets, kind, D, f, f_const, (float*)h->tetdata, h->d_status);
+        else
+            tet_gram_f64_kernel<<<grid_for(h->nt, 256), 256, 0, h->stream>>>(
+                h->nt, h->xyz, h->tets, kind, D, f, f_const, (double*)h->tetdata, h->d_status);
+    } else if (precision == ANIGPU_F32) {
         tet_prepare_f32_kernel<<<grid_for(h->nt, 256), 256, 0, h->stream>>>(
             h->nt, h->xyz, h->xyz2, h->tets, kind, D, f, f_const, (float*)h->tetdata, h->d_status);
-    else
+    } else {
         tet_prepare_f64_kernel<<<grid_for(h->nt, 256), 256, 0, h->stream>>>(
             h->nt, h->xyz, h->tets, kind, D, f, f_const, (double*)h->tetdata, h->d_status);
+    }
     ANI_LAUNCHED(h);
     time_mark(h, 1);
     RowParams p;
@@ -574,6 +882,7 @@ int run_assemble(anigpu_ctx* h, int kind, const double* D, const double* f, doub
     p.dir_bc = h->dir_bc;
     p.edofs = h->edofs;
     p.drop = drop_val;
+    p.vec_ok = ((uintptr_t)vals % 16) == 0 ? 1 : 0;
     // one launch per row range (vertex rows, edge rows) so that the shared-memory row
     // buffer fits the longest row of that range; the two run concurrently (the vertex
     // range on a side stream) so that the tail of one overlaps the other
@@ -588,12 +897,24 @@ int run_assemble(anigpu_ctx* h, int kind, const double* D, const double* f, doub
         p.cap = h->row_range_cap[rg];
         if (p.nrows <= p.row_begin) continue;
         cudaStream_t st = rg == 0 ? side : h->stream;
+        const bool f32 = precision == ANIGPU_F32;
         if (h->nloc_s == 10) {
-            rc = precision == ANIGPU_F32 ? launch_rows<float, 10>(h, p, tables, vals, rhs, touched, st)
-                                         : launch_rows<double, 10>(h, p, tables, vals, rhs, touched, st);
+            if (!gram)
+                rc = f32 ? launch_rows<float, 10, 0>(h, p, tables, vals, rhs, touched, st)
+                         : launch_rows<double, 10, 0>(h, p, tables, vals, rhs, touched, st);
+            else if (rg == 0)
+                rc = f32 ? launch_rows<float, 10, 1>(h, p, tables, vals, rhs, touched, st)
+                         : launch_rows<double, 10, 1>(h, p, tables, vals, rhs, touched, st);
+            else
+                rc = f32 ? launch_rows<float, 10, 2>(h, p, tables, vals, rhs, touched, st)
+                         : launch_rows<double, 10, 2>(h, p, tables, vals, rhs, touched, st);
         } else {
-            rc = precision == ANIGPU_F32 ? launch_rows<float, 4>(h, p, tables, vals, rhs, touched, st)
-                                         : launch_rows<double, 4>(h, p, tables, vals, rhs, touched, st);
+            if (!gram)
+                rc = f32 ? launch_rows<float, 4, 0>(h, p, tables, vals, rhs, touched, st)
+                         : launch_rows<double, 4, 0>(h, p, tables, vals, rhs, touched, st);
+            else
+                rc = f32 ? launch_rows<float, 4, 1>(h, p, tables, vals, rhs, touched, st)
+                         : launch_rows<double, 4, 1>(h, p, tables, vals, rhs, touched, st);
         }
         if (rc) return rc;
     }
@@ -711,6 +1032,14 @@ bool noalloc_tables(int space, int order, double* T, int* nf_out) {
         for (int n = 0; n < q; ++n) s += ww[n] * val[n][i];
         T[(size_t)nf * nf * 8 + i] = s;
     }
+    // columns into canonical order, in place (fixed storage: one row of 10 x 8 at a time)
+    for (int i = 0; i < nf; ++i) {
+        double row[10 * 8];
+        double* Ti = T + (size_t)i * nf * 8;
+        for (int c = 0; c < nf; ++c)
+            for (int k = 0; k < 8; ++k) row[c * 8 + k] = Ti[canon_local(nf, i, c) * 8 + k];
+        for (int k = 0; k < nf * 8; ++k) Ti[k] = row[k];
+    }
     *nf_out = nf;
     return true;
 }
@@ -718,10 +1047,8 @@ bool noalloc_tables(int space, int order, double* T, int* nf_out) {
 template <typename Real, int NLOC, bool DIR, bool BCNZ, bool DROPCHK>
 int noalloc_rows(anigpu_ctx* h, const RowParams& p, const Real* tables, const Real* tetK, Real* vals, double* rhs) {
     const int warps = 2;
-    const size_t tab_bytes = ((sizeof(Real) * RowTab<Real, NLOC>::SIZE + 15) / 16) * 16;
-    const size_t row_bytes = (((size_t)p.cap * 33 * sizeof(Real)) + 15) / 16 * 16;
-    const size_t smem = tab_bytes + (32 * 16 + row_bytes) * warps;
-    auto kern = row_gather_kernel<Real, NLOC, DIR, BCNZ, false, DROPCHK>;
+    const size_t smem = RowSmem<Real, NLOC, 0, false>::total(p.cap, warps);
+    auto kern = row_gather_kernel<Real, NLOC, 0, DIR, BCNZ, false, DROPCHK>;
     ANI_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     kern<<<grid_for(p.nrows - p.row_begin, 32 * warps), 32 * warps, smem, h->stream>>>(p, tables, tetK, vals, rhs,
                                                                                         nullptr, h->d_status);
@@ -803,6 +1130,7 @@ extern "C" int anigpu_assemble_noalloc(anigpu_handle h, int tensor_kind, const d
     p.dir_bc = h->dir_bc;
     p.edofs = h->edofs;
     p.drop = drop_val;
+    p.vec_ok = ((uintptr_t)vals % 16) == 0 ? 1 : 0;
     for (int rg = 0; rg < 2; ++rg) {
         p.row_begin = h->row_range[rg];
         p.nrows = h->row_range[rg + 1];

@@ -264,8 +264,8 @@ __global__ void records_kernel(int64_t nrows, int nloc, const int64_t* __restric
     const int i = packed & 15;
     const int64_t rb = rowptr[r], re = rowptr[r + 1];
     uint32_t off[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (int j = 0; j < nloc; ++j) {
-        const int32_t c = edofs[t * nloc + j];
+    for (int j = 0; j < nloc; ++j) {  // canonical column j of row i
+        const int32_t c = edofs[t * nloc + canon_local(nloc, i, j)];
         off[j] = (uint32_t)(lower_bound_i32(col, rb, re, c) - rb);
     }
     ScatterRec rec;
@@ -276,14 +276,16 @@ __global__ void records_kernel(int64_t nrows, int nloc, const int64_t* __restric
     recs[k] = rec;
 }
 
-// Dirichlet bits of each record: bit 4+j set when local DOF j of the tet is Dirichlet
+// Dirichlet bits of each record: bit 4+c set when the DOF of canonical column c is Dirichlet
 __global__ void dirichlet_bits_kernel(int64_t nrec, int nloc, const int32_t* __restrict__ edofs,
                                       const uint8_t* __restrict__ mask, ScatterRec* __restrict__ recs) {
     const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (k >= nrec) return;
     ScatterRec rec = recs[k];
+    const int i = rec.meta & 15;
     uint32_t bits = 0;
-    for (int j = 0; j < nloc; ++j) bits |= (mask[edofs[(int64_t)rec.tet * nloc + j]] ? 1u : 0u) << j;
+    for (int c = 0; c < nloc; ++c)
+        bits |= (mask[edofs[(int64_t)rec.tet * nloc + canon_local(nloc, i, c)]] ? 1u : 0u) << c;
     rec.meta = (rec.meta & ~(0x3ffu << 4)) | (bits << 4);
     recs[k] = rec;
 }

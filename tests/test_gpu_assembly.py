@@ -45,7 +45,8 @@ def test_numbering_and_template_bit_exact(lib, restated, space, n, perturb):
     assert np.array_equal(col.cpu().numpy(), ref["col"])
 
 
-@pytest.mark.parametrize("space,kind,order", [(1, 0, 2), (1, 2, 2), (2, 3, 4), (2, 1, 4), (2, 3, 2), (2, 0, 5)])
+@pytest.mark.parametrize("space,kind,order", [(1, 0, 2), (1, 2, 2), (2, 3, 4), (2, 1, 4), (2, 3, 2), (2, 0, 5),
+                                              (2, 3, 1), (1, 3, 0)])
 def test_assembly_f64_matches_oracle(lib, restated, space, kind, order):
     import anigpu
     P = _problem(lib, restated, 4, space, 0.2, kind, order)
