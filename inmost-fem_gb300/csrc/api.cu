@@ -65,6 +65,7 @@ int anigpu_destroy(anigpu_handle h) {
     free_fcg(h);
     free_learned(h);
     void* ptrs[] = {h->xyz, h->xyz2, h->tets, h->tet_edges, h->edofs, h->inc_ptr, h->recs, h->dir_mask, h->dir_bc,
+                    h->dir_cptr, h->dir_coff,
                     h->tetdata, h->d_status, h->d_ref_tables};
     for (void* p : ptrs)
         if (p) cudaFree(p);

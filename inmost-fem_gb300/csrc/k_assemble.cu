@@ -214,8 +214,10 @@ __global__ void tet_prepare_f32_kernel(int64_t nt, const double* __restrict__ xy
 }
 
 // Gram form: G = |T| g^T D g for the four barycentric gradients g_0..g_3 (g_{a+1} = row a of
-// PSI, g_0 = -(g_1 + g_2 + g_3), poly_1.h), stored as G00 G11 G22 G33, then the six edges
-// G01 G02 G03 G12 G13 G23, then f|T| and 0: 12 values per tet.
+// PSI, g_0 = -(g_1 + g_2 + g_3), poly_1.h).  Stored: the six off-diagonal entries by local
+// edge, G01 G02 G03 G12 G13 G23, then f|T| and 0 (8 values, two 16-byte loads per tet).  The
+// diagonal is not stored: the gradients sum to zero, so G_pp = -sum_{q != p} G_pq, which
+// the row gather forms from the off-diagonal entries of the row it is computing anyway.
 template <typename R>
 __device__ __forceinline__ void gram_from_psi(const R* PSI, const R* d, R mes, R* out) {
     R g[4][3], Dg[4][3];
@@ -234,16 +236,12 @@ __device__ __forceinline__ void gram_from_psi(const R* PSI, const R* d, R mes, R
         Dg[p][2] = d[2] * g[p][0] + d[4] * g[p][1] + d[5] * g[p][2];
     }
     auto dot = [&](int p, int q) { return mes * (g[p][0] * Dg[q][0] + g[p][1] * Dg[q][1] + g[p][2] * Dg[q][2]); };
-    out[0] = dot(0, 0);
-    out[1] = dot(1, 1);
-    out[2] = dot(2, 2);
-    out[3] = dot(3, 3);
-    out[4] = dot(0, 1);
-    out[5] = dot(0, 2);
-    out[6] = dot(0, 3);
-    out[7] = dot(1, 2);
-    out[8] = dot(1, 3);
-    out[9] = dot(2, 3);
+    out[0] = dot(0, 1);
+    out[1] = dot(0, 2);
+    out[2] = dot(0, 3);
+    out[3] = dot(1, 2);
+    out[4] = dot(1, 3);
+    out[5] = dot(2, 3);
 }
 
 __global__ void tet_gram_f64_kernel(int64_t nt, const double* __restrict__ xyz, const int32_t* __restrict__ tets,
@@ -260,20 +258,20 @@ __global__ void tet_gram_f64_kernel(int64_t nt, const double* __restrict__ xyz, 
         e[k + 3] = xyz[3 * (int64_t)v.z + k] - x0;
         e[k + 6] = xyz[3 * (int64_t)v.w + k] - x0;
     }
-    double d[6], PSI[9], G[12];
+    double d[6], PSI[9], G[8];
     load_sym(kind, D, t, d);
     const double det = inverse3(e, PSI);
     const double mes = fabs(det) / 6.0;
     gram_from_psi(PSI, d, mes, G);
-    G[10] = (f ? f[t] : f_const) * mes;
-    G[11] = 0;
+    G[6] = (f ? f[t] : f_const) * mes;
+    G[7] = 0;
     bool bad = !(det != 0.0);
 #pragma unroll
-    for (int k = 0; k < 11; ++k) bad |= !isfinite(G[k]);
+    for (int k = 0; k < 7; ++k) bad |= !isfinite(G[k]);
     if (bad) atomicExch(status, ANIGPU_ERR_NONFINITE);
-    double2* o = reinterpret_cast<double2*>(out + 12 * t);
+    double2* o = reinterpret_cast<double2*>(out + 8 * t);
 #pragma unroll
-    for (int q = 0; q < 6; ++q) o[q] = make_double2(G[2 * q], G[2 * q + 1]);
+    for (int q = 0; q < 4; ++q) o[q] = make_double2(G[2 * q], G[2 * q + 1]);
 }
 
 __global__ void tet_gram_f32_kernel(int64_t nt, const double* __restrict__ xyz, const float2* __restrict__ xyz2,
@@ -309,7 +307,7 @@ __global__ void tet_gram_f32_kernel(int64_t nt, const double* __restrict__ xyz, 
         d[1] = d[2] = d[4] = 0.f;
     }
     const float fv = d2f_rn(f ? f[t] : f_const);
-    float PSI[9], G[12];
+    float PSI[9], G[8];
     const float det = inverse3(e, PSI);
     const float l0 = e[0] * e[0] + e[1] * e[1] + e[2] * e[2];
     const float l1 = e[3] * e[3] + e[4] * e[4] + e[5] * e[5];
@@ -320,7 +318,7 @@ __global__ void tet_gram_f32_kernel(int64_t nt, const double* __restrict__ xyz, 
         gram_from_psi(PSI, d, mes, G);
     } else {
         // badly shaped (or degenerate) tet: Jacobian, inverse and Gram matrix in FP64
-        double ed[9], P64[9], dd[6], G64[10];
+        double ed[9], P64[9], dd[6], G64[6];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             const double x0 = xyz[3 * (int64_t)v.x + k];
@@ -333,20 +331,19 @@ __global__ void tet_gram_f32_kernel(int64_t nt, const double* __restrict__ xyz, 
         const double mes64 = fabs(det64) / 6.0;
         gram_from_psi(P64, dd, mes64, G64);
 #pragma unroll
-        for (int k = 0; k < 10; ++k) G[k] = (float)G64[k];
+        for (int k = 0; k < 6; ++k) G[k] = (float)G64[k];
         mes = (float)mes64;
         if (!(det64 != 0.0)) atomicExch(status, ANIGPU_ERR_NONFINITE);
     }
-    G[10] = fv * mes;
-    G[11] = 0.f;
+    G[6] = fv * mes;
+    G[7] = 0.f;
     bool bad = false;
 #pragma unroll
-    for (int k = 0; k < 11; ++k) bad |= !isfinite(G[k]);
+    for (int k = 0; k < 7; ++k) bad |= !isfinite(G[k]);
     if (bad) atomicExch(status, ANIGPU_ERR_NONFINITE);
-    float4* o = reinterpret_cast<float4*>(out + 12 * t);
+    float4* o = reinterpret_cast<float4*>(out + 8 * t);
     o[0] = make_float4(G[0], G[1], G[2], G[3]);
     o[1] = make_float4(G[4], G[5], G[6], G[7]);
-    o[2] = make_float4(G[8], G[9], G[10], G[11]);
 }
 
 // ---------------------------------------------------------------- phase 2
@@ -359,18 +356,34 @@ struct RowParams {
     const uint8_t* dir_mask;
     const double* dir_bc;
     const int32_t* edofs;
+    const int64_t* dir_cptr;  // Dirichlet columns of each non-Dirichlet row ...
+    const uint8_t* dir_coff;  // ... as offsets within the row
     int cap;  // row buffer capacity (>= longest row)
     int vec_ok;  // the value array is 16-byte aligned: vector stores
     double drop;
 };
 
 
-// per-tet block of N values (N = 8 table form, 12 Gram form), loaded with 16-byte loads
+// per-tet block of N = 8 values (32-byte aligned: 32 bytes FP32, 64 bytes FP64), read with
+// 256-bit loads through the read-only path: one L1 wavefront per lane and block (FP32)
 template <typename Real, int N>
 struct KVec {
     Real v[N];
     __device__ __forceinline__ void load(const Real* p) {
-        if (sizeof(Real) == 4) {
+        if (N == 8 && sizeof(Real) == 4) {
+            float* f = reinterpret_cast<float*>(v);
+            asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                : "=f"(f[0]), "=f"(f[1]), "=f"(f[2]), "=f"(f[3]), "=f"(f[4]), "=f"(f[5]), "=f"(f[6]), "=f"(f[7])
+                : "l"(p));
+        } else if (N == 8) {
+            double* d = reinterpret_cast<double*>(v);
+            asm("ld.global.nc.v4.f64 {%0,%1,%2,%3}, [%4];"
+                : "=d"(d[0]), "=d"(d[1]), "=d"(d[2]), "=d"(d[3])
+                : "l"(p));
+            asm("ld.global.nc.v4.f64 {%0,%1,%2,%3}, [%4];"
+                : "=d"(d[4]), "=d"(d[5]), "=d"(d[6]), "=d"(d[7])
+                : "l"(p + 4));
+        } else if (sizeof(Real) == 4) {
 #pragma unroll
             for (int q = 0; q < N / 4; ++q) {
                 const float4 w = reinterpret_cast<const float4*>(p)[q];
@@ -395,23 +408,23 @@ struct KVec {
 };
 
 // Gram-form element rows in canonical column order (FORM 1: vertex rows, FORM 2: P2 edge
-// rows); G = K.v: G00 G11 G22 G33, G01 G02 G03 G12 G13 G23, f|T|.  Returns f|T| E[phi_i].
+// rows); G = K.v: G01 G02 G03 G12 G13 G23, f|T|.  The diagonal entries come from the
+// off-diagonal ones of the same row (G_pp = -sum_{q != p} G_pq).  Returns f|T| E[phi_i].
 template <typename Real, int NLOC, int FORM>
 __device__ __forceinline__ Real gram_row(const Real* G, int i, Real* a) {
-    const Real d0 = G[0], d1 = G[1], d2 = G[2], d3 = G[3];
-    const Real e0 = G[4], e1 = G[5], e2 = G[6], e3 = G[7], e4 = G[8], e5 = G[9];
+    const Real e0 = G[0], e1 = G[1], e2 = G[2], e3 = G[3], e4 = G[4], e5 = G[5];
     if (FORM == 1) {
-        // vertex i and the others o1 < o2 < o3: G_ii, G_io1, G_io2, G_io3
-        const Real gii = i == 0 ? d0 : i == 1 ? d1 : i == 2 ? d2 : d3;
+        // vertex i and the others o1 < o2 < o3: G_io1, G_io2, G_io3 and G_ii
         const Real g1 = i <= 1 ? e0 : i == 2 ? e1 : e2;
         const Real g2 = i == 0 ? e1 : i <= 2 ? e3 : e4;
         const Real g3 = i == 0 ? e2 : i == 1 ? e4 : e5;
+        const Real gii = -((g1 + g2) + g3);
         if (NLOC == 4) {
             a[0] = gii;
             a[1] = g1;
             a[2] = g2;
             a[3] = g3;
-            return Real(0.25) * G[10];
+            return Real(0.25) * G[6];
         } else {
             const Real m2 = Real(-0.2), p6 = Real(0.6);
             a[0] = p6 * gii;
@@ -425,18 +438,18 @@ __device__ __forceinline__ Real gram_row(const Real* G, int i, Real* a) {
             a[7] = m2 * (g1 + g2);
             a[8] = m2 * (g1 + g3);
             a[9] = m2 * (g2 + g3);
-            return Real(-0.05) * G[10];
+            return Real(-0.05) * G[6];
         }
     } else {
         // edge k = (a,b) with the other vertices c < d
         const int k = i - 4;
-        const Real gaa = k <= 2 ? d0 : k <= 4 ? d1 : d2;
-        const Real gbb = k == 0 ? d1 : (k == 1 || k == 3) ? d2 : d3;
         const Real gab = k == 0 ? e0 : k == 1 ? e1 : k == 2 ? e2 : k == 3 ? e3 : k == 4 ? e4 : e5;
         const Real gac = (k == 0 || k == 5) ? e1 : e0;
         const Real gad = k <= 1 ? e2 : k == 2 ? e1 : k == 3 ? e4 : e3;
         const Real gbc = k <= 1 ? e3 : k == 2 ? e4 : k == 3 ? e1 : e2;
         const Real gbd = (k == 0 || k == 5) ? e4 : e5;
+        const Real gaa = -((gab + gac) + gad);
+        const Real gbb = -((gab + gbc) + gbd);
         const Real m2 = Real(-0.2), p6 = Real(0.6), p8 = Real(0.8), p16 = Real(1.6);
         a[0] = fma(m2, gaa, p6 * gab);
         a[1] = fma(m2, gbb, p6 * gab);
@@ -449,7 +462,7 @@ __device__ __forceinline__ Real gram_row(const Real* G, int i, Real* a) {
         a[7] = fma(p8, sb + gbc, p16 * gac);
         a[8] = fma(p8, sb + gbd, p16 * gad);
         a[9] = p8 * ((gac + gad) + (gbc + gbd));
-        return Real(0.2) * G[10];
+        return Real(0.2) * G[6];
     }
 }
 
@@ -486,11 +499,26 @@ struct RowSmem {
 
 // prefetch depths of the row gather (per-tet blocks, records)
 #ifndef ROW_KD
-#define ROW_KD 2
+#define ROW_KD 3
 #endif
 #ifndef ROW_RD
-#define ROW_RD 4
+#define ROW_RD 5
 #endif
+#ifndef ROW_UNROLL
+#define ROW_UNROLL 4
+#endif
+#ifndef ROW_RED
+#define ROW_RED 0
+#endif
+constexpr int kRowUnroll = ROW_UNROLL;
+
+// records k and k+1 (k even; the record array has one record of padding at its end)
+__device__ __forceinline__ void load_rec_pair(const ScatterRec* p, ScatterRec& lo, ScatterRec& hi) {
+    asm("ld.global.nc.v8.u32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=r"(lo.tet), "=r"(lo.meta), "=r"(lo.off03), "=r"(lo.off47), "=r"(hi.tet), "=r"(hi.meta), "=r"(hi.off03),
+          "=r"(hi.off47)
+        : "l"(p));
+}
 
 // byte c & 3 of w, zero-extended
 __device__ __forceinline__ uint32_t byte_of(uint32_t w, int c) { return __byte_perm(w, 0u, 0x4440u + (uint32_t)(c & 3)); }
@@ -503,7 +531,11 @@ __global__ void __launch_bounds__(64) row_gather_kernel(RowParams p, const Real*
                                                         int* __restrict__ status) {
     using Tab = RowTab<Real, NLOC>;
     using Sm = RowSmem<Real, NLOC, FORM, TOUCH>;
-    constexpr int KS = FORM == 0 ? 8 : 12;  // values per tet block
+    constexpr int KS = 8;  // values per tet block (K or G, then f|T|)
+    // Dirichlet columns: masked per element value where the masked value is needed (the
+    // rhs update of a non-zero boundary value, the touched map); otherwise every value is
+    // added and the Dirichlet columns of the row are set to zero at the end
+    constexpr bool MASKCOLS = DIR && (BCNZ || TOUCH);
     constexpr int VEC = Sm::VEC;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -567,20 +599,28 @@ __global__ void __launch_bounds__(64) row_gather_kernel(RowParams p, const Real*
     for (int j = 0; j < KD; ++j) Kq[j].zero();
 #pragma unroll
     for (int j = 0; j < RD; ++j) Rq[j] = ScatterRec{0u, 0u, 0u, 0u};
+    // records ahead of the queue are read in aligned pairs: when the next index is even the
+    // pair is loaded and its second record kept for the following iteration
+    ScatterRec pend = ScatterRec{0u, 0u, 0u, 0u};
     if (nloop > 0) {
 #pragma unroll
         for (int j = 0; j < RD; ++j) Rq[j] = p.recs[ib + min(j, last)];
 #pragma unroll
         for (int j = 0; j < KD; ++j) Kq[j].load(tetK + KS * (int64_t)Rq[j].tet);
+        const int64_t r0i = ib + min(RD, last);
+        if (r0i & 1) pend = p.recs[r0i];
     }
+#pragma unroll kRowUnroll
     for (int k = 0; k < nloop; ++k) {
         KVec<Real, KS> Kn;
         Kn.load(tetK + KS * (int64_t)Rq[KD].tet);
-        const ScatterRec Rn = p.recs[ib + min(k + RD, last)];
+        const int64_t ridx = ib + min(k + RD, last);
+        ScatterRec Rn = pend;
+        if (!(ridx & 1)) load_rec_pair(p.recs + ridx, Rn, pend);
         const ScatterRec r0 = Rq[0];
         const KVec<Real, KS>& K0 = Kq[0];
         const int i = r0.meta & 15;
-        const uint32_t dm = DIR ? (r0.meta >> 4) & 0x3ffu : 0u;
+        const uint32_t dm = MASKCOLS ? (r0.meta >> 4) & 0x3ffu : 0u;
         Real F;
         Real a[NLOC];
         if (FORM != 0) {
@@ -621,7 +661,7 @@ __global__ void __launch_bounds__(64) row_gather_kernel(RowParams p, const Real*
             const uint32_t w = j < 4 ? r0.off03 : (j < 8 ? r0.off47 : (r0.meta >> 16));
             o[j] = (int)byte_of(w, j);
             const Real v = a[j];
-            const bool colDir = DIR && ((dm >> j) & 1u);
+            const bool colDir = MASKCOLS && ((dm >> j) & 1u);
             if (BCNZ && colDir)  // applyDir on a Dirichlet column (dc_on_dof.h:39-45), canonical order
                 F -= v * Real(p.dir_bc[p.edofs[(int64_t)r0.tet * NLOC + canon_local(NLOC, i, j)]]);
             // the drop rule |a| > drop_val (assembler.inl:416-418).  Without a touched map and
@@ -631,12 +671,18 @@ __global__ void __launch_bounds__(64) row_gather_kernel(RowParams p, const Real*
             a[j] = add ? v : Real(0);
             if (TOUCH) myTouch[o[j]] |= (uint8_t)(add ? 1 : 0);
         }
-        // the NLOC slots of one element row are distinct columns: independent updates
-        Real cur[NLOC];
+        // the NLOC slots of one element row are distinct columns: independent updates; every
+        // slot of the row belongs to this lane alone, so the order of its additions is fixed
+        if (ROW_RED && sizeof(Real) == 4) {
 #pragma unroll
-        for (int j = 0; j < NLOC; ++j) cur[j] = myRow[o[j]];
+            for (int j = 0; j < NLOC; ++j) atomicAdd(&myRow[o[j]], a[j]);
+        } else {
+            Real cur[NLOC];
 #pragma unroll
-        for (int j = 0; j < NLOC; ++j) myRow[o[j]] = cur[j] + a[j];
+            for (int j = 0; j < NLOC; ++j) cur[j] = myRow[o[j]];
+#pragma unroll
+            for (int j = 0; j < NLOC; ++j) myRow[o[j]] = cur[j] + a[j];
+        }
         racc += F;
 #pragma unroll
         for (int j = 0; j + 1 < KD; ++j) Kq[j] = Kq[j + 1];
@@ -663,6 +709,8 @@ __global__ void __launch_bounds__(64) row_gather_kernel(RowParams p, const Real*
             for (int q = 0; q < deg; ++q) F += bcr;
         } else {
             F = (double)racc;
+            if (DIR && !MASKCOLS)
+                for (int64_t q = p.dir_cptr[row]; q < p.dir_cptr[row + 1]; ++q) myRow[p.dir_coff[q]] = Real(0);
         }
         bad |= !isfinite(F);
         rhs[row] = F;
@@ -850,7 +898,7 @@ int run_assemble(anigpu_ctx* h, int kind, const double* D, const double* f, doub
         if (!anigpu_quad_rule(order, &pp, &ww, &q)) return set_err(h, ANIGPU_ERR_UNSUPPORTED, "quadrature order");
     }
     const size_t rsz = precision == ANIGPU_F32 ? 4 : 8;
-    const size_t need = (size_t)h->nt * (gram ? 12 : 8) * rsz;
+    const size_t need = (size_t)h->nt * 8 * rsz;
     if (h->tetdata_bytes < need) {
         if (h->tetdata) cudaFree(h->tetdata);
         h->tetdata = nullptr;
@@ -883,6 +931,8 @@ int run_assemble(anigpu_ctx* h, int kind, const double* D, const double* f, doub
     p.edofs = h->edofs;
     p.drop = drop_val;
     p.vec_ok = ((uintptr_t)vals % 16) == 0 ? 1 : 0;
+    p.dir_cptr = h->dir_cptr;
+    p.dir_coff = h->dir_coff;
     // one launch per row range (vertex rows, edge rows) so that the shared-memory row
     // buffer fits the longest row of that range; the two run concurrently (the vertex
     // range on a side stream) so that the tail of one overlaps the other
@@ -1131,6 +1181,8 @@ extern "C" int anigpu_assemble_noalloc(anigpu_handle h, int tensor_kind, const d
     p.edofs = h->edofs;
     p.drop = drop_val;
     p.vec_ok = ((uintptr_t)vals % 16) == 0 ? 1 : 0;
+    p.dir_cptr = h->dir_cptr;
+    p.dir_coff = h->dir_coff;
     for (int rg = 0; rg < 2; ++rg) {
         p.row_begin = h->row_range[rg];
         p.nrows = h->row_range[rg + 1];
