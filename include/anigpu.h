@@ -170,6 +170,17 @@ int anigpu_assemble(anigpu_handle h, int tensor_kind, const double* D, const dou
 int anigpu_assemble_noalloc(anigpu_handle h, int tensor_kind, const double* D, const double* f, double f_const,
                             int order, int precision, void* vals, double* rhs, double drop_val);
 
+/* anigpu_assemble without the wait: the kernels are enqueued on the handle's stream and the
+ * call returns (no counterpart in the reference, whose Assemble is synchronous).  Argument
+ * errors are returned at once; a non-finite value is recorded on the device and reported by
+ * the next anigpu_status, so that back-to-back assemblies (or a CUDA graph of them) keep
+ * the GPU busy.  The caller keeps D, f, vals, rhs and touched alive until the stream passes. */
+int anigpu_assemble_async(anigpu_handle h, int tensor_kind, const double* D, const double* f, double f_const,
+                          int order, int precision, void* vals, double* rhs, uint8_t* touched, double drop_val);
+/* waits for the handle's stream; ANIGPU_ERR_NONFINITE (and clears it) when an assembly since
+ * the last check met a non-finite value, else ANIGPU_OK */
+int anigpu_status(anigpu_handle h);
+
 /* the drop-rule pattern (assembler without template): keep touched slots and the diagonal
  * (set_elements_on_matrix_diagonal, assembler.inl:114-135).  In-place on rowptr/col/vals;
  * returns the new nnz through nnz_out. */

@@ -59,6 +59,8 @@ SIGNATURES = {
     "anigpu_dof_coords": (_i, [_vp, _vp]),
     "anigpu_set_dirichlet": (_i, [_vp, _vp, _vp]),
     "anigpu_assemble": (_i, [_vp, _i, _vp, _vp, _d, _i, _i, _vp, _vp, _vp, _d]),
+    "anigpu_assemble_async": (_i, [_vp, _i, _vp, _vp, _d, _i, _i, _vp, _vp, _vp, _d]),
+    "anigpu_status": (_i, [_vp]),
     "anigpu_assemble_noalloc": (_i, [_vp, _i, _vp, _vp, _d, _i, _i, _vp, _vp, _d]),
     "anigpu_csr_compact": (_i, [_vp, _vp, _vp, _vp, _i, _vp, ctypes.POINTER(_i64)]),
     "anigpu_solve": (_i, [_vp, _i, _vp, _i, _vp, _vp, _d, _i64, ctypes.POINTER(SolveStats)]),
@@ -315,8 +317,9 @@ class Anigpu:
 
     @_streamed
     def assemble(self, kind=TENSOR_NULL, D=None, f=None, f_const=1.0, order=2, precision=F64, vals=None, rhs=None,
-                 touched=False, drop=1e-100):
-        """AssemblerT::Assemble: returns (vals[nnz], rhs[ndof], touched[nnz] or None)."""
+                 touched=False, drop=1e-100, sync=True):
+        """AssemblerT::Assemble: returns (vals[nnz], rhs[ndof], touched[nnz] or None).  With
+        sync=False the kernels are only enqueued; status() reports a non-finite value later."""
         torch = self.torch
         dev = f"cuda:{self.device}"
         dt = torch.float64 if precision == F64 else torch.float32
@@ -327,9 +330,17 @@ class Anigpu:
         tch = torch.empty(self.nnz, dtype=torch.uint8, device=dev) if touched else None
         Dd = self._dev(D, torch.float64) if D is not None else None
         fd = self._dev(f, torch.float64) if f is not None else None
-        self._check(self.lib.anigpu_assemble(self.h, kind, _ptr(Dd), _ptr(fd), float(f_const), order, precision,
-                                             _ptr(vals), _ptr(rhs), _ptr(tch), float(drop)))
+        fn = self.lib.anigpu_assemble if sync else self.lib.anigpu_assemble_async
+        self._check(fn(self.h, kind, _ptr(Dd), _ptr(fd), float(f_const), order, precision, _ptr(vals), _ptr(rhs),
+                       _ptr(tch), float(drop)))
+        if not sync:
+            self._keep = (Dd, fd)  # inputs stay alive until the enqueued kernels have read them
         return vals, rhs, tch
+
+    def status(self):
+        """Waits for the handle's stream; raises AnigpuError on a non-finite value recorded
+        by an assembly since the last check."""
+        self._check(self.lib.anigpu_status(self.h))
 
     @_streamed
     def csr_compact(self, rowptr, col, vals, precision, touched):

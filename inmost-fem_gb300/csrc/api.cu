@@ -256,6 +256,26 @@ int anigpu_assemble(anigpu_handle h, int tensor_kind, const double* D, const dou
     return ANIGPU_OK;
 }
 
+int anigpu_assemble_async(anigpu_handle h, int tensor_kind, const double* D, const double* f, double f_const,
+                          int order, int precision, void* vals, double* rhs, uint8_t* touched, double drop_val) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    return run_assemble(h, tensor_kind, D, f, f_const, order, precision, vals, rhs, touched, drop_val);
+}
+
+int anigpu_status(anigpu_handle h) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    int st = 0;
+    ANI_CUDA(h, cudaMemcpyAsync(&st, h->d_status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    ANI_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (st) {
+        ANI_CUDA(h, cudaMemsetAsync(h->d_status, 0, sizeof(int), h->stream));
+        return set_err(h, st, "non-finite value in assembly (AssemblerT status -1)");
+    }
+    return ANIGPU_OK;
+}
+
 int anigpu_csr_compact(anigpu_handle h, int64_t* rowptr, int32_t* col, void* vals, int precision,
                        const uint8_t* touched, int64_t* nnz_out) {
     CHECK_H(h);

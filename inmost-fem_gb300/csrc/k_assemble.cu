@@ -845,7 +845,12 @@ static int launch_rows_t(anigpu_ctx* h, const RowParams& p, const void* tables, 
     const int warps = 2;
     const size_t smem = RowSmem<Real, NLOC, FORM, TOUCH>::total(p.cap, warps);
     auto kern = row_gather_kernel<Real, NLOC, FORM, DIR, BCNZ, TOUCH, DROPCHK>;
-    ANI_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    static int smem_set[64] = {};  // per device: the largest dynamic shared memory set so far
+    const int slot = h->device >= 0 && h->device < 64 ? h->device : 0;
+    if ((int)smem > smem_set[slot]) {
+        ANI_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        smem_set[slot] = (int)smem;
+    }
     kern<<<grid_for(p.nrows - p.row_begin, 32 * warps), 32 * warps, smem, st>>>(
         p, (const Real*)tables, (const Real*)h->tetdata, (Real*)vals, rhs, touched, h->d_status);
     ANI_LAUNCHED(h);

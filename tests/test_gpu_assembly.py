@@ -176,3 +176,21 @@ def test_spmv_matches_oracle(lib, restated):
     ref = P["ref"]
     yo = restated.spmv(ref["rowptr"], ref["col"], ref["vals"], xx)
     assert np.abs(y - yo).max() <= 1e-12 * np.abs(yo).max()
+
+
+def test_async_assembly_and_status(lib, restated):
+    """anigpu_assemble_async enqueues without waiting; anigpu_status reports (and clears) a
+    non-finite value met by any assembly since the last check."""
+    import anigpu
+    P = _problem(lib, restated, 4, 2, 0.2, anigpu.TENSOR_TET_SYM, 4)
+    v_sync, r_sync, _ = lib.assemble(anigpu.TENSOR_TET_SYM, P["D"], None, 1.0, 4, anigpu.F32)
+    v_async, r_async, _ = lib.assemble(anigpu.TENSOR_TET_SYM, P["D"], None, 1.0, 4, anigpu.F32, sync=False)
+    lib.status()
+    assert bool((v_sync == v_async).all()) and bool((r_sync == r_async).all())
+    D = P["D"].copy()
+    D[3, 0] = np.inf  # injected on the host
+    lib.assemble(anigpu.TENSOR_TET_SYM, D, None, 1.0, 4, anigpu.F32, sync=False)  # returns at once
+    with pytest.raises(anigpu.AnigpuError) as e:
+        lib.status()
+    assert e.value.code == anigpu.ERR_NONFINITE
+    lib.status()  # cleared
