@@ -40,7 +40,7 @@ UNIT = "tets/s"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=64, help="cubes per axis (64 -> 1,572,864 tets)")
@@ -79,10 +79,15 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            # the timed region starts only once the sampler is producing samples
+            t0 = time.time()
+            while not self.lines and time.time() - t0 < 10 and self.proc.poll() is None:
+                time.sleep(0.01)
+            self.lines.clear()
         except Exception:
             self.proc = None
         return self
@@ -247,36 +252,58 @@ def run_ours(args):
             traffic = None
 
     # end to end through the public API with host buffers: H2D of the step's inputs
-    # (coordinates and tensors, pinned), assembly, D2H of the matrix values and rhs
+    # (coordinates and tensors, pinned), assembly, D2H of the matrix values and rhs.  Steps are
+    # pipelined over two buffer sets: the uploads of step k+1 and the downloads of step k-1
+    # run on their own streams (copy engines) while step k assembles; every step still copies
+    # its own inputs up and its own result down.
     xyz_h = torch.tensor(xyz).pin_memory()
     D_h = torch.tensor(D6).pin_memory()
-    vals_h = torch.empty(nnz, dtype=torch.float32).pin_memory()
-    rhs_h = torch.empty(ndof, dtype=torch.float64).pin_memory()
-    xyz_d = torch.empty_like(xyz_h, device=dev)
-    D_d2 = torch.empty_like(D_h, device=dev)
+    vals_h = [torch.empty(nnz, dtype=torch.float32).pin_memory() for _ in range(2)]
+    rhs_h = [torch.empty(ndof, dtype=torch.float64).pin_memory() for _ in range(2)]
+    xyz_d = [torch.empty_like(xyz_h, device=dev) for _ in range(2)]
+    D_d2 = [torch.empty_like(D_h, device=dev) for _ in range(2)]
+    vals_o = [vals32, torch.empty_like(vals32)]
+    rhs_o = [rhs, torch.empty_like(rhs)]
     h2d = xyz_h.numel() * 8 + D_h.numel() * 8
     d2h = nnz * 4 + ndof * 8
+    up, down = torch.cuda.Stream(device=dev), torch.cuda.Stream(device=dev)
+    mk = lambda: [torch.cuda.Event() for _ in range(2)]  # noqa: E731
+    in_ready, in_free, out_ready, out_free = mk(), mk(), mk(), mk()
 
-    def e2e_step():
+    def e2e_step(k):
+        b = k & 1
+        with torch.cuda.stream(up):
+            if k >= 2:
+                up.wait_event(in_free[b])
+            xyz_d[b].copy_(xyz_h, non_blocking=True)
+            D_d2[b].copy_(D_h, non_blocking=True)
+            in_ready[b].record(up)
         with torch.cuda.stream(stream):
-            xyz_d.copy_(xyz_h, non_blocking=True)
-            D_d2.copy_(D_h, non_blocking=True)
-        lib.update_coords(xyz_d)
-        lib.assemble(anigpu.TENSOR_TET_SYM, D_d2, None, 1.0, 4, anigpu.F32, vals32, rhs)
-        with torch.cuda.stream(stream):
-            vals_h.copy_(vals32, non_blocking=True)
-            rhs_h.copy_(rhs, non_blocking=True)
+            stream.wait_event(in_ready[b])
+            if k >= 2:
+                stream.wait_event(out_free[b])
+            lib.update_coords(xyz_d[b])
+            lib.assemble(anigpu.TENSOR_TET_SYM, D_d2[b], None, 1.0, 4, anigpu.F32, vals_o[b], rhs_o[b], sync=False)
+            in_free[b].record(stream)
+            out_ready[b].record(stream)
+        with torch.cuda.stream(down):
+            down.wait_event(out_ready[b])
+            vals_h[b].copy_(vals_o[b], non_blocking=True)
+            rhs_h[b].copy_(rhs_o[b], non_blocking=True)
+            out_free[b].record(down)
 
-    for _ in range(3):
-        e2e_step()
+    for k in range(4):
+        e2e_step(k)
+    lib.status()
     torch.cuda.synchronize()
-    ee = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(up)
     for k in range(args.steps):
-        ee[k][0].record(stream)
-        e2e_step()
-        ee[k][1].record(stream)
+        e2e_step(k)
+    e1.record(down)
+    lib.status()
     torch.cuda.synchronize()
-    e2e_ms = float(np.mean([a.elapsed_time(b) for a, b in ee]))
+    e2e_ms = e0.elapsed_time(e1) / args.steps
     if pg:
         t = torch.tensor([e2e_ms], device=dev)
         pg.all_reduce(t, op=pg.ReduceOp.MAX)
