@@ -15,7 +15,7 @@ WEIGHTS_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights"
 DEFAULT_WEIGHTS = os.path.join(WEIGHTS_DIR, "p2_aniso_l4.npy")
 
 
-def training_pairs(lib, vals, b, ks=(0, 1, 2, 4, 8, 16, 32, 64, 128), rtol=1e-10):
+def training_pairs(lib, vals, b, ks=(0, 1, 2, 4, 8, 16, 32, 64, 128, 256), rtol=1e-10):
     """Pairs (r_k, x* - x_k) for Jacobi-PCG iterates x_k of A x = b (FP32 values)."""
     torch = lib.torch
     b = lib._dev(b, torch.float64)
@@ -72,15 +72,16 @@ def load_default(prec):
 def main(argv=None):
     """Train the default parameters on seeded synthetic P2 problems (perturbed Kuhn cube,
     anisotropic per-tet tensors with log-normal eigenvalues) and save them:
-        python -m anigpu.learned --n 12 --systems 24 --steps 1500 --out weights/p2_aniso_l4.npy"""
+        python -m anigpu.learned --n 12 --systems 200 --steps 2000 --out weights/p2_aniso_l4.npy
+    (200 systems x 10 Jacobi-PCG iterates = 2,000 residual/correction pairs)"""
     import argparse
     import time
 
     from anigpu import meshgen
     ap = argparse.ArgumentParser()
     ap.add_argument("--n", type=int, default=12)
-    ap.add_argument("--systems", type=int, default=24)
-    ap.add_argument("--steps", type=int, default=1500)
+    ap.add_argument("--systems", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--lr", type=float, default=3e-3)
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--out", default=DEFAULT_WEIGHTS)

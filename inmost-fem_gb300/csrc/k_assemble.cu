@@ -510,6 +510,11 @@ struct RowSmem {
 #ifndef ROW_RED
 #define ROW_RED 0
 #endif
+#ifdef ROW_MINB
+#define ROW_BOUNDS __launch_bounds__(64, ROW_MINB)
+#else
+#define ROW_BOUNDS __launch_bounds__(64)
+#endif
 constexpr int kRowUnroll = ROW_UNROLL;
 
 // records k and k+1 (k even; the record array has one record of padding at its end)
@@ -525,7 +530,7 @@ __device__ __forceinline__ uint32_t byte_of(uint32_t w, int c) { return __byte_p
 
 // FORM 0: table form (any row kind); FORM 1: Gram form, vertex rows; FORM 2: Gram form, P2 edge rows
 template <typename Real, int NLOC, int FORM, bool DIR, bool BCNZ, bool TOUCH, bool DROPCHK>
-__global__ void __launch_bounds__(64) row_gather_kernel(RowParams p, const Real* __restrict__ tables,
+__global__ void ROW_BOUNDS row_gather_kernel(RowParams p, const Real* __restrict__ tables,
                                                         const Real* __restrict__ tetK, Real* __restrict__ vals,
                                                         double* __restrict__ rhs, uint8_t* __restrict__ touched_out,
                                                         int* __restrict__ status) {
