@@ -222,6 +222,29 @@ int anigpu_gnn_coefficients(anigpu_handle h, float* coef);
 int anigpu_gnn_loss_grad(anigpu_handle h, const double* r, const double* e, double* loss_host);
 int anigpu_gnn_adam(anigpu_handle h, float lr, float beta1, float beta2, float eps, int step, float grad_scale);
 
+/* ---- batched uneven instances (no counterpart in the reference, which assembles and solves one
+ * mesh at a time: examples/tutorials/ex1.cpp:120-163).  Upload the disjoint union of the meshes
+ * (vertex and tet ids offset per instance) with anigpu_mesh_upload, set it up and its Dirichlet DOFs
+ * as one problem, then
+ *   set_instances: tet_offsets (host, ninst+1, from 0 to nt) give the tets of each instance; builds the
+ *     DOF -> instance map and the row tiles (each within one instance), and autotunes the solver's
+ *     lanes per CSR row on vals_for_tuning (F64 values of this template; NULL skips the tuning);
+ *   info: number of tiles, chosen lanes per row, the timings of the candidates 2, 4, 8, 16 (ms), and
+ *     whether the last run looped on the device (1) or was driven from the host (0);
+ *   run: the whole job as one CUDA graph launch where the toolkit has conditional graph nodes:
+ *     the F64 assembly into vals (when rhs_assembled is not NULL; tensor kind and data as
+ *     anigpu_assemble), then Jacobi-PCG from x = 0 on every instance at once with per-instance
+ *     scalars and convergence (||b_i - A_i x_i|| <= rtol ||b_i||, FP64), looping on the device until
+ *     every instance has converged or maxit iterations were taken.  b and x are f64[ndof]; stats
+ *     (host, ninst) receive per instance: iterations, iterations of the whole batch, FP64 true
+ *     relative residual, seconds of the whole job.  Returns ANIGPU_ERR_NOT_CONVERGED when an
+ *     instance missed the tolerance. */
+int anigpu_batch_set_instances(anigpu_handle h, int ninst, const int64_t* tet_offsets, const double* vals_for_tuning);
+int anigpu_batch_info(anigpu_handle h, int* ntiles, int* lanes_per_row, float* tune_ms, int* device_loop);
+int anigpu_batch_run(anigpu_handle h, int tensor_kind, const double* D, const double* f, double f_const, int order,
+                     double* vals, double* rhs_assembled, const double* b, double* x, double rtol, int64_t maxit,
+                     anigpu_solve_stats* stats);
+
 /* y = A x on the handle's template (F64 or F32 values, f64 vectors) */
 int anigpu_spmv(anigpu_handle h, const void* vals, int precision, const double* x, double* y);
 

@@ -65,6 +65,9 @@ SIGNATURES = {
     "anigpu_csr_compact": (_i, [_vp, _vp, _vp, _vp, _i, _vp, ctypes.POINTER(_i64)]),
     "anigpu_solve": (_i, [_vp, _i, _vp, _i, _vp, _vp, _d, _i64, ctypes.POINTER(SolveStats)]),
     "anigpu_spmv": (_i, [_vp, _vp, _i, _vp, _vp]),
+    "anigpu_batch_set_instances": (_i, [_vp, _i, _vp, _vp]),
+    "anigpu_batch_info": (_i, [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i), _vp, ctypes.POINTER(_i)]),
+    "anigpu_batch_run": (_i, [_vp, _i, _vp, _vp, _d, _i, _vp, _vp, _vp, _vp, _d, _i64, _vp]),
     "anigpu_gnn_init": (_i, [_vp, _i, _i, ctypes.c_uint64]),
     "anigpu_gnn_num_params": (_i64, [_vp]),
     "anigpu_gnn_get_params": (_i, [_vp, _vp, _i64]),
@@ -336,6 +339,45 @@ class Anigpu:
         if not sync:
             self._keep = (Dd, fd)  # inputs stay alive until the enqueued kernels have read them
         return vals, rhs, tch
+
+    # -------------------------------------------------------------- batched instances
+    @_streamed
+    def batch_set_instances(self, tet_offsets, vals_for_tuning=None):
+        """The uploaded mesh is the disjoint union of instances; tet_offsets[i]..tet_offsets[i+1]
+        are the tets of instance i.  Builds the instance map and tiles, autotunes on the values."""
+        import numpy as np
+        toff = np.ascontiguousarray(tet_offsets, dtype=np.int64)
+        self.ninst = toff.size - 1
+        self._check(self.lib.anigpu_batch_set_instances(self.h, self.ninst, toff.ctypes.data, _ptr(vals_for_tuning)))
+
+    def batch_info(self):
+        import numpy as np
+        nt, lanes, loop = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        ms = np.zeros(4, dtype=np.float32)
+        self._check(self.lib.anigpu_batch_info(self.h, ctypes.byref(nt), ctypes.byref(lanes), ms.ctypes.data,
+                                               ctypes.byref(loop)))
+        return dict(ntiles=nt.value, lanes_per_row=lanes.value, tune_ms=ms.tolist(), device_loop=loop.value)
+
+    @_streamed
+    def batch_run(self, b, kind=TENSOR_NULL, D=None, f=None, f_const=1.0, order=2, vals=None, assemble=True,
+                  rtol=1e-8, maxit=100000, check=True):
+        """Assemble (FP64, into vals) and solve every instance by Jacobi-PCG in one graph launch.
+        Returns (x, vals, stats[ninst])."""
+        torch = self.torch
+        dev = f"cuda:{self.device}"
+        if vals is None:
+            vals = torch.empty(self.nnz, dtype=torch.float64, device=dev)
+        rhs = torch.empty(self.ndof, dtype=torch.float64, device=dev) if assemble else None
+        b = self._dev(b, torch.float64)
+        x = torch.empty_like(b)
+        Dd = self._dev(D, torch.float64) if D is not None else None
+        fd = self._dev(f, torch.float64) if f is not None else None
+        st = (SolveStats * self.ninst)()
+        rc = self.lib.anigpu_batch_run(self.h, kind, _ptr(Dd), _ptr(fd), float(f_const), order, _ptr(vals), _ptr(rhs),
+                                       _ptr(b), _ptr(x), float(rtol), int(maxit), ctypes.cast(st, ctypes.c_void_p))
+        if check:
+            self._check(rc)
+        return x, vals, list(st)
 
     def status(self):
         """Waits for the handle's stream; raises AnigpuError on a non-finite value recorded

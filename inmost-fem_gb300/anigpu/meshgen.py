@@ -123,3 +123,15 @@ def random_tets(nt, seed=3, scale=1.0):
     off[:, 2, 1] += 0.6 * scale
     off[:, 3, 2] += 0.6 * scale
     return np.ascontiguousarray((base + off).reshape(nt, 12))
+
+
+def union(meshes):
+    """Disjoint union of meshes [(xyz, tets), ...]: concatenated coordinates, tets with vertex ids
+    offset per mesh, and the tet offsets of the meshes (len(meshes) + 1)."""
+    xs, ts, toff, voff = [], [], [0], 0
+    for xyz, tets in meshes:
+        xs.append(np.asarray(xyz, dtype=np.float64))
+        ts.append(np.asarray(tets, dtype=np.int32) + voff)
+        voff += xyz.shape[0]
+        toff.append(toff[-1] + tets.shape[0])
+    return np.concatenate(xs), np.concatenate(ts), np.asarray(toff, dtype=np.int64)

@@ -114,6 +114,7 @@ struct anigpu_ctx {
     size_t solve_ws_bytes = 0;
     void* learned = nullptr;       // learned preconditioner state
     void* fcg_ws = nullptr;        // flexible-CG workspace and its captured graphs
+    void* batch_ws = nullptr;      // batched-instances map, tiles and solver workspace
 
     // per-phase timing (anigpu_set_timing)
     bool timing = false;
@@ -192,3 +193,9 @@ int run_spmv(anigpu_ctx* h, const void* vals, int precision, const double* x, do
 int run_solve(anigpu_ctx* h, int method, const void* vals, int precision, const double* b, double* x, double rtol,
               int64_t maxit, anigpu_solve_stats* st);
 void free_solver(anigpu_ctx* h);
+// batched instances (k_batch.cu)
+void free_batch(anigpu_ctx* h);
+int batch_set_instances(anigpu_ctx* h, int ninst, const int64_t* toff_host, const void* vals_for_tuning);
+int batch_info(anigpu_ctx* h, int* ntiles, int* lanes, float* tune_ms, int* device_loop);
+int batch_run(anigpu_ctx* h, int kind, const double* D, const double* f, double f_const, int order, double* vals,
+              double* rhs_assembled, const double* b, double* x, double rtol, int64_t maxit, anigpu_solve_stats* st);

@@ -64,6 +64,7 @@ int anigpu_destroy(anigpu_handle h) {
     free_solver(h);
     free_fcg(h);
     free_learned(h);
+    free_batch(h);
     void* ptrs[] = {h->xyz, h->xyz2, h->tets, h->tet_edges, h->edofs, h->inc_ptr, h->recs, h->dir_mask, h->dir_bc,
                     h->dir_cptr, h->dir_coff,
                     h->tetdata, h->d_status, h->d_ref_tables};
@@ -152,6 +153,7 @@ int anigpu_mesh_upload(anigpu_handle h, int64_t nv, const double* xyz, int64_t n
         return set_err(h, ANIGPU_ERR_UNSUPPORTED, "mesh too large for 32-bit vertex / 27-bit tet ids");
     cudaSetDevice(h->device);
     learned_invalidate(h);  // bindings and captured solver graphs refer to the old mesh
+    free_batch(h);
     int rc = dev_alloc(h, &h->xyz, (size_t)nv * 3);
     if (rc) return rc;
     rc = dev_alloc(h, &h->tets, (size_t)nt * 4);
@@ -182,6 +184,7 @@ int anigpu_problem_setup(anigpu_handle h, int space) {
     CHECK_H(h);
     cudaSetDevice(h->device);
     learned_invalidate(h);
+    free_batch(h);
     return setup_problem(h, space);
 }
 
@@ -261,6 +264,25 @@ int anigpu_assemble_async(anigpu_handle h, int tensor_kind, const double* D, con
     CHECK_H(h);
     cudaSetDevice(h->device);
     return run_assemble(h, tensor_kind, D, f, f_const, order, precision, vals, rhs, touched, drop_val);
+}
+
+int anigpu_batch_set_instances(anigpu_handle h, int ninst, const int64_t* tet_offsets, const double* vals_for_tuning) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    return batch_set_instances(h, ninst, tet_offsets, vals_for_tuning);
+}
+
+int anigpu_batch_info(anigpu_handle h, int* ntiles, int* lanes_per_row, float* tune_ms, int* device_loop) {
+    CHECK_H(h);
+    return batch_info(h, ntiles, lanes_per_row, tune_ms, device_loop);
+}
+
+int anigpu_batch_run(anigpu_handle h, int tensor_kind, const double* D, const double* f, double f_const, int order,
+                     double* vals, double* rhs_assembled, const double* b, double* x, double rtol, int64_t maxit,
+                     anigpu_solve_stats* stats) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    return batch_run(h, tensor_kind, D, f, f_const, order, vals, rhs_assembled, b, x, rtol, maxit, stats);
 }
 
 int anigpu_status(anigpu_handle h) {
