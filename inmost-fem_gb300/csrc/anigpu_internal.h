@@ -97,7 +97,7 @@ struct anigpu_ctx {
     uint8_t* dir_mask = nullptr;   // ndof
     double* dir_bc = nullptr;      // ndof
     int64_t* dir_cptr = nullptr;   // nds+1: per non-Dirichlet scalar row, its Dirichlet columns ...
-    uint8_t* dir_coff = nullptr;   // ... as offsets within the row (ascending)
+    uint16_t* dir_coff = nullptr;  // ... as offsets within the row (ascending)
     bool bc_nonzero = false;
     bool has_dirichlet = false;
     int order_assembled = -1;

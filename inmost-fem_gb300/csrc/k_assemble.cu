@@ -357,7 +357,7 @@ struct RowParams {
     const double* dir_bc;
     const int32_t* edofs;
     const int64_t* dir_cptr;  // Dirichlet columns of each non-Dirichlet row ...
-    const uint8_t* dir_coff;  // ... as offsets within the row
+    const uint16_t* dir_coff;  // ... as offsets within the row
     int cap;  // row buffer capacity (>= longest row)
     int vec_ok;  // the value array is 16-byte aligned: vector stores
     double drop;
@@ -759,6 +759,342 @@ __global__ void ROW_BOUNDS row_gather_kernel(RowParams p, const Real* __restrict
     if (bad) atomicExch(status, ANIGPU_ERR_NONFINITE);
 }
 
+// ---------------------------------------------------------------- vector P2 (linear elasticity)
+// Operator<GRAD, FemVec<3, FEM_P2>> with the isotropic Lame tensor
+//     D[(j,c),(l,d)] = lambda delta_jc delta_ld + mu (delta_cd delta_jl + delta_cl delta_jd)
+// (gradient index j + 3 c for derivative j of component c; lin_elast.cpp:100-118).  With exact
+// integration (order >= 2) the block (row component c, column component d) of an element row is the
+// scalar Gram formula of its row kind with G_pq replaced by
+//     B^{cd}_pq = |T| (lambda g_p^c g_q^d + mu (delta_cd g_p.g_q + g_p^d g_q^c))
+// (p on the row side: B is not symmetric in p, q for c != d); rows of B also sum to zero over q.
+// Per tet: g_1, g_2, g_3 (g_0 = -(g_1 + g_2 + g_3)), lambda|T|, mu|T|, f|T|: a 16-value block.
+template <typename R>
+__device__ __forceinline__ void lame_block(const R* PSI, R lam, R mu, R mes, R fm, R* out) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        out[3 * a] = PSI[a];
+        out[3 * a + 1] = PSI[a + 3];
+        out[3 * a + 2] = PSI[a + 6];
+    }
+    out[9] = lam * mes;
+    out[10] = mu * mes;
+    out[11] = fm * mes;
+    out[12] = out[13] = out[14] = out[15] = R(0);
+}
+
+__global__ void tet_lame_f64_kernel(int64_t nt, const double* __restrict__ xyz, const int32_t* __restrict__ tets,
+                                    const double* __restrict__ D, const double* __restrict__ f, double f_const,
+                                    double* __restrict__ out, int* __restrict__ status) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= nt) return;
+    const int4 v = reinterpret_cast<const int4*>(tets)[t];
+    double e[9], PSI[9], B[16];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const double x0 = xyz[3 * (int64_t)v.x + k];
+        e[k + 0] = xyz[3 * (int64_t)v.y + k] - x0;
+        e[k + 3] = xyz[3 * (int64_t)v.z + k] - x0;
+        e[k + 6] = xyz[3 * (int64_t)v.w + k] - x0;
+    }
+    const double det = inverse3(e, PSI);
+    lame_block(PSI, D[2 * t], D[2 * t + 1], fabs(det) / 6.0, f ? f[t] : f_const, B);
+    bool bad = !(det != 0.0);
+#pragma unroll
+    for (int k = 0; k < 12; ++k) bad |= !isfinite(B[k]);
+    if (bad) atomicExch(status, ANIGPU_ERR_NONFINITE);
+    double2* o = reinterpret_cast<double2*>(out + 16 * t);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) o[q] = make_double2(B[2 * q], B[2 * q + 1]);
+}
+
+__global__ void tet_lame_f32_kernel(int64_t nt, const double* __restrict__ xyz, const float2* __restrict__ xyz2,
+                                    const int32_t* __restrict__ tets, const double* __restrict__ D,
+                                    const double* __restrict__ f, double f_const, float* __restrict__ out,
+                                    int* __restrict__ status) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= nt) return;
+    const int4 v = reinterpret_cast<const int4*>(tets)[t];
+    float e[9];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float2 x0 = xyz2[3 * (int64_t)v.x + k];
+        const float2 x1 = xyz2[3 * (int64_t)v.y + k];
+        const float2 x2 = xyz2[3 * (int64_t)v.z + k];
+        const float2 x3 = xyz2[3 * (int64_t)v.w + k];
+        e[k + 0] = (x1.x - x0.x) + (x1.y - x0.y);
+        e[k + 3] = (x2.x - x0.x) + (x2.y - x0.y);
+        e[k + 6] = (x3.x - x0.x) + (x3.y - x0.y);
+    }
+    const double2 lm = reinterpret_cast<const double2*>(D)[t];
+    const float lam = d2f_rn(lm.x), mu = d2f_rn(lm.y), fv = d2f_rn(f ? f[t] : f_const);
+    float PSI[9], B[16];
+    const float det = inverse3(e, PSI);
+    const float l0 = e[0] * e[0] + e[1] * e[1] + e[2] * e[2];
+    const float l1 = e[3] * e[3] + e[4] * e[4] + e[5] * e[5];
+    const float l2 = e[6] * e[6] + e[7] * e[7] + e[8] * e[8];
+    if (det * det > 0.0025f * l0 * l1 * l2) {
+        lame_block(PSI, lam, mu, fabsf(det) * (1.0f / 6.0f), fv, B);
+    } else {  // badly shaped tet: Jacobian and inverse in FP64
+        double ed[9], P64[9];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const double x0 = xyz[3 * (int64_t)v.x + k];
+            ed[k + 0] = xyz[3 * (int64_t)v.y + k] - x0;
+            ed[k + 3] = xyz[3 * (int64_t)v.z + k] - x0;
+            ed[k + 6] = xyz[3 * (int64_t)v.w + k] - x0;
+        }
+        const double det64 = inverse3(ed, P64);
+        double B64[16];
+        lame_block(P64, lm.x, lm.y, fabs(det64) / 6.0, f ? f[t] : f_const, B64);
+#pragma unroll
+        for (int k = 0; k < 16; ++k) B[k] = (float)B64[k];
+        if (!(det64 != 0.0)) atomicExch(status, ANIGPU_ERR_NONFINITE);
+    }
+    bool bad = false;
+#pragma unroll
+    for (int k = 0; k < 12; ++k) bad |= !isfinite(B[k]);
+    if (bad) atomicExch(status, ANIGPU_ERR_NONFINITE);
+    float4* o = reinterpret_cast<float4*>(out + 16 * t);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) o[q] = make_float4(B[4 * q], B[4 * q + 1], B[4 * q + 2], B[4 * q + 3]);
+}
+
+template <typename Real>
+struct VBlock {
+    Real v[16];
+    __device__ __forceinline__ void load(const Real* p) {
+        KVec<Real, 8> a, b;
+        a.load(p);
+        b.load(p + 8);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            v[k] = a.v[k];
+            v[8 + k] = b.v[k];
+        }
+    }
+    __device__ __forceinline__ void zero() {
+#pragma unroll
+        for (int k = 0; k < 16; ++k) v[k] = Real(0);
+    }
+};
+
+template <typename Real>
+__device__ __forceinline__ void gvec(const Real* v, int p, Real* g) {
+    // gradient of barycentric p from the block: g_1..g_3 stored, g_0 = -(g_1 + g_2 + g_3)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const Real g1 = v[c], g2 = v[3 + c], g3 = v[6 + c];
+        g[c] = p == 0 ? -((g1 + g2) + g3) : p == 1 ? g1 : p == 2 ? g2 : g3;
+    }
+}
+
+template <typename Real>
+__device__ __forceinline__ Real sel3(const Real* g, int c) {
+    return c == 0 ? g[0] : c == 1 ? g[1] : g[2];
+}
+
+// B^{cd}_pq from the row-side gradient gp (gpc = gp[c]) and the column-side gq (gqc = gq[c])
+template <typename Real>
+__device__ __forceinline__ Real lameB(Real lam, Real mu, const Real* gp, Real gpc, const Real* gq, Real gqc,
+                                      Real dot, int c, int d) {
+    const Real gpd = sel3(gp, d), gqd = sel3(gq, d);
+    Real b = lam * gpc * gqd + mu * gpd * gqc;
+    if (c == d) b += mu * dot;
+    return b;
+}
+
+// one lane per vector row (component c = blockIdx.y, scalar row r); FORM 1 vertex rows, 2 edge rows
+template <typename Real, int FORM, bool DIR>
+__global__ void __launch_bounds__(64) vec_row_gather_kernel(RowParams p, int64_t nds, const int64_t* __restrict__ vrowptr,
+                                                            const Real* __restrict__ tetB, Real* __restrict__ vals,
+                                                            double* __restrict__ rhs, int* __restrict__ status) {
+    constexpr int VEC = 16 / (int)sizeof(Real);
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarps = blockDim.x >> 5;
+    const int c = blockIdx.y;
+    const int64_t row0 = p.row_begin + ((int64_t)blockIdx.x * nwarps + warp) * 32;
+    if (row0 >= p.nrows) return;
+    const int64_t rend = row0 + 32 < p.nrows ? row0 + 32 : p.nrows;
+    const int64_t cbase = vrowptr[c * nds + row0];
+    const int clen = (int)(vrowptr[c * nds + rend] - cbase);
+    const int shift = (int)(cbase & (VEC - 1));
+    const size_t chunk_bytes = (((size_t)32 * 3 * p.cap + VEC) * sizeof(Real) + 15) / 16 * 16;
+    unsigned char* wbase = smem_raw + chunk_bytes * warp;
+    Real* sC = reinterpret_cast<Real*>(wbase) + shift;
+    {
+        const int nvec = (shift + clen + VEC - 1) / VEC;
+        int4* z = reinterpret_cast<int4*>(wbase);
+        for (int k = lane; k < nvec; k += 32) z[k] = make_int4(0, 0, 0, 0);
+    }
+    const int64_t r = row0 + lane;
+    const int64_t R = c * nds + r;
+    const bool valid = r < p.nrows;
+    int64_t ib = 0;
+    int deg = 0, base = 0, L = 0;
+    bool isdir = false;
+    if (valid) {
+        ib = p.inc_ptr[r];
+        deg = (int)(p.inc_ptr[r + 1] - ib);
+        base = (int)(vrowptr[R] - cbase);
+        L = (int)(p.rowptr[r + 1] - p.rowptr[r]);
+        if (DIR) isdir = p.dir_mask[R] != 0;
+    }
+    __syncwarp();
+    Real* myRow = sC + base;
+    Real racc = Real(0);
+    const int nloop = isdir ? 0 : deg;
+    const int last = nloop - 1;
+    constexpr int KD = 2, RD = 4;
+    VBlock<Real> Kq[KD];
+    ScatterRec Rq[RD];
+#pragma unroll
+    for (int j = 0; j < KD; ++j) Kq[j].zero();
+#pragma unroll
+    for (int j = 0; j < RD; ++j) Rq[j] = ScatterRec{0u, 0u, 0u, 0u};
+    if (nloop > 0) {
+#pragma unroll
+        for (int j = 0; j < RD; ++j) Rq[j] = p.recs[ib + min(j, last)];
+#pragma unroll
+        for (int j = 0; j < KD; ++j) Kq[j].load(tetB + 16 * (int64_t)Rq[j].tet);
+    }
+    const Real m2 = Real(-0.2), p6 = Real(0.6), p8 = Real(0.8), p16 = Real(1.6);
+    for (int k = 0; k < nloop; ++k) {
+        VBlock<Real> Kn;
+        Kn.load(tetB + 16 * (int64_t)Rq[KD].tet);
+        const ScatterRec Rn = p.recs[ib + min(k + RD, last)];
+        const ScatterRec r0 = Rq[0];
+        const Real* bv = Kq[0].v;
+        const int i = r0.meta & 15;
+        const Real lam = bv[9], mu = bv[10];
+        int o[10];
+#pragma unroll
+        for (int j = 0; j < 10; ++j) {
+            const uint32_t w = j < 4 ? r0.off03 : (j < 8 ? r0.off47 : (r0.meta >> 16));
+            o[j] = (int)byte_of(w, j);
+        }
+        if (FORM == 1) {
+            // vertex i, others o1 < o2 < o3
+            const int q1 = i == 0 ? 1 : 0, q2 = i <= 1 ? 2 : 1, q3 = i <= 2 ? 3 : 2;
+            Real gi[3], g1[3], g2[3], g3[3];
+            gvec(bv, i, gi);
+            gvec(bv, q1, g1);
+            gvec(bv, q2, g2);
+            gvec(bv, q3, g3);
+            const Real gic = sel3(gi, c), g1c = sel3(g1, c), g2c = sel3(g2, c), g3c = sel3(g3, c);
+            const Real d1 = gi[0] * g1[0] + gi[1] * g1[1] + gi[2] * g1[2];
+            const Real d2 = gi[0] * g2[0] + gi[1] * g2[1] + gi[2] * g2[2];
+            const Real d3 = gi[0] * g3[0] + gi[1] * g3[1] + gi[2] * g3[2];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                const Real b1 = lameB(lam, mu, gi, gic, g1, g1c, d1, c, d);
+                const Real b2 = lameB(lam, mu, gi, gic, g2, g2c, d2, c, d);
+                const Real b3 = lameB(lam, mu, gi, gic, g3, g3c, d3, c, d);
+                const Real bii = -((b1 + b2) + b3);
+                Real a[10];
+                a[0] = p6 * bii;
+                a[1] = m2 * b1;
+                a[2] = m2 * b2;
+                a[3] = m2 * b3;
+                const Real t = m2 * bii;
+                a[4] = fma(p6, b1, t);
+                a[5] = fma(p6, b2, t);
+                a[6] = fma(p6, b3, t);
+                a[7] = m2 * (b1 + b2);
+                a[8] = m2 * (b1 + b3);
+                a[9] = m2 * (b2 + b3);
+                Real* rowd = myRow + d * L;
+                Real cur[10];
+#pragma unroll
+                for (int j = 0; j < 10; ++j) cur[j] = rowd[o[j]];
+#pragma unroll
+                for (int j = 0; j < 10; ++j) rowd[o[j]] = cur[j] + a[j];
+            }
+            racc += Real(-0.05) * bv[11];
+        } else {
+            // edge k = (a,b), others c_ < d_
+            const int e = i - 4;
+            const int va = e <= 2 ? 0 : e <= 4 ? 1 : 2;
+            const int vb = e == 0 ? 1 : (e == 1 || e == 3) ? 2 : 3;
+            const int vc = (e <= 2) ? (e == 0 ? 2 : 1) : 0;
+            const int vd = e == 0 ? 3 : e == 1 ? 3 : e == 2 ? 2 : e == 3 ? 3 : e == 4 ? 2 : 1;
+            Real ga[3], gb[3], gc[3], gd[3];
+            gvec(bv, va, ga);
+            gvec(bv, vb, gb);
+            gvec(bv, vc, gc);
+            gvec(bv, vd, gd);
+            const Real gac_ = sel3(ga, c), gbc_ = sel3(gb, c), gcc_ = sel3(gc, c), gdc_ = sel3(gd, c);
+            const Real dab = ga[0] * gb[0] + ga[1] * gb[1] + ga[2] * gb[2];
+            const Real dac = ga[0] * gc[0] + ga[1] * gc[1] + ga[2] * gc[2];
+            const Real dad = ga[0] * gd[0] + ga[1] * gd[1] + ga[2] * gd[2];
+            const Real dbc = gb[0] * gc[0] + gb[1] * gc[1] + gb[2] * gc[2];
+            const Real dbd = gb[0] * gd[0] + gb[1] * gd[1] + gb[2] * gd[2];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                const Real Bab = lameB(lam, mu, ga, gac_, gb, gbc_, dab, c, d);
+                const Real Bba = lameB(lam, mu, gb, gbc_, ga, gac_, dab, c, d);
+                const Real Bac = lameB(lam, mu, ga, gac_, gc, gcc_, dac, c, d);
+                const Real Bad = lameB(lam, mu, ga, gac_, gd, gdc_, dad, c, d);
+                const Real Bbc = lameB(lam, mu, gb, gbc_, gc, gcc_, dbc, c, d);
+                const Real Bbd = lameB(lam, mu, gb, gbc_, gd, gdc_, dbd, c, d);
+                const Real Baa = -((Bab + Bac) + Bad), Bbb = -((Bba + Bbc) + Bbd);
+                Real a[10];
+                a[0] = fma(m2, Baa, p6 * Bba);
+                a[1] = fma(p6, Bab, m2 * Bbb);
+                a[2] = m2 * (Bac + Bbc);
+                a[3] = m2 * (Bad + Bbd);
+                a[4] = fma(p16, Baa + Bbb, p8 * (Bab + Bba));
+                a[5] = fma(p8, (Baa + Bac) + Bba, p16 * Bbc);
+                a[6] = fma(p8, (Baa + Bad) + Bba, p16 * Bbd);
+                a[7] = fma(p8, (Bab + Bbb) + Bbc, p16 * Bac);
+                a[8] = fma(p8, (Bab + Bbb) + Bbd, p16 * Bad);
+                a[9] = p8 * ((Bac + Bad) + (Bbc + Bbd));
+                Real* rowd = myRow + d * L;
+                Real cur[10];
+#pragma unroll
+                for (int j = 0; j < 10; ++j) cur[j] = rowd[o[j]];
+#pragma unroll
+                for (int j = 0; j < 10; ++j) rowd[o[j]] = cur[j] + a[j];
+            }
+            racc += Real(0.2) * bv[11];
+        }
+#pragma unroll
+        for (int j = 0; j + 1 < KD; ++j) Kq[j] = Kq[j + 1];
+        Kq[KD - 1] = Kn;
+#pragma unroll
+        for (int j = 0; j + 1 < RD; ++j) Rq[j] = Rq[j + 1];
+        Rq[RD - 1] = Rn;
+    }
+    bool bad = false;
+    if (valid) {
+        double F;
+        if (DIR && isdir) {
+            if (deg > 0) {  // diagonal = number of incident tets
+                const ScatterRec rd = p.recs[ib];
+                const int dc = canon_diag(10, rd.meta & 15);
+                const int od = (int)byte_of(dc < 4 ? rd.off03 : rd.off47, dc);
+                myRow[c * L + od] = Real(deg);
+            }
+            F = 0;  // homogeneous boundary values only in the vector path
+        } else {
+            F = (double)racc;
+            if (DIR)
+                for (int64_t q = p.dir_cptr[R]; q < p.dir_cptr[R + 1]; ++q) myRow[p.dir_coff[q]] = Real(0);
+        }
+        bad |= !isfinite(F);
+        rhs[R] = F;
+    }
+    __syncwarp();
+    Real fin = Real(0);
+    for (int k = lane; k < clen; k += 32) {
+        const Real v = sC[k];
+        fin = fma(v, Real(0), fin);
+        vals[cbase + k] = v;
+    }
+    bad |= !isfinite(fin);
+    if (bad) atomicExch(status, ANIGPU_ERR_NONFINITE);
+}
+
 // ---------------------------------------------------------------- CSR compaction
 __global__ void compact_count_kernel(int64_t n, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
                                      const uint8_t* __restrict__ touched, unsigned long long* __restrict__ cnt) {
@@ -885,10 +1221,89 @@ static int launch_rows(anigpu_ctx* h, const RowParams& p, const void* tables, vo
 #undef LR
 }
 
+// vector P2 with the Lame tensor: tet blocks, then vertex-row and edge-row gathers (x 3 components)
+static int run_assemble_vec(anigpu_ctx* h, int kind, const double* D, const double* f, double f_const, int order,
+                            int precision, void* vals, double* rhs, uint8_t* touched, double drop_val) {
+    (void)drop_val;
+    if (kind != ANIGPU_TENSOR_LAME)
+        return set_err(h, ANIGPU_ERR_UNSUPPORTED, "vector P2 assembly takes ANIGPU_TENSOR_LAME (lambda, mu per tet)");
+    if (order < 2)
+        return set_err(h, ANIGPU_ERR_UNSUPPORTED, "vector P2 assembly needs quadrature order >= 2 (exact integration)");
+    if (!D) return set_err(h, ANIGPU_ERR_ARG, "tensor data is NULL");
+    if (!vals || !rhs) return set_err(h, ANIGPU_ERR_ARG, "NULL output");
+    if (touched) return set_err(h, ANIGPU_ERR_UNSUPPORTED, "no touched map for vector P2 assembly");
+    if (h->bc_nonzero) return set_err(h, ANIGPU_ERR_UNSUPPORTED, "vector P2 assembly supports zero boundary values only");
+    if (precision != ANIGPU_F32 && precision != ANIGPU_F64) return set_err(h, ANIGPU_ERR_ARG, "precision");
+    const double *pp, *ww;
+    int q;
+    if (!anigpu_quad_rule(order, &pp, &ww, &q)) return set_err(h, ANIGPU_ERR_UNSUPPORTED, "quadrature order");
+    const size_t rsz = precision == ANIGPU_F32 ? 4 : 8;
+    const size_t need = (size_t)h->nt * 16 * rsz;
+    if (h->tetdata_bytes < need) {
+        if (h->tetdata) cudaFree(h->tetdata);
+        h->tetdata = nullptr;
+        ANI_CUDA(h, cudaMalloc(&h->tetdata, need));
+        h->tetdata_bytes = need;
+    }
+    time_mark(h, 0);
+    if (precision == ANIGPU_F32)
+        tet_lame_f32_kernel<<<grid_for(h->nt, 256), 256, 0, h->stream>>>(h->nt, h->xyz, h->xyz2, h->tets, D, f, f_const,
+                                                                       (float*)h->tetdata, h->d_status);
+    else
+        tet_lame_f64_kernel<<<grid_for(h->nt, 256), 256, 0, h->stream>>>(h->nt, h->xyz, h->tets, D, f, f_const,
+                                                                       (double*)h->tetdata, h->d_status);
+    ANI_LAUNCHED(h);
+    time_mark(h, 1);
+    RowParams p;
+    p.inc_ptr = h->inc_ptr;
+    p.recs = h->recs;
+    p.rowptr = h->rowptr_s;
+    p.dir_mask = h->dir_mask;
+    p.dir_bc = h->dir_bc;
+    p.edofs = h->edofs;
+    p.drop = 0;
+    p.vec_ok = 0;
+    p.dir_cptr = h->dir_cptr;
+    p.dir_coff = h->dir_coff;
+    cudaStream_t side = h->side_stream ? h->side_stream : h->stream;
+    if (side != h->stream) {
+        ANI_CUDA(h, cudaEventRecord(h->fork_ev, h->stream));
+        ANI_CUDA(h, cudaStreamWaitEvent(side, h->fork_ev, 0));
+    }
+    const bool dir = h->has_dirichlet;
+    for (int rg = 0; rg < 2; ++rg) {
+        p.row_begin = h->row_range[rg];
+        p.nrows = h->row_range[rg + 1];
+        p.cap = h->row_range_cap[rg];
+        if (p.nrows <= p.row_begin) continue;
+        cudaStream_t st = rg == 0 ? side : h->stream;
+        const int warps = 2;
+        const size_t smem = ((((size_t)32 * 3 * p.cap + 16 / rsz) * rsz + 15) / 16 * 16) * warps;
+        const dim3 grid(grid_for(p.nrows - p.row_begin, 32 * warps), 3);
+#define VLAUNCH(R, F, DD)                                                                                          do {                                                                                                               auto kern = vec_row_gather_kernel<R, F, DD>;                                                                   ANI_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));              kern<<<grid, 32 * warps, smem, st>>>(p, h->nds, h->rowptr, (const R*)h->tetdata, (R*)vals, rhs,                                                     h->d_status);                                                         } while (0)
+        if (precision == ANIGPU_F32) {
+            if (rg == 0) { if (dir) VLAUNCH(float, 1, true); else VLAUNCH(float, 1, false); }
+            else { if (dir) VLAUNCH(float, 2, true); else VLAUNCH(float, 2, false); }
+        } else {
+            if (rg == 0) { if (dir) VLAUNCH(double, 1, true); else VLAUNCH(double, 1, false); }
+            else { if (dir) VLAUNCH(double, 2, true); else VLAUNCH(double, 2, false); }
+        }
+#undef VLAUNCH
+        ANI_LAUNCHED(h);
+    }
+    if (side != h->stream) {
+        ANI_CUDA(h, cudaEventRecord(h->join_ev, side));
+        ANI_CUDA(h, cudaStreamWaitEvent(h->stream, h->join_ev, 0));
+    }
+    time_mark(h, 2);
+    return ANIGPU_OK;
+}
+
 int run_assemble(anigpu_ctx* h, int kind, const double* D, const double* f, double f_const, int order,
                  int precision, void* vals, double* rhs, uint8_t* touched, double drop_val) {
     if (h->space < 0) return set_err(h, ANIGPU_ERR_STATE, "anigpu_problem_setup not called");
-    if (h->space == ANIGPU_VEC3_P2) return set_err(h, ANIGPU_ERR_UNSUPPORTED, "vector assembly not built yet");
+    if (h->space == ANIGPU_VEC3_P2)
+        return run_assemble_vec(h, kind, D, f, f_const, order, precision, vals, rhs, touched, drop_val);
     if (kind != ANIGPU_TENSOR_NULL && kind != ANIGPU_TENSOR_CONST_SCALAR && kind != ANIGPU_TENSOR_TET_SCALAR &&
         kind != ANIGPU_TENSOR_TET_SYM)
         return set_err(h, ANIGPU_ERR_UNSUPPORTED, "assembly tensor kind must be NULL, CONST_SCALAR, TET_SCALAR or TET_SYM");

@@ -301,13 +301,13 @@ __global__ void dircol_count_kernel(int64_t n, const int64_t* __restrict__ rowpt
 }
 __global__ void dircol_fill_kernel(int64_t n, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
                                    const uint8_t* __restrict__ mask, const int64_t* __restrict__ cptr,
-                                   uint8_t* __restrict__ coff) {
+                                   uint16_t* __restrict__ coff) {
     const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (r >= n || mask[r]) return;
     int64_t w = cptr[r];
     const int64_t b = rowptr[r];
     for (int64_t k = b; k < rowptr[r + 1]; ++k)
-        if (mask[col[k]]) coff[w++] = (uint8_t)(k - b);
+        if (mask[col[k]]) coff[w++] = (uint16_t)(k - b);
 }
 
 // vector template: rows (c, r) -> c*nds + r; columns [c'*nds + col_s] for c' = 0..2
@@ -643,16 +643,16 @@ int setup_dirichlet_bits(anigpu_ctx* h) {
     const int64_t nrec = h->nt * h->nloc_s;
     dirichlet_bits_kernel<<<grid_for(nrec, 256), 256, 0, h->stream>>>(nrec, h->nloc_s, h->edofs, h->dir_mask, h->recs);
     ANI_LAUNCHED(h);
-    if (!h->has_dirichlet || h->ncomp != 1) return ANIGPU_OK;
-    // per non-Dirichlet row, the offsets of its Dirichlet columns: the assembly adds every
-    // element value and zeroes these entries at the end (applyDir zeroes column k of every
-    // element matrix, so their sums are exactly zero)
+    if (!h->has_dirichlet) return ANIGPU_OK;
+    // per non-Dirichlet row (of the full template: vector rows for FemVec), the offsets of its
+    // Dirichlet columns: the assembly adds every element value and zeroes these entries at the end
+    // (applyDir zeroes column k of every element matrix, so their sums are exactly zero)
     cudaStream_t s = h->stream;
-    const int64_t n = h->nds;
+    const int64_t n = h->ndof;
     unsigned long long* cnt = nullptr;
     ANI_CUDA(h, cudaMallocAsync((void**)&cnt, sizeof(unsigned long long) * (n + 1), s));
     ANI_CUDA(h, cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * (n + 1), s));
-    dircol_count_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, h->rowptr_s, h->col_s, h->dir_mask, cnt);
+    dircol_count_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, h->rowptr, h->col, h->dir_mask, cnt);
     ANI_LAUNCHED(h);
     RC(dev_alloc(h, &h->dir_cptr, (size_t)n + 1));
     RC(scan_counts(h, cnt, n, h->dir_cptr));
@@ -661,7 +661,7 @@ int setup_dirichlet_bits(anigpu_ctx* h) {
     ANI_CUDA(h, cudaStreamSynchronize(s));
     ANI_CUDA(h, cudaFreeAsync(cnt, s));
     RC(dev_alloc(h, &h->dir_coff, (size_t)std::max<int64_t>(total, 1)));
-    dircol_fill_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, h->rowptr_s, h->col_s, h->dir_mask, h->dir_cptr, h->dir_coff);
+    dircol_fill_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, h->rowptr, h->col, h->dir_mask, h->dir_cptr, h->dir_coff);
     ANI_LAUNCHED(h);
     return ANIGPU_OK;
 }

@@ -109,6 +109,8 @@ class Restated:
         tets = np.ascontiguousarray(tets, dtype=np.int32)
         nloc = {1: 4, 2: 10, 5: 30}[space]
         e = np.zeros((tets.shape[0], nloc), dtype=np.int32)
+        if space != 1 and tet_edges is None:
+            raise ValueError("element_dofs: spaces with edge DOFs need the tet edge table")
         te = np.ascontiguousarray(tet_edges, dtype=np.int32) if tet_edges is not None else np.zeros((1, 6), np.int32)
         nd = self.L.orc_element_dofs(space, nv, ne, tets.shape[0], _p(tets), _p(te), _p(e))
         return nd, e
@@ -174,7 +176,7 @@ class Restated:
         Returns dict(rowptr, col, vals, rhs, touched, edofs, ndof)."""
         nv = xyz.shape[0]
         t = self.orient(xyz, tets)
-        ne, te = self.edges(nv, t) if space == 2 else (0, None)
+        ne, te = self.edges(nv, t) if space in (2, 5) else (0, None)
         ndof, ed = self.element_dofs(space, nv, ne, t, te)
         rp, col = self.csr_template(ndof, ed)
         XY = np.ascontiguousarray(xyz[t].reshape(-1, 12))

@@ -194,3 +194,48 @@ def test_async_assembly_and_status(lib, restated):
         lib.status()
     assert e.value.code == anigpu.ERR_NONFINITE
     lib.status()  # cleared
+
+
+def _lame9(lam, mu):
+    """The Lame tensor as the 9x9 GENERAL tensor of Operator<GRAD, FemVec<3,P2>>: index j + 3 c for
+    derivative j of component c (lin_elast.cpp:100-118); symmetric, so its column-major layout is
+    the same as its row-major one."""
+    D = np.zeros((lam.size, 9, 9))
+    for c1 in range(3):
+        for j1 in range(3):
+            for c2 in range(3):
+                for j2 in range(3):
+                    D[:, j1 + 3 * c1, j2 + 3 * c2] = (lam * (j1 == c1) * (j2 == c2)
+                                                      + mu * ((c1 == c2) * (j1 == j2) + (c1 == j2) * (j1 == c2)))
+    return D.reshape(lam.size, 81)
+
+
+@pytest.mark.parametrize("n,clamped", [(3, False), (4, True)])
+def test_vector_p2_lame_matches_oracle(lib, restated, n, clamped):
+    """Vector P2 linear elasticity (config 5 operator): FP64 assembly with per-tet Lame parameters
+    equals the restated assembler with the 9x9 GENERAL tensor; FP32 within 5e-5 per row."""
+    import anigpu
+    from anigpu import meshgen
+    xyz, tets = meshgen.kuhn_cube(n, perturb=0.2, seed=5)
+    nt = tets.shape[0]
+    E = np.exp(0.5 * meshgen.normal(61, nt))
+    nu = 0.2 + 0.25 * meshgen.uniform(62, nt)
+    lam, mu = E * nu / ((1 + nu) * (1 - 2 * nu)), E / (2 * (1 + nu))
+    lib.mesh_upload(xyz, tets)
+    ndof, nnz = lib.problem_setup(anigpu.VEC3_P2)
+    coords = lib.dof_coords().cpu().numpy()
+    mask = (np.abs(coords[:, 0]) < 1e-12).astype(np.uint8) if clamped else meshgen.boundary_mask(coords)
+    lib.set_dirichlet(mask)
+    LM = np.stack([lam, mu], axis=1)
+    vals, rhs, _ = lib.assemble(anigpu.TENSOR_LAME, LM, None, 0.5, 4, anigpu.F64)
+    ref = restated.assemble_problem(xyz, tets, 5, 4, _lame9(lam, mu), 0.5, 4, dirichlet=(mask, None))
+    rp, col = lib.csr_template()
+    assert np.array_equal(rp.cpu().numpy(), ref["rowptr"]) and np.array_equal(col.cpu().numpy(), ref["col"])
+    v = vals.cpu().numpy()
+    assert np.abs(v - ref["vals"]).max() <= 1e-12 * np.abs(ref["vals"]).max()
+    assert np.abs(rhs.cpu().numpy() - ref["rhs"]).max() <= 1e-12 * max(np.abs(ref["rhs"]).max(), 1e-300)
+    v32, _, _ = lib.assemble(anigpu.TENSOR_LAME, LM, None, 0.5, 4, anigpu.F32)
+    rows = np.repeat(np.arange(ndof), np.diff(ref["rowptr"]))
+    rown = np.sqrt(np.bincount(rows, ref["vals"] ** 2))
+    err = np.sqrt(np.bincount(rows, (v32.double().cpu().numpy() - ref["vals"]) ** 2)) / np.maximum(rown, 1e-300)
+    assert err.max() <= 5e-5
