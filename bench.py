@@ -47,6 +47,7 @@ def parse():
     ap.add_argument("--no-solve", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-instances workload")
     ap.add_argument("--batched-instances", type=int, default=256)
+    ap.add_argument("--no-elasticity", action="store_true", help="skip the vector-P2 elasticity workload")
     ap.add_argument("--cpu-sample", type=int, default=0, help="tets in the CPU-baseline sample (0 = auto)")
     return ap.parse_args()
 
@@ -129,6 +130,81 @@ def run_batched(args, local):
     out["tets"] = total_tets
     out["seconds"] = total_s
     out["tets_per_s"] = total_tets / total_s
+    return out
+
+
+def run_elasticity(args, local, peak):
+    """Vector P2 linear elasticity on 48^3 x 6 perturbed Kuhn tets (663,552 tets): per-tet Lame
+    parameters from E ~ lognormal(0, 0.5^2), nu ~ U[0.2, 0.45]; clamped face x = 0; unit traction
+    (1, 0, 0) on x = 1 as its consistent P2 nodal loads (area/3 on each edge DOF of a face, 0 on the
+    vertices); FP32 assembly timed back to back, then FP64 Jacobi-PCG (FP64 assembly) and IR-CG32
+    (FP32 assembly) to 1e-8."""
+    import torch
+
+    import anigpu
+    from anigpu import meshgen
+    n = 48
+    xyz, tets = meshgen.kuhn_cube(n, perturb=0.2, seed=48)
+    nt, nv = tets.shape[0], xyz.shape[0]
+    E = np.exp(0.5 * meshgen.normal(4801, nt))
+    nu = 0.2 + 0.25 * meshgen.uniform(4802, nt)
+    LM = np.stack([E * nu / ((1 + nu) * (1 - 2 * nu)), E / (2 * (1 + nu))], axis=1)
+    lib = anigpu.Anigpu(local)
+    dev = f"cuda:{local}"
+    lib.mesh_upload(xyz, tets)
+    ndof, nnz = lib.problem_setup(anigpu.VEC3_P2)
+    coords = lib.dof_coords().cpu().numpy()
+    lib.set_dirichlet((np.abs(coords[:, 0]) < 1e-12).astype(np.uint8))
+    # traction load: faces with all three vertices on x = 1 (boundary vertices are not perturbed)
+    ed = lib.element_dofs().cpu().numpy()
+    b = np.zeros(ndof)
+    on = np.abs(xyz[:, 0] - 1.0) < 1e-12
+    faces = [(0, 1, 2), (0, 1, 3), (0, 2, 3), (1, 2, 3)]
+    edge_of = {(0, 1): 4, (0, 2): 5, (0, 3): 6, (1, 2): 7, (1, 3): 8, (2, 3): 9}
+    # local vertex order of element_dofs is the oriented one; recover it from the DOF ids (vertex DOFs = ids)
+    tl = ed[:, :4]
+    for f in faces:
+        sel = on[tl[:, f[0]]] & on[tl[:, f[1]]] & on[tl[:, f[2]]]
+        if not sel.any():
+            continue
+        p0, p1, p2 = xyz[tl[sel, f[0]]], xyz[tl[sel, f[1]]], xyz[tl[sel, f[2]]]
+        area = 0.5 * np.linalg.norm(np.cross(p1 - p0, p2 - p0), axis=1)
+        for a_, b_ in ((f[0], f[1]), (f[0], f[2]), (f[1], f[2])):
+            np.add.at(b, ed[sel, edge_of[(a_, b_)]], area / 3.0)
+    D_dev = torch.tensor(LM, device=dev)
+    vals32 = torch.empty(nnz, dtype=torch.float32, device=dev)
+    rhs = torch.empty(ndof, dtype=torch.float64, device=dev)
+    for _ in range(3):
+        lib.assemble(anigpu.TENSOR_LAME, D_dev, None, 0.0, 4, anigpu.F32, vals32, rhs)
+    steps = 50
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    torch.cuda.synchronize()
+    for k in range(steps):
+        ev[k][0].record(lib.stream)
+        lib.assemble(anigpu.TENSOR_LAME, D_dev, None, 0.0, 4, anigpu.F32, vals32, rhs, sync=False)
+        ev[k][1].record(lib.stream)
+    lib.status()
+    torch.cuda.synchronize()
+    ms = float(np.mean([a.elapsed_time(c) for a, c in ev]))
+    b_alg = nt * 16 + nv * 24 + nt * 16 + nnz * 4 + ndof * 8
+    vals64 = torch.empty(nnz, dtype=torch.float64, device=dev)
+    lib.set_timing(True)
+    lib.assemble(anigpu.TENSOR_LAME, D_dev, None, 0.0, 4, anigpu.F64, vals64, rhs)
+    lib.assemble(anigpu.TENSOR_LAME, D_dev, None, 0.0, 4, anigpu.F64, vals64, rhs)
+    f64_ms = sum(lib.last_timing())
+    lib.set_timing(False)
+    bd = torch.tensor(b, device=dev)
+    out = {"workload": f"vector P2 elasticity, 48^3x6 perturbed Kuhn ({nt} tets, {ndof} DOFs, {nnz} nnz), order 4",
+           "f32_assembly": {"ms": ms, "tets_per_s": nt / (ms * 1e-3),
+                            "roofline_frac": b_alg / (ms * 1e-3) / 1e9 / peak, "algorithmic_bytes": b_alg},
+           "f64_assembly_ms": f64_ms}
+    for name, method, vv, prec in (("jacobi_pcg_f64", anigpu.SOLVE_JACOBI_PCG, vals64, anigpu.F64),
+                                   ("ir_cg32", anigpu.SOLVE_IR_CG32, vals32, anigpu.F32)):
+        for _ in range(2):
+            x, st = lib.solve(vv, bd, method, prec, rtol=1e-8, maxit=200000, check=False)
+        out[name] = {"seconds": st.seconds, "iterations": st.iterations, "rel_residual_f64": st.rel_residual}
+    out["max_x_displacement"] = float(x[:ndof // 3].max().item())
+    lib.close()
     return out
 
 
@@ -441,6 +517,9 @@ def run_ours(args):
     batched = None
     if not args.no_batched and rank == 0:
         batched = run_batched(args, local)
+    elasticity = None
+    if not args.no_elasticity and rank == 0:
+        elasticity = run_elasticity(args, local, peak)
 
     if rank != 0:
         return
@@ -475,6 +554,7 @@ def run_ours(args):
         "setup_s": setup_s,
         "solve": solve,
         "batched": batched,
+        "elasticity": elasticity,
     }
     print(json.dumps(line), flush=True)
 
