@@ -40,7 +40,10 @@ constexpr int kMaxP = 1024;          // block partials per reduction
 constexpr int kBatch = 16;           // even: the status parity of a batch starts at 0
 constexpr double kDelta = 0.1;       // residual replacement threshold (ratio of norms)
 constexpr int kStallBatches = 8;     // batches without a new smallest residual -> Jacobi
-constexpr int kW = 8;                // lanes per CSR row
+#ifndef FCG_W
+#define FCG_W 4
+#endif
+constexpr int kW = FCG_W;            // lanes per CSR row
 
 struct FcgScalars {
     double rz;        // r.z of the current direction

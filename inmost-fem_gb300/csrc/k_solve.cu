@@ -24,6 +24,9 @@ namespace {
 
 constexpr int kBlock = 256;
 constexpr int kMaxBlocks = 2048;
+#ifndef SOLVE_W_P2
+#define SOLVE_W_P2 4
+#endif
 
 struct PcgScalars {
     double rz[2];     // r.z by iteration parity
@@ -339,9 +342,15 @@ int ensure_ws(anigpu_ctx* h, SolveWs** out) {
     return ANIGPU_OK;
 }
 
+// lanes per CSR row of the SpMV kernels (2, 4 or 8)
 int row_width(anigpu_ctx* h) {
+#ifdef SOLVE_W_FORCE
+    (void)h;
+    return SOLVE_W_FORCE;
+#else
     const double avg = h->ndof ? (double)h->nnz / (double)h->ndof : 1.0;
-    return avg > 12 ? 8 : 4;
+    return avg > 48 ? 8 : (avg > 12 ? SOLVE_W_P2 : 2);
+#endif
 }
 
 int nblocks_for(anigpu_ctx* h, int64_t work_items) {
@@ -537,9 +546,11 @@ int run_spmv(anigpu_ctx* h, const void* vals, int precision, const double* x, do
 #define SPMV(VR, WW) spmv_kernel<VR, double, WW><<<g, kBlock, 0, h->stream>>>(n, h->rowptr, h->col, (const VR*)vals, x, y)
     if (precision == ANIGPU_F32) {
         if (W == 8) SPMV(float, 8);
+        else if (W == 2) SPMV(float, 2);
         else SPMV(float, 4);
     } else {
         if (W == 8) SPMV(double, 8);
+        else if (W == 2) SPMV(double, 2);
         else SPMV(double, 4);
     }
 #undef SPMV
@@ -562,22 +573,17 @@ int run_solve(anigpu_ctx* h, int method, const void* vals, int precision, const 
     cudaEventRecord(e0, h->stream);
     const int W = row_width(h);
     switch (method) {
+#define BY_W(FN, VR)                                                                              \
+    (W == 8 ? FN<VR, 8>(h, w, (const VR*)vals, b, x, rtol, maxit, st)                             \
+            : W == 2 ? FN<VR, 2>(h, w, (const VR*)vals, b, x, rtol, maxit, st)                    \
+                     : FN<VR, 4>(h, w, (const VR*)vals, b, x, rtol, maxit, st))
         case ANIGPU_SOLVE_JACOBI_PCG:
-            if (precision == ANIGPU_F64)
-                rc = W == 8 ? solve_jacobi_pcg<double, 8>(h, w, (const double*)vals, b, x, rtol, maxit, st)
-                            : solve_jacobi_pcg<double, 4>(h, w, (const double*)vals, b, x, rtol, maxit, st);
-            else
-                rc = W == 8 ? solve_jacobi_pcg<float, 8>(h, w, (const float*)vals, b, x, rtol, maxit, st)
-                            : solve_jacobi_pcg<float, 4>(h, w, (const float*)vals, b, x, rtol, maxit, st);
+            rc = precision == ANIGPU_F64 ? BY_W(solve_jacobi_pcg, double) : BY_W(solve_jacobi_pcg, float);
             break;
         case ANIGPU_SOLVE_IR_CG32:
-            if (precision == ANIGPU_F64)
-                rc = W == 8 ? solve_ir_cg32<double, 8>(h, w, (const double*)vals, b, x, rtol, maxit, st)
-                            : solve_ir_cg32<double, 4>(h, w, (const double*)vals, b, x, rtol, maxit, st);
-            else
-                rc = W == 8 ? solve_ir_cg32<float, 8>(h, w, (const float*)vals, b, x, rtol, maxit, st)
-                            : solve_ir_cg32<float, 4>(h, w, (const float*)vals, b, x, rtol, maxit, st);
+            rc = precision == ANIGPU_F64 ? BY_W(solve_ir_cg32, double) : BY_W(solve_ir_cg32, float);
             break;
+#undef BY_W
         case ANIGPU_SOLVE_FCG_LEARNED:
             rc = run_fcg_learned(h, vals, precision, b, x, rtol, maxit, st);
             break;
