@@ -607,21 +607,21 @@ __global__ void ROW_BOUNDS row_gather_kernel(RowParams p, const Real* __restrict
     // records ahead of the queue are read in aligned pairs: when the next index is even the
     // pair is loaded and its second record kept for the following iteration
     ScatterRec pend = ScatterRec{0u, 0u, 0u, 0u};
-    if (nloop > 0) {
+    // loads past the row's last incidence are skipped (their values are never used)
 #pragma unroll
-        for (int j = 0; j < RD; ++j) Rq[j] = p.recs[ib + min(j, last)];
+    for (int j = 0; j < RD; ++j)
+        if (j <= last) Rq[j] = p.recs[ib + j];
 #pragma unroll
-        for (int j = 0; j < KD; ++j) Kq[j].load(tetK + KS * (int64_t)Rq[j].tet);
-        const int64_t r0i = ib + min(RD, last);
-        if (r0i & 1) pend = p.recs[r0i];
-    }
+    for (int j = 0; j < KD; ++j)
+        if (j <= last) Kq[j].load(tetK + KS * (int64_t)Rq[j].tet);
+    if (RD <= last && ((ib + RD) & 1)) pend = p.recs[ib + RD];
 #pragma unroll kRowUnroll
     for (int k = 0; k < nloop; ++k) {
         KVec<Real, KS> Kn;
-        Kn.load(tetK + KS * (int64_t)Rq[KD].tet);
-        const int64_t ridx = ib + min(k + RD, last);
+        if (k + KD <= last) Kn.load(tetK + KS * (int64_t)Rq[KD].tet);
+        const int64_t ridx = ib + k + RD;
         ScatterRec Rn = pend;
-        if (!(ridx & 1)) load_rec_pair(p.recs + ridx, Rn, pend);
+        if (k + RD <= last && !(ridx & 1)) load_rec_pair(p.recs + ridx, Rn, pend);
         const ScatterRec r0 = Rq[0];
         const KVec<Real, KS>& K0 = Kq[0];
         const int i = r0.meta & 15;
