@@ -2,7 +2,8 @@
 // FP64 residual replacement (a new component: the reference hands its matrix to INMOST's
 // ILU-Krylov solver, examples/tutorials/ex1.cpp:161-163).
 //
-// Iteration k (FCG(1): one A-orthogonalisation against the previous direction):
+// Iteration k (FCG(1): one A-orthogonalisation against the previous direction; the scalars of
+// a step are formed once by one-block kernels that the vector kernels read):
 //     q = A p ;  alpha = r.z / p.q ;  d += alpha p ;  r -= alpha q
 //     z = M r ;  beta = -(z.q) / (p.q) ;  p = z + beta p
 // d is an FP32 correction that is folded into the FP64 solution x at every residual
@@ -47,6 +48,10 @@ constexpr int kW = FCG_W;            // lanes per CSR row
 
 struct FcgScalars {
     double rz;        // r.z of the current direction
+    double pq;        // p.q of the current step
+    double alpha, beta;
+    int brk;          // p.q of the current step is not positive (or not finite): no update
+    int pad;
     double rr;        // recursive ||r||^2 after the last step
     double rrep2;     // kDelta^2 * ||r||^2 at the last replacement
     double tol2;      // (rtol ||b||)^2
@@ -107,21 +112,32 @@ __global__ void __launch_bounds__(kB) spmv_dot_kernel(int64_t n, const int64_t* 
     if (threadIdx.x == 0) part[blockIdx.x] = t;
 }
 
-// alpha = rz / pq ; d += alpha p ; r -= alpha q ; partials of r.r
+// alpha = rz / pq, once (one block): the update kernels read it
+__global__ void alpha_kernel(const double* __restrict__ part_pq, int nb_pq, FcgScalars* __restrict__ sc,
+                             const int* __restrict__ stop) {
+    __shared__ double sh[33];
+    if (*stop) return;
+    const double pq = sum_parts_d(part_pq, nb_pq, sh);
+    if (threadIdx.x == 0) {
+        const double al = sc->rz / pq;
+        sc->pq = pq;
+        sc->brk = (!(pq > 0) || !isfinite(al)) ? 1 : 0;
+        sc->alpha = sc->brk ? 0.0 : al;
+    }
+}
+
+// d += alpha p ; r -= alpha q ; partials of r.r
 __global__ void __launch_bounds__(kB) update_kernel(int64_t n, float* __restrict__ d, float* __restrict__ r,
                                                     const float* __restrict__ p, const float* __restrict__ q,
-                                                    const double* __restrict__ part_pq, int nb_pq,
                                                     double* __restrict__ part_rr, const FcgScalars* __restrict__ sc,
                                                     const int* __restrict__ stop) {
     __shared__ double sh[33];
     if (*stop) return;
-    const double pq = sum_parts_d(part_pq, nb_pq, sh);
-    const double al = sc->rz / pq;
-    if (!(pq > 0) || !isfinite(al)) {  // breakdown: no update; the status check stops the batch
+    if (sc->brk) {  // breakdown: no update; the status check stops the batch
         if (threadIdx.x == 0) part_rr[blockIdx.x] = 0;
         return;
     }
-    const float a = (float)al;
+    const float a = (float)sc->alpha;
     float arr = 0.f;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         d[i] = fmaf(a, p[i], d[i]);
@@ -155,40 +171,43 @@ __global__ void __launch_bounds__(kB) jacobi_dot_kernel(int64_t n, const float* 
     if (threadIdx.x == 0) part_zq[blockIdx.x] = t;
 }
 
-// beta = -(z.q)/(p.q) ; p = z + beta p ; status of this step
-__global__ void __launch_bounds__(kB) pupdate_kernel(int64_t n, float* __restrict__ p, const float* __restrict__ z,
-                                                     const double* __restrict__ part_rz,
-                                                     const double* __restrict__ part_zq, int nb_vec,
-                                                     const double* __restrict__ part_pq, int nb_pq,
-                                                     const double* __restrict__ part_rr, FcgScalars* __restrict__ sc,
-                                                     int par) {
+// beta = -(z.q)/(p.q) and the status of this step, once (one block)
+__global__ void beta_kernel(const double* __restrict__ part_rz, const double* __restrict__ part_zq, int nb_prec,
+                            const double* __restrict__ part_rr, int nb_vec, FcgScalars* __restrict__ sc, int par) {
     __shared__ double sh[33];
     const int prev = sc->st[par ^ 1];
     if (prev) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) sc->st[par] = prev;  // carry the stop through the batch
+        if (threadIdx.x == 0) sc->st[par] = prev;  // carry the stop through the batch
         return;
     }
-    const double rz = sum_parts_d(part_rz, nb_vec, sh);
-    const double zq = sum_parts_d(part_zq, nb_vec, sh);
-    const double pq = sum_parts_d(part_pq, nb_pq, sh);
+    const double rz = sum_parts_d(part_rz, nb_prec, sh);
+    const double zq = sum_parts_d(part_zq, nb_prec, sh);
     const double rr = sum_parts_d(part_rr, nb_vec, sh);
-    const float beta = pq > 0 ? (float)(-zq / pq) : 0.f;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        p[i] = fmaf(beta, p[i], z[i]);
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        int s = 0;
-        if (!(pq > 0) || !(rz > 0) || !isfinite(rz) || !isfinite(rr) || !isfinite(zq)) {
+    if (threadIdx.x == 0) {
+        const double pq = sc->pq;
+        sc->beta = pq > 0 ? -zq / pq : 0.0;
+        if (sc->brk || !(rz > 0) || !isfinite(rz) || !isfinite(rr) || !isfinite(zq)) {
             sc->st[par] = 2;  // breakdown: the step is not counted and the scalars stay
             return;
         }
         sc->rz = rz;
         sc->rr = rr;
         sc->iter += 1;
-        if (rr <= sc->tol2) s = 1;
-        else if (rr <= sc->rrep2) s = 3;
-        else if (sc->iter >= sc->maxit) s = 4;
-        sc->st[par] = s;
+        int st = 0;
+        if (rr <= sc->tol2) st = 1;
+        else if (rr <= sc->rrep2) st = 3;
+        else if (sc->iter >= sc->maxit) st = 4;
+        sc->st[par] = st;
     }
+}
+
+// p = z + beta p (skipped when the previous step stopped the batch)
+__global__ void __launch_bounds__(kB) pupdate_kernel(int64_t n, float* __restrict__ p, const float* __restrict__ z,
+                                                     const FcgScalars* __restrict__ sc, int par) {
+    if (sc->st[par ^ 1]) return;
+    const float beta = (float)sc->beta;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = fmaf(beta, p[i], z[i]);
 }
 
 // x += d ; d = 0
@@ -255,6 +274,7 @@ __global__ void restart_scalars_kernel(FcgScalars* __restrict__ sc, const double
         sc->rrep2 = kDelta * kDelta * rr;
         sc->tol2 = tol2;
         sc->maxit = maxit;
+        sc->brk = 0;
         if (first) sc->iter = 0;
         sc->st[0] = 0;
         sc->st[1] = 0;
@@ -322,15 +342,15 @@ struct Ctx {
     const double* b;
     double* x;
     int64_t n;
-    int nb_rows, nb_vec;
+    int nb_rows, nb_vec, nb_prec;  // nb_prec: blocks (partials) of the preconditioner's r.z, z.q
     double *part_pq, *part_rr, *part_bb, *part_rz, *part_zq;
 };
 
 // z = M r (mode 0) or D^-1 r (mode 1); partials of r.z (and z.qold)
 int precond(Ctx& c, int mode, const float* qold, const int* stop) {
-    if (mode == 0) return gnn_precond_f32(c.h, c.w->r, c.w->z, qold, c.part_rz, c.part_zq, c.nb_vec, stop);
-    jacobi_dot_kernel<<<c.nb_vec, kB, 0, c.h->stream>>>(c.n, c.w->r, c.w->dinv, qold, c.w->z, c.part_rz, c.part_zq,
-                                                        stop);
+    if (mode == 0) return gnn_precond_f32(c.h, c.w->r, c.w->z, qold, c.part_rz, c.part_zq, c.nb_prec, stop);
+    jacobi_dot_kernel<<<c.nb_prec, kB, 0, c.h->stream>>>(c.n, c.w->r, c.w->dinv, qold, c.w->z, c.part_rz, c.part_zq,
+                                                         stop);
     ANI_LAUNCHED(c.h);
     return ANIGPU_OK;
 }
@@ -342,11 +362,14 @@ int one_iteration(Ctx& c, int mode, int par) {
     const int* stop = &w->sc->st[par ^ 1];
     spmv_dot_kernel<<<c.nb_rows, kB, 0, s>>>(c.n, h->rowptr, h->col, c.vals, w->p, w->q, c.part_pq, stop);
     ANI_LAUNCHED(h);
-    update_kernel<<<c.nb_vec, kB, 0, s>>>(c.n, w->d, w->r, w->p, w->q, c.part_pq, c.nb_rows, c.part_rr, w->sc, stop);
+    alpha_kernel<<<1, kB, 0, s>>>(c.part_pq, c.nb_rows, w->sc, stop);
+    ANI_LAUNCHED(h);
+    update_kernel<<<c.nb_vec, kB, 0, s>>>(c.n, w->d, w->r, w->p, w->q, c.part_rr, w->sc, stop);
     ANI_LAUNCHED(h);
     RC_(precond(c, mode, w->q, stop));
-    pupdate_kernel<<<c.nb_vec, kB, 0, s>>>(c.n, w->p, w->z, c.part_rz, c.part_zq, c.nb_vec, c.part_pq, c.nb_rows,
-                                           c.part_rr, w->sc, par);
+    beta_kernel<<<1, kB, 0, s>>>(c.part_rz, c.part_zq, c.nb_prec, c.part_rr, c.nb_vec, w->sc, par);
+    ANI_LAUNCHED(h);
+    pupdate_kernel<<<c.nb_vec, kB, 0, s>>>(c.n, w->p, w->z, w->sc, par);
     ANI_LAUNCHED(h);
     return ANIGPU_OK;
 }
@@ -407,7 +430,7 @@ int restart(Ctx& c, int mode, bool reset_p, double rr, double tol2, int64_t maxi
     cudaStream_t s = h->stream;
     RC_(precond(c, mode, nullptr, nullptr));
     if (reset_p) ANI_CUDA(h, cudaMemcpyAsync(c.w->p, c.w->z, sizeof(float) * c.n, cudaMemcpyDeviceToDevice, s));
-    restart_scalars_kernel<<<1, kB, 0, s>>>(c.w->sc, c.part_rz, c.nb_vec, rr, tol2, (long long)maxit, first ? 1 : 0);
+    restart_scalars_kernel<<<1, kB, 0, s>>>(c.w->sc, c.part_rz, c.nb_prec, rr, tol2, (long long)maxit, first ? 1 : 0);
     ANI_LAUNCHED(h);
     return ANIGPU_OK;
 }
@@ -436,9 +459,10 @@ int run_fcg_learned(anigpu_ctx* h, const void* vals, int precision, const double
         w->key_vals = vals;
         w->key_gen = gnn_bind_generation(h);
     }
-    Ctx c{h, w, (const float*)vals, b, x, h->ndof, 0, 0, nullptr, nullptr, nullptr, nullptr, nullptr};
+    Ctx c{h, w, (const float*)vals, b, x, h->ndof, 0, 0, 0, nullptr, nullptr, nullptr, nullptr, nullptr};
     c.nb_rows = nblocks(c.n * kW);
     c.nb_vec = nblocks(c.n);
+    c.nb_prec = c.nb_vec;
     c.part_pq = w->part;
     c.part_rr = w->part + kMaxP;
     c.part_bb = w->part + 2 * kMaxP;  // follows part_rr: checkpoint sums both with one kernel

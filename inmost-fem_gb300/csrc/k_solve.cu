@@ -4,13 +4,14 @@
 //
 //   * CSR SpMV: a group of W lanes per row (W = 8 for P2-like rows, 4 for P1), FP64 or
 //     FP32 values, FP64 or FP32 vectors, accumulation in the vector type.
-//   * Jacobi-PCG: three kernels per iteration
+//   * Jacobi-PCG: five kernels per iteration
 //       spmv_dot   q = A p, block partials of p.q
-//       update     alpha = rz/pq; x += alpha p; r -= alpha q; z = Dinv r; partials r.z, r.r
-//       pupdate    beta = rz_new/rz; p = z + beta p; convergence flag
-//     Every global reduction is two-stage with a fixed order (per-block tree, then every
-//     consumer block sums the block partials in index order), so runs are bitwise
-//     reproducible.  The scalars live on the device; a converged solve sets a device flag
+//       alpha      (one block) alpha = rz / pq
+//       update     x += alpha p; r -= alpha q; z = Dinv r; partials r.z, r.r
+//       beta       (one block) beta = rz_new / rz; convergence flag
+//       pupdate    p = z + beta p
+//     Every global reduction is two-stage with a fixed order (per-block tree, then one block
+//     sums the block partials in index order), so runs are bitwise reproducible.  The scalars live on the device; a converged solve sets a device flag
 //     after which the remaining kernels of a batch return immediately, so batches of
 //     iterations run from a captured CUDA graph without host round trips.
 //   * IR_CG32: FP32-SpMV Jacobi-CG on FP32 vectors inside FP64 iterative refinement
@@ -30,10 +31,11 @@ constexpr int kMaxBlocks = 2048;
 
 struct PcgScalars {
     double rz[2];     // r.z by iteration parity
-    double pq;        // unused slot kept for alignment
+    double alpha;     // step length of the current iteration
     double bb;        // ||b||^2 (or of the refinement rhs)
     double tol2;      // (rtol * ||b||)^2
     double rr;        // last ||r||^2
+    double beta;      // direction update of the current iteration
     long long iter;   // completed iterations
     long long maxit;
     int done;         // 1 converged, 2 breakdown / maxit
@@ -115,19 +117,24 @@ __global__ void __launch_bounds__(kBlock) spmv_dot_kernel(int64_t n, const int64
     if (threadIdx.x == 0) part[blockIdx.x] = tot;
 }
 
-// alpha = rz/pq ; x += alpha p ; r -= alpha q ; z = dinv r ; partials r.z and r.r
-template <typename T, typename X>
-__global__ void __launch_bounds__(kBlock) update_kernel(int64_t n, int parity, X* __restrict__ x, T* __restrict__ r,
-                                                        T* __restrict__ z, const T* __restrict__ p,
-                                                        const T* __restrict__ q, const T* __restrict__ dinv,
-                                                        const double* __restrict__ part_pq, int nb,
-                                                        double* __restrict__ part_rz, double* __restrict__ part_rr,
-                                                        PcgScalars* __restrict__ sc) {
+// alpha = rz / pq, once (one block); the vector kernels read it
+__global__ void alpha_kernel(int parity, const double* __restrict__ part_pq, int nb, PcgScalars* __restrict__ sc) {
     __shared__ double sh[33];
     if (sc->done) return;
     const double pq = sum_partials(part_pq, nb, sh);
-    const double rz = sc->rz[parity];
-    const double alpha = rz / pq;
+    if (threadIdx.x == 0) sc->alpha = sc->rz[parity] / pq;
+}
+
+// x += alpha p ; r -= alpha q ; z = dinv r ; partials r.z and r.r
+template <typename T, typename X>
+__global__ void __launch_bounds__(kBlock) update_kernel(int64_t n, X* __restrict__ x, T* __restrict__ r,
+                                                        T* __restrict__ z, const T* __restrict__ p,
+                                                        const T* __restrict__ q, const T* __restrict__ dinv,
+                                                        double* __restrict__ part_rz, double* __restrict__ part_rr,
+                                                        const PcgScalars* __restrict__ sc) {
+    __shared__ double sh[33];
+    if (sc->done) return;
+    const double alpha = sc->alpha;
     const T a = (T)alpha;
     const X ax = (X)alpha;
     T arz = 0, arr = 0;
@@ -149,27 +156,32 @@ __global__ void __launch_bounds__(kBlock) update_kernel(int64_t n, int parity, X
     }
 }
 
-// beta = rz_new / rz ; p = z + beta p ; convergence / breakdown flags
-template <typename T>
-__global__ void __launch_bounds__(kBlock) pupdate_kernel(int64_t n, int parity, T* __restrict__ p,
-                                                         const T* __restrict__ z, const double* __restrict__ part_rz,
-                                                         const double* __restrict__ part_rr, int nb,
-                                                         PcgScalars* __restrict__ sc) {
+// beta = rz_new / rz and the convergence / breakdown flags, once (one block)
+__global__ void beta_kernel(int parity, const double* __restrict__ part_rz, const double* __restrict__ part_rr, int nb,
+                            PcgScalars* __restrict__ sc) {
     __shared__ double sh[33];
     if (sc->done) return;
     const double rz_new = sum_partials(part_rz, nb, sh);
     const double rr = sum_partials(part_rr, nb, sh);
-    const double beta = rz_new / sc->rz[parity];
-    const T b = (T)beta;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        p[i] = z[i] + b * p[i];
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (threadIdx.x == 0) {
+        const double beta = rz_new / sc->rz[parity];
+        sc->beta = beta;
         sc->rz[parity ^ 1] = rz_new;
         sc->rr = rr;
         sc->iter += 1;
         if (rr <= sc->tol2) sc->done = 1;
         else if (!isfinite(rr) || !isfinite(beta) || sc->iter >= sc->maxit) sc->done = 2;
     }
+}
+
+// p = z + beta p
+template <typename T>
+__global__ void __launch_bounds__(kBlock) pupdate_kernel(int64_t n, T* __restrict__ p, const T* __restrict__ z,
+                                                         const PcgScalars* __restrict__ sc) {
+    if (sc->done) return;
+    const T b = (T)sc->beta;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = z[i] + b * p[i];
 }
 
 // r = b - A x (FP64 vectors), z = dinv r, p = z; partials r.z, r.r, b.b
@@ -390,9 +402,10 @@ int pcg_core(anigpu_ctx* h, SolveWs* w, const VR* vals, const double* b, X* x, T
             for (int it = 0; it < kBatch; ++it) {
                 const int par = it & 1;
                 spmv_dot_kernel<VR, T, W><<<nb_rows, kBlock, 0, s>>>(n, h->rowptr, h->col, vals, p, q, part_pq, w->sc);
-                update_kernel<T, X><<<nb_vec, kBlock, 0, s>>>(n, par, x, r, z, p, q, dinv, part_pq, nb_rows, part_rz,
-                                                             part_rr, w->sc);
-                pupdate_kernel<T><<<nb_vec, kBlock, 0, s>>>(n, par, p, z, part_rz, part_rr, nb_vec, w->sc);
+                alpha_kernel<<<1, kBlock, 0, s>>>(par, part_pq, nb_rows, w->sc);
+                update_kernel<T, X><<<nb_vec, kBlock, 0, s>>>(n, x, r, z, p, q, dinv, part_rz, part_rr, w->sc);
+                beta_kernel<<<1, kBlock, 0, s>>>(par, part_rz, part_rr, nb_vec, w->sc);
+                pupdate_kernel<T><<<nb_vec, kBlock, 0, s>>>(n, p, z, w->sc);
             }
             if (cudaStreamEndCapture(s, &graph) == cudaSuccess && graph) {
                 if (cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) exec = nullptr;
@@ -406,15 +419,16 @@ int pcg_core(anigpu_ctx* h, SolveWs* w, const VR* vals, const double* b, X* x, T
     while (true) {
         if (exec) {
             ANI_CUDA(h, cudaGraphLaunch(exec, s));
-            h->launches += 3 * kBatch;
+            h->launches += 5 * kBatch;
         } else {
             for (int it = 0; it < kBatch; ++it) {
                 const int par = it & 1;
                 spmv_dot_kernel<VR, T, W><<<nb_rows, kBlock, 0, s>>>(n, h->rowptr, h->col, vals, p, q, part_pq, w->sc);
-                update_kernel<T, X><<<nb_vec, kBlock, 0, s>>>(n, par, x, r, z, p, q, dinv, part_pq, nb_rows, part_rz,
-                                                             part_rr, w->sc);
-                pupdate_kernel<T><<<nb_vec, kBlock, 0, s>>>(n, par, p, z, part_rz, part_rr, nb_vec, w->sc);
-                h->launches += 3;
+                alpha_kernel<<<1, kBlock, 0, s>>>(par, part_pq, nb_rows, w->sc);
+                update_kernel<T, X><<<nb_vec, kBlock, 0, s>>>(n, x, r, z, p, q, dinv, part_rz, part_rr, w->sc);
+                beta_kernel<<<1, kBlock, 0, s>>>(par, part_rz, part_rr, nb_vec, w->sc);
+                pupdate_kernel<T><<<nb_vec, kBlock, 0, s>>>(n, p, z, w->sc);
+                h->launches += 5;
             }
             ANI_CUDA(h, cudaGetLastError());
         }
