@@ -137,8 +137,9 @@ def run_elasticity(args, local, peak):
     """Vector P2 linear elasticity on 48^3 x 6 perturbed Kuhn tets (663,552 tets): per-tet Lame
     parameters from E ~ lognormal(0, 0.5^2), nu ~ U[0.2, 0.45]; clamped face x = 0; unit traction
     (1, 0, 0) on x = 1 as its consistent P2 nodal loads (area/3 on each edge DOF of a face, 0 on the
-    vertices); FP32 assembly timed back to back, then FP64 Jacobi-PCG (FP64 assembly) and IR-CG32
-    (FP32 assembly) to 1e-8."""
+    vertices); FP32 assembly timed back to back, then FP64 Jacobi-PCG (FP64 assembly), IR-CG32
+    (FP32 assembly) and flexible CG with the learned preconditioner (FP32 assembly, FP64 residual
+    replacement) to 1e-8."""
     import torch
 
     import anigpu
@@ -204,6 +205,29 @@ def run_elasticity(args, local, peak):
             x, st = lib.solve(vv, bd, method, prec, rtol=1e-8, maxit=200000, check=False)
         out[name] = {"seconds": st.seconds, "iterations": st.iterations, "rel_residual_f64": st.rel_residual}
     out["max_x_displacement"] = float(x[:ndof // 3].max().item())
+    try:
+        from anigpu import learned
+        prec = anigpu.LearnedPreconditioner(lib, layers=4, act=anigpu.BF16, seed=1)
+        trained = os.path.exists(learned.ELASTIC_WEIGHTS)
+        if trained:
+            learned.load_default(prec, "elastic")
+        for _ in range(2):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            prec.bind(vals32, anigpu.F32, anigpu.TENSOR_LAME, D_dev)
+            torch.cuda.synchronize()
+            bind_s = time.perf_counter() - t0
+            xl, st = lib.solve(vals32, bd, anigpu.SOLVE_FCG_LEARNED, anigpu.F32, rtol=1e-8, maxit=200000,
+                               check=True)
+        r64 = bd - lib.spmv(vals64, xl, anigpu.F64)
+        out["fcg_learned"] = {"seconds": st.seconds, "bind_seconds": bind_s, "iterations": st.iterations,
+                              "replacements": st.outer_iterations, "fallback_steps": st.fallback_steps,
+                              "rel_residual_f64": st.rel_residual,
+                              "rel_residual_vs_f64_matrix": float(r64.norm() / bd.norm()),
+                              "weights": "trained (anigpu/weights)" if trained else "untrained",
+                              "speedup_vs_jacobi_pcg_f64": out["jacobi_pcg_f64"]["seconds"] / (bind_s + st.seconds)}
+    except anigpu.AnigpuError as e:
+        out["fcg_learned"] = {"unavailable": str(e)}
     lib.close()
     return out
 

@@ -195,18 +195,21 @@ int anigpu_solve(anigpu_handle h, int method, const void* vals, int precision, c
 /* ---- learned preconditioner for ANIGPU_SOLVE_FCG_LEARNED (no counterpart in the reference,
  * whose solves go through INMOST's ILU-Krylov, examples/tutorials/ex1.cpp:161-163).
  *   M r = D^-1 r + P Dc^-1/2 B B^T Dc^-1/2 P^T r,   B = sum_{k<4} diag(a_k) A_hat^k
- *   (symmetric positive definite by construction).  P interpolates vertex values onto the P2
- *   DOFs, Dc = the vertex diagonal, A_hat = -Dc^-1/2 A_vv' Dc^-1/2 over the vertex-vertex
- *   couplings.  The per-vertex coefficients a (4 per vertex) come from a message-passing
- *   network on that vertex graph, run once per bind on static features (log A_vv and the
- *   local mean of log(trace D / 3)).  Hidden width 64, `layers` residual layers, activations
+ *   (symmetric positive definite by construction).  Coarse nodes are the vertex DOFs of every
+ *   component (ANIGPU_P2: nv nodes; ANIGPU_VEC3_P2: 3 nv nodes, node c*nv + v = vertex v of
+ *   component c).  P interpolates vertex values onto the P2 DOFs of the same component, Dc =
+ *   the coarse diagonal, A_hat = -Dc^-1/2 A_cc' Dc^-1/2 over the off-diagonal couplings between
+ *   coarse nodes (across components too).  The per-node coefficients a (4 per node) come from a
+ *   message-passing network on that coarse graph, run once per bind on static features (log of
+ *   the diagonal and the local mean of log(trace D / 3), for ANIGPU_TENSOR_LAME of
+ *   log(lambda + 2 mu)).  Hidden width 64, `layers` residual layers, activations
  *   in act_precision (ANIGPU_BF16, or ANIGPU_F32 for gradient checks), FP32 accumulation,
  *   FP32 master parameters.
  * init: random parameters (seeded; the untrained B is the identity); get/set_params: the flat
  *   FP32 parameter vector (checkpoint); bind: the system the preconditioner serves (values of
- *   a P2 problem, and the per-tet tensor for the features), runs the network;
+ *   a P2 or vector P2 problem, and the per-tet tensor for the features), runs the network;
  * apply: z = M r (f64 vectors); apply_f32: z = M r with the fused FP32 kernels the solver
- *   uses (f32[ndof] vectors); coefficients: a as f32[nv][4] into a device buffer;
+ *   uses (f32[ndof] vectors); coefficients: a as f32[ncomp*nv][4] into a device buffer;
  * loss_grad: L = (M r - e)^T A (M r - e) / (e^T A e) for a pair (r, e = A^-1 r), gradients
  *   accumulated; adam: one Adam step on the accumulated gradients (then zeroed), network re-run. */
 int anigpu_gnn_init(anigpu_handle h, int layers, int act_precision, uint64_t seed);

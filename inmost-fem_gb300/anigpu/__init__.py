@@ -470,10 +470,11 @@ class LearnedPreconditioner:
         return z
 
     def coefficients(self):
-        """The network output a, float32 [nv, 4]."""
+        """The network output a, float32 [ncomp * nv, 4] (row c * nv + v: vertex v, component c)."""
         torch = self.lib.torch
+        ncomp = 3 if self.lib.space in (VEC3_P1, VEC3_P2) else 1
         with self.lib.on_stream():
-            a = torch.empty((self.lib.nv, 4), dtype=torch.float32, device=f"cuda:{self.lib.device}")
+            a = torch.empty((ncomp * self.lib.nv, 4), dtype=torch.float32, device=f"cuda:{self.lib.device}")
             self.lib._check(self.lib.lib.anigpu_gnn_coefficients(self.lib.h, _ptr(a)))
         return a
 

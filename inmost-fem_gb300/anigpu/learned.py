@@ -13,6 +13,7 @@ import anigpu
 
 WEIGHTS_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights")
 DEFAULT_WEIGHTS = os.path.join(WEIGHTS_DIR, "p2_aniso_l4.npy")
+ELASTIC_WEIGHTS = os.path.join(WEIGHTS_DIR, "p2_elastic_l4.npy")
 
 
 def training_pairs(lib, vals, b, ks=(0, 1, 2, 4, 8, 16, 32, 64, 128, 256), rtol=1e-10):
@@ -62,50 +63,82 @@ def mean_loss(prec, systems):
     return tot / max(cnt, 1)
 
 
-def load_default(prec):
-    """Set the committed trained parameters (P2, anisotropic tensors, 4 layers)."""
-    w = np.load(DEFAULT_WEIGHTS)
+def load_default(prec, problem="aniso"):
+    """Set committed trained parameters: "aniso" (scalar P2, anisotropic tensors) or "elastic"
+    (vector P2 elasticity, per-tet Lame parameters); 4 layers."""
+    w = np.load(DEFAULT_WEIGHTS if problem == "aniso" else ELASTIC_WEIGHTS)
     prec.set_params(w)
     return w
 
 
+def lame_params(nt, seed):
+    """Per-tet (lambda, mu) from E ~ lognormal(0, 0.5^2), nu ~ U[0.2, 0.45]."""
+    from anigpu import meshgen
+    E = np.exp(0.5 * meshgen.normal(seed, nt))
+    nu = 0.2 + 0.25 * meshgen.uniform(seed + 1, nt)
+    return np.stack([E * nu / ((1 + nu) * (1 - 2 * nu)), E / (2 * (1 + nu))], axis=1)
+
+
+def make_systems(lib, problem, n, count, seed0=0):
+    """Seeded synthetic training systems on a perturbed Kuhn cube of n^3 x 6 tets.
+    aniso: scalar P2, anisotropic per-tet tensors (log-normal eigenvalues), Dirichlet boundary.
+    elastic: vector P2, per-tet Lame parameters, clamped face x = 0."""
+    from anigpu import meshgen
+    xyz, tets = meshgen.kuhn_cube(n, perturb=0.2, seed=7)
+    nt = tets.shape[0]
+    lib.mesh_upload(xyz, tets)
+    if problem == "aniso":
+        lib.problem_setup(anigpu.P2)
+        mask = meshgen.boundary_mask(lib.dof_coords().cpu().numpy())
+        kind = anigpu.TENSOR_TET_SYM
+    else:
+        lib.problem_setup(anigpu.VEC3_P2)
+        mask = (np.abs(lib.dof_coords().cpu().numpy()[:, 0]) < 1e-12).astype(np.uint8)
+        kind = anigpu.TENSOR_LAME
+    lib.set_dirichlet(mask)
+    systems = []
+    for sd in range(seed0, seed0 + count):
+        D = meshgen.aniso_tensors(nt, 1.5, 100 + sd) if problem == "aniso" else lame_params(nt, 2 * sd + 300)
+        v, _, _ = lib.assemble(kind, D, None, 1.0, 4, anigpu.F32)
+        v = v.clone()
+        b = meshgen.normal(500 + sd, lib.ndof) * (1 - mask)
+        systems.append((v, kind, D, training_pairs(lib, v, b)))
+    return systems
+
+
 def main(argv=None):
-    """Train the default parameters on seeded synthetic P2 problems (perturbed Kuhn cube,
-    anisotropic per-tet tensors with log-normal eigenvalues) and save them:
-        python -m anigpu.learned --n 12 --systems 200 --steps 2000 --out weights/p2_aniso_l4.npy
-    (200 systems x 10 Jacobi-PCG iterates = 2,000 residual/correction pairs)"""
+    """Train parameters on seeded synthetic problems and save them:
+        python -m anigpu.learned --problem aniso --n 12 --systems 200 --steps 2000
+        python -m anigpu.learned --problem elastic --n 8 --systems 64 --steps 1500
+    (each system gives 10 Jacobi-PCG iterates = 10 residual/correction pairs)"""
     import argparse
     import time
 
-    from anigpu import meshgen
     ap = argparse.ArgumentParser()
-    ap.add_argument("--n", type=int, default=12)
-    ap.add_argument("--systems", type=int, default=200)
-    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--problem", choices=("aniso", "elastic"), default="aniso")
+    ap.add_argument("--n", type=int, default=None)
+    ap.add_argument("--systems", type=int, default=None)
+    ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--lr", type=float, default=3e-3)
     ap.add_argument("--seed", type=int, default=1)
-    ap.add_argument("--out", default=DEFAULT_WEIGHTS)
+    ap.add_argument("--out", default=None)
     a = ap.parse_args(argv)
+    elastic = a.problem == "elastic"
+    n = a.n or (8 if elastic else 12)
+    count = a.systems or (64 if elastic else 200)
+    steps = a.steps or (1500 if elastic else 2000)
+    out = a.out or (ELASTIC_WEIGHTS if elastic else DEFAULT_WEIGHTS)
     lib = anigpu.Anigpu(0)
-    xyz, tets = meshgen.kuhn_cube(a.n, perturb=0.2, seed=7)
-    lib.mesh_upload(xyz, tets)
-    lib.problem_setup(anigpu.P2)
-    mask = meshgen.boundary_mask(lib.dof_coords().cpu().numpy())
-    lib.set_dirichlet(mask)
-    systems = []
-    for sd in range(a.systems):
-        D = meshgen.aniso_tensors(tets.shape[0], 1.5, 100 + sd)
-        v, _, _ = lib.assemble(anigpu.TENSOR_TET_SYM, D, None, 1.0, 4, anigpu.F32)
-        v = v.clone()
-        b = meshgen.normal(500 + sd, lib.ndof) * (1 - mask)
-        systems.append((v, anigpu.TENSOR_TET_SYM, D, training_pairs(lib, v, b)))
+    t0 = time.time()
+    systems = make_systems(lib, a.problem, n, count)
+    print(f"{count} systems ({lib.ndof} DOFs) in {time.time() - t0:.1f} s")
     prec = anigpu.LearnedPreconditioner(lib, layers=4, act=anigpu.BF16, seed=a.seed)
     t0 = time.time()
-    train(prec, systems, a.steps, lr=a.lr, lr_final=a.lr / 3, log_every=max(1, a.steps // 10))
-    print(f"trained {a.steps} steps in {time.time() - t0:.1f} s; mean loss {mean_loss(prec, systems[:4]):.4f}")
-    os.makedirs(os.path.dirname(os.path.abspath(a.out)), exist_ok=True)
-    np.save(a.out, prec.get_params())
-    print("saved", a.out)
+    train(prec, systems, steps, lr=a.lr, lr_final=a.lr / 3, log_every=max(1, steps // 10))
+    print(f"trained {steps} steps in {time.time() - t0:.1f} s; mean loss {mean_loss(prec, systems[:4]):.4f}")
+    os.makedirs(os.path.dirname(os.path.abspath(out)), exist_ok=True)
+    np.save(out, prec.get_params())
+    print("saved", out)
 
 
 if __name__ == "__main__":

@@ -15,7 +15,9 @@
 //
 // Fallback: Jacobi (z = D^-1 r).  The solve switches to it for the rest of the call when a step
 // breaks down (r.z <= 0 or p.q <= 0, non-finite values) or when the residual stops decreasing
-// (no new smallest residual over kStallBatches batches); the direction restarts from z.  Steps
+// (no new smallest residual over max(kStallBatches, half the batches run so far) batches: the
+// residual norm of CG is not monotone and its plateaus grow with the condition number); the
+// direction restarts from z.  Steps
 // taken with the Jacobi direction are counted in fallback_steps.
 //
 // The scalars live on the device.  Iterations run in captured batches of kBatch; each kernel
@@ -23,10 +25,12 @@
 // no kernel reads a word that another block of the same launch writes) and returns at once
 // when it is set.  Dot products are FP32 per thread and FP64 across threads, two-stage with a
 // fixed order, so runs reproduce bit for bit.
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
 #include "learned.h"
+#include "spmv_vec3.cuh"
 
 #define RC_(x)               \
     do {                     \
@@ -40,7 +44,7 @@ constexpr int kB = 256;
 constexpr int kMaxP = 1024;          // block partials per reduction
 constexpr int kBatch = 16;           // even: the status parity of a batch starts at 0
 constexpr double kDelta = 0.1;       // residual replacement threshold (ratio of norms)
-constexpr int kStallBatches = 8;     // batches without a new smallest residual -> Jacobi
+constexpr int kStallBatches = 32;    // batches without a new smallest residual -> Jacobi (at least)
 #ifndef FCG_W
 #define FCG_W 4
 #endif
@@ -106,6 +110,35 @@ __global__ void __launch_bounds__(kB) spmv_dot_kernel(int64_t n, const int64_t* 
         if (row < n && lane == 0) {
             q[row] = s;
             acc = fmaf(s, p[row], acc);
+        }
+    }
+    const double t = block_sum_d((double)acc, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+// q = A p ; partials of p.q -- vector (3-component) template, SPMV3_W lanes per scalar row
+__global__ void __launch_bounds__(kB) spmv3_dot_kernel(int64_t nds, int64_t nnz_s, const int64_t* __restrict__ rowptr_s,
+                                                       const int32_t* __restrict__ col_s,
+                                                       const float* __restrict__ vals, const float* __restrict__ p,
+                                                       float* __restrict__ q, double* __restrict__ part,
+                                                       const int* __restrict__ stop) {
+    __shared__ double sh[33];
+    if (*stop) return;
+    constexpr int W = SPMV3_W;
+    const int64_t rows_per_block = kB / W;
+    const int lane = threadIdx.x & (W - 1);
+    float acc = 0.f;
+    for (int64_t base = blockIdx.x * rows_per_block; base < nds; base += (int64_t)gridDim.x * rows_per_block) {
+        const int64_t r = base + threadIdx.x / W;
+        float s0, s1, s2;
+        vec3_rows<W>(r, lane, nds, nnz_s, rowptr_s, col_s, vals, p, s0, s1, s2);
+        if (r < nds && lane == 0) {
+            q[r] = s0;
+            q[nds + r] = s1;
+            q[2 * nds + r] = s2;
+            acc = fmaf(s0, p[r], acc);
+            acc = fmaf(s1, p[nds + r], acc);
+            acc = fmaf(s2, p[2 * nds + r], acc);
         }
     }
     const double t = block_sum_d((double)acc, sh);
@@ -343,6 +376,7 @@ struct Ctx {
     double* x;
     int64_t n;
     int nb_rows, nb_vec, nb_prec;  // nb_prec: blocks (partials) of the preconditioner's r.z, z.q
+    int nb_pq;                     // blocks (partials) of the SpMV's p.q
     double *part_pq, *part_rr, *part_bb, *part_rz, *part_zq;
 };
 
@@ -360,9 +394,13 @@ int one_iteration(Ctx& c, int mode, int par) {
     FcgWs* w = c.w;
     cudaStream_t s = h->stream;
     const int* stop = &w->sc->st[par ^ 1];
-    spmv_dot_kernel<<<c.nb_rows, kB, 0, s>>>(c.n, h->rowptr, h->col, c.vals, w->p, w->q, c.part_pq, stop);
+    if (h->ncomp == 3)
+        spmv3_dot_kernel<<<c.nb_pq, kB, 0, s>>>(h->nds, h->nnz_s, h->rowptr_s, h->col_s, c.vals, w->p, w->q, c.part_pq,
+                                                stop);
+    else
+        spmv_dot_kernel<<<c.nb_pq, kB, 0, s>>>(c.n, h->rowptr, h->col, c.vals, w->p, w->q, c.part_pq, stop);
     ANI_LAUNCHED(h);
-    alpha_kernel<<<1, kB, 0, s>>>(c.part_pq, c.nb_rows, w->sc, stop);
+    alpha_kernel<<<1, kB, 0, s>>>(c.part_pq, c.nb_pq, w->sc, stop);
     ANI_LAUNCHED(h);
     update_kernel<<<c.nb_vec, kB, 0, s>>>(c.n, w->d, w->r, w->p, w->q, c.part_rr, w->sc, stop);
     ANI_LAUNCHED(h);
@@ -459,8 +497,9 @@ int run_fcg_learned(anigpu_ctx* h, const void* vals, int precision, const double
         w->key_vals = vals;
         w->key_gen = gnn_bind_generation(h);
     }
-    Ctx c{h, w, (const float*)vals, b, x, h->ndof, 0, 0, 0, nullptr, nullptr, nullptr, nullptr, nullptr};
+    Ctx c{h, w, (const float*)vals, b, x, h->ndof, 0, 0, 0, 0, nullptr, nullptr, nullptr, nullptr, nullptr};
     c.nb_rows = nblocks(c.n * kW);
+    c.nb_pq = h->ncomp == 3 ? nblocks(h->nds * SPMV3_W) : c.nb_rows;
     c.nb_vec = nblocks(c.n);
     c.nb_prec = c.nb_vec;
     c.part_pq = w->part;
@@ -482,10 +521,11 @@ int run_fcg_learned(anigpu_ctx* h, const void* vals, int precision, const double
     if (rel > rtol && maxit > 0) {
         RC_(restart(c, mode, true, rr, tol2, maxit, true));
         double best = rr;
-        int stall = 0;
+        int64_t stall = 0, nbatch = 0;
         int64_t last_iter = 0;
         while (true) {
             RC_(batch(c, mode));
+            ++nbatch;
             ANI_CUDA(h, cudaMemcpyAsync(&hs, w->sc, sizeof(FcgScalars), cudaMemcpyDeviceToHost, s));
             ANI_CUDA(h, cudaStreamSynchronize(s));
             if (mode == 1) fallback += hs.iter - last_iter;
@@ -495,7 +535,7 @@ int run_fcg_learned(anigpu_ctx* h, const void* vals, int precision, const double
             if (hs.rr < best) {
                 best = hs.rr;
                 stall = 0;
-            } else if (++stall >= kStallBatches && mode == 0) {
+            } else if (++stall >= std::max<int64_t>(kStallBatches, nbatch / 2) && mode == 0) {
                 to_jacobi = true;
             }
             if (status == 2 && mode == 0) to_jacobi = true;

@@ -49,6 +49,24 @@ __device__ __forceinline__ __nv_bfloat16 cvt<__nv_bfloat16>(float v) {
     return __float2bfloat16_rn(v);
 }
 
+// coarse nodes are the vertex DOFs of every component: coarse id c*nv + v <-> fine DOF c*nds + v
+// (scalar P2: nds = ndof and the two numberings agree); fine DOF c*nds + nv + e is edge e of
+// component c.  At most 3 components, so the component is found by two compares.
+struct CMap {
+    int64_t nv, nds;
+    __device__ __forceinline__ int comp_fine(int64_t d) const { return d >= nds ? (d >= 2 * nds ? 2 : 1) : 0; }
+    __device__ __forceinline__ int comp_coarse(int64_t cid) const { return cid >= nv ? (cid >= 2 * nv ? 2 : 1) : 0; }
+    __device__ __forceinline__ int64_t fine_of(int64_t cid) const {
+        const int c = comp_coarse(cid);
+        return c * nds + (cid - c * nv);
+    }
+    __device__ __forceinline__ int64_t coarse_of(int64_t d) const {
+        const int c = comp_fine(d);
+        const int64_t s = d - c * nds;
+        return s < nv ? c * nv + s : -1;
+    }
+};
+
 struct Gnn {
     int layers = 4, act = ANIGPU_BF16;  // act: ANIGPU_F32 or ANIGPU_BF16
     int64_t nparam = 0;
@@ -58,7 +76,8 @@ struct Gnn {
     float* m2 = nullptr;
     float* wk = nullptr;     // parameters as the kernels see them (rounded to BF16 when act is BF16)
     // bound system
-    int64_t nc = 0;          // coarse nodes (vertices)
+    int64_t nc = 0;          // coarse nodes (vertex DOFs of every component)
+    CMap map{0, 0};
     int64_t nf = 0;          // fine DOFs
     int64_t* crow = nullptr; // coarse graph CSR
     int32_t* ccol = nullptr;
@@ -128,44 +147,48 @@ __global__ void fine_diag_kernel(int64_t n, const int64_t* __restrict__ rowptr, 
     diag[r] = d;
 }
 
-__global__ void coarse_count_kernel(int64_t nc, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
-                                    unsigned long long* __restrict__ cnt) {
+__global__ void coarse_count_kernel(int64_t nc, CMap m, const int64_t* __restrict__ rowptr,
+                                    const int32_t* __restrict__ col, unsigned long long* __restrict__ cnt) {
     const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (r >= nc) return;
+    const int64_t fr = m.fine_of(r);
     unsigned long long c = 0;
-    for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k) c += (col[k] < nc && col[k] != r) ? 1 : 0;
+    for (int64_t k = rowptr[fr]; k < rowptr[fr + 1]; ++k) c += (col[k] != fr && m.coarse_of(col[k]) >= 0) ? 1 : 0;
     cnt[r] = c;
 }
 
-__global__ void coarse_fill_kernel(int64_t nc, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
-                                   const void* __restrict__ vals, int f32, const float* __restrict__ diag,
-                                   const int64_t* __restrict__ crow, int32_t* __restrict__ ccol,
-                                   float* __restrict__ cval, float* __restrict__ isd) {
+__global__ void coarse_fill_kernel(int64_t nc, CMap m, const int64_t* __restrict__ rowptr,
+                                   const int32_t* __restrict__ col, const void* __restrict__ vals, int f32,
+                                   const float* __restrict__ diag, const int64_t* __restrict__ crow,
+                                   int32_t* __restrict__ ccol, float* __restrict__ cval, float* __restrict__ isd) {
     const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (r >= nc) return;
+    const int64_t fr = m.fine_of(r);
     int64_t w = crow[r];
-    const float dr = diag[r];
+    const float dr = diag[fr];
     isd[r] = dr > 0.f ? rsqrtf(dr) : 0.f;
-    for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k) {
+    for (int64_t k = rowptr[fr]; k < rowptr[fr + 1]; ++k) {
         const int32_t c = col[k];
-        if (c < nc && c != r) {
+        const int64_t cc = m.coarse_of(c);
+        if (c != fr && cc >= 0) {
             const float a = f32 ? ((const float*)vals)[k] : (float)((const double*)vals)[k];
             const float dd = dr * diag[c];
-            ccol[w] = c;
+            ccol[w] = (int32_t)cc;
             cval[w] = dd > 0.f ? -a * rsqrtf(dd) : 0.f;
             ++w;
         }
     }
 }
 
-// static features: log(A_vv), mean over incident tets of log(trace(D)/3)
-__global__ void static_feat_kernel(int64_t nc, const float* __restrict__ diag_f, const int64_t* __restrict__ inc_ptr,
-                                   const ScatterRec* __restrict__ recs, int kind, const double* __restrict__ D,
-                                   float* __restrict__ feat) {
-    const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (v >= nc) return;
-    const float d = diag_f[v];
-    feat[NF * v] = d > 0.f ? logf(d) : 0.f;
+// static features: log(A_vv), mean over incident tets of log(trace(D)/3) (Lame: of lambda + 2 mu)
+__global__ void static_feat_kernel(int64_t nc, CMap m, const float* __restrict__ diag_f,
+                                   const int64_t* __restrict__ inc_ptr, const ScatterRec* __restrict__ recs, int kind,
+                                   const double* __restrict__ D, float* __restrict__ feat) {
+    const int64_t cid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (cid >= nc) return;
+    const int64_t v = cid % m.nv;
+    const float d = diag_f[m.fine_of(cid)];
+    feat[NF * cid] = d > 0.f ? logf(d) : 0.f;
     float s = 0.f;
     const int64_t b = inc_ptr[v], e = inc_ptr[v + 1];
     for (int64_t k = b; k < e; ++k) {
@@ -174,9 +197,10 @@ __global__ void static_feat_kernel(int64_t nc, const float* __restrict__ diag_f,
         if (kind == ANIGPU_TENSOR_TET_SYM) tr = (float)((D[6 * t] + D[6 * t + 3] + D[6 * t + 5]) / 3.0);
         else if (kind == ANIGPU_TENSOR_TET_SCALAR) tr = (float)D[t];
         else if (kind == ANIGPU_TENSOR_CONST_SCALAR) tr = (float)D[0];
+        else if (kind == ANIGPU_TENSOR_LAME) tr = (float)(D[2 * t] + 2.0 * D[2 * t + 1]);
         s += logf(fmaxf(tr, 1e-30f));
     }
-    feat[NF * v + 1] = e > b ? s / (float)(e - b) : 0.f;
+    feat[NF * cid + 1] = e > b ? s / (float)(e - b) : 0.f;
 }
 
 __global__ void edge_ends_kernel(int64_t ne, int64_t nv, const int64_t* __restrict__ inc_ptr,
@@ -273,29 +297,36 @@ __global__ void feat_center_kernel(int64_t nc, int nb, const float* __restrict__
 
 // ------------------------------------------------------------ transfers
 // out_v = isd_v * (x_v + 1/2 sum over the edge DOFs e of v of x_e)        (Dc^-1/2 P^T x)
+// (v a coarse node; the edges are those of v's vertex, in v's component)
 template <typename T>
-__global__ void restrict_kernel(int64_t nc, const T* __restrict__ x, const int64_t* __restrict__ vrow,
+__global__ void restrict_kernel(int64_t nc, CMap m, const T* __restrict__ x, const int64_t* __restrict__ vrow,
                                 const int32_t* __restrict__ vedge, const float* __restrict__ isd,
                                 float* __restrict__ out) {
     const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (v >= nc) return;
+    const int c = m.comp_coarse(v);
+    const int64_t vs = v - c * m.nv;
+    const T* xc = x + c * m.nds;
     float s = 0.f;
-    for (int64_t k = vrow[v]; k < vrow[v + 1]; ++k) s += (float)x[vedge[k]];
-    out[v] = isd[v] * fmaf(0.5f, s, (float)x[v]);
+    for (int64_t k = vrow[vs]; k < vrow[vs + 1]; ++k) s += (float)xc[vedge[k]];
+    out[v] = isd[v] * fmaf(0.5f, s, (float)xc[vs]);
 }
 
 // z = dinv .* r + P c
 template <typename T>
-__global__ void prolong_kernel(int64_t nf, int64_t nv, const T* __restrict__ r, const float* __restrict__ diag_f,
+__global__ void prolong_kernel(int64_t nf, CMap m, const T* __restrict__ r, const float* __restrict__ diag_f,
                                const float* __restrict__ c, const int32_t* __restrict__ ends, T* __restrict__ z) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= nf) return;
     const float d = diag_f[i];
     T v = d != 0.f ? r[i] / (T)d : r[i];
-    if (i < nv) v += (T)c[i];
+    const int comp = m.comp_fine(i);
+    const int64_t s = i - comp * m.nds;
+    const float* cc = c + comp * m.nv;
+    if (s < m.nv) v += (T)cc[s];
     else {
-        const int64_t e = i - nv;
-        v += (T)0.5 * ((T)c[ends[2 * e]] + (T)c[ends[2 * e + 1]]);
+        const int64_t e = s - m.nv;
+        v += (T)0.5 * ((T)cc[ends[2 * e]] + (T)cc[ends[2 * e + 1]]);
     }
     z[i] = v;
 }
@@ -352,7 +383,7 @@ __device__ __forceinline__ float cw_sum(float s) {
 }
 
 // u = Dc^-1/2 P^T r ; t = a_{K-1} .* u
-__global__ void __launch_bounds__(256) restrict_scale_kernel(int64_t nc, const float* __restrict__ r,
+__global__ void __launch_bounds__(256) restrict_scale_kernel(int64_t nc, CMap m, const float* __restrict__ r,
                                                              const int64_t* __restrict__ vrow,
                                                              const int32_t* __restrict__ vedge,
                                                              const float* __restrict__ isd,
@@ -361,12 +392,15 @@ __global__ void __launch_bounds__(256) restrict_scale_kernel(int64_t nc, const f
     if (stop && *stop) return;
     const int64_t v = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / CW;
     const int lane = threadIdx.x & (CW - 1);
+    const int c = m.comp_coarse(v);
+    const int64_t vs = v - c * m.nv;
+    const float* rc = r + c * m.nds;
     float s = 0.f;
     if (v < nc)
-        for (int64_t k = vrow[v] + lane; k < vrow[v + 1]; k += CW) s += r[vedge[k]];
+        for (int64_t k = vrow[vs] + lane; k < vrow[vs + 1]; k += CW) s += rc[vedge[k]];
     s = cw_sum(s);
     if (v < nc && lane == 0) {
-        const float uu = isd[v] * fmaf(0.5f, s, r[v]);
+        const float uu = isd[v] * fmaf(0.5f, s, rc[vs]);
         u[v] = uu;
         t[v] = coef[K * v + K - 1] * uu;
     }
@@ -411,7 +445,7 @@ __global__ void __launch_bounds__(256) combine4_kernel(int64_t nc, const int64_t
 }
 
 // z = D^-1 r + P c ; block partials of r.z and z.qold (FP32 per thread, FP64 across the block)
-__global__ void __launch_bounds__(256) prolong_dot_kernel(int64_t nf, int64_t nv, const float* __restrict__ r,
+__global__ void __launch_bounds__(256) prolong_dot_kernel(int64_t nf, CMap m, const float* __restrict__ r,
                                                           const float* __restrict__ diag_f,
                                                           const float* __restrict__ c,
                                                           const int32_t* __restrict__ ends,
@@ -425,10 +459,13 @@ __global__ void __launch_bounds__(256) prolong_dot_kernel(int64_t nf, int64_t nv
         const float d = diag_f[i];
         const float ri = r[i];
         float zi = d != 0.f ? ri / d : ri;
-        if (i < nv) zi += c[i];
+        const int comp = m.comp_fine(i);
+        const int64_t s = i - comp * m.nds;
+        const float* cc = c + comp * m.nv;
+        if (s < m.nv) zi += cc[s];
         else {
-            const int64_t e = i - nv;
-            zi = fmaf(0.5f, c[ends[2 * e]] + c[ends[2 * e + 1]], zi);
+            const int64_t e = s - m.nv;
+            zi = fmaf(0.5f, cc[ends[2 * e]] + cc[ends[2 * e + 1]], zi);
         }
         z[i] = zi;
         arz = fmaf(ri, zi, arz);
@@ -848,7 +885,7 @@ int powers(anigpu_ctx* h, Gnn* g, const float* x, float* pw) {
 template <typename T>
 int apply_impl(anigpu_ctx* h, Gnn* g, const T* r, T* z) {
     cudaStream_t s = h->stream;
-    restrict_kernel<T><<<nblk(g->nc, 256), 256, 0, s>>>(g->nc, r, g->vrow, g->vedge, g->isd_c, g->u);
+    restrict_kernel<T><<<nblk(g->nc, 256), 256, 0, s>>>(g->nc, g->map, r, g->vrow, g->vedge, g->isd_c, g->u);
     ANI_LAUNCHED(h);
     // w = B^T u = sum_k A_hat^k (a_k .* u); then P_k = A_hat^k w; c = isd .* sum_k a_k .* P_k
     float* wv = g->qv;  // w lives in qv[0..nc) until the backward pass needs qv
@@ -856,7 +893,7 @@ int apply_impl(anigpu_ctx* h, Gnn* g, const T* r, T* z) {
     RC(powers(h, g, wv, g->pw));
     combine_kernel<<<nblk(g->nc, 256), 256, 0, s>>>(g->nc, g->coef, g->pw, g->isd_c, g->cc);
     ANI_LAUNCHED(h);
-    prolong_kernel<T><<<nblk(g->nf, 256), 256, 0, s>>>(g->nf, h->nv, r, g->diag_f, g->cc, g->edge_ends, z);
+    prolong_kernel<T><<<nblk(g->nf, 256), 256, 0, s>>>(g->nf, g->map, r, g->diag_f, g->cc, g->edge_ends, z);
     ANI_LAUNCHED(h);
     return ANIGPU_OK;
 }
@@ -870,7 +907,7 @@ int gnn_precond_f32(anigpu_ctx* h, const float* r, float* z, const float* qold, 
     Gnn* g = gnn(h);
     cudaStream_t s = h->stream;
     const unsigned bc = nblk(g->nc * CW, 256);
-    restrict_scale_kernel<<<bc, 256, 0, s>>>(g->nc, r, g->vrow, g->vedge, g->isd_c, g->coef, g->u, g->t0, stop);
+    restrict_scale_kernel<<<bc, 256, 0, s>>>(g->nc, g->map, r, g->vrow, g->vedge, g->isd_c, g->coef, g->u, g->t0, stop);
     ANI_LAUNCHED(h);
     float* cur = g->t0;
     float* nxt = g->t1;
@@ -887,7 +924,7 @@ int gnn_precond_f32(anigpu_ctx* h, const float* r, float* z, const float* qold, 
     }
     combine4_kernel<<<bc, 256, 0, s>>>(g->nc, g->crow, g->ccol, g->cval, g->pw, g->coef, g->isd_c, g->cc, stop);
     ANI_LAUNCHED(h);
-    prolong_dot_kernel<<<nb, 256, 0, s>>>(g->nf, h->nv, r, g->diag_f, g->cc, g->edge_ends, qold, z, part_rz, part_zq,
+    prolong_dot_kernel<<<nb, 256, 0, s>>>(g->nf, g->map, r, g->diag_f, g->cc, g->edge_ends, qold, z, part_rz, part_zq,
                                           stop);
     ANI_LAUNCHED(h);
     return ANIGPU_OK;
@@ -968,13 +1005,16 @@ int gnn_params(anigpu_ctx* h, float* host, int64_t n, int set, int which) {
 int gnn_bind(anigpu_ctx* h, const void* vals, int precision, int kind, const double* D) {
     Gnn* g = gnn(h);
     if (!g) return set_err(h, ANIGPU_ERR_STATE, "anigpu_gnn_init not called");
-    if (h->space != ANIGPU_P2) return set_err(h, ANIGPU_ERR_UNSUPPORTED, "the learned preconditioner needs a P2 problem");
+    if (h->space != ANIGPU_P2 && h->space != ANIGPU_VEC3_P2)
+        return set_err(h, ANIGPU_ERR_UNSUPPORTED, "the learned preconditioner needs a P2 or vector P2 problem");
     if (!vals) return set_err(h, ANIGPU_ERR_ARG, "NULL values");
     if (kind != ANIGPU_TENSOR_NULL && !D) return set_err(h, ANIGPU_ERR_ARG, "NULL tensor");
     cudaStream_t s = h->stream;
     const int f32 = precision == ANIGPU_F32;
-    const bool resize = g->nc != h->nv || g->nf != h->ndof;
-    g->nc = h->nv;
+    const int64_t nc = h->ncomp * h->nv;
+    const bool resize = g->nc != nc || g->nf != h->ndof || g->map.nv != h->nv || g->map.nds != h->nds;
+    g->nc = nc;
+    g->map = CMap{h->nv, h->nds};
     g->nf = h->ndof;
     if (resize) {
         RC(dev_alloc(h, &g->crow, g->nc + 1));
@@ -982,7 +1022,7 @@ int gnn_bind(anigpu_ctx* h, const void* vals, int precision, int kind, const dou
         RC(dev_alloc(h, &g->isd_c, g->nc));
         RC(dev_alloc(h, &g->feat, NF * g->nc));
         RC(dev_alloc(h, &g->edge_ends, 2 * std::max<int64_t>(h->ne, 1)));
-        RC(dev_alloc(h, &g->vrow, g->nc + 1));
+        RC(dev_alloc(h, &g->vrow, h->nv + 1));
         RC(dev_alloc(h, &g->vedge, 2 * std::max<int64_t>(h->ne, 1)));
         RC(dev_alloc(h, &g->dpart, 2 * kMaxPart));
         RC(dev_alloc(h, &g->coef, (size_t)K * g->nc));
@@ -1010,7 +1050,7 @@ int gnn_bind(anigpu_ctx* h, const void* vals, int precision, int kind, const dou
     unsigned long long* cnt = nullptr;
     ANI_CUDA(h, cudaMallocAsync((void**)&cnt, sizeof(unsigned long long) * (g->nc + 1), s));
     ANI_CUDA(h, cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * (g->nc + 1), s));
-    coarse_count_kernel<<<nblk(g->nc, 256), 256, 0, s>>>(g->nc, h->rowptr, h->col, cnt);
+    coarse_count_kernel<<<nblk(g->nc, 256), 256, 0, s>>>(g->nc, g->map, h->rowptr, h->col, cnt);
     ANI_LAUNCHED(h);
     RC(scan_counts(h, cnt, g->nc, g->crow));
     int64_t cnnz = 0;
@@ -1022,10 +1062,10 @@ int gnn_bind(anigpu_ctx* h, const void* vals, int precision, int kind, const dou
         RC(dev_alloc(h, &g->cval, std::max<int64_t>(cnnz, 1)));
         g->cnnz = cnnz;
     }
-    coarse_fill_kernel<<<nblk(g->nc, 256), 256, 0, s>>>(g->nc, h->rowptr, h->col, vals, f32, g->diag_f, g->crow,
+    coarse_fill_kernel<<<nblk(g->nc, 256), 256, 0, s>>>(g->nc, g->map, h->rowptr, h->col, vals, f32, g->diag_f, g->crow,
                                                         g->ccol, g->cval, g->isd_c);
     ANI_LAUNCHED(h);
-    static_feat_kernel<<<nblk(g->nc, 256), 256, 0, s>>>(g->nc, g->diag_f, h->inc_ptr, h->recs, kind, D, g->feat);
+    static_feat_kernel<<<nblk(g->nc, 256), 256, 0, s>>>(g->nc, g->map, g->diag_f, h->inc_ptr, h->recs, kind, D, g->feat);
     ANI_LAUNCHED(h);
     const int nb = (int)std::min<int64_t>(kMaxPart, nblk(g->nc, 256));
     feat_partial_kernel<<<nb, 256, 0, s>>>(g->nc, g->feat, g->part);
@@ -1037,15 +1077,15 @@ int gnn_bind(anigpu_ctx* h, const void* vals, int precision, int kind, const dou
     ANI_LAUNCHED(h);
     {
         unsigned long long* vc = nullptr;
-        ANI_CUDA(h, cudaMallocAsync((void**)&vc, sizeof(unsigned long long) * 2 * (g->nc + 1), s));
-        ANI_CUDA(h, cudaMemsetAsync(vc, 0, sizeof(unsigned long long) * 2 * (g->nc + 1), s));
+        ANI_CUDA(h, cudaMallocAsync((void**)&vc, sizeof(unsigned long long) * 2 * (h->nv + 1), s));
+        ANI_CUDA(h, cudaMemsetAsync(vc, 0, sizeof(unsigned long long) * 2 * (h->nv + 1), s));
         const unsigned eb = nblk(std::max<int64_t>(h->ne, 1), 256);
         vedge_count_kernel<<<eb, 256, 0, s>>>(h->ne, g->edge_ends, vc);
         ANI_LAUNCHED(h);
-        RC(scan_counts(h, vc, g->nc, g->vrow));
-        vedge_fill_kernel<<<eb, 256, 0, s>>>(h->ne, h->nv, g->edge_ends, g->vrow, vc + g->nc + 1, g->vedge);
+        RC(scan_counts(h, vc, h->nv, g->vrow));
+        vedge_fill_kernel<<<eb, 256, 0, s>>>(h->ne, h->nv, g->edge_ends, g->vrow, vc + h->nv + 1, g->vedge);
         ANI_LAUNCHED(h);
-        vedge_sort_kernel<<<nblk(g->nc, 256), 256, 0, s>>>(g->nc, g->vrow, g->vedge);
+        vedge_sort_kernel<<<nblk(h->nv, 256), 256, 0, s>>>(h->nv, g->vrow, g->vedge);
         ANI_LAUNCHED(h);
         ANI_CUDA(h, cudaFreeAsync(vc, s));
     }
@@ -1112,7 +1152,7 @@ int gnn_loss_grad(anigpu_ctx* h, const double* r, const double* e, double* loss)
     *loss = dq / eae;
     // dL/dc = 2/eAe P^T q ; g' = Dc^-1/2 dL/dc = 2/eAe * restrict(q) (restrict includes Dc^-1/2)
     float* gp = g->cc;
-    restrict_kernel<double><<<nblk(g->nc, 256), 256, 0, s>>>(g->nc, q, g->vrow, g->vedge, g->isd_c, gp);
+    restrict_kernel<double><<<nblk(g->nc, 256), 256, 0, s>>>(g->nc, g->map, q, g->vrow, g->vedge, g->isd_c, gp);
     ANI_LAUNCHED(h);
     scale_kernel<<<nblk(g->nc, 256), 256, 0, s>>>(g->nc, (float)(2.0 / eae), gp);
     ANI_LAUNCHED(h);

@@ -20,6 +20,7 @@
 
 #include "anigpu_internal.h"
 #include "learned.h"
+#include "spmv_vec3.cuh"
 
 namespace {
 
@@ -115,6 +116,47 @@ __global__ void __launch_bounds__(kBlock) spmv_dot_kernel(int64_t n, const int64
     }
     const double tot = block_reduce_sum((double)acc, sh);
     if (threadIdx.x == 0) part[blockIdx.x] = tot;
+}
+
+// q = A p ; partial p.q -- vector (3-component) template, W lanes per scalar row
+template <typename VR, typename T, int W>
+__global__ void __launch_bounds__(kBlock) spmv3_dot_kernel(int64_t nds, int64_t nnz_s,
+                                                           const int64_t* __restrict__ rowptr_s,
+                                                           const int32_t* __restrict__ col_s,
+                                                           const VR* __restrict__ vals, const T* __restrict__ p,
+                                                           T* __restrict__ q, double* __restrict__ part,
+                                                           const PcgScalars* __restrict__ sc) {
+    __shared__ double sh[33];
+    if (sc->done) return;
+    const int64_t rows_per_block = kBlock / W;
+    const int lane = threadIdx.x & (W - 1);
+    T acc = 0;
+    for (int64_t base = blockIdx.x * rows_per_block; base < nds; base += (int64_t)gridDim.x * rows_per_block) {
+        const int64_t r = base + threadIdx.x / W;
+        T s0, s1, s2;
+        vec3_rows<W>(r, lane, nds, nnz_s, rowptr_s, col_s, vals, p, s0, s1, s2);
+        if (r < nds && lane == 0) {
+            q[r] = s0;
+            q[nds + r] = s1;
+            q[2 * nds + r] = s2;
+            acc += s0 * p[r] + s1 * p[nds + r] + s2 * p[2 * nds + r];
+        }
+    }
+    const double tot = block_reduce_sum((double)acc, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = tot;
+}
+
+// q = A p ; partial p.q with the kernel that fits the template; returns the partial count
+template <typename VR, typename T, int W>
+int launch_spmv_dot(anigpu_ctx* h, int nb_rows, int nb3, const VR* vals, const T* p, T* q, double* part,
+                    const PcgScalars* sc) {
+    if (h->ncomp == 3) {
+        spmv3_dot_kernel<VR, T, SPMV3_W><<<nb3, kBlock, 0, h->stream>>>(h->nds, h->nnz_s, h->rowptr_s, h->col_s,
+                                                                        vals, p, q, part, sc);
+        return nb3;
+    }
+    spmv_dot_kernel<VR, T, W><<<nb_rows, kBlock, 0, h->stream>>>(h->ndof, h->rowptr, h->col, vals, p, q, part, sc);
+    return nb_rows;
 }
 
 // alpha = rz / pq, once (one block); the vector kernels read it
@@ -381,6 +423,8 @@ int pcg_core(anigpu_ctx* h, SolveWs* w, const VR* vals, const double* b, X* x, T
     const int64_t n = h->ndof;
     cudaStream_t s = h->stream;
     const int nb_rows = nblocks_for(h, n * W);
+    const int nb3 = nblocks_for(h, h->nds * SPMV3_W);
+    const int nb_pq = h->ncomp == 3 ? nb3 : nb_rows;
     const int nb_vec = nblocks_for(h, n);
     double* part_pq = w->part;
     double* part_rz = w->part + kMaxBlocks;
@@ -401,8 +445,8 @@ int pcg_core(anigpu_ctx* h, SolveWs* w, const VR* vals, const double* b, X* x, T
         if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
             for (int it = 0; it < kBatch; ++it) {
                 const int par = it & 1;
-                spmv_dot_kernel<VR, T, W><<<nb_rows, kBlock, 0, s>>>(n, h->rowptr, h->col, vals, p, q, part_pq, w->sc);
-                alpha_kernel<<<1, kBlock, 0, s>>>(par, part_pq, nb_rows, w->sc);
+                launch_spmv_dot<VR, T, W>(h, nb_rows, nb3, vals, p, q, part_pq, w->sc);
+                alpha_kernel<<<1, kBlock, 0, s>>>(par, part_pq, nb_pq, w->sc);
                 update_kernel<T, X><<<nb_vec, kBlock, 0, s>>>(n, x, r, z, p, q, dinv, part_rz, part_rr, w->sc);
                 beta_kernel<<<1, kBlock, 0, s>>>(par, part_rz, part_rr, nb_vec, w->sc);
                 pupdate_kernel<T><<<nb_vec, kBlock, 0, s>>>(n, p, z, w->sc);
@@ -423,8 +467,8 @@ int pcg_core(anigpu_ctx* h, SolveWs* w, const VR* vals, const double* b, X* x, T
         } else {
             for (int it = 0; it < kBatch; ++it) {
                 const int par = it & 1;
-                spmv_dot_kernel<VR, T, W><<<nb_rows, kBlock, 0, s>>>(n, h->rowptr, h->col, vals, p, q, part_pq, w->sc);
-                alpha_kernel<<<1, kBlock, 0, s>>>(par, part_pq, nb_rows, w->sc);
+                launch_spmv_dot<VR, T, W>(h, nb_rows, nb3, vals, p, q, part_pq, w->sc);
+                alpha_kernel<<<1, kBlock, 0, s>>>(par, part_pq, nb_pq, w->sc);
                 update_kernel<T, X><<<nb_vec, kBlock, 0, s>>>(n, x, r, z, p, q, dinv, part_rz, part_rr, w->sc);
                 beta_kernel<<<1, kBlock, 0, s>>>(par, part_rz, part_rr, nb_vec, w->sc);
                 pupdate_kernel<T><<<nb_vec, kBlock, 0, s>>>(n, p, z, w->sc);

@@ -33,14 +33,17 @@ def _sp(r, c, v, shape):
 
 
 class GnnOracle:
-    """Built from the P2 system (CSR of the matrix the GPU used), the oriented tets, the
-    element DOF table and the per-tet symmetric tensors (d00 d01 d02 d11 d12 d22)."""
+    """Built from the P2 (or vector P2) system (CSR of the matrix the GPU used), the oriented
+    tets, the scalar element DOF table and the per-tet tensors: symmetric (d00 d01 d02 d11 d12
+    d22) or, with lame=True, (lambda, mu).  With ncomp components the fine DOF c*nds + s is
+    scalar DOF s of component c and the coarse node c*nv + v is vertex v of component c."""
 
-    def __init__(self, rowptr, col, vals, tets, edofs, D6, nv, layers=4):
+    def __init__(self, rowptr, col, vals, tets, edofs, D, nv, layers=4, ncomp=1, lame=False):
         self.L = layers
-        self.nv = nv
         n = rowptr.size - 1
-        self.n = n
+        nds = n // ncomp
+        nc = ncomp * nv
+        self.n, self.nv, self.nc = n, nv, nc
         rows = np.repeat(np.arange(n), np.diff(rowptr))
         vals = np.asarray(vals, dtype=np.float64)
         self.A = _sp(rows, col, vals, (n, n))
@@ -48,34 +51,48 @@ class GnnOracle:
         m = rows == col
         diag[rows[m]] = vals[m]
         self.diag_f = torch.tensor(diag)
-        self.isd = torch.tensor(1.0 / np.sqrt(diag[:nv]))
-        # coarse graph: vertex-vertex off-diagonal entries, A_hat = -a / sqrt(d_v d_w)
-        sel = (rows < nv) & (col < nv) & (rows != col)
-        r, c, a = rows[sel], col[sel], vals[sel]
-        self.Ahat = _sp(r, c, -a / np.sqrt(diag[r] * diag[c]), (nv, nv))
-        # prolongation: vertex DOF -> its vertex; edge DOF -> mean of its two vertices
+        # fine DOF -> coarse node (-1 for edge DOFs) and back
+        fine = np.arange(n)
+        comp, s = fine // nds, fine % nds
+        coarse_of = np.where(s < nv, comp * nv + s, -1)
+        cid = np.arange(nc)
+        fine_of = (cid // nv) * nds + cid % nv
+        dc = diag[fine_of]
+        self.isd = torch.tensor(1.0 / np.sqrt(dc))
+        # coarse graph: off-diagonal entries between vertex DOFs, A_hat = -a / sqrt(d_v d_w)
+        cr, cc = coarse_of[rows], coarse_of[col]
+        sel = (cr >= 0) & (cc >= 0) & (rows != col)
+        r, c, a = cr[sel], cc[sel], vals[sel]
+        self.Ahat = _sp(r, c, -a / np.sqrt(dc[r] * dc[c]), (nc, nc))
+        # prolongation per component: vertex DOF -> its vertex; edge DOF -> mean of its two vertices
         I = [0, 0, 0, 1, 1, 2]
         J = [1, 2, 3, 2, 3, 3]
         ends = {}
         for t in range(tets.shape[0]):
             for e in range(6):
                 ends[int(edofs[t, 4 + e])] = (int(tets[t, I[e]]), int(tets[t, J[e]]))
-        pr, pc, pv = list(range(nv)), list(range(nv)), [1.0] * nv
-        for d, (a0, b0) in ends.items():
-            pr += [d, d]
-            pc += [a0, b0]
-            pv += [0.5, 0.5]
-        self.P = _sp(pr, pc, pv, (n, nv))
+        pr, pc, pv = [], [], []
+        for k in range(ncomp):
+            pr += list(k * nds + np.arange(nv))
+            pc += list(k * nv + np.arange(nv))
+            pv += [1.0] * nv
+            for d, (a0, b0) in ends.items():
+                pr += [k * nds + d, k * nds + d]
+                pc += [k * nv + a0, k * nv + b0]
+                pv += [0.5, 0.5]
+        self.P = _sp(pr, pc, pv, (n, nc))
         self.PT = self.P.t().coalesce()
-        # static features: log A_vv and the mean of log(trace D / 3) over the incident tets
-        f1 = np.log(diag[:nv])
-        tr = (D6[:, 0] + D6[:, 3] + D6[:, 5]) / 3.0
+        # static features: log A_vv and the mean over the incident tets of log(trace D / 3)
+        # (Lame: of lambda + 2 mu), the second shared by the components of a vertex
+        f1 = np.log(dc)
+        D = np.asarray(D, dtype=np.float64)
+        tr = D[:, 0] + 2.0 * D[:, 1] if lame else (D[:, 0] + D[:, 3] + D[:, 5]) / 3.0
         acc = np.zeros(nv)
         cnt = np.zeros(nv)
         for k in range(4):
             np.add.at(acc, tets[:, k], np.log(tr))
             np.add.at(cnt, tets[:, k], 1.0)
-        f2 = acc / np.maximum(cnt, 1)
+        f2 = np.tile(acc / np.maximum(cnt, 1), ncomp)
         self.fs = torch.tensor(np.stack([f1 - f1.mean(), f2 - f2.mean()], axis=1))
 
     def params(self, w):
@@ -88,7 +105,7 @@ class GnnOracle:
         for l in range(1, self.L + 1):
             g = torch.sparse.mm(self.Ahat, h)
             h = h + torch.relu(g @ P[f"W{l}"] + P[f"b{l}"])
-        return h @ P["wout"] + P["bout"]          # (nv, K)
+        return h @ P["wout"] + P["bout"]          # (nc, K)
 
     def _mv(self, x):
         return torch.sparse.mm(self.Ahat, x[:, None])[:, 0]

@@ -239,3 +239,40 @@ def test_vector_p2_lame_matches_oracle(lib, restated, n, clamped):
     rown = np.sqrt(np.bincount(rows, ref["vals"] ** 2))
     err = np.sqrt(np.bincount(rows, (v32.double().cpu().numpy() - ref["vals"]) ** 2)) / np.maximum(rown, 1e-300)
     assert err.max() <= 5e-5
+
+
+def test_vector_p2_solves_match_oracle(lib, restated):
+    """Vector P2 elasticity solves (block SpMV of the 3-component template): FP64 Jacobi-PCG
+    against the oracle's Jacobi-PCG on the same system (iterations within 2, solution), and
+    IR-CG32 to an FP64 true residual of 1e-8 on its FP32 matrix."""
+    import anigpu
+    from anigpu import meshgen
+    xyz, tets = meshgen.kuhn_cube(5, perturb=0.2, seed=5)
+    nt = tets.shape[0]
+    E = np.exp(0.5 * meshgen.normal(81, nt))
+    nu = 0.2 + 0.25 * meshgen.uniform(82, nt)
+    lam, mu = E * nu / ((1 + nu) * (1 - 2 * nu)), E / (2 * (1 + nu))
+    lib.mesh_upload(xyz, tets)
+    ndof, _ = lib.problem_setup(anigpu.VEC3_P2)
+    coords = lib.dof_coords().cpu().numpy()
+    mask = (np.abs(coords[:, 0]) < 1e-12).astype(np.uint8)
+    lib.set_dirichlet(mask)
+    LM = np.stack([lam, mu], axis=1)
+    vals, _, _ = lib.assemble(anigpu.TENSOR_LAME, LM, None, 0.0, 4, anigpu.F64)
+    rp, col = lib.csr_template()
+    rp, col, v = rp.cpu().numpy(), col.cpu().numpy(), vals.cpu().numpy()
+    b = meshgen.normal(83, ndof) * (1 - mask)
+    x, st = lib.solve(vals, b, anigpu.SOLVE_JACOBI_PCG, anigpu.F64, rtol=1e-10, maxit=100000)
+    xh = x.cpu().numpy()
+    assert st.rel_residual <= 1e-10
+    assert restated.true_residual(rp, col, v, xh, b) <= 1e-10
+    xo, it_o, _ = restated.jacobi_pcg(rp, col, v, b, 1e-10, 100000)
+    assert abs(st.iterations - it_o) <= max(2, 0.02 * it_o)  # summation order differs from the CSR walk
+    assert np.abs(xh - xo).max() <= 1e-7 * np.abs(xo).max()
+    # the product itself against the oracle SpMV
+    y = lib.spmv(vals, xh, anigpu.F64).cpu().numpy()
+    assert np.abs(y - restated.spmv(rp, col, v, xh)).max() <= 1e-12 * np.abs(y).max()
+    v32, _, _ = lib.assemble(anigpu.TENSOR_LAME, LM, None, 0.0, 4, anigpu.F32)
+    x32, st32 = lib.solve(v32, b, anigpu.SOLVE_IR_CG32, anigpu.F32, rtol=1e-8, maxit=200000)
+    assert st32.rel_residual <= 1e-8
+    assert restated.true_residual(rp, col, v32.double().cpu().numpy(), x32.cpu().numpy(), b) <= 1e-8

@@ -169,3 +169,59 @@ def test_training_lowers_loss_and_iterations(lib, restated):
     assert s1.rel_residual <= 1e-8 and s1.fallback_steps == 0
     assert s1.iterations <= s0.iterations
     assert s1.iterations < sj.iterations
+
+
+def _elastic_system(lib, n, seed):
+    """Vector P2 elasticity: per-tet Lame parameters, clamped face x = 0, FP32 assembly."""
+    import anigpu
+    from anigpu import meshgen
+    xyz, tets = meshgen.kuhn_cube(n, perturb=0.2, seed=7)
+    nt = tets.shape[0]
+    E = np.exp(0.5 * meshgen.normal(seed, nt))
+    nu = 0.2 + 0.25 * meshgen.uniform(seed + 1, nt)
+    LM = np.stack([E * nu / ((1 + nu) * (1 - 2 * nu)), E / (2 * (1 + nu))], axis=1)
+    lib.mesh_upload(xyz, tets)
+    lib.problem_setup(anigpu.VEC3_P2)
+    coords = lib.dof_coords().cpu().numpy()
+    mask = (np.abs(coords[:, 0]) < 1e-12).astype(np.uint8)
+    lib.set_dirichlet(mask)
+    vals, _, _ = lib.assemble(anigpu.TENSOR_LAME, LM, None, 0.0, 4, anigpu.F32)
+    return dict(xyz=xyz, tets=tets, D=LM, mask=mask, vals=vals.clone())
+
+
+def test_vector_p2_learned_matches_oracle(lib, restated):
+    """Vector P2 (3 components): coarse nodes are (component, vertex) pairs.  Network, M r in
+    FP64 and FP32, symmetry of M and the backward kernels against the FP64 autograd oracle."""
+    import anigpu
+    from oracle.gnn_oracle import GnnOracle
+    S = _elastic_system(lib, 3, 71)
+    prec = anigpu.LearnedPreconditioner(lib, layers=4, act=anigpu.F32, seed=5)
+    w = (prec.get_params() + 0.05 * np.random.default_rng(3).standard_normal(prec.get_params().size)
+         ).astype(np.float32)
+    prec.set_params(w)
+    prec.bind(S["vals"], anigpu.F32, anigpu.TENSOR_LAME, S["D"])
+    rp, col = lib.csr_template()
+    O = GnnOracle(rp.cpu().numpy(), col.cpu().numpy(), S["vals"].double().cpu().numpy(),
+                  restated.orient(S["xyz"], S["tets"]), lib.element_dofs().cpu().numpy(), S["D"],
+                  S["xyz"].shape[0], 4, ncomp=3, lame=True)
+    assert prec.coefficients().shape[0] == 3 * S["xyz"].shape[0]
+    assert _rel(prec.coefficients().cpu().numpy(), O.coefficients_np(w)) <= 1e-5
+    rng = np.random.default_rng(4)
+    r = rng.standard_normal(lib.ndof) * (1 - S["mask"])
+    z_or = O.apply(w, r).detach().numpy()
+    assert _rel(prec.apply(r).cpu().numpy(), z_or) <= 1e-5
+    assert _rel(prec.apply_f32(r).double().cpu().numpy(), z_or) <= 1e-5
+    y = rng.standard_normal(lib.ndof)
+    Mr, My = prec.apply(r).cpu().numpy(), prec.apply(y).cpu().numpy()
+    assert abs(y @ Mr - r @ My) <= 1e-5 * np.linalg.norm(Mr) * np.linalg.norm(y)
+    x, _ = lib.solve(S["vals"], r, anigpu.SOLVE_IR_CG32, anigpu.F32, rtol=1e-11, maxit=100000)
+    e = x.cpu().numpy()
+    prec.zero_grads()
+    L = prec.loss_grad(r, e)
+    L_or, g_or = O.loss_and_grad(w, r, e)
+    assert abs(L - L_or) <= 1e-5 * L_or
+    assert _rel(prec.get_grads(), g_or) <= 1e-4
+    prec.zero_grads()
+    xs, st = lib.solve(S["vals"], r, anigpu.SOLVE_FCG_LEARNED, anigpu.F32, rtol=1e-8, maxit=100000)
+    assert st.rel_residual <= 1e-8 and st.fallback_steps == 0
+    assert _rel(xs.cpu().numpy(), e) <= 1e-3
