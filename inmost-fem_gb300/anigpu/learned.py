@@ -109,7 +109,7 @@ def make_systems(lib, problem, n, count, seed0=0):
 def main(argv=None):
     """Train parameters on seeded synthetic problems and save them:
         python -m anigpu.learned --problem aniso --n 12 --systems 200 --steps 2000
-        python -m anigpu.learned --problem elastic --n 8 --systems 64 --steps 1500
+        python -m anigpu.learned --problem elastic --n 8 --systems 200 --steps 3000
     (each system gives 10 Jacobi-PCG iterates = 10 residual/correction pairs)"""
     import argparse
     import time
@@ -125,8 +125,8 @@ def main(argv=None):
     a = ap.parse_args(argv)
     elastic = a.problem == "elastic"
     n = a.n or (8 if elastic else 12)
-    count = a.systems or (64 if elastic else 200)
-    steps = a.steps or (1500 if elastic else 2000)
+    count = a.systems or 200
+    steps = a.steps or (3000 if elastic else 2000)
     out = a.out or (ELASTIC_WEIGHTS if elastic else DEFAULT_WEIGHTS)
     lib = anigpu.Anigpu(0)
     t0 = time.time()
