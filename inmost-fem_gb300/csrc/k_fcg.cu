@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(kB) spmv_dot_kernel(int64_t n, const int64_t* 
 }
 
 // q = A p ; partials of p.q -- vector (3-component) template, SPMV3_W lanes per scalar row
-__global__ void __launch_bounds__(kB) spmv3_dot_kernel(int64_t nds, int64_t nnz_s, const int64_t* __restrict__ rowptr_s,
+__global__ void __launch_bounds__(kB, SPMV3_MINB_F32) spmv3_dot_kernel(int64_t nds, int64_t nnz_s, const int64_t* __restrict__ rowptr_s,
                                                        const int32_t* __restrict__ col_s,
                                                        const float* __restrict__ vals, const float* __restrict__ p,
                                                        float* __restrict__ q, double* __restrict__ part,

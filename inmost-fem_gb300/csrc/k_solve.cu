@@ -120,7 +120,7 @@ __global__ void __launch_bounds__(kBlock) spmv_dot_kernel(int64_t n, const int64
 
 // q = A p ; partial p.q -- vector (3-component) template, W lanes per scalar row
 template <typename VR, typename T, int W>
-__global__ void __launch_bounds__(kBlock) spmv3_dot_kernel(int64_t nds, int64_t nnz_s,
+__global__ void __launch_bounds__(kBlock, SPMV3_MINB) spmv3_dot_kernel(int64_t nds, int64_t nnz_s,
                                                            const int64_t* __restrict__ rowptr_s,
                                                            const int32_t* __restrict__ col_s,
                                                            const VR* __restrict__ vals, const T* __restrict__ p,

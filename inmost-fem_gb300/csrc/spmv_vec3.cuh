@@ -9,6 +9,21 @@
 #pragma once
 #include <cstdint>
 
+// lanes per scalar row of the vector kernels, unroll of their column loop, resident blocks
+#ifndef SPMV3_W
+#define SPMV3_W 4
+#endif
+#ifndef SPMV3_UNROLL
+#define SPMV3_UNROLL 2
+#endif
+#ifndef SPMV3_MINB
+#define SPMV3_MINB 1
+#endif
+#ifndef SPMV3_MINB_F32
+#define SPMV3_MINB_F32 4  // FP32-only kernels: 64 registers, four 256-thread blocks per SM
+#endif
+constexpr int kSpmv3Unroll = SPMV3_UNROLL;
+
 template <int W, typename VR, typename T>
 __device__ __forceinline__ void vec3_rows(int64_t r, int lane, int64_t nds, int64_t nnz_s,
                                           const int64_t* __restrict__ rowptr_s, const int32_t* __restrict__ col_s,
@@ -22,6 +37,7 @@ __device__ __forceinline__ void vec3_rows(int64_t r, int lane, int64_t nds, int6
         const VR* v0 = vals + 3 * b;
         const VR* v1 = v0 + cs;
         const VR* v2 = v1 + cs;
+#pragma unroll kSpmv3Unroll
         for (int k = lane; k < len; k += W) {
             const int64_t t = col_s[b + k];
             const T x0 = x[t], x1 = x[nds + t], x2 = x[2 * nds + t];
@@ -47,8 +63,3 @@ __device__ __forceinline__ void vec3_rows(int64_t r, int lane, int64_t nds, int6
     s1 = a1;
     s2 = a2;
 }
-
-// lanes per scalar row of the vector kernels
-#ifndef SPMV3_W
-#define SPMV3_W 4
-#endif
