@@ -109,6 +109,24 @@ int anigpu_fem3dtet(anigpu_handle h, int opA, int opB, int tensor_kind, int orde
 int anigpu_quadrature(int order, double* p_host, double* w_host, int cap);
 /* physical quadrature points XYG[nt][q][3] (internalFem3DtetGeomInit_XYG, core.inl:249-269) */
 int anigpu_quadrature_points(anigpu_handle h, int order, int64_t nt, const double* XY, double* XYG);
+
+/* ---- evaluation of Op(u) at points of each tet (FP64).
+ * anigpu_fem3d_apply is Ani::fem3DapplyL (anifem++/fem/operations/eval.h:13-18,93-111, eval.inl:93-111)
+ *   over the whole batch: XYL[npts][4] barycentric points shared by every tet (the reference's
+ *   fused XYL), dofs[nt][nf] the element DOF values (the columns of its dofs matrix),
+ *   opU[nt][npts][dim] (per tet the vectorised Op(u) at each point, its opU_r column).
+ * anigpu_fem3d_apply_x is Ani::fem3DapplyX (eval.h:27-32,112-125, eval.inl:103-151): X[nt][npts][3]
+ *   physical points per tet, turned into barycentric coordinates as getBaryCoord does
+ *   (core.inl:120-137; points outside the tet extrapolate the tet's polynomial).
+ * anigpu_eval_solution: the same for the set-up problem and a global DOF vector x[ndof] (device),
+ *   op = ANIGPU_IDEN or ANIGPU_GRAD on the problem's space, points barycentric in the oriented
+ *   local vertex order (the order of anigpu_element_dofs); opU[nt][npts][dim].
+ * Errors: unknown operator code (ANIGPU_ERR_UNSUPPORTED), npts < 1 or NULL arrays (ANIGPU_ERR_ARG). */
+int anigpu_fem3d_apply(anigpu_handle h, int op, int64_t nt, const double* XY, int npts, const double* XYL,
+                       const double* dofs, double* opU);
+int anigpu_fem3d_apply_x(anigpu_handle h, int op, int64_t nt, const double* XY, int npts, const double* X,
+                         const double* dofs, double* opU);
+int anigpu_eval_solution(anigpu_handle h, int op, const double* x, int npts, const double* XYL, double* opU);
 /* element-level Dirichlet on a batch of element matrices (Ani::applyDir,
  * anifem++/fem/operations/dc_on_dof.h:39-45): for every tet t and local DOF k with bit k of
  * mask[t] set, applies applyDir(A_t, F_t, k, bc[t*n + k]) in ascending k.  A: F64, n x n. */

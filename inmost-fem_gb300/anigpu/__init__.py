@@ -49,6 +49,9 @@ SIGNATURES = {
     "anigpu_fem3dtet": (_i, [_vp, _i, _i, _i, _i, _i, _i64, _vp, _vp, _vp]),
     "anigpu_quadrature": (_i, [_i, _vp, _vp, _i]),
     "anigpu_quadrature_points": (_i, [_vp, _i, _i64, _vp, _vp]),
+    "anigpu_fem3d_apply": (_i, [_vp, _i, _i64, _vp, _i, _vp, _vp, _vp]),
+    "anigpu_fem3d_apply_x": (_i, [_vp, _i, _i64, _vp, _i, _vp, _vp, _vp]),
+    "anigpu_eval_solution": (_i, [_vp, _i, _vp, _i, _vp, _vp]),
     "anigpu_apply_dir": (_i, [_vp, _i64, _i, _vp, _vp, _vp, _vp]),
     "anigpu_mesh_upload": (_i, [_vp, _i64, _vp, _i64, _vp]),
     "anigpu_mesh_update_coords": (_i, [_vp, _vp]),
@@ -254,6 +257,46 @@ class Anigpu:
         q = quadrature(order)[1].size
         out = torch.empty((nt, q, 3), dtype=torch.float64, device=XY.device)
         self._check(self.lib.anigpu_quadrature_points(self.h, order, nt, _ptr(XY), _ptr(out)))
+        return out
+
+    @_streamed
+    def fem3d_apply(self, op, XY, XYL, dofs):
+        """Op(u) at barycentric points XYL[npts, 4] shared by every tet (Ani::fem3DapplyL):
+        opU[nt, npts, dim] from the element DOF values dofs[nt, nf]."""
+        torch = self.torch
+        XY = self._dev(XY, torch.float64)
+        nt = XY.numel() // 12
+        _, dim = op_info(op)
+        P = self._dev(XYL, torch.float64).reshape(-1, 4)
+        d = self._dev(dofs, torch.float64)
+        out = torch.empty((nt, P.shape[0], dim), dtype=torch.float64, device=XY.device)
+        self._check(self.lib.anigpu_fem3d_apply(self.h, op, nt, _ptr(XY), P.shape[0], _ptr(P), _ptr(d), _ptr(out)))
+        return out
+
+    @_streamed
+    def fem3d_apply_x(self, op, XY, X, dofs):
+        """Op(u) at physical points X[nt, npts, 3] of each tet (Ani::fem3DapplyX)."""
+        torch = self.torch
+        XY = self._dev(XY, torch.float64)
+        nt = XY.numel() // 12
+        _, dim = op_info(op)
+        Xd = self._dev(X, torch.float64).reshape(nt, -1, 3)
+        d = self._dev(dofs, torch.float64)
+        out = torch.empty((nt, Xd.shape[1], dim), dtype=torch.float64, device=XY.device)
+        self._check(self.lib.anigpu_fem3d_apply_x(self.h, op, nt, _ptr(XY), Xd.shape[1], _ptr(Xd), _ptr(d),
+                                                  _ptr(out)))
+        return out
+
+    @_streamed
+    def eval_solution(self, op, x, XYL):
+        """IDEN or GRAD of the global solution x of the set-up problem at barycentric points
+        XYL[npts, 4] of every tet (oriented local order): opU[nt, npts, dim]."""
+        torch = self.torch
+        _, dim = op_info(10 * self.space + op)
+        P = self._dev(XYL, torch.float64).reshape(-1, 4)
+        xd = self._dev(x, torch.float64)
+        out = torch.empty((self.nt, P.shape[0], dim), dtype=torch.float64, device=f"cuda:{self.device}")
+        self._check(self.lib.anigpu_eval_solution(self.h, op, _ptr(xd), P.shape[0], _ptr(P), _ptr(out)))
         return out
 
     @_streamed

@@ -173,6 +173,8 @@ inline unsigned grid_for(int64_t n, int block) {
 int launch_fem3dtet(anigpu_ctx* h, int opA, int opB, int kind, int order, int precision, int64_t nt,
                     const double* XY, const double* D, void* A);
 int launch_quad_points(anigpu_ctx* h, int order, int64_t nt, const double* XY, double* XYG);
+int launch_fem3d_apply(anigpu_ctx* h, int op, int64_t nt, const double* XY, int npts, const double* pts, int phys,
+                       const double* dofs, const double* x, double* out);
 int launch_apply_dir(anigpu_ctx* h, int64_t nt, int n, double* A, double* F, const uint32_t* mask, const double* bc);
 // setup (k_setup.cu)
 int setup_orient(anigpu_ctx* h);

@@ -139,6 +139,30 @@ int anigpu_quadrature_points(anigpu_handle h, int order, int64_t nt, const doubl
     return launch_quad_points(h, order, nt, XY, XYG);
 }
 
+int anigpu_fem3d_apply(anigpu_handle h, int op, int64_t nt, const double* XY, int npts, const double* XYL,
+                       const double* dofs, double* opU) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    if (!XY) return set_err(h, ANIGPU_ERR_ARG, "NULL coordinates");
+    return launch_fem3d_apply(h, op, nt, XY, npts, XYL, 0, dofs, nullptr, opU);
+}
+
+int anigpu_fem3d_apply_x(anigpu_handle h, int op, int64_t nt, const double* XY, int npts, const double* X,
+                         const double* dofs, double* opU) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    if (!XY) return set_err(h, ANIGPU_ERR_ARG, "NULL coordinates");
+    return launch_fem3d_apply(h, op, nt, XY, npts, X, 1, dofs, nullptr, opU);
+}
+
+int anigpu_eval_solution(anigpu_handle h, int op, const double* x, int npts, const double* XYL, double* opU) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    if (h->space < 0) return set_err(h, ANIGPU_ERR_STATE, "anigpu_problem_setup not called");
+    if (op != ANIGPU_IDEN && op != ANIGPU_GRAD) return set_err(h, ANIGPU_ERR_ARG, "op must be ANIGPU_IDEN or ANIGPU_GRAD");
+    return launch_fem3d_apply(h, ANIGPU_OP(h->space, op), h->nt, nullptr, npts, XYL, 0, nullptr, x, opU);
+}
+
 int anigpu_apply_dir(anigpu_handle h, int64_t nt, int n, double* A, double* F, const uint32_t* mask,
                      const double* bc) {
     CHECK_H(h);

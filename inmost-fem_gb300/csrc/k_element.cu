@@ -12,6 +12,7 @@
 #include <cstring>
 
 #include "anigpu_internal.h"
+#include "basis_eval.h"
 #include "quad_tables.h"
 
 namespace {
@@ -193,6 +194,82 @@ __global__ void apply_dir_kernel(int64_t nt, int n, double* __restrict__ A, doub
     }
 }
 
+// ---------------------------------------------------------------- evaluation of Op(u)
+// Ani::fem3DapplyL / fem3DapplyX (anifem++/fem/operations/eval.inl:93-151 -> core.inl:370-404):
+// Op(u) at points of each tet, opU[t][n][k].  One thread per (tet, point): geometry (PSI) of
+// the tet, the point's barycentric coordinates (given, or from a physical point through PSI
+// as getBaryCoord does, core.inl:120-137), the scalar basis there, and per component the sum
+// over the local DOFs in ascending order.
+struct ApplyParams {
+    int nf, dim, nfs, ncomp, op, base;
+    int npts, phys;           // phys: pts are per-tet physical points [nt][npts][3]
+    const double* pts;        // barycentric [npts][4] when !phys
+    const double* XY;         // [nt][12], or null: the handle's mesh (xyz + oriented tets)
+    const double* xyz;
+    const int32_t* tets;
+    const double* dofs;       // [nt][nf], or null: the global vector x through the DOF table
+    const double* x;
+    const int32_t* edofs;     // [nt][nloc] scalar element DOFs
+    int nloc;
+    int64_t nds;              // scalar DOFs (component c of scalar DOF s is c*nds + s)
+    double* out;
+};
+
+__global__ void __launch_bounds__(128) fem3d_apply_kernel(ApplyParams p, int64_t nt) {
+    const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (idx >= nt * p.npts) return;
+    const int64_t t = idx / p.npts;
+    const int n = (int)(idx - t * p.npts);
+    double X[12];
+    if (p.XY) {
+#pragma unroll
+        for (int k = 0; k < 12; ++k) X[k] = p.XY[12 * t + k];
+    } else {
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const int64_t node = p.tets[4 * t + v];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) X[3 * v + i] = p.xyz[3 * node + i];
+        }
+    }
+    double PSI[9], mes;
+    tet_geometry(X, PSI, &mes);
+    double l[4];
+    if (p.phys) {
+        const double* x = p.pts + 3 * idx;
+        const double dr[3] = {x[0] - X[0], x[1] - X[1], x[2] - X[2]};
+        l[1] = l[2] = l[3] = 0.0;
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+#pragma unroll
+            for (int i = 0; i < 3; ++i) l[i + 1] += PSI[i + 3 * j] * dr[j];
+        l[0] = 1.0 - l[1] - l[2] - l[3];
+    } else {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) l[k] = p.pts[4 * n + k];
+    }
+    double v[20], g[20][3];
+    ani_eval_space(p.base, l, v, g);
+    double* o = p.out + idx * p.dim;
+    for (int c = 0; c < p.ncomp; ++c) {
+        double s[3] = {0.0, 0.0, 0.0};
+        for (int i = 0; i < p.nfs; ++i) {
+            const double d = p.dofs ? p.dofs[(int64_t)p.nf * t + c * p.nfs + i]
+                                    : p.x[c * p.nds + p.edofs[(int64_t)p.nloc * t + i]];
+            if (p.op == ANIGPU_IDEN) {
+                s[0] += v[i] * d;
+            } else {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) s[k] += (PSI[0 + 3 * k] * g[i][0] + PSI[1 + 3 * k] * g[i][1] + PSI[2 + 3 * k] * g[i][2]) * d;
+            }
+        }
+        if (p.op == ANIGPU_IDEN) o[c] = s[0];
+        else
+#pragma unroll
+            for (int k = 0; k < 3; ++k) o[3 * c + k] = s[k];
+    }
+}
+
 }  // namespace
 
 int get_basis_dev(anigpu_ctx* h, int space, int order, const double** dev, ScalarBasisTable* host) {
@@ -283,6 +360,45 @@ int launch_apply_dir(anigpu_ctx* h, int64_t nt, int n, double* A, double* F, con
     if (n <= 0 || n > 32 || nt < 0 || !A || !F || !mask) return set_err(h, ANIGPU_ERR_ARG, "apply_dir arguments");
     if (nt == 0) return ANIGPU_OK;
     apply_dir_kernel<<<grid_for(nt, 128), 128, 0, h->stream>>>(nt, n, A, F, mask, bc);
+    ANI_LAUNCHED(h);
+    return ANIGPU_OK;
+}
+
+// Op(u) at points: per-tet coordinates and DOFs (XY, dofs non-null) or the handle's mesh and a
+// global vector x (XY = dofs = null).
+int launch_fem3d_apply(anigpu_ctx* h, int op, int64_t nt, const double* XY, int npts, const double* pts, int phys,
+                       const double* dofs, const double* x, double* out) {
+    int nf, dim, base, nc, o;
+    if (!op_info(op, &nf, &dim, &base, &nc, &o)) return set_err(h, ANIGPU_ERR_UNSUPPORTED, "unknown operator code");
+    if (nt < 0 || npts < 1) return set_err(h, ANIGPU_ERR_ARG, "nt < 0 or no points");
+    if (!pts || !out) return set_err(h, ANIGPU_ERR_ARG, "NULL points or output");
+    if (nt == 0) return ANIGPU_OK;
+    ApplyParams p{};
+    p.nf = nf;
+    p.dim = dim;
+    p.nfs = nf / nc;
+    p.ncomp = nc;
+    p.op = o;
+    p.base = base;
+    p.npts = npts;
+    p.phys = phys;
+    p.pts = pts;
+    p.out = out;
+    if (XY) {
+        if (!dofs) return set_err(h, ANIGPU_ERR_ARG, "NULL element DOF values");
+        p.XY = XY;
+        p.dofs = dofs;
+    } else {
+        if (!h->tets || !h->edofs) return set_err(h, ANIGPU_ERR_STATE, "anigpu_problem_setup not called");
+        if (!x) return set_err(h, ANIGPU_ERR_ARG, "NULL solution vector");
+        p.xyz = h->xyz;
+        p.tets = h->tets;
+        p.x = x;
+        p.edofs = h->edofs;
+        p.nloc = h->nloc_s;
+        p.nds = h->nds;
+    }
+    fem3d_apply_kernel<<<grid_for(nt * npts, 128), 128, 0, h->stream>>>(p, nt);
     ANI_LAUNCHED(h);
     return ANIGPU_OK;
 }

@@ -297,6 +297,46 @@ int orc_fem3dtet(int codeA, int codeB, int kind, int order, long nt, const doubl
     return 0;
 }
 
+/* ---------------------------------------------------------------- evaluation */
+
+/* Op(u) at points of each tet (fem3DapplyL, eval.inl:93-111 -> core.inl:370-404; fem3DapplyX,
+ * eval.inl:127-151 with getBaryCoord, core.inl:120-137).  phys = 0: pts are npts barycentric
+ * points [npts][4] shared by every tet; phys = 1: pts are per-tet physical points [nt][npts][3],
+ * turned into barycentric coordinates with the tet's PSI.  dofs[nt][nf]; opU[nt][npts][dim]
+ * (opU[t][k + dim*n], the reference's vec(opU at point n) blocks).  Sums over the local DOFs
+ * in ascending order (fusive_A_mul_B, core.inl:382). */
+int orc_fem3d_apply(int code, long nt, const double* XY, int npts, const double* pts, int phys,
+                    const double* dofs, double* opU) {
+    int nf, dim;
+    if (orc_op_info(code, &nf, &dim) != 0 || npts < 1) return -1;
+    double U[MAXDIM * MAXNF];
+    for (long t = 0; t < nt; ++t) {
+        const double* X = XY + 12 * t;
+        double PSI[9], mes;
+        tet_geom(X, PSI, &mes);
+        for (int n = 0; n < npts; ++n) {
+            double l[4];
+            if (phys) {
+                const double* x = pts + 3 * ((size_t)npts * t + n);
+                double dr[3] = {x[0] - X[0], x[1] - X[1], x[2] - X[2]};
+                l[1] = l[2] = l[3] = 0;
+                for (int j = 0; j < 3; ++j)
+                    for (int i = 0; i < 3; ++i) l[i + 1] += PSI[i + 3 * j] * dr[j];
+                l[0] = 1 - l[1] - l[2] - l[3];
+            } else {
+                for (int k = 0; k < 4; ++k) l[k] = pts[4 * n + k];
+            }
+            apply_op(code, l, PSI, U);
+            for (int k = 0; k < dim; ++k) {
+                double s = 0;
+                for (int i = 0; i < nf; ++i) s += U[k + dim * i] * dofs[(size_t)nf * t + i];
+                opU[((size_t)npts * t + n) * dim + k] = s;
+            }
+        }
+    }
+    return 0;
+}
+
 /* Ani::applyDir (dc_on_dof.h:39-45) */
 void orc_apply_dir(int n, double* A, double* F, int k, double bc) {
     for (int i = 0; i < n; ++i) F[i] -= A[i + n * k] * bc;

@@ -24,6 +24,10 @@ int orc_quad_rule(int order, double* p /*4*np*/, double* w /*np*/, int cap);
 int orc_quad_points(int order, long nt, const double* XY, double* XYG);
 /* element matrices A[nt][nfA][nfB] (col-major nfB x nfA per tet), int_tet.inl:93-122 */
 int orc_fem3dtet(int codeA, int codeB, int kind, int order, long nt, const double* XY, const double* D, double* A);
+/* Op(u) at points of each tet: fem3DapplyL (phys 0: shared barycentric points [npts][4]) or
+ * fem3DapplyX (phys 1: per-tet physical points [nt][npts][3]); opU[nt][npts][dim] */
+int orc_fem3d_apply(int code, long nt, const double* XY, int npts, const double* pts, int phys,
+                    const double* dofs, double* opU);
 /* Ani::applyDir (dc_on_dof.h:39-45) on one col-major n x n element matrix */
 void orc_apply_dir(int n, double* A, double* F, int k, double bc);
 

@@ -25,6 +25,19 @@ def _p(a):
     return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
 
 
+def _apply(fn, nf_dim, code, XY, pts, dofs, phys):
+    nf, dim = nf_dim
+    XY = np.ascontiguousarray(XY, dtype=np.float64)
+    nt = XY.size // 12
+    pts = np.ascontiguousarray(pts, dtype=np.float64)
+    npts = pts.shape[-2] if phys else pts.shape[0]
+    dofs = np.ascontiguousarray(dofs, dtype=np.float64).reshape(nt, nf)
+    out = np.zeros((nt, npts, dim))
+    rc = fn(code, nt, _p(XY), npts, _p(pts), 1 if phys else 0, _p(dofs), _p(out))
+    assert rc == 0, rc
+    return out
+
+
 def build_restated():
     if not os.path.exists(RESTATE_PATH):
         subprocess.run(["make", "-C", HERE, "restate"], check=True, capture_output=True)
@@ -39,6 +52,7 @@ class Restated:
         L.orc_quad_points.argtypes = [_i, _l, _vp, _vp]
         L.orc_fem3dtet.argtypes = [_i, _i, _i, _i, _l, _vp, _vp, _vp]
         L.orc_apply_dir.argtypes = [_i, _vp, _vp, _i, _d]
+        L.orc_fem3d_apply.argtypes = [_i, _l, _vp, _i, _vp, _i, _vp, _vp]
         L.orc_orient.argtypes = [_vp, _l, _vp]
         L.orc_edges.argtypes = [_l, _l, _vp, _vp]
         L.orc_edges.restype = _l
@@ -93,6 +107,11 @@ class Restated:
     def apply_dir(self, A, F, k, bc):
         n = F.shape[0]
         self.L.orc_apply_dir(n, _p(A), _p(F), k, bc)
+
+    def fem3d_apply(self, code, XY, pts, dofs, phys=False):
+        """Op(u) at points of each tet, opU[nt, npts, dim]: fem3DapplyL (pts [npts, 4] barycentric,
+        shared) or fem3DapplyX (phys: pts [nt, npts, 3] physical)."""
+        return _apply(self.L.orc_fem3d_apply, self.op_info(code), code, XY, pts, dofs, phys)
 
     def orient(self, xyz, tets):
         t = np.ascontiguousarray(tets, dtype=np.int32).copy()
@@ -215,6 +234,7 @@ class Reference:
         L.ref_applyDir.argtypes = [_vp, _vp, _i, _i, _d]
         L.ref_time_p2_sym.argtypes = [_l, _vp, _vp, _i, _i, _vp]
         L.ref_time_p2_sym.restype = _d
+        L.ref_fem3d_apply.argtypes = [_i, _l, _vp, _i, _vp, _i, _vp, _vp]
         self.L = L
 
     def fem3dtet(self, codeA, codeB, kind, order, XY, D=None, fn=0, nfA=None, nfB=None):
@@ -225,6 +245,9 @@ class Reference:
         rc = self.L.ref_fem3dtet(codeA, codeB, kind, order, nt, _p(XY), _p(Dd), fn, _p(A))
         assert rc == 0, rc
         return A
+
+    def fem3d_apply(self, code, XY, pts, dofs, nf, dim, phys=False):
+        return _apply(self.L.ref_fem3d_apply, (nf, dim), code, XY, pts, dofs, phys)
 
     def quadrature(self, order):
         p = np.zeros(4 * 128)

@@ -7,7 +7,8 @@
 // memoryless stack overload; and :30-57 for the PlainMemory overload used above
 // order 6) for the operator pairs the parity tests need, and exposes
 // Ani::tetrahedron_quadrature_formulas (anifem++/fem/quadrature_formulas.cpp:526)
-// and Ani::applyDir (anifem++/fem/operations/dc_on_dof.h:39-45).
+// Ani::applyDir (anifem++/fem/operations/dc_on_dof.h:39-45) and Ani::fem3DapplyL/X
+// (anifem++/fem/operations/eval.h, eval.inl:93-151).
 #include "anifem++/fem/operations/operations.h"
 #include "anifem++/fem/operators.h"
 #include "anifem++/fem/spaces/spaces.h"
@@ -140,6 +141,31 @@ int run(const Req& r) {
 #define V1 FemVec<3, FEM_P1>
 #define V2 FemVec<3, FEM_P2>
 
+// Ani::fem3DapplyL (eval.inl:93-111) for phys == 0: npts shared barycentric points [npts][4];
+// Ani::fem3DapplyX (eval.inl:103-125) for phys == 1: per-tet physical points [nt][npts][3].
+// dofs[nt][nf]; opU[nt][npts*dim].  One tet per call (fusion 1), at most 24 points.
+template <typename Op>
+int apply_tets(long nt, const double* XY, int npts, const double* pts, int phys, const double* dofs, double* opU) {
+    constexpr int nf = Op::Nfa::value, dim = Op::Dim::value;
+    if (npts < 1 || npts > 24) return -3;
+    std::vector<double> l(pts, pts + (phys ? 0 : 4 * npts));
+    for (long t = 0; t < nt; ++t) {
+        const double* X = XY + 12 * t;
+        std::vector<double> d(dofs + (size_t)nf * t, dofs + (size_t)nf * (t + 1));
+        double* out = opU + (size_t)npts * dim * t;
+        if (phys) {
+            ArrayView<const double> Xv(pts + (size_t)3 * npts * t, 3 * npts);
+            fem3DapplyX<Op>(X, X + 3, X + 6, X + 9, Xv, ArrayView<double>(d.data(), nf),
+                            ArrayView<double>(out, (size_t)npts * dim));
+        } else {
+            DenseMatrix<const double> XY0(X, 3, 1), XY1(X + 3, 3, 1), XY2(X + 6, 3, 1), XY3(X + 9, 3, 1);
+            DenseMatrix<> dm(d.data(), nf, 1), om(out, (size_t)npts * dim, 1);
+            fem3DapplyL<Op>(XY0, XY1, XY2, XY3, ArrayView<double>(l.data(), 4 * npts), dm, om);
+        }
+    }
+    return 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -169,6 +195,32 @@ int ref_fem3dtet(int codeA, int codeB, int kind, int order, long nt, const doubl
         PAIR(12, 22, G1, G2)
         PAIR(22, 12, G2, G1)
 #undef PAIR
+    } catch (const std::exception&) {
+        return -2;
+    }
+    return -1;
+}
+
+int ref_fem3d_apply(int code, long nt, const double* XY, int npts, const double* pts, int phys,
+                    const double* dofs, double* opU) {
+    try {
+#define OP(c, OPT) if (code == (c)) return apply_tets<OPT>(nt, XY, npts, pts, phys, dofs, opU);
+        using I0 = Operator<IDEN, P0>; using I1 = Operator<IDEN, P1>; using G1 = Operator<GRAD, P1>;
+        using I2 = Operator<IDEN, P2>; using G2 = Operator<GRAD, P2>; using I3 = Operator<IDEN, P3>;
+        using G3 = Operator<GRAD, P3>; using IV1 = Operator<IDEN, V1>; using GV1 = Operator<GRAD, V1>;
+        using IV2 = Operator<IDEN, V2>; using GV2 = Operator<GRAD, V2>;
+        OP(1, I0)
+        OP(11, I1)
+        OP(12, G1)
+        OP(21, I2)
+        OP(22, G2)
+        OP(31, I3)
+        OP(32, G3)
+        OP(41, IV1)
+        OP(42, GV1)
+        OP(51, IV2)
+        OP(52, GV2)
+#undef OP
     } catch (const std::exception&) {
         return -2;
     }

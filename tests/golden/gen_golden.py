@@ -11,7 +11,9 @@ Writes tests/golden/golden.npz with
   * quad_<order>     the reference's tetrahedron rules (quadrature_formulas.cpp:526);
   * case_<name>_*    inputs and outputs of the reference's fem3Dtet (compiled from its
                      sources by oracle/Makefile) on seeded random tets, for every operator
-                     pair and tensor kind the GPU path provides.
+                     pair and tensor kind the GPU path provides;
+  * apply_<code>_*   the reference's fem3DapplyL (order-4 quadrature points) and fem3DapplyX
+                     (seeded physical points) on the same tets for every operator code.
 """
 import os
 import re
@@ -121,6 +123,19 @@ def main():
                 out[f"case_{name}_A"] = A
                 cases.append(name)
     out["case_names"] = np.array(cases)
+    # fem3DapplyL at the order-4 quadrature points and fem3DapplyX at seeded physical points (some
+    # outside the tet), for every operator code, on the same tets
+    p4, _ = R.quadrature(4)
+    out["apply_XYL"] = p4
+    out["apply_X"] = meshgen.uniform(41, nt * 7 * 3).reshape(nt, 7, 3) * 3.0 - 1.0
+    apply_codes = [1, 11, 12, 21, 22, 31, 32, 41, 42, 51, 52]
+    for code in apply_codes:
+        nf, dim = op_nf_dim(code)
+        dofs = meshgen.normal(50 + code, nt * nf).reshape(nt, nf)
+        out[f"apply_{code}_dofs"] = dofs
+        out[f"apply_{code}_L"] = R.fem3d_apply(code, XY, p4, dofs, nf, dim)
+        out[f"apply_{code}_X"] = R.fem3d_apply(code, XY, out["apply_X"], dofs, nf, dim, phys=True)
+    out["apply_codes"] = np.array(apply_codes)
     path = os.path.join(HERE, "golden.npz")
     np.savez_compressed(path, **out)
     print(path, len(cases), "cases", os.path.getsize(path), "bytes")

@@ -111,3 +111,58 @@ def test_errors_are_reported(lib):
     with pytest.raises(anigpu.AnigpuError) as e:
         lib.fem3dtet(22, 21, XY, None, anigpu.TENSOR_NULL, 2)  # identity of incompatible dims (3 vs 1)
     assert e.value.code == anigpu.ERR_ARG
+
+
+def test_fem3d_apply_matches_reference(lib, golden):
+    """anigpu_fem3d_apply / _apply_x (FP64) against the reference's fem3DapplyL / fem3DapplyX
+    outputs for every operator code: within 1e-12 of the largest value per tet."""
+    XY = golden["tets_XY"]
+    for code in golden["apply_codes"]:
+        code = int(code)
+        dofs = golden[f"apply_{code}_dofs"]
+        got_l = lib.fem3d_apply(code, XY, golden["apply_XYL"], dofs).cpu().numpy()
+        got_x = lib.fem3d_apply_x(code, XY, golden["apply_X"], dofs).cpu().numpy()
+        for got, ref in ((got_l, golden[f"apply_{code}_L"]), (got_x, golden[f"apply_{code}_X"])):
+            assert got.shape == ref.shape
+            scale = np.maximum(np.abs(ref).reshape(ref.shape[0], -1).max(axis=1), 1e-300)
+            err = np.abs(got - ref).reshape(ref.shape[0], -1).max(axis=1) / scale
+            assert err.max() <= 1e-12, (code, err.max())
+
+
+@pytest.mark.parametrize("space", [1, 2, 5])
+def test_eval_solution_matches_oracle_and_reproduces_quadratics(lib, restated, space):
+    """anigpu_eval_solution on a set-up problem: IDEN and GRAD of a global vector at the order-4
+    quadrature points equal the restated fem3DapplyL on the gathered element DOFs; the P2
+    interpolant of a quadratic field reproduces the field and its gradient exactly."""
+    import anigpu
+    from anigpu import meshgen
+    xyz, tets = meshgen.kuhn_cube(4, perturb=0.2, seed=3)
+    lib.mesh_upload(xyz, tets)
+    ndof, _ = lib.problem_setup(space)
+    ncomp = 3 if space == 5 else 1
+    ot = restated.orient(xyz, tets)
+    XY = xyz[ot].reshape(-1, 12)
+    ed = lib.element_dofs().cpu().numpy()
+    nds = ndof // ncomp
+    p4, _ = restated.quadrature(4)
+    x = meshgen.normal(77 + space, ndof)
+    gd = np.concatenate([x[c * nds + ed] for c in range(ncomp)], axis=1)  # [nt, ncomp*nloc]
+    base = {1: 1, 2: 2, 5: 2}[space]
+    code_space = space if space != 5 else 5
+    for op in (anigpu.IDEN, anigpu.GRAD):
+        got = lib.eval_solution(op, x, p4).cpu().numpy()
+        ref = restated.fem3d_apply(10 * code_space + op, XY, p4, gd)
+        assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max(), op
+    if base == 2:
+        c = lib.dof_coords().cpu().numpy()
+        f = lambda P: P[..., 0] ** 2 + P[..., 1] * P[..., 2] - 0.5 * P[..., 2]  # noqa: E731
+        u = f(c)
+        val = lib.eval_solution(anigpu.IDEN, u, p4).cpu().numpy()
+        grad = lib.eval_solution(anigpu.GRAD, u, p4).cpu().numpy()
+        XG = restated.quad_points(4, XY)
+        gx = np.stack([2 * XG[..., 0], XG[..., 2], XG[..., 1] - 0.5], axis=-1)
+        k = ncomp  # every component holds the same field when ncomp = 3
+        assert np.abs(val[..., 0] - f(XG)).max() <= 1e-12
+        assert np.abs(grad[..., :3] - gx).max() <= 1e-11
+        if k == 3:
+            assert np.abs(val[..., 2] - f(XG)).max() <= 1e-12

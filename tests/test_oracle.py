@@ -169,3 +169,18 @@ def test_oracle_pcg_solves_poisson(restated):
     assert it > 0 and rel <= 1e-10
     assert restated.true_residual(prob["rowptr"], prob["col"], prob["vals"], x, prob["rhs"]) <= 1e-9
     assert np.all(x[mask == 1] == 0)
+
+
+def test_oracle_apply_matches_reference(restated, golden):
+    """fem3DapplyL (shared barycentric points) and fem3DapplyX (physical points, some outside the
+    tet) of the restatement against the reference's own (eval.inl:93-151), every operator code."""
+    XY = golden["tets_XY"]
+    for code in golden["apply_codes"]:
+        code = int(code)
+        dofs = golden[f"apply_{code}_dofs"]
+        for key, pts, phys in (("L", golden["apply_XYL"], False), ("X", golden["apply_X"], True)):
+            ref = golden[f"apply_{code}_{key}"]
+            got = restated.fem3d_apply(code, XY, pts, dofs, phys=phys)
+            assert got.shape == ref.shape
+            scale = max(np.abs(ref).max(), 1e-300)
+            assert np.abs(got - ref).max() <= 1e-13 * scale, (code, key)
