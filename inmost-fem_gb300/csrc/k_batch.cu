@@ -6,7 +6,9 @@
 //
 //   * the instance map: the instance of every DOF (from the tet ranges of the instances) and row
 //     tiles of at most kTileRows consecutive DOFs of one instance, so that every reduction of the
-//     solver is a per-tile partial followed by a fixed-order per-instance sum (deterministic);
+//     solver is a per-tile partial followed by a fixed-order per-instance sum (deterministic).
+//     One warp works on one tile (a fixed shuffle tree for its partials, no block barrier), eight
+//     tiles in flight per 256-thread block;
 //   * Jacobi-PCG with per-instance scalars and convergence: five kernels per iteration (q = A p
 //     with per-tile p.q; per-instance alpha; x, r, z update with per-tile r.z, r.r; per-instance
 //     beta and convergence; p update).  Tiles of converged instances return at once, so the cost
@@ -64,6 +66,15 @@ __device__ inline double bsum(double v, double* sh) {
     return s;  // thread 0
 }
 
+// one warp per tile: every reduction of a tile is a fixed shuffle tree, no block barrier
+constexpr int kWarps = 8;  // warps (tiles in flight) per 256-thread block
+
+__device__ inline double wsum(double v) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
 // ---------------------------------------------------------------- instance map
 __global__ void dof_inst_kernel(int64_t nt, int nloc, const int32_t* __restrict__ edofs,
                                 const int64_t* __restrict__ toff, int ninst, int32_t* __restrict__ inst,
@@ -114,29 +125,30 @@ __global__ void bdiag_kernel(int64_t n, const int64_t* __restrict__ rowptr, cons
     dinv[r] = d != 0 ? 1.0 / d : 1.0;
 }
 
-// x = 0, r = b, z = dinv r, p = z; partials r.z and b.b per tile
-__global__ void binit_kernel(int ntiles, const int64_t* __restrict__ tstart, const double* __restrict__ b,
-                             const double* __restrict__ dinv, double* __restrict__ x, double* __restrict__ r,
-                             double* __restrict__ z, double* __restrict__ p, double* __restrict__ part_rz,
-                             double* __restrict__ part_rr) {
-    __shared__ double sh[32];
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        const int64_t i = tstart[t] + threadIdx.x;
+// x = 0, r = b, z = dinv r, p = z; partials r.z and b.b per tile (one warp per tile)
+__global__ void __launch_bounds__(256) binit_kernel(int ntiles, const int64_t* __restrict__ tstart,
+                                                    const double* __restrict__ b, const double* __restrict__ dinv,
+                                                    double* __restrict__ x, double* __restrict__ r,
+                                                    double* __restrict__ z, double* __restrict__ p,
+                                                    double* __restrict__ part_rz, double* __restrict__ part_rr) {
+    const int lane = threadIdx.x & 31;
+    for (int t = blockIdx.x * kWarps + (threadIdx.x >> 5); t < ntiles; t += gridDim.x * kWarps) {
+        const int64_t t0 = tstart[t], t1 = tstart[t + 1];
         double arz = 0, arr = 0;
-        if (threadIdx.x < kTileRows && i < tstart[t + 1]) {
+        for (int64_t i = t0 + lane; i < t1; i += 32) {
             const double ri = b[i], zi = dinv[i] * ri;
             x[i] = 0;
             r[i] = ri;
             z[i] = zi;
             p[i] = zi;
-            arz = ri * zi;
-            arr = ri * ri;
+            arz += ri * zi;
+            arr += ri * ri;
         }
-        const double s1 = bsum(arz, sh);
-        const double s2 = bsum(arr, sh);
-        if (threadIdx.x == 0) {
-            part_rz[t] = s1;
-            part_rr[t] = s2;
+        arz = wsum(arz);
+        arr = wsum(arr);
+        if (lane == 0) {
+            part_rz[t] = arz;
+            part_rr[t] = arr;
         }
     }
 }
@@ -167,32 +179,38 @@ __global__ void binst_init_kernel(int ninst, const int32_t* __restrict__ itp, co
     }
 }
 
+// q = A p per tile, partial p.q (one warp per tile: 32/W rows per pass, W lanes per row)
 template <int W>
-__global__ void bspmv_dot_kernel(int ntiles, const int64_t* __restrict__ tstart, const int32_t* __restrict__ tinst,
-                                 const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
-                                 const double* __restrict__ vals, const double* __restrict__ p, double* __restrict__ q,
-                                 const InstScalars* __restrict__ sc, double* __restrict__ part) {
-    __shared__ double sh[32];
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        if (sc[tinst[t]].done) {  // block-uniform
-            if (threadIdx.x == 0) part[t] = 0;
+__global__ void __launch_bounds__(256) bspmv_dot_kernel(int ntiles, const int64_t* __restrict__ tstart,
+                                                        const int32_t* __restrict__ tinst,
+                                                        const int64_t* __restrict__ rowptr,
+                                                        const int32_t* __restrict__ col,
+                                                        const double* __restrict__ vals, const double* __restrict__ p,
+                                                        double* __restrict__ q, const InstScalars* __restrict__ sc,
+                                                        double* __restrict__ part) {
+    const int lane32 = threadIdx.x & 31, sub = lane32 / W, lane = lane32 & (W - 1);
+    for (int t = blockIdx.x * kWarps + (threadIdx.x >> 5); t < ntiles; t += gridDim.x * kWarps) {
+        if (sc[tinst[t]].done) {  // warp-uniform
+            if (lane32 == 0) part[t] = 0;
             continue;
         }
-        const int64_t row = tstart[t] + threadIdx.x / W;
-        const int lane = threadIdx.x & (W - 1);
-        const bool ok = row < tstart[t + 1];
-        double s = 0;
-        if (ok)
-            for (int64_t k = rowptr[row] + lane; k < rowptr[row + 1]; k += W) s += vals[k] * p[col[k]];
-#pragma unroll
-        for (int o = W / 2; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, W);
+        const int64_t t0 = tstart[t], t1 = tstart[t + 1];
         double acc = 0;
-        if (ok && lane == 0) {
-            q[row] = s;
-            acc = s * p[row];
+        for (int64_t base = t0; base < t1; base += 32 / W) {
+            const int64_t row = base + sub;
+            const bool ok = row < t1;
+            double s = 0;
+            if (ok)
+                for (int64_t k = rowptr[row] + lane; k < rowptr[row + 1]; k += W) s += vals[k] * p[col[k]];
+#pragma unroll
+            for (int o = W / 2; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, W);
+            if (ok && lane == 0) {
+                q[row] = s;
+                acc += s * p[row];
+            }
         }
-        const double tot = bsum(acc, sh);
-        if (threadIdx.x == 0) part[t] = tot;
+        acc = wsum(acc);
+        if (lane32 == 0) part[t] = acc;
     }
 }
 
@@ -208,35 +226,37 @@ __global__ void balpha_kernel(int ninst, const int32_t* __restrict__ itp, const 
     }
 }
 
-__global__ void bupdate_kernel(int ntiles, const int64_t* __restrict__ tstart, const int32_t* __restrict__ tinst,
-                               double* __restrict__ x, double* __restrict__ r, double* __restrict__ z,
-                               const double* __restrict__ p, const double* __restrict__ q,
-                               const double* __restrict__ dinv, const InstScalars* __restrict__ sc,
-                               double* __restrict__ part_rz, double* __restrict__ part_rr) {
-    __shared__ double sh[32];
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+__global__ void __launch_bounds__(256) bupdate_kernel(int ntiles, const int64_t* __restrict__ tstart,
+                                                      const int32_t* __restrict__ tinst, double* __restrict__ x,
+                                                      double* __restrict__ r, double* __restrict__ z,
+                                                      const double* __restrict__ p, const double* __restrict__ q,
+                                                      const double* __restrict__ dinv,
+                                                      const InstScalars* __restrict__ sc,
+                                                      double* __restrict__ part_rz, double* __restrict__ part_rr) {
+    const int lane = threadIdx.x & 31;
+    for (int t = blockIdx.x * kWarps + (threadIdx.x >> 5); t < ntiles; t += gridDim.x * kWarps) {
         const InstScalars& s = sc[tinst[t]];
-        if (s.done) {
-            if (threadIdx.x == 0) part_rz[t] = part_rr[t] = 0;
+        if (s.done) {  // warp-uniform
+            if (lane == 0) part_rz[t] = part_rr[t] = 0;
             continue;
         }
         const double a = s.alpha;
-        const int64_t i = tstart[t] + threadIdx.x;
+        const int64_t t0 = tstart[t], t1 = tstart[t + 1];
         double arz = 0, arr = 0;
-        if (threadIdx.x < kTileRows && i < tstart[t + 1]) {
+        for (int64_t i = t0 + lane; i < t1; i += 32) {
             x[i] += a * p[i];
             const double ri = r[i] - a * q[i];
             const double zi = dinv[i] * ri;
             r[i] = ri;
             z[i] = zi;
-            arz = ri * zi;
-            arr = ri * ri;
+            arz += ri * zi;
+            arr += ri * ri;
         }
-        const double s1 = bsum(arz, sh);
-        const double s2 = bsum(arr, sh);
-        if (threadIdx.x == 0) {
-            part_rz[t] = s1;
-            part_rr[t] = s2;
+        arz = wsum(arz);
+        arr = wsum(arr);
+        if (lane == 0) {
+            part_rz[t] = arz;
+            part_rr[t] = arr;
         }
     }
 }
@@ -261,14 +281,16 @@ __global__ void bbeta_kernel(int ninst, const int32_t* __restrict__ itp, const i
     }
 }
 
-__global__ void bpupdate_kernel(int ntiles, const int64_t* __restrict__ tstart, const int32_t* __restrict__ tinst,
-                                double* __restrict__ p, const double* __restrict__ z,
-                                const InstScalars* __restrict__ sc) {
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+__global__ void __launch_bounds__(256) bpupdate_kernel(int ntiles, const int64_t* __restrict__ tstart,
+                                                       const int32_t* __restrict__ tinst, double* __restrict__ p,
+                                                       const double* __restrict__ z,
+                                                       const InstScalars* __restrict__ sc) {
+    const int lane = threadIdx.x & 31;
+    for (int t = blockIdx.x * kWarps + (threadIdx.x >> 5); t < ntiles; t += gridDim.x * kWarps) {
         const InstScalars& s = sc[tinst[t]];
         if (s.done) continue;
-        const int64_t i = tstart[t] + threadIdx.x;
-        if (threadIdx.x < kTileRows && i < tstart[t + 1]) p[i] = z[i] + s.beta * p[i];
+        const double beta = s.beta;
+        for (int64_t i = tstart[t] + lane; i < tstart[t + 1]; i += 32) p[i] = z[i] + beta * p[i];
     }
 }
 
@@ -294,26 +316,30 @@ __global__ void bcheck_kernel(int ninst, const InstScalars* __restrict__ sc, Bat
 
 // true residual b - A x per tile (FP64), partial ||r||^2
 template <int W>
-__global__ void bresid_kernel(int ntiles, const int64_t* __restrict__ tstart, const int64_t* __restrict__ rowptr,
-                              const int32_t* __restrict__ col, const double* __restrict__ vals,
-                              const double* __restrict__ x, const double* __restrict__ b, double* __restrict__ part) {
-    __shared__ double sh[32];
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        const int64_t row = tstart[t] + threadIdx.x / W;
-        const int lane = threadIdx.x & (W - 1);
-        const bool ok = row < tstart[t + 1];
-        double s = 0;
-        if (ok)
-            for (int64_t k = rowptr[row] + lane; k < rowptr[row + 1]; k += W) s += vals[k] * x[col[k]];
-#pragma unroll
-        for (int o = W / 2; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, W);
+__global__ void __launch_bounds__(256) bresid_kernel(int ntiles, const int64_t* __restrict__ tstart,
+                                                     const int64_t* __restrict__ rowptr,
+                                                     const int32_t* __restrict__ col, const double* __restrict__ vals,
+                                                     const double* __restrict__ x, const double* __restrict__ b,
+                                                     double* __restrict__ part) {
+    const int lane32 = threadIdx.x & 31, sub = lane32 / W, lane = lane32 & (W - 1);
+    for (int t = blockIdx.x * kWarps + (threadIdx.x >> 5); t < ntiles; t += gridDim.x * kWarps) {
+        const int64_t t0 = tstart[t], t1 = tstart[t + 1];
         double acc = 0;
-        if (ok && lane == 0) {
-            const double ri = b[row] - s;
-            acc = ri * ri;
+        for (int64_t base = t0; base < t1; base += 32 / W) {
+            const int64_t row = base + sub;
+            const bool ok = row < t1;
+            double s = 0;
+            if (ok)
+                for (int64_t k = rowptr[row] + lane; k < rowptr[row + 1]; k += W) s += vals[k] * x[col[k]];
+#pragma unroll
+            for (int o = W / 2; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, W);
+            if (ok && lane == 0) {
+                const double ri = b[row] - s;
+                acc += ri * ri;
+            }
         }
-        const double tot = bsum(acc, sh);
-        if (threadIdx.x == 0) part[t] = tot;
+        acc = wsum(acc);
+        if (lane32 == 0) part[t] = acc;
     }
 }
 
@@ -346,11 +372,12 @@ struct BatchWs {
     int conditional = 0;             // the last job ran as one graph with a device-side loop
 };
 
-int grid_tiles(int ntiles) { return std::max(1, std::min(ntiles, 152 * 16)); }
+// blocks of 256 threads (8 tiles in flight each), at most 8 blocks per SM on 152 SMs
+int grid_tiles(int ntiles) { return std::max(1, std::min((ntiles + kWarps - 1) / kWarps, 152 * 8)); }
 
 template <int W>
 void launch_spmv_dot(anigpu_ctx* h, BatchWs* w, const double* vals, cudaStream_t s) {
-    bspmv_dot_kernel<W><<<grid_tiles(w->ntiles), kTileRows * W, 0, s>>>(w->ntiles, w->tstart, w->tinst, h->rowptr,
+    bspmv_dot_kernel<W><<<grid_tiles(w->ntiles), 256, 0, s>>>(w->ntiles, w->tstart, w->tinst, h->rowptr,
                                                                        h->col, vals, w->p, w->q, w->sc, w->part);
 }
 void spmv_dot(anigpu_ctx* h, BatchWs* w, const double* vals, cudaStream_t s) {
@@ -367,11 +394,11 @@ int one_iteration(anigpu_ctx* h, BatchWs* w, const double* vals, int64_t maxit, 
     const int gt = grid_tiles(w->ntiles);
     spmv_dot(h, w, vals, s);
     balpha_kernel<<<w->ninst, 128, 0, s>>>(w->ninst, w->itp, w->it, w->part, w->sc);
-    bupdate_kernel<<<gt, kTileRows, 0, s>>>(w->ntiles, w->tstart, w->tinst, w->x, w->r, w->z, w->p, w->q, w->dinv,
+    bupdate_kernel<<<gt, 256, 0, s>>>(w->ntiles, w->tstart, w->tinst, w->x, w->r, w->z, w->p, w->q, w->dinv,
                                             w->sc, w->part + w->ntiles, w->part + 2 * w->ntiles);
     bbeta_kernel<<<w->ninst, 128, 0, s>>>(w->ninst, w->itp, w->it, w->part + w->ntiles, w->part + 2 * w->ntiles,
                                           (long long)maxit, w->sc);
-    bpupdate_kernel<<<gt, kTileRows, 0, s>>>(w->ntiles, w->tstart, w->tinst, w->p, w->z, w->sc);
+    bpupdate_kernel<<<gt, 256, 0, s>>>(w->ntiles, w->tstart, w->tinst, w->p, w->z, w->sc);
     h->launches += 4;
     ANI_CUDA(h, cudaGetLastError());
     return ANIGPU_OK;
@@ -552,7 +579,7 @@ int batch_run(anigpu_ctx* h, int kind, const double* D, const double* f, double 
     auto prologue = [&]() -> int {
         if (assemble) RC_(run_assemble(h, kind, D, f, f_const, order, ANIGPU_F64, vals, rhs_assembled, nullptr, 1e-100));
         bdiag_kernel<<<grid_for(w->n, 256), 256, 0, s>>>(w->n, h->rowptr, h->col, vals, w->dinv);
-        binit_kernel<<<gt, kTileRows, 0, s>>>(w->ntiles, w->tstart, b, w->dinv, x, w->r, w->z, w->p, w->part,
+        binit_kernel<<<gt, 256, 0, s>>>(w->ntiles, w->tstart, b, w->dinv, x, w->r, w->z, w->p, w->part,
                                               w->part + w->ntiles);
         binst_init_kernel<<<w->ninst, 128, 0, s>>>(w->ninst, w->itp, w->it, w->part, w->part + w->ntiles, rtol, w->sc);
         h->launches += 3;
@@ -632,10 +659,10 @@ int batch_run(anigpu_ctx* h, int kind, const double* D, const double* f, double 
     cudaEventRecord(e1, s);
     // statistics: FP64 true residual per instance
     switch (w->W) {
-        case 2: bresid_kernel<2><<<gt, kTileRows * 2, 0, s>>>(w->ntiles, w->tstart, h->rowptr, h->col, vals, x, b, w->part); break;
-        case 8: bresid_kernel<8><<<gt, kTileRows * 8, 0, s>>>(w->ntiles, w->tstart, h->rowptr, h->col, vals, x, b, w->part); break;
-        case 16: bresid_kernel<16><<<gt, kTileRows * 16, 0, s>>>(w->ntiles, w->tstart, h->rowptr, h->col, vals, x, b, w->part); break;
-        default: bresid_kernel<4><<<gt, kTileRows * 4, 0, s>>>(w->ntiles, w->tstart, h->rowptr, h->col, vals, x, b, w->part);
+        case 2: bresid_kernel<2><<<gt, 256, 0, s>>>(w->ntiles, w->tstart, h->rowptr, h->col, vals, x, b, w->part); break;
+        case 8: bresid_kernel<8><<<gt, 256, 0, s>>>(w->ntiles, w->tstart, h->rowptr, h->col, vals, x, b, w->part); break;
+        case 16: bresid_kernel<16><<<gt, 256, 0, s>>>(w->ntiles, w->tstart, h->rowptr, h->col, vals, x, b, w->part); break;
+        default: bresid_kernel<4><<<gt, 256, 0, s>>>(w->ntiles, w->tstart, h->rowptr, h->col, vals, x, b, w->part);
     }
     binst_sum_kernel<<<w->ninst, 128, 0, s>>>(w->ninst, w->itp, w->it, w->part, w->isum);
     ANI_LAUNCHED(h);
