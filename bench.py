@@ -136,8 +136,8 @@ def run_batched(args, local):
 def run_elasticity(args, local, peak):
     """Vector P2 linear elasticity on 48^3 x 6 perturbed Kuhn tets (663,552 tets): per-tet Lame
     parameters from E ~ lognormal(0, 0.5^2), nu ~ U[0.2, 0.45]; clamped face x = 0; unit traction
-    (1, 0, 0) on x = 1 as its consistent P2 nodal loads (area/3 on each edge DOF of a face, 0 on the
-    vertices); FP32 assembly timed back to back, then FP64 Jacobi-PCG (FP64 assembly), IR-CG32
+    (1, 0, 0) on x = 1 integrated by the library's face integral (anigpu_fem3dface); FP32 assembly
+    timed back to back, then FP64 Jacobi-PCG (FP64 assembly), IR-CG32
     (FP32 assembly) and flexible CG with the learned preconditioner (FP32 assembly, FP64 residual
     replacement) to 1e-8."""
     import torch
@@ -156,22 +156,24 @@ def run_elasticity(args, local, peak):
     ndof, nnz = lib.problem_setup(anigpu.VEC3_P2)
     coords = lib.dof_coords().cpu().numpy()
     lib.set_dirichlet((np.abs(coords[:, 0]) < 1e-12).astype(np.uint8))
-    # traction load: faces with all three vertices on x = 1 (boundary vertices are not perturbed)
+    # traction load: the face integral of t . v over the faces with all three vertices on x = 1
+    # (boundary vertices are not perturbed), fem3Dface<IDEN P0, IDEN FemVec<3,P2>> with t = (1, 0, 0)
+    # as a 3x1 tensor, order 2, scattered through the element DOF table (component-major blocks)
     ed = lib.element_dofs().cpu().numpy()
+    nds = ndof // 3
     b = np.zeros(ndof)
     on = np.abs(xyz[:, 0] - 1.0) < 1e-12
-    faces = [(0, 1, 2), (0, 1, 3), (0, 2, 3), (1, 2, 3)]
-    edge_of = {(0, 1): 4, (0, 2): 5, (0, 3): 6, (1, 2): 7, (1, 3): 8, (2, 3): 9}
-    # local vertex order of element_dofs is the oriented one; recover it from the DOF ids (vertex DOFs = ids)
-    tl = ed[:, :4]
-    for f in faces:
-        sel = on[tl[:, f[0]]] & on[tl[:, f[1]]] & on[tl[:, f[2]]]
-        if not sel.any():
+    tl = ed[:, :4]  # oriented local vertex order (vertex DOF id = vertex id)
+    for face, f in enumerate(((0, 1, 2), (1, 2, 3), (2, 3, 0), (3, 0, 1))):  # face k = {k, k+1, k+2 mod 4}
+        sel = np.nonzero(on[tl[:, f[0]]] & on[tl[:, f[1]]] & on[tl[:, f[2]]])[0]
+        if sel.size == 0:
             continue
-        p0, p1, p2 = xyz[tl[sel, f[0]]], xyz[tl[sel, f[1]]], xyz[tl[sel, f[2]]]
-        area = 0.5 * np.linalg.norm(np.cross(p1 - p0, p2 - p0), axis=1)
-        for a_, b_ in ((f[0], f[1]), (f[0], f[2]), (f[1], f[2])):
-            np.add.at(b, ed[sel, edge_of[(a_, b_)]], area / 3.0)
+        XYf = xyz[tl[sel]].reshape(-1, 12)
+        trac = np.tile([1.0, 0.0, 0.0], (sel.size, 1))
+        Fe = lib.fem3dface(10 * anigpu.P0 + anigpu.IDEN, 10 * anigpu.VEC3_P2 + anigpu.IDEN, XYf, face,
+                           trac, anigpu.TENSOR_TET_GENERAL, 2).cpu().numpy().reshape(sel.size, 30)
+        for c in range(3):
+            np.add.at(b, c * nds + ed[sel], Fe[:, 10 * c:10 * (c + 1)])
     D_dev = torch.tensor(LM, device=dev)
     vals32 = torch.empty(nnz, dtype=torch.float32, device=dev)
     rhs = torch.empty(ndof, dtype=torch.float64, device=dev)
@@ -537,6 +539,22 @@ def run_ours(args):
                                     "speedup_vs_jacobi_pcg_f64": solve["jacobi_pcg_f64"]["seconds"] / tot}
         except anigpu.AnigpuError as e:
             solve["fcg_learned"] = {"unavailable": str(e)}
+        # post-processing: gradient of the solution at the 14 order-4 quadrature points of every
+        # tet (fem3DapplyL over the mesh), FP64
+        p4 = torch.tensor(anigpu.quadrature(4)[0], device=dev)
+        for _ in range(3):
+            g = lib.eval_solution(anigpu.GRAD, x, p4)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        torch.cuda.synchronize()
+        ev[0].record(lib.stream)
+        for _ in range(10):
+            g = lib.eval_solution(anigpu.GRAD, x, p4)
+        ev[1].record(lib.stream)
+        torch.cuda.synchronize()
+        ems = ev[0].elapsed_time(ev[1]) / 10
+        solve["eval_gradient"] = {"ms": ems, "points_per_s": nt * p4.shape[0] / (ems * 1e-3),
+                                  "output_bytes": g.numel() * 8,
+                                  "output_GBps": g.numel() * 8 / (ems * 1e-3) / 1e9}
 
     batched = None
     if not args.no_batched and rank == 0:

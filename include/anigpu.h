@@ -110,6 +110,30 @@ int anigpu_quadrature(int order, double* p_host, double* w_host, int cap);
 /* physical quadrature points XYG[nt][q][3] (internalFem3DtetGeomInit_XYG, core.inl:249-269) */
 int anigpu_quadrature_points(anigpu_handle h, int order, int64_t nt, const double* XY, double* XYG);
 
+/* ---- face integrals: the fused batch of Ani::fem3Dface (anifem++/fem/operations/int_face.h:13-19,
+ * int_face.inl:12-44): A = int over face `face` of (D OpA(u)) . OpB(v), the same element engine as
+ * anigpu_fem3dtet with the triangle rule of `order` (0..9; the reference's stack-memory fem3Dface
+ * limit is 9, int_face.inl:22-23) mapped onto the face and |face| as the measure.  face k is the
+ * face of vertices {k, k+1, k+2 mod 4} of every tet of the batch (face 0 = {X0,X1,X2}, 1 =
+ * {X1,X2,X3}, 2 = {X2,X3,X0}, 3 = {X3,X0,X1}).  Tensor kinds and layouts as for anigpu_fem3dtet;
+ * POINT data follow the points of anigpu_face_quadrature_points.  Neumann loads are
+ * OpA = IDEN P0 (1 DOF) with the load as the tensor (a 3x1 GENERAL tensor for a vector traction
+ * on IDEN FemVec<3,.>), Robin terms OpA = OpB = IDEN.  The rules are the reference's triangle
+ * family (triangle_quadrature_formulas, quadrature_formulas.cpp:109), recomputed. */
+int anigpu_fem3dface(anigpu_handle h, int opA, int opB, int tensor_kind, int order, int precision, int64_t nt,
+                     const double* XY, int face, const double* D, void* A);
+/* Ani::fem3DfaceN (int_face.h:28-34, int_face.inl:48-78): int over the face of ((D OpA(u)) . N) . OpB(v)
+ * with N the outward unit normal of the face (Ani::face_normal, geometry.h:77-93).  The tensor has
+ * 3*dimB rows (row l + 3k: normal component l of output row k, DotWithNormalHelper, core.h:175-190):
+ * e.g. a pressure p I as a 9x1 GENERAL tensor with OpA = IDEN P0 gives the load p n . v, and
+ * OpA = GRAD, OpB = IDEN with the NULL tensor gives the normal derivative term (grad u . n) v. */
+int anigpu_fem3dface_n(anigpu_handle h, int opA, int opB, int tensor_kind, int order, int precision, int64_t nt,
+                       const double* XY, int face, const double* D, void* A);
+/* triangle rule (host arrays): p[3*np] barycentric on the face, w[np] summing to 1; returns np or <0 */
+int anigpu_face_quadrature(int order, double* p_host, double* w_host, int cap);
+/* physical points of the face rule, XYG[nt][q][3] */
+int anigpu_face_quadrature_points(anigpu_handle h, int order, int face, int64_t nt, const double* XY, double* XYG);
+
 /* ---- evaluation of Op(u) at points of each tet (FP64).
  * anigpu_fem3d_apply is Ani::fem3DapplyL (anifem++/fem/operations/eval.h:13-18,93-111, eval.inl:93-111)
  *   over the whole batch: XYL[npts][4] barycentric points shared by every tet (the reference's

@@ -49,6 +49,10 @@ SIGNATURES = {
     "anigpu_fem3dtet": (_i, [_vp, _i, _i, _i, _i, _i, _i64, _vp, _vp, _vp]),
     "anigpu_quadrature": (_i, [_i, _vp, _vp, _i]),
     "anigpu_quadrature_points": (_i, [_vp, _i, _i64, _vp, _vp]),
+    "anigpu_fem3dface": (_i, [_vp, _i, _i, _i, _i, _i, _i64, _vp, _i, _vp, _vp]),
+    "anigpu_fem3dface_n": (_i, [_vp, _i, _i, _i, _i, _i, _i64, _vp, _i, _vp, _vp]),
+    "anigpu_face_quadrature": (_i, [_i, _vp, _vp, _i]),
+    "anigpu_face_quadrature_points": (_i, [_vp, _i, _i, _i64, _vp, _vp]),
     "anigpu_fem3d_apply": (_i, [_vp, _i, _i64, _vp, _i, _vp, _vp, _vp]),
     "anigpu_fem3d_apply_x": (_i, [_vp, _i, _i64, _vp, _i, _vp, _vp, _vp]),
     "anigpu_eval_solution": (_i, [_vp, _i, _vp, _i, _vp, _vp]),
@@ -122,6 +126,18 @@ def op_info(code):
     nc = 3 if space in (VEC3_P1, VEC3_P2) else 1
     bd = 1 if op == IDEN else 3
     return nfs * nc, bd * nc
+
+
+def face_quadrature(order):
+    """(points[np,3], weights[np]) of the triangle rule of the face integrals."""
+    import numpy as np
+    lib = load_library()
+    p = np.zeros(3 * 256)
+    w = np.zeros(256)
+    n = lib.anigpu_face_quadrature(order, p.ctypes.data, w.ctypes.data, 256)
+    if n <= 0:
+        raise AnigpuError(n, "unsupported face quadrature order")
+    return p[:3 * n].reshape(n, 3).copy(), w[:n].copy()
 
 
 def quadrature(order):
@@ -257,6 +273,35 @@ class Anigpu:
         q = quadrature(order)[1].size
         out = torch.empty((nt, q, 3), dtype=torch.float64, device=XY.device)
         self._check(self.lib.anigpu_quadrature_points(self.h, order, nt, _ptr(XY), _ptr(out)))
+        return out
+
+    @_streamed
+    def fem3dface(self, opA, opB, XY, face, D=None, kind=TENSOR_NULL, order=5, precision=F64, out=None,
+                  normal=False):
+        """Face-integral element matrices (Ani::fem3Dface; Ani::fem3DfaceN with normal=True, the
+        tensor then having 3*dimB rows contracted with the outward normal) over face `face` (0..3)
+        of every tet: A[nt, nfA, nfB], the same layout as fem3dtet."""
+        torch = self.torch
+        XY = self._dev(XY, torch.float64)
+        nt = XY.numel() // 12
+        nfA, _ = op_info(opA)
+        nfB, _ = op_info(opB)
+        dt = torch.float64 if precision == F64 else torch.float32
+        if out is None:
+            out = torch.empty((nt, nfA, nfB), dtype=dt, device=XY.device)
+        Dd = self._dev(D, torch.float64) if D is not None else None
+        call = self.lib.anigpu_fem3dface_n if normal else self.lib.anigpu_fem3dface
+        self._check(call(self.h, opA, opB, kind, order, precision, nt, _ptr(XY), face, _ptr(Dd), _ptr(out)))
+        return out
+
+    @_streamed
+    def face_quadrature_points(self, order, face, XY):
+        torch = self.torch
+        XY = self._dev(XY, torch.float64)
+        nt = XY.numel() // 12
+        q = face_quadrature(order)[1].size
+        out = torch.empty((nt, q, 3), dtype=torch.float64, device=XY.device)
+        self._check(self.lib.anigpu_face_quadrature_points(self.h, order, face, nt, _ptr(XY), _ptr(out)))
         return out
 
     @_streamed

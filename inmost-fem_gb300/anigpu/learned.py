@@ -121,6 +121,7 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--lr", type=float, default=3e-3)
     ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--layers", type=int, default=4)
     ap.add_argument("--out", default=None)
     a = ap.parse_args(argv)
     elastic = a.problem == "elastic"
@@ -132,7 +133,7 @@ def main(argv=None):
     t0 = time.time()
     systems = make_systems(lib, a.problem, n, count)
     print(f"{count} systems ({lib.ndof} DOFs) in {time.time() - t0:.1f} s")
-    prec = anigpu.LearnedPreconditioner(lib, layers=4, act=anigpu.BF16, seed=a.seed)
+    prec = anigpu.LearnedPreconditioner(lib, layers=a.layers, act=anigpu.BF16, seed=a.seed)
     t0 = time.time()
     train(prec, systems, steps, lr=a.lr, lr_final=a.lr / 3, log_every=max(1, steps // 10))
     print(f"trained {steps} steps in {time.time() - t0:.1f} s; mean loss {mean_loss(prec, systems[:4]):.4f}")

@@ -21,6 +21,9 @@ struct ScalarBasisTable {
     std::vector<double> grad;       // grad[(n*nf + i)*3 + d]  d/dxi_d of phi_i
 };
 bool make_scalar_basis(int space, int order, ScalarBasisTable* t);
+// the same at the points of the triangle rule of `order` mapped onto face `face` of the tet
+// (face k = vertices k, k+1, k+2 mod 4, fem3Dface, int_face.inl:31-36); weights of that rule
+bool make_scalar_basis_face(int space, int order, int face, ScalarBasisTable* t);
 int eval_scalar_basis_at(int space, const double* l, double* val, double (*grad)[3]);
 int scalar_space_nf(int space);
 // op code helpers (code = 10*space + op)
@@ -126,7 +129,7 @@ struct anigpu_ctx {
     std::vector<std::pair<int, double*>> basis_dev;
 };
 // device table for (space, order): q*nf values then q*nf*3 gradients, then q weights
-int get_basis_dev(anigpu_ctx* h, int space, int order, const double** dev, ScalarBasisTable* host);
+int get_basis_dev(anigpu_ctx* h, int space, int order, const double** dev, ScalarBasisTable* host, int face = -1);
 
 // ------------------------------------------------------------------ helpers
 // record timing event k (k = 0 starts the call) when timing is enabled
@@ -171,8 +174,8 @@ inline unsigned grid_for(int64_t n, int block) {
 // ------------------------------------------------------------------ kernel entry points (host side)
 // element level (k_element.cu)
 int launch_fem3dtet(anigpu_ctx* h, int opA, int opB, int kind, int order, int precision, int64_t nt,
-                    const double* XY, const double* D, void* A);
-int launch_quad_points(anigpu_ctx* h, int order, int64_t nt, const double* XY, double* XYG);
+                    const double* XY, const double* D, void* A, int face = -1, int normal = 0);
+int launch_quad_points(anigpu_ctx* h, int order, int64_t nt, const double* XY, double* XYG, int face = -1);
 int launch_fem3d_apply(anigpu_ctx* h, int op, int64_t nt, const double* XY, int npts, const double* pts, int phys,
                        const double* dofs, const double* x, double* out);
 int launch_apply_dir(anigpu_ctx* h, int64_t nt, int n, double* A, double* F, const uint32_t* mask, const double* bc);

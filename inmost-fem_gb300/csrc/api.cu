@@ -7,6 +7,7 @@
 #include "anigpu_internal.h"
 #include "learned.h"
 #include "quad_tables.h"
+#include "tri_quad_tables.h"
 
 int set_err(anigpu_ctx* h, int code, const std::string& msg) {
     if (h) h->err = msg;
@@ -137,6 +138,39 @@ int anigpu_quadrature_points(anigpu_handle h, int order, int64_t nt, const doubl
     CHECK_H(h);
     cudaSetDevice(h->device);
     return launch_quad_points(h, order, nt, XY, XYG);
+}
+
+int anigpu_fem3dface(anigpu_handle h, int opA, int opB, int tensor_kind, int order, int precision, int64_t nt,
+                     const double* XY, int face, const double* D, void* A) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    if (face < 0 || face > 3) return set_err(h, ANIGPU_ERR_ARG, "face number must be 0..3");
+    return launch_fem3dtet(h, opA, opB, tensor_kind, order, precision, nt, XY, D, A, face);
+}
+
+int anigpu_fem3dface_n(anigpu_handle h, int opA, int opB, int tensor_kind, int order, int precision, int64_t nt,
+                       const double* XY, int face, const double* D, void* A) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    if (face < 0 || face > 3) return set_err(h, ANIGPU_ERR_ARG, "face number must be 0..3");
+    return launch_fem3dtet(h, opA, opB, tensor_kind, order, precision, nt, XY, D, A, face, 1);
+}
+
+int anigpu_face_quadrature(int order, double* p_host, double* w_host, int cap) {
+    const double *p, *w;
+    int np;
+    if (order < 0 || order > ANIGPU_TRI_MAX_ORDER || !anigpu_tri_rule(order, &p, &w, &np)) return ANIGPU_ERR_UNSUPPORTED;
+    if (np > cap) return ANIGPU_ERR_ARG;
+    if (p_host) std::memcpy(p_host, p, sizeof(double) * 3 * np);
+    if (w_host) std::memcpy(w_host, w, sizeof(double) * np);
+    return np;
+}
+
+int anigpu_face_quadrature_points(anigpu_handle h, int order, int face, int64_t nt, const double* XY, double* XYG) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    if (face < 0 || face > 3) return set_err(h, ANIGPU_ERR_ARG, "face number must be 0..3");
+    return launch_quad_points(h, order, nt, XY, XYG, face);
 }
 
 int anigpu_fem3d_apply(anigpu_handle h, int op, int64_t nt, const double* XY, int npts, const double* XYL,

@@ -5,6 +5,7 @@
 
 #include "anigpu_internal.h"
 #include "quad_tables.h"
+#include "tri_quad_tables.h"
 #include "basis_eval.h"
 
 namespace {
@@ -57,6 +58,38 @@ bool make_scalar_basis(int space, int order, ScalarBasisTable* t) {
     for (int n = 0; n < q; ++n) {
         double v[20], g[20][3];
         eval_space(space, p + 4 * n, v, g);
+        for (int i = 0; i < nf; ++i) {
+            t->val[(size_t)n * nf + i] = v[i];
+            for (int d = 0; d < 3; ++d) t->grad[((size_t)n * nf + i) * 3 + d] = g[i][d];
+        }
+    }
+    return true;
+}
+
+bool make_scalar_basis_face(int space, int order, int face, ScalarBasisTable* t) {
+    const double *p3, *w;
+    int q;
+    if (face < 0 || face > 3 || order < 0 || order > ANIGPU_TRI_MAX_ORDER) return false;
+    if (!anigpu_tri_rule(order, &p3, &w, &q)) return false;
+    const int nf = scalar_space_nf(space);
+    if (nf < 0) return false;
+    t->space = space;
+    t->order = order;
+    t->q = q;
+    t->nf = nf;
+    t->pts.assign((size_t)4 * q, 0.0);
+    for (int n = 0; n < q; ++n) {  // int_face.inl:31-36
+        t->pts[4 * n + face] = p3[3 * n + 0];
+        t->pts[4 * n + (face + 1) % 4] = p3[3 * n + 1];
+        t->pts[4 * n + (face + 2) % 4] = p3[3 * n + 2];
+        t->pts[4 * n + (face + 3) % 4] = 0.0;
+    }
+    t->wts.assign(w, w + q);
+    t->val.assign((size_t)q * nf, 0.0);
+    t->grad.assign((size_t)q * nf * 3, 0.0);
+    for (int n = 0; n < q; ++n) {
+        double v[20], g[20][3];
+        eval_space(space, t->pts.data() + 4 * n, v, g);
         for (int i = 0; i < nf; ++i) {
             t->val[(size_t)n * nf + i] = v[i];
             for (int d = 0; d < 3; ++d) t->grad[((size_t)n * nf + i) * 3 + d] = g[i][d];

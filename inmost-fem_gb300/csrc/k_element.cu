@@ -28,8 +28,72 @@ struct OpDesc {
 struct ElemParams {
     OpDesc A, B;
     int q, kind;
+    int face;         // -1: the tet integral; 0..3: the integral over face k (fem3Dface)
+    int normal;       // fem3DfaceN: the tensor has 3*dimB rows, contracted with the outward normal
     const double* w;  // device weights
 };
+
+// outward unit normal and area of face k (Ani::face_normal, geometry.h:77-93, on the coordinates
+// relative to X0; the fourth vertex decides the orientation)
+__device__ inline double face_normal(const double* X, int face, double* nrm) {
+    double P[4][3];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+        const int node = (face + v) & 3;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) P[v][i] = node == 0 ? 0.0 : X[3 * node + i] - X[i];
+    }
+    double a[3] = {P[1][0] - P[0][0], P[1][1] - P[0][1], P[1][2] - P[0][2]};
+    const double b[3] = {P[2][0] - P[0][0], P[2][1] - P[0][1], P[2][2] - P[0][2]};
+    nrm[0] = a[1] * b[2] - a[2] * b[1];
+    nrm[1] = -a[0] * b[2] + a[2] * b[0];
+    nrm[2] = a[0] * b[1] - a[1] * b[0];
+    const double len = sqrt(nrm[0] * nrm[0] + nrm[1] * nrm[1] + nrm[2] * nrm[2]);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) a[i] = P[3][i] - P[0][i];
+    const double vol = nrm[0] * a[0] + nrm[1] * a[1] + nrm[2] * a[2];
+    const double sc = vol > 0 ? -len : len;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) nrm[i] /= sc;
+    return len / 2;
+}
+
+// entry (k, j) of the dB x dA tensor at point n of tet t, with applyDU's meaning of the
+// identity-type kinds (diff_tensor.h:275-552): NULL/SCALAR are s*I when dA == dB, a column of s
+// when dA == 1
+__device__ inline double tensor_at(int kind, const double* D, int64_t t, int n, int q, int dA, int dB, int k, int j) {
+    switch (kind) {
+        case ANIGPU_TENSOR_NULL:
+        case ANIGPU_TENSOR_CONST_SCALAR:
+        case ANIGPU_TENSOR_TET_SCALAR: {
+            const double s = kind == ANIGPU_TENSOR_NULL ? 1.0 : (kind == ANIGPU_TENSOR_CONST_SCALAR ? D[0] : D[t]);
+            return (dA == dB) ? (k == j ? s : 0.0) : s;
+        }
+        case ANIGPU_TENSOR_TET_SYM: {
+            const double* s6 = D + 6 * t;
+            const int lo = k < j ? k : j, hi = k < j ? j : k;
+            return s6[lo == 0 ? hi : (lo == 1 ? 2 + hi : 5)];
+        }
+        case ANIGPU_TENSOR_TET_GENERAL: return D[(size_t)dA * dB * t + k + dB * j];
+        default: return D[(size_t)dA * dB * (n + (size_t)q * t) + k + dB * j];
+    }
+}
+
+// area of face k = vertices k, k+1, k+2 (mod 4), from the coordinates relative to X0 as the
+// reference's XYP (tri_area, geometry.h:67-72; int_face.inl:40-43)
+__device__ inline double face_area(const double* X, int face) {
+    double P[3][3];
+#pragma unroll
+    for (int v = 0; v < 3; ++v) {
+        const int node = (face + v) & 3;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) P[v][i] = node == 0 ? 0.0 : X[3 * node + i] - X[i];
+    }
+    const double a[3] = {P[0][0] - P[2][0], P[0][1] - P[2][1], P[0][2] - P[2][2]};
+    const double b[3] = {P[1][0] - P[2][0], P[1][1] - P[2][1], P[1][2] - P[2][2]};
+    const double c[3] = {a[1] * b[2] - a[2] * b[1], -a[0] * b[2] + a[2] * b[0], a[0] * b[1] - a[1] * b[0]};
+    return sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]) / 2;
+}
 
 __device__ inline void tet_geometry(const double* X, double* PSI, double* mes) {
     // internalFem3DtetGeomInit_Tet (core.inl:217-247) with inverse3x3 (geometry.h:26-44)
@@ -79,8 +143,8 @@ __global__ void __launch_bounds__(kThreads) fem3dtet_kernel(ElemParams p, int64_
     double* sTabA = smem;
     double* sTabB = sTabA + tabA;
     double* sW = sTabB + tabB;
-    double* sGeo = sW + q;              // PSI[9], mes
-    double* sD = sGeo + 10;             // dB*dA
+    double* sGeo = sW + q;              // PSI[9], mes, outward normal[3]
+    double* sD = sGeo + 13;             // dB*dA
     Real* sU = reinterpret_cast<Real*>(sD + ANIGPU_MAX_DIM * ANIGPU_MAX_DIM);
     Real* sV = sU + dA * nfA;
     Real* sDU = sV + dB * nfB;
@@ -91,7 +155,11 @@ __global__ void __launch_bounds__(kThreads) fem3dtet_kernel(ElemParams p, int64_
     const int nD = dA * dB;
     for (int64_t t = blockIdx.x; t < nt; t += gridDim.x) {
         __syncthreads();
-        if (threadIdx.x == 0) tet_geometry(XY + 12 * t, sGeo, sGeo + 9);
+        if (threadIdx.x == 0) {
+            tet_geometry(XY + 12 * t, sGeo, sGeo + 9);
+            if (p.normal) sGeo[9] = face_normal(XY + 12 * t, p.face, sGeo + 10);
+            else if (p.face >= 0) sGeo[9] = face_area(XY + 12 * t, p.face);
+        }
         Real acc[kMaxOwned];
 #pragma unroll
         for (int m = 0; m < kMaxOwned; ++m) acc[m] = Real(0);
@@ -103,31 +171,18 @@ __global__ void __launch_bounds__(kThreads) fem3dtet_kernel(ElemParams p, int64_
                 sU[e] = op_value<Real>(p.A, sTabA, q, n, e % dA, e / dA, sGeo);
             for (int e = threadIdx.x; e < dB * nfB; e += blockDim.x)
                 sV[e] = op_value<Real>(p.B, sTabB, q, n, e % dB, e / dB, sGeo);
-            // dense D(k,j), column-major dB x dA, with applyDU semantics for NULL/SCALAR
+            // dense D(k,j), column-major dB x dA; fem3DfaceN: rows l + 3k of the 3dB x dA tensor
+            // contracted with the normal (DotWithNormalHelper::ProcessNormal, core.h:175-190)
             for (int e = threadIdx.x; e < nD; e += blockDim.x) {
                 const int k = e % dB, j = e / dB;
-                double v;
-                switch (p.kind) {
-                    case ANIGPU_TENSOR_NULL:
-                    case ANIGPU_TENSOR_CONST_SCALAR:
-                    case ANIGPU_TENSOR_TET_SCALAR: {
-                        const double s = p.kind == ANIGPU_TENSOR_NULL
-                                             ? 1.0
-                                             : (p.kind == ANIGPU_TENSOR_CONST_SCALAR ? D[0] : D[t]);
-                        v = (dA == dB) ? (k == j ? s : 0.0) : s;  // dimA==1: column of s
-                        break;
-                    }
-                    case ANIGPU_TENSOR_TET_SYM: {
-                        const double* s6 = D + 6 * t;
-                        const int lo = k < j ? k : j, hi = k < j ? j : k;
-                        const int idx = lo == 0 ? hi : (lo == 1 ? 2 + hi : 5);
-                        v = s6[idx];
-                        break;
-                    }
-                    case ANIGPU_TENSOR_TET_GENERAL: v = D[(size_t)nD * t + e]; break;
-                    default: v = D[(size_t)nD * (n + (size_t)q * t) + e]; break;
+                if (!p.normal) {
+                    sD[e] = tensor_at(p.kind, D, t, n, q, dA, dB, k, j);
+                } else {
+                    double v = 0.0;
+#pragma unroll
+                    for (int l = 0; l < 3; ++l) v += tensor_at(p.kind, D, t, n, q, dA, 3 * dB, l + 3 * k, j) * sGeo[10 + l];
+                    sD[e] = v;
                 }
-                sD[e] = v;
             }
             __syncthreads();
             const Real wv = Real(sW[n] * mes);
@@ -272,11 +327,12 @@ __global__ void __launch_bounds__(128) fem3d_apply_kernel(ApplyParams p, int64_t
 
 }  // namespace
 
-int get_basis_dev(anigpu_ctx* h, int space, int order, const double** dev, ScalarBasisTable* host) {
+int get_basis_dev(anigpu_ctx* h, int space, int order, const double** dev, ScalarBasisTable* host, int face) {
     ScalarBasisTable tab;
-    if (!make_scalar_basis(space, order, &tab)) return set_err(h, ANIGPU_ERR_UNSUPPORTED, "unsupported space/order");
+    const bool ok = face < 0 ? make_scalar_basis(space, order, &tab) : make_scalar_basis_face(space, order, face, &tab);
+    if (!ok) return set_err(h, ANIGPU_ERR_UNSUPPORTED, "unsupported space/order");
     if (host) *host = tab;
-    const int key = 100 * space + order;
+    const int key = 100 * space + order + 10000 * (face + 1);
     for (auto& kv : h->basis_dev)
         if (kv.first == key) {
             *dev = kv.second;
@@ -296,7 +352,7 @@ int get_basis_dev(anigpu_ctx* h, int space, int order, const double** dev, Scala
 }
 
 int launch_fem3dtet(anigpu_ctx* h, int opA, int opB, int kind, int order, int precision, int64_t nt,
-                    const double* XY, const double* D, void* A) {
+                    const double* XY, const double* D, void* A, int face, int normal) {
     int nfA, dA, bsA, ncA, oA, nfB, dB, bsB, ncB, oB;
     if (!op_info(opA, &nfA, &dA, &bsA, &ncA, &oA) || !op_info(opB, &nfB, &dB, &bsB, &ncB, &oB))
         return set_err(h, ANIGPU_ERR_UNSUPPORTED, "unknown operator code");
@@ -304,29 +360,34 @@ int launch_fem3dtet(anigpu_ctx* h, int opA, int opB, int kind, int order, int pr
     if (nt == 0) return ANIGPU_OK;
     if (kind < ANIGPU_TENSOR_NULL || kind > ANIGPU_TENSOR_POINT)
         return set_err(h, ANIGPU_ERR_UNSUPPORTED, "tensor kind");
-    if (kind == ANIGPU_TENSOR_TET_SYM && (dA != 3 || dB != 3))
+    const int dBt = normal ? 3 * dB : dB;  // rows of the tensor the caller supplies
+    if (normal && face < 0) return set_err(h, ANIGPU_ERR_ARG, "the normal needs a face");
+    if (kind == ANIGPU_TENSOR_TET_SYM && (dA != 3 || dBt != 3))
         return set_err(h, ANIGPU_ERR_ARG, "TET_SYM needs 3x3 operators");
     if ((kind == ANIGPU_TENSOR_NULL || kind == ANIGPU_TENSOR_CONST_SCALAR || kind == ANIGPU_TENSOR_TET_SCALAR) &&
-        dA != dB && !(nfA == 1 && dA == 1))
+        dA != dBt && !(nfA == 1 && dA == 1))
         // diff_tensor.h:314-317: identity defined only for operators of the same dimension
         return set_err(h, ANIGPU_ERR_ARG, "Identity tensor defined only for compatible operators A and B");
     if (kind != ANIGPU_TENSOR_NULL && D == nullptr) return set_err(h, ANIGPU_ERR_ARG, "tensor data is NULL");
     if (!XY || !A) return set_err(h, ANIGPU_ERR_ARG, "NULL coordinates or output");
     const double *tA, *tB;
     ScalarBasisTable hA;
-    int rc = get_basis_dev(h, bsA, order, &tA, &hA);
+    if (face > 3) return set_err(h, ANIGPU_ERR_ARG, "face number must be 0..3");
+    int rc = get_basis_dev(h, bsA, order, &tA, &hA, face);
     if (rc) return rc;
-    rc = get_basis_dev(h, bsB, order, &tB, nullptr);
+    rc = get_basis_dev(h, bsB, order, &tB, nullptr, face);
     if (rc) return rc;
     ElemParams p;
     p.A = {nfA, dA, nfA / ncA, dA / ncA, ncA, oA, tA};
     p.B = {nfB, dB, nfB / ncB, dB / ncB, ncB, oB, tB};
     p.q = hA.q;
     p.kind = kind;
+    p.face = face;
+    p.normal = normal ? 1 : 0;
     p.w = tA + (size_t)hA.q * hA.nf * 4;
     const size_t tabs = (size_t)p.q * (p.A.nfs + p.B.nfs) * 4;
     const size_t rsz = precision == ANIGPU_F32 ? sizeof(float) : sizeof(double);
-    const size_t smem = sizeof(double) * (tabs + p.q + 10 + ANIGPU_MAX_DIM * ANIGPU_MAX_DIM) +
+    const size_t smem = sizeof(double) * (tabs + p.q + 13 + ANIGPU_MAX_DIM * ANIGPU_MAX_DIM) +
                         rsz * (size_t)(dA * nfA + dB * nfB + dB * nfA);
     int dev_sms = 148;
     cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, h->device);
@@ -344,10 +405,11 @@ int launch_fem3dtet(anigpu_ctx* h, int opA, int opB, int kind, int order, int pr
     return ANIGPU_OK;
 }
 
-int launch_quad_points(anigpu_ctx* h, int order, int64_t nt, const double* XY, double* XYG) {
+int launch_quad_points(anigpu_ctx* h, int order, int64_t nt, const double* XY, double* XYG, int face) {
     const double* tab;
     ScalarBasisTable host;
-    int rc = get_basis_dev(h, ANIGPU_P1, order, &tab, &host);
+    if (face > 3) return set_err(h, ANIGPU_ERR_ARG, "face number must be 0..3");
+    int rc = get_basis_dev(h, ANIGPU_P1, order, &tab, &host, face);
     if (rc) return rc;
     if (nt <= 0) return nt < 0 ? set_err(h, ANIGPU_ERR_ARG, "nt < 0") : ANIGPU_OK;
     const double* pts = tab + (size_t)host.q * host.nf * 4 + host.q;

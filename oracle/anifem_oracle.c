@@ -14,6 +14,7 @@
 #include <time.h>
 
 #include "../inmost-fem_gb300/csrc/quad_tables.h"
+#include "../inmost-fem_gb300/csrc/tri_quad_tables.h"
 
 #define MAXNF 30
 #define MAXDIM 9
@@ -250,20 +251,74 @@ static void gradgrad_sym(int space, int order, long nt, const double* XY, const 
     (void)g;
 }
 
-/* A(ib, ia) = sum_n w_n |T| sum_k V_k(ib) sum_j D(k,j) U_j(ia)
- * (core.inl:277-367: U = OpA(apply), DU (diff_tensor.h:488-552), A = V^T DU (core.inl:28-60)) */
-int orc_fem3dtet(int codeA, int codeB, int kind, int order, long nt, const double* XY, const double* D, double* A) {
+/* triangle area (Ani::tri_area, geometry.h:67-72) of face k = vertices k, k+1, k+2 (mod 4),
+ * from the coordinates relative to X0 as in the reference's XYP (int_face.inl:40-43) */
+static double face_area(const double* X, int face) {
+    double P[3][3];
+    for (int v = 0; v < 3; ++v) {
+        int node = (face + v) % 4;
+        for (int i = 0; i < 3; ++i) P[v][i] = node == 0 ? 0.0 : X[3 * node + i] - X[i];
+    }
+    double a[3] = {P[0][0] - P[2][0], P[0][1] - P[2][1], P[0][2] - P[2][2]};
+    double b[3] = {P[1][0] - P[2][0], P[1][1] - P[2][1], P[1][2] - P[2][2]};
+    double c[3] = {a[1] * b[2] - a[2] * b[1], -a[0] * b[2] + a[2] * b[0], a[0] * b[1] - a[1] * b[0]};
+    return sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]) / 2;
+}
+
+/* outward unit normal and area of face k (Ani::face_normal, geometry.h:77-93) on the coordinates
+ * relative to X0 (int_face.inl:72-76); the fourth vertex decides the orientation */
+static double face_normal(const double* X, int face, double* nrm) {
+    double P[4][3];
+    for (int v = 0; v < 4; ++v) {
+        int node = (face + v) % 4;
+        for (int i = 0; i < 3; ++i) P[v][i] = node == 0 ? 0.0 : X[3 * node + i] - X[i];
+    }
+    double a[3] = {P[1][0] - P[0][0], P[1][1] - P[0][1], P[1][2] - P[0][2]};
+    double b[3] = {P[2][0] - P[0][0], P[2][1] - P[0][1], P[2][2] - P[0][2]};
+    nrm[0] = a[1] * b[2] - a[2] * b[1];
+    nrm[1] = -a[0] * b[2] + a[2] * b[0];
+    nrm[2] = a[0] * b[1] - a[1] * b[0];
+    double len = sqrt(nrm[0] * nrm[0] + nrm[1] * nrm[1] + nrm[2] * nrm[2]);
+    for (int i = 0; i < 3; ++i) a[i] = P[3][i] - P[0][i];
+    double vol = nrm[0] * a[0] + nrm[1] * a[1] + nrm[2] * a[2];
+    for (int i = 0; i < 3; ++i) nrm[i] /= (vol > 0 ? -len : len);
+    return len / 2;
+}
+
+/* points of the triangle rule mapped onto face k (int_face.inl:31-36): 4 barycentric each */
+static int face_points(int order, int face, double* pts, const double** ww) {
+    const double* p3;
+    int q;
+    if (order < 0 || order > ANIGPU_TRI_MAX_ORDER || !anigpu_tri_rule(order, &p3, ww, &q)) return -1;
+    for (int n = 0; n < q; ++n) {
+        pts[4 * n + face] = p3[3 * n + 0];
+        pts[4 * n + (face + 1) % 4] = p3[3 * n + 1];
+        pts[4 * n + (face + 2) % 4] = p3[3 * n + 2];
+        pts[4 * n + (face + 3) % 4] = 0.0;
+    }
+    return q;
+}
+
+/* A(ib, ia) = sum_n w_n mes sum_k V_k(ib) sum_j D(k,j) U_j(ia)
+ * (core.inl:277-367: U = OpA(apply), DU (diff_tensor.h:488-552), A = V^T DU (core.inl:28-60));
+ * mes = |T| for the tet integral (face < 0), the face area for fem3Dface (int_face.inl:12-44) */
+/* normal != 0 (fem3DfaceN, int_face.inl:48-78): the tensor has 3*dB rows; DU's rows l + 3k are
+ * contracted with the outward normal (DotWithNormalHelper::ProcessNormal, core.h:175-190), which
+ * is the same as contracting the tensor's rows first; mes = the area from face_normal */
+static int elem_core(int codeA, int codeB, int kind, const double* pp, const double* ww, int q, int face, int normal,
+                     long nt, const double* XY, const double* D, double* A) {
     int nfA, dA, nfB, dB;
     if (orc_op_info(codeA, &nfA, &dA) || orc_op_info(codeB, &nfB, &dB)) return -1;
-    if ((kind == ORC_TET_SYM) && (dA != 3 || dB != 3)) return -1;
-    if ((kind == ORC_NULL || kind == ORC_CONST_SCALAR || kind == ORC_TET_SCALAR) && dA != dB && dA != 1) return -1;
-    const double *pp, *ww;
-    int q;
-    if (!anigpu_quad_rule(order, &pp, &ww, &q)) return -1;
+    int dBt = normal ? 3 * dB : dB;
+    if ((kind == ORC_TET_SYM) && (dA != 3 || dBt != 3)) return -1;
+    if ((kind == ORC_NULL || kind == ORC_CONST_SCALAR || kind == ORC_TET_SCALAR) && dA != dBt && dA != 1) return -1;
     double U[MAXDIM * MAXNF], V[MAXDIM * MAXNF], Dm[MAXDIM * MAXDIM], DU[MAXDIM * MAXNF];
+    double Dfull[3 * MAXDIM * MAXDIM];
     for (long t = 0; t < nt; ++t) {
-        double PSI[9], mes;
+        double PSI[9], mes, nrm[3];
         tet_geom(XY + 12 * t, PSI, &mes);
+        if (normal) mes = face_normal(XY + 12 * t, face, nrm);
+        else if (face >= 0) mes = face_area(XY + 12 * t, face);
         double* At = A + (size_t)t * nfA * nfB;
         memset(At, 0, sizeof(double) * nfA * nfB);
         for (int n = 0; n < q; ++n) {
@@ -275,10 +330,18 @@ int orc_fem3dtet(int codeA, int codeB, int kind, int order, long nt, const doubl
                 case ORC_CONST_SCALAR: src = D; break;
                 case ORC_TET_SCALAR: src = D + t; break;
                 case ORC_TET_SYM: src = D + 6 * t; break;
-                case ORC_TET_GENERAL: src = D + (size_t)dA * dB * t; break;
-                case ORC_POINT: src = D + (size_t)dA * dB * (n + (size_t)q * t); break;
+                case ORC_TET_GENERAL: src = D + (size_t)dA * dBt * t; break;
+                case ORC_POINT: src = D + (size_t)dA * dBt * (n + (size_t)q * t); break;
             }
-            expand_tensor(kind, src, dA, dB, Dm);
+            if (!normal) {
+                expand_tensor(kind, src, dA, dB, Dm);
+            } else {
+                expand_tensor(kind, src, dA, dBt, Dfull);
+                for (int k = 0; k < dB; ++k)
+                    for (int j = 0; j < dA; ++j)
+                        Dm[k + dB * j] = Dfull[(0 + 3 * k) + dBt * j] * nrm[0] + Dfull[(1 + 3 * k) + dBt * j] * nrm[1] +
+                                         Dfull[(2 + 3 * k) + dBt * j] * nrm[2];
+            }
             double wv = ww[n] * mes;
             for (int ia = 0; ia < nfA; ++ia)
                 for (int k = 0; k < dB; ++k) {
@@ -295,6 +358,61 @@ int orc_fem3dtet(int codeA, int codeB, int kind, int order, long nt, const doubl
         }
     }
     return 0;
+}
+
+int orc_fem3dtet(int codeA, int codeB, int kind, int order, long nt, const double* XY, const double* D, double* A) {
+    const double *pp, *ww;
+    int q;
+    if (!anigpu_quad_rule(order, &pp, &ww, &q)) return -1;
+    return elem_core(codeA, codeB, kind, pp, ww, q, -1, 0, nt, XY, D, A);
+}
+
+int orc_fem3dface(int codeA, int codeB, int kind, int order, int face, long nt, const double* XY, const double* D,
+                  double* A) {
+    double pts[4 * ANIGPU_TRI_MAX_POINTS];
+    const double* ww;
+    if (face < 0 || face > 3) return -1;
+    int q = face_points(order, face, pts, &ww);
+    if (q < 0) return -1;
+    return elem_core(codeA, codeB, kind, pts, ww, q, face, 0, nt, XY, D, A);
+}
+
+int orc_fem3dface_n(int codeA, int codeB, int kind, int order, int face, long nt, const double* XY, const double* D,
+                    double* A) {
+    double pts[4 * ANIGPU_TRI_MAX_POINTS];
+    const double* ww;
+    if (face < 0 || face > 3) return -1;
+    int q = face_points(order, face, pts, &ww);
+    if (q < 0) return -1;
+    return elem_core(codeA, codeB, kind, pts, ww, q, face, 1, nt, XY, D, A);
+}
+
+int orc_tri_rule(int order, double* p, double* w, int cap) {
+    const double *pp, *ww;
+    int np;
+    if (order < 0 || order > ANIGPU_TRI_MAX_ORDER || !anigpu_tri_rule(order, &pp, &ww, &np)) return -1;
+    if (np > cap) return -np;
+    memcpy(p, pp, sizeof(double) * 3 * np);
+    memcpy(w, ww, sizeof(double) * np);
+    return np;
+}
+
+int orc_face_quad_points(int order, int face, long nt, const double* XY, double* XYG) {
+    double pts[4 * ANIGPU_TRI_MAX_POINTS];
+    const double* ww;
+    if (face < 0 || face > 3) return -1;
+    int q = face_points(order, face, pts, &ww);
+    if (q < 0) return -1;
+    for (long t = 0; t < nt; ++t) {
+        const double* X = XY + 12 * t;
+        for (int n = 0; n < q; ++n)
+            for (int k = 0; k < 3; ++k) {
+                double s = X[k];
+                for (int l = 0; l < 3; ++l) s += pts[l + 1 + 4 * n] * (X[3 * (l + 1) + k] - X[k]);
+                XYG[3 * (n + (size_t)q * t) + k] = s;
+            }
+    }
+    return q;
 }
 
 /* ---------------------------------------------------------------- evaluation */

@@ -28,6 +28,17 @@ int orc_fem3dtet(int codeA, int codeB, int kind, int order, long nt, const doubl
  * fem3DapplyX (phys 1: per-tet physical points [nt][npts][3]); opU[nt][npts][dim] */
 int orc_fem3d_apply(int code, long nt, const double* XY, int npts, const double* pts, int phys,
                     const double* dofs, double* opU);
+/* face integrals (fem3Dface, int_face.inl:12-44): same layout as orc_fem3dtet, the triangle rule of
+ * `order` mapped onto face k = vertices {k, k+1, k+2 mod 4}, measure = the face area */
+int orc_fem3dface(int codeA, int codeB, int kind, int order, int face, long nt, const double* XY, const double* D,
+                  double* A);
+/* fem3DfaceN (int_face.inl:48-78): the tensor has 3*dimB rows, contracted with the outward normal */
+int orc_fem3dface_n(int codeA, int codeB, int kind, int order, int face, long nt, const double* XY, const double* D,
+                    double* A);
+/* the triangle rule of the face integrals (the table the product uses): p[3*np], w[np] */
+int orc_tri_rule(int order, double* p, double* w, int cap);
+/* physical points of that rule XYG[nt][q][3]; returns q */
+int orc_face_quad_points(int order, int face, long nt, const double* XY, double* XYG);
 /* Ani::applyDir (dc_on_dof.h:39-45) on one col-major n x n element matrix */
 void orc_apply_dir(int n, double* A, double* F, int k, double bc);
 

@@ -53,6 +53,10 @@ class Restated:
         L.orc_fem3dtet.argtypes = [_i, _i, _i, _i, _l, _vp, _vp, _vp]
         L.orc_apply_dir.argtypes = [_i, _vp, _vp, _i, _d]
         L.orc_fem3d_apply.argtypes = [_i, _l, _vp, _i, _vp, _i, _vp, _vp]
+        L.orc_fem3dface.argtypes = [_i, _i, _i, _i, _i, _l, _vp, _vp, _vp]
+        L.orc_face_quad_points.argtypes = [_i, _i, _l, _vp, _vp]
+        L.orc_tri_rule.argtypes = [_i, _vp, _vp, _i]
+        L.orc_fem3dface_n.argtypes = [_i, _i, _i, _i, _i, _l, _vp, _vp, _vp]
         L.orc_orient.argtypes = [_vp, _l, _vp]
         L.orc_edges.argtypes = [_l, _l, _vp, _vp]
         L.orc_edges.restype = _l
@@ -107,6 +111,34 @@ class Restated:
     def apply_dir(self, A, F, k, bc):
         n = F.shape[0]
         self.L.orc_apply_dir(n, _p(A), _p(F), k, bc)
+
+    def fem3dface(self, codeA, codeB, kind, order, face, XY, D=None, normal=False):
+        """Face-integral element matrices (fem3Dface; fem3DfaceN with normal), same layout as fem3dtet."""
+        XY = np.ascontiguousarray(XY, dtype=np.float64)
+        nt = XY.size // 12
+        nfA, _ = self.op_info(codeA)
+        nfB, _ = self.op_info(codeB)
+        A = np.zeros((nt, nfA, nfB))
+        Dd = None if D is None else np.ascontiguousarray(D, dtype=np.float64)
+        fn = self.L.orc_fem3dface_n if normal else self.L.orc_fem3dface
+        rc = fn(codeA, codeB, kind, order, face, nt, _p(XY), _p(Dd), _p(A))
+        assert rc == 0, rc
+        return A
+
+    def tri_rule(self, order):
+        p = np.zeros(3 * 64)
+        w = np.zeros(64)
+        n = self.L.orc_tri_rule(order, _p(p), _p(w), 64)
+        assert n > 0
+        return p[:3 * n].reshape(n, 3).copy(), w[:n].copy()
+
+    def face_quad_points(self, order, face, XY):
+        XY = np.ascontiguousarray(XY, dtype=np.float64)
+        nt = XY.size // 12
+        out = np.zeros(nt * 64 * 3)
+        q = self.L.orc_face_quad_points(order, face, nt, _p(XY), _p(out))
+        assert q > 0
+        return out[:nt * q * 3].reshape(nt, q, 3).copy()
 
     def fem3d_apply(self, code, XY, pts, dofs, phys=False):
         """Op(u) at points of each tet, opU[nt, npts, dim]: fem3DapplyL (pts [npts, 4] barycentric,
@@ -235,6 +267,9 @@ class Reference:
         L.ref_time_p2_sym.argtypes = [_l, _vp, _vp, _i, _i, _vp]
         L.ref_time_p2_sym.restype = _d
         L.ref_fem3d_apply.argtypes = [_i, _l, _vp, _i, _vp, _i, _vp, _vp]
+        L.ref_fem3dface.argtypes = [_i, _i, _i, _i, _i, _l, _vp, _vp, _i, _vp]
+        L.ref_fem3dface_n.argtypes = [_i, _i, _i, _i, _i, _l, _vp, _vp, _i, _vp]
+        L.ref_tri_quadrature.argtypes = [_i, _vp, _vp, _i, _vp]
         self.L = L
 
     def fem3dtet(self, codeA, codeB, kind, order, XY, D=None, fn=0, nfA=None, nfB=None):
@@ -245,6 +280,24 @@ class Reference:
         rc = self.L.ref_fem3dtet(codeA, codeB, kind, order, nt, _p(XY), _p(Dd), fn, _p(A))
         assert rc == 0, rc
         return A
+
+    def fem3dface(self, codeA, codeB, kind, order, face, XY, D=None, fn=0, nfA=None, nfB=None, normal=False):
+        XY = np.ascontiguousarray(XY, dtype=np.float64)
+        nt = XY.size // 12
+        A = np.zeros((nt, nfA, nfB))
+        Dd = None if D is None else np.ascontiguousarray(D, dtype=np.float64)
+        call = self.L.ref_fem3dface_n if normal else self.L.ref_fem3dface
+        rc = call(codeA, codeB, kind, order, face, nt, _p(XY), _p(Dd), fn, _p(A))
+        assert rc == 0, rc
+        return A
+
+    def tri_quadrature(self, order):
+        p = np.zeros(3 * 256)
+        w = np.zeros(256)
+        sym = np.zeros(3, dtype=np.int32)
+        n = self.L.ref_tri_quadrature(order, _p(p), _p(w), 256, _p(sym))
+        assert n > 0
+        return p[:3 * n].reshape(n, 3).copy(), w[:n].copy()
 
     def fem3d_apply(self, code, XY, pts, dofs, nf, dim, phys=False):
         return _apply(self.L.ref_fem3d_apply, (nf, dim), code, XY, pts, dofs, phys)

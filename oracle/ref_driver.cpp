@@ -62,6 +62,10 @@ struct Req {
     double* A;
 };
 
+// face of the fem3Dface requests (-1: fem3Dtet); g_normal: fem3DfaceN (tensor rows x 3)
+int g_face = -1;
+int g_normal = 0;
+
 template <typename OpA, typename OpB, typename Traits, typename F>
 void run_pairs(const Req& r, const F& functor_for_tet) {
     constexpr int nfA = OpA::Nfa::value, nfB = OpB::Nfa::value;
@@ -71,7 +75,11 @@ void run_pairs(const Req& r, const F& functor_for_tet) {
             XY2(const_cast<double*>(X + 6), 3, 1), XY3(const_cast<double*>(X + 9), 3, 1);
         DenseMatrix<> A(r.A + (size_t)t * nfA * nfB, nfB, nfA, nfA * nfB);
         auto f = functor_for_tet(t);
-        if (r.order <= 6) {
+        if (g_face >= 0 && g_normal) {
+            fem3DfaceN<OpA, OpB, Traits>(make_tetras(X, X + 3, X + 6, X + 9, 1), g_face, f, A, r.order);
+        } else if (g_face >= 0) {
+            fem3Dface<OpA, OpB, Traits>(make_tetras(X, X + 3, X + 6, X + 9, 1), g_face, f, A, r.order);
+        } else if (r.order <= 6) {
             fem3Dtet<OpA, OpB, Traits>(XY0, XY1, XY2, XY3, f, A, r.order);
         } else {
             auto req = fem3Dtet_memory_requirements<OpA, OpB>(r.order, 1);
@@ -85,7 +93,7 @@ void run_pairs(const Req& r, const F& functor_for_tet) {
 template <typename OpA, typename OpB>
 int run(const Req& r) {
     constexpr int dA = OpA::Dim::value, dB = OpB::Dim::value;
-    const size_t nD = (size_t)dA * dB;
+    const size_t nD = (size_t)dA * dB * (g_normal ? 3 : 1);
     switch (r.kind) {
         case K_NULL:
             run_pairs<OpA, OpB, DfuncTraits<TENSOR_NULL, true>>(r, [](long) { return TensorNull<>; });
@@ -194,6 +202,8 @@ int ref_fem3dtet(int codeA, int codeB, int kind, int order, long nt, const doubl
         PAIR(1, 51, I0, IV2)
         PAIR(12, 22, G1, G2)
         PAIR(22, 12, G2, G1)
+        PAIR(22, 21, G2, I2)
+        PAIR(12, 11, G1, I1)
 #undef PAIR
     } catch (const std::exception&) {
         return -2;
@@ -227,6 +237,25 @@ int ref_fem3d_apply(int code, long nt, const double* XY, int npts, const double*
     return -1;
 }
 
+// Ani::fem3Dface (anifem++/fem/operations/int_face.inl:12-44) for the same operator pairs,
+// face `face` of every tet of the batch
+int ref_fem3dface(int codeA, int codeB, int kind, int order, int face, long nt, const double* XY, const double* D,
+                  int fn, double* A) {
+    g_face = face;
+    const int rc = ref_fem3dtet(codeA, codeB, kind, order, nt, XY, D, fn, A);
+    g_face = -1;
+    return rc;
+}
+
+// Ani::fem3DfaceN (anifem++/fem/operations/int_face.inl:48-78): tensors of 3*dimB x dimA
+int ref_fem3dface_n(int codeA, int codeB, int kind, int order, int face, long nt, const double* XY,
+                    const double* D, int fn, double* A) {
+    g_normal = 1;
+    const int rc = ref_fem3dface(codeA, codeB, kind, order, face, nt, XY, D, fn, A);
+    g_normal = 0;
+    return rc;
+}
+
 int ref_quadrature(int order, double* p, double* w, int cap) {
     auto f = tetrahedron_quadrature_formulas(order);
     int np = f.GetNumPoints();
@@ -236,6 +265,21 @@ int ref_quadrature(int order, double* p, double* w, int cap) {
         for (int k = 0; k < 4; ++k) p[4 * i + k] = f.p[4 * i + k];
         w[i] = pw.w;
     }
+    return np;
+}
+
+// Ani::triangle_quadrature_formulas (anifem++/fem/quadrature_formulas.cpp:109): points as 3
+// barycentric coordinates, weights; returns the number of points (-np when cap is short);
+// sym receives the orbit counts (#s1, #s3, #s6)
+int ref_tri_quadrature(int order, double* p, double* w, int cap, int* sym) {
+    auto f = triangle_quadrature_formulas(order);
+    int np = f.GetNumPoints();
+    if (np > cap) return -np;
+    for (int i = 0; i < np; ++i) {
+        for (int k = 0; k < 3; ++k) p[3 * i + k] = f.p[3 * i + k];
+        w[i] = f.w[i];
+    }
+    for (int k = 0; k < 3; ++k) sym[k] = f.sym[k];
     return np;
 }
 

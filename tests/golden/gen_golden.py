@@ -13,7 +13,10 @@ Writes tests/golden/golden.npz with
                      sources by oracle/Makefile) on seeded random tets, for every operator
                      pair and tensor kind the GPU path provides;
   * apply_<code>_*   the reference's fem3DapplyL (order-4 quadrature points) and fem3DapplyX
-                     (seeded physical points) on the same tets for every operator code.
+                     (seeded physical points) on the same tets for every operator code;
+  * tri_<order>_*    the reference's triangle rules (quadrature_formulas.cpp:109);
+  * face_<name>_*    the reference's fem3Dface (int_face.inl:12-44) on the same tets, every face;
+  * facen_<name>_*   the reference's fem3DfaceN (int_face.inl:48-78), tensors of 3*dimB rows.
 """
 import os
 import re
@@ -136,6 +139,52 @@ def main():
         out[f"apply_{code}_L"] = R.fem3d_apply(code, XY, p4, dofs, nf, dim)
         out[f"apply_{code}_X"] = R.fem3d_apply(code, XY, out["apply_X"], dofs, nf, dim, phys=True)
     out["apply_codes"] = np.array(apply_codes)
+    # the reference's triangle rules and fem3Dface (every face, orders 0..9) on the same tets
+    for o in range(10):
+        p3, w3 = R.tri_quadrature(o)
+        out[f"tri_{o}_p"] = p3
+        out[f"tri_{o}_w"] = w3
+    face_cases = []
+    for (ca, cb) in [(1, 21), (21, 21), (1, 51), (11, 11), (1, 11), (22, 22), (12, 12)]:
+        nfA, dA = op_nf_dim(ca)
+        nfB, dB = op_nf_dim(cb)
+        gen = (meshgen.uniform(61 + ca + cb, nt * dA * dB) - 0.5).reshape(nt, dA * dB)
+        kinds = [("tgeneral", 4, gen)]
+        if dA == dB or dA == 1:
+            kinds += [("null", 0, None), ("tscalar", 2, scalar_tet)]
+        for order in (1, 2, 4, 7, 9):
+            for face in range(4):
+                for kname, kind, D in kinds:
+                    name = f"{ca}_{cb}_{kname}_o{order}_f{face}"
+                    out[f"face_{name}_A"] = R.fem3dface(ca, cb, kind, order, face, XY, D, nfA=nfA, nfB=nfB)
+                    if D is not None:
+                        out[f"face_{name}_D"] = np.asarray(D, dtype=np.float64)
+                    face_cases.append(name)
+                name = f"{ca}_{cb}_point0_o{order}_f{face}"
+                out[f"face_{name}_A"] = R.fem3dface(ca, cb, 5, order, face, XY, None, fn=0, nfA=nfA, nfB=nfB)
+                face_cases.append(name)
+    out["face_case_names"] = np.array(face_cases)
+    # fem3DfaceN: tensors of 3*dimB rows contracted with the outward normal
+    facen_cases = []
+    for (ca, cb) in [(1, 51), (1, 21), (22, 21), (12, 11)]:
+        nfA, dA = op_nf_dim(ca)
+        nfB, dB = op_nf_dim(cb)
+        dBt = 3 * dB
+        kinds = [("tgeneral", 4, (meshgen.uniform(71 + ca + cb, nt * dA * dBt) - 0.5).reshape(nt, dA * dBt))]
+        if dA == dBt or dA == 1:
+            kinds += [("null", 0, None), ("tscalar", 2, scalar_tet)]
+        if dA == 3 and dBt == 3:
+            kinds += [("tsym", 3, sym6)]
+        for order in (2, 5, 8):
+            for face in range(4):
+                for kname, kind, D in kinds:
+                    name = f"{ca}_{cb}_{kname}_o{order}_f{face}"
+                    out[f"facen_{name}_A"] = R.fem3dface(ca, cb, kind, order, face, XY, D, nfA=nfA, nfB=nfB,
+                                                         normal=True)
+                    if D is not None:
+                        out[f"facen_{name}_D"] = np.asarray(D, dtype=np.float64)
+                    facen_cases.append(name)
+    out["facen_case_names"] = np.array(facen_cases)
     path = os.path.join(HERE, "golden.npz")
     np.savez_compressed(path, **out)
     print(path, len(cases), "cases", os.path.getsize(path), "bytes")

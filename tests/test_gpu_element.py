@@ -32,7 +32,6 @@ def test_fem3dtet_f64_matches_reference(lib, golden):
         name = str(name)
         A = _run_case(lib, golden, name, anigpu.F64)
         err = rel_err_per_tet(A, golden[f"case_{name}_A"])
-        worst = max(worst, err)
         assert err <= 1e-12, (name, err)
     print("worst FP64 relative error per tet:", worst)
 
@@ -166,3 +165,38 @@ def test_eval_solution_matches_oracle_and_reproduces_quadratics(lib, restated, s
         assert np.abs(grad[..., :3] - gx).max() <= 1e-11
         if k == 3:
             assert np.abs(val[..., 2] - f(XG)).max() <= 1e-12
+
+
+def test_fem3dface_matches_reference(lib, golden):
+    """anigpu_fem3dface (FP64) against the reference's fem3Dface on every face, orders 1-9, constant,
+    per-tet and per-point tensors: within 1e-12 per tet."""
+    import anigpu
+    XY = golden["tets_XY"]
+    for name in golden["face_case_names"]:
+        name = str(name)
+        ca, cb = (int(v) for v in name.split("_")[:2])
+        kname, order, face = name.split("_")[2], int(name.split("_")[3][1:]), int(name.split("_")[4][1:])
+        nfA, dA = op_nf_dim(ca)
+        nfB, dB = op_nf_dim(cb)
+        if kname.startswith("point"):
+            q = lib.face_quadrature_points(order, face, XY).cpu().numpy()
+            D = point_tensor(int(kname[5:]), q, dB, dA)
+            A = lib.fem3dface(ca, cb, XY, face, D, anigpu.TENSOR_POINT, order)
+        else:
+            D = golden[f"face_{name}_D"] if f"face_{name}_D" in golden.files else None
+            A = lib.fem3dface(ca, cb, XY, face, D, KIND_CODE[kname], order)
+        err = rel_err_per_tet(A.cpu().numpy(), golden[f"face_{name}_A"])
+        assert err <= 1e-12, (name, err)
+
+
+def test_fem3dface_n_matches_reference(lib, golden):
+    """anigpu_fem3dface_n (FP64) against the reference's fem3DfaceN: within 1e-12 per tet."""
+    XY = golden["tets_XY"]
+    for name in golden["facen_case_names"]:
+        name = str(name)
+        ca, cb = (int(v) for v in name.split("_")[:2])
+        kname, order, face = name.split("_")[2], int(name.split("_")[3][1:]), int(name.split("_")[4][1:])
+        D = golden[f"facen_{name}_D"] if f"facen_{name}_D" in golden.files else None
+        A = lib.fem3dface(ca, cb, XY, face, D, KIND_CODE[kname], order, normal=True)
+        err = rel_err_per_tet(A.cpu().numpy(), golden[f"facen_{name}_A"])
+        assert err <= 1e-12, (name, err)

@@ -69,7 +69,6 @@ def test_oracle_matches_reference_fem3dtet(restated, golden):
             D = golden[f"case_{name}_D"] if f"case_{name}_D" in golden.files else None
             A = restated.fem3dtet(ca, cb, KIND_CODE[kind], order, XY, D)
         err = rel_err_per_tet(A, Aref)
-        worst = max(worst, err)
         assert err <= 1e-12, (name, err)
     assert worst <= 1e-12
 
@@ -184,3 +183,55 @@ def test_oracle_apply_matches_reference(restated, golden):
             assert got.shape == ref.shape
             scale = max(np.abs(ref).max(), 1e-300)
             assert np.abs(got - ref).max() <= 1e-13 * scale, (code, key)
+
+
+@pytest.mark.parametrize("order", range(10))
+def test_triangle_rules_match_reference(restated, golden, order):
+    """The recomputed triangle rules of the face integrals equal the reference's
+    (triangle_quadrature_formulas, quadrature_formulas.cpp:109) as sets of (point, weight)."""
+    p, w = restated.tri_rule(order)
+    pr, wr = golden[f"tri_{order}_p"], golden[f"tri_{order}_w"]
+    assert p.shape == pr.shape
+    for pt, wt in zip(pr, wr):
+        d = np.abs(p - pt).max(axis=1)
+        k = int(np.argmin(d))
+        assert d[k] <= 1e-15 and abs(w[k] - wt) <= 1e-15
+    assert abs(w.sum() - 1) <= 1e-15
+
+
+def _face_case(name):
+    """'<codeA>_<codeB>_<kind>_o<order>_f<face>' -> its parts"""
+    ca, cb, kname, o, f = name.split("_")
+    return int(ca), int(cb), kname, int(o[1:]), int(f[1:])
+
+
+def test_oracle_fem3dface_matches_reference(restated, golden):
+    """fem3Dface of the restatement against the reference's own (int_face.inl:12-44): every face,
+    orders 1-9, constant, per-tet and per-point tensors."""
+    XY = golden["tets_XY"]
+    for name in golden["face_case_names"]:
+        ca, cb, kname, order, face = _face_case(str(name))
+        if kname.startswith("point"):
+            nfA, dA = op_nf_dim(ca)
+            nfB, dB = op_nf_dim(cb)
+            D = point_tensor(int(kname[5:]), restated.face_quad_points(order, face, XY), dB, dA)
+            A = restated.fem3dface(ca, cb, 5, order, face, XY, D)
+        else:
+            D = golden[f"face_{name}_D"] if f"face_{name}_D" in golden.files else None
+            A = restated.fem3dface(ca, cb, KIND_CODE[kname], order, face, XY, D)
+        ref = golden[f"face_{name}_A"]
+        err = rel_err_per_tet(A, ref)
+        assert err <= 1e-12, (name, err)
+
+
+def test_oracle_fem3dface_n_matches_reference(restated, golden):
+    """fem3DfaceN (the tensor's 3*dimB rows contracted with the outward normal) of the restatement
+    against the reference's own (int_face.inl:48-78): traction from a general tensor, normal
+    derivative (NULL), flux (D grad u).n (SYM)."""
+    XY = golden["tets_XY"]
+    for name in golden["facen_case_names"]:
+        ca, cb, kname, order, face = _face_case(str(name))
+        D = golden[f"facen_{name}_D"] if f"facen_{name}_D" in golden.files else None
+        A = restated.fem3dface(ca, cb, KIND_CODE[kname], order, face, XY, D, normal=True)
+        err = rel_err_per_tet(A, golden[f"facen_{name}_A"])
+        assert err <= 1e-12, (name, err)
