@@ -361,6 +361,8 @@ struct RowParams {
     int cap;  // row buffer capacity (>= longest row)
     int vec_ok;  // the value array is 16-byte aligned: vector stores
     double drop;
+    const int32_t* vcol;  // vector template columns (non-zero boundary values of the vector path)
+    int bcnz;             // vector path: non-zero boundary values
 };
 
 
@@ -1075,11 +1077,22 @@ __global__ void __launch_bounds__(64) vec_row_gather_kernel(RowParams p, int64_t
                 const int od = (int)byte_of(dc < 4 ? rd.off03 : rd.off47, dc);
                 myRow[c * L + od] = Real(deg);
             }
-            F = 0;  // homogeneous boundary values only in the vector path
+            // rhs = bc per incident tet (applyDir sets F(k) = bc in every element, dc_on_dof.h:39-45)
+            const double bcr = p.bcnz ? p.dir_bc[R] : 0.0;
+            F = 0;
+            for (int q = 0; q < deg; ++q) F += bcr;
         } else {
             F = (double)racc;
-            if (DIR)
-                for (int64_t q = p.dir_cptr[R]; q < p.dir_cptr[R + 1]; ++q) myRow[p.dir_coff[q]] = Real(0);
+            if (DIR) {
+                // Dirichlet columns: F -= A(i,k) bc_k with the assembled A(i,k) (the sum over the tets of
+                // applyDir's per-element F -= A(:,k) bc), then the column is eliminated
+                const int64_t vb = vrowptr[R];
+                for (int64_t q = p.dir_cptr[R]; q < p.dir_cptr[R + 1]; ++q) {
+                    const int off = p.dir_coff[q];
+                    if (p.bcnz) F -= (double)myRow[off] * p.dir_bc[p.vcol[vb + off]];
+                    myRow[off] = Real(0);
+                }
+            }
         }
         bad |= !isfinite(F);
         rhs[R] = F;
@@ -1232,7 +1245,6 @@ static int run_assemble_vec(anigpu_ctx* h, int kind, const double* D, const doub
     if (!D) return set_err(h, ANIGPU_ERR_ARG, "tensor data is NULL");
     if (!vals || !rhs) return set_err(h, ANIGPU_ERR_ARG, "NULL output");
     if (touched) return set_err(h, ANIGPU_ERR_UNSUPPORTED, "no touched map for vector P2 assembly");
-    if (h->bc_nonzero) return set_err(h, ANIGPU_ERR_UNSUPPORTED, "vector P2 assembly supports zero boundary values only");
     if (precision != ANIGPU_F32 && precision != ANIGPU_F64) return set_err(h, ANIGPU_ERR_ARG, "precision");
     const double *pp, *ww;
     int q;
@@ -1265,6 +1277,8 @@ static int run_assemble_vec(anigpu_ctx* h, int kind, const double* D, const doub
     p.vec_ok = 0;
     p.dir_cptr = h->dir_cptr;
     p.dir_coff = h->dir_coff;
+    p.vcol = h->col;
+    p.bcnz = h->bc_nonzero ? 1 : 0;
     cudaStream_t side = h->side_stream ? h->side_stream : h->stream;
     if (side != h->stream) {
         ANI_CUDA(h, cudaEventRecord(h->fork_ev, h->stream));

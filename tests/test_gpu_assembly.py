@@ -210,10 +210,11 @@ def _lame9(lam, mu):
     return D.reshape(lam.size, 81)
 
 
-@pytest.mark.parametrize("n,clamped", [(3, False), (4, True)])
-def test_vector_p2_lame_matches_oracle(lib, restated, n, clamped):
+@pytest.mark.parametrize("n,clamped,bcnz", [(3, False, False), (4, True, False), (4, True, True), (3, False, True)])
+def test_vector_p2_lame_matches_oracle(lib, restated, n, clamped, bcnz):
     """Vector P2 linear elasticity (config 5 operator): FP64 assembly with per-tet Lame parameters
-    equals the restated assembler with the 9x9 GENERAL tensor; FP32 within 5e-5 per row."""
+    equals the restated assembler with the 9x9 GENERAL tensor; FP32 within 5e-5 per row; with
+    non-zero boundary displacements (different per component) the right-hand side too."""
     import anigpu
     from anigpu import meshgen
     xyz, tets = meshgen.kuhn_cube(n, perturb=0.2, seed=5)
@@ -225,10 +226,14 @@ def test_vector_p2_lame_matches_oracle(lib, restated, n, clamped):
     ndof, nnz = lib.problem_setup(anigpu.VEC3_P2)
     coords = lib.dof_coords().cpu().numpy()
     mask = (np.abs(coords[:, 0]) < 1e-12).astype(np.uint8) if clamped else meshgen.boundary_mask(coords)
-    lib.set_dirichlet(mask)
+    bc = None
+    if bcnz:
+        comp = np.repeat(np.arange(3), ndof // 3)
+        bc = (0.1 * coords[:, 1] - 0.05 * coords[:, 2] + 0.02 * (comp + 1)) * mask
+    lib.set_dirichlet(mask, bc)
     LM = np.stack([lam, mu], axis=1)
     vals, rhs, _ = lib.assemble(anigpu.TENSOR_LAME, LM, None, 0.5, 4, anigpu.F64)
-    ref = restated.assemble_problem(xyz, tets, 5, 4, _lame9(lam, mu), 0.5, 4, dirichlet=(mask, None))
+    ref = restated.assemble_problem(xyz, tets, 5, 4, _lame9(lam, mu), 0.5, 4, dirichlet=(mask, bc))
     rp, col = lib.csr_template()
     assert np.array_equal(rp.cpu().numpy(), ref["rowptr"]) and np.array_equal(col.cpu().numpy(), ref["col"])
     v = vals.cpu().numpy()
