@@ -134,6 +134,31 @@ int anigpu_face_quadrature(int order, double* p_host, double* w_host, int cap);
 /* physical points of the face rule, XYG[nt][q][3] */
 int anigpu_face_quadrature_points(anigpu_handle h, int order, int face, int64_t nt, const double* XY, double* XYG);
 
+/* ---- global enumerations (GlobEnumeration::ASSEMBLING_TYPE, anifem++/inmost_interface/
+ * global_enumerator.h:392-404; same values).  anigpu_problem_setup numbers the DOFs NATURAL
+ * (VAR DIM ELEM_TYPE ELEM_ID DOF_ID: component-major blocks, nodes before edges); the other types
+ * order the same key differently.  For the spaces of this library (one variable, one DOF per node
+ * or edge) they give three numberings of DOF (component c, scalar DOF s): NATURAL c*nds + s;
+ * ANITYPE and BYELEMTYPE: nodes of component 0, 1, 2, then edges of component 0, 1, 2; MINIBLOCKS,
+ * DIMUNION and ETDIMBLOCKS: the components of a node or edge together (ncomp*s + c).  Scalar spaces:
+ * all equal NATURAL.
+ * setup: the permutation, the template in the new numbering and the map of every template slot;
+ * template: rowptr[ndof+1] / col[nnz] of that template (rows sorted) and perm[ndof] (new index of
+ * each NATURAL DOF), any may be NULL; apply: values (precision F32/F64) and right-hand side of an
+ * assembled system into the new numbering (one gather, not in place; either pair may be NULL);
+ * to_natural: a vector of the new numbering (e.g. a solution) back to NATURAL. */
+#define ANIGPU_ENUM_ANITYPE 0
+#define ANIGPU_ENUM_MINIBLOCKS 1
+#define ANIGPU_ENUM_NATURAL 2
+#define ANIGPU_ENUM_DIMUNION 3
+#define ANIGPU_ENUM_BYELEMTYPE 4
+#define ANIGPU_ENUM_ETDIMBLOCKS 5
+int anigpu_enumeration_setup(anigpu_handle h, int type);
+int anigpu_enumeration_template(anigpu_handle h, int64_t* rowptr, int32_t* col, int64_t* perm);
+int anigpu_enumeration_apply(anigpu_handle h, const void* vals_in, int precision, const double* rhs_in, void* vals_out,
+                             double* rhs_out);
+int anigpu_enumeration_to_natural(anigpu_handle h, const double* x_in, double* x_out);
+
 /* ---- evaluation of Op(u) at points of each tet (FP64).
  * anigpu_fem3d_apply is Ani::fem3DapplyL (anifem++/fem/operations/eval.h:13-18,93-111, eval.inl:93-111)
  *   over the whole batch: XYL[npts][4] barycentric points shared by every tet (the reference's

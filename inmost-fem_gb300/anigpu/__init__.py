@@ -23,6 +23,8 @@ ERR_NONFINITE, ERR_BAD_ELEMENT, ERR_ARG, ERR_UNSUPPORTED, ERR_CUDA, ERR_NOT_CONV
     -1, -2, -3, -4, -5, -6, -7, -8)
 P0, P1, P2, P3, VEC3_P1, VEC3_P2 = 0, 1, 2, 3, 4, 5
 IDEN, GRAD = 1, 2
+# GlobEnumeration::ASSEMBLING_TYPE (global_enumerator.h:392-404)
+ENUM_ANITYPE, ENUM_MINIBLOCKS, ENUM_NATURAL, ENUM_DIMUNION, ENUM_BYELEMTYPE, ENUM_ETDIMBLOCKS = 0, 1, 2, 3, 4, 5
 TENSOR_NULL, TENSOR_CONST_SCALAR, TENSOR_TET_SCALAR, TENSOR_TET_SYM, TENSOR_TET_GENERAL, TENSOR_POINT = range(6)
 TENSOR_LAME = 7
 F64, F32, BF16 = 0, 1, 2
@@ -53,6 +55,10 @@ SIGNATURES = {
     "anigpu_fem3dface_n": (_i, [_vp, _i, _i, _i, _i, _i, _i64, _vp, _i, _vp, _vp]),
     "anigpu_face_quadrature": (_i, [_i, _vp, _vp, _i]),
     "anigpu_face_quadrature_points": (_i, [_vp, _i, _i, _i64, _vp, _vp]),
+    "anigpu_enumeration_setup": (_i, [_vp, _i]),
+    "anigpu_enumeration_template": (_i, [_vp, _vp, _vp, _vp]),
+    "anigpu_enumeration_apply": (_i, [_vp, _vp, _i, _vp, _vp, _vp]),
+    "anigpu_enumeration_to_natural": (_i, [_vp, _vp, _vp]),
     "anigpu_fem3d_apply": (_i, [_vp, _i, _i64, _vp, _i, _vp, _vp, _vp]),
     "anigpu_fem3d_apply_x": (_i, [_vp, _i, _i64, _vp, _i, _vp, _vp, _vp]),
     "anigpu_eval_solution": (_i, [_vp, _i, _vp, _i, _vp, _vp]),
@@ -302,6 +308,37 @@ class Anigpu:
         q = face_quadrature(order)[1].size
         out = torch.empty((nt, q, 3), dtype=torch.float64, device=XY.device)
         self._check(self.lib.anigpu_face_quadrature_points(self.h, order, face, nt, _ptr(XY), _ptr(out)))
+        return out
+
+    @_streamed
+    def enumeration_setup(self, etype):
+        """Renumbering of the set-up problem into enumeration etype (ENUM_*); returns
+        (rowptr, col, perm) of the new template (perm: new index of each NATURAL DOF)."""
+        torch = self.torch
+        self._check(self.lib.anigpu_enumeration_setup(self.h, etype))
+        dev = f"cuda:{self.device}"
+        rp = torch.empty(self.ndof + 1, dtype=torch.int64, device=dev)
+        col = torch.empty(self.nnz, dtype=torch.int32, device=dev)
+        perm = torch.empty(self.ndof, dtype=torch.int64, device=dev)
+        self._check(self.lib.anigpu_enumeration_template(self.h, _ptr(rp), _ptr(col), _ptr(perm)))
+        return rp, col, perm
+
+    @_streamed
+    def enumeration_apply(self, vals, precision, rhs=None):
+        """Values (and right-hand side) of an assembled NATURAL system in the set-up enumeration."""
+        torch = self.torch
+        vout = torch.empty_like(vals)
+        rout = torch.empty_like(rhs) if rhs is not None else None
+        self._check(self.lib.anigpu_enumeration_apply(self.h, _ptr(vals), precision, _ptr(rhs), _ptr(vout),
+                                                      _ptr(rout)))
+        return vout, rout
+
+    @_streamed
+    def enumeration_to_natural(self, x):
+        torch = self.torch
+        xd = self._dev(x, torch.float64)
+        out = torch.empty_like(xd)
+        self._check(self.lib.anigpu_enumeration_to_natural(self.h, _ptr(xd), _ptr(out)))
         return out
 
     @_streamed

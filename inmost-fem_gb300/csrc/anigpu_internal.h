@@ -118,6 +118,7 @@ struct anigpu_ctx {
     void* learned = nullptr;       // learned preconditioner state
     void* fcg_ws = nullptr;        // flexible-CG workspace and its captured graphs
     void* batch_ws = nullptr;      // batched-instances map, tiles and solver workspace
+    void* enum_ws = nullptr;       // renumbering to a non-NATURAL enumeration
 
     // per-phase timing (anigpu_set_timing)
     bool timing = false;
@@ -176,6 +177,12 @@ inline unsigned grid_for(int64_t n, int block) {
 int launch_fem3dtet(anigpu_ctx* h, int opA, int opB, int kind, int order, int precision, int64_t nt,
                     const double* XY, const double* D, void* A, int face = -1, int normal = 0);
 int launch_quad_points(anigpu_ctx* h, int order, int64_t nt, const double* XY, double* XYG, int face = -1);
+// enumerations (k_enum.cu)
+void free_enum(anigpu_ctx* h);
+int enum_setup(anigpu_ctx* h, int type);
+int enum_template(anigpu_ctx* h, int64_t* rowptr, int32_t* col, int64_t* perm);
+int enum_apply(anigpu_ctx* h, const void* vals_in, int precision, const double* rhs_in, void* vals_out, double* rhs_out);
+int enum_to_natural(anigpu_ctx* h, const double* x_in, double* x_out);
 int launch_fem3d_apply(anigpu_ctx* h, int op, int64_t nt, const double* XY, int npts, const double* pts, int phys,
                        const double* dofs, const double* x, double* out);
 int launch_apply_dir(anigpu_ctx* h, int64_t nt, int n, double* A, double* F, const uint32_t* mask, const double* bc);

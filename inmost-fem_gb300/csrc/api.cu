@@ -66,6 +66,7 @@ int anigpu_destroy(anigpu_handle h) {
     free_fcg(h);
     free_learned(h);
     free_batch(h);
+    free_enum(h);
     void* ptrs[] = {h->xyz, h->xyz2, h->tets, h->tet_edges, h->edofs, h->inc_ptr, h->recs, h->dir_mask, h->dir_bc,
                     h->dir_cptr, h->dir_coff,
                     h->tetdata, h->d_status, h->d_ref_tables};
@@ -173,6 +174,31 @@ int anigpu_face_quadrature_points(anigpu_handle h, int order, int face, int64_t 
     return launch_quad_points(h, order, nt, XY, XYG, face);
 }
 
+int anigpu_enumeration_setup(anigpu_handle h, int type) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    return enum_setup(h, type);
+}
+
+int anigpu_enumeration_template(anigpu_handle h, int64_t* rowptr, int32_t* col, int64_t* perm) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    return enum_template(h, rowptr, col, perm);
+}
+
+int anigpu_enumeration_apply(anigpu_handle h, const void* vals_in, int precision, const double* rhs_in, void* vals_out,
+                             double* rhs_out) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    return enum_apply(h, vals_in, precision, rhs_in, vals_out, rhs_out);
+}
+
+int anigpu_enumeration_to_natural(anigpu_handle h, const double* x_in, double* x_out) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    return enum_to_natural(h, x_in, x_out);
+}
+
 int anigpu_fem3d_apply(anigpu_handle h, int op, int64_t nt, const double* XY, int npts, const double* XYL,
                        const double* dofs, double* opU) {
     CHECK_H(h);
@@ -212,6 +238,7 @@ int anigpu_mesh_upload(anigpu_handle h, int64_t nv, const double* xyz, int64_t n
     cudaSetDevice(h->device);
     learned_invalidate(h);  // bindings and captured solver graphs refer to the old mesh
     free_batch(h);
+    free_enum(h);
     int rc = dev_alloc(h, &h->xyz, (size_t)nv * 3);
     if (rc) return rc;
     rc = dev_alloc(h, &h->tets, (size_t)nt * 4);
@@ -243,6 +270,7 @@ int anigpu_problem_setup(anigpu_handle h, int space) {
     cudaSetDevice(h->device);
     learned_invalidate(h);
     free_batch(h);
+    free_enum(h);
     return setup_problem(h, space);
 }
 

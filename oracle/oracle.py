@@ -315,3 +315,42 @@ class Reference:
         A = np.zeros((nt, 100))
         sec = self.L.ref_time_p2_sym(nt, _p(XY), _p(D6), order, nthreads, _p(A))
         return sec, A
+
+
+# GlobEnumeration::ASSEMBLING_TYPE key orders (anifem++/inmost_interface/global_enumerator.h:392-404):
+# the DOFs are sorted lexicographically by these fields of their natural index
+_ENUM_KEYS = {
+    0: ("ELEM_TYPE", "VAR", "DIM", "DOF_ID", "ELEM_ID"),   # ANITYPE
+    1: ("ELEM_TYPE", "ELEM_ID", "VAR", "DIM", "DOF_ID"),   # MINIBLOCKS
+    2: ("VAR", "DIM", "ELEM_TYPE", "ELEM_ID", "DOF_ID"),   # NATURAL
+    3: ("VAR", "ELEM_TYPE", "ELEM_ID", "DOF_ID", "DIM"),   # DIMUNION
+    4: ("ELEM_TYPE", "VAR", "DIM", "ELEM_ID", "DOF_ID"),   # BYELEMTYPE
+    5: ("ELEM_TYPE", "VAR", "ELEM_ID", "DOF_ID", "DIM"),   # ETDIMBLOCKS
+}
+
+
+def enumeration_perm(nv, nds, ncomp, etype):
+    """New index of every NATURAL DOF (component c, scalar DOF s: a node for s < nv, else edge
+    s - nv) under enumeration etype: the rank of its natural index (VAR 0, DIM c, ELEM_TYPE node 0 /
+    edge 1, ELEM_ID, DOF_ID 0) in the lexicographic order of that type's key."""
+    n = nds * ncomp
+    R = np.arange(n)
+    c, s = R // nds, R % nds
+    fields = {"VAR": np.zeros(n, dtype=np.int64), "DIM": c, "ELEM_TYPE": (s >= nv).astype(np.int64),
+              "ELEM_ID": np.where(s < nv, s, s - nv), "DOF_ID": np.zeros(n, dtype=np.int64)}
+    keys = [fields[k] for k in _ENUM_KEYS[etype]]
+    order = np.lexsort(keys[::-1])  # the first field is the most significant
+    perm = np.empty(n, dtype=np.int64)
+    perm[order] = np.arange(n)
+    return perm
+
+
+def permute_csr(rowptr, col, vals, perm):
+    """P A P^T of a CSR matrix (rows and columns renumbered by perm), rows sorted by column."""
+    n = rowptr.size - 1
+    rows = np.repeat(np.arange(n), np.diff(rowptr))
+    nr, nc = perm[rows], perm[col]
+    order = np.lexsort((nc, nr))
+    rp = np.zeros(n + 1, dtype=np.int64)
+    np.add.at(rp, nr + 1, 1)
+    return np.cumsum(rp), nc[order].astype(np.int32), np.asarray(vals)[order]

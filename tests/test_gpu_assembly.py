@@ -281,3 +281,39 @@ def test_vector_p2_solves_match_oracle(lib, restated):
     x32, st32 = lib.solve(v32, b, anigpu.SOLVE_IR_CG32, anigpu.F32, rtol=1e-8, maxit=200000)
     assert st32.rel_residual <= 1e-8
     assert restated.true_residual(rp, col, v32.double().cpu().numpy(), x32.cpu().numpy(), b) <= 1e-8
+
+
+@pytest.mark.parametrize("space", [1, 2, 5])
+def test_enumerations_match_oracle(lib, restated, space):
+    """Every GlobEnumeration type: the GPU's permutation, renumbered template and renumbered
+    values / right-hand side equal the oracle's lexicographic ordering applied to the NATURAL
+    system (bit for bit); a vector comes back to NATURAL."""
+    import anigpu
+    from anigpu import meshgen
+    from oracle.oracle import enumeration_perm, permute_csr
+    xyz, tets = meshgen.kuhn_cube(3, perturb=0.2, seed=4)
+    lib.mesh_upload(xyz, tets)
+    ndof, nnz = lib.problem_setup(space)
+    ncomp = 3 if space == 5 else 1
+    lib.set_dirichlet(meshgen.boundary_mask(lib.dof_coords().cpu().numpy()))
+    if space == 5:
+        nt = tets.shape[0]
+        LM = np.stack([np.full(nt, 1.5), np.full(nt, 1.0)], axis=1)
+        vals, rhs, _ = lib.assemble(anigpu.TENSOR_LAME, LM, None, 0.5, 4, anigpu.F64)
+    else:
+        vals, rhs, _ = lib.assemble(anigpu.TENSOR_NULL, None, None, 1.0, 4, anigpu.F64)
+    rp, col = lib.csr_template()
+    rp, col, v, b = rp.cpu().numpy(), col.cpu().numpy(), vals.cpu().numpy(), rhs.cpu().numpy()
+    nv = xyz.shape[0]
+    for etype in range(6):
+        perm = enumeration_perm(nv, ndof // ncomp, ncomp, etype)
+        rp_o, col_o, v_o = permute_csr(rp, col, v, perm)
+        grp, gcol, gperm = lib.enumeration_setup(etype)
+        assert np.array_equal(gperm.cpu().numpy(), perm), etype
+        assert np.array_equal(grp.cpu().numpy(), rp_o) and np.array_equal(gcol.cpu().numpy(), col_o), etype
+        gv, gb = lib.enumeration_apply(vals, anigpu.F64, rhs)
+        assert np.array_equal(gv.cpu().numpy(), v_o), etype
+        b_o = np.empty_like(b)
+        b_o[perm] = b
+        assert np.array_equal(gb.cpu().numpy(), b_o), etype
+        assert np.array_equal(lib.enumeration_to_natural(gb).cpu().numpy(), b), etype
