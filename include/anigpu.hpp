@@ -1,0 +1,143 @@
+/* C++ runtime-space layer over the anigpu C ABI (header only).
+ *
+ * Mirrors the reference's runtime operator / space interface, so that code written against
+ *   Ani::ApplyOp / Ani::ApplyOpBase   (anifem++/fem/operators.h:418-450)
+ *   Ani::FemSpace::getOP(OperatorType) (anifem++/fem/fem_space.h:404-589)
+ *   Ani::fem3Dtet / fem3Dface / fem3DfaceN / fem3DapplyL / fem3DapplyX with runtime operators
+ *     (anifem++/fem/operations/int_tet.h:111-147, int_face.h, eval.h:80-87)
+ * finds the same names: an ApplyOp is an operator code (10*space + op) with Nfa(), Dim() and
+ * Order(); a FemSpace hands out its operators; the integrals run the library's batched kernels on
+ * device arrays.  Errors come back as std::runtime_error, as the reference throws them.
+ *
+ * Spaces: P0, P1, P2, P3 and FemVec<3, P1 | P2> (component-major DOF blocks, the reference's
+ * FemVec order).  Operators: IDEN, GRAD. */
+#ifndef ANIGPU_HPP
+#define ANIGPU_HPP
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+
+#include "anigpu.h"
+
+namespace anigpu {
+
+enum OperatorType { IDEN = ANIGPU_IDEN, GRAD = ANIGPU_GRAD };
+
+inline void check(anigpu_handle h, int rc) {
+    if (rc != ANIGPU_OK) {
+        const char* msg = h ? anigpu_last_error(h) : "";
+        throw std::runtime_error("anigpu error " + std::to_string(rc) + ": " + (msg ? msg : ""));
+    }
+}
+
+/* An operator applied to a space: Operator<OP, FEM> as a runtime value. */
+class ApplyOp {
+public:
+    ApplyOp() = default;
+    explicit ApplyOp(int code) : code_(code) {
+        const int space = code / 10, op = code % 10;
+        if ((op != ANIGPU_IDEN && op != ANIGPU_GRAD) || space < ANIGPU_P0 || space > ANIGPU_VEC3_P2)
+            throw std::invalid_argument("unknown operator code " + std::to_string(code));
+    }
+    int code() const { return code_; }
+    int space() const { return code_ / 10; }
+    OperatorType type() const { return static_cast<OperatorType>(code_ % 10); }
+    unsigned ncomp() const { return space() == ANIGPU_VEC3_P1 || space() == ANIGPU_VEC3_P2 ? 3u : 1u; }
+    unsigned base_space() const { return ncomp() == 3 ? (unsigned)space() - 3u : (unsigned)space(); }
+    /* local DOFs of the operator's space (Operator::Nfa) */
+    unsigned Nfa() const {
+        static const unsigned nfs[4] = {1, 4, 10, 20};
+        return nfs[base_space()] * ncomp();
+    }
+    /* rows of the operator's value at a point (Operator::Dim) */
+    unsigned Dim() const { return (type() == IDEN ? 1u : 3u) * ncomp(); }
+    /* polynomial order of the operator's value */
+    unsigned Order() const {
+        const unsigned p = base_space();
+        return type() == GRAD ? (p > 0 ? p - 1 : 0) : p;
+    }
+    bool operator==(const ApplyOp& o) const { return code_ == o.code_; }
+    bool operator!=(const ApplyOp& o) const { return code_ != o.code_; }
+
+private:
+    int code_ = 10 * ANIGPU_P1 + ANIGPU_IDEN;
+};
+
+/* A finite element space as a runtime value (Ani::FemSpace). */
+class FemSpace {
+public:
+    FemSpace() = default;
+    static FemSpace P0() { return FemSpace(ANIGPU_P0); }
+    static FemSpace P1() { return FemSpace(ANIGPU_P1); }
+    static FemSpace P2() { return FemSpace(ANIGPU_P2); }
+    static FemSpace P3() { return FemSpace(ANIGPU_P3); }
+    /* FemVec<3, base> for base P1 or P2 */
+    static FemSpace Vec3(const FemSpace& base) {
+        if (base.space_ == ANIGPU_P1) return FemSpace(ANIGPU_VEC3_P1);
+        if (base.space_ == ANIGPU_P2) return FemSpace(ANIGPU_VEC3_P2);
+        throw std::invalid_argument("FemVec<3, .> of P1 or P2 only");
+    }
+    int space() const { return space_; }
+    ApplyOp getOP(OperatorType op) const { return ApplyOp(10 * space_ + op); }
+    /* local DOFs per tet (dofMap().NumDofsOnTet()) */
+    unsigned NumDofsOnTet() const { return getOP(IDEN).Nfa(); }
+    std::string typeName() const {
+        static const char* names[6] = {"P0", "P1", "P2", "P3", "P1^3", "P2^3"};
+        return names[space_];
+    }
+    bool operator==(const FemSpace& o) const { return space_ == o.space_; }
+
+private:
+    explicit FemSpace(int s) : space_(s) {}
+    int space_ = ANIGPU_P1;
+};
+
+/* A = int over each tet of (D OpA(u)) . OpB(v): nt element matrices, column-major nfB x nfA per
+ * tet (device arrays; XY: nt x 4 vertices x 3 coordinates). */
+inline void fem3Dtet(anigpu_handle h, int64_t nt, const double* XY, const ApplyOp& opA, const ApplyOp& opB,
+                     int tensor_kind, const double* D, void* A, int order = 5, int precision = ANIGPU_F64) {
+    check(h, anigpu_fem3dtet(h, opA.code(), opB.code(), tensor_kind, order, precision, nt, XY, D, A));
+}
+
+/* the same over face `face` of every tet (fem3Dface) or with the outward normal (fem3DfaceN) */
+inline void fem3Dface(anigpu_handle h, int64_t nt, const double* XY, int face, const ApplyOp& opA,
+                      const ApplyOp& opB, int tensor_kind, const double* D, void* A, int order = 5,
+                      int precision = ANIGPU_F64) {
+    check(h, anigpu_fem3dface(h, opA.code(), opB.code(), tensor_kind, order, precision, nt, XY, face, D, A));
+}
+inline void fem3DfaceN(anigpu_handle h, int64_t nt, const double* XY, int face, const ApplyOp& opA,
+                       const ApplyOp& opB, int tensor_kind, const double* D, void* A, int order = 5,
+                       int precision = ANIGPU_F64) {
+    check(h, anigpu_fem3dface_n(h, opA.code(), opB.code(), tensor_kind, order, precision, nt, XY, face, D, A));
+}
+
+/* Op(u) at shared barycentric points XYL[npts][4] (fem3DapplyL) or per-tet physical points
+ * X[nt][npts][3] (fem3DapplyX); dofs[nt][Nfa]; opU[nt][npts][Dim] */
+inline void fem3DapplyL(anigpu_handle h, int64_t nt, const double* XY, int npts, const double* XYL,
+                        const ApplyOp& op, const double* dofs, double* opU) {
+    check(h, anigpu_fem3d_apply(h, op.code(), nt, XY, npts, XYL, dofs, opU));
+}
+inline void fem3DapplyX(anigpu_handle h, int64_t nt, const double* XY, int npts, const double* X, const ApplyOp& op,
+                        const double* dofs, double* opU) {
+    check(h, anigpu_fem3d_apply_x(h, op.code(), nt, XY, npts, X, dofs, opU));
+}
+
+/* owning handle */
+class Context {
+public:
+    explicit Context(int device = 0) { check(nullptr, anigpu_create(&h_, device)); }
+    ~Context() {
+        if (h_) anigpu_destroy(h_);
+    }
+    Context(const Context&) = delete;
+    Context& operator=(const Context&) = delete;
+    anigpu_handle get() const { return h_; }
+
+private:
+    anigpu_handle h_ = nullptr;
+};
+
+}  // namespace anigpu
+
+#endif

@@ -141,4 +141,4 @@ class GnnOracle:
         Ae = torch.sparse.mm(self.A, e[:, None])[:, 0]
         loss = (d @ Ad) / (e @ Ae)
         loss.backward()
-        return float(loss), wt.grad.numpy().copy()
+        return float(loss.detach()), wt.grad.numpy().copy()

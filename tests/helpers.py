@@ -1,4 +1,6 @@
 """Shared helpers of the parity tests."""
+import os
+
 import numpy as np
 
 EPS = np.finfo(np.float64).eps
@@ -54,3 +56,18 @@ def parse_case(name):
 
 
 KIND_CODE = {"null": 0, "cscalar": 1, "tscalar": 2, "tsym": 3, "tgeneral": 4}
+
+
+def build_runtime_space_test(outdir):
+    """Compile tests/cpp/runtime_space.cpp against include/anigpu.hpp and the built library."""
+    import subprocess
+    import anigpu
+    repo = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    libdir = os.path.dirname(anigpu.LIB_PATH)
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    exe = os.path.join(outdir, "runtime_space")
+    cmd = ["g++", "-std=c++17", "-O1", "-I", os.path.join(repo, "include"), "-I", os.path.join(cuda, "include"),
+           os.path.join(repo, "tests", "cpp", "runtime_space.cpp"), "-o", exe, "-L", libdir, "-lanigpu",
+           f"-Wl,-rpath,{libdir}", "-L", os.path.join(cuda, "lib64"), "-lcudart", f"-Wl,-rpath,{os.path.join(cuda, 'lib64')}"]
+    subprocess.run(cmd, check=True, capture_output=True)
+    return exe

@@ -85,3 +85,15 @@ def test_config2_sizes():
     # P2 DOFs = vertices + edges of the Kuhn mesh
     ne = 3 * n * (n + 1) ** 2 + 3 * n * n * (n + 1) + n ** 3
     assert (n + 1) ** 3 + ne == 2146689
+
+
+def test_runtime_space_header_host(tmp_path):
+    """The C++ runtime-space layer (include/anigpu.hpp, mirroring Ani::FemSpace / ApplyOp):
+    operator metadata and argument errors, compiled with g++ against the library (no GPU)."""
+    import subprocess
+
+    from helpers import build_runtime_space_test
+    exe = build_runtime_space_test(str(tmp_path))
+    r = subprocess.run([exe, "host"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert "host ok" in r.stdout

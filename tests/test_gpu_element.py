@@ -200,3 +200,23 @@ def test_fem3dface_n_matches_reference(lib, golden):
         A = lib.fem3dface(ca, cb, XY, face, D, KIND_CODE[kname], order, normal=True)
         err = rel_err_per_tet(A.cpu().numpy(), golden[f"facen_{name}_A"])
         assert err <= 1e-12, (name, err)
+
+
+def test_runtime_space_layer_on_gpu(lib, golden, tmp_path):
+    """fem3Dtet / fem3Dface through the C++ runtime-space layer equal the same calls through the
+    C ABI, and an invalid face comes back as std::runtime_error."""
+    import subprocess
+
+    import anigpu
+    from helpers import build_runtime_space_test
+    exe = build_runtime_space_test(str(tmp_path))
+    XY = np.ascontiguousarray(golden["tets_XY"], dtype=np.float64)
+    nt = XY.shape[0]
+    XY.tofile(tmp_path / "xy.bin")
+    r = subprocess.run([exe, "gpu", str(tmp_path / "xy.bin"), str(tmp_path / "out.bin")], capture_output=True,
+                       text=True)
+    assert r.returncode == 0, r.stderr
+    out = np.fromfile(tmp_path / "out.bin", dtype=np.float64)
+    A = lib.fem3dtet(22, 22, XY, None, anigpu.TENSOR_NULL, 4).cpu().numpy().reshape(-1)
+    F = lib.fem3dface(1, 21, XY, 1, None, anigpu.TENSOR_NULL, 4).cpu().numpy().reshape(-1)
+    assert np.array_equal(out[:nt * 100], A) and np.array_equal(out[nt * 100:], F)
