@@ -36,6 +36,12 @@ extern "C" {
 #define ANIGPU_P3 3
 #define ANIGPU_VEC3_P1 4
 #define ANIGPU_VEC3_P2 5
+/* scalar spaces of the element level only (anifem++/fem/operators.h:26-34, spaces/*.h):
+ * Crouzeix-Raviart (4 face DOFs, 1 - 3 lambda of the opposite vertex), edge bubbles
+ * (4 lambda_i lambda_j in edge order), the volume bubble (256 lambda_0 lambda_1 lambda_2 lambda_3) */
+#define ANIGPU_CR1 6
+#define ANIGPU_B2 7
+#define ANIGPU_B4 8
 #define ANIGPU_IDEN 1
 #define ANIGPU_GRAD 2
 #define ANIGPU_OP(space, op) (10 * (space) + (op))

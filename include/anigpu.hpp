@@ -9,8 +9,8 @@
  * Order(); a FemSpace hands out its operators; the integrals run the library's batched kernels on
  * device arrays.  Errors come back as std::runtime_error, as the reference throws them.
  *
- * Spaces: P0, P1, P2, P3 and FemVec<3, P1 | P2> (component-major DOF blocks, the reference's
- * FemVec order).  Operators: IDEN, GRAD. */
+ * Spaces: P0, P1, P2, P3, CR1, B2, B4 and FemVec<3, P1 | P2> (component-major DOF blocks, the
+ * reference's FemVec order).  Operators: IDEN, GRAD. */
 #ifndef ANIGPU_HPP
 #define ANIGPU_HPP
 
@@ -37,7 +37,7 @@ public:
     ApplyOp() = default;
     explicit ApplyOp(int code) : code_(code) {
         const int space = code / 10, op = code % 10;
-        if ((op != ANIGPU_IDEN && op != ANIGPU_GRAD) || space < ANIGPU_P0 || space > ANIGPU_VEC3_P2)
+        if ((op != ANIGPU_IDEN && op != ANIGPU_GRAD) || space < ANIGPU_P0 || space > ANIGPU_B4)
             throw std::invalid_argument("unknown operator code " + std::to_string(code));
     }
     int code() const { return code_; }
@@ -47,14 +47,15 @@ public:
     unsigned base_space() const { return ncomp() == 3 ? (unsigned)space() - 3u : (unsigned)space(); }
     /* local DOFs of the operator's space (Operator::Nfa) */
     unsigned Nfa() const {
-        static const unsigned nfs[4] = {1, 4, 10, 20};
+        static const unsigned nfs[9] = {1, 4, 10, 20, 0, 0, 4, 6, 1};
         return nfs[base_space()] * ncomp();
     }
     /* rows of the operator's value at a point (Operator::Dim) */
     unsigned Dim() const { return (type() == IDEN ? 1u : 3u) * ncomp(); }
     /* polynomial order of the operator's value */
     unsigned Order() const {
-        const unsigned p = base_space();
+        static const unsigned deg[9] = {0, 1, 2, 3, 1, 2, 1, 2, 4};
+        const unsigned p = deg[space()];
         return type() == GRAD ? (p > 0 ? p - 1 : 0) : p;
     }
     bool operator==(const ApplyOp& o) const { return code_ == o.code_; }
@@ -72,6 +73,9 @@ public:
     static FemSpace P1() { return FemSpace(ANIGPU_P1); }
     static FemSpace P2() { return FemSpace(ANIGPU_P2); }
     static FemSpace P3() { return FemSpace(ANIGPU_P3); }
+    static FemSpace CR1() { return FemSpace(ANIGPU_CR1); }
+    static FemSpace B2() { return FemSpace(ANIGPU_B2); }
+    static FemSpace B4() { return FemSpace(ANIGPU_B4); }
     /* FemVec<3, base> for base P1 or P2 */
     static FemSpace Vec3(const FemSpace& base) {
         if (base.space_ == ANIGPU_P1) return FemSpace(ANIGPU_VEC3_P1);
@@ -83,7 +87,7 @@ public:
     /* local DOFs per tet (dofMap().NumDofsOnTet()) */
     unsigned NumDofsOnTet() const { return getOP(IDEN).Nfa(); }
     std::string typeName() const {
-        static const char* names[6] = {"P0", "P1", "P2", "P3", "P1^3", "P2^3"};
+        static const char* names[9] = {"P0", "P1", "P2", "P3", "P1^3", "P2^3", "CR1", "B2", "B4"};
         return names[space_];
     }
     bool operator==(const FemSpace& o) const { return space_ == o.space_; }

@@ -18,6 +18,9 @@ int scalar_space_nf(int space) {
         case ANIGPU_P1: return 4;
         case ANIGPU_P2: return 10;
         case ANIGPU_P3: return 20;
+        case ANIGPU_CR1: return 4;
+        case ANIGPU_B2: return 6;
+        case ANIGPU_B4: return 1;
     }
     return -1;
 }

@@ -8,6 +8,7 @@
 //       4 lambda_I lambda_J in edge order (0,1),(0,2),(0,3),(1,2),(1,3),(2,3)
 //   P3  anifem++/fem/spaces/poly_3.h:12-110  vertices, two DOFs per edge (same edge order),
 //       faces 27 lambda_a lambda_b lambda_c for faces {0,1,2},{1,2,3},{0,2,3},{0,1,3}
+//   CR1 crouzeix_raviart_1.h:12-80, B2 bubble_2.h:12-80, B4 bubble_4.h:11-84
 // Reference gradients are d/dxi_d with lambda_0 = 1 - xi_1 - xi_2 - xi_3, lambda_k = xi_k.
 #pragma once
 #include "anigpu.h"
@@ -70,6 +71,26 @@ ANI_HD inline int ani_eval_space(int space, const double* l, double* v, double (
                     g[16 + f][d] = 27 * (ani_dlam(a, d) * l[b] * l[c] + l[a] * ani_dlam(b, d) * l[c] + l[a] * l[b] * ani_dlam(c, d));
             }
             return 20;
+        case ANIGPU_CR1:  // crouzeix_raviart_1.h: DOF i on the face opposite vertex {3,0,1,2}[i]
+            for (int i = 0; i < 4; ++i) {
+                const int o = (i + 3) & 3;
+                v[i] = 1 - 3 * l[o];
+                for (int d = 0; d < 3; ++d) g[i][d] = -3 * ani_dlam(o, d);
+            }
+            return 4;
+        case ANIGPU_B2:  // bubble_2.h: 4 lambda_I lambda_J on edge (I,J), edge order as P2
+            for (int e = 0; e < 6; ++e) {
+                const double a = l[kEI[e]], b = l[kEJ[e]];
+                v[e] = 4 * a * b;
+                for (int d = 0; d < 3; ++d) g[e][d] = 4 * (ani_dlam(kEI[e], d) * b + ani_dlam(kEJ[e], d) * a);
+            }
+            return 6;
+        case ANIGPU_B4:  // bubble_4.h: 256 lambda_0 lambda_1 lambda_2 lambda_3
+            v[0] = 256 * l[0] * l[1] * l[2] * l[3];
+            for (int d = 0; d < 3; ++d)
+                g[0][d] = 256 * (ani_dlam(0, d) * l[1] * l[2] * l[3] + ani_dlam(1, d) * l[0] * l[2] * l[3] +
+                                 ani_dlam(2, d) * l[0] * l[1] * l[3] + ani_dlam(3, d) * l[0] * l[1] * l[2]);
+            return 1;
     }
     return -1;
 }

@@ -78,13 +78,33 @@ static int scalar_basis(int space, const double* l, double* val, double (*g)[3])
                     g[16 + i][d] = 27 * (dl(a, d) * s2 * s3 + s1 * dl(b, d) * s3 + s1 * s2 * dl(c, d));
             }
             return 20;
+        case 6: /* CR1: crouzeix_raviart_1.h:34-38 (IPF3 = {3,0,1,2}), :68-80 */
+            for (i = 0; i < 4; ++i) {
+                int o = (i + 3) % 4;
+                val[i] = 1 - 3 * l[o];
+                for (d = 0; d < 3; ++d) g[i][d] = -3 * dl(o, d);
+            }
+            return 4;
+        case 7: /* B2: bubble_2.h:34-38 */
+            for (e = 0; e < 6; ++e) {
+                double a = l[EI[e]], b = l[EJ[e]];
+                val[e] = 4 * a * b;
+                for (d = 0; d < 3; ++d) g[e][d] = 4 * (dl(EI[e], d) * b + dl(EJ[e], d) * a);
+            }
+            return 6;
+        case 8: /* B4: bubble_4.h:30-34, :65-75 */
+            val[0] = 256 * l[0] * l[1] * l[2] * l[3];
+            for (d = 0; d < 3; ++d)
+                g[0][d] = 256 * (dl(0, d) * l[1] * l[2] * l[3] + dl(1, d) * l[0] * l[2] * l[3] +
+                                 dl(2, d) * l[0] * l[1] * l[3] + dl(3, d) * l[0] * l[1] * l[2]);
+            return 1;
     }
     return -1;
 }
 
 static int scalar_nf(int space) {
-    static const int nf[4] = {1, 4, 10, 20};
-    return (space >= 0 && space < 4) ? nf[space] : -1;
+    static const int nf[9] = {1, 4, 10, 20, -1, -1, 4, 6, 1};
+    return (space >= 0 && space < 9) ? nf[space] : -1;
 }
 
 int orc_op_info(int code, int* nf, int* dim) {

@@ -148,6 +148,9 @@ int run(const Req& r) {
 #define P3 FemFix<FEM_P3>
 #define V1 FemVec<3, FEM_P1>
 #define V2 FemVec<3, FEM_P2>
+#define CR FemFix<FEM_CR1>
+#define BB2 FemFix<FEM_B2>
+#define BB4 FemFix<FEM_B4>
 
 // Ani::fem3DapplyL (eval.inl:93-111) for phys == 0: npts shared barycentric points [npts][4];
 // Ani::fem3DapplyX (eval.inl:103-125) for phys == 1: per-tet physical points [nt][npts][3].
@@ -204,6 +207,18 @@ int ref_fem3dtet(int codeA, int codeB, int kind, int order, long nt, const doubl
         PAIR(22, 12, G2, G1)
         PAIR(22, 21, G2, I2)
         PAIR(12, 11, G1, I1)
+        using ICR = Operator<IDEN, CR>; using GCR = Operator<GRAD, CR>;
+        using IB2 = Operator<IDEN, BB2>; using GB2 = Operator<GRAD, BB2>;
+        using IB4 = Operator<IDEN, BB4>; using GB4 = Operator<GRAD, BB4>;
+        PAIR(61, 61, ICR, ICR)
+        PAIR(62, 62, GCR, GCR)
+        PAIR(1, 61, I0, ICR)
+        PAIR(71, 71, IB2, IB2)
+        PAIR(72, 72, GB2, GB2)
+        PAIR(81, 81, IB4, IB4)
+        PAIR(82, 82, GB4, GB4)
+        PAIR(11, 81, I1, IB4)
+        PAIR(81, 11, IB4, I1)
 #undef PAIR
     } catch (const std::exception&) {
         return -2;
@@ -230,6 +245,15 @@ int ref_fem3d_apply(int code, long nt, const double* XY, int npts, const double*
         OP(42, GV1)
         OP(51, IV2)
         OP(52, GV2)
+        using ICR = Operator<IDEN, CR>; using GCR = Operator<GRAD, CR>;
+        using IB2 = Operator<IDEN, BB2>; using GB2 = Operator<GRAD, BB2>;
+        using IB4 = Operator<IDEN, BB4>; using GB4 = Operator<GRAD, BB4>;
+        OP(61, ICR)
+        OP(62, GCR)
+        OP(71, IB2)
+        OP(72, GB2)
+        OP(81, IB4)
+        OP(82, GB4)
 #undef OP
     } catch (const std::exception&) {
         return -2;

@@ -33,7 +33,7 @@ from oracle.oracle import Reference  # noqa: E402
 from anigpu import meshgen  # noqa: E402
 
 # operator codes: 10*space + op (space 0 P0, 1 P1, 2 P2, 3 P3, 4 Vec3P1, 5 Vec3P2; op 1 IDEN, 2 GRAD)
-NF = {0: 1, 1: 4, 2: 10, 3: 20, 4: 12, 5: 30}
+NF = {0: 1, 1: 4, 2: 10, 3: 20, 4: 12, 5: 30, 6: 4, 7: 6, 8: 1}
 DIM = {1: 1, 2: 3}
 
 
@@ -100,7 +100,8 @@ def main():
     scalar_tet = np.exp(meshgen.normal(21, nt))
     sym6 = meshgen.aniso_tensors(nt, sigma=1.0, seed=22)
     for (ca, cb) in [(12, 12), (22, 22), (32, 32), (42, 42), (52, 52), (32, 42), (11, 11), (21, 21), (31, 31),
-                     (1, 11), (1, 21), (1, 51), (12, 22), (22, 12)]:
+                     (1, 11), (1, 21), (1, 51), (12, 22), (22, 12),
+                     (61, 61), (62, 62), (1, 61), (71, 71), (72, 72), (81, 81), (82, 82), (11, 81), (81, 11)]:
         nfA, dA = op_nf_dim(ca)
         nfB, dB = op_nf_dim(cb)
         kinds = []
@@ -131,7 +132,7 @@ def main():
     p4, _ = R.quadrature(4)
     out["apply_XYL"] = p4
     out["apply_X"] = meshgen.uniform(41, nt * 7 * 3).reshape(nt, 7, 3) * 3.0 - 1.0
-    apply_codes = [1, 11, 12, 21, 22, 31, 32, 41, 42, 51, 52]
+    apply_codes = [1, 11, 12, 21, 22, 31, 32, 41, 42, 51, 52, 61, 62, 71, 72, 81, 82]
     for code in apply_codes:
         nf, dim = op_nf_dim(code)
         dofs = meshgen.normal(50 + code, nt * nf).reshape(nt, nf)

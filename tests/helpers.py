@@ -21,7 +21,7 @@ def rel_err_per_tet(A, B):
     return float(np.max(np.linalg.norm(A - B, axis=1) / nb))
 
 
-NF = {0: 1, 1: 4, 2: 10, 3: 20, 4: 12, 5: 30}
+NF = {0: 1, 1: 4, 2: 10, 3: 20, 4: 12, 5: 30, 6: 4, 7: 6, 8: 1}
 DIM = {1: 1, 2: 3}
 
 
