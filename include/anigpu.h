@@ -42,6 +42,14 @@ extern "C" {
 #define ANIGPU_CR1 6
 #define ANIGPU_B2 7
 #define ANIGPU_B4 8
+/* vector-valued lowest-order spaces of the element level (spaces/nedelec_0.h, raviant_thomas_0.h):
+ * Nedelec ND0 (6 edge DOFs; IDEN dim 3, CURL dim 3, GRAD dim 9 = the skew part curl/2, DIV = 0) and
+ * Raviart-Thomas RT0 (4 face DOFs; IDEN dim 3, DIV dim 1, GRAD dim 9, CURL = 0).  Their operator
+ * codes use the reference's DIV = 3 and CURL = 4: 10*space + op, e.g. ANIGPU_OP(ANIGPU_RT0, ANIGPU_DIV). */
+#define ANIGPU_ND0 9
+#define ANIGPU_RT0 10
+#define ANIGPU_DIV 3
+#define ANIGPU_CURL 4
 #define ANIGPU_IDEN 1
 #define ANIGPU_GRAD 2
 #define ANIGPU_OP(space, op) (10 * (space) + (op))

@@ -9,8 +9,8 @@
  * Order(); a FemSpace hands out its operators; the integrals run the library's batched kernels on
  * device arrays.  Errors come back as std::runtime_error, as the reference throws them.
  *
- * Spaces: P0, P1, P2, P3, CR1, B2, B4 and FemVec<3, P1 | P2> (component-major DOF blocks, the
- * reference's FemVec order).  Operators: IDEN, GRAD. */
+ * Spaces: P0, P1, P2, P3, CR1, B2, B4, ND0, RT0 and FemVec<3, P1 | P2> (component-major DOF
+ * blocks, the reference's FemVec order).  Operators: IDEN, GRAD; DIV and CURL for ND0 / RT0. */
 #ifndef ANIGPU_HPP
 #define ANIGPU_HPP
 
@@ -22,7 +22,7 @@
 
 namespace anigpu {
 
-enum OperatorType { IDEN = ANIGPU_IDEN, GRAD = ANIGPU_GRAD };
+enum OperatorType { IDEN = ANIGPU_IDEN, GRAD = ANIGPU_GRAD, DIV = ANIGPU_DIV, CURL = ANIGPU_CURL };
 
 inline void check(anigpu_handle h, int rc) {
     if (rc != ANIGPU_OK) {
@@ -37,8 +37,10 @@ public:
     ApplyOp() = default;
     explicit ApplyOp(int code) : code_(code) {
         const int space = code / 10, op = code % 10;
-        if ((op != ANIGPU_IDEN && op != ANIGPU_GRAD) || space < ANIGPU_P0 || space > ANIGPU_B4)
-            throw std::invalid_argument("unknown operator code " + std::to_string(code));
+        const bool vec = space == ANIGPU_ND0 || space == ANIGPU_RT0;
+        const bool ok = vec ? (op >= ANIGPU_IDEN && op <= ANIGPU_CURL)
+                            : ((op == ANIGPU_IDEN || op == ANIGPU_GRAD) && space >= ANIGPU_P0 && space <= ANIGPU_B4);
+        if (!ok) throw std::invalid_argument("unknown operator code " + std::to_string(code));
     }
     int code() const { return code_; }
     int space() const { return code_ / 10; }
@@ -46,17 +48,24 @@ public:
     unsigned ncomp() const { return space() == ANIGPU_VEC3_P1 || space() == ANIGPU_VEC3_P2 ? 3u : 1u; }
     unsigned base_space() const { return ncomp() == 3 ? (unsigned)space() - 3u : (unsigned)space(); }
     /* local DOFs of the operator's space (Operator::Nfa) */
+    bool vector_valued() const { return space() == ANIGPU_ND0 || space() == ANIGPU_RT0; }
     unsigned Nfa() const {
-        static const unsigned nfs[9] = {1, 4, 10, 20, 0, 0, 4, 6, 1};
+        static const unsigned nfs[11] = {1, 4, 10, 20, 0, 0, 4, 6, 1, 6, 4};
         return nfs[base_space()] * ncomp();
     }
     /* rows of the operator's value at a point (Operator::Dim) */
-    unsigned Dim() const { return (type() == IDEN ? 1u : 3u) * ncomp(); }
+    unsigned Dim() const {
+        if (vector_valued()) {
+            static const unsigned dims[5] = {0, 3, 9, 1, 3};
+            return dims[type()];
+        }
+        return (type() == IDEN ? 1u : 3u) * ncomp();
+    }
     /* polynomial order of the operator's value */
     unsigned Order() const {
-        static const unsigned deg[9] = {0, 1, 2, 3, 1, 2, 1, 2, 4};
+        static const unsigned deg[11] = {0, 1, 2, 3, 1, 2, 1, 2, 4, 1, 1};
         const unsigned p = deg[space()];
-        return type() == GRAD ? (p > 0 ? p - 1 : 0) : p;
+        return type() == IDEN ? p : (p > 0 ? p - 1 : 0);
     }
     bool operator==(const ApplyOp& o) const { return code_ == o.code_; }
     bool operator!=(const ApplyOp& o) const { return code_ != o.code_; }
@@ -76,6 +85,8 @@ public:
     static FemSpace CR1() { return FemSpace(ANIGPU_CR1); }
     static FemSpace B2() { return FemSpace(ANIGPU_B2); }
     static FemSpace B4() { return FemSpace(ANIGPU_B4); }
+    static FemSpace ND0() { return FemSpace(ANIGPU_ND0); }
+    static FemSpace RT0() { return FemSpace(ANIGPU_RT0); }
     /* FemVec<3, base> for base P1 or P2 */
     static FemSpace Vec3(const FemSpace& base) {
         if (base.space_ == ANIGPU_P1) return FemSpace(ANIGPU_VEC3_P1);
@@ -87,7 +98,7 @@ public:
     /* local DOFs per tet (dofMap().NumDofsOnTet()) */
     unsigned NumDofsOnTet() const { return getOP(IDEN).Nfa(); }
     std::string typeName() const {
-        static const char* names[9] = {"P0", "P1", "P2", "P3", "P1^3", "P2^3", "CR1", "B2", "B4"};
+        static const char* names[11] = {"P0", "P1", "P2", "P3", "P1^3", "P2^3", "CR1", "B2", "B4", "ND0", "RT0"};
         return names[space_];
     }
     bool operator==(const FemSpace& o) const { return space_ == o.space_; }

@@ -23,6 +23,8 @@ ERR_NONFINITE, ERR_BAD_ELEMENT, ERR_ARG, ERR_UNSUPPORTED, ERR_CUDA, ERR_NOT_CONV
     -1, -2, -3, -4, -5, -6, -7, -8)
 P0, P1, P2, P3, VEC3_P1, VEC3_P2 = 0, 1, 2, 3, 4, 5
 CR1, B2, B4 = 6, 7, 8  # element level only
+ND0, RT0 = 9, 10        # vector-valued, element level only
+DIV, CURL = 3, 4
 IDEN, GRAD = 1, 2
 # GlobEnumeration::ASSEMBLING_TYPE (global_enumerator.h:392-404)
 ENUM_ANITYPE, ENUM_MINIBLOCKS, ENUM_NATURAL, ENUM_DIMUNION, ENUM_BYELEMTYPE, ENUM_ETDIMBLOCKS = 0, 1, 2, 3, 4, 5
@@ -129,6 +131,8 @@ class AnigpuError(RuntimeError):
 def op_info(code):
     """(nf, dim) of operator code 10*space + op (Operator<OP, FEM>::Nfa / Dim)."""
     space, op = divmod(code, 10)
+    if space in (ND0, RT0):
+        return (6 if space == ND0 else 4), {IDEN: 3, GRAD: 9, DIV: 1, CURL: 3}[op]
     nfs = {P0: 1, P1: 4, P2: 10, P3: 20, VEC3_P1: 4, VEC3_P2: 10, CR1: 4, B2: 6, B4: 1}[space]
     nc = 3 if space in (VEC3_P1, VEC3_P2) else 1
     bd = 1 if op == IDEN else 3

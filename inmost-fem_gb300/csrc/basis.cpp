@@ -27,6 +27,16 @@ int scalar_space_nf(int space) {
 
 bool op_info(int code, int* nf, int* dim, int* base_space, int* ncomp, int* op) {
     const int space = code / 10, o = code % 10;
+    if (space == ANIGPU_ND0 || space == ANIGPU_RT0) {  // vector-valued: IDEN, GRAD, DIV, CURL
+        if (o < ANIGPU_IDEN || o > ANIGPU_CURL) return false;
+        static const int dims[5] = {0, 3, 9, 1, 3};
+        *nf = space == ANIGPU_ND0 ? 6 : 4;
+        *dim = dims[o];
+        *base_space = space;
+        *ncomp = 1;
+        *op = o;
+        return true;
+    }
     if (o != ANIGPU_IDEN && o != ANIGPU_GRAD) return false;
     int base = space, nc = 1;
     if (space == ANIGPU_VEC3_P1 || space == ANIGPU_VEC3_P2) {

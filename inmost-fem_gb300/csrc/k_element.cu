@@ -21,8 +21,10 @@ constexpr int kThreads = 128;
 constexpr int kMaxOwned = (ANIGPU_MAX_NF * ANIGPU_MAX_NF + kThreads - 1) / kThreads;  // 8
 
 struct OpDesc {
-    int nf, dim, nfs, bd, ncomp, op;  // op: 1 IDEN, 2 GRAD
-    const double* tab;                // device basis table (vals q*nfs, grads q*nfs*3)
+    int nf, dim, nfs, bd, ncomp, op;  // op: 1 IDEN, 2 GRAD, 3 DIV, 4 CURL
+    int space;                        // base space; ND0 / RT0 are evaluated from the tet geometry
+    int tnf;                          // functions in the table: nfs, or 4 (the P1 table: lambda) for ND0 / RT0
+    const double* tab;                // device basis table (vals q*tnf, grads q*tnf*3)
 };
 
 struct ElemParams {
@@ -95,7 +97,7 @@ __device__ inline double face_area(const double* X, int face) {
     return sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]) / 2;
 }
 
-__device__ inline void tet_geometry(const double* X, double* PSI, double* mes) {
+__device__ inline void tet_geometry(const double* X, double* PSI, double* mes, double* det_out = nullptr) {
     // internalFem3DtetGeomInit_Tet (core.inl:217-247) with inverse3x3 (geometry.h:26-44)
     double m[9];
 #pragma unroll
@@ -118,17 +120,24 @@ __device__ inline void tet_geometry(const double* X, double* PSI, double* mes) {
                               M((i + 1) % 3, (j + 2) % 3) * M((i + 2) % 3, (j + 1) % 3)) / det;
 #undef M
     *mes = fabs(det) / 6.0;
+    if (det_out) *det_out = det;
 }
 
 // value of operator `o` for column `col`, row `k` at point n (block structure of FemVec,
 // operators.h:127-155: component c owns rows [c*bd,(c+1)*bd) and columns [c*nfs,(c+1)*nfs))
+// geo: PSI[9], mes, normal[3], vertex coordinates relative to X0 [12] (from 13), signed det (25)
 template <typename Real>
-__device__ inline Real op_value(const OpDesc& o, const double* tab, int q, int n, int k, int col, const double* PSI) {
+__device__ inline Real op_value(const OpDesc& o, const double* tab, int q, int n, int k, int col, const double* geo) {
+    const double* PSI = geo;
+    if (o.space == ANIGPU_ND0 || o.space == ANIGPU_RT0) {
+        const double* l = tab + (size_t)n * 4;  // P1 table values = barycentric coordinates
+        return Real(ani_vec_space_value(o.space, o.op, l, PSI, geo + 13, geo[25], col, k));
+    }
     const int c = col / o.nfs, i = col - c * o.nfs;
     const int kc = k / o.bd, kk = k - kc * o.bd;
     if (kc != c) return Real(0);
-    if (o.op == ANIGPU_IDEN) return Real(tab[n * o.nfs + i]);
-    const double* g = tab + (size_t)q * o.nfs + 3 * ((size_t)n * o.nfs + i);
+    if (o.op == ANIGPU_IDEN) return Real(tab[n * o.tnf + i]);
+    const double* g = tab + (size_t)q * o.tnf + 3 * ((size_t)n * o.tnf + i);
     // U_k = sum_j PSI(j,k) ghat_j (poly_2.h:91-97)
     return Real(PSI[0 + 3 * kk] * g[0] + PSI[1 + 3 * kk] * g[1] + PSI[2 + 3 * kk] * g[2]);
 }
@@ -139,12 +148,12 @@ __global__ void __launch_bounds__(kThreads) fem3dtet_kernel(ElemParams p, int64_
     extern __shared__ double smem[];
     const int q = p.q;
     const int nfA = p.A.nf, nfB = p.B.nf, dA = p.A.dim, dB = p.B.dim;
-    const size_t tabA = (size_t)q * p.A.nfs * 4, tabB = (size_t)q * p.B.nfs * 4;
+    const size_t tabA = (size_t)q * p.A.tnf * 4, tabB = (size_t)q * p.B.tnf * 4;
     double* sTabA = smem;
     double* sTabB = sTabA + tabA;
     double* sW = sTabB + tabB;
-    double* sGeo = sW + q;              // PSI[9], mes, outward normal[3]
-    double* sD = sGeo + 13;             // dB*dA
+    double* sGeo = sW + q;              // PSI[9], mes, outward normal[3], XYP[12], det
+    double* sD = sGeo + 26;             // dB*dA
     Real* sU = reinterpret_cast<Real*>(sD + ANIGPU_MAX_DIM * ANIGPU_MAX_DIM);
     Real* sV = sU + dA * nfA;
     Real* sDU = sV + dB * nfB;
@@ -156,7 +165,10 @@ __global__ void __launch_bounds__(kThreads) fem3dtet_kernel(ElemParams p, int64_
     for (int64_t t = blockIdx.x; t < nt; t += gridDim.x) {
         __syncthreads();
         if (threadIdx.x == 0) {
-            tet_geometry(XY + 12 * t, sGeo, sGeo + 9);
+            const double* X = XY + 12 * t;
+            tet_geometry(X, sGeo, sGeo + 9, sGeo + 25);
+            for (int v = 0; v < 4; ++v)
+                for (int i = 0; i < 3; ++i) sGeo[13 + 3 * v + i] = v == 0 ? 0.0 : X[3 * v + i] - X[i];
             if (p.normal) sGeo[9] = face_normal(XY + 12 * t, p.face, sGeo + 10);
             else if (p.face >= 0) sGeo[9] = face_area(XY + 12 * t, p.face);
         }
@@ -287,8 +299,8 @@ __global__ void __launch_bounds__(128) fem3d_apply_kernel(ApplyParams p, int64_t
             for (int i = 0; i < 3; ++i) X[3 * v + i] = p.xyz[3 * node + i];
         }
     }
-    double PSI[9], mes;
-    tet_geometry(X, PSI, &mes);
+    double PSI[9], mes, det;
+    tet_geometry(X, PSI, &mes, &det);
     double l[4];
     if (p.phys) {
         const double* x = p.pts + 3 * idx;
@@ -303,9 +315,25 @@ __global__ void __launch_bounds__(128) fem3d_apply_kernel(ApplyParams p, int64_t
 #pragma unroll
         for (int k = 0; k < 4; ++k) l[k] = p.pts[4 * n + k];
     }
+    double* o = p.out + idx * p.dim;
+    if (p.base == ANIGPU_ND0 || p.base == ANIGPU_RT0) {  // vector-valued, from the tet geometry
+        double P[12];
+#pragma unroll
+        for (int v = 0; v < 4; ++v)
+#pragma unroll
+            for (int i = 0; i < 3; ++i) P[3 * v + i] = v == 0 ? 0.0 : X[3 * v + i] - X[i];
+        for (int k = 0; k < p.dim; ++k) {
+            double s = 0.0;
+            for (int i = 0; i < p.nf; ++i) {
+                const double d = p.dofs ? p.dofs[(int64_t)p.nf * t + i] : p.x[p.edofs[(int64_t)p.nloc * t + i]];
+                s += ani_vec_space_value(p.base, p.op, l, PSI, P, det, i, k) * d;
+            }
+            o[k] = s;
+        }
+        return;
+    }
     double v[20], g[20][3];
     ani_eval_space(p.base, l, v, g);
-    double* o = p.out + idx * p.dim;
     for (int c = 0; c < p.ncomp; ++c) {
         double s[3] = {0.0, 0.0, 0.0};
         for (int i = 0; i < p.nfs; ++i) {
@@ -372,22 +400,23 @@ int launch_fem3dtet(anigpu_ctx* h, int opA, int opB, int kind, int order, int pr
     if (!XY || !A) return set_err(h, ANIGPU_ERR_ARG, "NULL coordinates or output");
     const double *tA, *tB;
     ScalarBasisTable hA;
+    const bool vecA = bsA == ANIGPU_ND0 || bsA == ANIGPU_RT0, vecB = bsB == ANIGPU_ND0 || bsB == ANIGPU_RT0;
     if (face > 3) return set_err(h, ANIGPU_ERR_ARG, "face number must be 0..3");
-    int rc = get_basis_dev(h, bsA, order, &tA, &hA, face);
+    int rc = get_basis_dev(h, vecA ? ANIGPU_P1 : bsA, order, &tA, &hA, face);
     if (rc) return rc;
-    rc = get_basis_dev(h, bsB, order, &tB, nullptr, face);
+    rc = get_basis_dev(h, vecB ? ANIGPU_P1 : bsB, order, &tB, nullptr, face);
     if (rc) return rc;
     ElemParams p;
-    p.A = {nfA, dA, nfA / ncA, dA / ncA, ncA, oA, tA};
-    p.B = {nfB, dB, nfB / ncB, dB / ncB, ncB, oB, tB};
+    p.A = {nfA, dA, nfA / ncA, dA / ncA, ncA, oA, bsA, vecA ? 4 : nfA / ncA, tA};
+    p.B = {nfB, dB, nfB / ncB, dB / ncB, ncB, oB, bsB, vecB ? 4 : nfB / ncB, tB};
     p.q = hA.q;
     p.kind = kind;
     p.face = face;
     p.normal = normal ? 1 : 0;
     p.w = tA + (size_t)hA.q * hA.nf * 4;
-    const size_t tabs = (size_t)p.q * (p.A.nfs + p.B.nfs) * 4;
+    const size_t tabs = (size_t)p.q * (p.A.tnf + p.B.tnf) * 4;
     const size_t rsz = precision == ANIGPU_F32 ? sizeof(float) : sizeof(double);
-    const size_t smem = sizeof(double) * (tabs + p.q + 13 + ANIGPU_MAX_DIM * ANIGPU_MAX_DIM) +
+    const size_t smem = sizeof(double) * (tabs + p.q + 26 + ANIGPU_MAX_DIM * ANIGPU_MAX_DIM) +
                         rsz * (size_t)(dA * nfA + dB * nfB + dB * nfA);
     int dev_sms = 148;
     cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, h->device);

@@ -109,6 +109,13 @@ static int scalar_nf(int space) {
 
 int orc_op_info(int code, int* nf, int* dim) {
     int space = code / 10, op = code % 10;
+    if (space == 9 || space == 10) { /* ND0 / RT0: IDEN 3, GRAD 9, DIV 1, CURL 3 */
+        static const int dims[5] = {0, 3, 9, 1, 3};
+        if (op < 1 || op > 4) return -1;
+        *nf = space == 9 ? 6 : 4;
+        *dim = dims[op];
+        return 0;
+    }
     int vec = (space == 4 || space == 5), base = vec ? space - 3 : space;
     int n = scalar_nf(base);
     if (n < 0 || (op != 1 && op != 2)) return -1;
@@ -118,10 +125,92 @@ int orc_op_info(int code, int* nf, int* dim) {
     return 0;
 }
 
+/* (a - c) x (b - c) (geometry.h:57-64) */
+static void cross3(const double* a, const double* b, const double* c, double* r) {
+    double u[3] = {a[0] - c[0], a[1] - c[1], a[2] - c[2]}, v[3] = {b[0] - c[0], b[1] - c[1], b[2] - c[2]};
+    r[0] = u[1] * v[2] - u[2] * v[1];
+    r[1] = -u[0] * v[2] + u[2] * v[0];
+    r[2] = u[0] * v[1] - u[1] * v[0];
+}
+
+/* physical gradient of lambda_v, component k: sum_m GRAD_P1(m, v) PSI(m, k) */
+static double glam(const double* PSI, int v, int k) {
+    return dl(v, 0) * PSI[0 + 3 * k] + dl(v, 1) * PSI[1 + 3 * k] + dl(v, 2) * PSI[2 + 3 * k];
+}
+
+/* ND0 (spaces/nedelec_0.h:12-183) and RT0 (spaces/raviant_thomas_0.h:12-190) at one point,
+ * U[k + dim*i]; P = vertex coordinates relative to X0 (the reference's XYP), det signed */
+static void apply_vec_space(int space, int op, const double* l, const double* PSI, const double* P, double det,
+                            double* U) {
+    static const int IPR[24] = {0, 1, 2, 3, 0, 2, 3, 1, 0, 3, 1, 2, 1, 2, 0, 3, 1, 3, 2, 0, 2, 3, 0, 1};
+    static const int IPF[16] = {0, 1, 2, 3, 1, 2, 3, 0, 0, 2, 3, 1, 0, 1, 3, 2};
+    int dim, nf;
+    orc_op_info(10 * space + op, &nf, &dim);
+    for (int i = 0; i < nf; ++i) {
+        double* u = U + dim * i;
+        if (space == 9) {
+            const int* ip = IPR + 4 * i;
+            double sq = 0, xn[3], xm[3], curl[3];
+            for (int k = 0; k < 3; ++k) sq += (P[3 * ip[0] + k] - P[3 * ip[1] + k]) * (P[3 * ip[0] + k] - P[3 * ip[1] + k]);
+            double s = sqrt(sq) / det;
+            cross3(P + 3 * ip[2], P + 3 * ip[3], P + 3 * ip[0], xn);
+            cross3(P + 3 * ip[2], P + 3 * ip[3], P + 3 * ip[1], xm);
+            for (int k = 0; k < 3; ++k) {
+                int k1 = (k + 1) % 3, k2 = (k + 2) % 3;
+                curl[k] = s * ((glam(PSI, ip[0], k1) * xn[k2] + glam(PSI, ip[1], k1) * xm[k2]) -
+                               (glam(PSI, ip[0], k2) * xn[k1] + glam(PSI, ip[1], k2) * xm[k1]));
+            }
+            if (op == 1)
+                for (int k = 0; k < 3; ++k) u[k] = s * (xn[k] * l[ip[0]] + xm[k] * l[ip[1]]);
+            else if (op == 3)
+                u[0] = 0;
+            else if (op == 4)
+                for (int k = 0; k < 3; ++k) u[k] = curl[k];
+            else { /* GRAD: nedelec_0.h:172-177 */
+                double a0 = curl[0] / 2, a1 = curl[1] / 2, a2 = curl[2] / 2;
+                u[0] = 0; u[3] = a2;  u[6] = -a1;
+                u[1] = -a2; u[4] = 0; u[7] = a0;
+                u[2] = a1; u[5] = -a0; u[8] = 0;
+            }
+        } else {
+            const int* ip = IPF + 4 * i;
+            double cr[3];
+            cross3(P + 3 * ip[0], P + 3 * ip[1], P + 3 * ip[2], cr);
+            double s = (sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]) / 2) / (fabs(det) / 2);
+            if (op == 1) {
+                for (int j = 0; j < 3; ++j) {
+                    double v = 0;
+                    for (int a = 0; a < 3; ++a) v += l[ip[a]] * (P[3 * ip[a] + j] - P[3 * ip[3] + j]);
+                    u[j] = s * v;
+                }
+            } else if (op == 4) {
+                for (int k = 0; k < 3; ++k) u[k] = 0;
+            } else if (op == 2) {
+                for (int j = 0; j < 3; ++j)
+                    for (int k = 0; k < 3; ++k) {
+                        double v = 0;
+                        for (int a = 0; a < 3; ++a) v += glam(PSI, ip[a], k) * (P[3 * ip[a] + j] - P[3 * ip[3] + j]);
+                        u[k + 3 * j] = s * v;
+                    }
+            } else {
+                double v = 0;
+                for (int j = 0; j < 3; ++j)
+                    for (int a = 0; a < 3; ++a) v += glam(PSI, ip[a], j) * (P[3 * ip[a] + j] - P[3 * ip[3] + j]);
+                u[0] = s * v;
+            }
+        }
+    }
+}
+
 /* Operator application at one point: U[k + dim*i] (operators.h:127-155 for FemVec:
- * component c occupies rows [c*bdim, (c+1)*bdim) and columns [c*nfs, (c+1)*nfs)). */
-static void apply_op(int code, const double* l, const double* PSI, double* U) {
+ * component c occupies rows [c*bdim, (c+1)*bdim) and columns [c*nfs, (c+1)*nfs)).
+ * P (relative vertex coordinates) and det serve the geometry-dependent ND0 / RT0. */
+static void apply_op(int code, const double* l, const double* PSI, const double* P, double det, double* U) {
     int space = code / 10, op = code % 10;
+    if (space == 9 || space == 10) {
+        apply_vec_space(space, op, l, PSI, P, det, U);
+        return;
+    }
     int vec = (space == 4 || space == 5), base = vec ? space - 3 : space;
     double val[20], g[20][3];
     int nfs = scalar_basis(base, l, val, g);
@@ -335,16 +424,18 @@ static int elem_core(int codeA, int codeB, int kind, const double* pp, const dou
     double U[MAXDIM * MAXNF], V[MAXDIM * MAXNF], Dm[MAXDIM * MAXDIM], DU[MAXDIM * MAXNF];
     double Dfull[3 * MAXDIM * MAXDIM];
     for (long t = 0; t < nt; ++t) {
-        double PSI[9], mes, nrm[3];
-        tet_geom(XY + 12 * t, PSI, &mes);
+        double PSI[9], mes, nrm[3], P[12];
+        double det = tet_geom(XY + 12 * t, PSI, &mes);
+        for (int v = 0; v < 4; ++v)
+            for (int i = 0; i < 3; ++i) P[3 * v + i] = v == 0 ? 0.0 : XY[12 * t + 3 * v + i] - XY[12 * t + i];
         if (normal) mes = face_normal(XY + 12 * t, face, nrm);
         else if (face >= 0) mes = face_area(XY + 12 * t, face);
         double* At = A + (size_t)t * nfA * nfB;
         memset(At, 0, sizeof(double) * nfA * nfB);
         for (int n = 0; n < q; ++n) {
             const double* l = pp + 4 * n;
-            apply_op(codeA, l, PSI, U); /* l = (lambda_0..lambda_3) as tabulated (int_tet.inl:116-121) */
-            apply_op(codeB, l, PSI, V);
+            apply_op(codeA, l, PSI, P, det, U); /* l = (lambda_0..lambda_3) as tabulated (int_tet.inl:116-121) */
+            apply_op(codeB, l, PSI, P, det, V);
             const double* src = NULL;
             switch (kind) {
                 case ORC_CONST_SCALAR: src = D; break;
@@ -450,8 +541,10 @@ int orc_fem3d_apply(int code, long nt, const double* XY, int npts, const double*
     double U[MAXDIM * MAXNF];
     for (long t = 0; t < nt; ++t) {
         const double* X = XY + 12 * t;
-        double PSI[9], mes;
-        tet_geom(X, PSI, &mes);
+        double PSI[9], mes, P[12];
+        double det = tet_geom(X, PSI, &mes);
+        for (int v = 0; v < 4; ++v)
+            for (int i = 0; i < 3; ++i) P[3 * v + i] = v == 0 ? 0.0 : X[3 * v + i] - X[i];
         for (int n = 0; n < npts; ++n) {
             double l[4];
             if (phys) {
@@ -464,7 +557,7 @@ int orc_fem3d_apply(int code, long nt, const double* XY, int npts, const double*
             } else {
                 for (int k = 0; k < 4; ++k) l[k] = pts[4 * n + k];
             }
-            apply_op(code, l, PSI, U);
+            apply_op(code, l, PSI, P, det, U);
             for (int k = 0; k < dim; ++k) {
                 double s = 0;
                 for (int i = 0; i < nf; ++i) s += U[k + dim * i] * dofs[(size_t)nf * t + i];

@@ -151,6 +151,8 @@ int run(const Req& r) {
 #define CR FemFix<FEM_CR1>
 #define BB2 FemFix<FEM_B2>
 #define BB4 FemFix<FEM_B4>
+#define ND FemFix<FEM_ND0>
+#define RT FemFix<FEM_RT0>
 
 // Ani::fem3DapplyL (eval.inl:93-111) for phys == 0: npts shared barycentric points [npts][4];
 // Ani::fem3DapplyX (eval.inl:103-125) for phys == 1: per-tet physical points [nt][npts][3].
@@ -219,6 +221,16 @@ int ref_fem3dtet(int codeA, int codeB, int kind, int order, long nt, const doubl
         PAIR(82, 82, GB4, GB4)
         PAIR(11, 81, I1, IB4)
         PAIR(81, 11, IB4, I1)
+        using IND = Operator<IDEN, ND>; using CND = Operator<CURL, ND>; using GND = Operator<GRAD, ND>;
+        using IRT = Operator<IDEN, RT>; using DRT = Operator<DIV, RT>; using GRT = Operator<GRAD, RT>;
+        PAIR(91, 91, IND, IND)
+        PAIR(94, 94, CND, CND)
+        PAIR(92, 92, GND, GND)
+        PAIR(101, 101, IRT, IRT)
+        PAIR(103, 103, DRT, DRT)
+        PAIR(102, 102, GRT, GRT)
+        PAIR(103, 1, DRT, I0)
+        PAIR(91, 101, IND, IRT)
 #undef PAIR
     } catch (const std::exception&) {
         return -2;
@@ -254,6 +266,18 @@ int ref_fem3d_apply(int code, long nt, const double* XY, int npts, const double*
         OP(72, GB2)
         OP(81, IB4)
         OP(82, GB4)
+        using IND = Operator<IDEN, ND>; using CND = Operator<CURL, ND>; using GND = Operator<GRAD, ND>;
+        using DND = Operator<DIV, ND>;
+        using IRT = Operator<IDEN, RT>; using DRT = Operator<DIV, RT>; using GRT = Operator<GRAD, RT>;
+        using CRT = Operator<CURL, RT>;
+        OP(91, IND)
+        OP(92, GND)
+        OP(93, DND)
+        OP(94, CND)
+        OP(101, IRT)
+        OP(102, GRT)
+        OP(103, DRT)
+        OP(104, CRT)
 #undef OP
     } catch (const std::exception&) {
         return -2;

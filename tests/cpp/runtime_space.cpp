@@ -26,6 +26,9 @@ static int host_checks() {
     if (v2.getOP(IDEN).code() != ANIGPU_OP(ANIGPU_VEC3_P2, ANIGPU_IDEN)) return fail("code");
     if (!(p2.getOP(GRAD) == ApplyOp(22)) || p2.getOP(GRAD) == p2.getOP(IDEN)) return fail("equality");
     if (v2.typeName() != "P2^3" || v2.NumDofsOnTet() != 30) return fail("names");
+    const FemSpace nd = FemSpace::ND0(), rt = FemSpace::RT0();
+    if (nd.getOP(CURL).Dim() != 3 || nd.getOP(GRAD).Dim() != 9 || nd.NumDofsOnTet() != 6) return fail("ND0");
+    if (rt.getOP(DIV).Dim() != 1 || rt.getOP(IDEN).Dim() != 3 || rt.getOP(DIV).code() != 103) return fail("RT0");
     bool threw = false;
     try {
         ApplyOp bad(27);

@@ -39,6 +39,8 @@ DIM = {1: 1, 2: 3}
 
 def op_nf_dim(code):
     space, op = divmod(code, 10)
+    if space in (9, 10):  # ND0, RT0
+        return (6 if space == 9 else 4), {1: 3, 2: 9, 3: 1, 4: 3}[op]
     nc = 3 if space in (4, 5) else 1
     return NF[space], DIM[op] * nc
 
@@ -101,7 +103,8 @@ def main():
     sym6 = meshgen.aniso_tensors(nt, sigma=1.0, seed=22)
     for (ca, cb) in [(12, 12), (22, 22), (32, 32), (42, 42), (52, 52), (32, 42), (11, 11), (21, 21), (31, 31),
                      (1, 11), (1, 21), (1, 51), (12, 22), (22, 12),
-                     (61, 61), (62, 62), (1, 61), (71, 71), (72, 72), (81, 81), (82, 82), (11, 81), (81, 11)]:
+                     (61, 61), (62, 62), (1, 61), (71, 71), (72, 72), (81, 81), (82, 82), (11, 81), (81, 11),
+                     (91, 91), (94, 94), (92, 92), (101, 101), (103, 103), (102, 102), (103, 1), (91, 101)]:
         nfA, dA = op_nf_dim(ca)
         nfB, dB = op_nf_dim(cb)
         kinds = []
@@ -132,7 +135,8 @@ def main():
     p4, _ = R.quadrature(4)
     out["apply_XYL"] = p4
     out["apply_X"] = meshgen.uniform(41, nt * 7 * 3).reshape(nt, 7, 3) * 3.0 - 1.0
-    apply_codes = [1, 11, 12, 21, 22, 31, 32, 41, 42, 51, 52, 61, 62, 71, 72, 81, 82]
+    apply_codes = [1, 11, 12, 21, 22, 31, 32, 41, 42, 51, 52, 61, 62, 71, 72, 81, 82,
+                   91, 92, 93, 94, 101, 102, 103, 104]
     for code in apply_codes:
         nf, dim = op_nf_dim(code)
         dofs = meshgen.normal(50 + code, nt * nf).reshape(nt, nf)

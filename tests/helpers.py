@@ -27,6 +27,8 @@ DIM = {1: 1, 2: 3}
 
 def op_nf_dim(code):
     space, op = divmod(code, 10)
+    if space in (9, 10):  # ND0, RT0: IDEN 3, GRAD 9, DIV 1, CURL 3
+        return (6 if space == 9 else 4), {1: 3, 2: 9, 3: 1, 4: 3}[op]
     nc = 3 if space in (4, 5) else 1
     return NF[space], DIM[op] * nc
 
