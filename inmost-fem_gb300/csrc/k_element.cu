@@ -263,10 +263,11 @@ __global__ void apply_dir_kernel(int64_t nt, int n, double* __restrict__ A, doub
 
 // ---------------------------------------------------------------- evaluation of Op(u)
 // Ani::fem3DapplyL / fem3DapplyX (anifem++/fem/operations/eval.inl:93-151 -> core.inl:370-404):
-// Op(u) at points of each tet, opU[t][n][k].  One thread per (tet, point): geometry (PSI) of
-// the tet, the point's barycentric coordinates (given, or from a physical point through PSI
-// as getBaryCoord does, core.inl:120-137), the scalar basis there, and per component the sum
-// over the local DOFs in ascending order.
+// Op(u) at points of each tet, opU[t][n][k].  One thread per tet: its geometry (PSI) once, its
+// DOF values once, then per point the barycentric coordinates (given, or from a physical point
+// through PSI as getBaryCoord does, core.inl:120-137) and the scalar basis there.  GRAD of a
+// Lagrange space combines the reference gradients with the DOF values first and maps the sum
+// with PSI^T once (3x3 instead of 3x3 per DOF; the same value up to rounding).
 struct ApplyParams {
     int nf, dim, nfs, ncomp, op, base;
     int npts, phys;           // phys: pts are per-tet physical points [nt][npts][3]
@@ -283,10 +284,8 @@ struct ApplyParams {
 };
 
 __global__ void __launch_bounds__(128) fem3d_apply_kernel(ApplyParams p, int64_t nt) {
-    const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (idx >= nt * p.npts) return;
-    const int64_t t = idx / p.npts;
-    const int n = (int)(idx - t * p.npts);
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= nt) return;
     double X[12];
     if (p.XY) {
 #pragma unroll
@@ -301,55 +300,166 @@ __global__ void __launch_bounds__(128) fem3d_apply_kernel(ApplyParams p, int64_t
     }
     double PSI[9], mes, det;
     tet_geometry(X, PSI, &mes, &det);
-    double l[4];
-    if (p.phys) {
-        const double* x = p.pts + 3 * idx;
-        const double dr[3] = {x[0] - X[0], x[1] - X[1], x[2] - X[2]};
-        l[1] = l[2] = l[3] = 0.0;
-#pragma unroll
-        for (int j = 0; j < 3; ++j)
-#pragma unroll
-            for (int i = 0; i < 3; ++i) l[i + 1] += PSI[i + 3 * j] * dr[j];
-        l[0] = 1.0 - l[1] - l[2] - l[3];
-    } else {
-#pragma unroll
-        for (int k = 0; k < 4; ++k) l[k] = p.pts[4 * n + k];
-    }
-    double* o = p.out + idx * p.dim;
-    if (p.base == ANIGPU_ND0 || p.base == ANIGPU_RT0) {  // vector-valued, from the tet geometry
-        double P[12];
+    double d[ANIGPU_MAX_NF];
+    for (int c = 0; c < p.ncomp; ++c)
+        for (int i = 0; i < p.nfs; ++i)
+            d[c * p.nfs + i] = p.dofs ? p.dofs[(int64_t)p.nf * t + c * p.nfs + i]
+                                      : p.x[c * p.nds + p.edofs[(int64_t)p.nloc * t + i]];
+    const bool vec = p.base == ANIGPU_ND0 || p.base == ANIGPU_RT0;
+    double P[12];
+    if (vec) {
 #pragma unroll
         for (int v = 0; v < 4; ++v)
 #pragma unroll
             for (int i = 0; i < 3; ++i) P[3 * v + i] = v == 0 ? 0.0 : X[3 * v + i] - X[i];
-        for (int k = 0; k < p.dim; ++k) {
-            double s = 0.0;
-            for (int i = 0; i < p.nf; ++i) {
-                const double d = p.dofs ? p.dofs[(int64_t)p.nf * t + i] : p.x[p.edofs[(int64_t)p.nloc * t + i]];
-                s += ani_vec_space_value(p.base, p.op, l, PSI, P, det, i, k) * d;
-            }
-            o[k] = s;
-        }
-        return;
     }
-    double v[20], g[20][3];
-    ani_eval_space(p.base, l, v, g);
-    for (int c = 0; c < p.ncomp; ++c) {
-        double s[3] = {0.0, 0.0, 0.0};
-        for (int i = 0; i < p.nfs; ++i) {
-            const double d = p.dofs ? p.dofs[(int64_t)p.nf * t + c * p.nfs + i]
-                                    : p.x[c * p.nds + p.edofs[(int64_t)p.nloc * t + i]];
+    for (int n = 0; n < p.npts; ++n) {
+        double l[4];
+        if (p.phys) {
+            const double* x = p.pts + 3 * ((int64_t)p.npts * t + n);
+            const double dr[3] = {x[0] - X[0], x[1] - X[1], x[2] - X[2]};
+            l[1] = l[2] = l[3] = 0.0;
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+#pragma unroll
+                for (int i = 0; i < 3; ++i) l[i + 1] += PSI[i + 3 * j] * dr[j];
+            l[0] = 1.0 - l[1] - l[2] - l[3];
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) l[k] = p.pts[4 * n + k];
+        }
+        double* o = p.out + ((int64_t)p.npts * t + n) * p.dim;
+        if (vec) {  // vector-valued, from the tet geometry
+            for (int k = 0; k < p.dim; ++k) {
+                double s = 0.0;
+                for (int i = 0; i < p.nf; ++i) s += ani_vec_space_value(p.base, p.op, l, PSI, P, det, i, k) * d[i];
+                o[k] = s;
+            }
+            continue;
+        }
+        double v[20], g[20][3];
+        ani_eval_space(p.base, l, v, g);
+        for (int c = 0; c < p.ncomp; ++c) {
+            const double* dc = d + c * p.nfs;
             if (p.op == ANIGPU_IDEN) {
-                s[0] += v[i] * d;
+                double s = 0.0;
+                for (int i = 0; i < p.nfs; ++i) s += v[i] * dc[i];
+                o[c] = s;
+            } else {
+                double r0 = 0.0, r1 = 0.0, r2 = 0.0;  // reference gradient of u
+                for (int i = 0; i < p.nfs; ++i) {
+                    r0 += g[i][0] * dc[i];
+                    r1 += g[i][1] * dc[i];
+                    r2 += g[i][2] * dc[i];
+                }
+#pragma unroll
+                for (int k = 0; k < 3; ++k) o[3 * c + k] = PSI[0 + 3 * k] * r0 + PSI[1 + 3 * k] * r1 + PSI[2 + 3 * k] * r2;
+            }
+        }
+    }
+}
+
+template <int BASE>
+struct LagrangeNf {
+    static constexpr int value = BASE == ANIGPU_P0 ? 1 : BASE == ANIGPU_P1 ? 4 : BASE == ANIGPU_P2 ? 10
+                               : BASE == ANIGPU_P3 ? 20 : BASE == ANIGPU_CR1 ? 4 : BASE == ANIGPU_B2 ? 6 : 1;
+};
+
+// values and reference gradients of the basis at shared barycentric points: table[n][4 * NFS]
+// (NFS values, then 3 NFS gradient entries)
+template <int BASE>
+__global__ void basis_table_kernel(int npts, const double* __restrict__ pts, double* __restrict__ table) {
+    constexpr int NFS = LagrangeNf<BASE>::value;
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= npts) return;
+    double v[NFS], g[NFS][3];
+    ani_eval_space(BASE, pts + 4 * n, v, g);
+    double* o = table + (size_t)4 * NFS * n;
+#pragma unroll
+    for (int i = 0; i < NFS; ++i) {
+        o[i] = v[i];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) o[NFS + 3 * i + d] = g[i][d];
+    }
+}
+
+// Lagrange-type spaces with the base space known at compile time: basis values, reference
+// gradients and DOF values in registers; with a table (shared barycentric points) the basis is
+// read from shared memory instead of evaluated per tet
+template <int BASE>
+__global__ void __launch_bounds__(128) fem3d_apply_lagrange_kernel(ApplyParams p, int64_t nt, const double* table) {
+    constexpr int NFS = LagrangeNf<BASE>::value;
+    extern __shared__ double sTab[];
+    if (table) {
+        for (int k = threadIdx.x; k < 4 * NFS * p.npts; k += blockDim.x) sTab[k] = table[k];
+        __syncthreads();
+    }
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= nt) return;
+    double X[12];
+    if (p.XY) {
+#pragma unroll
+        for (int k = 0; k < 12; ++k) X[k] = p.XY[12 * t + k];
+    } else {
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const int64_t node = p.tets[4 * t + v];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) X[3 * v + i] = p.xyz[3 * node + i];
+        }
+    }
+    double PSI[9], mes, det;
+    tet_geometry(X, PSI, &mes, &det);
+    for (int c = 0; c < p.ncomp; ++c) {
+        double d[NFS];
+#pragma unroll
+        for (int i = 0; i < NFS; ++i)
+            d[i] = p.dofs ? p.dofs[(int64_t)p.nf * t + c * NFS + i] : p.x[c * p.nds + p.edofs[(int64_t)p.nloc * t + i]];
+        for (int n = 0; n < p.npts; ++n) {
+            double l[4];
+            if (p.phys) {
+                const double* x = p.pts + 3 * ((int64_t)p.npts * t + n);
+                const double dr[3] = {x[0] - X[0], x[1] - X[1], x[2] - X[2]};
+                l[1] = l[2] = l[3] = 0.0;
+#pragma unroll
+                for (int j = 0; j < 3; ++j)
+#pragma unroll
+                    for (int i = 0; i < 3; ++i) l[i + 1] += PSI[i + 3 * j] * dr[j];
+                l[0] = 1.0 - l[1] - l[2] - l[3];
             } else {
 #pragma unroll
-                for (int k = 0; k < 3; ++k) s[k] += (PSI[0 + 3 * k] * g[i][0] + PSI[1 + 3 * k] * g[i][1] + PSI[2 + 3 * k] * g[i][2]) * d;
+                for (int k = 0; k < 4; ++k) l[k] = p.pts[4 * n + k];
+            }
+            double v[NFS], g[NFS][3];
+            if (table) {
+                const double* row = sTab + 4 * NFS * n;
+#pragma unroll
+                for (int i = 0; i < NFS; ++i) {
+                    v[i] = row[i];
+#pragma unroll
+                    for (int dd = 0; dd < 3; ++dd) g[i][dd] = row[NFS + 3 * i + dd];
+                }
+            } else {
+                ani_eval_space(BASE, l, v, g);
+            }
+            double* o = p.out + ((int64_t)p.npts * t + n) * p.dim;
+            if (p.op == ANIGPU_IDEN) {
+                double sv = 0.0;
+#pragma unroll
+                for (int i = 0; i < NFS; ++i) sv += v[i] * d[i];
+                o[c] = sv;
+            } else {
+                double r0 = 0.0, r1 = 0.0, r2 = 0.0;  // reference gradient of u
+#pragma unroll
+                for (int i = 0; i < NFS; ++i) {
+                    r0 += g[i][0] * d[i];
+                    r1 += g[i][1] * d[i];
+                    r2 += g[i][2] * d[i];
+                }
+#pragma unroll
+                for (int k = 0; k < 3; ++k) o[3 * c + k] = PSI[0 + 3 * k] * r0 + PSI[1 + 3 * k] * r1 + PSI[2 + 3 * k] * r2;
             }
         }
-        if (p.op == ANIGPU_IDEN) o[c] = s[0];
-        else
-#pragma unroll
-            for (int k = 0; k < 3; ++k) o[3 * c + k] = s[k];
     }
 }
 
@@ -489,7 +599,39 @@ int launch_fem3d_apply(anigpu_ctx* h, int op, int64_t nt, const double* XY, int 
         p.nloc = h->nloc_s;
         p.nds = h->nds;
     }
-    fem3d_apply_kernel<<<grid_for(nt * npts, 128), 128, 0, h->stream>>>(p, nt);
+    const unsigned g = grid_for(nt, 128);
+    cudaStream_t st = h->stream;
+    if (base == ANIGPU_ND0 || base == ANIGPU_RT0) {
+        fem3d_apply_kernel<<<g, 128, 0, st>>>(p, nt);
+        ANI_LAUNCHED(h);
+        return ANIGPU_OK;
+    }
+    // shared barycentric points: the basis table once (when it fits in shared memory)
+    const int nfs = p.nfs;
+    const size_t tab_bytes = sizeof(double) * 4 * nfs * (size_t)npts;
+    const bool use_table = !phys && tab_bytes <= 48 * 1024;
+    double* table = nullptr;
+    if (use_table) ANI_CUDA(h, cudaMallocAsync((void**)&table, tab_bytes, st));
+    const size_t smem = use_table ? tab_bytes : 0;
+#define APPLY_CASE(B)                                                                                   \
+    case B:                                                                                             \
+        if (use_table) {                                                                                \
+            basis_table_kernel<B><<<grid_for(npts, 64), 64, 0, st>>>(npts, pts, table);                 \
+            ANI_LAUNCHED(h);                                                                            \
+        }                                                                                               \
+        fem3d_apply_lagrange_kernel<B><<<g, 128, smem, st>>>(p, nt, table);                             \
+        break;
+    switch (base) {
+        APPLY_CASE(ANIGPU_P0)
+        APPLY_CASE(ANIGPU_P1)
+        APPLY_CASE(ANIGPU_P2)
+        APPLY_CASE(ANIGPU_P3)
+        APPLY_CASE(ANIGPU_CR1)
+        APPLY_CASE(ANIGPU_B2)
+        APPLY_CASE(ANIGPU_B4)
+    }
+#undef APPLY_CASE
     ANI_LAUNCHED(h);
+    if (table) ANI_CUDA(h, cudaFreeAsync(table, st));
     return ANIGPU_OK;
 }
