@@ -256,6 +256,21 @@ int anigpu_assemble_noalloc(anigpu_handle h, int tensor_kind, const double* D, c
  * errors are returned at once; a non-finite value is recorded on the device and reported by
  * the next anigpu_status, so that back-to-back assemblies (or a CUDA graph of them) keep
  * the GPU busy.  The caller keeps D, f, vals, rhs and touched alive until the stream passes. */
+/* General-path spaces: anigpu_problem_setup also takes ANIGPU_P0, ANIGPU_P3, ANIGPU_CR1, ANIGPU_B2,
+ * ANIGPU_B4, ANIGPU_ND0, ANIGPU_RT0.  Their DOFs are numbered NATURAL over nodes, edges, faces and
+ * cells (edge ids rank (min, max) vertex pairs, face ids sorted vertex triples), with oriented DOFs
+ * as AssemblerT's sign-encoded indices do (assembler.inl:48-54,136-190): the two P3 DOFs of an edge
+ * follow the edge's global direction (smaller to larger vertex id), ND0 DOFs carry the sign of
+ * their local edge direction against the global one, RT0 DOFs the sign of the tet's outward face
+ * normal against the global face normal (sorted vertex triple a < b < c: (X_b-X_a) x (X_c-X_a)).
+ * anigpu_assemble_general: A = sum over tets of s_i s_j fem3Dtet<opA, opB>(tensor) (FP64 values in
+ * the template, both operators on the problem's space), rhs_i = sum s_i fem3Dtet<IDEN P0, IDEN space>
+ * (rhs tensor: a scalar source for scalar spaces, a 3x1 GENERAL or POINT tensor for ND0 / RT0);
+ * rhs may be NULL.  Dirichlet DOFs (anigpu_set_dirichlet) as in the other paths.  Setup memory is
+ * about 24 nt nloc^2 bytes (sorts of the element-matrix entries); the fast kernels (anigpu_assemble),
+ * batching and enumerations take P1 / P2 / vector P2 only. */
+int anigpu_assemble_general(anigpu_handle h, int opA, int opB, int tensor_kind, const double* D, int rhs_kind,
+                            const double* F, int order, double* vals, double* rhs);
 int anigpu_assemble_async(anigpu_handle h, int tensor_kind, const double* D, const double* f, double f_const,
                           int order, int precision, void* vals, double* rhs, uint8_t* touched, double drop_val);
 /* waits for the handle's stream; ANIGPU_ERR_NONFINITE (and clears it) when an assembly since

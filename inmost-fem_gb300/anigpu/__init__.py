@@ -76,6 +76,7 @@ SIGNATURES = {
     "anigpu_set_dirichlet": (_i, [_vp, _vp, _vp]),
     "anigpu_assemble": (_i, [_vp, _i, _vp, _vp, _d, _i, _i, _vp, _vp, _vp, _d]),
     "anigpu_assemble_async": (_i, [_vp, _i, _vp, _vp, _d, _i, _i, _vp, _vp, _vp, _d]),
+    "anigpu_assemble_general": (_i, [_vp, _i, _i, _i, _vp, _i, _vp, _i, _vp, _vp]),
     "anigpu_status": (_i, [_vp]),
     "anigpu_assemble_noalloc": (_i, [_vp, _i, _vp, _vp, _d, _i, _i, _vp, _vp, _d]),
     "anigpu_csr_compact": (_i, [_vp, _vp, _vp, _vp, _i, _vp, ctypes.POINTER(_i64)]),
@@ -429,7 +430,7 @@ class Anigpu:
     @_streamed
     def element_dofs(self):
         torch = self.torch
-        nloc = 4 if self.space == P1 else 10
+        nloc = op_info(10 * self.space + IDEN)[0] if self.space not in (VEC3_P1, VEC3_P2) else 10
         e = torch.empty((self.nt, nloc), dtype=torch.int32, device=f"cuda:{self.device}")
         self._check(self.lib.anigpu_element_dofs(self.h, _ptr(e)))
         return e
@@ -447,6 +448,21 @@ class Anigpu:
         self._dmask = self._dev(mask, torch.uint8) if mask is not None else None
         self._dbc = self._dev(bc, torch.float64) if bc is not None else None
         self._check(self.lib.anigpu_set_dirichlet(self.h, _ptr(self._dmask), _ptr(self._dbc)))
+
+    @_streamed
+    def assemble_general(self, opA, opB, kind=TENSOR_NULL, D=None, rhs_kind=None, F=None, order=4):
+        """General-path spaces (P0, P3, CR1, B2, B4, ND0, RT0): FP64 values in the template and the
+        right-hand side (rhs_kind None: no right-hand side)."""
+        torch = self.torch
+        dev = f"cuda:{self.device}"
+        vals = torch.empty(self.nnz, dtype=torch.float64, device=dev)
+        rhs = torch.empty(self.ndof, dtype=torch.float64, device=dev) if rhs_kind is not None else None
+        Dd = self._dev(D, torch.float64) if D is not None else None
+        Fd = self._dev(F, torch.float64) if F is not None else None
+        self._check(self.lib.anigpu_assemble_general(self.h, opA, opB, kind, _ptr(Dd),
+                                                     rhs_kind if rhs_kind is not None else 0, _ptr(Fd), order,
+                                                     _ptr(vals), _ptr(rhs)))
+        return vals, rhs
 
     @_streamed
     def assemble(self, kind=TENSOR_NULL, D=None, f=None, f_const=1.0, order=2, precision=F64, vals=None, rhs=None,

@@ -12,7 +12,7 @@ REPO = os.path.dirname(ROOT)
 BUILD_DIR = os.path.join(ROOT, "_build")
 LIB_PATH = os.path.join(PKG_DIR, "libanigpu.so")
 
-SOURCES = ["api.cu", "k_element.cu", "k_setup.cu", "k_assemble.cu", "k_solve.cu", "k_learned.cu", "k_fcg.cu", "k_batch.cu", "k_enum.cu", "basis.cpp"]
+SOURCES = ["api.cu", "k_element.cu", "k_setup.cu", "k_assemble.cu", "k_solve.cu", "k_learned.cu", "k_fcg.cu", "k_batch.cu", "k_enum.cu", "k_general.cu", "basis.cpp"]
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", GENCODE, "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-Xcompiler", "-Wall", "-Xcompiler", "-Wno-unknown-pragmas"]

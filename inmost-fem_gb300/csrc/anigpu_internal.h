@@ -119,6 +119,7 @@ struct anigpu_ctx {
     void* fcg_ws = nullptr;        // flexible-CG workspace and its captured graphs
     void* batch_ws = nullptr;      // batched-instances map, tiles and solver workspace
     void* enum_ws = nullptr;       // renumbering to a non-NATURAL enumeration
+    void* gen_ws = nullptr;        // general-path spaces (P0, P3, CR1, B2, B4, ND0, RT0)
 
     // per-phase timing (anigpu_set_timing)
     bool timing = false;
@@ -177,6 +178,14 @@ inline unsigned grid_for(int64_t n, int block) {
 int launch_fem3dtet(anigpu_ctx* h, int opA, int opB, int kind, int order, int precision, int64_t nt,
                     const double* XY, const double* D, void* A, int face = -1, int normal = 0);
 int launch_quad_points(anigpu_ctx* h, int order, int64_t nt, const double* XY, double* XYG, int face = -1);
+// general-path spaces (k_general.cu)
+bool is_general_space(int space);
+void free_general(anigpu_ctx* h);
+int general_setup(anigpu_ctx* h, int space);
+int general_assemble(anigpu_ctx* h, int opA, int opB, int kind, const double* D, int rhs_kind, const double* F,
+                     int order, double* vals, double* rhs);
+int general_dof_coords(anigpu_ctx* h, double* out);
+const int8_t* general_signs(anigpu_ctx* h);
 // enumerations (k_enum.cu)
 void free_enum(anigpu_ctx* h);
 int enum_setup(anigpu_ctx* h, int type);

@@ -67,6 +67,7 @@ int anigpu_destroy(anigpu_handle h) {
     free_learned(h);
     free_batch(h);
     free_enum(h);
+    free_general(h);
     void* ptrs[] = {h->xyz, h->xyz2, h->tets, h->tet_edges, h->edofs, h->inc_ptr, h->recs, h->dir_mask, h->dir_bc,
                     h->dir_cptr, h->dir_coff,
                     h->tetdata, h->d_status, h->d_ref_tables};
@@ -219,7 +220,9 @@ int anigpu_eval_solution(anigpu_handle h, int op, const double* x, int npts, con
     CHECK_H(h);
     cudaSetDevice(h->device);
     if (h->space < 0) return set_err(h, ANIGPU_ERR_STATE, "anigpu_problem_setup not called");
-    if (op != ANIGPU_IDEN && op != ANIGPU_GRAD) return set_err(h, ANIGPU_ERR_ARG, "op must be ANIGPU_IDEN or ANIGPU_GRAD");
+    const bool vecsp = h->space == ANIGPU_ND0 || h->space == ANIGPU_RT0;
+    if (op != ANIGPU_IDEN && op != ANIGPU_GRAD && !(vecsp && (op == ANIGPU_DIV || op == ANIGPU_CURL)))
+        return set_err(h, ANIGPU_ERR_ARG, "op must be ANIGPU_IDEN or ANIGPU_GRAD (DIV, CURL for ND0 / RT0)");
     return launch_fem3d_apply(h, ANIGPU_OP(h->space, op), h->nt, nullptr, npts, XYL, 0, nullptr, x, opU);
 }
 
@@ -239,6 +242,7 @@ int anigpu_mesh_upload(anigpu_handle h, int64_t nv, const double* xyz, int64_t n
     learned_invalidate(h);  // bindings and captured solver graphs refer to the old mesh
     free_batch(h);
     free_enum(h);
+    free_general(h);
     int rc = dev_alloc(h, &h->xyz, (size_t)nv * 3);
     if (rc) return rc;
     rc = dev_alloc(h, &h->tets, (size_t)nt * 4);
@@ -271,6 +275,8 @@ int anigpu_problem_setup(anigpu_handle h, int space) {
     learned_invalidate(h);
     free_batch(h);
     free_enum(h);
+    if (is_general_space(space)) return general_setup(h, space);
+    free_general(h);
     return setup_problem(h, space);
 }
 
@@ -309,6 +315,7 @@ int anigpu_dof_coords(anigpu_handle h, double* xyz) {
     if (h->space < 0) return set_err(h, ANIGPU_ERR_STATE, "anigpu_problem_setup not called");
     if (!xyz) return set_err(h, ANIGPU_ERR_ARG, "NULL");
     cudaSetDevice(h->device);
+    if (is_general_space(h->space)) return general_dof_coords(h, xyz);
     return setup_dof_coords(h, xyz);
 }
 
@@ -334,6 +341,22 @@ int anigpu_assemble(anigpu_handle h, int tensor_kind, const double* D, const dou
     CHECK_H(h);
     cudaSetDevice(h->device);
     int rc = run_assemble(h, tensor_kind, D, f, f_const, order, precision, vals, rhs, touched, drop_val);
+    if (rc) return rc;
+    int st = 0;
+    ANI_CUDA(h, cudaMemcpyAsync(&st, h->d_status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    ANI_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (st) {
+        ANI_CUDA(h, cudaMemsetAsync(h->d_status, 0, sizeof(int), h->stream));
+        return set_err(h, st, "non-finite value in assembly (AssemblerT status -1)");
+    }
+    return ANIGPU_OK;
+}
+
+int anigpu_assemble_general(anigpu_handle h, int opA, int opB, int tensor_kind, const double* D, int rhs_kind,
+                            const double* F, int order, double* vals, double* rhs) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    int rc = general_assemble(h, opA, opB, tensor_kind, D, rhs_kind, F, order, vals, rhs);
     if (rc) return rc;
     int st = 0;
     ANI_CUDA(h, cudaMemcpyAsync(&st, h->d_status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));

@@ -1316,6 +1316,8 @@ static int run_assemble_vec(anigpu_ctx* h, int kind, const double* D, const doub
 int run_assemble(anigpu_ctx* h, int kind, const double* D, const double* f, double f_const, int order,
                  int precision, void* vals, double* rhs, uint8_t* touched, double drop_val) {
     if (h->space < 0) return set_err(h, ANIGPU_ERR_STATE, "anigpu_problem_setup not called");
+    if (is_general_space(h->space))
+        return set_err(h, ANIGPU_ERR_UNSUPPORTED, "this space assembles through anigpu_assemble_general");
     if (h->space == ANIGPU_VEC3_P2)
         return run_assemble_vec(h, kind, D, f, f_const, order, precision, vals, rhs, touched, drop_val);
     if (kind != ANIGPU_TENSOR_NULL && kind != ANIGPU_TENSOR_CONST_SCALAR && kind != ANIGPU_TENSOR_TET_SCALAR &&

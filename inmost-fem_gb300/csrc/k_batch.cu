@@ -433,7 +433,8 @@ void free_batch(anigpu_ctx* h) {
 
 int batch_set_instances(anigpu_ctx* h, int ninst, const int64_t* toff_host, const void* vals_for_tuning) {
     if (h->space < 0) return set_err(h, ANIGPU_ERR_STATE, "anigpu_problem_setup not called");
-    if (h->ncomp != 1) return set_err(h, ANIGPU_ERR_UNSUPPORTED, "batched instances need a scalar space");
+    if (h->space != ANIGPU_P1 && h->space != ANIGPU_P2)
+        return set_err(h, ANIGPU_ERR_UNSUPPORTED, "batched instances need a P1 or P2 problem");
     if (ninst < 1 || ninst > (1 << 24) || !toff_host) return set_err(h, ANIGPU_ERR_ARG, "instances");
     if (toff_host[0] != 0 || toff_host[ninst] != h->nt) return set_err(h, ANIGPU_ERR_ARG, "tet offsets must span 0..nt");
     for (int i = 0; i < ninst; ++i)

@@ -278,6 +278,7 @@ struct ApplyParams {
     const double* dofs;       // [nt][nf], or null: the global vector x through the DOF table
     const double* x;
     const int32_t* edofs;     // [nt][nloc] scalar element DOFs
+    const int8_t* sign;       // [nt][nloc] orientation signs of the global DOFs (oriented spaces) or null
     int nloc;
     int64_t nds;              // scalar DOFs (component c of scalar DOF s is c*nds + s)
     double* out;
@@ -304,7 +305,8 @@ __global__ void __launch_bounds__(128) fem3d_apply_kernel(ApplyParams p, int64_t
     for (int c = 0; c < p.ncomp; ++c)
         for (int i = 0; i < p.nfs; ++i)
             d[c * p.nfs + i] = p.dofs ? p.dofs[(int64_t)p.nf * t + c * p.nfs + i]
-                                      : p.x[c * p.nds + p.edofs[(int64_t)p.nloc * t + i]];
+                                      : p.x[c * p.nds + p.edofs[(int64_t)p.nloc * t + i]] *
+                                            (p.sign ? (double)p.sign[(int64_t)p.nloc * t + i] : 1.0);
     const bool vec = p.base == ANIGPU_ND0 || p.base == ANIGPU_RT0;
     double P[12];
     if (vec) {
@@ -414,7 +416,9 @@ __global__ void __launch_bounds__(128) fem3d_apply_lagrange_kernel(ApplyParams p
         double d[NFS];
 #pragma unroll
         for (int i = 0; i < NFS; ++i)
-            d[i] = p.dofs ? p.dofs[(int64_t)p.nf * t + c * NFS + i] : p.x[c * p.nds + p.edofs[(int64_t)p.nloc * t + i]];
+            d[i] = p.dofs ? p.dofs[(int64_t)p.nf * t + c * NFS + i]
+                          : p.x[c * p.nds + p.edofs[(int64_t)p.nloc * t + i]] *
+                                (p.sign ? (double)p.sign[(int64_t)p.nloc * t + i] : 1.0);
         for (int n = 0; n < p.npts; ++n) {
             double l[4];
             if (p.phys) {
@@ -596,6 +600,7 @@ int launch_fem3d_apply(anigpu_ctx* h, int op, int64_t nt, const double* XY, int 
         p.tets = h->tets;
         p.x = x;
         p.edofs = h->edofs;
+        p.sign = general_signs(h);  // null on the fast-path spaces
         p.nloc = h->nloc_s;
         p.nds = h->nds;
     }

@@ -131,6 +131,7 @@ void free_enum(anigpu_ctx* h) {
 int enum_setup(anigpu_ctx* h, int type) {
     if (type < ANIGPU_ENUM_ANITYPE || type > ANIGPU_ENUM_ETDIMBLOCKS) return set_err(h, ANIGPU_ERR_ARG, "enumeration type");
     if (h->space < 0) return set_err(h, ANIGPU_ERR_STATE, "anigpu_problem_setup not called");
+    if (is_general_space(h->space)) return set_err(h, ANIGPU_ERR_UNSUPPORTED, "enumerations for P1, P2 and vector P2");
     free_enum(h);
     EnumWs* w = new EnumWs();
     h->enum_ws = w;

@@ -641,8 +641,11 @@ int setup_dirichlet_bits(anigpu_ctx* h) {
     // node are constrained together for the scalar-structured records); the per-component
     // mask itself is used by the assembly for rows.
     const int64_t nrec = h->nt * h->nloc_s;
-    dirichlet_bits_kernel<<<grid_for(nrec, 256), 256, 0, h->stream>>>(nrec, h->nloc_s, h->edofs, h->dir_mask, h->recs);
-    ANI_LAUNCHED(h);
+    if (!is_general_space(h->space)) {  // the record bits of the fast P1/P2 gathers
+        dirichlet_bits_kernel<<<grid_for(nrec, 256), 256, 0, h->stream>>>(nrec, h->nloc_s, h->edofs, h->dir_mask,
+                                                                          h->recs);
+        ANI_LAUNCHED(h);
+    }
     if (!h->has_dirichlet) return ANIGPU_OK;
     // per non-Dirichlet row (of the full template: vector rows for FemVec), the offsets of its
     // Dirichlet columns: the assembly adds every element value and zeroes these entries at the end

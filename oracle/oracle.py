@@ -354,3 +354,110 @@ def permute_csr(rowptr, col, vals, perm):
     rp = np.zeros(n + 1, dtype=np.int64)
     np.add.at(rp, nr + 1, 1)
     return np.cumsum(rp), nc[order].astype(np.int32), np.asarray(vals)[order]
+
+
+# ---------------------------------------------------------------- general-path spaces
+# DOFs per (node, edge, face, cell) and local DOFs per tet of the general-path spaces
+_GEN_LAYOUT = {0: ((0, 0, 0, 1), 1), 3: ((1, 2, 1, 0), 20), 6: ((0, 0, 1, 0), 4), 7: ((0, 1, 0, 0), 6),
+               8: ((0, 0, 0, 1), 1), 9: ((0, 1, 0, 0), 6), 10: ((0, 0, 1, 0), 4)}
+_EI, _EJ = [0, 0, 0, 1, 1, 2], [1, 2, 3, 2, 3, 3]
+_FV = [(0, 1, 2), (1, 2, 3), (0, 2, 3), (0, 1, 3)]
+_FOPP = [3, 0, 1, 2]
+
+
+def _local_dofs(space):
+    """(entity type 0 node / 1 edge / 2 face / 3 cell, local entity, DOF within the entity) per local DOF"""
+    if space == 3:
+        return [(0, v, 0) for v in range(4)] + [(1, e, k) for e in range(6) for k in range(2)] + \
+               [(2, f, 0) for f in range(4)]
+    if space in (6, 10):
+        return [(2, f, 0) for f in range(4)]
+    if space in (7, 9):
+        return [(1, e, 0) for e in range(6)]
+    return [(3, 0, 0)]
+
+
+def general_numbering(xyz, t, space):
+    """Global DOF and orientation sign of every (tet, local DOF) of a general-path space on the
+    oriented tets t (NATURAL: nodes, edges ranked by (min, max), faces ranked by sorted triples,
+    cells; P3 edge pairs in the global edge direction; ND0 / RT0 signs; see the library's
+    k_general.cu for the convention)."""
+    nv, nt = xyz.shape[0], t.shape[0]
+    per, nloc = _GEN_LAYOUT[space]
+    ek = np.stack([np.minimum(t[:, _EI], t[:, _EJ]), np.maximum(t[:, _EI], t[:, _EJ])], axis=-1).astype(np.int64)
+    ekey = ek[..., 0] * nv + ek[..., 1]
+    ue, eid = np.unique(ekey.reshape(-1), return_inverse=True)
+    eid = eid.reshape(nt, 6)
+    ft = np.sort(np.stack([t[:, list(f)] for f in _FV], axis=1), axis=-1).astype(np.int64)
+    fkey = (ft[..., 0] * nv + ft[..., 1]) * nv + ft[..., 2]
+    uf, fid = np.unique(fkey.reshape(-1), return_inverse=True)
+    fid = fid.reshape(nt, 4)
+    ne, nf = ue.size, uf.size
+    off = [0, nv * per[0], nv * per[0] + ne * per[1], nv * per[0] + ne * per[1] + nf * per[2]]
+    ndof = off[3] + nt * per[3]
+    gd = np.zeros((nt, nloc), dtype=np.int64)
+    sg = np.ones((nt, nloc), dtype=np.int64)
+    for i, (typ, ent, k) in enumerate(_local_dofs(space)):
+        if typ == 0:
+            gd[:, i] = off[0] + t[:, ent] * per[0] + k
+        elif typ == 1:
+            I, J = t[:, _EI[ent]], t[:, _EJ[ent]]
+            kk = np.where((per[1] == 2) & (I > J), 1 - k, k)
+            gd[:, i] = off[1] + eid[:, ent] * per[1] + kk
+            if space == 9:
+                sg[:, i] = np.where(I < J, 1, -1)
+        elif typ == 2:
+            gd[:, i] = off[2] + fid[:, ent] * per[2] + k
+            if space == 10:
+                a, b, c = ft[:, ent, 0], ft[:, ent, 1], ft[:, ent, 2]
+                n = np.cross(xyz[b] - xyz[a], xyz[c] - xyz[a])
+                d = np.einsum("ij,ij->i", n, xyz[t[:, _FV[ent][0]]] - xyz[t[:, _FOPP[ent]]])
+                sg[:, i] = np.where(d > 0, 1, -1)
+        else:
+            gd[:, i] = off[3] + np.arange(nt) * per[3] + k
+    return gd, sg, ndof
+
+
+def general_assemble(restated, xyz, tets, space, codeA, codeB, kind, D, order, rhs_kind=None, F=None,
+                     dirichlet=None):
+    """Restatement of the general-path global assembly: signed sum of fem3Dtet element matrices
+    (and fem3Dtet<IDEN P0, IDEN space> right-hand sides) into the template of all element pairs,
+    Dirichlet rows / columns as the library's paths do.  Returns dict(rowptr, col, vals, rhs, gdof,
+    sign, ndof, oriented)."""
+    t = restated.orient(xyz, tets)
+    gd, sg, ndof = general_numbering(xyz, t, space)
+    nt, nloc = gd.shape
+    XY = np.ascontiguousarray(xyz[t].reshape(-1, 12))
+    A = restated.fem3dtet(codeA, codeB, kind, order, XY, D)            # A[t, j, i] = A_t(i, j)
+    rows = np.repeat(gd, nloc, axis=1).reshape(-1)                      # (t, i, j) -> g_i
+    cols = np.tile(gd, (1, nloc)).reshape(-1)                           # (t, i, j) -> g_j
+    w = (sg[:, :, None] * sg[:, None, :]).reshape(-1) * np.transpose(A, (0, 2, 1)).reshape(-1)
+    key = rows * ndof + cols
+    uk, inv = np.unique(key, return_inverse=True)
+    vals = np.zeros(uk.size)
+    np.add.at(vals, inv, w)
+    r, c = uk // ndof, uk % ndof
+    rowptr = np.zeros(ndof + 1, dtype=np.int64)
+    np.add.at(rowptr, r + 1, 1)
+    rowptr = np.cumsum(rowptr)
+    col = c.astype(np.int32)
+    rhs = np.zeros(ndof)
+    if rhs_kind is not None:
+        Fe = restated.fem3dtet(1, 10 * space + 1, rhs_kind, order, XY, F)[:, 0, :]
+        np.add.at(rhs, gd.reshape(-1), (sg * Fe).reshape(-1))
+    if dirichlet is not None:
+        mask, bc = dirichlet
+        bc = np.zeros(ndof) if bc is None else np.asarray(bc, dtype=np.float64)
+        cnt = np.bincount(gd.reshape(-1), minlength=ndof)
+        for row in range(ndof):
+            sl = slice(rowptr[row], rowptr[row + 1])
+            if mask[row]:
+                vals[sl] = 0.0
+                vals[sl][col[sl] == row] = cnt[row]
+                rhs[row] = cnt[row] * bc[row]
+            else:
+                m = mask[col[sl]].astype(bool)
+                rhs[row] -= np.sum(vals[sl][m] * bc[col[sl][m]])
+                v = vals[sl]
+                v[m] = 0.0
+    return dict(rowptr=rowptr, col=col, vals=vals, rhs=rhs, gdof=gd, sign=sg, ndof=ndof, oriented=t)
