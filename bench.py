@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-instances workload")
     ap.add_argument("--batched-instances", type=int, default=256)
     ap.add_argument("--no-elasticity", action="store_true", help="skip the vector-P2 elasticity workload")
+    ap.add_argument("--no-widened", action="store_true", help="skip the element-level / face / general-path rows")
     ap.add_argument("--cpu-sample", type=int, default=0, help="tets in the CPU-baseline sample (0 = auto)")
     return ap.parse_args()
 
@@ -230,6 +231,71 @@ def run_elasticity(args, local, peak):
                               "speedup_vs_jacobi_pcg_f64": out["jacobi_pcg_f64"]["seconds"] / (bind_s + st.seconds)}
     except anigpu.AnigpuError as e:
         out["fcg_learned"] = {"unavailable": str(e)}
+    lib.close()
+    return out
+
+
+def _time_ms(lib, fn, reps=5):
+    """mean device time of fn() over reps calls on the handle's stream (after one warm call)"""
+    import torch
+    fn()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(lib.stream)
+    for _ in range(reps):
+        fn()
+    e1.record(lib.stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def run_widened(args, local):
+    """Throughput of the rows next to the hot path: the element-level batch (fem3Dtet, P2 GRAD.GRAD
+    with per-tet symmetric tensors, order 4, FP64 and FP32), face integrals (fem3Dface IDEN P0 x IDEN
+    P2, order 4, face 0 of every tet), the general-path assembly (P3 GRAD.GRAD on 16^3x6 tets, FP64)
+    and the renumbering of a vector P2 system into MINIBLOCKS (32^3x6 tets, FP32 values)."""
+    import torch
+
+    import anigpu
+    from anigpu import meshgen
+    out = {}
+    dev = f"cuda:{local}"
+    lib = anigpu.Anigpu(local)
+    xyz, tets = meshgen.kuhn_cube(48, perturb=0.2, seed=31)
+    nt = tets.shape[0]
+    XY = torch.tensor(xyz[tets].reshape(-1, 12), device=dev)
+    D6 = torch.tensor(meshgen.aniso_tensors(nt, 1.5, 32), device=dev)
+    for name, prec in (("fem3dtet_p2_f64", anigpu.F64), ("fem3dtet_p2_f32", anigpu.F32)):
+        A = torch.empty((nt, 10, 10), dtype=torch.float64 if prec == anigpu.F64 else torch.float32, device=dev)
+        ms = _time_ms(lib, lambda: lib.fem3dtet(22, 22, XY, D6, anigpu.TENSOR_TET_SYM, 4, prec, out=A))
+        out[name] = {"tets": nt, "ms": ms, "tets_per_s": nt / (ms * 1e-3)}
+    F = torch.empty((nt, 1, 10), dtype=torch.float64, device=dev)
+    ms = _time_ms(lib, lambda: lib.fem3dface(1, 21, XY, 0, None, anigpu.TENSOR_NULL, 4, out=F))
+    out["fem3dface_p2_rhs"] = {"tets": nt, "ms": ms, "faces_per_s": nt / (ms * 1e-3)}
+    # general path: P3 on 16^3 x 6 tets
+    xyz3, tets3 = meshgen.kuhn_cube(16, perturb=0.2, seed=33)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    lib.mesh_upload(xyz3, tets3)
+    ndof, nnz = lib.problem_setup(anigpu.P3)
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    ms = _time_ms(lib, lambda: lib.assemble_general(32, 32, anigpu.TENSOR_NULL, None, anigpu.TENSOR_CONST_SCALAR,
+                                                    np.array([1.0]), 4), reps=3)
+    out["general_p3"] = {"tets": int(tets3.shape[0]), "dofs": ndof, "nnz": nnz, "setup_s": setup_s, "ms": ms,
+                         "tets_per_s": tets3.shape[0] / (ms * 1e-3)}
+    # renumbering: vector P2 on 32^3 x 6 tets into MINIBLOCKS
+    xyzv, tetsv = meshgen.kuhn_cube(32, perturb=0.2, seed=34)
+    ntv = tetsv.shape[0]
+    lib.mesh_upload(xyzv, tetsv)
+    ndof, nnz = lib.problem_setup(anigpu.VEC3_P2)
+    LM = np.stack([np.full(ntv, 1.5), np.full(ntv, 1.0)], axis=1)
+    v32, r, _ = lib.assemble(anigpu.TENSOR_LAME, LM, None, 0.0, 4, anigpu.F32)
+    v32, r = v32.clone(), r.clone()
+    lib.enumeration_setup(anigpu.ENUM_MINIBLOCKS)
+    ms = _time_ms(lib, lambda: lib.enumeration_apply(v32, anigpu.F32, r))
+    moved = nnz * (4 + 4 + 8) + ndof * 24  # values in and out, slot map, rhs in/out and permutation
+    out["enumeration_miniblocks"] = {"dofs": ndof, "nnz": nnz, "ms": ms, "GBps": moved / (ms * 1e-3) / 1e9}
     lib.close()
     return out
 
@@ -562,6 +628,9 @@ def run_ours(args):
     elasticity = None
     if not args.no_elasticity and rank == 0:
         elasticity = run_elasticity(args, local, peak)
+    widened = None
+    if not args.no_widened and rank == 0:
+        widened = run_widened(args, local)
 
     if rank != 0:
         return
@@ -597,6 +666,7 @@ def run_ours(args):
         "solve": solve,
         "batched": batched,
         "elasticity": elasticity,
+        "widened": widened,
     }
     print(json.dumps(line), flush=True)
 

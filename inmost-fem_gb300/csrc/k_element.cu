@@ -18,7 +18,6 @@
 namespace {
 
 constexpr int kThreads = 128;
-constexpr int kMaxOwned = (ANIGPU_MAX_NF * ANIGPU_MAX_NF + kThreads - 1) / kThreads;  // 8
 
 struct OpDesc {
     int nf, dim, nfs, bd, ncomp, op;  // op: 1 IDEN, 2 GRAD, 3 DIV, 4 CURL
@@ -32,6 +31,7 @@ struct ElemParams {
     int q, kind;
     int face;         // -1: the tet integral; 0..3: the integral over face k (fem3Dface)
     int normal;       // fem3DfaceN: the tensor has 3*dimB rows, contracted with the outward normal
+    int same;         // OpA == OpB: V is U
     const double* w;  // device weights
 };
 
@@ -97,8 +97,9 @@ __device__ inline double face_area(const double* X, int face) {
     return sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]) / 2;
 }
 
-__device__ inline void tet_geometry(const double* X, double* PSI, double* mes, double* det_out = nullptr) {
-    // internalFem3DtetGeomInit_Tet (core.inl:217-247) with inverse3x3 (geometry.h:26-44)
+// cofactors C of the edge matrix [X1-X0, X2-X0, X3-X0] arranged so that PSI = C / det is its
+// inverse (inverse3x3, geometry.h:26-44), and det
+__device__ inline void tet_cofactors(const double* X, double* C, double* det_out) {
     double m[9];
 #pragma unroll
     for (int c = 0; c < 3; ++c)
@@ -108,17 +109,25 @@ __device__ inline void tet_geometry(const double* X, double* PSI, double* mes, d
     const double da = M(1, 1) * M(2, 2) - M(1, 2) * M(2, 1);
     const double db = M(1, 2) * M(2, 0) - M(1, 0) * M(2, 2);
     const double dc = M(1, 0) * M(2, 1) - M(1, 1) * M(2, 0);
-    const double det = M(0, 0) * da + M(0, 1) * db + M(0, 2) * dc;
-    PSI[0] = da / det;
-    PSI[1] = db / det;
-    PSI[2] = dc / det;
+    *det_out = M(0, 0) * da + M(0, 1) * db + M(0, 2) * dc;
+    C[0] = da;
+    C[1] = db;
+    C[2] = dc;
 #pragma unroll
     for (int i = 1; i < 3; ++i)
 #pragma unroll
         for (int j = 0; j < 3; ++j)
-            PSI[j + 3 * i] = (M((i + 1) % 3, (j + 1) % 3) * M((i + 2) % 3, (j + 2) % 3) -
-                              M((i + 1) % 3, (j + 2) % 3) * M((i + 2) % 3, (j + 1) % 3)) / det;
+            C[j + 3 * i] = M((i + 1) % 3, (j + 1) % 3) * M((i + 2) % 3, (j + 2) % 3) -
+                           M((i + 1) % 3, (j + 2) % 3) * M((i + 2) % 3, (j + 1) % 3);
 #undef M
+}
+
+__device__ inline void tet_geometry(const double* X, double* PSI, double* mes, double* det_out = nullptr) {
+    // internalFem3DtetGeomInit_Tet (core.inl:217-247) with inverse3x3 (geometry.h:26-44)
+    double det;
+    tet_cofactors(X, PSI, &det);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) PSI[i] /= det;
     *mes = fabs(det) / 6.0;
     if (det_out) *det_out = det;
 }
@@ -142,9 +151,15 @@ __device__ inline Real op_value(const OpDesc& o, const double* tab, int q, int n
     return Real(PSI[0 + 3 * kk] * g[0] + PSI[1 + 3 * kk] * g[1] + PSI[2 + 3 * kk] * g[2]);
 }
 
+// One warp per tet (four tets in flight per 128-thread block): per quadrature point the warp
+// fills U, V (= U when both operators are the same), the tensor and DU = w |T| D U in its own
+// shared-memory region, then every lane adds V^T DU to the element entries it owns (e = lane + 32m,
+// kept in shared memory).  Only warp-level synchronisation; every entry sums its points in
+// ascending order and each point's contribution over k in ascending order.
 template <typename Real>
 __global__ void __launch_bounds__(kThreads) fem3dtet_kernel(ElemParams p, int64_t nt, const double* __restrict__ XY,
-                                                             const double* __restrict__ D, Real* __restrict__ A) {
+                                                             const double* __restrict__ D, Real* __restrict__ A,
+                                                             int wstride) {
     extern __shared__ double smem[];
     const int q = p.q;
     const int nfA = p.A.nf, nfB = p.B.nf, dA = p.A.dim, dB = p.B.dim;
@@ -152,40 +167,42 @@ __global__ void __launch_bounds__(kThreads) fem3dtet_kernel(ElemParams p, int64_
     double* sTabA = smem;
     double* sTabB = sTabA + tabA;
     double* sW = sTabB + tabB;
-    double* sGeo = sW + q;              // PSI[9], mes, outward normal[3], XYP[12], det
-    double* sD = sGeo + 26;             // dB*dA
-    Real* sU = reinterpret_cast<Real*>(sD + ANIGPU_MAX_DIM * ANIGPU_MAX_DIM);
-    Real* sV = sU + dA * nfA;
-    Real* sDU = sV + dB * nfB;
     for (size_t i = threadIdx.x; i < tabA; i += blockDim.x) sTabA[i] = p.A.tab[i];
     for (size_t i = threadIdx.x; i < tabB; i += blockDim.x) sTabB[i] = p.B.tab[i];
     for (int i = threadIdx.x; i < q; i += blockDim.x) sW[i] = p.w[i];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr int kWarps = kThreads / 32;
+    double* sGeo = sW + q + (size_t)warp * wstride;  // PSI[9], mes, normal[3], XYP[12], det
+    double* sD = sGeo + 26;                          // dB*dA
+    Real* sU = reinterpret_cast<Real*>(sD + ANIGPU_MAX_DIM * ANIGPU_MAX_DIM);
+    Real* sV = sU + dA * nfA;
+    Real* sDU = sV + (p.same ? 0 : dB * nfB);
+    Real* sAcc = sDU + dB * nfA;
+    const Real* V = p.same ? sU : sV;
     const int nent = nfA * nfB;
     const int nD = dA * dB;
-    for (int64_t t = blockIdx.x; t < nt; t += gridDim.x) {
-        __syncthreads();
-        if (threadIdx.x == 0) {
+    for (int64_t t = (int64_t)blockIdx.x * kWarps + warp; t < nt; t += (int64_t)gridDim.x * kWarps) {
+        if (lane == 0) {
             const double* X = XY + 12 * t;
             tet_geometry(X, sGeo, sGeo + 9, sGeo + 25);
             for (int v = 0; v < 4; ++v)
                 for (int i = 0; i < 3; ++i) sGeo[13 + 3 * v + i] = v == 0 ? 0.0 : X[3 * v + i] - X[i];
-            if (p.normal) sGeo[9] = face_normal(XY + 12 * t, p.face, sGeo + 10);
-            else if (p.face >= 0) sGeo[9] = face_area(XY + 12 * t, p.face);
+            if (p.normal) sGeo[9] = face_normal(X, p.face, sGeo + 10);
+            else if (p.face >= 0) sGeo[9] = face_area(X, p.face);
         }
-        Real acc[kMaxOwned];
-#pragma unroll
-        for (int m = 0; m < kMaxOwned; ++m) acc[m] = Real(0);
-        __syncthreads();
+        for (int e = lane; e < nent; e += 32) sAcc[e] = Real(0);
+        __syncwarp();
         const double mes = sGeo[9];
         for (int n = 0; n < q; ++n) {
             // U, V and the tensor at point n
-            for (int e = threadIdx.x; e < dA * nfA; e += blockDim.x)
-                sU[e] = op_value<Real>(p.A, sTabA, q, n, e % dA, e / dA, sGeo);
-            for (int e = threadIdx.x; e < dB * nfB; e += blockDim.x)
-                sV[e] = op_value<Real>(p.B, sTabB, q, n, e % dB, e / dB, sGeo);
+            for (int e = lane; e < dA * nfA; e += 32) sU[e] = op_value<Real>(p.A, sTabA, q, n, e % dA, e / dA, sGeo);
+            if (!p.same)
+                for (int e = lane; e < dB * nfB; e += 32)
+                    sV[e] = op_value<Real>(p.B, sTabB, q, n, e % dB, e / dB, sGeo);
             // dense D(k,j), column-major dB x dA; fem3DfaceN: rows l + 3k of the 3dB x dA tensor
             // contracted with the normal (DotWithNormalHelper::ProcessNormal, core.h:175-190)
-            for (int e = threadIdx.x; e < nD; e += blockDim.x) {
+            for (int e = lane; e < nD; e += 32) {
                 const int k = e % dB, j = e / dB;
                 if (!p.normal) {
                     sD[e] = tensor_at(p.kind, D, t, n, q, dA, dB, k, j);
@@ -196,32 +213,123 @@ __global__ void __launch_bounds__(kThreads) fem3dtet_kernel(ElemParams p, int64_
                     sD[e] = v;
                 }
             }
-            __syncthreads();
+            __syncwarp();
             const Real wv = Real(sW[n] * mes);
-            for (int e = threadIdx.x; e < dB * nfA; e += blockDim.x) {
+            for (int e = lane; e < dB * nfA; e += 32) {
                 const int k = e % dB, ia = e / dB;
                 Real s = 0;
                 for (int j = 0; j < dA; ++j) s += Real(sD[k + dB * j]) * sU[j + dA * ia];
                 sDU[e] = wv * s;
             }
-            __syncthreads();
-#pragma unroll
-            for (int m = 0; m < kMaxOwned; ++m) {
-                const int e = threadIdx.x + m * kThreads;
-                if (e < nent) {
-                    const int ib = e % nfB, ia = e / nfB;
-                    Real s = 0;
-                    for (int k = 0; k < dB; ++k) s += sV[k + dB * ib] * sDU[k + dB * ia];
-                    acc[m] += s;
-                }
+            __syncwarp();
+            for (int e = lane; e < nent; e += 32) {
+                const int ib = e % nfB, ia = e / nfB;
+                Real s = 0;
+                for (int k = 0; k < dB; ++k) s += V[k + dB * ib] * sDU[k + dB * ia];
+                sAcc[e] += s;
             }
-            __syncthreads();
+            __syncwarp();
         }
         Real* At = A + (size_t)nent * t;
+        for (int e = lane; e < nent; e += 32) At[e] = sAcc[e];
+        __syncwarp();
+    }
+}
+
+// Reference-tensor form for scalar Lagrange-type spaces, IDEN / GRAD operators and tensors constant
+// on a tet: U_n = L_A Uhat_n with L = PSI^T (GRAD) or 1 (IDEN), so
+//     A(ib, ia) = sum_{m,m'} M(m, m') T(ib, ia, m, m'),   M = mes L_B^T D L_A,
+//     T(ib, ia, m, m') = sum_n w_n Vhat_n(m, ib) Uhat_n(m', ia)   (per rule, operator pair and face)
+// -- the quadrature sum of fem3Dtet (core.inl:277-367) regrouped exactly.  With the same operator
+// on both sides and a symmetric tensor, M is symmetric and A(ib, ia) = A(ia, ib): the kernel then
+// forms the upper triangle only, from the six distinct M(m <= m') and T(m, m') + T(m', m) (FP64
+// FMA throughput bounds this kernel in double precision).  Phase 1: one thread per tet forms M in
+// FP64; phase 2: each warp builds the matrices of 32 tets, lanes over entries (or entry pairs),
+// staged in shared memory and written out coalesced.
+template <typename Real>
+__global__ void __launch_bounds__(128) fem3dtet_reftensor_kernel(int64_t nt, const double* __restrict__ XY, int kind,
+                                                                 const double* __restrict__ D, int dA, int dB,
+                                                                 int gradA, int gradB, int nfA, int nfB, int face,
+                                                                 int sym, const double* __restrict__ T,
+                                                                 Real* __restrict__ A) {
+    extern __shared__ double rsm[];
+    const int rA = gradA ? 3 : 1, rB = gradB ? 3 : 1;
+    const int nent = nfA * nfB;
+    const int rs = sym ? (rA == 3 ? 6 : 1) : rA * rB;      // M values per tet
+    const int nrow = sym ? nfA * (nfA + 1) / 2 : nent;     // entries (pairs) computed per tet
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    Real* sT = reinterpret_cast<Real*>(rsm);
+    Real* sM = sT + (size_t)nrow * rs;
+    Real* sOut = sM + 128 * 9 + (size_t)warp * nent;
+    int* sPair = reinterpret_cast<int*>(sM + 128 * 9 + (size_t)4 * nent);
+    for (int i = threadIdx.x; i < nrow * rs; i += blockDim.x) sT[i] = Real(T[i]);
+    if (sym)
+        for (int i = threadIdx.x; i < nrow; i += blockDim.x) sPair[i] = (int)T[(size_t)nrow * rs + i];
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < nt; base += (int64_t)gridDim.x * blockDim.x) {
+        __syncthreads();
+        const int64_t t = base + threadIdx.x;
+        if (t < nt) {
+            const double* X = XY + 12 * t;
+            // PSI = C / det with C the cofactors (tet_geometry); the 1/det of each GRAD side goes into
+            // the scale factor, one reciprocal per tet
+            double PSI[9], det;
+            tet_cofactors(X, PSI, &det);
+            const double mes = face >= 0 ? face_area(X, face) : fabs(det) / 6.0;
+            const double inv = 1.0 / det;
+            const double scale = mes * (gradA ? inv : 1.0) * (gradB ? inv : 1.0);
+            // L(j, m') = C(m', j) for GRAD, the 1x1 identity for IDEN; W = D L_A, M = scale L_B^T W
+            double W[3][3];
 #pragma unroll
-        for (int m = 0; m < kMaxOwned; ++m) {
-            const int e = threadIdx.x + m * kThreads;
-            if (e < nent) At[e] = acc[m];
+            for (int k = 0; k < 3; ++k)
+#pragma unroll
+                for (int mp = 0; mp < 3; ++mp) {
+                    double w = 0.0;
+#pragma unroll
+                    for (int j = 0; j < 3; ++j) {
+                        if (k >= dB || j >= dA) continue;
+                        const double la = gradA ? PSI[mp + 3 * j] : (j == mp ? 1.0 : 0.0);
+                        w += tensor_at(kind, D, t, 0, 1, dA, dB, k, j) * la;
+                    }
+                    W[k][mp] = w;
+                }
+            int c = 0;
+#pragma unroll
+            for (int m = 0; m < 3; ++m)
+#pragma unroll
+                for (int mp = 0; mp < 3; ++mp) {
+                    if (m >= rB || mp >= rA || (sym && mp < m)) continue;
+                    double v = 0.0;
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        if (k >= dB) continue;
+                        const double lb = gradB ? PSI[m + 3 * k] : (k == m ? 1.0 : 0.0);
+                        v += lb * W[k][mp];
+                    }
+                    sM[threadIdx.x * 9 + c++] = Real(scale * v);
+                }
+        }
+        __syncthreads();
+        for (int i = 0; i < 32; ++i) {
+            const int tl = warp * 32 + i;
+            const int64_t tt = base + tl;
+            if (tt >= nt) break;
+            const Real* M = sM + tl * 9;
+            for (int e = lane; e < nrow; e += 32) {
+                const Real* Te = sT + (size_t)e * rs;
+                Real s = 0;
+                for (int k = 0; k < rs; ++k) s += M[k] * Te[k];
+                if (sym) {
+                    const int ib = sPair[e] & 0xffff, ia = sPair[e] >> 16;
+                    sOut[ib + nfB * ia] = s;
+                    sOut[ia + nfB * ib] = s;
+                } else {
+                    sOut[e] = s;  // e = ib + nfB * ia (column-major nfB x nfA)
+                }
+            }
+            __syncwarp();
+            Real* At = A + (size_t)nent * tt;
+            for (int e = lane; e < nent; e += 32) At[e] = sOut[e];
+            __syncwarp();
         }
     }
 }
@@ -493,6 +601,80 @@ int get_basis_dev(anigpu_ctx* h, int space, int order, const double** dev, Scala
     return ANIGPU_OK;
 }
 
+// reference tensors T(ib, ia, m, m') = sum_n w_n Vhat_n(m, ib) Uhat_n(m', ia) of a scalar operator
+// pair on the rule of `order` (over face `face` when face >= 0), cached per handle; then the
+// two-phase kernel above
+static int launch_reftensor(anigpu_ctx* h, int opA, int opB, int order, int face, const ScalarBasisTable& hA,
+                            const ScalarBasisTable& hB, int kind, int precision, int64_t nt, const double* XY,
+                            const double* D, void* A) {
+    const int gradA = opA % 10 == ANIGPU_GRAD, gradB = opB % 10 == ANIGPU_GRAD;
+    const int rA = gradA ? 3 : 1, rB = gradB ? 3 : 1, rr = rA * rB;
+    const int nfA = hA.nf, nfB = hB.nf, q = hA.q;
+    const int dA = gradA ? 3 : 1, dB = gradB ? 3 : 1;
+    // same operator and a symmetric tensor: symmetric element matrix (upper triangle only)
+    const int sym = opA == opB && (kind == ANIGPU_TENSOR_NULL || kind == ANIGPU_TENSOR_CONST_SCALAR ||
+                                   kind == ANIGPU_TENSOR_TET_SCALAR || kind == ANIGPU_TENSOR_TET_SYM);
+    const int rs = sym ? (rA == 3 ? 6 : 1) : rr;
+    const int nrow = sym ? nfA * (nfA + 1) / 2 : nfA * nfB;
+    const int key = -(1 + opA + 128 * (opB + 128 * (order + 32 * (face + 1 + 8 * sym))));
+    const double* T = nullptr;
+    for (auto& kv : h->basis_dev)
+        if (kv.first == key) T = kv.second;
+    if (!T) {
+        std::vector<double> hT((size_t)nfA * nfB * rr, 0.0);
+        for (int ia = 0; ia < nfA; ++ia)
+            for (int ib = 0; ib < nfB; ++ib)
+                for (int m = 0; m < rB; ++m)
+                    for (int mp = 0; mp < rA; ++mp) {
+                        double s = 0.0;
+                        for (int n = 0; n < q; ++n) {
+                            const double vb = gradB ? hB.grad[((size_t)n * nfB + ib) * 3 + m] : hB.val[(size_t)n * nfB + ib];
+                            const double ua = gradA ? hA.grad[((size_t)n * nfA + ia) * 3 + mp] : hA.val[(size_t)n * nfA + ia];
+                            s += hA.wts[n] * vb * ua;
+                        }
+                        hT[((size_t)ib + (size_t)nfB * ia) * rr + m * rA + mp] = s;
+                    }
+        if (sym) {
+            // pairs ib <= ia; off-diagonal M terms carry T(m, m') + T(m', m)
+            std::vector<double> hS((size_t)nrow * (rs + 1), 0.0);
+            int pr = 0;
+            for (int ia = 0; ia < nfA; ++ia)
+                for (int ib = 0; ib <= ia; ++ib, ++pr) {
+                    const double* Te = &hT[((size_t)ib + (size_t)nfB * ia) * rr];
+                    int c = 0;
+                    for (int m = 0; m < rB; ++m)
+                        for (int mp = m; mp < rA; ++mp)
+                            hS[(size_t)pr * rs + c++] = mp == m ? Te[m * rA + m] : Te[m * rA + mp] + Te[mp * rA + m];
+                    hS[(size_t)nrow * rs + pr] = (double)(ib | (ia << 16));
+                }
+            hT.swap(hS);
+        }
+        double* d = nullptr;
+        ANI_CUDA(h, cudaMalloc((void**)&d, hT.size() * sizeof(double)));
+        ANI_CUDA(h, cudaMemcpy(d, hT.data(), hT.size() * sizeof(double), cudaMemcpyHostToDevice));
+        h->basis_dev.push_back({key, d});
+        T = d;
+    }
+    const size_t rsz = precision == ANIGPU_F32 ? sizeof(float) : sizeof(double);
+    constexpr int kRT = 128;
+    const size_t smem = rsz * ((size_t)nrow * rs + (size_t)kRT * 9 + (size_t)(kRT / 32) * nfA * nfB) +
+                        (sym ? sizeof(int) * nrow : 0);
+    int dev_sms = 148;
+    cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, h->device);
+    const unsigned grid = (unsigned)std::min<int64_t>((nt + kRT - 1) / kRT, (int64_t)dev_sms * 8);
+    if (precision == ANIGPU_F32) {
+        ANI_CUDA(h, cudaFuncSetAttribute(fem3dtet_reftensor_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        fem3dtet_reftensor_kernel<float><<<grid, kRT, smem, h->stream>>>(nt, XY, kind, D, dA, dB, gradA, gradB, nfA, nfB,
+                                                                          face, sym, T, (float*)A);
+    } else {
+        ANI_CUDA(h, cudaFuncSetAttribute(fem3dtet_reftensor_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        fem3dtet_reftensor_kernel<double><<<grid, kRT, smem, h->stream>>>(nt, XY, kind, D, dA, dB, gradA, gradB, nfA,
+                                                                           nfB, face, sym, T, (double*)A);
+    }
+    ANI_LAUNCHED(h);
+    return ANIGPU_OK;
+}
+
 int launch_fem3dtet(anigpu_ctx* h, int opA, int opB, int kind, int order, int precision, int64_t nt,
                     const double* XY, const double* D, void* A, int face, int normal) {
     int nfA, dA, bsA, ncA, oA, nfB, dB, bsB, ncB, oB;
@@ -518,8 +700,12 @@ int launch_fem3dtet(anigpu_ctx* h, int opA, int opB, int kind, int order, int pr
     if (face > 3) return set_err(h, ANIGPU_ERR_ARG, "face number must be 0..3");
     int rc = get_basis_dev(h, vecA ? ANIGPU_P1 : bsA, order, &tA, &hA, face);
     if (rc) return rc;
-    rc = get_basis_dev(h, vecB ? ANIGPU_P1 : bsB, order, &tB, nullptr, face);
+    ScalarBasisTable hB;
+    rc = get_basis_dev(h, vecB ? ANIGPU_P1 : bsB, order, &tB, &hB, face);
     if (rc) return rc;
+    if (precision != ANIGPU_F32 && precision != ANIGPU_F64) return set_err(h, ANIGPU_ERR_ARG, "precision");
+    if (!vecA && !vecB && ncA == 1 && ncB == 1 && !normal && kind != ANIGPU_TENSOR_POINT)
+        return launch_reftensor(h, opA, opB, order, face, hA, hB, kind, precision, nt, XY, D, A);
     ElemParams p;
     p.A = {nfA, dA, nfA / ncA, dA / ncA, ncA, oA, bsA, vecA ? 4 : nfA / ncA, tA};
     p.B = {nfB, dB, nfB / ncB, dB / ncB, ncB, oB, bsB, vecB ? 4 : nfB / ncB, tB};
@@ -528,19 +714,22 @@ int launch_fem3dtet(anigpu_ctx* h, int opA, int opB, int kind, int order, int pr
     p.face = face;
     p.normal = normal ? 1 : 0;
     p.w = tA + (size_t)hA.q * hA.nf * 4;
+    p.same = opA == opB ? 1 : 0;
     const size_t tabs = (size_t)p.q * (p.A.tnf + p.B.tnf) * 4;
     const size_t rsz = precision == ANIGPU_F32 ? sizeof(float) : sizeof(double);
-    const size_t smem = sizeof(double) * (tabs + p.q + 26 + ANIGPU_MAX_DIM * ANIGPU_MAX_DIM) +
-                        rsz * (size_t)(dA * nfA + dB * nfB + dB * nfA);
+    // per-warp region in doubles: geometry 26, tensor MAX_DIM^2, then U, V, DU and the entries
+    const size_t wreal = (size_t)dA * nfA + (p.same ? 0 : (size_t)dB * nfB) + (size_t)dB * nfA + (size_t)nfA * nfB;
+    const int wstride = (int)((26 + ANIGPU_MAX_DIM * ANIGPU_MAX_DIM) + (wreal * rsz + 7) / 8 + 1) & ~1;
+    const size_t smem = sizeof(double) * (tabs + p.q + (size_t)(kThreads / 32) * wstride);
     int dev_sms = 148;
     cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, h->device);
-    const unsigned grid = (unsigned)std::min<int64_t>(nt, (int64_t)dev_sms * 16);
+    const unsigned grid = (unsigned)std::min<int64_t>((nt + kThreads / 32 - 1) / (kThreads / 32), (int64_t)dev_sms * 16);
     if (precision == ANIGPU_F32) {
         ANI_CUDA(h, cudaFuncSetAttribute(fem3dtet_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        fem3dtet_kernel<float><<<grid, kThreads, smem, h->stream>>>(p, nt, XY, D, (float*)A);
+        fem3dtet_kernel<float><<<grid, kThreads, smem, h->stream>>>(p, nt, XY, D, (float*)A, wstride);
     } else if (precision == ANIGPU_F64) {
         ANI_CUDA(h, cudaFuncSetAttribute(fem3dtet_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        fem3dtet_kernel<double><<<grid, kThreads, smem, h->stream>>>(p, nt, XY, D, (double*)A);
+        fem3dtet_kernel<double><<<grid, kThreads, smem, h->stream>>>(p, nt, XY, D, (double*)A, wstride);
     } else {
         return set_err(h, ANIGPU_ERR_ARG, "precision");
     }

@@ -470,9 +470,9 @@ const int8_t* general_signs(anigpu_ctx* h) { return gws(h) ? gws(h)->sign : null
 
 namespace {
 
-// one thread per row: the row's slots zeroed, then for every incidence (ascending tets) the
-// signed element row added column by column (binary search of the column in the sorted row);
-// Dirichlet rows and columns as in the other assembly paths
+// per row: the row's slots zeroed, then for every incidence (ascending tets) the signed element
+// row added column by column (binary search of the column in the sorted row); Dirichlet rows and
+// columns as in the other assembly paths
 __global__ void general_gather_kernel(int64_t ndof, int nloc, const int64_t* __restrict__ rowptr,
                                       const int32_t* __restrict__ col, const int64_t* __restrict__ inc_ptr,
                                       const int32_t* __restrict__ inc, const int32_t* __restrict__ gdof,
@@ -480,11 +480,15 @@ __global__ void general_gather_kernel(int64_t ndof, int nloc, const int64_t* __r
                                       const double* __restrict__ F, const uint8_t* __restrict__ dir_mask,
                                       const double* __restrict__ dir_bc, int dir, int bcnz, double* __restrict__ vals,
                                       double* __restrict__ rhs, int* __restrict__ status) {
-    const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    // one warp per row: incidences in ascending order, lanes over the element row's columns (distinct
+    // columns within one incidence), so every entry sums its contributions in incidence order
+    const int lane = threadIdx.x & 31;
+    const int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     if (r >= ndof) return;
     const int64_t b = rowptr[r], e = rowptr[r + 1];
-    for (int64_t k = b; k < e; ++k) vals[k] = 0.0;
-    double f = 0.0;
+    for (int64_t k = b + lane; k < e; k += 32) vals[k] = 0.0;
+    __syncwarp();
+    double f = 0.0, fd = 0.0;
     const int64_t q0 = inc_ptr[r], q1 = inc_ptr[r + 1];
     const bool isdir = dir && dir_mask[r];
     if (!isdir) {
@@ -494,7 +498,7 @@ __global__ void general_gather_kernel(int64_t ndof, int nloc, const int64_t* __r
             const int i = (int)(slot - t * nloc);
             const double si = sign[slot];
             const double* At = A + (size_t)nloc * nloc * t;
-            for (int j = 0; j < nloc; ++j) {
+            for (int j = lane; j < nloc; j += 32) {
                 const int32_t c = gdof[(int64_t)nloc * t + j];
                 int64_t lo = b, hi = e;
                 while (lo < hi) {
@@ -504,24 +508,29 @@ __global__ void general_gather_kernel(int64_t ndof, int nloc, const int64_t* __r
                 }
                 vals[lo] += si * (double)sign[(int64_t)nloc * t + j] * At[i + nloc * j];
             }
+            __syncwarp();
             if (F) f += si * F[(int64_t)nloc * t + i];
         }
         if (dir) {
-            for (int64_t k = b; k < e; ++k)
+            for (int64_t k = b + lane; k < e; k += 32)
                 if (dir_mask[col[k]]) {
-                    if (bcnz) f -= vals[k] * dir_bc[col[k]];
+                    if (bcnz) fd += vals[k] * dir_bc[col[k]];
                     vals[k] = 0.0;
                 }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) fd += __shfl_xor_sync(0xffffffffu, fd, o);
+            f -= fd;
         }
     } else {
-        for (int64_t k = b; k < e; ++k)
+        for (int64_t k = b + lane; k < e; k += 32)
             if (col[k] == r) vals[k] = (double)(q1 - q0);
         for (int64_t q = q0; q < q1; ++q) f += bcnz ? dir_bc[r] : 0.0;
     }
+    __syncwarp();
     bool bad = !isfinite(f);
-    for (int64_t k = b; k < e; ++k) bad |= !isfinite(vals[k]);
-    if (bad) atomicExch(status, ANIGPU_ERR_NONFINITE);
-    if (rhs) rhs[r] = f;
+    for (int64_t k = b + lane; k < e; k += 32) bad |= !isfinite(vals[k]);
+    if (__any_sync(0xffffffffu, bad) && lane == 0) atomicExch(status, ANIGPU_ERR_NONFINITE);
+    if (rhs && lane == 0) rhs[r] = f;
 }
 
 }  // namespace
@@ -544,7 +553,7 @@ int general_assemble(anigpu_ctx* h, int opA, int opB, int kind, const double* D,
                             ANIGPU_F64, nt, w->XY, Fdata, w->F));
         F = w->F;
     }
-    general_gather_kernel<<<grid_for(h->ndof, 128), 128, 0, s>>>(
+    general_gather_kernel<<<grid_for(h->ndof * 32, 256), 256, 0, s>>>(
         h->ndof, (int)nloc, h->rowptr, h->col, w->inc_ptr, w->inc, h->edofs, w->sign, w->A, F, h->dir_mask, h->dir_bc,
         h->has_dirichlet ? 1 : 0, h->bc_nonzero ? 1 : 0, vals, rhs, h->d_status);
     ANI_LAUNCHED(h);
