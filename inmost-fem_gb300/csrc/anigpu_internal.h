@@ -129,6 +129,8 @@ struct anigpu_ctx {
     std::vector<void*> extra_allocs;
     // device copies of reference-element tables, keyed by 100*space + order
     std::vector<std::pair<int, double*>> basis_dev;
+    // lengths of the cached FP64 reference-tensor term lists (key as in basis_dev)
+    std::vector<std::pair<int, int>> reft_len;
 };
 // device table for (space, order): q*nf values then q*nf*3 gradients, then q weights
 int get_basis_dev(anigpu_ctx* h, int space, int order, const double** dev, ScalarBasisTable* host, int face = -1);

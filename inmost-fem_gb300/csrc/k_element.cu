@@ -13,6 +13,7 @@
 
 #include "anigpu_internal.h"
 #include "basis_eval.h"
+#include "fp_convert.cuh"
 #include "quad_tables.h"
 
 namespace {
@@ -334,6 +335,218 @@ __global__ void __launch_bounds__(128) fem3dtet_reftensor_kernel(int64_t nt, con
     }
 }
 
+// The same reference-tensor form with lanes over tets: every thread owns one tet (its M in
+// registers) and all threads walk the entries in the same order, so the walk is warp-uniform.
+// FP32: dense rows of T read as broadcast vectors.  FP64 (bound by the FP64 FMA rate): only the
+// non-zero terms of T, a flat list of (value, code) with code = m-index | last-term flag << 4 |
+// ib << 8 | ia << 20 -- the exact zeros of the reference tensor (about half of them for P2) cost
+// nothing.  Entries are staged per warp in shared memory (row stride nent + 1) and written out as
+// one contiguous, coalesced range of 32 element matrices.
+// cofactors C (PSI = C / det) and det of the edge matrix m = [X1-X0, X2-X0, X3-X0] (tet_cofactors)
+template <typename R>
+__device__ __forceinline__ R cofactors_of(const R* m, R* C) {
+#define M_(I, J) m[(I) + 3 * (J)]
+    C[0] = M_(1, 1) * M_(2, 2) - M_(1, 2) * M_(2, 1);
+    C[1] = M_(1, 2) * M_(2, 0) - M_(1, 0) * M_(2, 2);
+    C[2] = M_(1, 0) * M_(2, 1) - M_(1, 1) * M_(2, 0);
+#pragma unroll
+    for (int i = 1; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+            C[j + 3 * i] = M_((i + 1) % 3, (j + 1) % 3) * M_((i + 2) % 3, (j + 2) % 3) -
+                           M_((i + 1) % 3, (j + 2) % 3) * M_((i + 2) % 3, (j + 1) % 3);
+    return M_(0, 0) * C[0] + M_(0, 1) * C[1] + M_(0, 2) * C[2];
+#undef M_
+}
+
+// M = scale L_B^T D L_A with L = C^T (GRAD) or the 1x1 identity (IDEN), in the host's order of
+// the M terms (m-major; upper triangle when SYM); Dm(k, j) = D(k, j), zero outside dB x dA
+template <typename R, int RS, bool SYM>
+__device__ __forceinline__ void reft_m(const R* C, R scale, const R (&Dm)[3][3], int dA, int dB, int gradA, int gradB,
+                                       R (&M)[RS]) {
+    const int rA = gradA ? 3 : 1, rB = gradB ? 3 : 1;
+    R W[3][3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int mp = 0; mp < 3; ++mp) {
+            R w = R(0);
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                if (k >= dB || j >= dA) continue;
+                const R la = gradA ? C[mp + 3 * j] : (j == mp ? R(1) : R(0));
+                w += Dm[k][j] * la;
+            }
+            W[k][mp] = w;
+        }
+#pragma unroll
+    for (int m = 0; m < 3; ++m)
+#pragma unroll
+        for (int mp = 0; mp < 3; ++mp) {
+            if (m >= rB || mp >= rA || (SYM && mp < m)) continue;
+            R v = R(0);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                if (k >= dB) continue;
+                const R lb = gradB ? C[m + 3 * k] : (k == m ? R(1) : R(0));
+                v += lb * W[k][mp];
+            }
+            const int c = RS == 9 ? 3 * m + mp : RS == 6 ? 3 * m - m * (m - 1) / 2 + mp - m : RS == 3 ? m + mp : 0;
+            M[c] = scale * v;
+        }
+}
+
+// M of tet t in FP64 (the parity arithmetic)
+template <int RS, bool SYM>
+__device__ __forceinline__ void reft_m64(const double* X, int64_t t, int kind, const double* D, int dA, int dB,
+                                         int gradA, int gradB, int face, double (&M)[RS]) {
+    double e[9], C[9];
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int i = 0; i < 3; ++i) e[i + 3 * c] = X[3 * (c + 1) + i] - X[i];
+    const double det = cofactors_of(e, C);
+    const double mes = face >= 0 ? face_area(X, face) : fabs(det) / 6.0;
+    const double inv = 1.0 / det;
+    const double scale = mes * (gradA ? inv : 1.0) * (gradB ? inv : 1.0);
+    double Dm[3][3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) Dm[k][j] = (k < dB && j < dA) ? tensor_at(kind, D, t, 0, 1, dA, dB, k, j) : 0.0;
+    reft_m<double, RS, SYM>(C, scale, Dm, dA, dB, gradA, gradB, M);
+}
+
+// M of tet t for FP32 output: edges in FP64 (nine subtractions), everything after them in FP32
+// (FP64 -> FP32 by the integer conversion); a badly shaped tet (|det| <= 0.05 |e1||e2||e3|) is
+// redone in FP64
+template <int RS, bool SYM>
+__device__ __forceinline__ void reft_m32(const double* X, int64_t t, int kind, const double* D, int dA, int dB,
+                                         int gradA, int gradB, int face, float (&M)[RS]) {
+    float e[9], C[9];
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int i = 0; i < 3; ++i) e[i + 3 * c] = d2f_rn(X[3 * (c + 1) + i] - X[i]);
+    const float det = cofactors_of(e, C);
+    const float l0 = e[0] * e[0] + e[1] * e[1] + e[2] * e[2];
+    const float l1 = e[3] * e[3] + e[4] * e[4] + e[5] * e[5];
+    const float l2 = e[6] * e[6] + e[7] * e[7] + e[8] * e[8];
+    if (det * det > 0.0025f * l0 * l1 * l2) {
+        const float mes = face >= 0 ? d2f_rn(face_area(X, face)) : fabsf(det) * (1.0f / 6.0f);
+        const float inv = 1.0f / det;
+        const float scale = mes * (gradA ? inv : 1.0f) * (gradB ? inv : 1.0f);
+        float Dm[3][3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+                Dm[k][j] = (k < dB && j < dA) ? d2f_rn(tensor_at(kind, D, t, 0, 1, dA, dB, k, j)) : 0.0f;
+        reft_m<float, RS, SYM>(C, scale, Dm, dA, dB, gradA, gradB, M);
+    } else {
+        double M64[RS];
+        reft_m64<RS, SYM>(X, t, kind, D, dA, dB, gradA, gradB, face, M64);
+#pragma unroll
+        for (int k = 0; k < RS; ++k) M[k] = __double2float_rn(M64[k]);
+    }
+}
+
+template <int RS>
+__device__ __forceinline__ double select_m(const double (&M)[RS], int k) {
+    double v = M[0];
+#pragma unroll
+    for (int j = 1; j < RS; ++j) v = k == j ? M[j] : v;
+    return v;
+}
+
+template <typename Real, int RS, bool SYM>
+__global__ void __launch_bounds__(128) fem3dtet_reftensor_lanes_kernel(int64_t nt, const double* __restrict__ XY,
+                                                                       int kind, const double* __restrict__ D, int dA,
+                                                                       int dB, int gradA, int gradB, int nfA, int nfB,
+                                                                       int face, int nlist, const double* __restrict__ T,
+                                                                       Real* __restrict__ A) {
+    extern __shared__ __align__(16) double lsm[];
+    constexpr int RSP = (RS + 3) & ~3;
+    constexpr bool LIST = sizeof(Real) == 8;
+    const int nent = nfA * nfB, ostride = nent + 1;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // FP32: nlist rows of RSP values, then nlist codes (ib | ia << 16); FP64: four groups of nlist
+    // terms, their values, then their codes
+    Real* sT = reinterpret_cast<Real*>(lsm);
+    const int nval = LIST ? 4 * nlist : nlist * RSP;
+    const int ncode = LIST ? 4 * nlist : nlist;
+    uint32_t* sCode = reinterpret_cast<uint32_t*>(sT + nval);
+    Real* sOut = reinterpret_cast<Real*>(lsm + (((size_t)nval * sizeof(Real) + 4 * (size_t)ncode + 15) / 16) * 2) +
+                 (size_t)warp * 32 * ostride;
+    for (int i = threadIdx.x; i < nval; i += blockDim.x) sT[i] = Real(T[i]);
+    for (int i = threadIdx.x; i < ncode; i += blockDim.x) sCode[i] = (uint32_t)T[nval + i];
+    __syncthreads();
+    Real* myOut = sOut + (size_t)lane * ostride;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t wbase = (int64_t)blockIdx.x * blockDim.x + warp * 32; wbase < nt; wbase += stride) {
+        const int64_t t = wbase + lane;
+        const int64_t tc = t < nt ? t : nt - 1;  // lanes past the end compute the last tet again
+        if constexpr (LIST) {
+            double M[RS];
+            reft_m64<RS, SYM>(XY + 12 * tc, tc, kind, D, dA, dB, gradA, gradB, face, M);
+            // four independent streams over the term list (rows split into four groups of equal
+            // padded length; padding terms are zeros without a row end)
+            double s[4] = {0.0, 0.0, 0.0, 0.0};
+            for (int j = 0; j < nlist; ++j) {
+#pragma unroll
+                for (int g = 0; g < 4; ++g) {
+                    const uint32_t code = sCode[g * nlist + j];
+                    s[g] = fma(select_m<RS>(M, (int)(code & 15u)), (double)sT[g * nlist + j], s[g]);
+                    if (code & 16u) {
+                        const int ib = (code >> 8) & 0xfff, ia = code >> 20;
+                        myOut[ib + nfB * ia] = Real(s[g]);
+                        if (SYM) myOut[ia + nfB * ib] = Real(s[g]);
+                        s[g] = 0.0;
+                    }
+                }
+            }
+        } else {
+            float Mf[RS];
+            reft_m32<RS, SYM>(XY + 12 * tc, tc, kind, D, dA, dB, gradA, gradB, face, Mf);
+#pragma unroll 4
+            for (int e = 0; e < nlist; ++e) {
+                const Real* Te = sT + (size_t)e * RSP;
+                Real tv[RSP];
+#pragma unroll
+                for (int q = 0; q < RSP / 4; ++q) {
+                    const float4 w = reinterpret_cast<const float4*>(Te)[q];
+                    tv[4 * q] = w.x;
+                    tv[4 * q + 1] = w.y;
+                    tv[4 * q + 2] = w.z;
+                    tv[4 * q + 3] = w.w;
+                }
+                Real acc = Mf[0] * tv[0];
+#pragma unroll
+                for (int k = 1; k < RS; ++k) acc = fma(Mf[k], tv[k], acc);
+                const uint32_t code = sCode[e];
+                const int ib = code & 0xffff, ia = code >> 16;
+                myOut[ib + nfB * ia] = acc;
+                if (SYM) myOut[ia + nfB * ib] = acc;
+            }
+        }
+        __syncwarp();
+        const int ntw = (int)(nt - wbase < 32 ? nt - wbase : 32);
+        Real* gout = A + (size_t)nent * wbase;
+        int tl = lane / nent, el = lane - tl * nent;
+        const int step_t = 32 / nent, step_e = 32 - step_t * nent;
+        for (int idx = lane; idx < ntw * nent; idx += 32) {
+            gout[idx] = sOut[(size_t)tl * ostride + el];
+            tl += step_t;
+            el += step_e;
+            if (el >= nent) {
+                el -= nent;
+                ++tl;
+            }
+        }
+        __syncwarp();
+    }
+}
+
 __global__ void quad_points_kernel(int64_t nt, int q, const double* __restrict__ pts, const double* __restrict__ XY,
                                    double* __restrict__ XYG) {
     const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -602,8 +815,21 @@ int get_basis_dev(anigpu_ctx* h, int space, int order, const double** dev, Scala
 }
 
 // reference tensors T(ib, ia, m, m') = sum_n w_n Vhat_n(m, ib) Uhat_n(m', ia) of a scalar operator
-// pair on the rule of `order` (over face `face` when face >= 0), cached per handle; then the
-// two-phase kernel above
+// pair on the rule of `order` (over face `face` when face >= 0), cached per handle in the layout of
+// the kernel that uses them; then the kernel: lanes over tets for element matrices of at most
+// kLanesMaxEnt entries, lanes over entries above
+constexpr int kLanesMaxEnt = 100;
+
+template <typename Real, int RS, bool SYM>
+static int run_lanes(anigpu_ctx* h, unsigned grid, size_t smem, int64_t nt, const double* XY, int kind, const double* D,
+                     int dA, int dB, int gradA, int gradB, int nfA, int nfB, int face, int nlist, const double* T,
+                     void* A) {
+    auto kern = fem3dtet_reftensor_lanes_kernel<Real, RS, SYM>;
+    ANI_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<grid, 128, smem, h->stream>>>(nt, XY, kind, D, dA, dB, gradA, gradB, nfA, nfB, face, nlist, T, (Real*)A);
+    return ANIGPU_OK;
+}
+
 static int launch_reftensor(anigpu_ctx* h, int opA, int opB, int order, int face, const ScalarBasisTable& hA,
                             const ScalarBasisTable& hB, int kind, int precision, int64_t nt, const double* XY,
                             const double* D, void* A) {
@@ -611,15 +837,22 @@ static int launch_reftensor(anigpu_ctx* h, int opA, int opB, int order, int face
     const int rA = gradA ? 3 : 1, rB = gradB ? 3 : 1, rr = rA * rB;
     const int nfA = hA.nf, nfB = hB.nf, q = hA.q;
     const int dA = gradA ? 3 : 1, dB = gradB ? 3 : 1;
+    const bool f32 = precision == ANIGPU_F32;
     // same operator and a symmetric tensor: symmetric element matrix (upper triangle only)
     const int sym = opA == opB && (kind == ANIGPU_TENSOR_NULL || kind == ANIGPU_TENSOR_CONST_SCALAR ||
                                    kind == ANIGPU_TENSOR_TET_SCALAR || kind == ANIGPU_TENSOR_TET_SYM);
     const int rs = sym ? (rA == 3 ? 6 : 1) : rr;
     const int nrow = sym ? nfA * (nfA + 1) / 2 : nfA * nfB;
-    const int key = -(1 + opA + 128 * (opB + 128 * (order + 32 * (face + 1 + 8 * sym))));
+    const bool lanes = nfA * nfB <= kLanesMaxEnt;
+    const int layout = lanes ? (f32 ? 1 : 2) : 0;
+    const int key = -(1 + opA + 128 * (opB + 128 * (order + 32 * (face + 1 + 8 * (sym + 2 * layout)))));
+    const int rsp = (rs + 3) & ~3;
     const double* T = nullptr;
+    int nlist = 0;
     for (auto& kv : h->basis_dev)
         if (kv.first == key) T = kv.second;
+    for (auto& kv : h->reft_len)
+        if (kv.first == key) nlist = kv.second;
     if (!T) {
         std::vector<double> hT((size_t)nfA * nfB * rr, 0.0);
         for (int ia = 0; ia < nfA; ++ia)
@@ -634,9 +867,11 @@ static int launch_reftensor(anigpu_ctx* h, int opA, int opB, int order, int face
                         }
                         hT[((size_t)ib + (size_t)nfB * ia) * rr + m * rA + mp] = s;
                     }
+        // rows: (ib, ia) and rs coefficients of M; symmetric: pairs ib <= ia, off-diagonal M terms
+        // carrying T(m, m') + T(m', m)
+        std::vector<double> rows((size_t)nrow * rs);
+        std::vector<uint32_t> rcode(nrow);
         if (sym) {
-            // pairs ib <= ia; off-diagonal M terms carry T(m, m') + T(m', m)
-            std::vector<double> hS((size_t)nrow * (rs + 1), 0.0);
             int pr = 0;
             for (int ia = 0; ia < nfA; ++ia)
                 for (int ib = 0; ib <= ia; ++ib, ++pr) {
@@ -644,32 +879,114 @@ static int launch_reftensor(anigpu_ctx* h, int opA, int opB, int order, int face
                     int c = 0;
                     for (int m = 0; m < rB; ++m)
                         for (int mp = m; mp < rA; ++mp)
-                            hS[(size_t)pr * rs + c++] = mp == m ? Te[m * rA + m] : Te[m * rA + mp] + Te[mp * rA + m];
-                    hS[(size_t)nrow * rs + pr] = (double)(ib | (ia << 16));
+                            rows[(size_t)pr * rs + c++] = mp == m ? Te[m * rA + m] : Te[m * rA + mp] + Te[mp * rA + m];
+                    rcode[pr] = (uint32_t)(ib | (ia << 16));
                 }
-            hT.swap(hS);
+        } else {
+            for (int e = 0; e < nrow; ++e) {
+                std::copy(&hT[(size_t)e * rr], &hT[(size_t)e * rr] + rr, &rows[(size_t)e * rs]);
+                rcode[e] = (uint32_t)((e % nfB) | ((e / nfB) << 16));
+            }
+        }
+        std::vector<double> out;
+        if (layout == 0) {
+            out = rows;
+            if (sym)
+                for (int e = 0; e < nrow; ++e) out.push_back((double)rcode[e]);
+        } else if (layout == 1) {
+            out.assign((size_t)nrow * rsp, 0.0);
+            for (int e = 0; e < nrow; ++e)
+                for (int k = 0; k < rs; ++k) out[(size_t)e * rsp + k] = rows[(size_t)e * rs + k];
+            for (int e = 0; e < nrow; ++e) out.push_back((double)rcode[e]);
+        } else {
+            // non-zero terms only (a row with none keeps one zero term, so that it is written); the
+            // rows split into four consecutive groups of about equal term count, each padded with
+            // zero terms (no row end) to the longest group's length
+            double tmax = 0.0;
+            for (double v : rows) tmax = std::max(tmax, std::fabs(v));
+            std::vector<double> vals;
+            std::vector<uint32_t> codes;
+            std::vector<size_t> row_end(nrow);
+            for (int e = 0; e < nrow; ++e) {
+                const uint32_t ib = rcode[e] & 0xffffu, ia = rcode[e] >> 16;
+                const size_t first = vals.size();
+                for (int k = 0; k < rs; ++k) {
+                    const double v = rows[(size_t)e * rs + k];
+                    if (std::fabs(v) <= 1e-14 * tmax) continue;
+                    vals.push_back(v);
+                    codes.push_back((uint32_t)k | (ib << 8) | (ia << 20));
+                }
+                if (vals.size() == first) {
+                    vals.push_back(0.0);
+                    codes.push_back((ib << 8) | (ia << 20));
+                }
+                codes.back() |= 16u;
+                row_end[e] = vals.size();
+            }
+            size_t gb[5] = {0, 0, 0, 0, vals.size()};
+            for (int g = 1; g < 4; ++g) {
+                const size_t target = vals.size() * g / 4;
+                size_t b = gb[g - 1];
+                for (int e = 0; e < nrow; ++e)
+                    if (row_end[e] <= target) b = std::max(b, row_end[e]);
+                gb[g] = b;
+            }
+            size_t L = 1;
+            for (int g = 0; g < 4; ++g) L = std::max(L, gb[g + 1] - gb[g]);
+            out.assign(8 * L, 0.0);
+            for (int g = 0; g < 4; ++g)
+                for (size_t j = gb[g]; j < gb[g + 1]; ++j) {
+                    out[g * L + (j - gb[g])] = vals[j];
+                    out[4 * L + g * L + (j - gb[g])] = (double)codes[j];
+                }
+            nlist = (int)L;
+            h->reft_len.push_back({key, nlist});
         }
         double* d = nullptr;
-        ANI_CUDA(h, cudaMalloc((void**)&d, hT.size() * sizeof(double)));
-        ANI_CUDA(h, cudaMemcpy(d, hT.data(), hT.size() * sizeof(double), cudaMemcpyHostToDevice));
+        ANI_CUDA(h, cudaMalloc((void**)&d, out.size() * sizeof(double)));
+        ANI_CUDA(h, cudaMemcpy(d, out.data(), out.size() * sizeof(double), cudaMemcpyHostToDevice));
         h->basis_dev.push_back({key, d});
         T = d;
     }
-    const size_t rsz = precision == ANIGPU_F32 ? sizeof(float) : sizeof(double);
-    constexpr int kRT = 128;
-    const size_t smem = rsz * ((size_t)nrow * rs + (size_t)kRT * 9 + (size_t)(kRT / 32) * nfA * nfB) +
-                        (sym ? sizeof(int) * nrow : 0);
+    if (layout == 1) nlist = nrow;
     int dev_sms = 148;
     cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, h->device);
-    const unsigned grid = (unsigned)std::min<int64_t>((nt + kRT - 1) / kRT, (int64_t)dev_sms * 8);
-    if (precision == ANIGPU_F32) {
-        ANI_CUDA(h, cudaFuncSetAttribute(fem3dtet_reftensor_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        fem3dtet_reftensor_kernel<float><<<grid, kRT, smem, h->stream>>>(nt, XY, kind, D, dA, dB, gradA, gradB, nfA, nfB,
-                                                                          face, sym, T, (float*)A);
+    const size_t rsz = f32 ? sizeof(float) : sizeof(double);
+    constexpr int kRT = 128;
+    int rc = ANIGPU_OK;
+    if (lanes) {
+        const size_t nval = f32 ? (size_t)nlist * rsp : 4 * (size_t)nlist;
+        const size_t ncode = f32 ? (size_t)nlist : 4 * (size_t)nlist;
+        const size_t smem = (nval * rsz + 4 * ncode + 15) / 16 * 16 + rsz * (size_t)kRT * (nfA * nfB + 1);
+        const unsigned grid = (unsigned)std::min<int64_t>((nt + kRT - 1) / kRT, (int64_t)dev_sms * 16);
+#define RUN_LANES(R, RSV, SY) \
+    rc = run_lanes<R, RSV, SY>(h, grid, smem, nt, XY, kind, D, dA, dB, gradA, gradB, nfA, nfB, face, nlist, T, A)
+        if (f32) {
+            if (rs == 1) { if (sym) RUN_LANES(float, 1, true); else RUN_LANES(float, 1, false); }
+            else if (rs == 3) RUN_LANES(float, 3, false);
+            else if (rs == 6) RUN_LANES(float, 6, true);
+            else RUN_LANES(float, 9, false);
+        } else {
+            if (rs == 1) { if (sym) RUN_LANES(double, 1, true); else RUN_LANES(double, 1, false); }
+            else if (rs == 3) RUN_LANES(double, 3, false);
+            else if (rs == 6) RUN_LANES(double, 6, true);
+            else RUN_LANES(double, 9, false);
+        }
+#undef RUN_LANES
+        if (rc) return rc;
     } else {
-        ANI_CUDA(h, cudaFuncSetAttribute(fem3dtet_reftensor_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        fem3dtet_reftensor_kernel<double><<<grid, kRT, smem, h->stream>>>(nt, XY, kind, D, dA, dB, gradA, gradB, nfA,
-                                                                           nfB, face, sym, T, (double*)A);
+        const size_t smem = rsz * ((size_t)nrow * rs + (size_t)kRT * 9 + (size_t)(kRT / 32) * nfA * nfB) +
+                            (sym ? sizeof(int) * nrow : 0);
+        const unsigned grid = (unsigned)std::min<int64_t>((nt + kRT - 1) / kRT, (int64_t)dev_sms * 8);
+        if (f32) {
+            ANI_CUDA(h, cudaFuncSetAttribute(fem3dtet_reftensor_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            fem3dtet_reftensor_kernel<float><<<grid, kRT, smem, h->stream>>>(nt, XY, kind, D, dA, dB, gradA, gradB, nfA,
+                                                                              nfB, face, sym, T, (float*)A);
+        } else {
+            ANI_CUDA(h, cudaFuncSetAttribute(fem3dtet_reftensor_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            fem3dtet_reftensor_kernel<double><<<grid, kRT, smem, h->stream>>>(nt, XY, kind, D, dA, dB, gradA, gradB, nfA,
+                                                                               nfB, face, sym, T, (double*)A);
+        }
     }
     ANI_LAUNCHED(h);
     return ANIGPU_OK;
