@@ -335,13 +335,6 @@ __global__ void __launch_bounds__(128) fem3dtet_reftensor_kernel(int64_t nt, con
     }
 }
 
-// The same reference-tensor form with lanes over tets: every thread owns one tet (its M in
-// registers) and all threads walk the entries in the same order, so the walk is warp-uniform.
-// FP32: dense rows of T read as broadcast vectors.  FP64 (bound by the FP64 FMA rate): only the
-// non-zero terms of T, a flat list of (value, code) with code = m-index | last-term flag << 4 |
-// ib << 8 | ia << 20 -- the exact zeros of the reference tensor (about half of them for P2) cost
-// nothing.  Entries are staged per warp in shared memory (row stride nent + 1) and written out as
-// one contiguous, coalesced range of 32 element matrices.
 // cofactors C (PSI = C / det) and det of the edge matrix m = [X1-X0, X2-X0, X3-X0] (tet_cofactors)
 template <typename R>
 __device__ __forceinline__ R cofactors_of(const R* m, R* C) {
@@ -400,15 +393,21 @@ __device__ __forceinline__ void reft_m(const R* C, R scale, const R (&Dm)[3][3],
 template <int RS, bool SYM>
 __device__ __forceinline__ void reft_m64(const double* X, int64_t t, int kind, const double* D, int dA, int dB,
                                          int gradA, int gradB, int face, double (&M)[RS]) {
-    double e[9], C[9];
+    double C[9];
+    double scale;
+    if (face >= 0 && !gradA && !gradB) {
+        scale = face_area(X, face);  // face integral of values: no Jacobian needed
+    } else {
+        double e[9];
 #pragma unroll
-    for (int c = 0; c < 3; ++c)
+        for (int c = 0; c < 3; ++c)
 #pragma unroll
-        for (int i = 0; i < 3; ++i) e[i + 3 * c] = X[3 * (c + 1) + i] - X[i];
-    const double det = cofactors_of(e, C);
-    const double mes = face >= 0 ? face_area(X, face) : fabs(det) / 6.0;
-    const double inv = 1.0 / det;
-    const double scale = mes * (gradA ? inv : 1.0) * (gradB ? inv : 1.0);
+            for (int i = 0; i < 3; ++i) e[i + 3 * c] = X[3 * (c + 1) + i] - X[i];
+        const double det = cofactors_of(e, C);
+        const double mes = face >= 0 ? face_area(X, face) : fabs(det) / 6.0;
+        const double inv = 1.0 / det;
+        scale = mes * (gradA ? inv : 1.0) * (gradB ? inv : 1.0);
+    }
     double Dm[3][3];
 #pragma unroll
     for (int k = 0; k < 3; ++k)
@@ -451,6 +450,16 @@ __device__ __forceinline__ void reft_m32(const double* X, int64_t t, int kind, c
     }
 }
 
+// The same reference-tensor form with lanes over tets: every thread forms the M of one tet in
+// registers, and the 16 lanes of a half-warp walk the entries in the same order (uniform loads
+// and branches within the half-warp).
+// FP32: dense rows of T read as broadcast vectors.  FP64 (bound by the FP64 FMA rate): only the
+// non-zero terms of T, a flat list of (value, code) with code = m-index | last-term flag << 4 |
+// ib << 8 | ia << 20 -- the exact zeros of the reference tensor (about half of them for P2) cost
+// nothing.  A warp owns 32 tets and works on them in two halves of 16: each half-warp takes one
+// part of the entry list for all 16 tets (M passed by shuffle); the entries are staged in shared
+// memory (row stride nent + 1) and written out as one contiguous, coalesced range of 16 element
+// matrices.
 template <int RS>
 __device__ __forceinline__ double select_m(const double (&M)[RS], int k) {
     double v = M[0];
@@ -477,73 +486,103 @@ __global__ void __launch_bounds__(128) fem3dtet_reftensor_lanes_kernel(int64_t n
     const int ncode = LIST ? 4 * nlist : nlist;
     uint32_t* sCode = reinterpret_cast<uint32_t*>(sT + nval);
     Real* sOut = reinterpret_cast<Real*>(lsm + (((size_t)nval * sizeof(Real) + 4 * (size_t)ncode + 15) / 16) * 2) +
-                 (size_t)warp * 32 * ostride;
+                 (size_t)warp * 16 * ostride;
     for (int i = threadIdx.x; i < nval; i += blockDim.x) sT[i] = Real(T[i]);
     for (int i = threadIdx.x; i < ncode; i += blockDim.x) sCode[i] = (uint32_t)T[nval + i];
     __syncthreads();
-    Real* myOut = sOut + (size_t)lane * ostride;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t wbase = (int64_t)blockIdx.x * blockDim.x + warp * 32; wbase < nt; wbase += stride) {
         const int64_t t = wbase + lane;
         const int64_t tc = t < nt ? t : nt - 1;  // lanes past the end compute the last tet again
+        // M of this lane's tet; then two halves of 16 tets: lane l works on tet (l & 15) of the
+        // half, on the first (l < 16) or second part of the entry list, with that tet's M shuffled
+        // from its owner
+        Real Mo[RS];
         if constexpr (LIST) {
-            double M[RS];
-            reft_m64<RS, SYM>(XY + 12 * tc, tc, kind, D, dA, dB, gradA, gradB, face, M);
-            // four independent streams over the term list (rows split into four groups of equal
-            // padded length; padding terms are zeros without a row end)
-            double s[4] = {0.0, 0.0, 0.0, 0.0};
-            for (int j = 0; j < nlist; ++j) {
+            double M64[RS];
+            reft_m64<RS, SYM>(XY + 12 * tc, tc, kind, D, dA, dB, gradA, gradB, face, M64);
 #pragma unroll
-                for (int g = 0; g < 4; ++g) {
-                    const uint32_t code = sCode[g * nlist + j];
-                    s[g] = fma(select_m<RS>(M, (int)(code & 15u)), (double)sT[g * nlist + j], s[g]);
-                    if (code & 16u) {
-                        const int ib = (code >> 8) & 0xfff, ia = code >> 20;
-                        myOut[ib + nfB * ia] = Real(s[g]);
-                        if (SYM) myOut[ia + nfB * ib] = Real(s[g]);
-                        s[g] = 0.0;
+            for (int k = 0; k < RS; ++k) Mo[k] = M64[k];
+        } else {
+            float M32[RS];
+            reft_m32<RS, SYM>(XY + 12 * tc, tc, kind, D, dA, dB, gradA, gradB, face, M32);
+#pragma unroll
+            for (int k = 0; k < RS; ++k) Mo[k] = M32[k];
+        }
+        const int part = lane >> 4;
+        Real* myOut = sOut + (size_t)(lane & 15) * ostride;
+        for (int half = 0; half < 2; ++half) {
+            Real M[RS];
+#pragma unroll
+            for (int k = 0; k < RS; ++k) M[k] = __shfl_sync(0xffffffffu, Mo[k], (lane & 15) + 16 * half);
+            if constexpr (LIST) {
+                // two independent streams per lane over its part's two term groups (rows split
+                // into four groups of equal padded length; padding terms are zeros without a row end)
+                double s0 = 0.0, s1 = 0.0;
+                const uint32_t* c0 = sCode + (2 * part) * nlist;
+                const uint32_t* c1 = c0 + nlist;
+                const Real* v0 = sT + (2 * part) * nlist;
+                const Real* v1 = v0 + nlist;
+                for (int j = 0; j < nlist; ++j) {
+                    const uint32_t a = c0[j], b = c1[j];
+                    s0 = fma(select_m<RS>(M, (int)(a & 15u)), (double)v0[j], s0);
+                    s1 = fma(select_m<RS>(M, (int)(b & 15u)), (double)v1[j], s1);
+                    if (a & 16u) {
+                        const int ib = (a >> 8) & 0xfff, ia = a >> 20;
+                        myOut[ib + nfB * ia] = Real(s0);
+                        if (SYM) myOut[ia + nfB * ib] = Real(s0);
+                        s0 = 0.0;
+                    }
+                    if (b & 16u) {
+                        const int ib = (b >> 8) & 0xfff, ia = b >> 20;
+                        myOut[ib + nfB * ia] = Real(s1);
+                        if (SYM) myOut[ia + nfB * ib] = Real(s1);
+                        s1 = 0.0;
                     }
                 }
-            }
-        } else {
-            float Mf[RS];
-            reft_m32<RS, SYM>(XY + 12 * tc, tc, kind, D, dA, dB, gradA, gradB, face, Mf);
+            } else {
+                const int hrows = (nlist + 1) >> 1;
+                const int e0 = part * hrows;
 #pragma unroll 4
-            for (int e = 0; e < nlist; ++e) {
-                const Real* Te = sT + (size_t)e * RSP;
-                Real tv[RSP];
+                for (int r = 0; r < hrows; ++r) {
+                    const int e = e0 + r;
+                    if (e >= nlist) break;
+                    const Real* Te = sT + (size_t)e * RSP;
+                    Real tv[RSP];
 #pragma unroll
-                for (int q = 0; q < RSP / 4; ++q) {
-                    const float4 w = reinterpret_cast<const float4*>(Te)[q];
-                    tv[4 * q] = w.x;
-                    tv[4 * q + 1] = w.y;
-                    tv[4 * q + 2] = w.z;
-                    tv[4 * q + 3] = w.w;
+                    for (int q = 0; q < RSP / 4; ++q) {
+                        const float4 w = reinterpret_cast<const float4*>(Te)[q];
+                        tv[4 * q] = w.x;
+                        tv[4 * q + 1] = w.y;
+                        tv[4 * q + 2] = w.z;
+                        tv[4 * q + 3] = w.w;
+                    }
+                    Real acc = M[0] * tv[0];
+#pragma unroll
+                    for (int k = 1; k < RS; ++k) acc = fma(M[k], tv[k], acc);
+                    const uint32_t code = sCode[e];
+                    const int ib = code & 0xffff, ia = code >> 16;
+                    myOut[ib + nfB * ia] = acc;
+                    if (SYM) myOut[ia + nfB * ib] = acc;
                 }
-                Real acc = Mf[0] * tv[0];
-#pragma unroll
-                for (int k = 1; k < RS; ++k) acc = fma(Mf[k], tv[k], acc);
-                const uint32_t code = sCode[e];
-                const int ib = code & 0xffff, ia = code >> 16;
-                myOut[ib + nfB * ia] = acc;
-                if (SYM) myOut[ia + nfB * ib] = acc;
             }
-        }
-        __syncwarp();
-        const int ntw = (int)(nt - wbase < 32 ? nt - wbase : 32);
-        Real* gout = A + (size_t)nent * wbase;
-        int tl = lane / nent, el = lane - tl * nent;
-        const int step_t = 32 / nent, step_e = 32 - step_t * nent;
-        for (int idx = lane; idx < ntw * nent; idx += 32) {
-            gout[idx] = sOut[(size_t)tl * ostride + el];
-            tl += step_t;
-            el += step_e;
-            if (el >= nent) {
-                el -= nent;
-                ++tl;
+            __syncwarp();
+            const int64_t hbase = wbase + 16 * half;
+            const int ntw = (int)(nt - hbase < 16 ? (nt - hbase > 0 ? nt - hbase : 0) : 16);
+            Real* gout = A + (size_t)nent * hbase;
+            int tl = lane / nent, el = lane - tl * nent;
+            const int step_t = 32 / nent, step_e = 32 - step_t * nent;
+            for (int idx = lane; idx < ntw * nent; idx += 32) {
+                gout[idx] = sOut[(size_t)tl * ostride + el];
+                tl += step_t;
+                el += step_e;
+                if (el >= nent) {
+                    el -= nent;
+                    ++tl;
+                }
             }
+            __syncwarp();
         }
-        __syncwarp();
     }
 }
 
@@ -957,7 +996,7 @@ static int launch_reftensor(anigpu_ctx* h, int opA, int opB, int order, int face
     if (lanes) {
         const size_t nval = f32 ? (size_t)nlist * rsp : 4 * (size_t)nlist;
         const size_t ncode = f32 ? (size_t)nlist : 4 * (size_t)nlist;
-        const size_t smem = (nval * rsz + 4 * ncode + 15) / 16 * 16 + rsz * (size_t)kRT * (nfA * nfB + 1);
+        const size_t smem = (nval * rsz + 4 * ncode + 15) / 16 * 16 + rsz * (size_t)(kRT / 2) * (nfA * nfB + 1);
         const unsigned grid = (unsigned)std::min<int64_t>((nt + kRT - 1) / kRT, (int64_t)dev_sms * 16);
 #define RUN_LANES(R, RSV, SY) \
     rc = run_lanes<R, RSV, SY>(h, grid, smem, nt, XY, kind, D, dA, dB, gradA, gradB, nfA, nfB, face, nlist, T, A)
