@@ -380,6 +380,9 @@ def dist_setup(args):
     return world, rank, local, pg
 
 
+REF_FLOPS_PER_TET = 2 * (14 * 10 * 9 + 10 * 10 * 14 * 3)
+
+
 def cpu_baseline(xyz, tets, D6, sample, threads):
     """The reference's element-matrix loop (oracle port of fem3Dtet, P2 GRAD.GRAD,
     per-tet symmetric tensor, order 4) on `sample` tets over `threads` host threads."""
@@ -639,9 +642,14 @@ def run_ours(args):
         threads = os.cpu_count() or 1
         sample = args.cpu_sample or nt
         v, sec = cpu_baseline(xyz, tets, D6, sample, threads)
+        # the reference's default is the serial loop: one host thread on a smaller sample
+        s1 = min(sample, 100000)
+        v1, sec1 = cpu_baseline(xyz, tets, D6, s1, 1)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"fem3Dtet P2 GRAD.GRAD element matrices of the first {sample} tets "
-                         f"({sec:.1f} s), oracle port on {threads} host threads"}
+                         f"({sec:.1f} s), oracle port on {threads} host threads",
+               "single_thread": {"value": v1, "unit": UNIT, "cores": 1,
+                                 "sample": f"first {s1} tets ({sec1:.1f} s), one host thread"}}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -655,7 +663,11 @@ def run_ours(args):
                      "traffic": traffic, "peak_kind": peak_kind,
                      "kernel": "assembly = tet_gram + row_gather (vertex rows, edge rows): 3 launches, "
                                "timed back to back in the timed region",
-                     "algorithmic_bytes": b_alg, "ms": {"tet_prepare": prep_ms, "row_gather": rows_ms}},
+                     "algorithmic_bytes": b_alg, "ms": {"tet_prepare": prep_ms, "row_gather": rows_ms},
+                     # the reference formulation's arithmetic, for context: q*nf*dim^2 MACs for D.U plus
+                     # nf^2*q*dim for V^T.DU (P2, 14 points), 2 FLOPs per MAC
+                     "reference_flops_per_tet": REF_FLOPS_PER_TET,
+                     "reference_tflops_equivalent": REF_FLOPS_PER_TET * value / 1e12},
         "e2e": {"value": world * nt / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
         "gpu_launches": launches,
