@@ -155,7 +155,9 @@ int anigpu_face_quadrature_points(anigpu_handle h, int order, int face, int64_t 
  * or edge) they give three numberings of DOF (component c, scalar DOF s): NATURAL c*nds + s;
  * ANITYPE and BYELEMTYPE: nodes of component 0, 1, 2, then edges of component 0, 1, 2; MINIBLOCKS,
  * DIMUNION and ETDIMBLOCKS: the components of a node or edge together (ncomp*s + c).  Scalar spaces:
- * all equal NATURAL.
+ * all equal NATURAL.  General-path spaces (P0, P3, CR1, B2, B4, ND0, RT0; DOFs of an entity
+ * consecutive in NATURAL): all equal NATURAL except ANITYPE where an entity holds several DOFs
+ * (P3 edges: DOF 0 of every edge, then DOF 1 of every edge).
  * setup: the permutation, the template in the new numbering and the map of every template slot;
  * template: rowptr[ndof+1] / col[nnz] of that template (rows sorted) and perm[ndof] (new index of
  * each NATURAL DOF), any may be NULL; apply: values (precision F32/F64) and right-hand side of an

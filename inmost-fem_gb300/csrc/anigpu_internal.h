@@ -188,6 +188,8 @@ int general_assemble(anigpu_ctx* h, int opA, int opB, int kind, const double* D,
                      int order, double* vals, double* rhs);
 int general_dof_coords(anigpu_ctx* h, double* out);
 const int8_t* general_signs(anigpu_ctx* h);
+// DOFs per entity (node, edge, face, cell) and the first global DOF of each entity block (off[4] = ndof)
+bool general_dof_blocks(anigpu_ctx* h, int per[4], int64_t off[5]);
 // enumerations (k_enum.cu)
 void free_enum(anigpu_ctx* h);
 int enum_setup(anigpu_ctx* h, int type);

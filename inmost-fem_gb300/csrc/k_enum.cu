@@ -16,6 +16,13 @@
 //   MINIBLOCKS: slot (d, j) -> 3j + d
 //   ANITYPE:    slot (d, j) -> j < Ln ? d*Ln + j : 3Ln + d*Le + (j - Ln)   (Ln node columns, Le edge columns)
 // so that a renumbered assembly is one gather of the values.
+//
+// General-path spaces (one scalar variable; DOFs on nodes, edges, faces or cells, the DOFs of an
+// entity consecutive in NATURAL): only ANITYPE, whose key puts DOF_ID before ELEM_ID, differs from
+// NATURAL, and only where an entity holds several DOFs (P3: two per edge).  DOF k of entity E in the
+// block of entity type T goes to off_T + k*count_T + E.  Every entity in a row brings all its DOFs,
+// so the row's columns of type T are m_T entities x per_T DOFs starting at slot b_T, and slot
+// b_T + p*per_T + k moves to b_T + k*m_T + p.
 #include <algorithm>
 
 #include "anigpu_internal.h"
@@ -101,6 +108,74 @@ __global__ void slot_kernel(int64_t n, int kind, int64_t nds, int64_t nv, int nc
     }
 }
 
+struct GenBlocks {
+    int per[4];
+    int64_t off[5];  // off[4] = ndof
+};
+
+__device__ __forceinline__ int gen_type(const GenBlocks& g, int64_t s) {
+    int T = 0;
+#pragma unroll
+    for (int q = 1; q < 4; ++q)
+        if (s >= g.off[q] && g.off[q] < g.off[q + 1]) T = q;
+    return T;
+}
+
+__device__ __forceinline__ int64_t gen_new_index(const GenBlocks& g, int anitype, int64_t s) {
+    if (!anitype) return s;
+    const int T = gen_type(g, s);
+    const int p = g.per[T];
+    if (p <= 1) return s;
+    const int64_t cnt = (g.off[T + 1] - g.off[T]) / p, r = s - g.off[T];
+    return g.off[T] + (r % p) * cnt + r / p;
+}
+
+__global__ void gen_perm_kernel(int64_t n, GenBlocks g, int anitype, int64_t* __restrict__ perm,
+                                const int64_t* __restrict__ rowptr, unsigned long long* __restrict__ len_new) {
+    const int64_t R = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (R >= n) return;
+    const int64_t P = gen_new_index(g, anitype, R);
+    perm[R] = P;
+    len_new[P] = (unsigned long long)(rowptr[R + 1] - rowptr[R]);
+}
+
+// one block per NATURAL row (grid-stride): the row's type boundaries by binary search, then every
+// slot's new position and column
+__global__ void gen_slot_kernel(int64_t n, GenBlocks g, int anitype, const int64_t* __restrict__ rowptr,
+                                const int32_t* __restrict__ col, const int64_t* __restrict__ perm,
+                                const int64_t* __restrict__ rowptr_new, int32_t* __restrict__ col_new,
+                                int64_t* __restrict__ slot) {
+    for (int64_t row = blockIdx.x; row < n; row += gridDim.x) {
+        const int64_t b = rowptr[row], len = rowptr[row + 1] - b;
+        int64_t pos[5];
+#pragma unroll
+        for (int T = 0; T < 5; ++T) {
+            int64_t lo = 0, hi = len;
+            while (lo < hi) {
+                const int64_t mid = (lo + hi) / 2;
+                if (col[b + mid] < g.off[T]) lo = mid + 1;
+                else hi = mid;
+            }
+            pos[T] = lo;
+        }
+        const int64_t nb = rowptr_new[perm[row]];
+        for (int64_t k = threadIdx.x; k < len; k += blockDim.x) {
+            int T = 0;
+#pragma unroll
+            for (int q = 1; q < 4; ++q)
+                if (k >= pos[q]) T = q;
+            const int p = g.per[T];
+            int64_t j = k;
+            if (anitype && p > 1) {
+                const int64_t m = (pos[T + 1] - pos[T]) / p, r = k - pos[T];
+                j = pos[T] + (r % p) * m + r / p;
+            }
+            slot[b + k] = nb + j;
+            col_new[nb + j] = (int32_t)perm[col[b + k]];
+        }
+    }
+}
+
 template <typename Real>
 __global__ void gather_vals_kernel(int64_t nnz, const int64_t* __restrict__ slot, const Real* __restrict__ in,
                                    Real* __restrict__ out) {
@@ -131,7 +206,9 @@ void free_enum(anigpu_ctx* h) {
 int enum_setup(anigpu_ctx* h, int type) {
     if (type < ANIGPU_ENUM_ANITYPE || type > ANIGPU_ENUM_ETDIMBLOCKS) return set_err(h, ANIGPU_ERR_ARG, "enumeration type");
     if (h->space < 0) return set_err(h, ANIGPU_ERR_STATE, "anigpu_problem_setup not called");
-    if (is_general_space(h->space)) return set_err(h, ANIGPU_ERR_UNSUPPORTED, "enumerations for P1, P2 and vector P2");
+    const bool general = is_general_space(h->space);
+    GenBlocks gb{};
+    if (general && !general_dof_blocks(h, gb.per, gb.off)) return set_err(h, ANIGPU_ERR_STATE, "general problem not set up");
     free_enum(h);
     EnumWs* w = new EnumWs();
     h->enum_ws = w;
@@ -147,13 +224,20 @@ int enum_setup(anigpu_ctx* h, int type) {
     unsigned long long* len = nullptr;
     ANI_CUDA(h, cudaMallocAsync((void**)&len, sizeof(unsigned long long) * (w->n + 1), s));
     ANI_CUDA(h, cudaMemsetAsync(len, 0, sizeof(unsigned long long) * (w->n + 1), s));
-    perm_kernel<<<grid_for(w->n, 256), 256, 0, s>>>(w->n, kind, h->nds, h->nv, h->ncomp, w->perm, h->rowptr, len);
+    const int anitype = type == ANIGPU_ENUM_ANITYPE ? 1 : 0;
+    if (general)
+        gen_perm_kernel<<<grid_for(w->n, 256), 256, 0, s>>>(w->n, gb, anitype, w->perm, h->rowptr, len);
+    else
+        perm_kernel<<<grid_for(w->n, 256), 256, 0, s>>>(w->n, kind, h->nds, h->nv, h->ncomp, w->perm, h->rowptr, len);
     ANI_LAUNCHED(h);
     RC_(scan_counts(h, len, w->n, w->rowptr));
     ANI_CUDA(h, cudaFreeAsync(len, s));
     const unsigned blocks = (unsigned)std::min<int64_t>(w->n, 152 * 32);
-    slot_kernel<<<blocks, 128, 0, s>>>(w->n, kind, h->nds, h->nv, h->ncomp, h->rowptr, h->col, h->rowptr_s, h->col_s,
-                                       w->perm, w->rowptr, w->col, w->slot);
+    if (general)
+        gen_slot_kernel<<<blocks, 128, 0, s>>>(w->n, gb, anitype, h->rowptr, h->col, w->perm, w->rowptr, w->col, w->slot);
+    else
+        slot_kernel<<<blocks, 128, 0, s>>>(w->n, kind, h->nds, h->nv, h->ncomp, h->rowptr, h->col, h->rowptr_s,
+                                           h->col_s, w->perm, w->rowptr, w->col, w->slot);
     ANI_LAUNCHED(h);
     ANI_CUDA(h, cudaStreamSynchronize(s));
     return ANIGPU_OK;

@@ -16,9 +16,10 @@
 // swaps them; an ND0 DOF gets the sign + when its local edge (ip0, ip1) runs the global way; an RT0
 // DOF gets + when the tet's outward normal of the face agrees with the global face normal
 // (X_b - X_a) x (X_c - X_a) of the sorted vertex triple a < b < c.
-// Element matrices and right-hand sides come from the fem3Dtet kernel (FP64); one thread per row
-// walks the row's incidences in ascending tet order and adds s_i s_j A_t(i, j) into the row's
-// slots (binary search in the sorted row): deterministic, no atomics.  Dirichlet rows and columns
+// Element matrices and right-hand sides come from the fem3Dtet kernel (FP64); one warp per row
+// walks the row's incidences in ascending tet order, its lanes over the element row's columns, and
+// adds s_i s_j A_t(i, j) into the row's slots (binary search in the sorted row): deterministic, no
+// atomics.  Dirichlet rows and columns
 // follow the vector path: diagonal = number of incident tets, rhs = that number times the value,
 // A(i,k) bc_k moved to the right-hand side of the other rows.
 #include <cub/cub.cuh>
@@ -467,6 +468,17 @@ int general_dof_coords(anigpu_ctx* h, double* out) {
 }
 
 const int8_t* general_signs(anigpu_ctx* h) { return gws(h) ? gws(h)->sign : nullptr; }
+
+bool general_dof_blocks(anigpu_ctx* h, int per[4], int64_t off[5]) {
+    GenWs* w = gws(h);
+    if (!w) return false;
+    for (int T = 0; T < 4; ++T) {
+        per[T] = w->o.per[T];
+        off[T] = w->o.off[T];
+    }
+    off[4] = h->ndof;
+    return true;
+}
 
 namespace {
 

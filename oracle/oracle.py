@@ -418,6 +418,42 @@ def general_numbering(xyz, t, space):
     return gd, sg, ndof
 
 
+def general_blocks(xyz, t, space):
+    """DOFs per entity (node, edge, face, cell) of a general-path space and the first NATURAL DOF of
+    each entity block, off[4] = ndof."""
+    nv, nt = xyz.shape[0], t.shape[0]
+    per, _ = _GEN_LAYOUT[space]
+    ek = np.stack([np.minimum(t[:, _EI], t[:, _EJ]), np.maximum(t[:, _EI], t[:, _EJ])], axis=-1).astype(np.int64)
+    ne = np.unique((ek[..., 0] * nv + ek[..., 1]).reshape(-1)).size
+    ft = np.sort(np.stack([t[:, list(f)] for f in _FV], axis=1), axis=-1).astype(np.int64)
+    nf = np.unique(((ft[..., 0] * nv + ft[..., 1]) * nv + ft[..., 2]).reshape(-1)).size
+    counts = [nv, ne, nf, nt]
+    off = [0]
+    for T in range(4):
+        off.append(off[-1] + counts[T] * per[T])
+    return list(per), off
+
+
+def general_enumeration_perm(per, off, etype):
+    """New index of every NATURAL DOF of a general-path space (one scalar variable) under
+    enumeration etype: the rank of (VAR 0, DIM 0, ELEM_TYPE, ELEM_ID, DOF_ID) in the lexicographic
+    order of that type's key (global_enumerator.h:392-404)."""
+    n = off[4]
+    s = np.arange(n)
+    T = np.zeros(n, dtype=np.int64)
+    for q in range(1, 4):
+        T = np.where(s >= off[q], q, T)
+    p = np.maximum(np.asarray(per)[T], 1)
+    r = s - np.asarray(off)[T]
+    fields = {"VAR": np.zeros(n, dtype=np.int64), "DIM": np.zeros(n, dtype=np.int64), "ELEM_TYPE": T,
+              "ELEM_ID": r // p, "DOF_ID": r % p}
+    keys = [fields[k] for k in _ENUM_KEYS[etype]]
+    order = np.lexsort(keys[::-1])
+    perm = np.empty(n, dtype=np.int64)
+    perm[order] = np.arange(n)
+    return perm
+
+
 def general_assemble(restated, xyz, tets, space, codeA, codeB, kind, D, order, rhs_kind=None, F=None,
                      dirichlet=None):
     """Restatement of the general-path global assembly: signed sum of fem3Dtet element matrices

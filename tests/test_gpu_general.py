@@ -106,3 +106,36 @@ def test_nd0_rt0_reproduce_constant_field(lib, space, opK):
     p4 = anigpu.quadrature(4)[0]
     val = lib.eval_solution(anigpu.IDEN, x, p4).cpu().numpy()
     assert np.abs(val - u0).max() <= 1e-8
+
+
+@pytest.mark.parametrize("space,op", [(3, 32), (9, 94), (6, 62)])
+def test_general_enumerations_match_oracle(lib, space, op):
+    """Every GlobEnumeration type on a general-path system: permutation, renumbered template and
+    renumbered values / right-hand side equal the oracle's lexicographic ordering (ANITYPE splits
+    the two DOFs of every P3 edge; the rest is NATURAL), bit for bit."""
+    import anigpu
+    from oracle.oracle import general_blocks, general_enumeration_perm, permute_csr
+    xyz, tets = _mesh(3, seed=12)
+    lib.mesh_upload(xyz, tets)
+    ndof, nnz = lib.problem_setup(space)
+    nt = tets.shape[0]
+    rhs_kind, F = (4, np.tile([0.5, -1.0, 2.0], (nt, 1))) if space in (9, 10) else (1, np.array([1.5]))
+    vals, rhs = lib.assemble_general(op, op, anigpu.TENSOR_NULL, None, rhs_kind, F, 4)
+    rp, col = lib.csr_template()
+    rp, col, v, b = rp.cpu().numpy(), col.cpu().numpy(), vals.cpu().numpy(), rhs.cpu().numpy()
+    per, off = general_blocks(xyz, tets, space)
+    assert off[4] == ndof
+    for etype in range(6):
+        perm = general_enumeration_perm(per, off, etype)
+        if space != 3:
+            assert np.array_equal(perm, np.arange(ndof))
+        rp_o, col_o, v_o = permute_csr(rp, col, v, perm)
+        grp, gcol, gperm = lib.enumeration_setup(etype)
+        assert np.array_equal(gperm.cpu().numpy(), perm), etype
+        assert np.array_equal(grp.cpu().numpy(), rp_o) and np.array_equal(gcol.cpu().numpy(), col_o), etype
+        gv, gb = lib.enumeration_apply(vals, anigpu.F64, rhs)
+        assert np.array_equal(gv.cpu().numpy(), v_o), etype
+        b_o = np.empty_like(b)
+        b_o[perm] = b
+        assert np.array_equal(gb.cpu().numpy(), b_o), etype
+        assert np.array_equal(lib.enumeration_to_natural(gb).cpu().numpy(), b), etype

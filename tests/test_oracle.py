@@ -235,3 +235,25 @@ def test_oracle_fem3dface_n_matches_reference(restated, golden):
         A = restated.fem3dface(ca, cb, KIND_CODE[kname], order, face, XY, D, normal=True)
         err = rel_err_per_tet(A, golden[f"facen_{name}_A"])
         assert err <= 1e-12, (name, err)
+
+
+def test_general_enumeration_perm_closed_form():
+    """The oracle's lexicographic general-space enumerations: ANITYPE on P3 sends DOF k of edge e to
+    nv + k*ne + e and leaves nodes and faces in place; every other type, and every other
+    general-path space, is NATURAL."""
+    from anigpu import meshgen
+    from oracle.oracle import general_blocks, general_enumeration_perm
+    xyz, t = meshgen.kuhn_cube(3, perturb=0.2, seed=12)
+    per, off = general_blocks(xyz, t, 3)
+    s = np.arange(off[4])
+    nv, ne = off[1], (off[2] - off[1]) // 2
+    exp = s.copy()
+    m = (s >= nv) & (s < off[2])
+    exp[m] = nv + ((s[m] - nv) % 2) * ne + (s[m] - nv) // 2
+    assert np.array_equal(general_enumeration_perm(per, off, 0), exp)
+    for etype in range(1, 6):
+        assert np.array_equal(general_enumeration_perm(per, off, etype), s)
+    for space in (0, 6, 7, 8, 9, 10):
+        per, off = general_blocks(xyz, t, space)
+        for etype in range(6):
+            assert np.array_equal(general_enumeration_perm(per, off, etype), np.arange(off[4]))
