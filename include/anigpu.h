@@ -118,6 +118,18 @@ int anigpu_last_timing(anigpu_handle h, double* ms_host, int cap);
  *   order: quadrature order 0..6 (the stack-memory fem3Dtet limit, int_tet.inl:98-99) */
 int anigpu_fem3dtet(anigpu_handle h, int opA, int opB, int tensor_kind, int order, int precision, int64_t nt,
                     const double* XY, const double* D, void* A);
+
+/* the same with user-defined operators, the counterpart of Ani::ApplyOpCustom
+ * (anifem++/fem/operators.h:450-471) used through fem3Dtet with runtime operators
+ * (int_tet.h:111-147): the functor that fills U at the quadrature points becomes data.
+ *   UA: the A operator's values at the points of the rule of `order` (anigpu_quadrature_points
+ *       gives their coordinates), per tet and point a dimA x nfA column-major matrix:
+ *       UA[((t*q + n)*nfA + i)*dimA + k], doubles on the device
+ *   VB: the same for the B operator (dimB x nfB), or NULL when B is A
+ * 1 <= dim <= 9; tensor kinds and the identity-tensor rule as anigpu_fem3dtet; A as there. */
+int anigpu_fem3dtet_custom(anigpu_handle h, int dimA, int nfA, const double* UA, int dimB, int nfB, const double* VB,
+                           int tensor_kind, int order, int precision, int64_t nt, const double* XY, const double* D,
+                           void* A);
 /* quadrature rule (host arrays): p[4*np] barycentric, w[np] summing to 1; returns np or <0
  * (replaces tetrahedron_quadrature_formulas, anifem++/fem/quadrature_formulas.cpp:526) */
 int anigpu_quadrature(int order, double* p_host, double* w_host, int cap);

@@ -10,11 +10,14 @@
  * device arrays.  Errors come back as std::runtime_error, as the reference throws them.
  *
  * Spaces: P0, P1, P2, P3, CR1, B2, B4, ND0, RT0 and FemVec<3, P1 | P2> (component-major DOF
- * blocks, the reference's FemVec order).  Operators: IDEN, GRAD; DIV and CURL for ND0 / RT0. */
+ * blocks, the reference's FemVec order).  Operators: IDEN, GRAD; DIV and CURL for ND0 / RT0;
+ * user-defined operators (ApplyOpCustom) whose values the caller's device code supplies. */
 #ifndef ANIGPU_HPP
 #define ANIGPU_HPP
 
+#include <climits>
 #include <cstdint>
+#include <functional>
 #include <stdexcept>
 #include <string>
 
@@ -136,6 +139,52 @@ inline void fem3DapplyL(anigpu_handle h, int64_t nt, const double* XY, int npts,
 inline void fem3DapplyX(anigpu_handle h, int64_t nt, const double* XY, int npts, const double* X, const ApplyOp& op,
                         const double* dofs, double* opU) {
     check(h, anigpu_fem3d_apply_x(h, op.code(), nt, XY, npts, X, dofs, opU));
+}
+
+/* A user-defined operator (Ani::ApplyOpCustom, anifem++/fem/operators.h:450-471): a unique label
+ * (operators with equal labels are the same operator), Dim, Nfa, Order and a functor that writes
+ * the operator's values at the points of the quadrature rule of `order` for a batch of tets on the
+ * device: U[((t*q + n)*Nfa + i)*Dim + k], q = the rule's points (anigpu_quadrature).  The functor
+ * replaces the reference's applyOp(mem, U); it runs the caller's own device code. */
+class ApplyOpCustom {
+public:
+    using Fill = std::function<void(anigpu_handle h, int64_t nt, const double* XY, int order, double* U)>;
+    ApplyOpCustom(unsigned unique_label, Fill fill, unsigned dim, unsigned nfa, unsigned order = UINT_MAX)
+        : fill_(std::move(fill)), dim_(dim), nfa_(nfa), order_(order), label_(unique_label) {
+        if (dim < 1 || dim > 9 || nfa < 1) throw std::invalid_argument("custom operator: 1 <= Dim <= 9, Nfa >= 1");
+    }
+    unsigned Nfa() const { return nfa_; }
+    unsigned Dim() const { return dim_; }
+    unsigned Order() const { return order_; }
+    unsigned label() const { return label_; }
+    bool operator==(const ApplyOpCustom& o) const { return label_ == o.label_; }
+    bool operator!=(const ApplyOpCustom& o) const { return label_ != o.label_; }
+    void fill(anigpu_handle h, int64_t nt, const double* XY, int order, double* U) const { fill_(h, nt, XY, order, U); }
+    /* doubles of the device buffer that holds the operator's values for nt tets */
+    size_t values_size(int64_t nt, int order) const {
+        const int q = anigpu_quadrature(order, nullptr, nullptr, 1 << 20);
+        if (q <= 0) throw std::invalid_argument("no quadrature rule of order " + std::to_string(order));
+        return (size_t)nt * (size_t)q * nfa_ * dim_;
+    }
+
+private:
+    Fill fill_;
+    unsigned dim_, nfa_, order_, label_;
+};
+
+/* fem3Dtet with user-defined operators: fills UA (and VB when opB is another operator) through the
+ * operators' functors, then integrates; UA / VB hold values_size(nt, order) doubles each */
+inline void fem3Dtet(anigpu_handle h, int64_t nt, const double* XY, const ApplyOpCustom& opA,
+                     const ApplyOpCustom& opB, int tensor_kind, const double* D, void* A, double* UA, double* VB,
+                     int order = 5, int precision = ANIGPU_F64) {
+    opA.fill(h, nt, XY, order, UA);
+    const bool same = opA == opB;
+    if (!same) {
+        if (!VB) throw std::invalid_argument("a second operator needs its own value buffer");
+        opB.fill(h, nt, XY, order, VB);
+    }
+    check(h, anigpu_fem3dtet_custom(h, (int)opA.Dim(), (int)opA.Nfa(), UA, (int)opB.Dim(), (int)opB.Nfa(),
+                                    same ? nullptr : VB, tensor_kind, order, precision, nt, XY, D, A));
 }
 
 /* owning handle */

@@ -52,6 +52,7 @@ SIGNATURES = {
     "anigpu_set_timing": (_i, [_vp, _i]),
     "anigpu_last_timing": (_i, [_vp, _vp, _i]),
     "anigpu_fem3dtet": (_i, [_vp, _i, _i, _i, _i, _i, _i64, _vp, _vp, _vp]),
+    "anigpu_fem3dtet_custom": (_i, [_vp, _i, _i, _vp, _i, _i, _vp, _i, _i, _i, _i64, _vp, _vp, _vp]),
     "anigpu_quadrature": (_i, [_i, _vp, _vp, _i]),
     "anigpu_quadrature_points": (_i, [_vp, _i, _i64, _vp, _vp]),
     "anigpu_fem3dface": (_i, [_vp, _i, _i, _i, _i, _i, _i64, _vp, _i, _vp, _vp]),
@@ -275,6 +276,29 @@ class Anigpu:
         Dd = self._dev(D, torch.float64) if D is not None else None
         self._check(self.lib.anigpu_fem3dtet(self.h, opA, opB, kind, order, precision, nt, _ptr(XY), _ptr(Dd),
                                              _ptr(out)))
+        return out
+
+    @_streamed
+    def fem3dtet_custom(self, UA, XY, VB=None, D=None, kind=TENSOR_NULL, order=5, precision=F64, out=None):
+        """Element matrices with user-defined operators (Ani::ApplyOpCustom): UA[nt, q, nfA, dimA]
+        holds the A operator's values at the rule's points (quadrature_points gives them), VB the
+        B operator's (None: B is A).  A[nt, nfA, nfB] as fem3dtet."""
+        torch = self.torch
+        XY = self._dev(XY, torch.float64)
+        nt = XY.numel() // 12
+        UA = self._dev(UA, torch.float64)
+        nfA, dimA = int(UA.shape[-2]), int(UA.shape[-1])
+        if VB is not None:
+            VB = self._dev(VB, torch.float64)
+            nfB, dimB = int(VB.shape[-2]), int(VB.shape[-1])
+        else:
+            nfB, dimB = nfA, dimA
+        dt = torch.float64 if precision == F64 else torch.float32
+        if out is None:
+            out = torch.empty((nt, nfA, nfB), dtype=dt, device=XY.device)
+        Dd = self._dev(D, torch.float64) if D is not None else None
+        self._check(self.lib.anigpu_fem3dtet_custom(self.h, dimA, nfA, _ptr(UA), dimB, nfB, _ptr(VB), kind, order,
+                                                    precision, nt, _ptr(XY), _ptr(Dd), _ptr(out)))
         return out
 
     @_streamed

@@ -179,6 +179,8 @@ inline unsigned grid_for(int64_t n, int block) {
 // element level (k_element.cu)
 int launch_fem3dtet(anigpu_ctx* h, int opA, int opB, int kind, int order, int precision, int64_t nt,
                     const double* XY, const double* D, void* A, int face = -1, int normal = 0);
+int launch_fem3dtet_custom(anigpu_ctx* h, int dimA, int nfA, const double* UA, int dimB, int nfB, const double* VB,
+                           int kind, int order, int precision, int64_t nt, const double* XY, const double* D, void* A);
 int launch_quad_points(anigpu_ctx* h, int order, int64_t nt, const double* XY, double* XYG, int face = -1);
 // general-path spaces (k_general.cu)
 bool is_general_space(int space);

@@ -126,6 +126,14 @@ int anigpu_fem3dtet(anigpu_handle h, int opA, int opB, int tensor_kind, int orde
     return launch_fem3dtet(h, opA, opB, tensor_kind, order, precision, nt, XY, D, A);
 }
 
+int anigpu_fem3dtet_custom(anigpu_handle h, int dimA, int nfA, const double* UA, int dimB, int nfB, const double* VB,
+                           int tensor_kind, int order, int precision, int64_t nt, const double* XY, const double* D,
+                           void* A) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    return launch_fem3dtet_custom(h, dimA, nfA, UA, dimB, nfB, VB, tensor_kind, order, precision, nt, XY, D, A);
+}
+
 int anigpu_quadrature(int order, double* p_host, double* w_host, int cap) {
     const double *p, *w;
     int np;

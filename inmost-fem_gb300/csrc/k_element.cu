@@ -25,6 +25,7 @@ struct OpDesc {
     int space;                        // base space; ND0 / RT0 are evaluated from the tet geometry
     int tnf;                          // functions in the table: nfs, or 4 (the P1 table: lambda) for ND0 / RT0
     const double* tab;                // device basis table (vals q*tnf, grads q*tnf*3)
+    const double* user;               // custom operator: values per (tet, point), dim x nf column-major
 };
 
 struct ElemParams {
@@ -197,10 +198,13 @@ __global__ void __launch_bounds__(kThreads) fem3dtet_kernel(ElemParams p, int64_
         const double mes = sGeo[9];
         for (int n = 0; n < q; ++n) {
             // U, V and the tensor at point n
-            for (int e = lane; e < dA * nfA; e += 32) sU[e] = op_value<Real>(p.A, sTabA, q, n, e % dA, e / dA, sGeo);
+            for (int e = lane; e < dA * nfA; e += 32)
+                sU[e] = p.A.user ? Real(p.A.user[((size_t)t * q + n) * (dA * nfA) + e])
+                                 : op_value<Real>(p.A, sTabA, q, n, e % dA, e / dA, sGeo);
             if (!p.same)
                 for (int e = lane; e < dB * nfB; e += 32)
-                    sV[e] = op_value<Real>(p.B, sTabB, q, n, e % dB, e / dB, sGeo);
+                    sV[e] = p.B.user ? Real(p.B.user[((size_t)t * q + n) * (dB * nfB) + e])
+                                     : op_value<Real>(p.B, sTabB, q, n, e % dB, e / dB, sGeo);
             // dense D(k,j), column-major dB x dA; fem3DfaceN: rows l + 3k of the 3dB x dA tensor
             // contracted with the normal (DotWithNormalHelper::ProcessNormal, core.h:175-190)
             for (int e = lane; e < nD; e += 32) {
@@ -1031,6 +1035,9 @@ static int launch_reftensor(anigpu_ctx* h, int opA, int opB, int order, int face
     return ANIGPU_OK;
 }
 
+static int run_quadrature(anigpu_ctx* h, const ElemParams& p, int precision, int64_t nt, const double* XY,
+                          const double* D, void* A);
+
 int launch_fem3dtet(anigpu_ctx* h, int opA, int opB, int kind, int order, int precision, int64_t nt,
                     const double* XY, const double* D, void* A, int face, int normal) {
     int nfA, dA, bsA, ncA, oA, nfB, dB, bsB, ncB, oB;
@@ -1063,20 +1070,28 @@ int launch_fem3dtet(anigpu_ctx* h, int opA, int opB, int kind, int order, int pr
     if (!vecA && !vecB && ncA == 1 && ncB == 1 && !normal && kind != ANIGPU_TENSOR_POINT)
         return launch_reftensor(h, opA, opB, order, face, hA, hB, kind, precision, nt, XY, D, A);
     ElemParams p;
-    p.A = {nfA, dA, nfA / ncA, dA / ncA, ncA, oA, bsA, vecA ? 4 : nfA / ncA, tA};
-    p.B = {nfB, dB, nfB / ncB, dB / ncB, ncB, oB, bsB, vecB ? 4 : nfB / ncB, tB};
+    p.A = {nfA, dA, nfA / ncA, dA / ncA, ncA, oA, bsA, vecA ? 4 : nfA / ncA, tA, nullptr};
+    p.B = {nfB, dB, nfB / ncB, dB / ncB, ncB, oB, bsB, vecB ? 4 : nfB / ncB, tB, nullptr};
     p.q = hA.q;
     p.kind = kind;
     p.face = face;
     p.normal = normal ? 1 : 0;
     p.w = tA + (size_t)hA.q * hA.nf * 4;
     p.same = opA == opB ? 1 : 0;
+    return run_quadrature(h, p, precision, nt, XY, D, A);
+}
+
+// the warp-per-tet quadrature kernel on prepared parameters
+static int run_quadrature(anigpu_ctx* h, const ElemParams& p, int precision, int64_t nt, const double* XY,
+                          const double* D, void* A) {
+    const int nfA = p.A.nf, dA = p.A.dim, nfB = p.B.nf, dB = p.B.dim;
     const size_t tabs = (size_t)p.q * (p.A.tnf + p.B.tnf) * 4;
     const size_t rsz = precision == ANIGPU_F32 ? sizeof(float) : sizeof(double);
     // per-warp region in doubles: geometry 26, tensor MAX_DIM^2, then U, V, DU and the entries
     const size_t wreal = (size_t)dA * nfA + (p.same ? 0 : (size_t)dB * nfB) + (size_t)dB * nfA + (size_t)nfA * nfB;
     const int wstride = (int)((26 + ANIGPU_MAX_DIM * ANIGPU_MAX_DIM) + (wreal * rsz + 7) / 8 + 1) & ~1;
     const size_t smem = sizeof(double) * (tabs + p.q + (size_t)(kThreads / 32) * wstride);
+    if (smem > 227 * 1024) return set_err(h, ANIGPU_ERR_UNSUPPORTED, "element matrices too large for one warp's shared memory");
     int dev_sms = 148;
     cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, h->device);
     const unsigned grid = (unsigned)std::min<int64_t>((nt + kThreads / 32 - 1) / (kThreads / 32), (int64_t)dev_sms * 16);
@@ -1091,6 +1106,43 @@ int launch_fem3dtet(anigpu_ctx* h, int opA, int opB, int kind, int order, int pr
     }
     ANI_LAUNCHED(h);
     return ANIGPU_OK;
+}
+
+// fem3Dtet with user-defined operators (ApplyOpCustom, anifem++/fem/operators.h:450-471): the
+// operators' values at the points of the rule of `order` come from the caller, per tet and point a
+// dim x nf column-major matrix (UA[((t*q + n)*nf + i)*dim + k]); VB NULL: the B operator is A's
+int launch_fem3dtet_custom(anigpu_ctx* h, int dimA, int nfA, const double* UA, int dimB, int nfB, const double* VB,
+                           int kind, int order, int precision, int64_t nt, const double* XY, const double* D, void* A) {
+    if (nt < 0) return set_err(h, ANIGPU_ERR_ARG, "nt < 0");
+    if (dimA < 1 || dimA > ANIGPU_MAX_DIM || nfA < 1 || (VB && (dimB < 1 || dimB > ANIGPU_MAX_DIM || nfB < 1)))
+        return set_err(h, ANIGPU_ERR_ARG, "operator dimensions: 1 <= dim <= 9, nf >= 1");
+    if (!VB) {
+        dimB = dimA;
+        nfB = nfA;
+    }
+    if (nt == 0) return ANIGPU_OK;
+    if (kind < ANIGPU_TENSOR_NULL || kind > ANIGPU_TENSOR_POINT) return set_err(h, ANIGPU_ERR_UNSUPPORTED, "tensor kind");
+    if (kind == ANIGPU_TENSOR_TET_SYM && (dimA != 3 || dimB != 3)) return set_err(h, ANIGPU_ERR_ARG, "TET_SYM needs 3x3 operators");
+    if ((kind == ANIGPU_TENSOR_NULL || kind == ANIGPU_TENSOR_CONST_SCALAR || kind == ANIGPU_TENSOR_TET_SCALAR) &&
+        dimA != dimB && !(nfA == 1 && dimA == 1))
+        return set_err(h, ANIGPU_ERR_ARG, "Identity tensor defined only for compatible operators A and B");
+    if (kind != ANIGPU_TENSOR_NULL && D == nullptr) return set_err(h, ANIGPU_ERR_ARG, "tensor data is NULL");
+    if (!XY || !A || !UA) return set_err(h, ANIGPU_ERR_ARG, "NULL coordinates, operator values or output");
+    if (precision != ANIGPU_F32 && precision != ANIGPU_F64) return set_err(h, ANIGPU_ERR_ARG, "precision");
+    const double* t1;
+    ScalarBasisTable h1;
+    int rc = get_basis_dev(h, ANIGPU_P1, order, &t1, &h1, -1);  // the rule's weights
+    if (rc) return rc;
+    ElemParams p;
+    p.A = {nfA, dimA, nfA, dimA, 1, 0, -1, 0, t1, UA};
+    p.B = {nfB, dimB, nfB, dimB, 1, 0, -1, 0, t1, VB ? VB : UA};
+    p.q = h1.q;
+    p.kind = kind;
+    p.face = -1;
+    p.normal = 0;
+    p.w = t1 + (size_t)h1.q * h1.nf * 4;
+    p.same = VB ? 0 : 1;
+    return run_quadrature(h, p, precision, nt, XY, D, A);
 }
 
 int launch_quad_points(anigpu_ctx* h, int order, int64_t nt, const double* XY, double* XYG, int face) {

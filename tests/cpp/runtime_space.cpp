@@ -2,7 +2,9 @@
 //   runtime_space host               : operator/space metadata and argument errors (no GPU)
 //   runtime_space gpu <in> <out>     : fem3Dtet(GRAD P2, GRAD P2) and fem3Dface(IDEN P0, IDEN P2)
 //                                      through the layer on the tets of <in> (nt * 12 doubles),
-//                                      results to <out>; an invalid face must throw
+//                                      then fem3Dtet with a user-defined operator (ApplyOpCustom)
+//                                      whose functor evaluates GRAD of each P2 basis function with
+//                                      fem3DapplyL; results to <out>; an invalid face must throw
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -44,6 +46,9 @@ static int host_checks() {
         threw = true;
     }
     if (!threw) return fail("P3^3 accepted");
+    const ApplyOpCustom c1(3, ApplyOpCustom::Fill(), 6, 12, 1), c2(3, ApplyOpCustom::Fill(), 6, 12), c3(4, ApplyOpCustom::Fill(), 1, 4);
+    if (c1.Dim() != 6 || c1.Nfa() != 12 || c1.Order() != 1 || !(c1 == c2) || c1 == c3) return fail("custom operator");
+    if (c3.values_size(10, 4) != 10 * 14 * 4) return fail("custom operator values size");
     std::printf("host ok\n");
     return 0;
 }
@@ -72,9 +77,48 @@ static int gpu_run(const char* in, const char* out) {
         threw = std::strstr(e.what(), "face") != nullptr;
     }
     if (!threw) return fail("invalid face did not throw");
-    std::vector<double> A(nt * 100 + nt * 10);
+    std::vector<double> A(nt * 210);
     cudaMemcpy(A.data(), dA, sizeof(double) * nt * 100, cudaMemcpyDeviceToHost);
     cudaMemcpy(A.data() + nt * 100, dF, sizeof(double) * nt * 10, cudaMemcpyDeviceToHost);
+    // a custom operator: GRAD of the 10 P2 basis functions at the rule's points, from fem3DapplyL
+    // on unit DOF vectors, interleaved into U[((t*q + n)*10 + i)*3 + k]
+    ApplyOpCustom grad_p2(
+        7,
+        [](anigpu_handle h, int64_t n, const double* X, int order, double* U) {
+            const int q = anigpu_quadrature(order, nullptr, nullptr, 1 << 20);
+            std::vector<double> pts(4 * q), w(q), e((size_t)n * 10);
+            anigpu_quadrature(order, pts.data(), w.data(), q);
+            double *dP = nullptr, *dE = nullptr, *dG = nullptr;
+            cudaMalloc(&dP, sizeof(double) * 4 * q);
+            cudaMalloc(&dE, sizeof(double) * n * 10);
+            cudaMalloc(&dG, sizeof(double) * n * q * 3);
+            cudaMemcpy(dP, pts.data(), sizeof(double) * 4 * q, cudaMemcpyHostToDevice);
+            for (int i = 0; i < 10; ++i) {
+                for (int64_t t = 0; t < n; ++t)
+                    for (int j = 0; j < 10; ++j) e[t * 10 + j] = j == i ? 1.0 : 0.0;
+                cudaMemcpy(dE, e.data(), sizeof(double) * n * 10, cudaMemcpyHostToDevice);
+                fem3DapplyL(h, n, X, q, dP, FemSpace::P2().getOP(GRAD), dE, dG);
+                cudaMemcpy2D(U + 3 * i, sizeof(double) * 30, dG, sizeof(double) * 3, sizeof(double) * 3,
+                             (size_t)n * q, cudaMemcpyDeviceToDevice);
+            }
+            cudaFree(dP);
+            cudaFree(dE);
+            cudaFree(dG);
+        },
+        3, 10, 1);
+    double* dU = nullptr;
+    if (cudaMalloc(&dU, sizeof(double) * grad_p2.values_size(nt, 4))) return fail("cudaMalloc U");
+    fem3Dtet(ctx.get(), nt, dXY, grad_p2, grad_p2, ANIGPU_TENSOR_NULL, nullptr, dA, dU, nullptr, 4);
+    cudaMemcpy(A.data() + nt * 110, dA, sizeof(double) * nt * 100, cudaMemcpyDeviceToHost);
+    cudaFree(dU);
+    threw = false;
+    try {
+        ApplyOpCustom bad(8, ApplyOpCustom::Fill(), 12, 10);
+        (void)bad;
+    } catch (const std::invalid_argument&) {
+        threw = true;
+    }
+    if (!threw) return fail("custom operator with Dim 12 accepted");
     cudaFree(dXY);
     cudaFree(dA);
     cudaFree(dF);

@@ -5,6 +5,11 @@ import pytest
 
 from helpers import KIND_CODE, op_nf_dim, parse_case, point_tensor, ref_tol, rel_err_per_tet
 
+
+def op_info(code):
+    import anigpu
+    return anigpu.op_info(code)
+
 pytestmark = pytest.mark.gpu
 
 
@@ -220,4 +225,48 @@ def test_runtime_space_layer_on_gpu(lib, golden, tmp_path):
     out = np.fromfile(tmp_path / "out.bin", dtype=np.float64)
     A = lib.fem3dtet(22, 22, XY, None, anigpu.TENSOR_NULL, 4).cpu().numpy().reshape(-1)
     F = lib.fem3dface(1, 21, XY, 1, None, anigpu.TENSOR_NULL, 4).cpu().numpy().reshape(-1)
-    assert np.array_equal(out[:nt * 100], A) and np.array_equal(out[nt * 100:], F)
+    assert np.array_equal(out[:nt * 100], A) and np.array_equal(out[nt * 100:nt * 110], F)
+    # the ApplyOpCustom operator (GRAD P2 values from fem3DapplyL) integrates to fem3Dtet's matrix
+    C = out[nt * 110:]
+    assert rel_err_per_tet(C.reshape(nt, 100), A.reshape(nt, 100)) <= 1e-13
+
+
+@pytest.mark.parametrize("ca,cb,kind", [(22, 22, "tsym"), (12, 22, "tgeneral"), (21, 11, "point0"), (94, 94, "null")])
+def test_custom_operators_match_builtin(lib, golden, ca, cb, kind):
+    """anigpu_fem3dtet_custom (ApplyOpCustom) with the operators' values taken from fem3DapplyL on
+    unit DOF vectors gives the built-in fem3Dtet matrices (FP64 within 1e-13 per tet, FP32 within
+    2e-5): the user-operator path integrates exactly what it is given."""
+    import anigpu
+    XY = golden["tets_XY"]
+    nt = XY.shape[0]
+    order = 4
+    pts = anigpu.quadrature(order)[0]
+
+    def values(code):
+        nf, dim = op_info(code)
+        cols = []
+        for i in range(nf):
+            e = np.zeros((nt, nf))
+            e[:, i] = 1.0
+            cols.append(lib.fem3d_apply(code, XY, pts, e))
+        import torch
+        return torch.stack(cols, dim=2)  # [nt, q, nf, dim]
+
+    UA = values(ca)
+    VB = None if cb == ca else values(cb)
+    nfA, dA = op_info(ca)
+    nfB, dB = op_info(cb)
+    if kind.startswith("point"):
+        q = lib.quadrature_points(order, XY).cpu().numpy()
+        D, code = point_tensor(int(kind[5:]), q, dB, dA), anigpu.TENSOR_POINT
+    elif kind == "tsym":
+        D, code = np.tile([2.0, 0.3, -0.1, 1.5, 0.2, 1.1], (nt, 1)), anigpu.TENSOR_TET_SYM
+    elif kind == "tgeneral":
+        D, code = np.random.default_rng(5).normal(size=(nt, dB * dA)), anigpu.TENSOR_TET_GENERAL
+    else:
+        D, code = None, anigpu.TENSOR_NULL
+    ref = lib.fem3dtet(ca, cb, XY, D, code, order).cpu().numpy()
+    got = lib.fem3dtet_custom(UA, XY, VB, D, code, order).cpu().numpy()
+    assert rel_err_per_tet(got, ref) <= 1e-13
+    got32 = lib.fem3dtet_custom(UA, XY, VB, D, code, order, anigpu.F32).double().cpu().numpy()
+    assert rel_err_per_tet(got32, ref) <= 2e-5
