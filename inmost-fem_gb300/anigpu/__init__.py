@@ -73,11 +73,13 @@ SIGNATURES = {
     "anigpu_problem_info": (_i, [_vp, ctypes.POINTER(_i64), ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
     "anigpu_csr_template": (_i, [_vp, _vp, _vp]),
     "anigpu_element_dofs": (_i, [_vp, _vp]),
+    "anigpu_element_coords": (_i, [_vp, _vp]),
     "anigpu_dof_coords": (_i, [_vp, _vp]),
     "anigpu_set_dirichlet": (_i, [_vp, _vp, _vp]),
     "anigpu_assemble": (_i, [_vp, _i, _vp, _vp, _d, _i, _i, _vp, _vp, _vp, _d]),
     "anigpu_assemble_async": (_i, [_vp, _i, _vp, _vp, _d, _i, _i, _vp, _vp, _vp, _d]),
     "anigpu_assemble_general": (_i, [_vp, _i, _i, _i, _vp, _i, _vp, _i, _vp, _vp]),
+    "anigpu_assemble_general_elements": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "anigpu_status": (_i, [_vp]),
     "anigpu_assemble_noalloc": (_i, [_vp, _i, _vp, _vp, _d, _i, _i, _vp, _vp, _d]),
     "anigpu_csr_compact": (_i, [_vp, _vp, _vp, _vp, _i, _vp, ctypes.POINTER(_i64)]),
@@ -452,6 +454,14 @@ class Anigpu:
         return rp, col
 
     @_streamed
+    def element_coords(self):
+        """XY[nt, 12]: every tet's vertex coordinates in the library's reoriented local order."""
+        torch = self.torch
+        out = torch.empty((self.nt, 12), dtype=torch.float64, device=f"cuda:{self.device}")
+        self._check(self.lib.anigpu_element_coords(self.h, _ptr(out)))
+        return out
+
+    @_streamed
     def element_dofs(self):
         torch = self.torch
         nloc = op_info(10 * self.space + IDEN)[0] if self.space not in (VEC3_P1, VEC3_P2) else 10
@@ -486,6 +496,20 @@ class Anigpu:
         self._check(self.lib.anigpu_assemble_general(self.h, opA, opB, kind, _ptr(Dd),
                                                      rhs_kind if rhs_kind is not None else 0, _ptr(Fd), order,
                                                      _ptr(vals), _ptr(rhs)))
+        return vals, rhs
+
+    @_streamed
+    def assemble_general_elements(self, Aelem, Felem=None):
+        """General-path spaces: scatter of caller-computed element matrices Aelem[nt, nloc, nloc]
+        (fem3dtet's layout, local unsigned basis) and right-hand sides Felem[nt, nloc] (or None),
+        with the orientation signs and Dirichlet DOFs applied (the local-assembler contract)."""
+        torch = self.torch
+        dev = f"cuda:{self.device}"
+        A = self._dev(Aelem, torch.float64)
+        Fd = self._dev(Felem, torch.float64) if Felem is not None else None
+        vals = torch.empty(self.nnz, dtype=torch.float64, device=dev)
+        rhs = torch.empty(self.ndof, dtype=torch.float64, device=dev) if Fd is not None else None
+        self._check(self.lib.anigpu_assemble_general_elements(self.h, _ptr(A), _ptr(Fd), _ptr(vals), _ptr(rhs)))
         return vals, rhs
 
     @_streamed

@@ -308,6 +308,28 @@ int anigpu_csr_template(anigpu_handle h, int64_t* rowptr, int32_t* col) {
     return ANIGPU_OK;
 }
 
+namespace {
+__global__ void element_coords_kernel(int64_t nt, const double* __restrict__ xyz, const int32_t* __restrict__ tets,
+                                      double* __restrict__ XY) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;  // (tet, vertex, coordinate)
+    if (i >= nt * 12) return;
+    const int64_t t = i / 12;
+    const int r = (int)(i - 12 * t), v = r / 3, c = r - 3 * v;
+    XY[i] = xyz[3 * (int64_t)tets[4 * t + v] + c];
+}
+}  // namespace
+
+int anigpu_element_coords(anigpu_handle h, double* XY) {
+    CHECK_H(h);
+    if (h->nt <= 0 || !h->tets) return set_err(h, ANIGPU_ERR_STATE, "no mesh uploaded");
+    if (!XY) return set_err(h, ANIGPU_ERR_ARG, "NULL");
+    cudaSetDevice(h->device);
+    element_coords_kernel<<<grid_for(h->nt * 12, 256), 256, 0, h->stream>>>(h->nt, h->xyz, h->tets, XY);
+    ANI_LAUNCHED(h);
+    ANI_CUDA(h, cudaStreamSynchronize(h->stream));
+    return ANIGPU_OK;
+}
+
 int anigpu_element_dofs(anigpu_handle h, int32_t* edofs) {
     CHECK_H(h);
     if (h->space < 0) return set_err(h, ANIGPU_ERR_STATE, "anigpu_problem_setup not called");
@@ -365,6 +387,23 @@ int anigpu_assemble_general(anigpu_handle h, int opA, int opB, int tensor_kind, 
     CHECK_H(h);
     cudaSetDevice(h->device);
     int rc = general_assemble(h, opA, opB, tensor_kind, D, rhs_kind, F, order, vals, rhs);
+    if (rc) return rc;
+    int st = 0;
+    ANI_CUDA(h, cudaMemcpyAsync(&st, h->d_status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    ANI_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (st) {
+        ANI_CUDA(h, cudaMemsetAsync(h->d_status, 0, sizeof(int), h->stream));
+        return set_err(h, st, "non-finite value in assembly (AssemblerT status -1)");
+    }
+    return ANIGPU_OK;
+}
+
+int anigpu_assemble_general_elements(anigpu_handle h, const double* Aelem, const double* Felem, double* vals,
+                                     double* rhs) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    if (!is_general_space(h->space)) return set_err(h, ANIGPU_ERR_STATE, "a general-path problem is not set up");
+    int rc = general_gather(h, Aelem, Felem, vals, rhs);
     if (rc) return rc;
     int st = 0;
     ANI_CUDA(h, cudaMemcpyAsync(&st, h->d_status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));

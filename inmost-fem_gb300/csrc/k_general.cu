@@ -565,8 +565,17 @@ int general_assemble(anigpu_ctx* h, int opA, int opB, int kind, const double* D,
                             ANIGPU_F64, nt, w->XY, Fdata, w->F));
         F = w->F;
     }
-    general_gather_kernel<<<grid_for(h->ndof * 32, 256), 256, 0, s>>>(
-        h->ndof, (int)nloc, h->rowptr, h->col, w->inc_ptr, w->inc, h->edofs, w->sign, w->A, F, h->dir_mask, h->dir_bc,
+    return general_gather(h, w->A, F, vals, rhs);
+}
+
+// the signed row gather of element matrices A [nt][nloc][nloc] (column-major per tet, the layout of
+// fem3Dtet) and element right-hand sides F [nt][nloc] (or NULL) into the template
+int general_gather(anigpu_ctx* h, const double* A, const double* F, double* vals, double* rhs) {
+    GenWs* w = gws(h);
+    if (!w || h->space != w->space) return set_err(h, ANIGPU_ERR_STATE, "general problem not set up");
+    if (!A || !vals) return set_err(h, ANIGPU_ERR_ARG, "NULL element matrices or values");
+    general_gather_kernel<<<grid_for(h->ndof * 32, 256), 256, 0, h->stream>>>(
+        h->ndof, w->nloc, h->rowptr, h->col, w->inc_ptr, w->inc, h->edofs, w->sign, A, F, h->dir_mask, h->dir_bc,
         h->has_dirichlet ? 1 : 0, h->bc_nonzero ? 1 : 0, vals, rhs, h->d_status);
     ANI_LAUNCHED(h);
     return ANIGPU_OK;

@@ -139,3 +139,37 @@ def test_general_enumerations_match_oracle(lib, space, op):
         b_o[perm] = b
         assert np.array_equal(gb.cpu().numpy(), b_o), etype
         assert np.array_equal(lib.enumeration_to_natural(gb).cpu().numpy(), b), etype
+
+
+@pytest.mark.parametrize("space,opK,opM", [(9, 94, 91), (3, 32, 31), (10, 103, 101)])
+def test_general_assembly_from_element_matrices(lib, space, opK, opM):
+    """The local-assembler contract: element matrices the caller sums itself (K + M per tet, from
+    two fem3Dtet calls on the library's oriented tets) scatter to the sum of the two assembled
+    matrices up to one rounding per entry; the right-hand side likewise; Dirichlet rows are the
+    unit rows scaled by their number of tets, as in every path."""
+    import anigpu
+    from anigpu import meshgen
+    xyz, tets = _mesh(3, seed=13)
+    nt = tets.shape[0]
+    lib.mesh_upload(xyz, tets)
+    lib.problem_setup(space)
+    coords = lib.dof_coords().cpu().numpy()
+    lib.set_dirichlet(meshgen.boundary_mask(coords))
+    rhs_kind, F = (4, np.tile([0.5, -1.0, 2.0], (nt, 1))) if space in (9, 10) else (1, np.array([1.5]))
+    K, rhs = lib.assemble_general(opK, opK, anigpu.TENSOR_NULL, None, rhs_kind, F, 4)
+    M, _ = lib.assemble_general(opM, opM, anigpu.TENSOR_NULL, None, None, None, 4)
+    # the same element matrices computed by the caller, on the oriented tets the library uses
+    XY = lib.element_coords()
+    Ak = lib.fem3dtet(opK, opK, XY, None, anigpu.TENSOR_NULL, 4)
+    Am = lib.fem3dtet(opM, opM, XY, None, anigpu.TENSOR_NULL, 4)
+    Fe = lib.fem3dtet(1, 10 * space + 1, XY, F if rhs_kind == 4 else np.full(nt, F[0]),
+                      anigpu.TENSOR_TET_GENERAL if rhs_kind == 4 else anigpu.TENSOR_TET_SCALAR, 4)
+    v, r = lib.assemble_general_elements(Ak + Am, Fe.reshape(nt, -1))
+    ref = (K + M).cpu().numpy()
+    # a Dirichlet row is the unit row scaled by its number of tets, whatever the matrices were
+    rp = lib.csr_template()[0].cpu().numpy()
+    dmask = meshgen.boundary_mask(coords).astype(bool)
+    on_dir = dmask[np.repeat(np.arange(rp.size - 1), np.diff(rp))]
+    ref[on_dir] = K.cpu().numpy()[on_dir]
+    assert np.abs(v.cpu().numpy() - ref).max() <= 1e-13 * np.abs(ref).max()
+    assert np.abs(r.cpu().numpy() - rhs.cpu().numpy()).max() <= 1e-13 * np.abs(rhs.cpu().numpy()).max()
