@@ -231,7 +231,7 @@ int anigpu_element_dofs(anigpu_handle h, int32_t* edofs);
 /* coordinates of every tet's vertices in the library's (reoriented) local order, XY[nt*12] (f64,
  * device): the TetrasT columns a local assembler sees (ElementalAssembler nodes,
  * elemental_assembler.h:221), so that element matrices computed from them by anigpu_fem3dtet fit
- * anigpu_element_dofs and anigpu_assemble_general_elements */
+ * anigpu_element_dofs and anigpu_assemble_elements */
 int anigpu_element_coords(anigpu_handle h, double* XY);
 /* coordinates of every DOF's node: xyz[ndof*3] (f64, device).  Vertex DOFs sit at the
  * vertex, P2 edge DOFs at the edge midpoint (DOF_coord<FEM_P2>, anifem++/fem/operators.h:750-767);
@@ -288,8 +288,9 @@ int anigpu_assemble_noalloc(anigpu_handle h, int tensor_kind, const double* D, c
  * rhs may be NULL.  Dirichlet DOFs (anigpu_set_dirichlet) as in the other paths.  Setup memory is
  * about 24 nt nloc^2 bytes (sorts of the element-matrix entries); the fast kernels (anigpu_assemble)
  * and batching take P1 / P2 / vector P2 only.
- * anigpu_assemble_general_elements: the same scatter of element matrices and right-hand sides that
- * the caller computed, the counterpart of AssemblerT::Assemble with a user local-assembler function
+ * anigpu_assemble_elements (every scalar space: P1, P2 and the general-path spaces): the scatter of
+ * element matrices and right-hand sides that the caller computed, FP64 values in the problem's
+ * template, the counterpart of AssemblerT::Assemble with a user local-assembler function
  * (assembler.inl:314-487; ElementalAssembler, elemental_assembler.h:118-219): Aelem [nt][nloc][nloc]
  * (column-major per tet in the local, unsigned basis: fem3Dtet's layout, e.g. sums of
  * anigpu_fem3dtet / anigpu_fem3dtet_custom outputs), Felem [nt][nloc] or NULL, device doubles;
@@ -297,7 +298,7 @@ int anigpu_assemble_noalloc(anigpu_handle h, int tensor_kind, const double* D, c
  * Dirichlet rows and columns. */
 int anigpu_assemble_general(anigpu_handle h, int opA, int opB, int tensor_kind, const double* D, int rhs_kind,
                             const double* F, int order, double* vals, double* rhs);
-int anigpu_assemble_general_elements(anigpu_handle h, const double* Aelem, const double* Felem, double* vals,
+int anigpu_assemble_elements(anigpu_handle h, const double* Aelem, const double* Felem, double* vals,
                                      double* rhs);
 int anigpu_assemble_async(anigpu_handle h, int tensor_kind, const double* D, const double* f, double f_const,
                           int order, int precision, void* vals, double* rhs, uint8_t* touched, double drop_val);

@@ -79,7 +79,7 @@ SIGNATURES = {
     "anigpu_assemble": (_i, [_vp, _i, _vp, _vp, _d, _i, _i, _vp, _vp, _vp, _d]),
     "anigpu_assemble_async": (_i, [_vp, _i, _vp, _vp, _d, _i, _i, _vp, _vp, _vp, _d]),
     "anigpu_assemble_general": (_i, [_vp, _i, _i, _i, _vp, _i, _vp, _i, _vp, _vp]),
-    "anigpu_assemble_general_elements": (_i, [_vp, _vp, _vp, _vp, _vp]),
+    "anigpu_assemble_elements": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "anigpu_status": (_i, [_vp]),
     "anigpu_assemble_noalloc": (_i, [_vp, _i, _vp, _vp, _d, _i, _i, _vp, _vp, _d]),
     "anigpu_csr_compact": (_i, [_vp, _vp, _vp, _vp, _i, _vp, ctypes.POINTER(_i64)]),
@@ -499,17 +499,18 @@ class Anigpu:
         return vals, rhs
 
     @_streamed
-    def assemble_general_elements(self, Aelem, Felem=None):
-        """General-path spaces: scatter of caller-computed element matrices Aelem[nt, nloc, nloc]
-        (fem3dtet's layout, local unsigned basis) and right-hand sides Felem[nt, nloc] (or None),
-        with the orientation signs and Dirichlet DOFs applied (the local-assembler contract)."""
+    def assemble_elements(self, Aelem, Felem=None):
+        """Scalar spaces (P1, P2, general path): scatter of caller-computed element matrices
+        Aelem[nt, nloc, nloc] (fem3dtet's layout, local unsigned basis, on element_coords()) and
+        right-hand sides Felem[nt, nloc] (or None) into the template, FP64, with the orientation
+        signs and Dirichlet DOFs applied (the local-assembler contract)."""
         torch = self.torch
         dev = f"cuda:{self.device}"
         A = self._dev(Aelem, torch.float64)
         Fd = self._dev(Felem, torch.float64) if Felem is not None else None
         vals = torch.empty(self.nnz, dtype=torch.float64, device=dev)
         rhs = torch.empty(self.ndof, dtype=torch.float64, device=dev) if Fd is not None else None
-        self._check(self.lib.anigpu_assemble_general_elements(self.h, _ptr(A), _ptr(Fd), _ptr(vals), _ptr(rhs)))
+        self._check(self.lib.anigpu_assemble_elements(self.h, _ptr(A), _ptr(Fd), _ptr(vals), _ptr(rhs)))
         return vals, rhs
 
     @_streamed

@@ -398,12 +398,13 @@ int anigpu_assemble_general(anigpu_handle h, int opA, int opB, int tensor_kind, 
     return ANIGPU_OK;
 }
 
-int anigpu_assemble_general_elements(anigpu_handle h, const double* Aelem, const double* Felem, double* vals,
+int anigpu_assemble_elements(anigpu_handle h, const double* Aelem, const double* Felem, double* vals,
                                      double* rhs) {
     CHECK_H(h);
     cudaSetDevice(h->device);
-    if (!is_general_space(h->space)) return set_err(h, ANIGPU_ERR_STATE, "a general-path problem is not set up");
-    int rc = general_gather(h, Aelem, Felem, vals, rhs);
+    if (h->space < 0) return set_err(h, ANIGPU_ERR_STATE, "anigpu_problem_setup not called");
+    int rc = is_general_space(h->space) ? general_gather(h, Aelem, Felem, vals, rhs)
+                                        : elements_scatter(h, Aelem, Felem, vals, rhs);
     if (rc) return rc;
     int st = 0;
     ANI_CUDA(h, cudaMemcpyAsync(&st, h->d_status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));

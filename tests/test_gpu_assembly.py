@@ -317,3 +317,41 @@ def test_enumerations_match_oracle(lib, restated, space):
         b_o[perm] = b
         assert np.array_equal(gb.cpu().numpy(), b_o), etype
         assert np.array_equal(lib.enumeration_to_natural(gb).cpu().numpy(), b), etype
+
+
+@pytest.mark.parametrize("space,bcnz", [(1, False), (2, False), (2, True)])
+def test_assembly_from_element_matrices_fast_template(lib, restated, space, bcnz):
+    """The local-assembler contract on the P1 / P2 template: element matrices computed by the caller
+    (GRAD.GRAD with per-tet SYM tensors from fem3Dtet on the library's oriented tets, plus the
+    P0 x P_k right-hand side) scatter to the same system as anigpu_assemble, Dirichlet rows and
+    columns (zero or non-zero boundary values) included; a reaction term added to the element
+    matrices shows up as the assembled mass matrix."""
+    import anigpu
+    from anigpu import meshgen
+    xyz, tets = meshgen.kuhn_cube(4, perturb=0.2, seed=21)
+    nt = tets.shape[0]
+    lib.mesh_upload(xyz, tets)
+    lib.problem_setup(space)
+    c = lib.dof_coords().cpu().numpy()
+    mask = meshgen.boundary_mask(c)
+    bc = (0.5 + c[:, 0] - c[:, 2]) * mask if bcnz else None
+    lib.set_dirichlet(mask, bc)
+    D6 = meshgen.aniso_tensors(nt, 1.0, 22)
+    vals, rhs, _ = lib.assemble(anigpu.TENSOR_TET_SYM, D6, None, 1.5, 4, anigpu.F64)
+    XY = lib.element_coords()
+    g = 10 * space + 2
+    A = lib.fem3dtet(g, g, XY, D6, anigpu.TENSOR_TET_SYM, 4)
+    F = lib.fem3dtet(1, 10 * space + 1, XY, np.array([1.5]), anigpu.TENSOR_CONST_SCALAR, 4).reshape(nt, -1)
+    v, r = lib.assemble_elements(A, F)
+    ref_v, ref_r = vals.cpu().numpy(), rhs.cpu().numpy()
+    assert np.abs(v.cpu().numpy() - ref_v).max() <= 1e-12 * np.abs(ref_v).max()
+    assert np.abs(r.cpu().numpy() - ref_r).max() <= 1e-12 * np.abs(ref_r).max()
+    # reaction term: K + M from the element matrices equals K plus the scattered mass matrices
+    M = lib.fem3dtet(10 * space + 1, 10 * space + 1, XY, None, anigpu.TENSOR_NULL, 4)
+    vkm, _ = lib.assemble_elements(A + M, F)
+    vm, _ = lib.assemble_elements(M, None)
+    rp = lib.csr_template()[0].cpu().numpy()
+    on_dir = mask.astype(bool)[np.repeat(np.arange(rp.size - 1), np.diff(rp))]
+    exp = v.cpu().numpy() + vm.cpu().numpy()
+    exp[on_dir] = v.cpu().numpy()[on_dir]
+    assert np.abs(vkm.cpu().numpy() - exp).max() <= 1e-13 * np.abs(exp).max()

@@ -164,7 +164,7 @@ def test_general_assembly_from_element_matrices(lib, space, opK, opM):
     Am = lib.fem3dtet(opM, opM, XY, None, anigpu.TENSOR_NULL, 4)
     Fe = lib.fem3dtet(1, 10 * space + 1, XY, F if rhs_kind == 4 else np.full(nt, F[0]),
                       anigpu.TENSOR_TET_GENERAL if rhs_kind == 4 else anigpu.TENSOR_TET_SCALAR, 4)
-    v, r = lib.assemble_general_elements(Ak + Am, Fe.reshape(nt, -1))
+    v, r = lib.assemble_elements(Ak + Am, Fe.reshape(nt, -1))
     ref = (K + M).cpu().numpy()
     # a Dirichlet row is the unit row scaled by its number of tets, whatever the matrices were
     rp = lib.csr_template()[0].cpu().numpy()
