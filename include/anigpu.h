@@ -288,7 +288,7 @@ int anigpu_assemble_noalloc(anigpu_handle h, int tensor_kind, const double* D, c
  * rhs may be NULL.  Dirichlet DOFs (anigpu_set_dirichlet) as in the other paths.  Setup memory is
  * about 24 nt nloc^2 bytes (sorts of the element-matrix entries); the fast kernels (anigpu_assemble)
  * and batching take P1 / P2 / vector P2 only.
- * anigpu_assemble_elements (every scalar space: P1, P2 and the general-path spaces): the scatter of
+ * anigpu_assemble_elements (P1, P2, vector P2 and the general-path spaces): the scatter of
  * element matrices and right-hand sides that the caller computed, FP64 values in the problem's
  * template, the counterpart of AssemblerT::Assemble with a user local-assembler function
  * (assembler.inl:314-487; ElementalAssembler, elemental_assembler.h:118-219): Aelem [nt][nloc][nloc]

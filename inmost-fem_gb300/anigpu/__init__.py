@@ -500,7 +500,7 @@ class Anigpu:
 
     @_streamed
     def assemble_elements(self, Aelem, Felem=None):
-        """Scalar spaces (P1, P2, general path): scatter of caller-computed element matrices
+        """P1, P2, vector P2 and the general-path spaces: scatter of caller-computed element matrices
         Aelem[nt, nloc, nloc] (fem3dtet's layout, local unsigned basis, on element_coords()) and
         right-hand sides Felem[nt, nloc] (or None) into the template, FP64, with the orientation
         signs and Dirichlet DOFs applied (the local-assembler contract)."""

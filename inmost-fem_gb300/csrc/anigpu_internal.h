@@ -190,7 +190,7 @@ int general_assemble(anigpu_ctx* h, int opA, int opB, int kind, const double* D,
                      int order, double* vals, double* rhs);
 int general_dof_coords(anigpu_ctx* h, double* out);
 int general_gather(anigpu_ctx* h, const double* A, const double* F, double* vals, double* rhs);
-// the fast path's template (scalar P1 / P2): scatter of caller-computed element matrices (k_assemble.cu)
+// the fast path's template (P1, P2, vector P2): scatter of caller-computed element matrices (k_assemble.cu)
 int elements_scatter(anigpu_ctx* h, const double* A, const double* F, double* vals, double* rhs);
 const int8_t* general_signs(anigpu_ctx* h);
 // DOFs per entity (node, edge, face, cell) and the first global DOF of each entity block (off[4] = ndof)

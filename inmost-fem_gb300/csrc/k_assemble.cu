@@ -1102,40 +1102,48 @@ __global__ void compact_count_kernel(int64_t n, const int64_t* __restrict__ rowp
     for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k) c += (touched[k] || col[k] == r) ? 1 : 0;
     cnt[r] = c;
 }
-// Scatter of caller-computed element matrices (scalar P1 / P2, the local-assembler contract): one
-// warp per row; for every incidence in the records' order (ascending tets) lane c adds the element
-// row's canonical column c, A_t(i, canon_local(i, c)), at the record's offset of that column -- the
-// columns of one incidence are distinct, so every entry sums its contributions in tet order.
-// Dirichlet rows: zero except the diagonal = number of incident tets; Dirichlet columns of the
-// other rows: A(i, k) bc_k moved to the right-hand side, then zeroed.
-__global__ void elements_gather_kernel(int64_t nrows, int nloc, const int64_t* __restrict__ rowptr,
-                                       const int32_t* __restrict__ col, const int64_t* __restrict__ inc_ptr,
-                                       const ScatterRec* __restrict__ recs, const double* __restrict__ A,
-                                       const double* __restrict__ F, const uint8_t* __restrict__ dir_mask,
-                                       const double* __restrict__ dir_bc, int dir, int bcnz,
-                                       double* __restrict__ vals, double* __restrict__ rhs,
+// Scatter of caller-computed element matrices (P1, P2, FemVec<3,P2>; the local-assembler contract):
+// one warp per row; for every incidence in the records' order (ascending tets) lane d*nloc + c adds
+// the element row's entry at component d, canonical column c: A_t(ci, d canon_local(i, c)), at the
+// record's offset of that column in block d of the row (a vector row (c, r) holds block d = the
+// scalar row's columns of component d).  The columns of one incidence are distinct, so every entry
+// sums its contributions in tet order.  Dirichlet rows: zero except the diagonal = number of
+// incident tets; Dirichlet columns of the other rows: A(i, k) bc_k moved to the right-hand side,
+// then zeroed.
+__global__ void elements_gather_kernel(int64_t nds, int ncomp, int nloc, const int64_t* __restrict__ rowptr,
+                                       const int32_t* __restrict__ col, const int64_t* __restrict__ rowptr_s,
+                                       const int64_t* __restrict__ inc_ptr, const ScatterRec* __restrict__ recs,
+                                       const double* __restrict__ A, const double* __restrict__ F,
+                                       const uint8_t* __restrict__ dir_mask, const double* __restrict__ dir_bc,
+                                       int dir, int bcnz, double* __restrict__ vals, double* __restrict__ rhs,
                                        int* __restrict__ status) {
     const int lane = threadIdx.x & 31;
-    const int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    if (r >= nrows) return;
-    const int64_t b = rowptr[r], e = rowptr[r + 1];
+    const int64_t R = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (R >= nds * ncomp) return;
+    const int c = (int)(R / nds);
+    const int64_t r = R - (int64_t)c * nds;
+    const int NL = ncomp * nloc;
+    const int64_t b = rowptr[R], e = rowptr[R + 1];
+    const int64_t L = rowptr_s[r + 1] - rowptr_s[r];
     for (int64_t k = b + lane; k < e; k += 32) vals[k] = 0.0;
     __syncwarp();
     const int64_t q0 = inc_ptr[r], q1 = inc_ptr[r + 1];
-    const bool isdir = dir && dir_mask[r];
+    const bool isdir = dir && dir_mask[R];
     double f = 0.0, fd = 0.0;
     if (!isdir) {
+        const int d = lane / nloc, cc = lane - d * nloc;
         for (int64_t q = q0; q < q1; ++q) {
             const ScatterRec rec = recs[q];
             const int64_t t = rec.tet;
             const int i = (int)(rec.meta & 15u);
-            if (lane < nloc) {
-                const uint32_t w = lane < 4 ? rec.off03 : (lane < 8 ? rec.off47 : (rec.meta >> 16));
-                const int o = (int)byte_of(w, lane);
-                vals[b + o] += A[(size_t)nloc * nloc * t + i + nloc * canon_local(nloc, i, lane)];
+            if (lane < NL) {
+                const uint32_t w = cc < 4 ? rec.off03 : (cc < 8 ? rec.off47 : (rec.meta >> 16));
+                const int o = (int)byte_of(w, cc);
+                vals[b + d * L + o] +=
+                    A[(size_t)NL * NL * t + (c * nloc + i) + (size_t)NL * (d * nloc + canon_local(nloc, i, cc))];
             }
             __syncwarp();
-            if (F) f += F[(int64_t)nloc * t + i];
+            if (F) f += F[(int64_t)NL * t + c * nloc + i];
         }
         if (dir) {
             for (int64_t k = b + lane; k < e; k += 32)
@@ -1151,15 +1159,16 @@ __global__ void elements_gather_kernel(int64_t nrows, int nloc, const int64_t* _
         if (lane == 0 && q1 > q0) {
             const ScatterRec rd = recs[q0];
             const int dc = canon_diag(nloc, (int)(rd.meta & 15u));
-            vals[b + (int)byte_of(dc < 4 ? rd.off03 : rd.off47, dc)] = (double)(q1 - q0);
+            vals[b + c * L + (int)byte_of(dc < 4 ? rd.off03 : rd.off47, dc)] = (double)(q1 - q0);
         }
-        for (int64_t q = q0; q < q1; ++q) f += dir_bc[r];
+        const double bcr = bcnz ? dir_bc[R] : 0.0;
+        for (int64_t q = q0; q < q1; ++q) f += bcr;
     }
     __syncwarp();
     bool bad = !isfinite(f);
     for (int64_t k = b + lane; k < e; k += 32) bad |= !isfinite(vals[k]);
     if (__any_sync(0xffffffffu, bad) && lane == 0) atomicExch(status, ANIGPU_ERR_NONFINITE);
-    if (rhs && lane == 0) rhs[r] = f;
+    if (rhs && lane == 0) rhs[R] = f;
 }
 
 template <typename Real>
@@ -1463,12 +1472,12 @@ int run_assemble(anigpu_ctx* h, int kind, const double* D, const double* f, doub
 }
 
 int elements_scatter(anigpu_ctx* h, const double* A, const double* F, double* vals, double* rhs) {
-    if (h->space != ANIGPU_P1 && h->space != ANIGPU_P2)
-        return set_err(h, ANIGPU_ERR_UNSUPPORTED, "element-matrix assembly: scalar spaces (vector P2: anigpu_assemble)");
+    if (h->space != ANIGPU_P1 && h->space != ANIGPU_P2 && h->space != ANIGPU_VEC3_P2)
+        return set_err(h, ANIGPU_ERR_UNSUPPORTED, "element-matrix assembly: P1, P2, vector P2 or a general-path space");
     if (!A || !vals) return set_err(h, ANIGPU_ERR_ARG, "NULL element matrices or values");
-    elements_gather_kernel<<<grid_for(h->nds * 32, 256), 256, 0, h->stream>>>(
-        h->nds, h->nloc_s, h->rowptr_s, h->col_s, h->inc_ptr, h->recs, A, F, h->dir_mask, h->dir_bc,
-        h->has_dirichlet ? 1 : 0, h->bc_nonzero ? 1 : 0, vals, rhs, h->d_status);
+    elements_gather_kernel<<<grid_for(h->nds * h->ncomp * 32, 256), 256, 0, h->stream>>>(
+        h->nds, h->ncomp, h->nloc_s, h->rowptr, h->col, h->rowptr_s, h->inc_ptr, h->recs, A, F, h->dir_mask,
+        h->dir_bc, h->has_dirichlet ? 1 : 0, h->bc_nonzero ? 1 : 0, vals, rhs, h->d_status);
     ANI_LAUNCHED(h);
     return ANIGPU_OK;
 }

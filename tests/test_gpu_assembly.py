@@ -355,3 +355,35 @@ def test_assembly_from_element_matrices_fast_template(lib, restated, space, bcnz
     exp = v.cpu().numpy() + vm.cpu().numpy()
     exp[on_dir] = v.cpu().numpy()[on_dir]
     assert np.abs(vkm.cpu().numpy() - exp).max() <= 1e-13 * np.abs(exp).max()
+
+
+@pytest.mark.parametrize("bcnz", [False, True])
+def test_vector_p2_from_element_matrices(lib, bcnz):
+    """The reference's own elasticity form, fem3Dtet<GRAD P2^3, GRAD P2^3> with the 9x9 GENERAL Lame
+    tensor per tet (lin_elast.cpp:100-118), computed by the caller on the library's oriented tets
+    and scattered into the vector template, equals the fast Lame assembly (FP64, 1e-12), right-hand
+    side and per-component Dirichlet values included."""
+    import anigpu
+    from anigpu import meshgen
+    xyz, tets = meshgen.kuhn_cube(3, perturb=0.2, seed=23)
+    nt = tets.shape[0]
+    E = np.exp(0.5 * meshgen.normal(63, nt))
+    nu = 0.2 + 0.25 * meshgen.uniform(64, nt)
+    lam, mu = E * nu / ((1 + nu) * (1 - 2 * nu)), E / (2 * (1 + nu))
+    lib.mesh_upload(xyz, tets)
+    ndof, nnz = lib.problem_setup(anigpu.VEC3_P2)
+    coords = lib.dof_coords().cpu().numpy()
+    mask = (np.abs(coords[:, 0]) < 1e-12).astype(np.uint8)
+    bc = None
+    if bcnz:
+        comp = np.repeat(np.arange(3), ndof // 3)
+        bc = (0.1 * coords[:, 1] - 0.05 * coords[:, 2] + 0.02 * (comp + 1)) * mask
+    lib.set_dirichlet(mask, bc)
+    vals, rhs, _ = lib.assemble(anigpu.TENSOR_LAME, np.stack([lam, mu], axis=1), None, 0.5, 4, anigpu.F64)
+    XY = lib.element_coords()
+    A = lib.fem3dtet(52, 52, XY, _lame9(lam, mu), anigpu.TENSOR_TET_GENERAL, 4)
+    F = lib.fem3dtet(1, 51, XY, np.array([0.5]), anigpu.TENSOR_CONST_SCALAR, 4).reshape(nt, -1)
+    v, r = lib.assemble_elements(A, F)
+    ref_v, ref_r = vals.cpu().numpy(), rhs.cpu().numpy()
+    assert np.abs(v.cpu().numpy() - ref_v).max() <= 1e-12 * np.abs(ref_v).max()
+    assert np.abs(r.cpu().numpy() - ref_r).max() <= 1e-12 * np.abs(ref_r).max()
