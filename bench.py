@@ -252,8 +252,10 @@ def _time_ms(lib, fn, reps=5):
 def run_widened(args, local):
     """Throughput of the rows next to the hot path: the element-level batch (fem3Dtet, P2 GRAD.GRAD
     with per-tet symmetric tensors, order 4, FP64 and FP32), face integrals (fem3Dface IDEN P0 x IDEN
-    P2, order 4, face 0 of every tet), the general-path assembly (P3 GRAD.GRAD on 16^3x6 tets, FP64)
-    and the renumbering of a vector P2 system into MINIBLOCKS (32^3x6 tets, FP32 values)."""
+    P2, order 4, face 0 of every tet), the general-path assembly (P3 GRAD.GRAD on 16^3x6 tets, FP64),
+    the scatter of caller-computed element matrices into the P2 template (48^3x6 tets), a
+    user-defined operator's integral (16^3x6 tets) and the renumbering of a vector P2 system into
+    MINIBLOCKS (32^3x6 tets, FP32 values)."""
     import torch
 
     import anigpu
@@ -284,6 +286,30 @@ def run_widened(args, local):
                                                     np.array([1.0]), 4), reps=3)
     out["general_p3"] = {"tets": int(tets3.shape[0]), "dofs": ndof, "nnz": nnz, "setup_s": setup_s, "ms": ms,
                          "tets_per_s": tets3.shape[0] / (ms * 1e-3)}
+    # the local-assembler contract on the P2 template: element matrices computed by the caller
+    # (fem3Dtet on the oriented tets) scattered by anigpu_assemble_elements, 48^3 x 6 tets, FP64
+    lib.mesh_upload(xyz, tets)
+    ndof2, nnz2 = lib.problem_setup(anigpu.P2)
+    lib.set_dirichlet(meshgen.boundary_mask(lib.dof_coords().cpu().numpy()))
+    XYo = lib.element_coords()
+    Ael = lib.fem3dtet(22, 22, XYo, D6, anigpu.TENSOR_TET_SYM, 4)
+    Fel = lib.fem3dtet(1, 21, XYo, np.array([1.0]), anigpu.TENSOR_CONST_SCALAR, 4).reshape(nt, -1)
+    ms = _time_ms(lib, lambda: lib.assemble_elements(Ael, Fel))
+    moved = nt * (100 + 10) * 8 + nt * 10 * 16 + nnz2 * 8 + ndof2 * 8  # element data, records, values, rhs
+    out["assemble_elements_p2"] = {"tets": nt, "dofs": ndof2, "nnz": nnz2, "ms": ms,
+                                   "tets_per_s": nt / (ms * 1e-3), "GBps": moved / (ms * 1e-3) / 1e9}
+    del Ael, Fel
+    # user-defined operator (ApplyOpCustom): GRAD P2 values per (tet, point) supplied by the caller,
+    # integrated with a per-tet SYM tensor, order 4, FP64, on 16^3 x 6 tets
+    xyzc, tetsc = meshgen.kuhn_cube(16, perturb=0.2, seed=35)
+    ntc = tetsc.shape[0]
+    XYc = torch.tensor(xyzc[tetsc].reshape(-1, 12), device=dev)
+    pts = anigpu.quadrature(4)[0]
+    U = torch.stack([lib.fem3d_apply(22, XYc, pts, np.eye(10)[np.full(ntc, i)]) for i in range(10)], dim=2)
+    Dc = torch.tensor(meshgen.aniso_tensors(ntc, 1.5, 36), device=dev)
+    ms = _time_ms(lib, lambda: lib.fem3dtet_custom(U, XYc, None, Dc, anigpu.TENSOR_TET_SYM, 4))
+    out["fem3dtet_custom_p2"] = {"tets": ntc, "ms": ms, "tets_per_s": ntc / (ms * 1e-3),
+                                 "operator_bytes_per_tet": int(U[0].numel() * 8)}
     # renumbering: vector P2 on 32^3 x 6 tets into MINIBLOCKS
     xyzv, tetsv = meshgen.kuhn_cube(32, perturb=0.2, seed=34)
     ntv = tetsv.shape[0]

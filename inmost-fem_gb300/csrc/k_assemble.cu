@@ -1110,22 +1110,25 @@ __global__ void compact_count_kernel(int64_t n, const int64_t* __restrict__ rowp
 // sums its contributions in tet order.  Dirichlet rows: zero except the diagonal = number of
 // incident tets; Dirichlet columns of the other rows: A(i, k) bc_k moved to the right-hand side,
 // then zeroed.
-__global__ void elements_gather_kernel(int64_t nds, int ncomp, int nloc, const int64_t* __restrict__ rowptr,
+__global__ void elements_gather_kernel(int64_t nds, int ncomp, int nloc, int cap, const int64_t* __restrict__ rowptr,
                                        const int32_t* __restrict__ col, const int64_t* __restrict__ rowptr_s,
                                        const int64_t* __restrict__ inc_ptr, const ScatterRec* __restrict__ recs,
                                        const double* __restrict__ A, const double* __restrict__ F,
                                        const uint8_t* __restrict__ dir_mask, const double* __restrict__ dir_bc,
                                        int dir, int bcnz, double* __restrict__ vals, double* __restrict__ rhs,
                                        int* __restrict__ status) {
+    extern __shared__ double erow[];  // per warp: the row being summed (cap values)
     const int lane = threadIdx.x & 31;
     const int64_t R = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    if (R >= nds * ncomp) return;
+    if (R >= nds * ncomp) return;  // warp-uniform; no block-wide barrier follows
+    double* row = erow + (size_t)(threadIdx.x >> 5) * cap;
     const int c = (int)(R / nds);
     const int64_t r = R - (int64_t)c * nds;
     const int NL = ncomp * nloc;
-    const int64_t b = rowptr[R], e = rowptr[R + 1];
-    const int64_t L = rowptr_s[r + 1] - rowptr_s[r];
-    for (int64_t k = b + lane; k < e; k += 32) vals[k] = 0.0;
+    const int64_t b = rowptr[R];
+    const int len = (int)(rowptr[R + 1] - b);
+    const int L = (int)(rowptr_s[r + 1] - rowptr_s[r]);
+    for (int k = lane; k < len; k += 32) row[k] = 0.0;
     __syncwarp();
     const int64_t q0 = inc_ptr[r], q1 = inc_ptr[r + 1];
     const bool isdir = dir && dir_mask[R];
@@ -1139,17 +1142,17 @@ __global__ void elements_gather_kernel(int64_t nds, int ncomp, int nloc, const i
             if (lane < NL) {
                 const uint32_t w = cc < 4 ? rec.off03 : (cc < 8 ? rec.off47 : (rec.meta >> 16));
                 const int o = (int)byte_of(w, cc);
-                vals[b + d * L + o] +=
+                row[d * L + o] +=
                     A[(size_t)NL * NL * t + (c * nloc + i) + (size_t)NL * (d * nloc + canon_local(nloc, i, cc))];
             }
             __syncwarp();
             if (F) f += F[(int64_t)NL * t + c * nloc + i];
         }
         if (dir) {
-            for (int64_t k = b + lane; k < e; k += 32)
-                if (dir_mask[col[k]]) {
-                    if (bcnz) fd += vals[k] * dir_bc[col[k]];
-                    vals[k] = 0.0;
+            for (int k = lane; k < len; k += 32)
+                if (dir_mask[col[b + k]]) {
+                    if (bcnz) fd += row[k] * dir_bc[col[b + k]];
+                    row[k] = 0.0;
                 }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) fd += __shfl_xor_sync(0xffffffffu, fd, o);
@@ -1159,14 +1162,18 @@ __global__ void elements_gather_kernel(int64_t nds, int ncomp, int nloc, const i
         if (lane == 0 && q1 > q0) {
             const ScatterRec rd = recs[q0];
             const int dc = canon_diag(nloc, (int)(rd.meta & 15u));
-            vals[b + c * L + (int)byte_of(dc < 4 ? rd.off03 : rd.off47, dc)] = (double)(q1 - q0);
+            row[c * L + (int)byte_of(dc < 4 ? rd.off03 : rd.off47, dc)] = (double)(q1 - q0);
         }
         const double bcr = bcnz ? dir_bc[R] : 0.0;
         for (int64_t q = q0; q < q1; ++q) f += bcr;
     }
     __syncwarp();
     bool bad = !isfinite(f);
-    for (int64_t k = b + lane; k < e; k += 32) bad |= !isfinite(vals[k]);
+    for (int k = lane; k < len; k += 32) {
+        const double v = row[k];
+        bad |= !isfinite(v);
+        vals[b + k] = v;
+    }
     if (__any_sync(0xffffffffu, bad) && lane == 0) atomicExch(status, ANIGPU_ERR_NONFINITE);
     if (rhs && lane == 0) rhs[R] = f;
 }
@@ -1475,8 +1482,12 @@ int elements_scatter(anigpu_ctx* h, const double* A, const double* F, double* va
     if (h->space != ANIGPU_P1 && h->space != ANIGPU_P2 && h->space != ANIGPU_VEC3_P2)
         return set_err(h, ANIGPU_ERR_UNSUPPORTED, "element-matrix assembly: P1, P2, vector P2 or a general-path space");
     if (!A || !vals) return set_err(h, ANIGPU_ERR_ARG, "NULL element matrices or values");
-    elements_gather_kernel<<<grid_for(h->nds * h->ncomp * 32, 256), 256, 0, h->stream>>>(
-        h->nds, h->ncomp, h->nloc_s, h->rowptr, h->col, h->rowptr_s, h->inc_ptr, h->recs, A, F, h->dir_mask,
+    const int cap = h->max_row_len_s * h->ncomp;  // the longest row of the template
+    const size_t smem = sizeof(double) * 8 * (size_t)cap;
+    if (smem > 227 * 1024) return set_err(h, ANIGPU_ERR_UNSUPPORTED, "template rows too long for the element scatter");
+    ANI_CUDA(h, cudaFuncSetAttribute(elements_gather_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    elements_gather_kernel<<<grid_for(h->nds * h->ncomp * 32, 256), 256, smem, h->stream>>>(
+        h->nds, h->ncomp, h->nloc_s, cap, h->rowptr, h->col, h->rowptr_s, h->inc_ptr, h->recs, A, F, h->dir_mask,
         h->dir_bc, h->has_dirichlet ? 1 : 0, h->bc_nonzero ? 1 : 0, vals, rhs, h->d_status);
     ANI_LAUNCHED(h);
     return ANIGPU_OK;
