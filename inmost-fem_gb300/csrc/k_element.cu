@@ -1,14 +1,18 @@
 // Element level: the batched fem3Dtet (every operator pair, every tensor kind), the
 // physical quadrature points and the element-level Dirichlet elimination.
 //
-// This is the quadrature-faithful path that mirrors Ani::fem3Dtet
-// (anifem++/fem/operations/int_tet.inl:93-122 -> core.inl:277-367):
+// Ani::fem3Dtet (anifem++/fem/operations/int_tet.inl:93-122 -> core.inl:277-367) computes
 //     U = OpA(phi) at every quadrature point, V = OpB(phi),
 //     DU = w_n |T| D(x_n) U          (internal_Dfunc::applyDU, diff_tensor.h:275-994)
 //     A  = V^T DU                      (fusive_AT_mul_B, core.inl:28-60)
-// One CTA per tetrahedron (grid-stride); the reference-element tables of both spaces
-// are staged once per CTA in shared memory, U/V/DU of one quadrature point live in
-// shared memory, and each thread owns a fixed set of entries of A in registers.
+// Three kernels, chosen per call by launch_fem3dtet:
+//   fem3dtet_reftensor_lanes_kernel  scalar spaces, IDEN/GRAD, tensors constant on a tet, at most
+//                                    100 entries: the same sum regrouped through reference tensors
+//                                    (lanes over tets);
+//   fem3dtet_reftensor_kernel        the same with lanes over entries, for larger matrices;
+//   fem3dtet_kernel                  everything else (FemVec, ND0/RT0, per-point tensors,
+//                                    fem3DfaceN, user-defined operators): one warp per tet, the
+//                                    per-point quadrature in shared memory.
 #include <cstring>
 
 #include "anigpu_internal.h"
