@@ -1118,6 +1118,9 @@ __global__ void elements_gather_kernel(int64_t nds, int ncomp, int nloc, int cap
                                        int dir, int bcnz, double* __restrict__ vals, double* __restrict__ rhs,
                                        int* __restrict__ status) {
     extern __shared__ double erow[];  // per warp: the row being summed (cap values)
+    __shared__ int8_t canon[100];     // canon_local(nloc, i, c) at i * nloc + c
+    for (int k = threadIdx.x; k < nloc * nloc; k += blockDim.x) canon[k] = (int8_t)canon_local(nloc, k / nloc, k % nloc);
+    __syncthreads();
     const int lane = threadIdx.x & 31;
     const int64_t R = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     if (R >= nds * ncomp) return;  // warp-uniform; no block-wide barrier follows
@@ -1142,8 +1145,7 @@ __global__ void elements_gather_kernel(int64_t nds, int ncomp, int nloc, int cap
             if (lane < NL) {
                 const uint32_t w = cc < 4 ? rec.off03 : (cc < 8 ? rec.off47 : (rec.meta >> 16));
                 const int o = (int)byte_of(w, cc);
-                row[d * L + o] +=
-                    A[(size_t)NL * NL * t + (c * nloc + i) + (size_t)NL * (d * nloc + canon_local(nloc, i, cc))];
+                row[d * L + o] += A[(size_t)NL * NL * t + (c * nloc + i) + (size_t)NL * (d * nloc + canon[i * nloc + cc])];
             }
             __syncwarp();
             if (F) f += F[(int64_t)NL * t + c * nloc + i];
