@@ -260,9 +260,10 @@ int anigpu_assemble(anigpu_handle h, int tensor_kind, const double* D, const dou
  * and latency-critical loops that cannot afford cudaMalloc's implicit device-wide
  * synchronisation.  Same arguments and results as anigpu_assemble without the touched map.
  * It calls no cudaMalloc, cudaFree or other allocating routine: its scratch (the per-tet
- * blocks and the reference tables) is a fixed 16 MiB device array inside the library, which
- * every GPU that loads the library holds until the process exits.  Limit: 524,288 tets in
- * F32, 262,144 in F64; larger meshes are rejected with ANIGPU_ERR_ARG and a message.  The
+ * blocks and the reference tables) is a fixed device array inside the library (16 MiB of
+ * per-tet blocks plus 16 KiB of tables), which every GPU that loads the library holds until the
+ * process exits.  Limit: 524,288 tets in F32 (32 bytes a tet), 262,144 in F64 (64 bytes a
+ * tet); larger meshes are rejected with ANIGPU_ERR_ARG and a message.  The
  * handle must already be set up (anigpu_problem_setup and anigpu_set_dirichlet allocate).
  * The first call on a device looks up the array's device address (cudaGetSymbolAddress) and
  * should come before any stream capture.  All calls share the one array: calls that overlap

@@ -73,13 +73,13 @@ def build_library(verbose=False, force=False):
 
 def build_oracle(with_reference=True, verbose=False):
     """Build the oracle (test infrastructure): the C restatement always, and the
-    reference's own fem3Dtet when the reference sources are present on this machine."""
+    reference's own fem3Dtet when ANIFEM_REF_ROOT names a checkout of the reference sources."""
     oracle = os.path.join(REPO, "oracle")
     r = subprocess.run(["make", "-C", oracle, "restate"], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + r.stdout + r.stderr)
-    ref_root = os.environ.get("ANIFEM_REF_ROOT", "/root/reference")
-    if with_reference and os.path.isdir(os.path.join(ref_root, "anifem++")):
+    ref_root = os.environ.get("ANIFEM_REF_ROOT", "")
+    if with_reference and ref_root and os.path.isdir(os.path.join(ref_root, "anifem++")):
         r = subprocess.run(["make", "-C", oracle, "ref", f"REF_ROOT={ref_root}"], capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("reference oracle build failed:\n" + r.stdout + r.stderr)

@@ -1551,7 +1551,8 @@ int run_compact(anigpu_ctx* h, int64_t* rowptr, int32_t* col, void* vals, int pr
 // library holds it (kNoallocScratchBytes) until the process exits.
 namespace {
 constexpr size_t kNoallocTableBytes = 16u << 10;  // reference tables, at the start
-constexpr size_t kNoallocScratchBytes = 16u << 20;
+constexpr size_t kNoallocBlockBytes = 16u << 20;  // per-tet blocks: 524,288 tets in FP32, 262,144 in FP64
+constexpr size_t kNoallocScratchBytes = kNoallocTableBytes + kNoallocBlockBytes;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
 constexpr int kNoallocMaxDevices = 64;
 void* g_noalloc_dev_ptr[kNoallocMaxDevices] = {};
@@ -1659,12 +1660,13 @@ extern "C" int anigpu_assemble_noalloc(anigpu_handle h, int tensor_kind, const d
     if (precision != ANIGPU_F32 && precision != ANIGPU_F64) return set_err(h, ANIGPU_ERR_ARG, "precision");
     const size_t rsz = precision == ANIGPU_F32 ? 4 : 8;
     const size_t need = (size_t)h->nt * 8 * rsz;
-    if (need > kNoallocScratchBytes - kNoallocTableBytes)
+    if (need > kNoallocBlockBytes)
         return set_err(h, ANIGPU_ERR_ARG,
                        "anigpu_assemble_noalloc: mesh too large for the fixed scratch (" +
                            std::to_string(h->nt) + " tets need " + std::to_string(need) + " bytes, limit " +
-                           std::to_string(kNoallocScratchBytes - kNoallocTableBytes) +
-                           " bytes: 524288 tets in FP32, 262144 in FP64)");
+                           std::to_string(kNoallocBlockBytes) + " bytes: " +
+                           std::to_string(kNoallocBlockBytes / 32) + " tets in FP32, " +
+                           std::to_string(kNoallocBlockBytes / 64) + " in FP64)");
     unsigned char* scratch = nullptr;
     int rc = noalloc_scratch(h, &scratch);
     if (rc) return rc;
@@ -1691,7 +1693,7 @@ extern "C" int anigpu_assemble_noalloc(anigpu_handle h, int tensor_kind, const d
         tet_prepare_f64_kernel<<<grid_for(h->nt, 256), 256, 0, h->stream>>>(
             h->nt, h->xyz, h->tets, tensor_kind, D, f, f_const, (double*)tetK, h->d_status);
     ANI_LAUNCHED(h);
-    RowParams p;
+    RowParams p{};
     p.inc_ptr = h->inc_ptr;
     p.recs = h->recs;
     p.rowptr = h->rowptr_s;

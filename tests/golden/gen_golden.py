@@ -76,7 +76,9 @@ def point_tensor(fn, X, nr, nc):
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref_root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("ANIFEM_REF_ROOT", "")
+    if not ref_root:
+        raise SystemExit("usage: gen_golden.py REF_ROOT (or set ANIFEM_REF_ROOT)")
     if not Reference.available():
         raise SystemExit("build the reference oracle first: make -C oracle ref")
     R = Reference()
