@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--no-elasticity", action="store_true", help="skip the vector-P2 elasticity workload")
     ap.add_argument("--no-widened", action="store_true", help="skip the element-level / face / general-path rows")
     ap.add_argument("--cpu-sample", type=int, default=0, help="tets in the CPU-baseline sample (0 = auto)")
+    ap.add_argument("--no-parity", action="store_true", help="skip the full-size oracle check after the timed steps")
+    ap.add_argument("--no-config1", action="store_true", help="skip the P1 Poisson (config 1) line")
     return ap.parse_args()
 
 
@@ -335,6 +337,80 @@ def peaks():
         return 6800.0, "fallback"
 
 
+class NvmlClockSampler:
+    """SM clocks and throttle reasons of this process's GPU read through NVML (libnvidia-ml, the
+    driver's library) every millisecond during the timed region, so that timed regions of a few
+    milliseconds still get samples.  The GPU is found by its UUID (CUDA and NVML index GPUs
+    differently when CUDA_VISIBLE_DEVICES is set)."""
+    # nvmlClocksEventReasons bits
+    BITS = {"sw_power_cap": 0x4, "hw_slowdown": 0x8, "sw_thermal_slowdown": 0x20, "hw_thermal_slowdown": 0x40}
+
+    def __init__(self, device):
+        import ctypes
+        self.ct = ctypes
+        self.device = device
+        self.samples = []
+        self.ok = False
+        self.stop = threading.Event()
+        try:
+            import torch
+            self.nvml = ctypes.CDLL("libnvidia-ml.so.1")
+            if self.nvml.nvmlInit_v2() != 0:
+                return
+            h = ctypes.c_void_p()
+            uuid = str(torch.cuda.get_device_properties(device).uuid)
+            got = -1
+            for cand in (uuid, "GPU-" + uuid):
+                got = self.nvml.nvmlDeviceGetHandleByUUID(cand.encode(), ctypes.byref(h))
+                if got == 0:
+                    break
+            if got != 0:
+                return
+            self.h = h
+            mx = ctypes.c_uint()
+            self.nvml.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx))  # NVML_CLOCK_SM
+            self.smax = float(mx.value)
+            self.ok = True
+        except Exception:
+            self.ok = False
+
+    def _run(self):
+        ct = self.ct
+        clk, rs = ct.c_uint(), ct.c_ulonglong()
+        get_reasons = getattr(self.nvml, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            self.nvml.nvmlDeviceGetCurrentClocksThrottleReasons
+        while not self.stop.is_set():
+            if self.nvml.nvmlDeviceGetClockInfo(self.h, 1, ct.byref(clk)) == 0 and \
+                    get_reasons(self.h, ct.byref(rs)) == 0:
+                self.samples.append((float(clk.value), int(rs.value)))
+            time.sleep(0.001)
+
+    def __enter__(self):
+        if self.ok:
+            self.t = threading.Thread(target=self._run, daemon=True)
+            self.t.start()
+            t0 = time.time()
+            while not self.samples and time.time() - t0 < 2:
+                time.sleep(0.001)
+        return self
+
+    def __exit__(self, *a):
+        if self.ok:
+            self.stop.set()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        sm = [c for c, _ in self.samples]
+        reasons = sorted(nm for nm, bit in self.BITS.items() if any(r & bit for _, r in self.samples))
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": self.smax if self.ok else None,
+                "reasons": reasons, "samples": len(sm), "source": "nvml, 1 ms"}
+
+
+def clock_sampler(device):
+    s = NvmlClockSampler(device)
+    return s if s.ok else ClockSampler(device)
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons during the timed region."""
     Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
@@ -420,6 +496,88 @@ def cpu_baseline(xyz, tets, D6, sample, threads):
     return sample / sec, sec
 
 
+def oracle_parity(xyz, tets, D6, mask, vals64, rhs64, vals32, rowptr, col, threads):
+    """Outside the timed region: the restated assembler (oracle, all host threads) on the full
+    workload against the GPU's FP64 and FP32 assemblies.  Its phase times are the CPU baseline of
+    the whole FP64 assembly (element loop + Dirichlet + CSR scatter; a restatement of AssemblerT)."""
+    from anigpu import meshgen
+    from oracle.oracle import TET_SYM, Restated
+    orc = Restated()
+    ref = orc.assemble_problem_mt(xyz, tets, 2, TET_SYM, D6, 1.0, 4, dirichlet=(mask, None), threads=threads)
+    same = bool(np.array_equal(rowptr, ref["rowptr"]) and np.array_equal(col, ref["col"]))
+    vmax = np.abs(ref["vals"]).max()
+    f64_vals = float(np.abs(vals64 - ref["vals"]).max() / vmax)
+    f64_rhs = float(np.abs(rhs64 - ref["rhs"]).max() / np.abs(ref["rhs"]).max())
+    n = rowptr.size - 1
+    rows = np.repeat(np.arange(n), np.diff(ref["rowptr"]))
+    rown = np.sqrt(np.bincount(rows, ref["vals"] ** 2, minlength=n))
+    err = np.sqrt(np.bincount(rows, (vals32.astype(np.float64) - ref["vals"]) ** 2, minlength=n)) / np.maximum(rown, 1e-300)
+    sec = ref["seconds"]
+    return {
+        "checked": True, "template_equal": same, "f64_max_rel_err": f64_vals, "f64_rhs_max_rel_err": f64_rhs,
+        "parity_checked": bool(same and f64_vals <= 1e-12 and f64_rhs <= 1e-12),
+        "fp32_error": {"row_rel_err_max": float(err.max()), "row_rel_err_median": float(np.median(err)),
+                       "definition": "per CSR row ||a32 - a64_oracle|| / ||a64_oracle||"},
+        "fp64_redo_tets": meshgen.fp64_redo_count(xyz, tets),
+        "oracle": {"threads": ref["threads"], "seconds": sec},
+    }, ref
+
+
+def run_config1(local):
+    """The plain FP64 method on the P1 Poisson system: 16^3 x 6 Kuhn tets (unperturbed), identity
+    tensor, order 2, f = 1, homogeneous Dirichlet, Jacobi-PCG to 1e-10; GPU against the oracle's
+    restated assembler and CPU Jacobi-PCG (serial, a restatement)."""
+    import torch
+
+    import anigpu
+    from anigpu import meshgen
+    from oracle.oracle import NULL, Restated
+    orc = Restated()
+    xyz, tets = meshgen.kuhn_cube(16)
+    lib = anigpu.Anigpu(local)
+    lib.mesh_upload(xyz, tets)
+    ndof, nnz = lib.problem_setup(anigpu.P1)
+    mask = meshgen.boundary_mask(lib.dof_coords().cpu().numpy())
+    lib.set_dirichlet(mask)
+    for _ in range(3):
+        vals, rhs, _ = lib.assemble(anigpu.TENSOR_NULL, None, None, 1.0, 2, anigpu.F64)
+    reps = 20
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(lib.stream)
+    for _ in range(reps):
+        lib.assemble(anigpu.TENSOR_NULL, None, None, 1.0, 2, anigpu.F64, vals, rhs, sync=False)
+    e1.record(lib.stream)
+    lib.status()
+    torch.cuda.synchronize()
+    asm_ms = e0.elapsed_time(e1) / reps
+    for _ in range(2):
+        x, st = lib.solve(vals, rhs, anigpu.SOLVE_JACOBI_PCG, anigpu.F64, rtol=1e-10, maxit=100000)
+    t0 = time.perf_counter()
+    ref = orc.assemble_problem(xyz, tets, 1, NULL, None, 1.0, 2, dirichlet=(mask, None))
+    cpu_asm_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    xo, it_o, rel_o = orc.jacobi_pcg(ref["rowptr"], ref["col"], ref["vals"], ref["rhs"], 1e-10, 100000)
+    cpu_pcg_s = time.perf_counter() - t0
+    rp, col = lib.csr_template()
+    tr = orc.true_residual(ref["rowptr"], ref["col"], ref["vals"], x.cpu().numpy(), ref["rhs"])
+    out = {
+        "workload": f"P1 Poisson, 16^3x6 Kuhn tets ({tets.shape[0]} tets, {ndof} DOFs, {nnz} nnz), identity tensor, "
+                    f"order 2, homogeneous Dirichlet, FP64 Jacobi-PCG to 1e-10",
+        "assembly_ms": asm_ms, "assembly_tets_per_s": tets.shape[0] / (asm_ms * 1e-3),
+        "pcg_seconds": st.seconds, "pcg_iterations": st.iterations, "rel_residual_f64": tr,
+        "time_to_solution_s": asm_ms * 1e-3 + st.seconds,
+        "parity": {"template_equal": bool(np.array_equal(rp.cpu().numpy(), ref["rowptr"]) and
+                                          np.array_equal(col.cpu().numpy(), ref["col"])),
+                   "vals_max_rel_err": float(np.abs(vals.cpu().numpy() - ref["vals"]).max() / np.abs(ref["vals"]).max()),
+                   "oracle_pcg_iterations": it_o},
+        "cpu_restated": {"assembly_s": cpu_asm_s, "pcg_s": cpu_pcg_s, "pcg_iterations": it_o, "threads": 1,
+                         "kind": "restatement (oracle assembler and Jacobi-PCG, serial: the reference's default)"},
+    }
+    lib.close()
+    return out
+
+
 def run_reference(args):
     world, rank, local, pg = dist_setup(args)
     if rank != 0:
@@ -492,7 +650,7 @@ def run_ours(args):
     # throughput: assemblies enqueued back to back (anigpu_assemble_async), status checked once
     launches0 = lib.launch_count()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    with ClockSampler(local) as clk:
+    with clock_sampler(local) as clk:
         torch.cuda.synchronize()
         for k in range(args.steps):
             ev[k][0].record(stream)
@@ -632,6 +790,23 @@ def run_ours(args):
                                     "rel_residual_vs_f64_matrix": float(r64.norm() / rhs64.norm()),
                                     "weights": "trained (anigpu/weights)" if trained else "untrained",
                                     "speedup_vs_jacobi_pcg_f64": solve["jacobi_pcg_f64"]["seconds"] / tot}
+            # the same preconditioner and FP32 inner operator, with the FP64-assembled system judging
+            # every residual replacement and the stop: the FP64 relative residual on the FP64 system
+            for _ in range(2):
+                x2, st2 = lib.solve_refined(vals32, vals64, rhs64, anigpu.SOLVE_FCG_LEARNED, rtol=1e-8,
+                                            maxit=200000, check=False)
+            tot2 = bind_s + st2.seconds
+            solve["fcg_learned_refined_f64"] = {
+                "seconds": st2.seconds, "bind_seconds": bind_s, "iterations": st2.iterations,
+                "replacements": st2.outer_iterations, "fallback_steps": st2.fallback_steps,
+                "rel_residual_vs_f64_matrix": st2.rel_residual,
+                "speedup_vs_jacobi_pcg_f64": solve["jacobi_pcg_f64"]["seconds"] / tot2}
+            for _ in range(2):
+                x3, st3 = lib.solve_refined(vals32, vals64, rhs64, anigpu.SOLVE_IR_CG32, rtol=1e-8, maxit=200000,
+                                            check=False)
+            solve["ir_cg32_refined_f64"] = {"seconds": st3.seconds, "iterations": st3.iterations,
+                                            "outer": st3.outer_iterations,
+                                            "rel_residual_vs_f64_matrix": st3.rel_residual}
         except anigpu.AnigpuError as e:
             solve["fcg_learned"] = {"unavailable": str(e)}
         # post-processing: gradient of the solution at the 14 order-4 quadrature points of every
@@ -661,9 +836,14 @@ def run_ours(args):
     if not args.no_widened and rank == 0:
         widened = run_widened(args, local)
 
+    config1 = None
+    if not args.no_config1 and rank == 0:
+        config1 = run_config1(local)
+
     if rank != 0:
         return
     cpu = None
+    parity = None
     if world == 1:
         threads = os.cpu_count() or 1
         sample = args.cpu_sample or nt
@@ -676,6 +856,32 @@ def run_ours(args):
                          f"({sec:.1f} s), oracle port on {threads} host threads",
                "single_thread": {"value": v1, "unit": UNIT, "cores": 1,
                                  "sample": f"first {s1} tets ({sec1:.1f} s), one host thread"}}
+        cal = os.path.join(REPO, "oracle", "port_calibration.json")
+        if os.path.exists(cal):
+            with open(cal) as fh:
+                cpu["port_calibration"] = json.load(fh)
+        if not args.no_parity:
+            rp_t, col_t = lib.csr_template()
+            parity, ref = oracle_parity(xyz, tets, D6, mask, vals64.cpu().numpy(), rhs64.cpu().numpy(),
+                                        vals32.cpu().numpy(), rp_t.cpu().numpy(), col_t.cpu().numpy(), threads)
+            osec = parity["oracle"]["seconds"]
+            cpu_asm = osec["elements"] + osec["dirichlet"] + osec["scatter"]
+            cpu["assembly_f64"] = {
+                "kind": "restatement (oracle element loop + applyDir + CSR scatter of the whole mesh)",
+                "cores": threads, "seconds": cpu_asm, "value": nt / cpu_asm, "unit": UNIT,
+                "scatter_seconds": osec["scatter"], "elements_seconds": osec["elements"],
+                "gpu_f64_over_cpu_f64": (nt / (f64_ms * 1e-3)) / (nt / cpu_asm)}
+            if solve and "jacobi_pcg_f64" in solve:
+                from oracle.oracle import Restated
+                spi = Restated().pcg_seconds_per_iteration(ref["rowptr"], ref["col"], ref["vals"], ref["rhs"], 20,
+                                                           threads)
+                it = solve["jacobi_pcg_f64"]["iterations"]
+                cpu["solve_jacobi_pcg_f64"] = {
+                    "kind": "restatement (FP64 Jacobi-PCG on the oracle CSR, all host threads; the reference "
+                            "solves through INMOST)", "cores": threads, "seconds_per_iteration": spi,
+                    "iterations": it, "seconds_to_1e-8": spi * it,
+                    "sample": "20 iterations timed, times the GPU's iteration count to 1e-8"}
+            del ref
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -699,7 +905,9 @@ def run_ours(args):
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
+        "parity": parity,
         "f64_assembly": {"ms": f64_ms, "value": nt / (f64_ms * 1e-3), "unit": UNIT},
+        "config1": config1,
         "setup_s": setup_s,
         "solve": solve,
         "batched": batched,

@@ -36,7 +36,7 @@ extern "C" {
 #define ANIGPU_P3 3
 #define ANIGPU_VEC3_P1 4
 #define ANIGPU_VEC3_P2 5
-/* scalar spaces of the element level only (anifem++/fem/operators.h:26-34, spaces/*.h):
+/* scalar spaces of the element level only (anifem++/fem/operators.h:26-34 and the spaces/ headers):
  * Crouzeix-Raviart (4 face DOFs, 1 - 3 lambda of the opposite vertex), edge bubbles
  * (4 lambda_i lambda_j in edge order), the volume bubble (256 lambda_0 lambda_1 lambda_2 lambda_3) */
 #define ANIGPU_CR1 6
@@ -115,7 +115,9 @@ int anigpu_last_timing(anigpu_handle h, double* ms_host, int cap);
  *   D : tensor data by kind (see above), doubles
  *   A : nt * nfB * nfA values (F64 or F32 by precision), per tet column-major nfB x nfA,
  *       A(i_test, j_trial), exactly the DenseMatrix A of fem3Dtet
- *   order: quadrature order 0..6 (the stack-memory fem3Dtet limit, int_tet.inl:98-99) */
+ *   order: quadrature order 0..20 (the rules of tetrahedron_quadrature_formulas; the
+ *          memoryless fem3Dtet stops at 6, int_tet.inl:98-99, its PlainMemory overload,
+ *          int_tet.inl:30-57, takes them all) */
 int anigpu_fem3dtet(anigpu_handle h, int opA, int opB, int tensor_kind, int order, int precision, int64_t nt,
                     const double* XY, const double* D, void* A);
 
@@ -233,6 +235,10 @@ int anigpu_element_dofs(anigpu_handle h, int32_t* edofs);
  * elemental_assembler.h:221), so that element matrices computed from them by anigpu_fem3dtet fit
  * anigpu_element_dofs and anigpu_assemble_elements */
 int anigpu_element_coords(anigpu_handle h, double* XY);
+/* vertex ids of every tet in the same reoriented local order, tets[nt*4] (i32, device or host):
+ * which mesh node each local node of anigpu_element_coords is (the ElementalAssembler's node
+ * list, elemental_assembler.h:221, after reorderNodesOnTetrahedron, ordering.inl:9-26) */
+int anigpu_element_nodes(anigpu_handle h, int32_t* tets);
 /* coordinates of every DOF's node: xyz[ndof*3] (f64, device).  Vertex DOFs sit at the
  * vertex, P2 edge DOFs at the edge midpoint (DOF_coord<FEM_P2>, anifem++/fem/operators.h:750-767);
  * vector components repeat the scalar coordinates. */
@@ -318,6 +324,13 @@ int anigpu_csr_compact(anigpu_handle h, int64_t* rowptr, int32_t* col, void* val
  * and the result).  Convergence: ||b - A x||_2 <= rtol * ||b||_2 in FP64. */
 int anigpu_solve(anigpu_handle h, int method, const void* vals, int precision, const double* b, double* x,
                  double rtol, int64_t maxit, anigpu_solve_stats* stats);
+/* The same solve of the FP64-assembled system vals64 (the system the reference solves) with its
+ * FP32-assembled counterpart vals32 as the operator of the inner iterations: IR_CG32 (outer residual
+ * b - A64 x, inner FP32 CG on vals32) or FCG_LEARNED (FCG on vals32, bound by anigpu_gnn_bind; every
+ * residual replacement and the convergence test use b - A64 x in FP64).  Convergence: ||b - A64 x||
+ * <= rtol ||b||.  No counterpart in the reference (its solver is INMOST's, ex1.cpp:161-163). */
+int anigpu_solve_refined(anigpu_handle h, int method, const float* vals32, const double* vals64, const double* b,
+                         double* x, double rtol, int64_t maxit, anigpu_solve_stats* stats);
 /* ---- learned preconditioner for ANIGPU_SOLVE_FCG_LEARNED (no counterpart in the reference,
  * whose solves go through INMOST's ILU-Krylov, examples/tutorials/ex1.cpp:161-163).
  *   M r = D^-1 r + P Dc^-1/2 B B^T Dc^-1/2 P^T r,   B = sum_{k<4} diag(a_k) A_hat^k

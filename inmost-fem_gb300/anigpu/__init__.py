@@ -74,6 +74,7 @@ SIGNATURES = {
     "anigpu_csr_template": (_i, [_vp, _vp, _vp]),
     "anigpu_element_dofs": (_i, [_vp, _vp]),
     "anigpu_element_coords": (_i, [_vp, _vp]),
+    "anigpu_element_nodes": (_i, [_vp, _vp]),
     "anigpu_dof_coords": (_i, [_vp, _vp]),
     "anigpu_set_dirichlet": (_i, [_vp, _vp, _vp]),
     "anigpu_assemble": (_i, [_vp, _i, _vp, _vp, _d, _i, _i, _vp, _vp, _vp, _d]),
@@ -84,6 +85,7 @@ SIGNATURES = {
     "anigpu_assemble_noalloc": (_i, [_vp, _i, _vp, _vp, _d, _i, _i, _vp, _vp, _d]),
     "anigpu_csr_compact": (_i, [_vp, _vp, _vp, _vp, _i, _vp, ctypes.POINTER(_i64)]),
     "anigpu_solve": (_i, [_vp, _i, _vp, _i, _vp, _vp, _d, _i64, ctypes.POINTER(SolveStats)]),
+    "anigpu_solve_refined": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _d, _i64, ctypes.POINTER(SolveStats)]),
     "anigpu_spmv": (_i, [_vp, _vp, _i, _vp, _vp]),
     "anigpu_batch_set_instances": (_i, [_vp, _i, _vp, _vp]),
     "anigpu_batch_info": (_i, [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i), _vp, ctypes.POINTER(_i)]),
@@ -159,9 +161,9 @@ def quadrature(order):
     """(points[np,4], weights[np]) -- tetrahedron_quadrature_formulas(order)."""
     import numpy as np
     lib = load_library()
-    p = np.zeros(4 * 64)
-    w = np.zeros(64)
-    n = lib.anigpu_quadrature(order, p.ctypes.data, w.ctypes.data, 64)
+    p = np.zeros(4 * 1024)
+    w = np.zeros(1024)
+    n = lib.anigpu_quadrature(order, p.ctypes.data, w.ctypes.data, 1024)
     if n < 0:
         raise AnigpuError(n, f"no quadrature rule of order {order}")
     return p[:4 * n].reshape(n, 4).copy(), w[:n].copy()
@@ -604,6 +606,20 @@ class Anigpu:
         st = SolveStats()
         rc = self.lib.anigpu_solve(self.h, method, _ptr(vals), precision, _ptr(b), _ptr(x), float(rtol), int(maxit),
                                    ctypes.byref(st))
+        if check:
+            self._check(rc)
+        return x, st
+
+    def solve_refined(self, vals32, vals64, b, method=SOLVE_FCG_LEARNED, x0=None, rtol=1e-8, maxit=100000,
+                      check=True):
+        """Solve the FP64-assembled system vals64 with the FP32-assembled vals32 as the inner operator
+        (anigpu_solve_refined): every residual replacement and the convergence test use FP64 b - A64 x."""
+        torch = self.torch
+        b = self._dev(b, torch.float64)
+        x = torch.zeros_like(b) if x0 is None else self._dev(x0, torch.float64).clone()
+        st = SolveStats()
+        rc = self.lib.anigpu_solve_refined(self.h, method, _ptr(vals32), _ptr(vals64), _ptr(b), _ptr(x), float(rtol),
+                                           int(maxit), ctypes.byref(st))
         if check:
             self._check(rc)
         return x, st

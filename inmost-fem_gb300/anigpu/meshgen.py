@@ -135,3 +135,44 @@ def union(meshes):
         voff += xyz.shape[0]
         toff.append(toff[-1] + tets.shape[0])
     return np.concatenate(xs), np.concatenate(ts), np.asarray(toff, dtype=np.int64)
+
+
+def p2_aniso_workload(n, seed=2024):
+    """The P2 anisotropic-diffusion workload: n^3 x 6 Kuhn tets, interior vertices perturbed by
+    U(-0.2h, 0.2h), per-tet tensors D = R diag(exp g) R^T with g ~ N(0, 1.5^2).
+    Returns (xyz, tets, D sym6)."""
+    xyz, tets = kuhn_cube(n, perturb=0.2, seed=seed)
+    return xyz, tets, aniso_tensors(tets.shape[0], 1.5, seed + 1)
+
+
+def elasticity_workload(n, seed=48):
+    """The vector-P2 elasticity workload: n^3 x 6 perturbed Kuhn tets, per-tet Lame parameters from
+    E ~ lognormal(0, 0.5^2), nu ~ U[0.2, 0.45].  Returns (xyz, tets, LM [nt, 2] = (lambda, mu))."""
+    xyz, tets = kuhn_cube(n, perturb=0.2, seed=seed)
+    nt = tets.shape[0]
+    E = np.exp(0.5 * normal(seed * 100 + 1, nt))
+    nu = 0.2 + 0.25 * uniform(seed * 100 + 2, nt)
+    return xyz, tets, np.stack([E * nu / ((1 + nu) * (1 - 2 * nu)), E / (2 * (1 + nu))], axis=1)
+
+
+def lame9(lam, mu):
+    """The Lame tensor as the 9x9 GENERAL tensor of Operator<GRAD, FemVec<3,P2>> (index j + 3c for
+    derivative j of component c), [nt, 81]; symmetric, so column- and row-major agree."""
+    lam, mu = np.asarray(lam), np.asarray(mu)
+    D = np.zeros((lam.size, 9, 9))
+    for c1 in range(3):
+        for j1 in range(3):
+            for c2 in range(3):
+                for j2 in range(3):
+                    D[:, j1 + 3 * c1, j2 + 3 * c2] = (lam * (j1 == c1) * (j2 == c2)
+                                                      + mu * ((c1 == c2) * (j1 == j2) + (c1 == j2) * (j1 == c2)))
+    return D.reshape(lam.size, 81)
+
+
+def fp64_redo_count(xyz, tets):
+    """Tets that the FP32 kernels redo in FP64 geometry: |det| <= 0.05 |e1| |e2| |e3| for the
+    edges e_k = X_k - X_0."""
+    X = xyz[tets]
+    e = X[:, 1:] - X[:, :1]
+    det = np.abs(np.einsum("ti,ti->t", e[:, 0], np.cross(e[:, 1], e[:, 2])))
+    return int((det <= 0.05 * np.prod(np.linalg.norm(e, axis=2), axis=1)).sum())

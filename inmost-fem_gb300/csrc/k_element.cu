@@ -38,6 +38,7 @@ struct ElemParams {
     int face;         // -1: the tet integral; 0..3: the integral over face k (fem3Dface)
     int normal;       // fem3DfaceN: the tensor has 3*dimB rows, contracted with the outward normal
     int same;         // OpA == OpB: V is U
+    int tab_shared;   // basis tables staged in shared memory (else read through L1 from global memory)
     const double* w;  // device weights
 };
 
@@ -169,12 +170,14 @@ __global__ void __launch_bounds__(kThreads) fem3dtet_kernel(ElemParams p, int64_
     extern __shared__ double smem[];
     const int q = p.q;
     const int nfA = p.A.nf, nfB = p.B.nf, dA = p.A.dim, dB = p.B.dim;
-    const size_t tabA = (size_t)q * p.A.tnf * 4, tabB = (size_t)q * p.B.tnf * 4;
-    double* sTabA = smem;
-    double* sTabB = sTabA + tabA;
-    double* sW = sTabB + tabB;
-    for (size_t i = threadIdx.x; i < tabA; i += blockDim.x) sTabA[i] = p.A.tab[i];
-    for (size_t i = threadIdx.x; i < tabB; i += blockDim.x) sTabB[i] = p.B.tab[i];
+    // basis tables: staged in shared memory when they fit (every rule up to order 6); the rules
+    // of orders 7-20 (up to 552 points) are read from global memory through L1
+    const size_t tabA = p.tab_shared ? (size_t)q * p.A.tnf * 4 : 0, tabB = p.tab_shared ? (size_t)q * p.B.tnf * 4 : 0;
+    double* sW = smem + tabA + tabB;
+    for (size_t i = threadIdx.x; i < tabA; i += blockDim.x) smem[i] = p.A.tab[i];
+    for (size_t i = threadIdx.x; i < tabB; i += blockDim.x) smem[tabA + i] = p.B.tab[i];
+    const double* sTabA = p.tab_shared ? smem : p.A.tab;
+    const double* sTabB = p.tab_shared ? smem + tabA : p.B.tab;
     for (int i = threadIdx.x; i < q; i += blockDim.x) sW[i] = p.w[i];
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1073,7 +1076,7 @@ int launch_fem3dtet(anigpu_ctx* h, int opA, int opB, int kind, int order, int pr
     if (precision != ANIGPU_F32 && precision != ANIGPU_F64) return set_err(h, ANIGPU_ERR_ARG, "precision");
     if (!vecA && !vecB && ncA == 1 && ncB == 1 && !normal && kind != ANIGPU_TENSOR_POINT)
         return launch_reftensor(h, opA, opB, order, face, hA, hB, kind, precision, nt, XY, D, A);
-    ElemParams p;
+    ElemParams p{};
     p.A = {nfA, dA, nfA / ncA, dA / ncA, ncA, oA, bsA, vecA ? 4 : nfA / ncA, tA, nullptr};
     p.B = {nfB, dB, nfB / ncB, dB / ncB, ncB, oB, bsB, vecB ? 4 : nfB / ncB, tB, nullptr};
     p.q = hA.q;
@@ -1094,17 +1097,20 @@ static int run_quadrature(anigpu_ctx* h, const ElemParams& p, int precision, int
     // per-warp region in doubles: geometry 26, tensor MAX_DIM^2, then U, V, DU and the entries
     const size_t wreal = (size_t)dA * nfA + (p.same ? 0 : (size_t)dB * nfB) + (size_t)dB * nfA + (size_t)nfA * nfB;
     const int wstride = (int)((26 + ANIGPU_MAX_DIM * ANIGPU_MAX_DIM) + (wreal * rsz + 7) / 8 + 1) & ~1;
-    const size_t smem = sizeof(double) * (tabs + p.q + (size_t)(kThreads / 32) * wstride);
+    ElemParams pk = p;
+    size_t smem = sizeof(double) * (tabs + p.q + (size_t)(kThreads / 32) * wstride);
+    pk.tab_shared = smem <= 96 * 1024 ? 1 : 0;
+    if (!pk.tab_shared) smem = sizeof(double) * (p.q + (size_t)(kThreads / 32) * wstride);
     if (smem > 227 * 1024) return set_err(h, ANIGPU_ERR_UNSUPPORTED, "element matrices too large for one warp's shared memory");
     int dev_sms = 148;
     cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, h->device);
     const unsigned grid = (unsigned)std::min<int64_t>((nt + kThreads / 32 - 1) / (kThreads / 32), (int64_t)dev_sms * 16);
     if (precision == ANIGPU_F32) {
         ANI_CUDA(h, cudaFuncSetAttribute(fem3dtet_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        fem3dtet_kernel<float><<<grid, kThreads, smem, h->stream>>>(p, nt, XY, D, (float*)A, wstride);
+        fem3dtet_kernel<float><<<grid, kThreads, smem, h->stream>>>(pk, nt, XY, D, (float*)A, wstride);
     } else if (precision == ANIGPU_F64) {
         ANI_CUDA(h, cudaFuncSetAttribute(fem3dtet_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        fem3dtet_kernel<double><<<grid, kThreads, smem, h->stream>>>(p, nt, XY, D, (double*)A, wstride);
+        fem3dtet_kernel<double><<<grid, kThreads, smem, h->stream>>>(pk, nt, XY, D, (double*)A, wstride);
     } else {
         return set_err(h, ANIGPU_ERR_ARG, "precision");
     }
@@ -1137,7 +1143,7 @@ int launch_fem3dtet_custom(anigpu_ctx* h, int dimA, int nfA, const double* UA, i
     ScalarBasisTable h1;
     int rc = get_basis_dev(h, ANIGPU_P1, order, &t1, &h1, -1);  // the rule's weights
     if (rc) return rc;
-    ElemParams p;
+    ElemParams p{};
     p.A = {nfA, dimA, nfA, dimA, 1, 0, -1, 0, t1, UA};
     p.B = {nfB, dimB, nfB, dimB, 1, 0, -1, 0, t1, VB ? VB : UA};
     p.q = h1.q;

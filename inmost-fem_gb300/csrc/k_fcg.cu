@@ -251,9 +251,11 @@ __global__ void fold_kernel(int64_t n, double* __restrict__ x, float* __restrict
     d[i] = 0.f;
 }
 
-// r = b - A x in FP64 arithmetic (r stored FP32); partials of r.r (and b.b when part_bb)
+// r = b - A x in FP64 arithmetic (r stored FP32); partials of r.r (and b.b when part_bb); A is the
+// FP32 system the iteration runs on, or the FP64-assembled system that judges convergence
+template <typename VT>
 __global__ void __launch_bounds__(kB) resid_kernel(int64_t n, const int64_t* __restrict__ rowptr,
-                                                   const int32_t* __restrict__ col, const float* __restrict__ vals,
+                                                   const int32_t* __restrict__ col, const VT* __restrict__ vals,
                                                    const double* __restrict__ x, const double* __restrict__ b,
                                                    float* __restrict__ r, double* __restrict__ part_rr,
                                                    double* __restrict__ part_bb) {
@@ -375,6 +377,7 @@ struct Ctx {
     const double* b;
     double* x;
     int64_t n;
+    const double* vals64;  // FP64 system of the residual replacements (null: the FP32 one)
     int nb_rows, nb_vec, nb_prec;  // nb_prec: blocks (partials) of the preconditioner's r.z, z.q
     int nb_pq;                     // blocks (partials) of the SpMV's p.q
     double *part_pq, *part_rr, *part_bb, *part_rz, *part_zq;
@@ -449,8 +452,12 @@ int checkpoint(Ctx& c, double* rr, double* bb) {
     cudaStream_t s = h->stream;
     fold_kernel<<<grid_for(c.n, kB), kB, 0, s>>>(c.n, c.x, c.w->d);
     ANI_LAUNCHED(h);
-    resid_kernel<<<c.nb_rows, kB, 0, s>>>(c.n, h->rowptr, h->col, c.vals, c.x, c.b, c.w->r, c.part_rr,
-                                          bb ? c.part_bb : nullptr);
+    if (c.vals64)
+        resid_kernel<double><<<c.nb_rows, kB, 0, s>>>(c.n, h->rowptr, h->col, c.vals64, c.x, c.b, c.w->r, c.part_rr,
+                                                      bb ? c.part_bb : nullptr);
+    else
+        resid_kernel<float><<<c.nb_rows, kB, 0, s>>>(c.n, h->rowptr, h->col, c.vals, c.x, c.b, c.w->r, c.part_rr,
+                                                     bb ? c.part_bb : nullptr);
     ANI_LAUNCHED(h);
     sums_kernel<<<1, kB, 0, s>>>(c.part_rr, c.nb_rows, bb ? 2 : 1, c.w->sums);  // part_bb = part_rr + kMaxP
     ANI_LAUNCHED(h);
@@ -487,7 +494,7 @@ void free_fcg(anigpu_ctx* h) {
 }
 
 int run_fcg_learned(anigpu_ctx* h, const void* vals, int precision, const double* b, double* x, double rtol,
-                    int64_t maxit, anigpu_solve_stats* st) {
+                    int64_t maxit, anigpu_solve_stats* st, const double* vals64) {
     if (precision != ANIGPU_F32) return set_err(h, ANIGPU_ERR_UNSUPPORTED, "FCG_LEARNED takes FP32 values");
     if (!gnn_bound_to(h, vals)) return set_err(h, ANIGPU_ERR_STATE, "anigpu_gnn_bind not called for these values");
     FcgWs* w;
@@ -497,7 +504,7 @@ int run_fcg_learned(anigpu_ctx* h, const void* vals, int precision, const double
         w->key_vals = vals;
         w->key_gen = gnn_bind_generation(h);
     }
-    Ctx c{h, w, (const float*)vals, b, x, h->ndof, 0, 0, 0, 0, nullptr, nullptr, nullptr, nullptr, nullptr};
+    Ctx c{h, w, (const float*)vals, b, x, h->ndof, vals64, 0, 0, 0, 0, nullptr, nullptr, nullptr, nullptr, nullptr};
     c.nb_rows = nblocks(c.n * kW);
     c.nb_pq = h->ncomp == 3 ? nblocks(h->nds * SPMV3_W) : c.nb_rows;
     c.nb_vec = nblocks(c.n);

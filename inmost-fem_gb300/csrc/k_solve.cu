@@ -538,12 +538,16 @@ __global__ void cast_f64_f32_kernel(int64_t n, const double* __restrict__ a, flo
 }
 
 // FP32-SpMV CG inside FP64 iterative refinement
+// (inner32: the FP32 system of the inner solves when it is not the outer system's rounding, e.g. an
+// FP32-assembled matrix under an FP64-assembled outer system)
 template <typename VR, int W>
 int solve_ir_cg32(anigpu_ctx* h, SolveWs* w, const VR* vals_in, const double* b, double* x, double rtol,
-                  int64_t maxit, anigpu_solve_stats* st) {
+                  int64_t maxit, anigpu_solve_stats* st, const float* inner32 = nullptr) {
     const int64_t n = h->ndof;
     const float* vals32;
-    if (sizeof(VR) == 4) {
+    if (inner32) {
+        vals32 = inner32;
+    } else if (sizeof(VR) == 4) {
         vals32 = (const float*)vals_in;
     } else {
         int rc = dev_alloc(h, &w->vals32, (size_t)h->nnz);
@@ -614,6 +618,41 @@ int run_spmv(anigpu_ctx* h, const void* vals, int precision, const double* x, do
 #undef SPMV
     ANI_LAUNCHED(h);
     return ANIGPU_OK;
+}
+
+int run_solve_refined(anigpu_ctx* h, int method, const float* vals32, const double* vals64, const double* b, double* x,
+                      double rtol, int64_t maxit, anigpu_solve_stats* st) {
+    if (h->space < 0) return set_err(h, ANIGPU_ERR_STATE, "anigpu_problem_setup not called");
+    if (!vals32 || !vals64 || !b || !x || !st) return set_err(h, ANIGPU_ERR_ARG, "NULL argument");
+    SolveWs* w;
+    int rc = ensure_ws(h, &w);
+    if (rc) return rc;
+    *st = anigpu_solve_stats{0, 0, 0.0, 0.0, 0};
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, h->stream);
+    const int W = row_width(h);
+    switch (method) {
+        case ANIGPU_SOLVE_IR_CG32:
+            rc = W == 8   ? solve_ir_cg32<double, 8>(h, w, vals64, b, x, rtol, maxit, st, vals32)
+                 : W == 2 ? solve_ir_cg32<double, 2>(h, w, vals64, b, x, rtol, maxit, st, vals32)
+                          : solve_ir_cg32<double, 4>(h, w, vals64, b, x, rtol, maxit, st, vals32);
+            break;
+        case ANIGPU_SOLVE_FCG_LEARNED:
+            rc = run_fcg_learned(h, vals32, ANIGPU_F32, b, x, rtol, maxit, st, vals64);
+            break;
+        default:
+            rc = set_err(h, ANIGPU_ERR_ARG, "refined solves take IR_CG32 or FCG_LEARNED");
+    }
+    cudaEventRecord(e1, h->stream);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    st->seconds = ms * 1e-3;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
 }
 
 int run_solve(anigpu_ctx* h, int method, const void* vals, int precision, const double* b, double* x, double rtol,

@@ -3,7 +3,8 @@
 #include "anigpu_internal.h"
 
 int run_fcg_learned(anigpu_ctx* h, const void* vals, int precision, const double* b, double* x, double rtol,
-                    int64_t maxit, anigpu_solve_stats* st);
+                    int64_t maxit, anigpu_solve_stats* st,
+                    const double* vals64 = nullptr);
 void free_learned(anigpu_ctx* h);
 // a new mesh or problem: the binding is dropped (bind again) and captured solver graphs freed
 void learned_invalidate(anigpu_ctx* h);

@@ -18,7 +18,6 @@
 
 #define MAXNF 30
 #define MAXDIM 9
-#define MAXQ 64
 
 /* ---------------------------------------------------------------- bases */
 
@@ -327,8 +326,10 @@ static void gradgrad_sym(int space, int order, long nt, const double* XY, const 
     anigpu_quad_rule(order, &pp, &ww, &q);
     int nf = scalar_nf(space);
     double val[20], g[20][3];
-    double U[MAXQ * 3 * 20], DU[MAXQ * 3 * 20];
-    double G[MAXQ][20][3];
+    /* rules of up to ANIGPU_QUAD_MAX_POINTS points: buffers on the heap */
+    double* U = (double*)malloc(sizeof(double) * 3 * 20 * (size_t)q);
+    double* DU = (double*)malloc(sizeof(double) * 3 * 20 * (size_t)q);
+    double (*G)[20][3] = (double (*)[20][3])malloc(sizeof(double) * 60 * (size_t)q);
     for (long t = 0; t < nt; ++t) {
         double PSI[9], mes;
         tet_geom(XY + 12 * t, PSI, &mes);
@@ -357,6 +358,9 @@ static void gradgrad_sym(int space, int order, long nt, const double* XY, const 
                 At[ib + nf * ia] = acc;
             }
     }
+    free(U);
+    free(DU);
+    free(G);
     (void)g;
 }
 
@@ -877,5 +881,304 @@ double orc_time_p2_sym(long nt, const double* XY, const double* D6, int order, i
         for (int i = 0; i < k; ++i) pthread_join(th[i], NULL);
     }
     clock_gettime(CLOCK_MONOTONIC, &t1);
+    return (t1.tv_sec - t0.tv_sec) + 1e-9 * (t1.tv_nsec - t0.tv_nsec);
+}
+
+/* ---------------------------------------------------------------- multi-threaded drivers
+ * The same restatements split over host threads, for full-size parity checks and the CPU
+ * baselines.  Every output value is computed with the same arithmetic and summation order as the
+ * serial functions above (threads own disjoint tets or rows), so the results are bitwise equal. */
+
+typedef void (*range_fn)(long b, long e, void* ctx);
+struct par_arg {
+    range_fn fn;
+    long b, e;
+    void* ctx;
+};
+static void* par_run(void* a) {
+    struct par_arg* p = (struct par_arg*)a;
+    p->fn(p->b, p->e, p->ctx);
+    return NULL;
+}
+static void par_for(long n, int nthreads, range_fn fn, void* ctx) {
+    if (nthreads <= 1 || n < 2) {
+        fn(0, n, ctx);
+        return;
+    }
+    if (nthreads > 256) nthreads = 256;
+    pthread_t th[256];
+    struct par_arg args[256];
+    long per = (n + nthreads - 1) / nthreads;
+    int k = 0;
+    for (int i = 0; i < nthreads; ++i) {
+        long b = i * per, e = b + per < n ? b + per : n;
+        if (b >= e) break;
+        args[k].fn = fn;
+        args[k].b = b;
+        args[k].e = e;
+        args[k].ctx = ctx;
+        pthread_create(&th[k], NULL, par_run, &args[k]);
+        ++k;
+    }
+    for (int i = 0; i < k; ++i) pthread_join(th[i], NULL);
+}
+
+struct elem_ctx {
+    int codeA, codeB, kind, q, nfA, nfB, dA, dB;
+    const double *pp, *ww, *XY, *D;
+    double* A;
+    int rc;
+};
+static void elem_range(long b, long e, void* c) {
+    struct elem_ctx* x = (struct elem_ctx*)c;
+    const double* D = x->D;
+    size_t per = 0;
+    switch (x->kind) {
+        case ORC_TET_SCALAR: per = 1; break;
+        case ORC_TET_SYM: per = 6; break;
+        case ORC_TET_GENERAL: per = (size_t)x->dA * x->dB; break;
+        case ORC_POINT: per = (size_t)x->dA * x->dB * x->q; break;
+    }
+    if (D) D += per * (size_t)b;
+    int rc = elem_core(x->codeA, x->codeB, x->kind, x->pp, x->ww, x->q, -1, 0, e - b, x->XY + 12 * b, D,
+                       x->A + (size_t)x->nfA * x->nfB * b);
+    if (rc) x->rc = rc;
+}
+
+/* orc_fem3dtet over nthreads host threads (contiguous tet chunks) */
+int orc_fem3dtet_mt(int codeA, int codeB, int kind, int order, long nt, const double* XY, const double* D, double* A,
+                    int nthreads) {
+    struct elem_ctx c;
+    if (!anigpu_quad_rule(order, &c.pp, &c.ww, &c.q)) return -1;
+    if (orc_op_info(codeA, &c.nfA, &c.dA) || orc_op_info(codeB, &c.nfB, &c.dB)) return -1;
+    c.codeA = codeA, c.codeB = codeB, c.kind = kind, c.XY = XY, c.D = D, c.A = A, c.rc = 0;
+    par_for(nt, nthreads, elem_range, &c);
+    return c.rc;
+}
+
+struct dir_ctx {
+    int nloc;
+    double *A, *F;
+    const int32_t* edofs;
+    const uint8_t* mask;
+    const double* bc;
+};
+static void dir_range(long b, long e, void* c) {
+    struct dir_ctx* x = (struct dir_ctx*)c;
+    for (long t = b; t < e; ++t)
+        for (int k = 0; k < x->nloc; ++k) {
+            const int32_t d = x->edofs[(size_t)x->nloc * t + k];
+            if (x->mask[d])
+                orc_apply_dir(x->nloc, x->A + (size_t)x->nloc * x->nloc * t, x->F + (size_t)x->nloc * t, k,
+                              x->bc ? x->bc[d] : 0.0);
+        }
+}
+
+/* applyDir on every element DOF whose global DOF is masked, local DOFs in ascending order (the
+ * element loop of a local assembler, dc_on_dof.h:24-45) */
+void orc_apply_dir_elems(long nt, int nloc, double* A, double* F, const int32_t* edofs, const uint8_t* mask,
+                         const double* bc, int nthreads) {
+    struct dir_ctx c = {nloc, A, F, edofs, mask, bc};
+    par_for(nt, nthreads, dir_range, &c);
+}
+
+struct tmpl_ctx {
+    int nloc;
+    const int32_t* edofs;
+    const int64_t *ip;
+    const int32_t* itet;
+    int64_t* rowptr; /* pass 1: counts in rowptr[r + 1]; pass 2: offsets */
+    int32_t* col;
+};
+static long row_columns(const struct tmpl_ctx* x, long r, int32_t** buf, long* cap) {
+    long deg = x->ip[r + 1] - x->ip[r];
+    if (deg * x->nloc + 1 > *cap) {
+        *cap = deg * x->nloc + 1;
+        *buf = (int32_t*)realloc(*buf, sizeof(int32_t) * (size_t)*cap);
+    }
+    long m = 0;
+    (*buf)[m++] = (int32_t)r;
+    for (int64_t k = x->ip[r]; k < x->ip[r + 1]; ++k)
+        for (int j = 0; j < x->nloc; ++j) (*buf)[m++] = x->edofs[(size_t)x->nloc * x->itet[k] + j];
+    qsort(*buf, m, sizeof(int32_t), cmp_i32);
+    long u = 0;
+    for (long k = 0; k < m; ++k)
+        if (k == 0 || (*buf)[k] != (*buf)[k - 1]) (*buf)[u++] = (*buf)[k];
+    return u;
+}
+static void tmpl_count(long b, long e, void* c) {
+    struct tmpl_ctx* x = (struct tmpl_ctx*)c;
+    long cap = 0;
+    int32_t* buf = NULL;
+    for (long r = b; r < e; ++r) x->rowptr[r + 1] = row_columns(x, r, &buf, &cap);
+    free(buf);
+}
+static void tmpl_fill(long b, long e, void* c) {
+    struct tmpl_ctx* x = (struct tmpl_ctx*)c;
+    long cap = 0;
+    int32_t* buf = NULL;
+    for (long r = b; r < e; ++r) {
+        long u = row_columns(x, r, &buf, &cap);
+        memcpy(x->col + x->rowptr[r], buf, sizeof(int32_t) * (size_t)u);
+    }
+    free(buf);
+}
+
+/* orc_csr_template over nthreads threads: the same rows (sorted unique DOFs of the incident
+ * tets plus the diagonal); pass 1 counts, pass 2 fills (col NULL: counts only, returns nnz) */
+long orc_csr_template_mt(long ndof, long nt, int nloc, const int32_t* edofs, int64_t* rowptr, int32_t* col,
+                         int nthreads) {
+    int64_t* ip;
+    int32_t* itet;
+    incidence(ndof, nt, nloc, edofs, &ip, &itet);
+    struct tmpl_ctx c = {nloc, edofs, ip, itet, rowptr, col};
+    rowptr[0] = 0;
+    par_for(ndof, nthreads, tmpl_count, &c);
+    for (long r = 0; r < ndof; ++r) rowptr[r + 1] += rowptr[r];
+    if (col) par_for(ndof, nthreads, tmpl_fill, &c);
+    long nnz = rowptr[ndof];
+    free(ip);
+    free(itet);
+    return nnz;
+}
+
+struct scat_ctx {
+    int nloc;
+    const int64_t *rowptr, *ip;
+    const int32_t *col, *edofs, *itet;
+    const double *Aelem, *Felem;
+    double drop;
+    double *vals, *rhs;
+    uint8_t* touched;
+    int rc;
+};
+static void scat_range(long b, long e, void* c) {
+    struct scat_ctx* x = (struct scat_ctx*)c;
+    const int n = x->nloc;
+    for (long r = b; r < e; ++r)
+        for (int64_t k = x->ip[r]; k < x->ip[r + 1]; ++k) { /* incident tets in ascending order */
+            const long t = x->itet[k];
+            const int32_t* ed = x->edofs + (size_t)n * t;
+            int i = 0;
+            while (i < n && ed[i] != r) ++i;
+            if (x->Felem) {
+                const double f = x->Felem[(size_t)n * t + i];
+                if (!isfinite(f)) x->rc = -1;
+                x->rhs[r] += f;
+            }
+            const double* Ae = x->Aelem + (size_t)n * n * t;
+            for (int j = 0; j < n; ++j) {
+                const double a = Ae[i + n * j];
+                if (!isfinite(a)) x->rc = -1;
+                if (fabs(a) > x->drop) {
+                    long s = find_slot(x->rowptr, x->col, r, ed[j]);
+                    if (s < 0) {
+                        x->rc = -2;
+                        continue;
+                    }
+                    x->vals[s] += a;
+                    if (x->touched) x->touched[s] = 1;
+                }
+            }
+        }
+}
+
+/* orc_scatter over nthreads threads: threads own rows and add each row's element rows in
+ * ascending tet order, the per-slot order of the serial tet loop (so the sums are bitwise equal) */
+int orc_scatter_mt(long ndof, const int64_t* rowptr, const int32_t* col, long nt, int nloc, const int32_t* edofs,
+                   const double* Aelem, const double* Felem, double drop, double* vals, double* rhs,
+                   uint8_t* touched, int nthreads) {
+    int64_t* ip;
+    int32_t* itet;
+    incidence(ndof, nt, nloc, edofs, &ip, &itet);
+    struct scat_ctx c = {nloc, rowptr, ip, col, edofs, itet, Aelem, Felem, drop, vals, rhs, touched, 0};
+    par_for(ndof, nthreads, scat_range, &c);
+    free(ip);
+    free(itet);
+    return c.rc;
+}
+
+struct vec_ctx {
+    long n;
+    const int64_t* rowptr;
+    const int32_t* col;
+    const double* vals;
+    double *x, *r, *z, *p, *q, *dinv;
+    double alpha, beta;
+    int op;
+    double part[256];
+    int nthreads;
+};
+static void pcg_range(long b, long e, void* c) {
+    struct vec_ctx* x = (struct vec_ctx*)c;
+    const long per = (x->n + x->nthreads - 1) / x->nthreads;
+    const int slot = (int)(b / (per > 0 ? per : 1));
+    double s = 0;
+    if (x->op == 0) { /* q = A p, partial p.q */
+        for (long i = b; i < e; ++i) {
+            double v = 0;
+            for (int64_t k = x->rowptr[i]; k < x->rowptr[i + 1]; ++k) v += x->vals[k] * x->p[x->col[k]];
+            x->q[i] = v;
+            s += x->p[i] * v;
+        }
+    } else if (x->op == 1) { /* x += a p, r -= a q, z = D^-1 r, partial r.z */
+        for (long i = b; i < e; ++i) {
+            x->x[i] += x->alpha * x->p[i];
+            x->r[i] -= x->alpha * x->q[i];
+            x->z[i] = x->dinv[i] * x->r[i];
+            s += x->r[i] * x->z[i];
+        }
+    } else { /* p = z + b p */
+        for (long i = b; i < e; ++i) x->p[i] = x->z[i] + x->beta * x->p[i];
+    }
+    x->part[slot] = s;
+}
+
+/* Seconds of `iters` Jacobi-PCG iterations (FP64, from x = 0) over nthreads threads: the CPU
+ * baseline of the solve (a restatement: the reference solves through INMOST).  Dot products are
+ * per-thread partial sums added in thread order. */
+double orc_pcg_time_mt(long n, const int64_t* rowptr, const int32_t* col, const double* vals, const double* b,
+                       long iters, int nthreads) {
+    if (nthreads > 256) nthreads = 256;
+    if (nthreads < 1) nthreads = 1;
+    struct vec_ctx c;
+    memset(&c, 0, sizeof(c));
+    c.n = n, c.rowptr = rowptr, c.col = col, c.vals = vals, c.nthreads = nthreads;
+    c.x = (double*)calloc(n, sizeof(double));
+    c.r = (double*)malloc(sizeof(double) * n);
+    c.z = (double*)malloc(sizeof(double) * n);
+    c.p = (double*)malloc(sizeof(double) * n);
+    c.q = (double*)malloc(sizeof(double) * n);
+    c.dinv = (double*)malloc(sizeof(double) * n);
+    for (long i = 0; i < n; ++i) {
+        long s = find_slot(rowptr, col, i, (int32_t)i);
+        double d = s >= 0 ? vals[s] : 0.0;
+        c.dinv[i] = d != 0 ? 1.0 / d : 1.0;
+        c.r[i] = b[i];
+        c.z[i] = c.dinv[i] * b[i];
+        c.p[i] = c.z[i];
+    }
+    double rz = dot(n, c.r, c.z);
+    struct timespec t0, t1;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    for (long it = 0; it < iters; ++it) {
+        memset(c.part, 0, sizeof(c.part));
+        c.op = 0;
+        par_for(n, nthreads, pcg_range, &c);
+        double pq = 0;
+        for (int k = 0; k < nthreads; ++k) pq += c.part[k];
+        c.alpha = rz / pq;
+        memset(c.part, 0, sizeof(c.part));
+        c.op = 1;
+        par_for(n, nthreads, pcg_range, &c);
+        double rz1 = 0;
+        for (int k = 0; k < nthreads; ++k) rz1 += c.part[k];
+        c.beta = rz1 / rz;
+        rz = rz1;
+        c.op = 2;
+        par_for(n, nthreads, pcg_range, &c);
+    }
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    free(c.x), free(c.r), free(c.z), free(c.p), free(c.q), free(c.dinv);
     return (t1.tv_sec - t0.tv_sec) + 1e-9 * (t1.tv_nsec - t0.tv_nsec);
 }

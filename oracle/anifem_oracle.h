@@ -71,6 +71,18 @@ long orc_jacobi_pcg(long n, const int64_t* rowptr, const int32_t* col, const dou
 /* CPU baseline: P2 GRAD.GRAD, per-tet symmetric tensor, over nthreads threads (contiguous chunks);
  * returns seconds */
 double orc_time_p2_sym(long nt, const double* XY, const double* D6, int order, int nthreads, double* A);
+/* multi-threaded drivers (bitwise equal to the serial functions; threads own tets or rows) */
+int orc_fem3dtet_mt(int codeA, int codeB, int kind, int order, long nt, const double* XY, const double* D, double* A,
+                    int nthreads);
+void orc_apply_dir_elems(long nt, int nloc, double* A, double* F, const int32_t* edofs, const uint8_t* mask,
+                         const double* bc, int nthreads);
+long orc_csr_template_mt(long ndof, long nt, int nloc, const int32_t* edofs, int64_t* rowptr, int32_t* col,
+                         int nthreads);
+int orc_scatter_mt(long ndof, const int64_t* rowptr, const int32_t* col, long nt, int nloc, const int32_t* edofs,
+                   const double* Aelem, const double* Felem, double drop, double* vals, double* rhs,
+                   uint8_t* touched, int nthreads);
+double orc_pcg_time_mt(long n, const int64_t* rowptr, const int32_t* col, const double* vals, const double* b,
+                       long iters, int nthreads);
 
 #ifdef __cplusplus
 }

@@ -74,7 +74,15 @@ class Restated:
         L.orc_jacobi_pcg.restype = _l
         L.orc_time_p2_sym.argtypes = [_l, _vp, _vp, _i, _i, _vp]
         L.orc_time_p2_sym.restype = _d
+        L.orc_fem3dtet_mt.argtypes = [_i, _i, _i, _i, _l, _vp, _vp, _vp, _i]
+        L.orc_apply_dir_elems.argtypes = [_l, _i, _vp, _vp, _vp, _vp, _vp, _i]
+        L.orc_csr_template_mt.argtypes = [_l, _l, _i, _vp, _vp, _vp, _i]
+        L.orc_csr_template_mt.restype = _l
+        L.orc_scatter_mt.argtypes = [_l, _vp, _vp, _l, _i, _vp, _vp, _vp, _d, _vp, _vp, _vp, _i]
+        L.orc_pcg_time_mt.argtypes = [_l, _vp, _vp, _vp, _vp, _l, _i]
+        L.orc_pcg_time_mt.restype = _d
         self.L = L
+        self.threads = os.cpu_count() or 1
 
     def op_info(self, code):
         nf, dim = _i(), _i()
@@ -82,9 +90,9 @@ class Restated:
         return nf.value, dim.value
 
     def quadrature(self, order):
-        p = np.zeros(4 * 64)
-        w = np.zeros(64)
-        n = self.L.orc_quad_rule(order, _p(p), _p(w), 64)
+        p = np.zeros(4 * 1024)
+        w = np.zeros(1024)
+        n = self.L.orc_quad_rule(order, _p(p), _p(w), 1024)
         assert n > 0
         return p[:4 * n].reshape(n, 4).copy(), w[:n].copy()
 
@@ -126,16 +134,16 @@ class Restated:
         return A
 
     def tri_rule(self, order):
-        p = np.zeros(3 * 64)
-        w = np.zeros(64)
-        n = self.L.orc_tri_rule(order, _p(p), _p(w), 64)
+        p = np.zeros(3 * 1024)
+        w = np.zeros(1024)
+        n = self.L.orc_tri_rule(order, _p(p), _p(w), 1024)
         assert n > 0
         return p[:3 * n].reshape(n, 3).copy(), w[:n].copy()
 
     def face_quad_points(self, order, face, XY):
         XY = np.ascontiguousarray(XY, dtype=np.float64)
         nt = XY.size // 12
-        out = np.zeros(nt * 64 * 3)
+        out = np.zeros(nt * 1024 * 3)
         q = self.L.orc_face_quad_points(order, face, nt, _p(XY), _p(out))
         assert q > 0
         return out[:nt * q * 3].reshape(nt, q, 3).copy()
@@ -252,6 +260,68 @@ class Restated:
                     nedges=ne)
 
 
+    # ---- multi-threaded drivers (bitwise equal to the serial ones), for full-size checks
+    def fem3dtet_mt(self, codeA, codeB, kind, order, XY, D=None, threads=None):
+        XY = np.ascontiguousarray(XY, dtype=np.float64)
+        nt = XY.size // 12
+        nfA, _ = self.op_info(codeA)
+        nfB, _ = self.op_info(codeB)
+        A = np.zeros((nt, nfA, nfB))
+        Dd = None if D is None else np.ascontiguousarray(D, dtype=np.float64)
+        rc = self.L.orc_fem3dtet_mt(codeA, codeB, kind, order, nt, _p(XY), _p(Dd), _p(A), threads or self.threads)
+        assert rc == 0, rc
+        return A
+
+    def assemble_problem_mt(self, xyz, tets, space, kind, D, f_const, order, dirichlet=None, threads=None):
+        """assemble_problem on all host threads: the same numbers (element loop and scatter split
+        over tets and rows), for meshes of millions of tets."""
+        import time
+        th = threads or self.threads
+        sec = {}
+        t0 = time.perf_counter()
+        nv = xyz.shape[0]
+        t = self.orient(xyz, tets)
+        ne, te = self.edges(nv, t) if space in (2, 5) else (0, None)
+        ndof, ed = self.element_dofs(space, nv, ne, t, te)
+        nloc = ed.shape[1]
+        rp = np.zeros(ndof + 1, dtype=np.int64)
+        nnz = self.L.orc_csr_template_mt(ndof, ed.shape[0], nloc, _p(ed), _p(rp), None, th)
+        col = np.zeros(nnz, dtype=np.int32)
+        self.L.orc_csr_template_mt(ndof, ed.shape[0], nloc, _p(ed), _p(rp), _p(col), th)
+        XY = np.ascontiguousarray(xyz[t].reshape(-1, 12))
+        t1 = time.perf_counter()
+        sec["setup"] = t1 - t0
+        code = 10 * space + 2
+        A = self.fem3dtet_mt(code, code, kind, order, XY, D, th)
+        F = np.ascontiguousarray(self.fem3dtet_mt(1, 10 * space + 1, CONST_SCALAR, order, XY, np.array([f_const]),
+                                                  th)[:, 0, :])
+        t2 = time.perf_counter()
+        sec["elements"] = t2 - t1
+        if dirichlet is not None:
+            mask, bc = dirichlet
+            mask = np.ascontiguousarray(mask, dtype=np.uint8)
+            bcv = None if bc is None else np.ascontiguousarray(bc, dtype=np.float64)
+            self.L.orc_apply_dir_elems(ed.shape[0], nloc, _p(A), _p(F), _p(ed), _p(mask), _p(bcv), th)
+        t3 = time.perf_counter()
+        sec["dirichlet"] = t3 - t2
+        vals = np.zeros(nnz)
+        rhs = np.zeros(ndof)
+        rc = self.L.orc_scatter_mt(ndof, _p(rp), _p(col), ed.shape[0], nloc, _p(ed), _p(A), _p(F), 1e-100, _p(vals),
+                                   _p(rhs), None, th)
+        sec["scatter"] = time.perf_counter() - t3
+        assert rc == 0, rc
+        return dict(rowptr=rp, col=col, vals=vals, rhs=rhs, edofs=ed, ndof=ndof, oriented=t, nedges=ne, seconds=sec,
+                    threads=th)
+
+    def pcg_seconds_per_iteration(self, rowptr, col, vals, b, iters=20, threads=None):
+        """Wall seconds per FP64 Jacobi-PCG iteration on all host threads (the CPU baseline of the
+        solve; a restatement: the reference solves through INMOST)."""
+        sec = self.L.orc_pcg_time_mt(rowptr.size - 1, _p(rowptr), _p(col),
+                                     _p(np.ascontiguousarray(vals, dtype=np.float64)),
+                                     _p(np.ascontiguousarray(b, dtype=np.float64)), iters, threads or self.threads)
+        return sec / iters
+
+
 class Reference:
     """The reference's own fem3Dtet (only where oracle/_ref/libanifem_ref.so was built)."""
 
@@ -292,10 +362,10 @@ class Reference:
         return A
 
     def tri_quadrature(self, order):
-        p = np.zeros(3 * 256)
-        w = np.zeros(256)
+        p = np.zeros(3 * 1024)
+        w = np.zeros(1024)
         sym = np.zeros(3, dtype=np.int32)
-        n = self.L.ref_tri_quadrature(order, _p(p), _p(w), 256, _p(sym))
+        n = self.L.ref_tri_quadrature(order, _p(p), _p(w), 1024, _p(sym))
         assert n > 0
         return p[:3 * n].reshape(n, 3).copy(), w[:n].copy()
 
@@ -303,9 +373,9 @@ class Reference:
         return _apply(self.L.ref_fem3d_apply, (nf, dim), code, XY, pts, dofs, phys)
 
     def quadrature(self, order):
-        p = np.zeros(4 * 128)
-        w = np.zeros(128)
-        n = self.L.ref_quadrature(order, _p(p), _p(w), 128)
+        p = np.zeros(4 * 1024)
+        w = np.zeros(1024)
+        n = self.L.ref_quadrature(order, _p(p), _p(w), 1024)
         return p[:4 * n].reshape(n, 4).copy(), w[:n].copy()
 
     def time_p2_sym(self, XY, D6, order, nthreads):

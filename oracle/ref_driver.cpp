@@ -75,7 +75,16 @@ void run_pairs(const Req& r, const F& functor_for_tet) {
             XY2(const_cast<double*>(X + 6), 3, 1), XY3(const_cast<double*>(X + 9), 3, 1);
         DenseMatrix<> A(r.A + (size_t)t * nfA * nfB, nfB, nfA, nfA * nfB);
         auto f = functor_for_tet(t);
-        if (g_face >= 0 && g_normal) {
+        if (g_face >= 0 && r.order > 9) {  // the PlainMemory overloads take triangle orders up to 20
+            auto req = g_normal ? fem3DfaceN_memory_requirements<OpA, OpB>(r.order, 1)
+                                : fem3Dface_memory_requirements<OpA, OpB>(r.order, 1);
+            std::vector<char> raw(req.enoughRawSize());
+            req.allocateFromRaw(raw.data(), raw.size());
+            if (g_normal)
+                fem3DfaceN<OpA, OpB, Traits>(make_tetras(X, X + 3, X + 6, X + 9, 1), g_face, f, A, req, r.order);
+            else
+                fem3Dface<OpA, OpB, Traits>(make_tetras(X, X + 3, X + 6, X + 9, 1), g_face, f, A, req, r.order);
+        } else if (g_face >= 0 && g_normal) {
             fem3DfaceN<OpA, OpB, Traits>(make_tetras(X, X + 3, X + 6, X + 9, 1), g_face, f, A, r.order);
         } else if (g_face >= 0) {
             fem3Dface<OpA, OpB, Traits>(make_tetras(X, X + 3, X + 6, X + 9, 1), g_face, f, A, r.order);

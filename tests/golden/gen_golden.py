@@ -15,6 +15,7 @@ Writes tests/golden/golden.npz with
   * apply_<code>_*   the reference's fem3DapplyL (order-4 quadrature points) and fem3DapplyX
                      (seeded physical points) on the same tets for every operator code;
   * tri_<order>_*    the reference's triangle rules (quadrature_formulas.cpp:109);
+  * sliver_<name>_*  the reference's fem3Dtet on badly shaped tets (slivers, caps, needles);
   * face_<name>_*    the reference's fem3Dface (int_face.inl:12-44) on the same tets, every face;
   * facen_<name>_*   the reference's fem3DfaceN (int_face.inl:48-78), tensors of 3*dimB rows.
 """
@@ -75,6 +76,36 @@ def point_tensor(fn, X, nr, nc):
     raise ValueError(fn)
 
 
+# operator pairs whose fixtures also cover orders 8, 13 and 20 (the PlainMemory overload of
+# fem3Dtet, int_tet.inl:30-57, takes orders up to 20)
+HIGH_ORDER_PAIRS = ((12, 12), (22, 22), (52, 52), (32, 32), (1, 21), (91, 91), (102, 102))
+
+
+def sliver_tets(seed=91):
+    """Badly shaped tets, each rotated, scaled and moved by seeded random values: slivers (four
+    nearly coplanar vertices), caps (a vertex close to the opposite face), needles, wedges and
+    spindles, with shape parameters e from 0.3 down to 1e-3."""
+    shapes = []
+    for e in (0.3, 0.1, 0.05, 0.02, 0.01, 1e-3):
+        shapes.append([(0, 0, 0), (1, 1, 0), (1, 0, e), (0, 1, e)])          # sliver
+        shapes.append([(0, 0, 0), (1, 0, 0), (0, 1, 0), (0.3, 0.3, e)])      # cap
+        shapes.append([(0, 0, 0), (1, 0, 0), (0.5, e, 0), (0.5, 0, e)])      # spindle
+        shapes.append([(0, 0, 0), (1, 0, 0), (1, e, 0), (0.3, 0.2, e)])      # wedge
+    shapes.append([(0, 0, 0), (1e-2, 0, 0), (0, 1e-2, 0), (0, 0, 1)])          # needle
+    n = len(shapes)
+    X = np.array(shapes, dtype=np.float64)                                  # n x 4 x 3
+    qv = meshgen.normal(seed, 4 * n).reshape(n, 4)
+    qv /= np.linalg.norm(qv, axis=1, keepdims=True)
+    w, x, y, z = qv.T
+    R = np.stack([1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w),
+                  2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w),
+                  2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)], axis=1).reshape(n, 3, 3)
+    scale = 0.5 + meshgen.uniform(seed + 1, n)
+    shift = (meshgen.uniform(seed + 2, 3 * n).reshape(n, 1, 3) - 0.5) * 200.0
+    X = np.einsum("tij,tvj->tvi", R, X) * scale[:, None, None] + shift
+    return np.ascontiguousarray(X.reshape(n, 12))
+
+
 def main():
     ref_root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("ANIFEM_REF_ROOT", "")
     if not ref_root:
@@ -92,7 +123,7 @@ def main():
     # the golden tests' tets (XY1p+3 etc. in int_tet_test.cpp:191-201 and :398-403)
     out["int_tet_test_tet_onepoint"] = np.array([0, 0, 0, 2, 1, 1, 1, 2, 1, 2, 1, 2], dtype=np.float64)
     out["int_tet_test_tet_rhs"] = np.array([0, 0, 0, 2, 1, 1, 1, 2, 1, 2, 1, 2], dtype=np.float64)
-    for o in range(7):
+    for o in range(21):
         p, w = R.quadrature(o)
         out[f"quad_{o}_p"] = p
         out[f"quad_{o}_w"] = w
@@ -116,7 +147,8 @@ def main():
             kinds += [("tsym", 3, sym6)]
         gen = (meshgen.uniform(31 + ca + cb, nt * dA * dB) - 0.5).reshape(nt, dA * dB)
         kinds += [("tgeneral", 4, gen)]
-        for order in (2, 4, 5, 6):
+        orders = (2, 3, 4, 5, 6) + ((8, 13, 20) if (ca, cb) in HIGH_ORDER_PAIRS else ())
+        for order in orders:
             for kname, kind, D in kinds:
                 name = f"{ca}_{cb}_{kname}_o{order}"
                 A = R.fem3dtet(ca, cb, kind, order, XY, D, nfA=nfA, nfB=nfB)
@@ -132,6 +164,28 @@ def main():
                 out[f"case_{name}_A"] = A
                 cases.append(name)
     out["case_names"] = np.array(cases)
+    # badly shaped tets (slivers, caps, needles, wedges; |det| / (|e1||e2||e3|) from 0.3 down to
+    # 1e-3), where the FP32 kernels redo the geometry in FP64
+    SX = sliver_tets()
+    out["sliver_XY"] = SX
+    ns = SX.shape[0]
+    sym6s = meshgen.aniso_tensors(ns, sigma=1.0, seed=23)
+    sliver_cases = []
+    for (ca, cb) in [(12, 12), (22, 22), (52, 52), (32, 32), (1, 21)]:
+        nfA, dA = op_nf_dim(ca)
+        nfB, dB = op_nf_dim(cb)
+        kinds = [("tgeneral", 4, (meshgen.uniform(81 + ca + cb, ns * dA * dB) - 0.5).reshape(ns, dA * dB))]
+        if dA == 3 and dB == 3:
+            kinds += [("tsym", 3, sym6s)]
+        if dA == dB or dA == 1:
+            kinds += [("null", 0, None)]
+        for kname, kind, D in kinds:
+            name = f"{ca}_{cb}_{kname}_o4"
+            out[f"sliver_{name}_A"] = R.fem3dtet(ca, cb, kind, 4, SX, D, nfA=nfA, nfB=nfB)
+            if D is not None:
+                out[f"sliver_{name}_D"] = np.asarray(D, dtype=np.float64)
+            sliver_cases.append(name)
+    out["sliver_case_names"] = np.array(sliver_cases)
     # fem3DapplyL at the order-4 quadrature points and fem3DapplyX at seeded physical points (some
     # outside the tet), for every operator code, on the same tets
     p4, _ = R.quadrature(4)
@@ -147,7 +201,7 @@ def main():
         out[f"apply_{code}_X"] = R.fem3d_apply(code, XY, out["apply_X"], dofs, nf, dim, phys=True)
     out["apply_codes"] = np.array(apply_codes)
     # the reference's triangle rules and fem3Dface (every face, orders 0..9) on the same tets
-    for o in range(10):
+    for o in range(21):
         p3, w3 = R.tri_quadrature(o)
         out[f"tri_{o}_p"] = p3
         out[f"tri_{o}_w"] = w3
@@ -159,7 +213,7 @@ def main():
         kinds = [("tgeneral", 4, gen)]
         if dA == dB or dA == 1:
             kinds += [("null", 0, None), ("tscalar", 2, scalar_tet)]
-        for order in (1, 2, 4, 7, 9):
+        for order in (1, 2, 4, 7, 9) + ((13, 20) if (ca, cb) in ((1, 21), (22, 22)) else ()):
             for face in range(4):
                 for kname, kind, D in kinds:
                     name = f"{ca}_{cb}_{kname}_o{order}_f{face}"

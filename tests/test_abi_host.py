@@ -47,10 +47,23 @@ def test_library_load_without_gpu_fails_loudly():
 def test_quadrature_from_library_matches_oracle(restated):
     import anigpu
     anigpu.load_library()
-    for o in range(7):
+    for o in range(21):
         p, w = anigpu.quadrature(o)
         po, wo = restated.quadrature(o)
         assert np.array_equal(p, po) and np.array_equal(w, wo)
+
+
+def test_drop_in_template_header_compiles():
+    """include/anigpu_fem.hpp with code spelled against AniFem++'s headers (tests/cpp/fem_template.cpp:
+    fem3Dtet<Operator<...>, Operator<...>, DfuncTraits<...>>, functors, GenerateElemMatRhs, Assembler)
+    compiles as C++14 and C++17 (no GPU needed; tests/test_gpu_template.py runs it)."""
+    import subprocess
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    for std in ("c++14", "c++17"):
+        r = subprocess.run(["g++", f"-std={std}", "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-I",
+                            os.path.join(REPO, "include"), "-I", os.path.join(cuda, "include"),
+                            os.path.join(REPO, "tests", "cpp", "fem_template.cpp")], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
 
 
 def test_splitmix_streams_are_fixed():

@@ -54,6 +54,41 @@ def test_fem3dtet_f32_error_bound(lib, golden):
     print("worst FP32 relative error per tet:", worst)
 
 
+def _run_sliver(lib, golden, name, precision):
+    from helpers import KIND_CODE
+    XY = golden["sliver_XY"]
+    ca, cb, kind, order = parse_case(name)
+    D = golden[f"sliver_{name}_D"] if f"sliver_{name}_D" in golden.files else None
+    return lib.fem3dtet(ca, cb, XY, D, KIND_CODE[kind], order, precision).double().cpu().numpy()
+
+
+def test_fem3dtet_slivers_f64_matches_reference(lib, golden):
+    """Badly shaped tets (|det| / (|e1||e2||e3|) from 0.58 down to 1e-6): FP64 within 1e-12 of the
+    reference's fem3Dtet."""
+    import anigpu
+    for name in golden["sliver_case_names"]:
+        name = str(name)
+        err = rel_err_per_tet(_run_sliver(lib, golden, name, anigpu.F64), golden[f"sliver_{name}_A"])
+        assert err <= 1e-12, (name, err)
+
+
+def test_fem3dtet_slivers_f32_error(lib, golden):
+    """The FP32 kernels on the same tets: those with |det| <= 0.05 |e1||e2||e3| take the FP64
+    geometry branch; every tet stays within the FP32 bound of 2e-5 relative (Frobenius, per tet)."""
+    import anigpu
+    XY = golden["sliver_XY"].reshape(-1, 4, 3)
+    e = XY[:, 1:] - XY[:, :1]
+    ratio = np.abs(np.linalg.det(e)) / np.prod(np.linalg.norm(e, axis=2), axis=1)
+    assert (ratio <= 0.05).sum() >= 10 and (ratio > 0.05).sum() >= 5  # both branches are exercised
+    worst = 0.0
+    for name in golden["sliver_case_names"]:
+        name = str(name)
+        err = rel_err_per_tet(_run_sliver(lib, golden, name, anigpu.F32), golden[f"sliver_{name}_A"])
+        worst = max(worst, err)
+        assert err <= 2e-5, (name, err)
+    print("worst FP32 relative error per tet on slivers:", worst)
+
+
 def test_golden_matrices_on_gpu(lib, golden):
     import anigpu
     XY = golden["int_tet_test_tet_onepoint"].reshape(1, 12)
@@ -111,7 +146,7 @@ def test_errors_are_reported(lib):
     import anigpu
     XY = np.zeros((1, 12))
     with pytest.raises(anigpu.AnigpuError) as e:
-        lib.fem3dtet(22, 22, XY, None, anigpu.TENSOR_NULL, 9)  # order above 6
+        lib.fem3dtet(22, 22, XY, None, anigpu.TENSOR_NULL, 21)  # order above 20
     assert e.value.code == anigpu.ERR_UNSUPPORTED
     with pytest.raises(anigpu.AnigpuError) as e:
         lib.fem3dtet(22, 21, XY, None, anigpu.TENSOR_NULL, 2)  # identity of incompatible dims (3 vs 1)

@@ -2,6 +2,8 @@
 and polynomial against the FP64 autograd oracle (oracle/gnn_oracle.py), the hand-written
 backward kernels against autograd gradients, symmetry of M, training that lowers the loss and
 the iteration count, and the Jacobi fallback."""
+import os
+
 import numpy as np
 import pytest
 
@@ -225,3 +227,28 @@ def test_vector_p2_learned_matches_oracle(lib, restated):
     xs, st = lib.solve(S["vals"], r, anigpu.SOLVE_FCG_LEARNED, anigpu.F32, rtol=1e-8, maxit=100000)
     assert st.rel_residual <= 1e-8 and st.fallback_steps == 0
     assert _rel(xs.cpu().numpy(), e) <= 1e-3
+
+
+def test_refined_solves_reach_tolerance_on_fp64_system(lib, restated):
+    """anigpu_solve_refined: the FP32-assembled matrix drives the inner iterations (FCG with the
+    trained preconditioner; FP32 CG in IR), the FP64-assembled matrix every residual replacement and
+    the stopping test; the solution's FP64 residual on the FP64 system, checked by the oracle, meets
+    1e-8 (the plain FP32 solves only meet it on the FP32 system)."""
+    import anigpu
+    from anigpu import learned, meshgen
+    xyz, tets, D = meshgen.p2_aniso_workload(8, seed=77)
+    lib.mesh_upload(xyz, tets)
+    lib.problem_setup(anigpu.P2)
+    lib.set_dirichlet(meshgen.boundary_mask(lib.dof_coords().cpu().numpy()))
+    v32, rhs32, _ = lib.assemble(anigpu.TENSOR_TET_SYM, D, None, 1.0, 4, anigpu.F32)
+    v64, rhs64, _ = lib.assemble(anigpu.TENSOR_TET_SYM, D, None, 1.0, 4, anigpu.F64)
+    rp, col = lib.csr_template()
+    rp, col = rp.cpu().numpy(), col.cpu().numpy()
+    prec = anigpu.LearnedPreconditioner(lib, layers=4, act=anigpu.BF16, seed=1)
+    if os.path.exists(learned.DEFAULT_WEIGHTS):
+        learned.load_default(prec)
+    prec.bind(v32, anigpu.F32, anigpu.TENSOR_TET_SYM, D)
+    for method in (anigpu.SOLVE_FCG_LEARNED, anigpu.SOLVE_IR_CG32):
+        x, st = lib.solve_refined(v32, v64, rhs64, method, rtol=1e-8, maxit=20000)
+        tr = restated.true_residual(rp, col, v64.cpu().numpy(), x.cpu().numpy(), rhs64.cpu().numpy())
+        assert st.rel_residual <= 1e-8 and tr <= 1.0001e-8, (method, st.rel_residual, tr)

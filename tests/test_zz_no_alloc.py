@@ -62,12 +62,13 @@ def _soup(lib, nt):
     lib.problem_setup(anigpu.P1)
 
 
-@pytest.mark.parametrize("precision,limit", [(1, 262_144), (0, 524_288)])
-def test_noalloc_limit_is_exact(lib, precision, limit):
+@pytest.mark.parametrize("prec_name,limit", [("F64", 262_144), ("F32", 524_288)])
+def test_noalloc_limit_is_exact(lib, prec_name, limit):
     """A mesh of exactly the documented number of tets is accepted, one more is rejected."""
     import torch
 
     import anigpu
+    precision = getattr(anigpu, prec_name)
     dt = torch.float64 if precision == anigpu.F64 else torch.float32
     for nt, ok in ((limit, True), (limit + 1, False)):
         _soup(lib, nt)
