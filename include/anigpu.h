@@ -97,6 +97,10 @@ int anigpu_create(anigpu_handle* h, int device);
 int anigpu_destroy(anigpu_handle h);
 /* run the handle's work on an existing stream (cudaStream_t), 0 = the handle's own */
 int anigpu_set_stream(anigpu_handle h, void* stream);
+/* the stream (cudaStream_t) the handle's work runs on; host code that copies the handle's outputs
+ * orders its copies on it (the handle's own stream does not synchronise with the legacy default
+ * stream) */
+int anigpu_get_stream(anigpu_handle h, void** stream);
 const char* anigpu_last_error(anigpu_handle h);
 /* kernels launched by this handle since creation (evidence for bench reports) */
 int64_t anigpu_launch_count(anigpu_handle h);
@@ -386,6 +390,29 @@ int anigpu_batch_info(anigpu_handle h, int* ntiles, int* lanes_per_row, float* t
 int anigpu_batch_run(anigpu_handle h, int tensor_kind, const double* D, const double* f, double f_const, int order,
                      double* vals, double* rhs_assembled, const double* b, double* x, double rtol, int64_t maxit,
                      anigpu_solve_stats* stats);
+/* Several batched jobs (handles on one device, each set up with its own instances: e.g. the P1
+ * instances and the P2 instances of one study) as ONE CUDA graph launch: per job the same
+ * assembly, initialisation and device-side solve loop as anigpu_batch_run, the jobs' node chains
+ * independent so that they run concurrently.  The launch is on the first job's stream; every job's
+ * stream waits for it.  Returns the first error (ANIGPU_ERR_NOT_CONVERGED when an instance of any
+ * job missed rtol; stats per job as anigpu_batch_run). */
+typedef struct anigpu_batch_job {
+    anigpu_handle h;
+    int tensor_kind;
+    const double* D;
+    const double* f;
+    double f_const;
+    int order;
+    double* vals;
+    double* rhs_assembled;
+    const double* b;
+    double* x;
+    anigpu_solve_stats* stats;
+} anigpu_batch_job;
+int anigpu_batch_run_jobs(int njobs, const anigpu_batch_job* jobs, double rtol, int64_t maxit);
+/* the assembly's autotuned rows per block of a batched job: warps of 32 rows (1 or 2) and the
+ * timings of the two candidates (ms per assembly, ms[2]), measured at the job's first run */
+int anigpu_batch_assembly_tuning(anigpu_handle h, int* row_warps, float* ms);
 
 /* y = A x on the handle's template (F64 or F32 values, f64 vectors) */
 int anigpu_spmv(anigpu_handle h, const void* vals, int precision, const double* x, double* y);

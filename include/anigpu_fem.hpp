@@ -330,6 +330,17 @@ inline void check_rc(anigpu_handle h, int rc, const char* what) {
 inline void check_cuda(cudaError_t e, const char* what) {
     if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
 }
+inline cudaStream_t handle_stream(anigpu_handle h) {
+    void* s = nullptr;
+    check_rc(h, anigpu_get_stream(h, &s), "anigpu_get_stream");
+    return static_cast<cudaStream_t>(s);
+}
+/* host <-> device copies ordered on the handle's stream, then waited for */
+inline void copy_on(anigpu_handle h, void* dst, const void* src, std::size_t bytes, cudaMemcpyKind kind) {
+    cudaStream_t st = handle_stream(h);
+    check_cuda(cudaMemcpyAsync(dst, src, bytes, kind, st), "cudaMemcpyAsync");
+    check_cuda(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+}
 
 /* one element-integral request: a batch of f tets with one operator pair, rule and face */
 struct Request {
@@ -481,11 +492,13 @@ private:
             case ANIGPU_TENSOR_TET_GENERAL: nd = (std::size_t)r.dA * r.dBt * nt; break;
             default: nd = r.d_len == 0 ? 0 : r.d_len / (std::size_t)r.f * nt; break;
         }
+        cudaStream_t st = handle_stream(h);
         double* dxy = static_cast<double*>(bxy_.get(sizeof(double) * nxy));
         double* dd = nd ? static_cast<double*>(bd_.get(sizeof(double) * nd)) : nullptr;
         double* da = static_cast<double*>(ba_.get(sizeof(double) * nout));
-        check_cuda(cudaMemcpy(dxy, xy, sizeof(double) * nxy, cudaMemcpyHostToDevice), "cudaMemcpy");
-        if (nd) check_cuda(cudaMemcpy(dd, d, sizeof(double) * nd, cudaMemcpyHostToDevice), "cudaMemcpy");
+        // every copy on the handle's stream: it does not synchronise with the legacy default stream
+        check_cuda(cudaMemcpyAsync(dxy, xy, sizeof(double) * nxy, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync");
+        if (nd) check_cuda(cudaMemcpyAsync(dd, d, sizeof(double) * nd, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync");
         int rc;
         if (r.face < 0)
             rc = anigpu_fem3dtet(h, r.codeA, r.codeB, r.kind, r.order, ANIGPU_F64, nt, dxy, dd, da);
@@ -495,7 +508,8 @@ private:
             rc = anigpu_fem3dface(h, r.codeA, r.codeB, r.kind, r.order, ANIGPU_F64, nt, dxy, r.face, dd, da);
         if (rc == ANIGPU_ERR_ARG || rc == ANIGPU_ERR_UNSUPPORTED) check_rc(h, rc, "fem3Dtet");
         check_rc(h, rc, "fem3Dtet (GPU)");
-        check_cuda(cudaMemcpy(out, da, sizeof(double) * nout, cudaMemcpyDeviceToHost), "cudaMemcpy");
+        check_cuda(cudaMemcpyAsync(out, da, sizeof(double) * nout, cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync");
+        check_cuda(cudaStreamSynchronize(st), "cudaStreamSynchronize");
     }
 
     anigpu_handle h_ = nullptr;
@@ -1012,8 +1026,10 @@ struct SparseMatrix {
         gpu_detail::check_cuda(cudaMalloc((void**)&vals, sizeof(double) * std::max<int64_t>(nz, 1)), "cudaMalloc");
         n = nrow, nnz = nz;
     }
+    /* host copies (after the device work of the assembly that filled the matrix) */
     void download(std::vector<int64_t>& rp, std::vector<int32_t>& c, std::vector<double>& v) const {
         rp.resize(n + 1), c.resize(nnz), v.resize(nnz);
+        gpu_detail::check_cuda(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
         gpu_detail::check_cuda(cudaMemcpy(rp.data(), rowptr, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost), "cudaMemcpy");
         gpu_detail::check_cuda(cudaMemcpy(c.data(), col, sizeof(int32_t) * nnz, cudaMemcpyDeviceToHost), "cudaMemcpy");
         gpu_detail::check_cuda(cudaMemcpy(v.data(), vals, sizeof(double) * nnz, cudaMemcpyDeviceToHost), "cudaMemcpy");
@@ -1038,6 +1054,7 @@ struct Vector {
     }
     void download(std::vector<double>& v) const {
         v.resize(n);
+        gpu_detail::check_cuda(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
         gpu_detail::check_cuda(cudaMemcpy(v.data(), data, sizeof(double) * n, cudaMemcpyDeviceToHost), "cudaMemcpy");
     }
 };
@@ -1074,9 +1091,10 @@ public:
         int32_t* dtets = nullptr;
         gpu_detail::check_cuda(cudaMalloc((void**)&dxyz, sizeof(double) * 3 * nv_), "cudaMalloc");
         gpu_detail::check_cuda(cudaMalloc((void**)&dtets, sizeof(int32_t) * 4 * nt_), "cudaMalloc");
-        cudaMemcpy(dxyz, xyz_.data(), sizeof(double) * 3 * nv_, cudaMemcpyHostToDevice);
-        cudaMemcpy(dtets, tets_.data(), sizeof(int32_t) * 4 * nt_, cudaMemcpyHostToDevice);
+        gpu_detail::copy_on(h_, dxyz, xyz_.data(), sizeof(double) * 3 * nv_, cudaMemcpyHostToDevice);
+        gpu_detail::copy_on(h_, dtets, tets_.data(), sizeof(int32_t) * 4 * nt_, cudaMemcpyHostToDevice);
         int rc = anigpu_mesh_upload(h_, nv_, dxyz, nt_, dtets);
+        gpu_detail::check_cuda(cudaStreamSynchronize(gpu_detail::handle_stream(h_)), "cudaStreamSynchronize");
         cudaFree(dxyz);
         cudaFree(dtets);
         gpu_detail::check_rc(h_, rc, "mesh upload");
@@ -1093,8 +1111,8 @@ public:
         elem_xy_.resize(12 * nt_);
         elem_nodes_.resize(4 * nt_);
         if (rc == ANIGPU_OK) {
-            cudaMemcpy(elem_xy_.data(), dxy, sizeof(double) * 12 * nt_, cudaMemcpyDeviceToHost);
-            cudaMemcpy(elem_nodes_.data(), dn, sizeof(int32_t) * 4 * nt_, cudaMemcpyDeviceToHost);
+            gpu_detail::copy_on(h_, elem_xy_.data(), dxy, sizeof(double) * 12 * nt_, cudaMemcpyDeviceToHost);
+            gpu_detail::copy_on(h_, elem_nodes_.data(), dn, sizeof(int32_t) * 4 * nt_, cudaMemcpyDeviceToHost);
         }
         cudaFree(dxy);
         cudaFree(dn);
@@ -1135,15 +1153,14 @@ public:
                     throw std::runtime_error("fem3Dtet replay: fewer element integrals than recorded (the local assembler "
                                              "must make the same calls on both passes)");
                 s.clear_records();
-                gpu_detail::check_cuda(cudaMemcpy(dA + nA * e0, Ae.data(), sizeof(double) * nA * (e1 - e0), cudaMemcpyHostToDevice),
-                                       "cudaMemcpy");
-                gpu_detail::check_cuda(cudaMemcpy(dF + nF * e0, Fe.data(), sizeof(double) * nF * (e1 - e0), cudaMemcpyHostToDevice),
-                                       "cudaMemcpy");
+                gpu_detail::copy_on(h_, dA + nA * e0, Ae.data(), sizeof(double) * nA * (e1 - e0), cudaMemcpyHostToDevice);
+                gpu_detail::copy_on(h_, dF + nF * e0, Fe.data(), sizeof(double) * nF * (e1 - e0), cudaMemcpyHostToDevice);
             }
             A.resize(ndof_, nnz_);
             b.resize(ndof_);
             gpu_detail::check_rc(h_, anigpu_csr_template(h_, A.rowptr, A.col), "Assemble");
             const int rc = anigpu_assemble_elements(h_, dA, dF, A.vals, b.data);
+            gpu_detail::check_cuda(cudaStreamSynchronize(gpu_detail::handle_stream(h_)), "cudaStreamSynchronize");
             if (rc == ANIGPU_ERR_NONFINITE)
                 status = -1;
             else

@@ -75,6 +75,7 @@ SIGNATURES = {
     "anigpu_element_dofs": (_i, [_vp, _vp]),
     "anigpu_element_coords": (_i, [_vp, _vp]),
     "anigpu_element_nodes": (_i, [_vp, _vp]),
+    "anigpu_get_stream": (_i, [_vp, ctypes.POINTER(_vp)]),
     "anigpu_dof_coords": (_i, [_vp, _vp]),
     "anigpu_set_dirichlet": (_i, [_vp, _vp, _vp]),
     "anigpu_assemble": (_i, [_vp, _i, _vp, _vp, _d, _i, _i, _vp, _vp, _vp, _d]),
@@ -90,6 +91,8 @@ SIGNATURES = {
     "anigpu_batch_set_instances": (_i, [_vp, _i, _vp, _vp]),
     "anigpu_batch_info": (_i, [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i), _vp, ctypes.POINTER(_i)]),
     "anigpu_batch_run": (_i, [_vp, _i, _vp, _vp, _d, _i, _vp, _vp, _vp, _vp, _d, _i64, _vp]),
+    "anigpu_batch_run_jobs": (_i, [_i, _vp, _d, _i64]),
+    "anigpu_batch_assembly_tuning": (_i, [_vp, _vp, _vp]),
     "anigpu_gnn_init": (_i, [_vp, _i, _i, ctypes.c_uint64]),
     "anigpu_gnn_num_params": (_i64, [_vp]),
     "anigpu_gnn_get_params": (_i, [_vp, _vp, _i64]),
@@ -576,6 +579,14 @@ class Anigpu:
             self._check(rc)
         return x, vals, list(st)
 
+    def batch_assembly_tuning(self):
+        """(rows per block in warps of 32, [ms for 1, 2 warps]) of the batch's assembly."""
+        import numpy as np
+        w = ctypes.c_int()
+        ms = np.zeros(2, dtype=np.float32)
+        self._check(self.lib.anigpu_batch_assembly_tuning(self.h, ctypes.byref(w), ms.ctypes.data))
+        return w.value, ms.tolist()
+
     def status(self):
         """Waits for the handle's stream; raises AnigpuError on a non-finite value recorded
         by an assembly since the last check."""
@@ -623,6 +634,48 @@ class Anigpu:
         if check:
             self._check(rc)
         return x, st
+
+
+class BatchJob(ctypes.Structure):
+    """anigpu_batch_job (include/anigpu.h)."""
+    _fields_ = [("h", ctypes.c_void_p), ("tensor_kind", ctypes.c_int), ("D", ctypes.c_void_p),
+                ("f", ctypes.c_void_p), ("f_const", ctypes.c_double), ("order", ctypes.c_int),
+                ("vals", ctypes.c_void_p), ("rhs_assembled", ctypes.c_void_p), ("b", ctypes.c_void_p),
+                ("x", ctypes.c_void_p), ("stats", ctypes.c_void_p)]
+
+
+def batch_run_jobs(jobs, rtol=1e-8, maxit=100000, check=True):
+    """Several batched jobs as one CUDA graph launch (anigpu_batch_run_jobs).  jobs: list of dicts
+    with keys lib (an Anigpu with instances set), b, kind, D, f, f_const, order and optionally vals.
+    Returns a list of (x, vals, stats) per job."""
+    import torch
+    arr = (BatchJob * len(jobs))()
+    keep, out = [], []
+    addr = lambda t: None if t is None else t.data_ptr()  # noqa: E731
+    for k, j in enumerate(jobs):
+        lib = j["lib"]
+        dev = f"cuda:{lib.device}"
+        vals = j.get("vals")
+        if vals is None:
+            vals = torch.empty(lib.nnz, dtype=torch.float64, device=dev)
+        rhs = torch.empty(lib.ndof, dtype=torch.float64, device=dev)
+        b = lib._dev(j["b"], torch.float64)
+        x = torch.empty_like(b)
+        D = lib._dev(j["D"], torch.float64) if j.get("D") is not None else None
+        f = lib._dev(j["f"], torch.float64) if j.get("f") is not None else None
+        st = (SolveStats * lib.ninst)()
+        h = lib.h.value if isinstance(lib.h, ctypes.c_void_p) else lib.h
+        arr[k] = BatchJob(h, j.get("kind", TENSOR_NULL), addr(D), addr(f), float(j.get("f_const", 1.0)),
+                          j.get("order", 2), addr(vals), addr(rhs), addr(b), addr(x), ctypes.addressof(st))
+        keep += [vals, rhs, b, x, D, f, st]
+        out.append((x, vals, st))
+    lib0 = jobs[0]["lib"]
+    torch.cuda.synchronize()
+    rc = lib0.lib.anigpu_batch_run_jobs(len(jobs), ctypes.cast(arr, ctypes.c_void_p), float(rtol), int(maxit))
+    torch.cuda.synchronize()
+    if check:
+        lib0._check(rc)
+    return [(x, vals, list(st)) for x, vals, st in out]
 
 
 class LearnedPreconditioner:

@@ -66,6 +66,7 @@ struct anigpu_ctx {
     cudaStream_t own_stream = nullptr;
     cudaStream_t side_stream = nullptr;  // second stream for concurrent launches inside one call
     cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+    int row_warps = 2;  // row-gather warps (32 rows each) per block; the batch autotuner sets it
     std::string err;
     int64_t launches = 0;
 
@@ -230,3 +231,5 @@ int batch_set_instances(anigpu_ctx* h, int ninst, const int64_t* toff_host, cons
 int batch_info(anigpu_ctx* h, int* ntiles, int* lanes, float* tune_ms, int* device_loop);
 int batch_run(anigpu_ctx* h, int kind, const double* D, const double* f, double f_const, int order, double* vals,
               double* rhs_assembled, const double* b, double* x, double rtol, int64_t maxit, anigpu_solve_stats* st);
+int batch_run_jobs(int njobs, const anigpu_batch_job* jobs, double rtol, int64_t maxit);
+int batch_assembly_tuning(anigpu_ctx* h, int* row_warps, float* ms);

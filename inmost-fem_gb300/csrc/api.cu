@@ -95,6 +95,13 @@ int anigpu_set_stream(anigpu_handle h, void* stream) {
     return ANIGPU_OK;
 }
 
+int anigpu_get_stream(anigpu_handle h, void** stream) {
+    CHECK_H(h);
+    if (!stream) return set_err(h, ANIGPU_ERR_ARG, "NULL");
+    *stream = (void*)h->stream;
+    return ANIGPU_OK;
+}
+
 const char* anigpu_last_error(anigpu_handle h) { return h ? h->err.c_str() : "invalid handle"; }
 
 int64_t anigpu_launch_count(anigpu_handle h) { return h ? h->launches : -1; }
@@ -442,6 +449,19 @@ int anigpu_batch_set_instances(anigpu_handle h, int ninst, const int64_t* tet_of
 int anigpu_batch_info(anigpu_handle h, int* ntiles, int* lanes_per_row, float* tune_ms, int* device_loop) {
     CHECK_H(h);
     return batch_info(h, ntiles, lanes_per_row, tune_ms, device_loop);
+}
+
+int anigpu_batch_run_jobs(int njobs, const anigpu_batch_job* jobs, double rtol, int64_t maxit) {
+    if (njobs < 1 || !jobs) return ANIGPU_ERR_ARG;
+    for (int k = 0; k < njobs; ++k)
+        if (!jobs[k].h) return ANIGPU_ERR_ARG;
+    cudaSetDevice(jobs[0].h->device);
+    return batch_run_jobs(njobs, jobs, rtol, maxit);
+}
+
+int anigpu_batch_assembly_tuning(anigpu_handle h, int* row_warps, float* ms) {
+    CHECK_H(h);
+    return batch_assembly_tuning(h, row_warps, ms);
 }
 
 int anigpu_batch_run(anigpu_handle h, int tensor_kind, const double* D, const double* f, double f_const, int order,

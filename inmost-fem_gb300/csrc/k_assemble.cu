@@ -1259,7 +1259,7 @@ static int get_row_tables(anigpu_ctx* h, int space, int order, int precision, co
 template <typename Real, int NLOC, int FORM, bool DIR, bool BCNZ, bool TOUCH, bool DROPCHK>
 static int launch_rows_t(anigpu_ctx* h, const RowParams& p, const void* tables, void* vals, double* rhs,
                          uint8_t* touched, cudaStream_t st) {
-    const int warps = 2;
+    const int warps = h->row_warps == 1 ? 1 : 2;  // at most 64 threads (the kernel's launch bounds)
     const size_t smem = RowSmem<Real, NLOC, FORM, TOUCH>::total(p.cap, warps);
     auto kern = row_gather_kernel<Real, NLOC, FORM, DIR, BCNZ, TOUCH, DROPCHK>;
     static int smem_set[64] = {};  // per device: the largest dynamic shared memory set so far

@@ -370,6 +370,8 @@ struct BatchWs {
     std::vector<int64_t> toff;
     float tune_ms[5] = {0, 0, 0, 0, 0};
     int conditional = 0;             // the last job ran as one graph with a device-side loop
+    int asm_tuned = 0;               // the assembly's rows per block were timed on this instance set
+    float asm_tune_ms[2] = {0, 0};   // assembly with 1, 2 warps (32 rows each) per block
 };
 
 // blocks of 256 threads (8 tiles in flight each), at most 8 blocks per SM on 152 SMs
@@ -552,118 +554,175 @@ int batch_info(anigpu_ctx* h, int* ntiles, int* lanes, float* tune_ms, int* devi
 }
 
 // the whole job: (optional) assembly, initialisation and every PCG iteration of every instance.
-// As one CUDA graph with a device-side while loop where conditional nodes are available,
-// else as host-driven launches of a captured body.
-int batch_run(anigpu_ctx* h, int kind, const double* D, const double* f, double f_const, int order, double* vals,
-              double* rhs_assembled, const double* b, double* x, double rtol, int64_t maxit, anigpu_solve_stats* st) {
-    BatchWs* w = ws(h);
-    if (!w) return set_err(h, ANIGPU_ERR_STATE, "anigpu_batch_set_instances not called");
-    if (!vals || !b || !x || !st) return set_err(h, ANIGPU_ERR_ARG, "NULL argument");
+// Several jobs (handles on one device, e.g. the P1 instances and the P2 instances) go into one
+// graph: per job a prologue (child graph) and a device-side while loop (conditional node) whose body
+// is kBatchIters iterations and a check kernel; the jobs' node chains are independent, so they run
+// concurrently within the one launch.  Where conditional nodes are unavailable the jobs run one after
+// the other as host-driven launches of their captured bodies.
+namespace {
+
+struct Job {
+    anigpu_ctx* h;
+    BatchWs* w;
+    int kind;
+    const double* D;
+    const double* f;
+    double f_const;
+    int order;
+    double* vals;
+    double* rhs_assembled;
+    const double* b;
+    double* x;
+    anigpu_solve_stats* st;
+    bool assemble;
+};
+
+int job_check(const Job& j, int64_t maxit) {
+    anigpu_ctx* h = j.h;
+    if (!j.w) return set_err(h, ANIGPU_ERR_STATE, "anigpu_batch_set_instances not called");
+    if (!j.vals || !j.b || !j.x || !j.st) return set_err(h, ANIGPU_ERR_ARG, "NULL argument");
     if (maxit < 1) return set_err(h, ANIGPU_ERR_ARG, "maxit");
+    return ANIGPU_OK;
+}
+
+// the assembly's rows per block (warps of 32 rows; the row gather is compiled for at most 64
+// threads per block): timed on this job's tensor once per instance set
+int tune_assembly(Job& j) {
+    anigpu_ctx* h = j.h;
+    BatchWs* w = j.w;
+    if (!j.assemble || w->asm_tuned) return ANIGPU_OK;
     cudaStream_t s = h->stream;
-    const int gt = grid_tiles(w->ntiles);
-    const bool assemble = rhs_assembled != nullptr;
-    if (assemble && h->tetdata_bytes < (size_t)h->nt * 8 * sizeof(double)) {
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int cand[2] = {1, 2};
+    float best = 1e30f;
+    int bestw = h->row_warps;
+    for (int c = 0; c < 2; ++c) {
+        h->row_warps = cand[c];
+        RC_(run_assemble(h, j.kind, j.D, j.f, j.f_const, j.order, ANIGPU_F64, j.vals, j.rhs_assembled, nullptr, 1e-100));
+        cudaEventRecord(e0, s);
+        for (int rep = 0; rep < 3; ++rep)
+            RC_(run_assemble(h, j.kind, j.D, j.f, j.f_const, j.order, ANIGPU_F64, j.vals, j.rhs_assembled, nullptr,
+                             1e-100));
+        cudaEventRecord(e1, s);
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        w->asm_tune_ms[c] = ms / 3;
+        if (ms < best) {
+            best = ms;
+            bestw = cand[c];
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    h->row_warps = bestw;
+    w->asm_tuned = 1;
+    RC_(status_check(h, "assembly"));
+    return ANIGPU_OK;
+}
+
+int job_prepare(Job& j, int64_t maxit) {
+    anigpu_ctx* h = j.h;
+    BatchWs* w = j.w;
+    if (j.assemble && h->tetdata_bytes < (size_t)h->nt * 8 * sizeof(double)) {
         // the per-tet blocks of the assembly: allocated before the graph is captured
         if (h->tetdata) cudaFree(h->tetdata);
         h->tetdata = nullptr;
         ANI_CUDA(h, cudaMalloc(&h->tetdata, (size_t)h->nt * 8 * sizeof(double)));
         h->tetdata_bytes = (size_t)h->nt * 8 * sizeof(double);
     }
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
-    cudaEventRecord(e0, s);
+    RC_(tune_assembly(j));
     BatchCtl c0{0, (long long)maxit, w->ninst, 0};
-    ANI_CUDA(h, cudaMemcpyAsync(w->ctl, &c0, sizeof(BatchCtl), cudaMemcpyHostToDevice, s));
-    // prologue: assembly (uncaptured first call sets kernel attributes), diagonal, initial residual
-    auto prologue = [&]() -> int {
-        if (assemble) RC_(run_assemble(h, kind, D, f, f_const, order, ANIGPU_F64, vals, rhs_assembled, nullptr, 1e-100));
-        bdiag_kernel<<<grid_for(w->n, 256), 256, 0, s>>>(w->n, h->rowptr, h->col, vals, w->dinv);
-        binit_kernel<<<gt, 256, 0, s>>>(w->ntiles, w->tstart, b, w->dinv, x, w->r, w->z, w->p, w->part,
-                                              w->part + w->ntiles);
-        binst_init_kernel<<<w->ninst, 128, 0, s>>>(w->ninst, w->itp, w->it, w->part, w->part + w->ntiles, rtol, w->sc);
-        h->launches += 3;
-        ANI_CUDA(h, cudaGetLastError());
-        return ANIGPU_OK;
-    };
-    auto body = [&](cudaGraphConditionalHandle hd, int use) -> int {
-        for (int k = 0; k < kBatchIters; ++k) RC_(one_iteration(h, w, vals, maxit, s));
-        bcheck_kernel<<<1, 256, 0, s>>>(w->ninst, w->sc, w->ctl, hd, use);
-        h->launches++;
-        ANI_CUDA(h, cudaGetLastError());
-        return ANIGPU_OK;
-    };
-    w->x = x;  // the iteration kernels update the caller's solution in place
+    ANI_CUDA(h, cudaMemcpyAsync(w->ctl, &c0, sizeof(BatchCtl), cudaMemcpyHostToDevice, h->stream));
+    ANI_CUDA(h, cudaStreamSynchronize(h->stream));
+    w->x = j.x;  // the iteration kernels update the caller's solution in place
     w->conditional = 0;
-    int rc = ANIGPU_OK;
-    {
-        // one graph: prologue (child graph) -> while(cond) { body }
-        cudaGraph_t pre = nullptr, g = nullptr;
-        cudaGraphExec_t exec = nullptr;
-        bool ok = false;
-        const int64_t l0 = h->launches;
-        if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
-            int prc = prologue();
-            cudaError_t e = cudaStreamEndCapture(s, &pre);
-            if (prc == ANIGPU_OK && e == cudaSuccess && pre && cudaGraphCreate(&g, 0) == cudaSuccess) {
-                cudaGraphNode_t preNode;
-                cudaGraphConditionalHandle hd;
-                if (cudaGraphAddChildGraphNode(&preNode, g, nullptr, 0, pre) == cudaSuccess &&
-                    cudaGraphConditionalHandleCreate(&hd, g, 1, cudaGraphCondAssignDefault) == cudaSuccess) {
-                    cudaGraphNodeParams np = {};
-                    np.type = cudaGraphNodeTypeConditional;
-                    np.conditional.handle = hd;
-                    np.conditional.type = cudaGraphCondTypeWhile;
-                    np.conditional.size = 1;
-                    cudaGraphNode_t cnode;
-                    if (cudaGraphAddNode(&cnode, g, &preNode, nullptr, 1, &np) == cudaSuccess) {
-                        cudaGraph_t bodyg = np.conditional.phGraph_out[0];
-                        if (cudaStreamBeginCaptureToGraph(s, bodyg, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) ==
-                            cudaSuccess) {
-                            int brc = body(hd, 1);
-                            cudaGraph_t outg = nullptr;
-                            e = cudaStreamEndCapture(s, &outg);
-                            ok = brc == ANIGPU_OK && e == cudaSuccess &&
-                                 cudaGraphInstantiate(&exec, g, 0) == cudaSuccess;
-                        }
-                    }
-                }
-            }
-        }
-        cudaGetLastError();
-        const int64_t per_graph = h->launches - l0;
-        h->launches = l0;
-        if (ok) {
-            w->conditional = 1;
-            const cudaError_t le = cudaGraphLaunch(exec, s);
-            if (le != cudaSuccess) rc = cuda_check(h, le, "cudaGraphLaunch");
-            // launches: prologue + body per executed round (rounds from the device counter below)
-            (void)per_graph;
-        }
-        if (exec) cudaGraphExecDestroy(exec);
-        if (g) cudaGraphDestroy(g);
-        if (pre) cudaGraphDestroy(pre);
-        if (rc) return rc;
-        if (!ok) {
-            // host-driven fallback: prologue, then captured bodies until the device says stop
-            RC_(prologue());
-            BatchCtl hc{};
-            while (true) {
-                RC_(body(0, 0));
-                ANI_CUDA(h, cudaMemcpyAsync(&hc, w->ctl, sizeof(BatchCtl), cudaMemcpyDeviceToHost, s));
-                ANI_CUDA(h, cudaStreamSynchronize(s));
-                if (hc.remaining == 0 || hc.iters >= hc.maxit) break;
-            }
-        }
+    return ANIGPU_OK;
+}
+
+// prologue: assembly, diagonal, initial residual
+int job_prologue(Job& j, double rtol) {
+    anigpu_ctx* h = j.h;
+    BatchWs* w = j.w;
+    cudaStream_t s = h->stream;
+    const int gt = grid_tiles(w->ntiles);
+    if (j.assemble) RC_(run_assemble(h, j.kind, j.D, j.f, j.f_const, j.order, ANIGPU_F64, j.vals, j.rhs_assembled, nullptr, 1e-100));
+    bdiag_kernel<<<grid_for(w->n, 256), 256, 0, s>>>(w->n, h->rowptr, h->col, j.vals, w->dinv);
+    binit_kernel<<<gt, 256, 0, s>>>(w->ntiles, w->tstart, j.b, w->dinv, j.x, w->r, w->z, w->p, w->part,
+                                    w->part + w->ntiles);
+    binst_init_kernel<<<w->ninst, 128, 0, s>>>(w->ninst, w->itp, w->it, w->part, w->part + w->ntiles, rtol, w->sc);
+    h->launches += 3;
+    ANI_CUDA(h, cudaGetLastError());
+    return ANIGPU_OK;
+}
+
+int job_body(Job& j, int64_t maxit, cudaGraphConditionalHandle hd, int use) {
+    anigpu_ctx* h = j.h;
+    BatchWs* w = j.w;
+    for (int k = 0; k < kBatchIters; ++k) RC_(one_iteration(h, w, j.vals, maxit, h->stream));
+    bcheck_kernel<<<1, 256, 0, h->stream>>>(w->ninst, w->sc, w->ctl, hd, use);
+    h->launches++;
+    ANI_CUDA(h, cudaGetLastError());
+    return ANIGPU_OK;
+}
+
+// job j's nodes in graph g: prologue child graph -> while(cond) { body }
+bool job_add_to_graph(Job& j, cudaGraph_t g, double rtol, int64_t maxit, cudaGraph_t* pre_out) {
+    anigpu_ctx* h = j.h;
+    cudaStream_t s = h->stream;
+    cudaGraph_t pre = nullptr;
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return false;
+    const int prc = job_prologue(j, rtol);
+    cudaError_t e = cudaStreamEndCapture(s, &pre);
+    *pre_out = pre;
+    if (prc != ANIGPU_OK || e != cudaSuccess || !pre) return false;
+    cudaGraphNode_t preNode;
+    cudaGraphConditionalHandle hd;
+    if (cudaGraphAddChildGraphNode(&preNode, g, nullptr, 0, pre) != cudaSuccess) return false;
+    if (cudaGraphConditionalHandleCreate(&hd, g, 1, cudaGraphCondAssignDefault) != cudaSuccess) return false;
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = hd;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t cnode;
+    if (cudaGraphAddNode(&cnode, g, &preNode, nullptr, 1, &np) != cudaSuccess) return false;
+    cudaGraph_t bodyg = np.conditional.phGraph_out[0];
+    if (cudaStreamBeginCaptureToGraph(s, bodyg, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+        return false;
+    const int brc = job_body(j, maxit, hd, 1);
+    cudaGraph_t outg = nullptr;
+    e = cudaStreamEndCapture(s, &outg);
+    return brc == ANIGPU_OK && e == cudaSuccess;
+}
+
+// host-driven fallback for one job: prologue, then captured bodies until the device says stop
+int job_run_host(Job& j, double rtol, int64_t maxit) {
+    anigpu_ctx* h = j.h;
+    RC_(job_prologue(j, rtol));
+    BatchCtl hc{};
+    while (true) {
+        RC_(job_body(j, maxit, 0, 0));
+        ANI_CUDA(h, cudaMemcpyAsync(&hc, j.w->ctl, sizeof(BatchCtl), cudaMemcpyDeviceToHost, h->stream));
+        ANI_CUDA(h, cudaStreamSynchronize(h->stream));
+        if (hc.remaining == 0 || hc.iters >= hc.maxit) break;
     }
-    cudaEventRecord(e1, s);
-    // statistics: FP64 true residual per instance
+    return ANIGPU_OK;
+}
+
+// statistics: FP64 true residual per instance; launch count of the job
+int job_finish(Job& j, double rtol, float ms, bool* all) {
+    anigpu_ctx* h = j.h;
+    BatchWs* w = j.w;
+    cudaStream_t s = h->stream;
+    const int gt = grid_tiles(w->ntiles);
     switch (w->W) {
-        case 2: bresid_kernel<2><<<gt, 256, 0, s>>>(w->ntiles, w->tstart, h->rowptr, h->col, vals, x, b, w->part); break;
-        case 8: bresid_kernel<8><<<gt, 256, 0, s>>>(w->ntiles, w->tstart, h->rowptr, h->col, vals, x, b, w->part); break;
-        case 16: bresid_kernel<16><<<gt, 256, 0, s>>>(w->ntiles, w->tstart, h->rowptr, h->col, vals, x, b, w->part); break;
-        default: bresid_kernel<4><<<gt, 256, 0, s>>>(w->ntiles, w->tstart, h->rowptr, h->col, vals, x, b, w->part);
+        case 2: bresid_kernel<2><<<gt, 256, 0, s>>>(w->ntiles, w->tstart, h->rowptr, h->col, j.vals, j.x, j.b, w->part); break;
+        case 8: bresid_kernel<8><<<gt, 256, 0, s>>>(w->ntiles, w->tstart, h->rowptr, h->col, j.vals, j.x, j.b, w->part); break;
+        case 16: bresid_kernel<16><<<gt, 256, 0, s>>>(w->ntiles, w->tstart, h->rowptr, h->col, j.vals, j.x, j.b, w->part); break;
+        default: bresid_kernel<4><<<gt, 256, 0, s>>>(w->ntiles, w->tstart, h->rowptr, h->col, j.vals, j.x, j.b, w->part);
     }
     binst_sum_kernel<<<w->ninst, 128, 0, s>>>(w->ninst, w->itp, w->it, w->part, w->isum);
     ANI_LAUNCHED(h);
@@ -674,16 +733,108 @@ int batch_run(anigpu_ctx* h, int kind, const double* D, const double* f, double 
     ANI_CUDA(h, cudaMemcpyAsync(hs.data(), w->sc, sizeof(InstScalars) * w->ninst, cudaMemcpyDeviceToHost, s));
     ANI_CUDA(h, cudaMemcpyAsync(&hc, w->ctl, sizeof(BatchCtl), cudaMemcpyDeviceToHost, s));
     ANI_CUDA(h, cudaStreamSynchronize(s));
+    h->launches += (j.assemble ? 3 : 0) + 3 + (hc.iters / kBatchIters) * (5 * kBatchIters + 1);
+    for (int i = 0; i < w->ninst; ++i) {
+        const double rel = hs[i].bb > 0 ? std::sqrt(rr[i] / hs[i].bb) : std::sqrt(rr[i]);
+        j.st[i] = anigpu_solve_stats{hs[i].iters, hc.iters, rel, ms * 1e-3, 0};
+        *all &= rel <= rtol;
+    }
+    return ANIGPU_OK;
+}
+
+int run_jobs(std::vector<Job>& jobs, double rtol, int64_t maxit) {
+    for (Job& j : jobs) RC_(job_check(j, maxit));
+    for (size_t k = 1; k < jobs.size(); ++k)
+        if (jobs[k].h->device != jobs[0].h->device)
+            return set_err(jobs[k].h, ANIGPU_ERR_ARG, "batched jobs of one launch must share a device");
+    for (Job& j : jobs) RC_(job_prepare(j, maxit));
+    anigpu_ctx* h0 = jobs[0].h;
+    cudaStream_t s0 = h0->stream;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    int rc = ANIGPU_OK;
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<cudaGraph_t> pres(jobs.size(), nullptr);
+    bool ok = cudaGraphCreate(&g, 0) == cudaSuccess;
+    for (size_t k = 0; k < jobs.size() && ok; ++k) {
+        const int64_t l0 = jobs[k].h->launches;
+        ok = job_add_to_graph(jobs[k], g, rtol, maxit, &pres[k]);
+        jobs[k].h->launches = l0;  // counted from the device's iteration count after the run
+    }
+    ok = ok && cudaGraphInstantiate(&exec, g, 0) == cudaSuccess;
+    cudaGetLastError();
+    // every job's inputs are ready on its own stream before the launch on the first job's stream
+    for (size_t k = 1; k < jobs.size(); ++k) {
+        ANI_CUDA(h0, cudaEventRecord(jobs[k].h->fork_ev, jobs[k].h->stream));
+        ANI_CUDA(h0, cudaStreamWaitEvent(s0, jobs[k].h->fork_ev, 0));
+    }
+    cudaEventRecord(e0, s0);
+    if (ok) {
+        for (Job& j : jobs) j.w->conditional = 1;
+        const cudaError_t le = cudaGraphLaunch(exec, s0);
+        if (le != cudaSuccess) rc = cuda_check(h0, le, "cudaGraphLaunch");
+    } else {
+        for (Job& j : jobs) {
+            if (j.h != h0) {
+                ANI_CUDA(h0, cudaEventRecord(h0->fork_ev, s0));
+                ANI_CUDA(j.h, cudaStreamWaitEvent(j.h->stream, h0->fork_ev, 0));
+            }
+            rc = job_run_host(j, rtol, maxit);
+            if (rc) break;
+            if (j.h != h0) {
+                ANI_CUDA(j.h, cudaEventRecord(j.h->join_ev, j.h->stream));
+                ANI_CUDA(h0, cudaStreamWaitEvent(s0, j.h->join_ev, 0));
+            }
+        }
+    }
+    cudaEventRecord(e1, s0);
+    cudaEventSynchronize(e1);
     float ms = 0;
     cudaEventElapsedTime(&ms, e0, e1);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    h->launches += (assemble ? 3 : 0) + 3 + (hc.iters / kBatchIters) * (5 * kBatchIters + 1);
-    bool all = true;
-    for (int i = 0; i < w->ninst; ++i) {
-        const double rel = hs[i].bb > 0 ? std::sqrt(rr[i] / hs[i].bb) : std::sqrt(rr[i]);
-        st[i] = anigpu_solve_stats{hs[i].iters, hc.iters, rel, ms * 1e-3, 0};
-        all &= rel <= rtol;
+    if (exec) cudaGraphExecDestroy(exec);
+    if (g) cudaGraphDestroy(g);
+    for (cudaGraph_t p : pres)
+        if (p) cudaGraphDestroy(p);
+    if (rc) return rc;
+    // the jobs' streams see the results: the launch ran on the first job's stream
+    for (size_t k = 1; k < jobs.size(); ++k) {
+        ANI_CUDA(h0, cudaEventRecord(h0->join_ev, s0));
+        ANI_CUDA(jobs[k].h, cudaStreamWaitEvent(jobs[k].h->stream, h0->join_ev, 0));
     }
-    return all ? ANIGPU_OK : set_err(h, ANIGPU_ERR_NOT_CONVERGED, "some instances did not reach the tolerance");
+    bool all = true;
+    for (Job& j : jobs) RC_(job_finish(j, rtol, ms, &all));
+    return all ? ANIGPU_OK : set_err(h0, ANIGPU_ERR_NOT_CONVERGED, "some instances did not reach the tolerance");
+}
+
+}  // namespace
+
+int batch_run(anigpu_ctx* h, int kind, const double* D, const double* f, double f_const, int order, double* vals,
+              double* rhs_assembled, const double* b, double* x, double rtol, int64_t maxit, anigpu_solve_stats* st) {
+    std::vector<Job> jobs{Job{h, ws(h), kind, D, f, f_const, order, vals, rhs_assembled, b, x, st, rhs_assembled != nullptr}};
+    return run_jobs(jobs, rtol, maxit);
+}
+
+int batch_run_jobs(int njobs, const anigpu_batch_job* in, double rtol, int64_t maxit) {
+    if (njobs < 1 || !in) return ANIGPU_ERR_ARG;
+    std::vector<Job> jobs;
+    for (int k = 0; k < njobs; ++k) {
+        const anigpu_batch_job& a = in[k];
+        if (!a.h) return ANIGPU_ERR_ARG;
+        jobs.push_back(Job{a.h, ws(a.h), a.tensor_kind, a.D, a.f, a.f_const, a.order, a.vals, a.rhs_assembled, a.b,
+                           a.x, a.stats, a.rhs_assembled != nullptr});
+    }
+    return run_jobs(jobs, rtol, maxit);
+}
+
+int batch_assembly_tuning(anigpu_ctx* h, int* row_warps, float* ms) {
+    BatchWs* w = ws(h);
+    if (!w) return set_err(h, ANIGPU_ERR_STATE, "anigpu_batch_set_instances not called");
+    if (row_warps) *row_warps = h->row_warps;
+    if (ms)
+        for (int c = 0; c < 2; ++c) ms[c] = w->asm_tune_ms[c];
+    return ANIGPU_OK;
 }

@@ -561,6 +561,86 @@ __global__ void __launch_bounds__(kBlk) dense_kernel(int64_t nc, const A* __rest
     Hout[v * C + lane + 32] = cvt<A>(ld(Hin + v * C + lane + 32) + fmaxf(z1, 0.f));
 }
 
+// The BF16 layer on the tensor cores: Z = G W + b, Hout = Hin + relu(Z) with
+// mma.sync.m16n8k16 (BF16 inputs, FP32 accumulation).  One warp computes a 16-node x 64-channel
+// tile: 4 k-steps x 8 n-tiles of 8 channels = 32 MMAs; A fragments (16 x 16 of G) are read straight
+// from global memory as BF16 pairs, B fragments from W^T staged once per block in shared memory as
+// BF16 (row n holds the 64 k of output channel n, padded to 72 so that the 8 rows of a fragment load
+// fall on distinct banks); the accumulators start at the bias.
+constexpr int kMmaWarps = 4;  // warps per block: 64 nodes
+constexpr int kWtStride = C + 8;
+
+__device__ __forceinline__ void mma_bf16_16816(float* d, const uint32_t* a, const uint32_t* b) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+__global__ void __launch_bounds__(kMmaWarps * 32) dense_mma_bf16_kernel(int64_t nc, const __nv_bfloat16* __restrict__ G,
+                                                                         const float* __restrict__ W,
+                                                                         const float* __restrict__ b,
+                                                                         const __nv_bfloat16* __restrict__ Hin,
+                                                                         __nv_bfloat16* __restrict__ Z,
+                                                                         __nv_bfloat16* __restrict__ Hout) {
+    __shared__ __align__(16) __nv_bfloat16 sWt[C * kWtStride];
+    for (int k = threadIdx.x; k < C * C; k += blockDim.x) {
+        const int kk = k / C, n = k - kk * C;  // W[kk][n] -> Wt[n][kk]
+        sWt[n * kWtStride + kk] = __float2bfloat16_rn(W[k]);
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int g = lane >> 2, t = lane & 3;
+    const int64_t v0 = ((int64_t)blockIdx.x * kMmaWarps + warp) * 16;
+    if (v0 >= nc) return;
+    const int64_t ra = v0 + g, rb = v0 + g + 8;
+    const bool oka = ra < nc, okb = rb < nc;
+    const uint32_t* Ga = reinterpret_cast<const uint32_t*>(G + (oka ? ra : 0) * C);
+    const uint32_t* Gb = reinterpret_cast<const uint32_t*>(G + (okb ? rb : 0) * C);
+    float acc[8][4];
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) {
+        const float b0 = b[nt * 8 + 2 * t], b1 = b[nt * 8 + 2 * t + 1];
+        acc[nt][0] = b0;
+        acc[nt][1] = b1;
+        acc[nt][2] = b0;
+        acc[nt][3] = b1;
+    }
+#pragma unroll
+    for (int ks = 0; ks < C / 16; ++ks) {
+        // A: rows g / g+8, columns ks*16 + 2t (+1) and + 8 (32-bit BF16 pairs)
+        uint32_t a[4];
+        const int c2 = (ks * 16 + 2 * t) >> 1;
+        a[0] = oka ? __ldg(Ga + c2) : 0u;
+        a[1] = okb ? __ldg(Gb + c2) : 0u;
+        a[2] = oka ? __ldg(Ga + c2 + 4) : 0u;
+        a[3] = okb ? __ldg(Gb + c2 + 4) : 0u;
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt) {
+            // B: k = ks*16 + 2t (+1) and + 8, n = nt*8 + g
+            const uint32_t* wt = reinterpret_cast<const uint32_t*>(sWt + (nt * 8 + g) * kWtStride + ks * 16 + 2 * t);
+            const uint32_t bb[2] = {wt[0], wt[4]};
+            mma_bf16_16816(acc[nt], a, bb);
+        }
+    }
+    // epilogue: Z and Hout = Hin + relu(Z), BF16 pairs (columns nt*8 + 2t, +1) of rows g and g+8
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) {
+        const int col = nt * 8 + 2 * t;
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            const int64_t row = half ? rb : ra;
+            if (!(half ? okb : oka)) continue;
+            const float z0 = acc[nt][2 * half], z1 = acc[nt][2 * half + 1];
+            *reinterpret_cast<__nv_bfloat162*>(Z + row * C + col) = __floats2bfloat162_rn(z0, z1);
+            const float2 hf = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(Hin + row * C + col));
+            *reinterpret_cast<__nv_bfloat162*>(Hout + row * C + col) =
+                __floats2bfloat162_rn(hf.x + fmaxf(z0, 0.f), hf.y + fmaxf(z1, 0.f));
+        }
+    }
+}
+
 // a = H W_out + b_out   (K outputs per node)
 template <typename A>
 __global__ void output_kernel(int64_t nc, const A* __restrict__ H, const float* __restrict__ wout,
@@ -805,9 +885,15 @@ int forward_t(anigpu_ctx* h, Gnn* g, const Layout& L) {
         spmm_kernel<A, A><<<wb, kBlk, 0, s>>>(nc, g->crow, g->ccol, g->cval, (const A*)act_ptr(g, 0, l - 1),
                                               (A*)act_ptr(g, 1, l), 0);
         ANI_LAUNCHED(h);
-        dense_kernel<A><<<wb, kBlk, 0, s>>>(nc, (const A*)act_ptr(g, 1, l), g->wk + L.W[l - 1], g->wk + L.b[l - 1],
-                                            (const A*)act_ptr(g, 0, l - 1), (A*)act_ptr(g, 2, l),
-                                            (A*)act_ptr(g, 0, l));
+        if (sizeof(A) == 2)  // BF16 activations: the tensor-core layer
+            dense_mma_bf16_kernel<<<(unsigned)((nc + 16 * kMmaWarps - 1) / (16 * kMmaWarps)), 32 * kMmaWarps, 0, s>>>(
+                nc, (const __nv_bfloat16*)act_ptr(g, 1, l), g->wk + L.W[l - 1], g->wk + L.b[l - 1],
+                (const __nv_bfloat16*)act_ptr(g, 0, l - 1), (__nv_bfloat16*)act_ptr(g, 2, l),
+                (__nv_bfloat16*)act_ptr(g, 0, l));
+        else
+            dense_kernel<A><<<wb, kBlk, 0, s>>>(nc, (const A*)act_ptr(g, 1, l), g->wk + L.W[l - 1],
+                                                g->wk + L.b[l - 1], (const A*)act_ptr(g, 0, l - 1),
+                                                (A*)act_ptr(g, 2, l), (A*)act_ptr(g, 0, l));
         ANI_LAUNCHED(h);
     }
     output_kernel<A><<<wb, kBlk, 0, s>>>(nc, (const A*)act_ptr(g, 0, g->layers), g->wk + L.wout, g->wk + L.bout,
