@@ -113,7 +113,7 @@ def test_ex1_local_assembler_matches_restated_assembler(run, restated):
     t = restated.orient(xyz, tets)
     XYo = np.ascontiguousarray(xyz[t].reshape(-1, 12))
     q2 = restated.quad_points(2, XYo)
-    D = (1 + q2[..., 0] ** 2)[..., None]
+    D = (1 + q2[..., 0] ** 2)[..., None] * np.eye(3).reshape(1, 1, 9)  # s I per point (GRAD . GRAD)
     bnd = (np.any(np.abs(xyz) < 1e-14, axis=1) | np.any(np.abs(xyz - 1) < 1e-14, axis=1)).astype(np.uint8)
     ref = restated.assemble_problem(xyz, tets, 1, POINT, D, 1.0, 2, dirichlet=(bnd, None))
     assert np.array_equal(out["ex1_rowptr"].astype(np.int64), ref["rowptr"])
