@@ -584,7 +584,13 @@ __global__ void __launch_bounds__(kMmaWarps * 32) dense_mma_bf16_kernel(int64_t 
                                                                          const __nv_bfloat16* __restrict__ Hin,
                                                                          __nv_bfloat16* __restrict__ Z,
                                                                          __nv_bfloat16* __restrict__ Hout) {
+    // per warp: its 16 x 64 tile of G (then of Hin) as BF16 and the 16 x 64 FP32 pre-activations,
+    // moved between global and shared memory with coalesced 16-byte accesses
+    constexpr int kAS = C + 8;  // BF16 row stride: 144 bytes, fragment loads on distinct banks
+    constexpr int kZS = C + 4;  // FP32 row stride
     __shared__ __align__(16) __nv_bfloat16 sWt[C * kWtStride];
+    __shared__ __align__(16) __nv_bfloat16 sA[kMmaWarps][16 * kAS];
+    __shared__ __align__(16) float sZf[kMmaWarps][16 * kZS];
     for (int k = threadIdx.x; k < C * C; k += blockDim.x) {
         const int kk = k / C, n = k - kk * C;  // W[kk][n] -> Wt[n][kk]
         sWt[n * kWtStride + kk] = __float2bfloat16_rn(W[k]);
@@ -594,10 +600,20 @@ __global__ void __launch_bounds__(kMmaWarps * 32) dense_mma_bf16_kernel(int64_t 
     const int g = lane >> 2, t = lane & 3;
     const int64_t v0 = ((int64_t)blockIdx.x * kMmaWarps + warp) * 16;
     if (v0 >= nc) return;
-    const int64_t ra = v0 + g, rb = v0 + g + 8;
-    const bool oka = ra < nc, okb = rb < nc;
-    const uint32_t* Ga = reinterpret_cast<const uint32_t*>(G + (oka ? ra : 0) * C);
-    const uint32_t* Gb = reinterpret_cast<const uint32_t*>(G + (okb ? rb : 0) * C);
+    __nv_bfloat16* A = sA[warp];
+    float* Zf = sZf[warp];
+    // 16 rows x 8 vectors of 8 BF16: lane handles vectors lane + 32 j
+    auto load_tile = [&](const __nv_bfloat16* src) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int idx = lane + 32 * j, r = idx >> 3, c8 = (idx & 7) * 8;
+            const int64_t v = v0 + r;
+            const uint4 val = v < nc ? __ldg(reinterpret_cast<const uint4*>(src + v * C + c8)) : make_uint4(0, 0, 0, 0);
+            *reinterpret_cast<uint4*>(A + r * kAS + c8) = val;
+        }
+        __syncwarp();
+    };
+    load_tile(G);
     float acc[8][4];
 #pragma unroll
     for (int nt = 0; nt < 8; ++nt) {
@@ -610,12 +626,9 @@ __global__ void __launch_bounds__(kMmaWarps * 32) dense_mma_bf16_kernel(int64_t 
 #pragma unroll
     for (int ks = 0; ks < C / 16; ++ks) {
         // A: rows g / g+8, columns ks*16 + 2t (+1) and + 8 (32-bit BF16 pairs)
-        uint32_t a[4];
-        const int c2 = (ks * 16 + 2 * t) >> 1;
-        a[0] = oka ? __ldg(Ga + c2) : 0u;
-        a[1] = okb ? __ldg(Gb + c2) : 0u;
-        a[2] = oka ? __ldg(Ga + c2 + 4) : 0u;
-        a[3] = okb ? __ldg(Gb + c2 + 4) : 0u;
+        const uint32_t* a0p = reinterpret_cast<const uint32_t*>(A + g * kAS + ks * 16 + 2 * t);
+        const uint32_t* a1p = reinterpret_cast<const uint32_t*>(A + (g + 8) * kAS + ks * 16 + 2 * t);
+        const uint32_t a[4] = {a0p[0], a1p[0], a0p[4], a1p[4]};
 #pragma unroll
         for (int nt = 0; nt < 8; ++nt) {
             // B: k = ks*16 + 2t (+1) and + 8, n = nt*8 + g
@@ -624,20 +637,33 @@ __global__ void __launch_bounds__(kMmaWarps * 32) dense_mma_bf16_kernel(int64_t 
             mma_bf16_16816(acc[nt], a, bb);
         }
     }
-    // epilogue: Z and Hout = Hin + relu(Z), BF16 pairs (columns nt*8 + 2t, +1) of rows g and g+8
+    // pre-activations to shared memory (FP32), then Hin over the G tile
 #pragma unroll
     for (int nt = 0; nt < 8; ++nt) {
         const int col = nt * 8 + 2 * t;
+        *reinterpret_cast<float2*>(Zf + g * kZS + col) = make_float2(acc[nt][0], acc[nt][1]);
+        *reinterpret_cast<float2*>(Zf + (g + 8) * kZS + col) = make_float2(acc[nt][2], acc[nt][3]);
+    }
+    __syncwarp();
+    load_tile(Hin);
+    // epilogue, coalesced: Z = bf16(z), Hout = bf16(Hin + relu(z)), 8 channels per vector
 #pragma unroll
-        for (int half = 0; half < 2; ++half) {
-            const int64_t row = half ? rb : ra;
-            if (!(half ? okb : oka)) continue;
-            const float z0 = acc[nt][2 * half], z1 = acc[nt][2 * half + 1];
-            *reinterpret_cast<__nv_bfloat162*>(Z + row * C + col) = __floats2bfloat162_rn(z0, z1);
-            const float2 hf = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(Hin + row * C + col));
-            *reinterpret_cast<__nv_bfloat162*>(Hout + row * C + col) =
-                __floats2bfloat162_rn(hf.x + fmaxf(z0, 0.f), hf.y + fmaxf(z1, 0.f));
+    for (int j = 0; j < 4; ++j) {
+        const int idx = lane + 32 * j, r = idx >> 3, c8 = (idx & 7) * 8;
+        const int64_t v = v0 + r;
+        if (v >= nc) continue;
+        const float* z = Zf + r * kZS + c8;
+        const __nv_bfloat162* hi = reinterpret_cast<const __nv_bfloat162*>(A + r * kAS + c8);
+        __align__(16) __nv_bfloat162 zo[4], ho[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const float z0 = z[2 * q], z1 = z[2 * q + 1];
+            const float2 hf = __bfloat1622float2(hi[q]);
+            zo[q] = __floats2bfloat162_rn(z0, z1);
+            ho[q] = __floats2bfloat162_rn(hf.x + fmaxf(z0, 0.f), hf.y + fmaxf(z1, 0.f));
         }
+        *reinterpret_cast<uint4*>(Z + v * C + c8) = *reinterpret_cast<const uint4*>(zo);
+        *reinterpret_cast<uint4*>(Hout + v * C + c8) = *reinterpret_cast<const uint4*>(ho);
     }
 }
 
@@ -768,6 +794,117 @@ __global__ void __launch_bounds__(kBlk) dense_bwd_kernel(int64_t nc, const float
     for (int a = 0; a < 4; ++a)
 #pragma unroll
         for (int q = 0; q < 4; ++q) wp[(tr + a) * C + tc + q] = acc[a][q];
+    if (threadIdx.x < C) bpart[(int64_t)blockIdx.x * C + threadIdx.x] = bacc;
+}
+
+// The same backward step on the tensor cores for BF16 activations (TF32 inputs, FP32 accumulation,
+// mma.sync m16n8k8): 32 nodes per chunk, staged in shared memory as FP32 (dZ, G); 4 warps.
+//   dG = dZ W^T : warp w computes nodes (w & 1)*16 .. +16 x output columns (w >> 1)*32 .. +32
+//   dW += G^T dZ: warp w owns the 16 rows w*16 .. +16 of dW (all 64 columns), K = the chunk's nodes
+// Row strides 68 (W) and 72 (dZ, G) keep the fragment loads on distinct banks (dZ's A-loads of dG
+// meet at most two-way conflicts).
+constexpr int kTcWarps = 4, kTcChunk = 32, kSW = C + 4, kSZ = C + 8;
+
+__device__ __forceinline__ uint32_t to_tf32(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ void mma_tf32_1688(float* d, const uint32_t* a, const uint32_t* b) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+__global__ void __launch_bounds__(kTcWarps * 32) dense_bwd_tc_kernel(int64_t nc, const float* __restrict__ dH,
+                                                                      const __nv_bfloat16* __restrict__ Z,
+                                                                      const __nv_bfloat16* __restrict__ G,
+                                                                      const float* __restrict__ W,
+                                                                      float* __restrict__ dZout, float* __restrict__ dG,
+                                                                      float* __restrict__ wpart,
+                                                                      float* __restrict__ bpart, int rows_per_block) {
+    __shared__ float sW[C * kSW];
+    __shared__ float sZ[kTcChunk * kSZ];
+    __shared__ float sG[kTcChunk * kSZ];
+    for (int k = threadIdx.x; k < C * C; k += blockDim.x) sW[(k / C) * kSW + (k % C)] = W[k];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int g = lane >> 2, t = lane & 3;
+    float accW[8][4];
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) accW[nt][q] = 0.f;
+    float bacc = 0.f;
+    const int64_t v0 = (int64_t)blockIdx.x * rows_per_block;
+    const int64_t vend = (v0 + rows_per_block < nc) ? v0 + rows_per_block : nc;
+    for (int64_t base = v0; base < vend; base += kTcChunk) {
+        __syncthreads();  // sW staged / the previous chunk's readers done
+        for (int e = threadIdx.x; e < kTcChunk * C; e += blockDim.x) {
+            const int r = e / C, c = e - r * C;
+            const int64_t v = base + r;
+            float z = 0.f, gg = 0.f;
+            if (v < vend) {
+                z = __bfloat162float(Z[v * C + c]) > 0.f ? dH[v * C + c] : 0.f;
+                gg = __bfloat162float(G[v * C + c]);
+                dZout[v * C + c] = z;
+            }
+            sZ[r * kSZ + c] = z;
+            sG[r * kSZ + c] = gg;
+        }
+        __syncthreads();
+        // dG = dZ W^T for this warp's 16 nodes x 32 columns
+        {
+            const int mt = w & 1, nh = w >> 1;
+            float acc[4][4];
+#pragma unroll
+            for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) acc[nt][q] = 0.f;
+            const float* zr0 = sZ + (mt * 16 + g) * kSZ;
+            const float* zr1 = zr0 + 8 * kSZ;
+#pragma unroll
+            for (int ks = 0; ks < C / 8; ++ks) {
+                const uint32_t a[4] = {to_tf32(zr0[ks * 8 + t]), to_tf32(zr1[ks * 8 + t]), to_tf32(zr0[ks * 8 + t + 4]),
+                                       to_tf32(zr1[ks * 8 + t + 4])};
+#pragma unroll
+                for (int nt = 0; nt < 4; ++nt) {
+                    const float* wr = sW + (nh * 32 + nt * 8 + g) * kSW + ks * 8 + t;  // W[j][n], n = k index
+                    const uint32_t b[2] = {to_tf32(wr[0]), to_tf32(wr[4])};
+                    mma_tf32_1688(acc[nt], a, b);
+                }
+            }
+#pragma unroll
+            for (int nt = 0; nt < 4; ++nt) {
+                const int col = nh * 32 + nt * 8 + 2 * t;
+                const int64_t ra = base + mt * 16 + g, rb = ra + 8;
+                if (ra < vend) *reinterpret_cast<float2*>(dG + ra * C + col) = make_float2(acc[nt][0], acc[nt][1]);
+                if (rb < vend) *reinterpret_cast<float2*>(dG + rb * C + col) = make_float2(acc[nt][2], acc[nt][3]);
+            }
+        }
+        // dW += G^T dZ: rows w*16 .. +16 of dW, K = the chunk's 32 nodes
+#pragma unroll
+        for (int ks = 0; ks < kTcChunk / 8; ++ks) {
+            const float* g0 = sG + (ks * 8 + t) * kSZ + w * 16 + g;
+            const float* g1 = sG + (ks * 8 + t + 4) * kSZ + w * 16 + g;
+            const uint32_t a[4] = {to_tf32(g0[0]), to_tf32(g0[8]), to_tf32(g1[0]), to_tf32(g1[8])};
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt) {
+                const uint32_t b[2] = {to_tf32(sZ[(ks * 8 + t) * kSZ + nt * 8 + g]),
+                                       to_tf32(sZ[(ks * 8 + t + 4) * kSZ + nt * 8 + g])};
+                mma_tf32_1688(accW[nt], a, b);
+            }
+        }
+        if (threadIdx.x < C)
+            for (int r = 0; r < kTcChunk; ++r) bacc += sZ[r * kSZ + threadIdx.x];
+    }
+    float* wp = wpart + (int64_t)blockIdx.x * C * C;
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) {
+        const int col = nt * 8 + 2 * t, row = w * 16 + g;
+        *reinterpret_cast<float2*>(wp + row * C + col) = make_float2(accW[nt][0], accW[nt][1]);
+        *reinterpret_cast<float2*>(wp + (row + 8) * C + col) = make_float2(accW[nt][2], accW[nt][3]);
+    }
     if (threadIdx.x < C) bpart[(int64_t)blockIdx.x * C + threadIdx.x] = bacc;
 }
 
@@ -917,8 +1054,13 @@ int backward_t(anigpu_ctx* h, Gnn* g, const Layout& L) {
     const int64_t rpb = std::max<int64_t>(32, ((nc + kMaxPart - 1) / kMaxPart + 31) / 32 * 32);
     const int nbw = (int)((nc + rpb - 1) / rpb);
     for (int l = g->layers; l >= 1; --l) {
-        dense_bwd_kernel<A><<<nbw, kBlk, 0, s>>>(nc, g->dH, (const A*)act_ptr(g, 2, l), (const A*)act_ptr(g, 1, l),
-                                                 g->wk + L.W[l - 1], g->dZ, g->dG, g->wpart, g->part, (int)rpb);
+        if (sizeof(A) == 2)  // BF16 activations: the tensor-core step
+            dense_bwd_tc_kernel<<<nbw, kTcWarps * 32, 0, s>>>(nc, g->dH, (const __nv_bfloat16*)act_ptr(g, 2, l),
+                                                              (const __nv_bfloat16*)act_ptr(g, 1, l), g->wk + L.W[l - 1],
+                                                              g->dZ, g->dG, g->wpart, g->part, (int)rpb);
+        else
+            dense_bwd_kernel<A><<<nbw, kBlk, 0, s>>>(nc, g->dH, (const A*)act_ptr(g, 2, l), (const A*)act_ptr(g, 1, l),
+                                                     g->wk + L.W[l - 1], g->dZ, g->dG, g->wpart, g->part, (int)rpb);
         ANI_LAUNCHED(h);
         reduce_parts_kernel<<<nblk(C * C, 256), 256, 0, s>>>(C * C, nbw, (int64_t)C * C, g->wpart, g->g + L.W[l - 1]);
         ANI_LAUNCHED(h);
