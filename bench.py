@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=0, help="tets in the CPU-baseline sample (0 = auto)")
     ap.add_argument("--no-parity", action="store_true", help="skip the full-size oracle check after the timed steps")
     ap.add_argument("--no-config1", action="store_true", help="skip the P1 Poisson (config 1) line")
+    ap.add_argument("--record-gather", action="store_true",
+                    help="gather the P2 edge rows from the scatter records instead of the rings")
     return ap.parse_args()
 
 
@@ -639,6 +641,10 @@ def run_ours(args):
     rhs = torch.empty(ndof, dtype=torch.float64, device=dev)
     stream = lib.stream
 
+    if args.record_gather:
+        lib.set_gather_layouts(False)
+    edge_rows = "rings" if all(lib.gather_layouts()) else "records"
+
     def step(sync):
         lib.assemble(anigpu.TENSOR_TET_SYM, D_dev, None, 1.0, 4, anigpu.F32, vals32, rhs, sync=sync)
 
@@ -900,8 +906,9 @@ def run_ours(args):
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                      "traffic": traffic, "peak_kind": peak_kind,
-                     "kernel": "assembly = tet_gram + row_gather (vertex rows, edge rows): 3 launches, "
+                     "kernel": "assembly = tet_gram + row_gather (vertex rows) + edge-row gather: 3 launches, "
                                "timed back to back in the timed region",
+                     "edge_rows": edge_rows,
                      "algorithmic_bytes": b_alg, "ms": {"tet_prepare": prep_ms, "row_gather": rows_ms},
                      # the reference formulation's arithmetic, for context: q*nf*dim^2 MACs for D.U plus
                      # nf^2*q*dim for V^T.DU (P2, 14 points), 2 FLOPs per MAC

@@ -230,6 +230,16 @@ int anigpu_mesh_update_coords(anigpu_handle h, const double* xyz);
  * forced) and the row-gather scatter records.  All on the device. */
 int anigpu_problem_setup(anigpu_handle h, int space);
 int anigpu_problem_info(anigpu_handle h, int64_t* ndof, int64_t* nnz, int64_t* nedges);
+/* Row layouts of the Gram-form gathers, built by anigpu_problem_setup: P2 edge rows in ring order
+ * (the tets around each edge walked face to face, so each value is written once) and vertex rows
+ * from lane-interleaved scatter records (one contiguous load per warp and step).
+ * *rings = 1 when every edge of the mesh has a ring; *enabled = whether assemblies use these
+ * layouts (default 1).  Calls that need a touched map or non-zero Dirichlet values, meshes without
+ * rings (edge rows) and the table form use the record gather.  Both sum the same element
+ * contributions (AssemblerT::Assemble, assembler.inl:314-487) in fixed, different orders: results
+ * agree to rounding. */
+int anigpu_gather_layouts(anigpu_handle h, int* rings, int* enabled);
+int anigpu_set_gather_layouts(anigpu_handle h, int enable);
 /* copy the template out: rowptr[ndof+1] (i64), col[nnz] (i32) -- device pointers */
 int anigpu_csr_template(anigpu_handle h, int64_t* rowptr, int32_t* col);
 /* element DOF table edofs[nt*nloc] (i32, device) */

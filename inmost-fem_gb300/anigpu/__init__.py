@@ -71,6 +71,8 @@ SIGNATURES = {
     "anigpu_mesh_update_coords": (_i, [_vp, _vp]),
     "anigpu_problem_setup": (_i, [_vp, _i]),
     "anigpu_problem_info": (_i, [_vp, ctypes.POINTER(_i64), ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
+    "anigpu_gather_layouts": (_i, [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i)]),
+    "anigpu_set_gather_layouts": (_i, [_vp, _i]),
     "anigpu_csr_template": (_i, [_vp, _vp, _vp]),
     "anigpu_element_dofs": (_i, [_vp, _vp]),
     "anigpu_element_coords": (_i, [_vp, _vp]),
@@ -449,6 +451,15 @@ class Anigpu:
         self._check(self.lib.anigpu_problem_info(self.h, ctypes.byref(nd), ctypes.byref(nz), ctypes.byref(ne)))
         self.ndof, self.nnz, self.nedges = nd.value, nz.value, ne.value
         return self.ndof, self.nnz
+
+    def gather_layouts(self):
+        """(rings, enabled): every P2 edge has a ring; the ring / interleaved gathers are used."""
+        a, e = ctypes.c_int(), ctypes.c_int()
+        self._check(self.lib.anigpu_gather_layouts(self.h, ctypes.byref(a), ctypes.byref(e)))
+        return bool(a.value), bool(e.value)
+
+    def set_gather_layouts(self, enable):
+        self._check(self.lib.anigpu_set_gather_layouts(self.h, 1 if enable else 0))
 
     @_streamed
     def csr_template(self):

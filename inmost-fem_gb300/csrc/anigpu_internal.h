@@ -93,6 +93,15 @@ struct anigpu_ctx {
     int32_t* col = nullptr;        // nnz   (== col_s for scalar spaces)
     int64_t* inc_ptr = nullptr;    // nds+1
     ScatterRec* recs = nullptr;    // nt*nloc_s
+    // P2 edge rows in ring order (the tets around each edge, consecutive tets sharing a face):
+    // per warp of 32 edge rows a header slot, then one 8-byte record per incident tet, lane-interleaved
+    uint2* ring = nullptr;
+    int64_t* ring_woff = nullptr;  // first slot of each warp (nwarps + 1)
+    bool ring_ok = false;          // every edge row of the mesh has a ring (else the record gather)
+    bool ring_enabled = true;      // anigpu_set_gather_layouts: rings and interleaved vertex records
+    // vertex rows' scatter records in the same lane-interleaved layout (no header)
+    ScatterRec* vrec = nullptr;
+    int64_t* vrec_woff = nullptr;
     int max_row_len_s = 0;
     int64_t row_range[3] = {0, 0, 0};  // scalar rows [vertex DOFs | edge DOFs]
     int row_range_cap[2] = {0, 0};     // longest row of each range
@@ -208,6 +217,7 @@ int launch_apply_dir(anigpu_ctx* h, int64_t nt, int n, double* A, double* F, con
 int setup_orient(anigpu_ctx* h);
 int setup_problem(anigpu_ctx* h, int space);
 int setup_dirichlet_bits(anigpu_ctx* h);
+int setup_row_layouts(anigpu_ctx* h);
 int setup_dof_coords(anigpu_ctx* h, double* out);
 // refresh the (hi, lo) float copy of the coordinates after an upload or update
 int setup_coords_split(anigpu_ctx* h);

@@ -69,7 +69,7 @@ int anigpu_destroy(anigpu_handle h) {
     free_enum(h);
     free_general(h);
     void* ptrs[] = {h->xyz, h->xyz2, h->tets, h->tet_edges, h->edofs, h->inc_ptr, h->recs, h->dir_mask, h->dir_bc,
-                    h->dir_cptr, h->dir_coff,
+                    h->dir_cptr, h->dir_coff, h->ring, h->ring_woff, h->vrec, h->vrec_woff,
                     h->tetdata, h->d_status, h->d_ref_tables};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -301,6 +301,19 @@ int anigpu_problem_info(anigpu_handle h, int64_t* ndof, int64_t* nnz, int64_t* n
     if (ndof) *ndof = h->ndof;
     if (nnz) *nnz = h->nnz;
     if (nedges) *nedges = h->ne;
+    return ANIGPU_OK;
+}
+
+int anigpu_gather_layouts(anigpu_handle h, int* rings, int* enabled) {
+    CHECK_H(h);
+    if (rings) *rings = h->ring_ok ? 1 : 0;
+    if (enabled) *enabled = h->ring_enabled ? 1 : 0;
+    return ANIGPU_OK;
+}
+
+int anigpu_set_gather_layouts(anigpu_handle h, int enable) {
+    CHECK_H(h);
+    h->ring_enabled = enable != 0;
     return ANIGPU_OK;
 }
 

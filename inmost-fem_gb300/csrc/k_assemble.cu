@@ -259,7 +259,13 @@ __global__ void tet_gram_f64_kernel(int64_t nt, const double* __restrict__ xyz, 
     for (int q = 0; q < 4; ++q) o[q] = make_double2(G[2 * q], G[2 * q + 1]);
 }
 
-__global__ void tet_gram_f32_kernel(int64_t nt, const double* __restrict__ xyz, const float2* __restrict__ xyz2,
+// six 256-thread blocks per SM (40 registers): the loads of more tets in flight; the few values
+// this moves to local memory belong to the FP64 redo of badly shaped tets
+#ifndef TET_GRAM_MINB
+#define TET_GRAM_MINB 6
+#endif
+#define TET_GRAM_BOUNDS __launch_bounds__(256, TET_GRAM_MINB)
+__global__ void TET_GRAM_BOUNDS tet_gram_f32_kernel(int64_t nt, const double* __restrict__ xyz, const float2* __restrict__ xyz2,
                                     const int32_t* __restrict__ tets, int kind, const double* __restrict__ D,
                                     const double* __restrict__ f, double f_const, float* __restrict__ out,
                                     int* __restrict__ status) {
@@ -515,6 +521,47 @@ __device__ __forceinline__ void load_rec_pair(const ScatterRec* p, ScatterRec& l
 // byte c & 3 of w, zero-extended
 __device__ __forceinline__ uint32_t byte_of(uint32_t w, int c) { return __byte_perm(w, 0u, 0x4440u + (uint32_t)(c & 3)); }
 
+// contiguous write-out of a warp's value range (shared index k <-> vals[cbase + k], same 16-byte
+// alignment): single values up to the first aligned vector, vectors over the middle, single values
+// at the end.  Returns a sum of value * 0 over the values written: non-finite iff one of them is.
+template <typename Real>
+__device__ __forceinline__ Real write_out_range(const Real* sC, int shift, int clen, int64_t cbase,
+                                                Real* __restrict__ vals, int vec_ok, int lane) {
+    constexpr int VEC = 16 / (int)sizeof(Real);
+    Real fin = Real(0);
+    const int head = shift == 0 ? 0 : (VEC - shift < clen ? VEC - shift : clen);
+    if (lane < head) {
+        const Real v = sC[lane];
+        fin = fma(v, Real(0), fin);
+        vals[cbase + lane] = v;
+    }
+    const int nbody = (clen - head) / VEC;
+    using V = typename std::conditional<sizeof(Real) == 4, float4, double2>::type;
+    const V* sv = reinterpret_cast<const V*>(sC + head);
+    V* gv = reinterpret_cast<V*>(vals + cbase + head);
+    for (int k = lane; k < (vec_ok ? nbody : 0); k += 32) {
+        const V v = sv[k];
+        if (sizeof(Real) == 4) {
+            const float4 f = *reinterpret_cast<const float4*>(&v);
+            fin = fma(Real(f.x), Real(0), fin);
+            fin = fma(Real(f.y), Real(0), fin);
+            fin = fma(Real(f.z), Real(0), fin);
+            fin = fma(Real(f.w), Real(0), fin);
+        } else {
+            const double2 f = *reinterpret_cast<const double2*>(&v);
+            fin = fma(Real(f.x), Real(0), fin);
+            fin = fma(Real(f.y), Real(0), fin);
+        }
+        gv[k] = v;
+    }
+    for (int k = (vec_ok ? head + nbody * VEC : head) + lane; k < clen; k += 32) {
+        const Real v = sC[k];
+        fin = fma(v, Real(0), fin);
+        vals[cbase + k] = v;
+    }
+    return fin;
+}
+
 // FORM 0: table form (any row kind); FORM 1: Gram form, vertex rows; FORM 2: Gram form, P2 edge rows
 template <typename Real, int NLOC, int FORM, bool DIR, bool BCNZ, bool TOUCH, bool DROPCHK>
 __global__ void ROW_BOUNDS row_gather_kernel(RowParams p, const Real* __restrict__ tables,
@@ -708,42 +755,490 @@ __global__ void ROW_BOUNDS row_gather_kernel(RowParams p, const Real* __restrict
         rhs[row] = F;
     }
     __syncwarp();
-    // contiguous write-out of the warp's value range: vectors over the aligned middle
-    Real fin = Real(0);
-    const int head = shift == 0 ? 0 : (VEC - shift < clen ? VEC - shift : clen);
-    if (lane < head) {
-        const Real v = sC[lane];
-        fin = fma(v, Real(0), fin);
-        vals[cbase + lane] = v;
-    }
-    const int nbody = (clen - head) / VEC;
-    using V = typename std::conditional<sizeof(Real) == 4, float4, double2>::type;
-    const V* sv = reinterpret_cast<const V*>(sC + head);
-    V* gv = reinterpret_cast<V*>(vals + cbase + head);
-    for (int k = lane; k < (p.vec_ok ? nbody : 0); k += 32) {
-        const V v = sv[k];
-        if (sizeof(Real) == 4) {
-            const float4 f = *reinterpret_cast<const float4*>(&v);
-            fin = fma(Real(f.x), Real(0), fin);
-            fin = fma(Real(f.y), Real(0), fin);
-            fin = fma(Real(f.z), Real(0), fin);
-            fin = fma(Real(f.w), Real(0), fin);
-        } else {
-            const double2 f = *reinterpret_cast<const double2*>(&v);
-            fin = fma(Real(f.x), Real(0), fin);
-            fin = fma(Real(f.y), Real(0), fin);
-        }
-        gv[k] = v;
-    }
-    for (int k = (p.vec_ok ? head + nbody * VEC : head) + lane; k < clen; k += 32) {
-        const Real v = sC[k];
-        fin = fma(v, Real(0), fin);
-        vals[cbase + k] = v;
-    }
+    Real fin = write_out_range<Real>(sC, shift, clen, cbase, vals, p.vec_ok, lane);
     if (TOUCH)
         for (int k = lane; k < clen; k += 32) touched_out[cbase + k] = sTouch[k];
     bad |= !isfinite(fin);
     if (bad) atomicExch(status, ANIGPU_ERR_NONFINITE);
+}
+
+// ---------------------------------------------------------------- P2 edge rows by rings
+// The tets around an edge (A, B) form a ring (a path for a boundary edge): consecutive tets
+// share a face (A, B, v).  Of the columns of the edge row, A, B and the edge itself collect every
+// tet of the ring; the ring vertex v and the edges (A, v), (B, v) collect the two tets on the face
+// (A, B, v) (one at the end of a path); the edge (P, N) opposite to (A, B) in a tet collects that
+// tet alone.  Walking the ring in order, a lane keeps A, B and the edge in registers and carries
+// the three columns of the face it is on from one tet to the next, so every value of the row is
+// written to shared memory exactly once, with no read-modify-write and no zeroing pass over the
+// columns the walk covers.  Each value is still the sum of its tets' contributions in a fixed
+// order (the ring order from the smallest tet id).
+//
+// Ring record (8 bytes), one per (edge row, incident tet), in ring order:
+//   x: tet id (bits 0-26), local edge k of (A, B) in the tet (27-29), A is the tet's local b (30),
+//      P is the tet's local d (31)  [local a < b: the edge's vertices, c < d: the other two]
+//   y: offsets within the row of N, (A, N), (B, N), (P, N), 8 bits each
+// Header (one per row, before its records):
+//   x: offsets of A, B, the edge (8 bits each), bit 24: closed ring
+//   y: offsets of the first face's vertex P0, (A, P0), (B, P0)
+// For warp w of the edge range the slots are ring[woff[w] + 32 s + lane]: the header at s = 0,
+// record j at s = j + 1, so the 32 lanes read 256 contiguous bytes per step.
+constexpr uint32_t kRingTetMask = (1u << 27) - 1;
+constexpr int kRingMax = 32;  // incident tets of an edge that the ring build takes
+
+// prefetch depths of the ring gather (per-tet blocks, records) and its unroll, a multiple of both
+#ifndef RING_KD
+#define RING_KD 2
+#endif
+#ifndef RING_RD
+#define RING_RD 4
+#endif
+#ifndef RING_UNROLL
+#define RING_UNROLL 4
+#endif
+constexpr int kRingUnroll = RING_UNROLL;
+
+template <typename Real, bool DIR, bool DROPCHK>
+__global__ void ROW_BOUNDS edge_ring_kernel(RowParams p, const uint2* __restrict__ ring,
+                                            const int64_t* __restrict__ woff, const Real* __restrict__ tetK,
+                                            Real* __restrict__ vals, double* __restrict__ rhs,
+                                            int* __restrict__ status) {
+    using Sm = RowSmem<Real, 10, 2, false>;
+    constexpr int KS = 8;
+    constexpr int VEC = Sm::VEC;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarps = blockDim.x >> 5;
+    const int64_t wg = (int64_t)blockIdx.x * nwarps + warp;
+    const int64_t row0 = p.row_begin + wg * 32;
+    if (row0 >= p.nrows) return;  // warp-uniform; no block-wide barrier follows
+    const int64_t rend = row0 + 32 < p.nrows ? row0 + 32 : p.nrows;
+    const int64_t cbase = p.rowptr[row0];
+    const int clen = (int)(p.rowptr[rend] - cbase);
+    const int shift = (int)(cbase & (VEC - 1));
+    unsigned char* wbase = smem_raw + Sm::warp_bytes(p.cap) * warp;
+    Real* sC = reinterpret_cast<Real*>(wbase) + shift;
+    {
+        const int nvec = (shift + clen + VEC - 1) / VEC;
+        int4* z = reinterpret_cast<int4*>(wbase);
+        for (int k = lane; k < nvec; k += 32) z[k] = make_int4(0, 0, 0, 0);
+    }
+    const int64_t row = row0 + lane;
+    const bool valid = row < p.nrows;
+    const uint2* rr = ring + woff[wg] + lane;
+    int deg = 0, base = 0;
+    bool isdir = false;
+    uint2 hd = make_uint2(0u, 0u);
+    if (valid) {
+        deg = (int)(p.inc_ptr[row + 1] - p.inc_ptr[row]);
+        base = (int)(p.rowptr[row] - cbase);
+        if (DIR) isdir = p.dir_mask[row] != 0;
+        hd = rr[0];
+    }
+    __syncwarp();
+    Real* myRow = sC + base;
+    const Real drop = Real(p.drop);
+    const int nloop = isdir ? 0 : deg;
+    const int last = nloop - 1;
+    constexpr int KD = RING_KD, RD = RING_RD;
+    static_assert(RD > KD, "records must run ahead of the blocks they address");
+    KVec<Real, KS> Kq[KD];
+    uint2 Rq[RD];
+#pragma unroll
+    for (int j = 0; j < KD; ++j) Kq[j].zero();
+#pragma unroll
+    for (int j = 0; j < RD; ++j) Rq[j] = make_uint2(0u, 0u);
+#pragma unroll
+    for (int j = 0; j < RD; ++j)
+        if (j <= last) Rq[j] = rr[32 * (j + 1)];
+#pragma unroll
+    for (int j = 0; j < KD; ++j)
+        if (j <= last) Kq[j].load(tetK + KS * (int64_t)(Rq[j].x & kRingTetMask));
+    const bool closed = (hd.x >> 24) & 1u;
+    Real cP = Real(0), cAP = Real(0), cBP = Real(0);  // the face carried to the next tet
+    Real fP = Real(0), fAP = Real(0), fBP = Real(0);  // the first face of a closed ring
+    uint32_t coff = hd.y;                             // offsets of the carried face's columns
+    Real accA = Real(0), accB = Real(0), accE = Real(0), racc = Real(0);
+#pragma unroll kRingUnroll
+    for (int k = 0; k < nloop; ++k) {
+        KVec<Real, KS> Kn;
+        if (k + KD <= last) Kn.load(tetK + KS * (int64_t)(Rq[KD].x & kRingTetMask));
+        uint2 Rn = make_uint2(0u, 0u);
+        if (k + RD <= last) Rn = rr[32 * (k + RD + 1)];
+        const uint2 r0 = Rq[0];
+        // the Gram entries of the edge (A, B) and of its four neighbours in the tet, in ring roles:
+        // local edge k = (a, b) with the other vertices c < d, then A = b if bit 30, P = d if bit 31
+        const Real* G = Kq[0].v;
+        const int le = (int)((r0.x >> 27) & 7u);
+        const Real gab = le == 0 ? G[0] : le == 1 ? G[1] : le == 2 ? G[2] : le == 3 ? G[3] : le == 4 ? G[4] : G[5];
+        const Real gac = (le == 0 || le == 5) ? G[1] : G[0];
+        const Real gad = le <= 1 ? G[2] : le == 2 ? G[1] : le == 3 ? G[4] : G[3];
+        const Real gbc = le <= 1 ? G[3] : le == 2 ? G[4] : le == 3 ? G[1] : G[2];
+        const Real gbd = (le == 0 || le == 5) ? G[4] : G[5];
+        const bool sab = (r0.x >> 30) & 1u, scd = (r0.x >> 31) & 1u;
+        const Real x1 = scd ? gad : gac, x2 = scd ? gac : gad;  // a with P, a with N
+        const Real y1 = scd ? gbd : gbc, y2 = scd ? gbc : gbd;  // b with P, b with N
+        const Real gAP = sab ? y1 : x1, gAN = sab ? y2 : x2;
+        const Real gBP = sab ? x1 : y1, gBN = sab ? x2 : y2;
+        // the element row of the edge (the Gram form of fem3Dtet's P2 GRAD.GRAD row, with
+        // G_AA = -(G_AB + G_AP + G_AN) and G_BB likewise eliminated)
+        const Real sA = gAP + gAN, sB = gBP + gBN;
+        const Real c2 = Real(0.2), c8 = Real(0.8), c16 = Real(1.6);
+        Real vA = fma(c2, sA, c8 * gab), vB = fma(c2, sB, c8 * gab);
+        Real vE = -c16 * ((gab + sA) + sB);
+        Real vP = -c2 * (gAP + gBP), vN = -c2 * (gAN + gBN);
+        Real vAP = fma(c16, gBP, -c8 * gAN), vAN = fma(c16, gBN, -c8 * gAP);
+        Real vBP = fma(c16, gAP, -c8 * gBN), vBN = fma(c16, gAN, -c8 * gBP);
+        Real vPN = c8 * (sA + sB);
+        const Real F = c2 * G[6];
+        if (DROPCHK) {
+            auto keep = [&](Real v) { return fabs(v) > drop ? v : Real(0); };
+            vA = keep(vA); vB = keep(vB); vE = keep(vE); vP = keep(vP); vN = keep(vN);
+            vAP = keep(vAP); vAN = keep(vAN); vBP = keep(vBP); vBN = keep(vBN); vPN = keep(vPN);
+        }
+        accA += vA;
+        accB += vB;
+        accE += vE;
+        racc += F;
+        // face P: the carried tet's part plus this tet's; final except the first face of a closed ring
+        const Real oP = cP + vP, oAP = cAP + vAP, oBP = cBP + vBP;
+        if (k == 0 && closed) {
+            fP = oP;
+            fAP = oAP;
+            fBP = oBP;
+        } else {
+            myRow[coff & 255u] = oP;
+            myRow[(coff >> 8) & 255u] = oAP;
+            myRow[(coff >> 16) & 255u] = oBP;
+        }
+        myRow[r0.y >> 24] = vPN;
+        cP = vN;
+        cAP = vAN;
+        cBP = vBN;
+        coff = r0.y;
+#pragma unroll
+        for (int j = 0; j + 1 < KD; ++j) Kq[j] = Kq[j + 1];
+        Kq[KD - 1] = Kn;
+#pragma unroll
+        for (int j = 0; j + 1 < RD; ++j) Rq[j] = Rq[j + 1];
+        Rq[RD - 1] = Rn;
+    }
+    bool bad = false;
+    if (valid) {
+        double F;
+        if (DIR && isdir) {
+            if (deg > 0) myRow[(hd.x >> 16) & 255u] = Real(deg);
+            const double bcr = p.dir_bc[row];
+            F = 0;
+            for (int q = 0; q < deg; ++q) F += bcr;
+        } else {
+            if (nloop > 0) {
+                // the last face: a closed ring ends on its first face
+                myRow[coff & 255u] = cP + fP;
+                myRow[(coff >> 8) & 255u] = cAP + fAP;
+                myRow[(coff >> 16) & 255u] = cBP + fBP;
+                myRow[hd.x & 255u] = accA;
+                myRow[(hd.x >> 8) & 255u] = accB;
+                myRow[(hd.x >> 16) & 255u] = accE;
+            }
+            F = (double)racc;
+            if (DIR)
+                for (int64_t q = p.dir_cptr[row]; q < p.dir_cptr[row + 1]; ++q) myRow[p.dir_coff[q]] = Real(0);
+        }
+        bad |= !isfinite(F);
+        rhs[row] = F;
+    }
+    __syncwarp();
+    const Real fin = write_out_range<Real>(sC, shift, clen, cbase, vals, p.vec_ok, lane);
+    bad |= !isfinite(fin);
+    if (bad) atomicExch(status, ANIGPU_ERR_NONFINITE);
+}
+
+// Vertex rows (Gram form) from lane-interleaved records: record j of lane l of warp w at
+// vrec[woff[w] + 32 j + l], so a warp reads one contiguous 512-byte range per step instead of 32
+// scattered records.  The diagonal (every incident tet) is summed in a register and written once;
+// the other columns of an element row are added into the shared-memory row as in row_gather_kernel.
+template <typename Real, int NLOC, bool DIR, bool DROPCHK>
+__global__ void ROW_BOUNDS vertex_ilv_kernel(RowParams p, const ScatterRec* __restrict__ vrec,
+                                             const int64_t* __restrict__ woff, const Real* __restrict__ tetK,
+                                             Real* __restrict__ vals, double* __restrict__ rhs,
+                                             int* __restrict__ status) {
+    using Sm = RowSmem<Real, NLOC, 1, false>;
+    constexpr int KS = 8;
+    constexpr int VEC = Sm::VEC;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarps = blockDim.x >> 5;
+    const int64_t wg = (int64_t)blockIdx.x * nwarps + warp;
+    const int64_t row0 = p.row_begin + wg * 32;
+    if (row0 >= p.nrows) return;  // warp-uniform; no block-wide barrier follows
+    const int64_t rend = row0 + 32 < p.nrows ? row0 + 32 : p.nrows;
+    const int64_t cbase = p.rowptr[row0];
+    const int clen = (int)(p.rowptr[rend] - cbase);
+    const int shift = (int)(cbase & (VEC - 1));
+    unsigned char* wbase = smem_raw + Sm::warp_bytes(p.cap) * warp;
+    Real* sC = reinterpret_cast<Real*>(wbase) + shift;
+    {
+        const int nvec = (shift + clen + VEC - 1) / VEC;
+        int4* z = reinterpret_cast<int4*>(wbase);
+        for (int k = lane; k < nvec; k += 32) z[k] = make_int4(0, 0, 0, 0);
+    }
+    const int64_t row = row0 + lane;
+    const bool valid = row < p.nrows;
+    const ScatterRec* rr = vrec + woff[wg] + lane;
+    int deg = 0, base = 0;
+    bool isdir = false;
+    if (valid) {
+        deg = (int)(p.inc_ptr[row + 1] - p.inc_ptr[row]);
+        base = (int)(p.rowptr[row] - cbase);
+        if (DIR) isdir = p.dir_mask[row] != 0;
+    }
+    __syncwarp();
+    Real* myRow = sC + base;
+    const Real drop = Real(p.drop);
+    const int nloop = isdir ? 0 : deg;
+    const int last = nloop - 1;
+    constexpr int KD = ROW_KD, RD = ROW_RD;
+    KVec<Real, KS> Kq[KD];
+    ScatterRec Rq[RD];
+#pragma unroll
+    for (int j = 0; j < KD; ++j) Kq[j].zero();
+#pragma unroll
+    for (int j = 0; j < RD; ++j) Rq[j] = ScatterRec{0u, 0u, 0u, 0u};
+#pragma unroll
+    for (int j = 0; j < RD; ++j)
+        if (j <= last) Rq[j] = rr[32 * j];
+#pragma unroll
+    for (int j = 0; j < KD; ++j)
+        if (j <= last) Kq[j].load(tetK + KS * (int64_t)Rq[j].tet);
+    // the diagonal's offset: column 0 of every record of the row (its own vertex)
+    int odiag = 0;
+    if (deg > 0) odiag = (int)((isdir ? rr[0].off03 : Rq[0].off03) & 255u);
+    Real accD = Real(0), racc = Real(0);
+#pragma unroll kRowUnroll
+    for (int k = 0; k < nloop; ++k) {
+        KVec<Real, KS> Kn;
+        if (k + KD <= last) Kn.load(tetK + KS * (int64_t)Rq[KD].tet);
+        ScatterRec Rn = ScatterRec{0u, 0u, 0u, 0u};
+        if (k + RD <= last) Rn = rr[32 * (k + RD)];
+        const ScatterRec r0 = Rq[0];
+        Real a[NLOC];
+        const Real F = gram_row<Real, NLOC, 1>(Kq[0].v, (int)(r0.meta & 15u), a);
+        if (DROPCHK) {
+#pragma unroll
+            for (int j = 0; j < NLOC; ++j) a[j] = fabs(a[j]) > drop ? a[j] : Real(0);
+        }
+        accD += a[0];
+        racc += F;
+        int o[NLOC];
+        Real cur[NLOC];
+#pragma unroll
+        for (int j = 1; j < NLOC; ++j) {
+            const uint32_t w = j < 4 ? r0.off03 : (j < 8 ? r0.off47 : (r0.meta >> 16));
+            o[j] = (int)byte_of(w, j);
+            cur[j] = myRow[o[j]];
+        }
+#pragma unroll
+        for (int j = 1; j < NLOC; ++j) myRow[o[j]] = cur[j] + a[j];
+#pragma unroll
+        for (int j = 0; j + 1 < KD; ++j) Kq[j] = Kq[j + 1];
+        Kq[KD - 1] = Kn;
+#pragma unroll
+        for (int j = 0; j + 1 < RD; ++j) Rq[j] = Rq[j + 1];
+        Rq[RD - 1] = Rn;
+    }
+    bool bad = false;
+    if (valid) {
+        double F;
+        if (DIR && isdir) {
+            if (deg > 0) myRow[odiag] = Real(deg);
+            const double bcr = p.dir_bc[row];
+            F = 0;
+            for (int q = 0; q < deg; ++q) F += bcr;
+        } else {
+            if (nloop > 0) myRow[odiag] = accD;
+            F = (double)racc;
+            if (DIR)
+                for (int64_t q = p.dir_cptr[row]; q < p.dir_cptr[row + 1]; ++q) myRow[p.dir_coff[q]] = Real(0);
+        }
+        bad |= !isfinite(F);
+        rhs[row] = F;
+    }
+    __syncwarp();
+    const Real fin = write_out_range<Real>(sC, shift, clen, cbase, vals, p.vec_ok, lane);
+    bad |= !isfinite(fin);
+    if (bad) atomicExch(status, ANIGPU_ERR_NONFINITE);
+}
+
+// slots of each warp of 32 rows in a lane-interleaved layout: 32 x (head + its largest
+// incident-tet count)
+__global__ void warp_slots_kernel(int64_t rb, int64_t re, int head, const int64_t* __restrict__ inc_ptr,
+                                  unsigned long long* __restrict__ cnt) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;  // blockDim: a multiple of 32
+    const int64_t r = rb + t;
+    const int deg = r < re ? (int)(inc_ptr[r + 1] - inc_ptr[r]) : 0;
+    const int m = __reduce_max_sync(0xffffffffu, deg);
+    if ((threadIdx.x & 31) == 0 && rb + t < re) cnt[t >> 5] = 32ull * (unsigned long long)(m + head);
+}
+
+// vertex rows' records in the lane-interleaved layout: record j of row rb + 32 w + l at
+// vrec[woff[w] + 32 j + l]
+__global__ void vertex_ilv_build_kernel(int64_t rb, int64_t re, const int64_t* __restrict__ inc_ptr,
+                                        const ScatterRec* __restrict__ recs, const int64_t* __restrict__ woff,
+                                        ScatterRec* __restrict__ vrec) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t r = rb + t;
+    if (r >= re) return;
+    ScatterRec* out = vrec + woff[t >> 5] + (t & 31);
+    const int64_t ib = inc_ptr[r];
+    const int deg = (int)(inc_ptr[r + 1] - ib);
+    for (int j = 0; j < deg; ++j) out[32 * j] = recs[ib + j];
+}
+
+// canonical column c of an edge row's scatter record: its offset within the row
+__device__ __forceinline__ uint32_t rec_off(const ScatterRec& r, int c) {
+    const uint32_t w = c < 4 ? r.off03 : (c < 8 ? r.off47 : (r.meta >> 16));
+    return (w >> (8 * (c & 3))) & 255u;
+}
+
+// ring build, pass 2: one thread per edge row orders the row's incident tets into its ring and
+// writes the header and the records; a row whose tets do not form one ring (a non-manifold edge,
+// more than kRingMax tets, an inconsistent record) sets *fail, and the mesh keeps the record gather
+__global__ void ring_build_kernel(int64_t rb, int64_t re, const int64_t* __restrict__ inc_ptr,
+                                  const ScatterRec* __restrict__ recs, const int32_t* __restrict__ tets,
+                                  const int64_t* __restrict__ woff, uint2* __restrict__ ring, int* __restrict__ fail) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t r = rb + t;
+    if (r >= re) return;
+    uint2* out = ring + woff[t >> 5] + (t & 31);
+    const int64_t ib = inc_ptr[r];
+    const int deg = (int)(inc_ptr[r + 1] - ib);
+    if (deg < 1 || deg > kRingMax) {
+        atomicOr(fail, 1);
+        return;
+    }
+    const int EI[6] = {0, 0, 0, 1, 1, 2}, EJ[6] = {1, 2, 3, 2, 3, 3};
+    int32_t gc[kRingMax], gd[kRingMax];
+    int32_t vA = -1, vB = -1;
+    for (int j = 0; j < deg; ++j) {
+        const ScatterRec rec = recs[ib + j];
+        const int i = (int)(rec.meta & 15u);
+        if (i < 4 || i > 9 || rec.tet > kRingTetMask) {
+            atomicOr(fail, 1);
+            return;
+        }
+        const int k = i - 4, la = EI[k], lb = EJ[k];
+        int lc = -1, ld = -1;
+        for (int l = 0; l < 4; ++l)
+            if (l != la && l != lb) {
+                if (lc < 0) lc = l;
+                else ld = l;
+            }
+        const int32_t* tv = tets + 4 * (int64_t)rec.tet;
+        const int32_t ga = tv[la], gb = tv[lb];
+        if (j == 0) {
+            vA = ga < gb ? ga : gb;
+            vB = ga < gb ? gb : ga;
+        } else if ((ga < gb ? ga : gb) != vA || (ga < gb ? gb : ga) != vB) {
+            atomicOr(fail, 1);
+            return;
+        }
+        gc[j] = tv[lc];
+        gd[j] = tv[ld];
+    }
+    // each ring vertex lies on two tets (one at the two ends of a path)
+    int ones = 0;
+    int32_t end0 = -1;
+    for (int j = 0; j < deg; ++j)
+        for (int h = 0; h < 2; ++h) {
+            const int32_t v = h ? gd[j] : gc[j];
+            int n = 0;
+            for (int q = 0; q < deg; ++q) n += (gc[q] == v) + (gd[q] == v);
+            if (n < 1 || n > 2) {
+                atomicOr(fail, 1);
+                return;
+            }
+            if (n == 1) {
+                ++ones;
+                if (end0 < 0) end0 = v;  // in the smallest tet that has an end
+            }
+        }
+    const bool closed = ones == 0;
+    if (!(ones == 0 || ones == 2) || (closed && deg < 3)) {
+        atomicOr(fail, 1);
+        return;
+    }
+    // walk: start at the smallest tet (closed) or at the path end in the smallest tet
+    int order[kRingMax];
+    int32_t pv[kRingMax];
+    int j0 = 0;
+    int32_t P0 = gc[0];
+    if (!closed) {
+        for (int j = 0; j < deg; ++j)
+            if (gc[j] == end0 || gd[j] == end0) {
+                j0 = j;
+                break;
+            }
+        P0 = end0;
+    }
+    uint32_t used = 1u << j0;
+    order[0] = j0;
+    pv[0] = P0;
+    int32_t N = gc[j0] == P0 ? gd[j0] : gc[j0];
+    for (int s = 1; s < deg; ++s) {
+        int js = -1;
+        for (int j = 0; j < deg; ++j)
+            if (!((used >> j) & 1u) && (gc[j] == N || gd[j] == N)) {
+                js = j;
+                break;
+            }
+        if (js < 0) {
+            atomicOr(fail, 1);
+            return;
+        }
+        used |= 1u << js;
+        order[s] = js;
+        pv[s] = N;
+        N = gc[js] == N ? gd[js] : gc[js];
+    }
+    if (closed ? N != P0 : N == P0) {
+        atomicOr(fail, 1);
+        return;
+    }
+    // records in ring order; the face offsets of consecutive tets must agree
+    uint32_t hx = 0, hy = 0, prevN = 0;
+    for (int s = 0; s < deg; ++s) {
+        const int j = order[s];
+        const ScatterRec rec = recs[ib + j];
+        const int k = (int)(rec.meta & 15u) - 4;
+        const int32_t* tv = tets + 4 * (int64_t)rec.tet;
+        const uint32_t sab = tv[EI[k]] != vA ? 1u : 0u;
+        const uint32_t scd = gc[j] != pv[s] ? 1u : 0u;
+        uint32_t o[10];
+        for (int c = 0; c < 10; ++c) o[c] = rec_off(rec, c);
+        const uint32_t oA = sab ? o[1] : o[0], oB = sab ? o[0] : o[1];
+        const uint32_t oP = scd ? o[3] : o[2], oN = scd ? o[2] : o[3];
+        const uint32_t aP = scd ? o[6] : o[5], aN = scd ? o[5] : o[6];
+        const uint32_t bP = scd ? o[8] : o[7], bN = scd ? o[7] : o[8];
+        const uint32_t oAP = sab ? bP : aP, oBP = sab ? aP : bP;
+        const uint32_t oAN = sab ? bN : aN, oBN = sab ? aN : bN;
+        const uint32_t face = oP | (oAP << 8) | (oBP << 16);
+        const uint32_t ends = oA | (oB << 8) | (o[4] << 16);
+        if (s == 0) {
+            hx = ends | (closed ? 1u << 24 : 0u);
+            hy = face;
+        } else if (face != prevN || ends != (hx & 0xffffffu)) {
+            atomicOr(fail, 1);
+            return;
+        }
+        prevN = oN | (oAN << 8) | (oBN << 16);
+        out[32 * (s + 1)] = make_uint2(rec.tet | ((uint32_t)k << 27) | (sab << 30) | (scd << 31),
+                                       prevN | (o[9] << 24));
+    }
+    if (closed && prevN != hy) {
+        atomicOr(fail, 1);
+        return;
+    }
+    out[0] = make_uint2(hx, hy);
 }
 
 // ---------------------------------------------------------------- vector P2 (linear elasticity)
@@ -1274,6 +1769,150 @@ static int launch_rows_t(anigpu_ctx* h, const RowParams& p, const void* tables, 
     return ANIGPU_OK;
 }
 
+template <typename Real, bool DIR, bool DROPCHK>
+static int launch_ring_t(anigpu_ctx* h, const RowParams& p, void* vals, double* rhs, cudaStream_t st) {
+    const int warps = h->row_warps == 1 ? 1 : 2;
+    const size_t smem = RowSmem<Real, 10, 2, false>::total(p.cap, warps);
+    auto kern = edge_ring_kernel<Real, DIR, DROPCHK>;
+    static int smem_set[64] = {};
+    const int slot = h->device >= 0 && h->device < 64 ? h->device : 0;
+    if ((int)smem > smem_set[slot]) {
+        ANI_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        smem_set[slot] = (int)smem;
+    }
+    kern<<<grid_for(p.nrows - p.row_begin, 32 * warps), 32 * warps, smem, st>>>(
+        p, h->ring, h->ring_woff, (const Real*)h->tetdata, (Real*)vals, rhs, h->d_status);
+    ANI_LAUNCHED(h);
+    return ANIGPU_OK;
+}
+
+template <typename Real, int NLOC, bool DIR, bool DROPCHK>
+static int launch_vilv_t(anigpu_ctx* h, const RowParams& p, void* vals, double* rhs, cudaStream_t st) {
+    const int warps = h->row_warps == 1 ? 1 : 2;
+    const size_t smem = RowSmem<Real, NLOC, 1, false>::total(p.cap, warps);
+    auto kern = vertex_ilv_kernel<Real, NLOC, DIR, DROPCHK>;
+    static int smem_set[64] = {};
+    const int slot = h->device >= 0 && h->device < 64 ? h->device : 0;
+    if ((int)smem > smem_set[slot]) {
+        ANI_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        smem_set[slot] = (int)smem;
+    }
+    kern<<<grid_for(p.nrows - p.row_begin, 32 * warps), 32 * warps, smem, st>>>(
+        p, h->vrec, h->vrec_woff, (const Real*)h->tetdata, (Real*)vals, rhs, h->d_status);
+    ANI_LAUNCHED(h);
+    return ANIGPU_OK;
+}
+
+// vertex rows (Gram form) from the interleaved records under the same conditions as the rings;
+// returns 1 when it did not launch
+template <typename Real, int NLOC>
+static int launch_vilv(anigpu_ctx* h, const RowParams& p, void* vals, double* rhs, uint8_t* touched,
+                       cudaStream_t st, int* rc) {
+    if (!h->vrec || !h->ring_enabled || touched || (h->has_dirichlet && h->bc_nonzero) || p.row_begin != 0) return 1;
+    const bool dir = h->has_dirichlet;
+    const bool dchk = sizeof(Real) == 8 || (float)p.drop != 0.0f;
+    if (dchk) *rc = dir ? launch_vilv_t<Real, NLOC, true, true>(h, p, vals, rhs, st)
+                        : launch_vilv_t<Real, NLOC, false, true>(h, p, vals, rhs, st);
+    else *rc = dir ? launch_vilv_t<Real, NLOC, true, false>(h, p, vals, rhs, st)
+                   : launch_vilv_t<Real, NLOC, false, false>(h, p, vals, rhs, st);
+    return 0;
+}
+
+// P2 edge rows in ring order where the mesh has rings and the call needs neither a touched map nor
+// per-value Dirichlet masks (non-zero boundary values); returns 1 when it did not launch
+template <typename Real>
+static int launch_ring(anigpu_ctx* h, const RowParams& p, void* vals, double* rhs, uint8_t* touched,
+                       cudaStream_t st, int* rc) {
+    if (!h->ring_ok || !h->ring_enabled || touched || (h->has_dirichlet && h->bc_nonzero) || p.row_begin != h->row_range[1]) return 1;
+    const bool dir = h->has_dirichlet;
+    const bool dchk = sizeof(Real) == 8 || (float)p.drop != 0.0f;
+    if (dchk) *rc = dir ? launch_ring_t<Real, true, true>(h, p, vals, rhs, st) : launch_ring_t<Real, false, true>(h, p, vals, rhs, st);
+    else *rc = dir ? launch_ring_t<Real, true, false>(h, p, vals, rhs, st) : launch_ring_t<Real, false, false>(h, p, vals, rhs, st);
+    return 0;
+}
+
+// lane-interleaved records of the vertex rows [0, row_range[1]) (P1: every row)
+static int setup_vertex_ilv(anigpu_ctx* h) {
+    if (h->vrec) cudaFree(h->vrec);
+    if (h->vrec_woff) cudaFree(h->vrec_woff);
+    h->vrec = nullptr;
+    h->vrec_woff = nullptr;
+    if (h->space != ANIGPU_P1 && h->space != ANIGPU_P2) return ANIGPU_OK;
+    const int64_t rb = h->row_range[0], re = h->row_range[1];
+    if (re <= rb) return ANIGPU_OK;
+    cudaStream_t s = h->stream;
+    const int64_t n = re - rb, nw = (n + 31) / 32;
+    unsigned long long* cnt = nullptr;
+    ANI_CUDA(h, cudaMallocAsync((void**)&cnt, sizeof(unsigned long long) * (nw + 1), s));
+    ANI_CUDA(h, cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * (nw + 1), s));
+    warp_slots_kernel<<<grid_for(n, 256), 256, 0, s>>>(rb, re, 0, h->inc_ptr, cnt);
+    ANI_LAUNCHED(h);
+    int rc = dev_alloc(h, &h->vrec_woff, (size_t)nw + 1);
+    if (rc) return rc;
+    rc = scan_counts(h, cnt, nw, h->vrec_woff);
+    if (rc) return rc;
+    int64_t total = 0;
+    ANI_CUDA(h, cudaMemcpyAsync(&total, h->vrec_woff + nw, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    ANI_CUDA(h, cudaStreamSynchronize(s));
+    ANI_CUDA(h, cudaFreeAsync(cnt, s));
+    rc = dev_alloc(h, &h->vrec, (size_t)total);
+    if (rc) return rc;
+    ANI_CUDA(h, cudaMemsetAsync(h->vrec, 0, sizeof(ScatterRec) * (size_t)total, s));
+    vertex_ilv_build_kernel<<<grid_for(n, 128), 128, 0, s>>>(rb, re, h->inc_ptr, h->recs, h->vrec_woff, h->vrec);
+    ANI_LAUNCHED(h);
+    return ANIGPU_OK;
+}
+
+int setup_row_layouts(anigpu_ctx* h) {
+    int rc = setup_vertex_ilv(h);
+    if (rc) return rc;
+    h->ring_ok = false;
+    if (h->ring) cudaFree(h->ring);
+    if (h->ring_woff) cudaFree(h->ring_woff);
+    h->ring = nullptr;
+    h->ring_woff = nullptr;
+    if (h->space != ANIGPU_P2 || h->nt - 1 > (int64_t)kRingTetMask) return ANIGPU_OK;
+    const int64_t rb = h->row_range[1], re = h->row_range[2];
+    if (re <= rb) return ANIGPU_OK;
+    cudaStream_t s = h->stream;
+    const int64_t n = re - rb, nw = (n + 31) / 32;
+    unsigned long long* cnt = nullptr;
+    ANI_CUDA(h, cudaMallocAsync((void**)&cnt, sizeof(unsigned long long) * (nw + 1), s));
+    ANI_CUDA(h, cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * (nw + 1), s));
+    warp_slots_kernel<<<grid_for(n, 256), 256, 0, s>>>(rb, re, 1, h->inc_ptr, cnt);
+    ANI_LAUNCHED(h);
+    rc = dev_alloc(h, &h->ring_woff, (size_t)nw + 1);
+    if (rc) return rc;
+    rc = scan_counts(h, cnt, nw, h->ring_woff);
+    if (rc) return rc;
+    int64_t total = 0;
+    ANI_CUDA(h, cudaMemcpyAsync(&total, h->ring_woff + nw, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    ANI_CUDA(h, cudaStreamSynchronize(s));
+    ANI_CUDA(h, cudaFreeAsync(cnt, s));
+    rc = dev_alloc(h, &h->ring, (size_t)total);
+    if (rc) return rc;
+    ANI_CUDA(h, cudaMemsetAsync(h->ring, 0, sizeof(uint2) * (size_t)total, s));
+    int* fail = nullptr;
+    ANI_CUDA(h, cudaMallocAsync((void**)&fail, sizeof(int), s));
+    ANI_CUDA(h, cudaMemsetAsync(fail, 0, sizeof(int), s));
+    ring_build_kernel<<<grid_for(n, 128), 128, 0, s>>>(rb, re, h->inc_ptr, h->recs, h->tets, h->ring_woff, h->ring,
+                                                       fail);
+    ANI_LAUNCHED(h);
+    int hf = 0;
+    ANI_CUDA(h, cudaMemcpyAsync(&hf, fail, sizeof(int), cudaMemcpyDeviceToHost, s));
+    ANI_CUDA(h, cudaStreamSynchronize(s));
+    ANI_CUDA(h, cudaFreeAsync(fail, s));
+    if (hf) {
+        cudaFree(h->ring);
+        cudaFree(h->ring_woff);
+        h->ring = nullptr;
+        h->ring_woff = nullptr;
+        return ANIGPU_OK;
+    }
+    h->ring_ok = true;
+    return ANIGPU_OK;
+}
+
 template <typename Real, int NLOC, int FORM>
 static int launch_rows(anigpu_ctx* h, const RowParams& p, const void* tables, void* vals, double* rhs,
                        uint8_t* touched, cudaStream_t st) {
@@ -1456,17 +2095,22 @@ int run_assemble(anigpu_ctx* h, int kind, const double* D, const double* f, doub
             if (!gram)
                 rc = f32 ? launch_rows<float, 10, 0>(h, p, tables, vals, rhs, touched, st)
                          : launch_rows<double, 10, 0>(h, p, tables, vals, rhs, touched, st);
-            else if (rg == 0)
-                rc = f32 ? launch_rows<float, 10, 1>(h, p, tables, vals, rhs, touched, st)
-                         : launch_rows<double, 10, 1>(h, p, tables, vals, rhs, touched, st);
-            else
+            else if (rg == 0) {
+                if ((f32 ? launch_vilv<float, 10>(h, p, vals, rhs, touched, st, &rc)
+                         : launch_vilv<double, 10>(h, p, vals, rhs, touched, st, &rc)) != 0)
+                    rc = f32 ? launch_rows<float, 10, 1>(h, p, tables, vals, rhs, touched, st)
+                             : launch_rows<double, 10, 1>(h, p, tables, vals, rhs, touched, st);
+            }
+            else if ((f32 ? launch_ring<float>(h, p, vals, rhs, touched, st, &rc)
+                          : launch_ring<double>(h, p, vals, rhs, touched, st, &rc)) != 0)
                 rc = f32 ? launch_rows<float, 10, 2>(h, p, tables, vals, rhs, touched, st)
                          : launch_rows<double, 10, 2>(h, p, tables, vals, rhs, touched, st);
         } else {
             if (!gram)
                 rc = f32 ? launch_rows<float, 4, 0>(h, p, tables, vals, rhs, touched, st)
                          : launch_rows<double, 4, 0>(h, p, tables, vals, rhs, touched, st);
-            else
+            else if ((f32 ? launch_vilv<float, 4>(h, p, vals, rhs, touched, st, &rc)
+                          : launch_vilv<double, 4>(h, p, vals, rhs, touched, st, &rc)) != 0)
                 rc = f32 ? launch_rows<float, 4, 1>(h, p, tables, vals, rhs, touched, st)
                          : launch_rows<double, 4, 1>(h, p, tables, vals, rhs, touched, st);
         }

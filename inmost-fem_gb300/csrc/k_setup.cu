@@ -581,6 +581,7 @@ int setup_problem(anigpu_ctx* h, int space) {
     h->has_dirichlet = false;
     h->bc_nonzero = false;
     RC(check_status(h, "problem setup"));
+    RC(setup_row_layouts(h));
     return ANIGPU_OK;
 }
 
