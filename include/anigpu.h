@@ -374,6 +374,11 @@ int anigpu_gnn_zero_grads(anigpu_handle h);
 int anigpu_gnn_bind(anigpu_handle h, const void* vals, int precision, int tensor_kind, const double* D);
 int anigpu_gnn_apply(anigpu_handle h, const double* r, double* z);
 int anigpu_gnn_apply_f32(anigpu_handle h, const float* r, float* z);
+/* The coarse products of the FP32 apply (restriction, Horner, powers, combination) as one
+ * cooperative launch with bounded grid barriers (enable = 1, the default) or as separate launches
+ * (0); takes effect at the next anigpu_gnn_bind.  *active: whether the current binding uses the
+ * single launch (it needs cooperative launches that CUDA graphs can capture). */
+int anigpu_gnn_coarse_chain(anigpu_handle h, int enable, int* active);
 int anigpu_gnn_coefficients(anigpu_handle h, float* coef);
 int anigpu_gnn_loss_grad(anigpu_handle h, const double* r, const double* e, double* loss_host);
 int anigpu_gnn_adam(anigpu_handle h, float lr, float beta1, float beta2, float eps, int step, float grad_scale);

@@ -104,6 +104,7 @@ SIGNATURES = {
     "anigpu_gnn_bind": (_i, [_vp, _vp, _i, _i, _vp]),
     "anigpu_gnn_apply": (_i, [_vp, _vp, _vp]),
     "anigpu_gnn_apply_f32": (_i, [_vp, _vp, _vp]),
+    "anigpu_gnn_coarse_chain": (_i, [_vp, _i, ctypes.POINTER(_i)]),
     "anigpu_gnn_coefficients": (_i, [_vp, _vp]),
     "anigpu_gnn_loss_grad": (_i, [_vp, _vp, _vp, ctypes.POINTER(_d)]),
     "anigpu_gnn_adam": (_i, [_vp, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, _i,
@@ -743,6 +744,14 @@ class LearnedPreconditioner:
             z = self.lib.torch.empty_like(r)
             self.lib._check(self.lib.lib.anigpu_gnn_apply_f32(self.lib.h, _ptr(r), _ptr(z)))
         return z
+
+    def coarse_chain(self, enable=None):
+        """Whether the bound preconditioner runs its coarse products as one cooperative launch;
+        enable=True/False selects it for the next bind."""
+        a = ctypes.c_int()
+        self.lib._check(self.lib.lib.anigpu_gnn_coarse_chain(self.lib.h, -1 if enable is None else int(bool(enable)),
+                                                             ctypes.byref(a)))
+        return bool(a.value)
 
     def coefficients(self):
         """The network output a, float32 [ncomp * nv, 4] (row c * nv + v: vertex v, component c)."""

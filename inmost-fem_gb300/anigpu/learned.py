@@ -106,11 +106,43 @@ def make_systems(lib, problem, n, count, seed0=0):
     return systems
 
 
+def evaluate(lib, weights, sizes, seed=2024):
+    """FCG iterations to 1e-8 on the benchmark family (P2, anisotropic per-tet tensors on a
+    perturbed n^3 x 6 Kuhn cube, seed 2024: not a training system) for each parameter file in
+    weights (None: the untrained net) and each n in sizes, with FP32 Jacobi-PCG for reference.
+    Returns {n: {name: iterations}}."""
+    import torch
+    from anigpu import meshgen
+    out = {}
+    for n in sizes:
+        xyz, tets = meshgen.kuhn_cube(n, perturb=0.2, seed=seed)
+        D = meshgen.aniso_tensors(tets.shape[0], 1.5, seed + 1)
+        lib.mesh_upload(xyz, tets)
+        lib.problem_setup(anigpu.P2)
+        lib.set_dirichlet(meshgen.boundary_mask(lib.dof_coords().cpu().numpy()))
+        Dd = torch.tensor(D, device=f"cuda:{lib.device}")
+        v, b, _ = lib.assemble(anigpu.TENSOR_TET_SYM, Dd, None, 1.0, 4, anigpu.F32)
+        v, b = v.clone(), b.clone()
+        _, st = lib.solve(v, b, anigpu.SOLVE_JACOBI_PCG, anigpu.F32, rtol=1e-8, maxit=1_000_000, check=False)
+        row = {"jacobi_pcg": st.iterations}
+        for name, wf in weights.items():
+            prec = anigpu.LearnedPreconditioner(lib, layers=4, act=anigpu.BF16, seed=1)
+            if wf is not None:
+                prec.set_params(np.load(wf))
+            prec.bind(v, anigpu.F32, anigpu.TENSOR_TET_SYM, Dd)
+            _, st = lib.solve(v, b, anigpu.SOLVE_FCG_LEARNED, anigpu.F32, rtol=1e-8, maxit=1_000_000, check=True)
+            row[name] = st.iterations
+        out[n] = row
+    return out
+
+
 def main(argv=None):
     """Train parameters on seeded synthetic problems and save them:
         python -m anigpu.learned --problem aniso --n 12 --systems 200 --steps 2000
         python -m anigpu.learned --problem elastic --n 8 --systems 200 --steps 3000
-    (each system gives 10 Jacobi-PCG iterates = 10 residual/correction pairs)"""
+    (each system gives 10 Jacobi-PCG iterates = 10 residual/correction pairs), or compare parameter
+    files on the benchmark family:
+        python -m anigpu.learned --evaluate 16,32,64 --weights other.npy"""
     import argparse
     import time
 
@@ -123,7 +155,19 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--layers", type=int, default=4)
     ap.add_argument("--out", default=None)
+    ap.add_argument("--evaluate", default=None,
+                    help="instead of training: FCG iterations on the benchmark family at these sizes, e.g. 16,32,64, "
+                         "for the committed parameters, the untrained net and the files given with --weights")
+    ap.add_argument("--weights", default="", help="comma-separated parameter files for --evaluate")
     a = ap.parse_args(argv)
+    if a.evaluate:
+        import json
+        lib = anigpu.Anigpu(0)
+        weights = {"committed": DEFAULT_WEIGHTS, "untrained": None}
+        for wf in filter(None, a.weights.split(",")):
+            weights[os.path.basename(wf)] = wf
+        print(json.dumps(evaluate(lib, weights, [int(x) for x in a.evaluate.split(",")])))
+        return
     elastic = a.problem == "elastic"
     n = a.n or (8 if elastic else 12)
     count = a.systems or 200

@@ -577,6 +577,12 @@ int anigpu_gnn_apply_f32(anigpu_handle h, const float* r, float* z) {
     ANI_CUDA(h, cudaStreamSynchronize(h->stream));
     return ANIGPU_OK;
 }
+int anigpu_gnn_coarse_chain(anigpu_handle h, int enable, int* active) {
+    CHECK_H(h);
+    if (enable >= 0) h->chain_enabled = enable != 0;
+    if (active) *active = gnn_chain_active(h);
+    return ANIGPU_OK;
+}
 int anigpu_gnn_coefficients(anigpu_handle h, float* coef) {
     CHECK_H(h);
     cudaSetDevice(h->device);

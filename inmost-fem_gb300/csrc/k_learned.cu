@@ -83,6 +83,14 @@ struct Gnn {
     int32_t* ccol = nullptr;
     float* cval = nullptr;
     int64_t cnnz = 0;
+    // the coarse graph again in slices of 32 rows (entry j of row 32 s + l at sbase[s] + 32 j + l,
+    // padded with zero entries to the slice's longest row) for the fused coarse chain
+    int64_t* sbase = nullptr;
+    int32_t* scol = nullptr;
+    float* sval = nullptr;
+    int64_t snnz = 0;
+    unsigned int* bar = nullptr;  // grid barrier of the fused chain: arrivals, generation, expired
+    int chain_grid = 0;           // co-resident blocks of the fused chain; 0: separate launches
     float* diag_f = nullptr;    // fine diagonal
     float* isd_c = nullptr;     // 1/sqrt(A_vv)
     float* feat = nullptr;      // static features [nc][NF]
@@ -491,6 +499,146 @@ __global__ void __launch_bounds__(256) prolong_dot_kernel(int64_t nf, CMap m, co
         part_rz[blockIdx.x] = ta;
         part_zq[blockIdx.x] = tb;
     }
+}
+
+// ------------------------------------------------------------ fused coarse chain (one cooperative launch)
+// The coarse part of M r as one kernel: restriction, the three Horner products, the two powers and
+// the combination (the work of restrict_scale, cspmv4 x 5 and combine4 above), separated by grid
+// barriers instead of kernel boundaries.  One thread per coarse row; the coarse graph is read in
+// 32-row slices (coalesced column and value loads).  The barrier waits are bounded: a wait that
+// expires records ANIGPU_ERR_TIMEOUT in *status and poisons the correction with NaN, which the
+// solver treats as a breakdown (Jacobi for the rest of the solve); no wait can hang.
+struct ChainArgs {
+    int64_t nc;
+    CMap map;
+    const float* r;
+    const int64_t* vrow;
+    const int32_t* vedge;
+    const float* isd;
+    const float* coef;
+    const int64_t* sbase;
+    const int32_t* scol;
+    const float* sval;
+    float *u, *t0, *t1, *pw, *cc;
+    unsigned int* bar;
+    int* status;
+    const int* stop;
+};
+
+constexpr unsigned kBarrierSpins = 1u << 22;  // ~0.3 s of 64-ns sleeps
+
+// all blocks of the (co-resident) grid: returns false when the wait expired
+__device__ __forceinline__ bool chain_barrier(unsigned int* bar, int* status) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        ok = 1;
+        volatile unsigned int* gen = bar + 1;
+        const unsigned int g0 = *gen;
+        __threadfence();
+        if (atomicAdd(bar, 1u) + 1u == gridDim.x) {
+            bar[0] = 0u;
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            unsigned int spins = 0;
+            while (*gen == g0) {
+                if (++spins > kBarrierSpins) {
+                    atomicExch(status, ANIGPU_ERR_TIMEOUT);
+                    atomicExch(bar + 2, 1u);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// row v of A_hat x from the slices (padding entries: column v, value 0)
+__device__ __forceinline__ float chain_spmv(const ChainArgs& a, int64_t v, const float* __restrict__ x) {
+    const int64_t s = v >> 5;
+    const int64_t b = a.sbase[s], e = a.sbase[s + 1];
+    const int lane = (int)(v & 31);
+    float acc = 0.f;
+#pragma unroll 4
+    for (int64_t q = b + lane; q < e; q += 32) acc = fmaf(a.sval[q], x[a.scol[q]], acc);
+    return acc;
+}
+
+__global__ void __launch_bounds__(256) coarse_chain_kernel(ChainArgs a) {
+    if (a.stop && *a.stop) return;  // the same value for every block: no barrier is entered
+    if (((volatile unsigned int*)a.bar)[2]) {  // an earlier launch's wait expired: the barrier is unusable
+        for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < a.nc; v += (int64_t)gridDim.x * blockDim.x)
+            a.cc[v] = __int_as_float(0x7fc00000);
+        return;
+    }
+    const int64_t nthr = (int64_t)gridDim.x * blockDim.x;
+    const int64_t t0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    bool ok = true;
+    // u = Dc^-1/2 P^T r ; t0 = a_3 u
+    for (int64_t v = t0; v < a.nc; v += nthr) {
+        const int c = a.map.comp_coarse(v);
+        const int64_t vs = v - c * a.map.nv;
+        const float* rc = a.r + c * a.map.nds;
+        float sum = 0.f;
+        for (int64_t k = a.vrow[vs]; k < a.vrow[vs + 1]; ++k) sum += rc[a.vedge[k]];
+        const float uu = a.isd[v] * fmaf(0.5f, sum, rc[vs]);
+        a.u[v] = uu;
+        a.t0[v] = a.coef[K * v + K - 1] * uu;
+    }
+    // Horner: t <- A_hat t + a_k u, k = 2, 1, 0 (the last into pw[0])
+    const float* src = a.t0;
+    for (int k = K - 2; k >= 0; --k) {
+        ok &= chain_barrier(a.bar, a.status);
+        float* dst = k == 0 ? a.pw : (src == a.t0 ? a.t1 : a.t0);
+        for (int64_t v = t0; v < a.nc; v += nthr) dst[v] = fmaf(a.coef[K * v + k], a.u[v], chain_spmv(a, v, src));
+        src = dst;
+    }
+    // powers P_k = A_hat P_{k-1}, k = 1, 2
+    for (int k = 1; k <= K - 2; ++k) {
+        ok &= chain_barrier(a.bar, a.status);
+        const float* x = a.pw + (int64_t)(k - 1) * a.nc;
+        float* y = a.pw + (int64_t)k * a.nc;
+        for (int64_t v = t0; v < a.nc; v += nthr) y[v] = chain_spmv(a, v, x);
+    }
+    // P_3 = A_hat P_2 ; c = isd .* sum_k a_k P_k
+    ok &= chain_barrier(a.bar, a.status);
+    for (int64_t v = t0; v < a.nc; v += nthr) {
+        float sum = a.coef[K * v + K - 1] * chain_spmv(a, v, a.pw + (int64_t)(K - 2) * a.nc);
+#pragma unroll
+        for (int k = K - 2; k >= 0; --k) sum = fmaf(a.coef[K * v + k], a.pw[(int64_t)k * a.nc + v], sum);
+        a.cc[v] = ok ? a.isd[v] * sum : __int_as_float(0x7fc00000);
+    }
+}
+
+// slices: 32 x (the longest row of each 32-row slice) entries
+__global__ void sell_count_kernel(int64_t nc, const int64_t* __restrict__ crow, unsigned long long* __restrict__ cnt) {
+    const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;  // blockDim: a multiple of 32
+    const int len = v < nc ? (int)(crow[v + 1] - crow[v]) : 0;
+    const int m = __reduce_max_sync(0xffffffffu, len);
+    if ((threadIdx.x & 31) == 0 && v < nc) cnt[v >> 5] = 32ull * (unsigned long long)m;
+}
+
+__global__ void sell_fill_kernel(int64_t nc, const int64_t* __restrict__ crow, const int32_t* __restrict__ ccol,
+                                 const float* __restrict__ cval, const int64_t* __restrict__ sbase,
+                                 int32_t* __restrict__ scol, float* __restrict__ sval) {
+    const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (v >= nc) return;
+    const int64_t s = v >> 5, b = crow[v];
+    const int len = (int)(crow[v + 1] - b), w = (int)((sbase[s + 1] - sbase[s]) >> 5);
+    for (int j = 0; j < w; ++j) {
+        const int64_t q = sbase[s] + 32 * j + (v & 31);
+        scol[q] = j < len ? ccol[b + j] : (int32_t)v;
+        sval[q] = j < len ? cval[b + j] : 0.f;
+    }
+}
+
+__global__ void chain_probe_kernel(int* out) {
+    if (out && threadIdx.x == 0 && blockIdx.x == 0) *out = 1;
 }
 
 // ------------------------------------------------------------ network forward
@@ -1128,12 +1276,88 @@ int apply_impl(anigpu_ctx* h, Gnn* g, const T* r, T* z) {
 
 }  // namespace
 
+// Whether a cooperative launch can be captured into a CUDA graph here (the solver's iterations
+// are graph-captured): a one-block launch of an empty kernel captured, instantiated and run on a
+// private stream, once per process.
+bool chain_capture_ok() {
+    static int known = -1;
+    if (known >= 0) return known == 1;
+    cudaStream_t st = nullptr;
+    cudaGraph_t gr = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    bool ok = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess;
+    if (ok) {
+        int* nul = nullptr;
+        void* args[] = {&nul};
+        ok = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+        if (ok) {
+            const cudaError_t e1 = cudaLaunchCooperativeKernel((const void*)chain_probe_kernel, dim3(1), dim3(32), args, 0, st);
+            const cudaError_t e2 = cudaStreamEndCapture(st, &gr);
+            ok = e1 == cudaSuccess && e2 == cudaSuccess && gr;
+        }
+        if (ok) ok = cudaGraphInstantiate(&ge, gr, 0) == cudaSuccess;
+        if (ok) ok = cudaGraphLaunch(ge, st) == cudaSuccess && cudaStreamSynchronize(st) == cudaSuccess;
+    }
+    if (ge) cudaGraphExecDestroy(ge);
+    if (gr) cudaGraphDestroy(gr);
+    if (st) cudaStreamDestroy(st);
+    (void)cudaGetLastError();
+    known = ok ? 1 : 0;
+    return ok;
+}
+
+// the slices of the coarse graph and the grid of the fused chain (0: the separate launches)
+int chain_setup(anigpu_ctx* h, Gnn* g) {
+    cudaStream_t s = h->stream;
+    const int64_t ns = (g->nc + 31) / 32;
+    unsigned long long* cnt = nullptr;
+    ANI_CUDA(h, cudaMallocAsync((void**)&cnt, sizeof(unsigned long long) * (ns + 1), s));
+    ANI_CUDA(h, cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * (ns + 1), s));
+    sell_count_kernel<<<nblk(g->nc, 256), 256, 0, s>>>(g->nc, g->crow, cnt);
+    ANI_LAUNCHED(h);
+    RC(dev_alloc(h, &g->sbase, (size_t)ns + 1));
+    RC(scan_counts(h, cnt, ns, g->sbase));
+    int64_t snnz = 0;
+    ANI_CUDA(h, cudaMemcpyAsync(&snnz, g->sbase + ns, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    ANI_CUDA(h, cudaStreamSynchronize(s));
+    ANI_CUDA(h, cudaFreeAsync(cnt, s));
+    if (snnz != g->snnz || !g->scol) {
+        RC(dev_alloc(h, &g->scol, (size_t)std::max<int64_t>(snnz, 1)));
+        RC(dev_alloc(h, &g->sval, (size_t)std::max<int64_t>(snnz, 1)));
+        g->snnz = snnz;
+    }
+    sell_fill_kernel<<<nblk(g->nc, 256), 256, 0, s>>>(g->nc, g->crow, g->ccol, g->cval, g->sbase, g->scol, g->sval);
+    ANI_LAUNCHED(h);
+    if (!g->bar) RC(dev_alloc(h, &g->bar, 3));
+    ANI_CUDA(h, cudaMemsetAsync(g->bar, 0, 3 * sizeof(unsigned int), s));
+    g->chain_grid = 0;
+    int coop = 0, nsm = 0, per_sm = 0;
+    ANI_CUDA(h, cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, h->device));
+    ANI_CUDA(h, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->device));
+    ANI_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, coarse_chain_kernel, 256, 0));
+    if (coop && per_sm > 0 && h->chain_enabled && chain_capture_ok())
+        g->chain_grid = (int)std::min<int64_t>((int64_t)per_sm * nsm, std::max<int64_t>(1, (g->nc + 255) / 256));
+    return ANIGPU_OK;
+}
+
 // z = M r in FP32 with fused kernels; nb blocks of partials for r.z and z.qold.  No
 // allocation and no synchronisation, so solver iterations around it can be graph-captured.
 int gnn_precond_f32(anigpu_ctx* h, const float* r, float* z, const float* qold, double* part_rz, double* part_zq,
                     int nb, const int* stop) {
     Gnn* g = gnn(h);
     cudaStream_t s = h->stream;
+    if (g->chain_grid > 0) {
+        ChainArgs a{g->nc, g->map, r, g->vrow, g->vedge, g->isd_c, g->coef, g->sbase, g->scol, g->sval,
+                    g->u, g->t0, g->t1, g->pw, g->cc, g->bar, h->d_status, stop};
+        void* args[] = {&a};
+        ANI_CUDA(h, cudaLaunchCooperativeKernel((const void*)coarse_chain_kernel, dim3(g->chain_grid), dim3(256), args,
+                                                0, s));
+        ANI_LAUNCHED(h);
+        prolong_dot_kernel<<<nb, 256, 0, s>>>(g->nf, g->map, r, g->diag_f, g->cc, g->edge_ends, qold, z, part_rz,
+                                              part_zq, stop);
+        ANI_LAUNCHED(h);
+        return ANIGPU_OK;
+    }
     const unsigned bc = nblk(g->nc * CW, 256);
     restrict_scale_kernel<<<bc, 256, 0, s>>>(g->nc, g->map, r, g->vrow, g->vedge, g->isd_c, g->coef, g->u, g->t0, stop);
     ANI_LAUNCHED(h);
@@ -1159,6 +1383,7 @@ int gnn_precond_f32(anigpu_ctx* h, const float* r, float* z, const float* qold, 
 }
 
 int64_t gnn_bind_generation(anigpu_ctx* h) { return gnn(h) ? gnn(h)->bind_gen : -1; }
+int gnn_chain_active(anigpu_ctx* h) { return gnn(h) && gnn(h)->bound && gnn(h)->chain_grid > 0 ? 1 : 0; }
 
 // ------------------------------------------------------------ entry points
 int gnn_init(anigpu_ctx* h, int layers, int act, uint64_t seed) {
@@ -1293,6 +1518,7 @@ int gnn_bind(anigpu_ctx* h, const void* vals, int precision, int kind, const dou
     coarse_fill_kernel<<<nblk(g->nc, 256), 256, 0, s>>>(g->nc, g->map, h->rowptr, h->col, vals, f32, g->diag_f, g->crow,
                                                         g->ccol, g->cval, g->isd_c);
     ANI_LAUNCHED(h);
+    RC(chain_setup(h, g));
     static_feat_kernel<<<nblk(g->nc, 256), 256, 0, s>>>(g->nc, g->map, g->diag_f, h->inc_ptr, h->recs, kind, D, g->feat);
     ANI_LAUNCHED(h);
     const int nb = (int)std::min<int64_t>(kMaxPart, nblk(g->nc, 256));
@@ -1435,7 +1661,8 @@ void free_learned(anigpu_ctx* h) {
     if (!g) return;
     void* ptrs[] = {g->w,      g->g,  g->m1, g->m2, g->wk, g->crow, g->ccol, g->cval, g->diag_f, g->isd_c,
                     g->feat,   g->edge_ends, g->vrow, g->vedge, g->dpart, g->coef, g->act_buf, g->u, g->pw, g->qv, g->t0, g->t1,
-                    g->cc,     g->ga, g->dH, g->dG, g->dZ, g->part, g->wpart, g->fine_tmp, g->fine_tmp2};
+                    g->cc,     g->ga, g->dH, g->dG, g->dZ, g->part, g->wpart, g->fine_tmp, g->fine_tmp2,
+                    g->sbase,  g->scol, g->sval, g->bar};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete g;

@@ -27,4 +27,5 @@ const float* gnn_fine_diag(anigpu_ctx* h);
 int gnn_precond_f32(anigpu_ctx* h, const float* r, float* z, const float* qold, double* part_rz, double* part_zq,
                     int nb, const int* stop);
 int64_t gnn_bind_generation(anigpu_ctx* h);
+int gnn_chain_active(anigpu_ctx* h);
 void free_fcg(anigpu_ctx* h);

@@ -68,6 +68,29 @@ def test_apply_matches_oracle(small):
     assert _rel(z32, z_or) <= 1e-5
 
 
+def test_coarse_chain_matches_separate_launches(small, lib):
+    """The coarse products as one cooperative launch (grid barriers) and as separate launches: the
+    same M r to FP32 rounding (different summation order in the coarse products), and FCG solves
+    that agree."""
+    import anigpu
+    prec = small["prec"]
+    assert prec.coarse_chain() is True  # cooperative launches capture into graphs on this GPU
+    z1 = prec.apply_f32(small["r"]).double().cpu().numpy()
+    x1, s1 = lib.solve(small["vals"], small["r"], anigpu.SOLVE_FCG_LEARNED, anigpu.F32, rtol=1e-8, maxit=10000)
+    prec.coarse_chain(False)
+    try:
+        prec.bind(small["vals"], anigpu.F32, anigpu.TENSOR_TET_SYM, small["D"])
+        assert prec.coarse_chain() is False
+        z0 = prec.apply_f32(small["r"]).double().cpu().numpy()
+        x0, s0 = lib.solve(small["vals"], small["r"], anigpu.SOLVE_FCG_LEARNED, anigpu.F32, rtol=1e-8, maxit=10000)
+    finally:
+        prec.coarse_chain(True)
+        prec.bind(small["vals"], anigpu.F32, anigpu.TENSOR_TET_SYM, small["D"])
+    assert _rel(z1, z0) <= 1e-6
+    assert abs(s1.iterations - s0.iterations) <= 2 and s1.fallback_steps == 0 and s0.fallback_steps == 0
+    assert _rel(x1.cpu().numpy(), x0.cpu().numpy()) <= 1e-6
+
+
 def test_preconditioner_is_symmetric_positive(small, lib):
     rng = np.random.default_rng(9)
     x = rng.standard_normal(lib.ndof)
