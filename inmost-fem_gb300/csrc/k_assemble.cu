@@ -1578,12 +1578,183 @@ __global__ void __launch_bounds__(64) vec_row_gather_kernel(RowParams p, int64_t
         rhs[R] = F;
     }
     __syncwarp();
-    Real fin = Real(0);
-    for (int k = lane; k < clen; k += 32) {
-        const Real v = sC[k];
-        fin = fma(v, Real(0), fin);
-        vals[cbase + k] = v;
+    const Real fin = write_out_range<Real>(sC, shift, clen, cbase, vals, p.vec_ok, lane);
+    bad |= !isfinite(fin);
+    if (bad) atomicExch(status, ANIGPU_ERR_NONFINITE);
+}
+
+// Vector P2 edge rows (component c = blockIdx.y) in ring order: the scalar rings, each column of the
+// scalar row standing for its three component columns d L + offset (the vector row repeats the
+// scalar row's columns once per column component d).  Per tet and d the element row is the scalar
+// edge row's Gram formula with G replaced by B^{cd} in ring roles; A, B and the edge are summed in
+// registers and the face columns carried, as in edge_ring_kernel, so every value is written once.
+template <typename Real, bool DIR>
+__global__ void __launch_bounds__(64) vec_edge_ring_kernel(RowParams p, int64_t nds, const int64_t* __restrict__ vrowptr,
+                                                           const uint2* __restrict__ ring,
+                                                           const int64_t* __restrict__ woff,
+                                                           const Real* __restrict__ tetB, Real* __restrict__ vals,
+                                                           double* __restrict__ rhs, int* __restrict__ status) {
+    constexpr int VEC = 16 / (int)sizeof(Real);
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarps = blockDim.x >> 5;
+    const int c = blockIdx.y;
+    const int64_t wg = (int64_t)blockIdx.x * nwarps + warp;
+    const int64_t row0 = p.row_begin + wg * 32;
+    if (row0 >= p.nrows) return;  // warp-uniform; no block-wide barrier follows
+    const int64_t rend = row0 + 32 < p.nrows ? row0 + 32 : p.nrows;
+    const int64_t cbase = vrowptr[c * nds + row0];
+    const int clen = (int)(vrowptr[c * nds + rend] - cbase);
+    const int shift = (int)(cbase & (VEC - 1));
+    const size_t chunk_bytes = (((size_t)32 * 3 * p.cap + VEC) * sizeof(Real) + 15) / 16 * 16;
+    unsigned char* wbase = smem_raw + chunk_bytes * warp;
+    Real* sC = reinterpret_cast<Real*>(wbase) + shift;
+    {
+        const int nvec = (shift + clen + VEC - 1) / VEC;
+        int4* z = reinterpret_cast<int4*>(wbase);
+        for (int k = lane; k < nvec; k += 32) z[k] = make_int4(0, 0, 0, 0);
     }
+    const int64_t r = row0 + lane;
+    const int64_t R = c * nds + r;
+    const bool valid = r < p.nrows;
+    const uint2* rr = ring + woff[wg] + lane;
+    int deg = 0, base = 0, L = 0;
+    bool isdir = false;
+    uint2 hd = make_uint2(0u, 0u);
+    if (valid) {
+        deg = (int)(p.inc_ptr[r + 1] - p.inc_ptr[r]);
+        base = (int)(vrowptr[R] - cbase);
+        L = (int)(p.rowptr[r + 1] - p.rowptr[r]);
+        if (DIR) isdir = p.dir_mask[R] != 0;
+        hd = rr[0];
+    }
+    __syncwarp();
+    Real* myRow = sC + base;
+    const int nloop = isdir ? 0 : deg;
+    const int last = nloop - 1;
+    constexpr int KD = 2, RD = 4;
+    VBlock<Real> Kq[KD];
+    uint2 Rq[RD];
+#pragma unroll
+    for (int j = 0; j < KD; ++j) Kq[j].zero();
+#pragma unroll
+    for (int j = 0; j < RD; ++j) Rq[j] = make_uint2(0u, 0u);
+#pragma unroll
+    for (int j = 0; j < RD; ++j)
+        if (j <= last) Rq[j] = rr[32 * (j + 1)];
+#pragma unroll
+    for (int j = 0; j < KD; ++j)
+        if (j <= last) Kq[j].load(tetB + 16 * (int64_t)(Rq[j].x & kRingTetMask));
+    const bool closed = (hd.x >> 24) & 1u;
+    Real cP[3], cAP[3], cBP[3], fP[3], fAP[3], fBP[3], accA[3], accB[3], accE[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) cP[d] = cAP[d] = cBP[d] = fP[d] = fAP[d] = fBP[d] = accA[d] = accB[d] = accE[d] = Real(0);
+    uint32_t coff = hd.y;
+    Real racc = Real(0);
+    const Real m2 = Real(-0.2), p6 = Real(0.6), p8 = Real(0.8), p16 = Real(1.6);
+    for (int k = 0; k < nloop; ++k) {
+        VBlock<Real> Kn;
+        if (k + KD <= last) Kn.load(tetB + 16 * (int64_t)(Rq[KD].x & kRingTetMask));
+        uint2 Rn = make_uint2(0u, 0u);
+        if (k + RD <= last) Rn = rr[32 * (k + RD + 1)];
+        const uint2 r0 = Rq[0];
+        const Real* bv = Kq[0].v;
+        const Real lam = bv[9], mu = bv[10];
+        // local vertices of the ring roles: local edge le = (a, b), others c_ < d_
+        const int le = (int)((r0.x >> 27) & 7u);
+        const int la = le <= 2 ? 0 : (le <= 4 ? 1 : 2);
+        const int lb = le == 0 ? 1 : ((le == 1 || le == 3) ? 2 : 3);
+        const int lc = le <= 2 ? (le == 0 ? 2 : 1) : 0;
+        const int ld = 6 - la - lb - lc;
+        const bool sab = (r0.x >> 30) & 1u, scd = (r0.x >> 31) & 1u;
+        Real gA[3], gB[3], gP[3], gN[3];
+        gvec(bv, sab ? lb : la, gA);
+        gvec(bv, sab ? la : lb, gB);
+        gvec(bv, scd ? ld : lc, gP);
+        gvec(bv, scd ? lc : ld, gN);
+        const Real gAc = sel3(gA, c), gBc = sel3(gB, c), gPc = sel3(gP, c), gNc = sel3(gN, c);
+        const Real dAB = gA[0] * gB[0] + gA[1] * gB[1] + gA[2] * gB[2];
+        const Real dAP = gA[0] * gP[0] + gA[1] * gP[1] + gA[2] * gP[2];
+        const Real dAN = gA[0] * gN[0] + gA[1] * gN[1] + gA[2] * gN[2];
+        const Real dBP = gB[0] * gP[0] + gB[1] * gP[1] + gB[2] * gP[2];
+        const Real dBN = gB[0] * gN[0] + gB[1] * gN[1] + gB[2] * gN[2];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const Real BAB = lameB(lam, mu, gA, gAc, gB, gBc, dAB, c, d);
+            const Real BBA = lameB(lam, mu, gB, gBc, gA, gAc, dAB, c, d);
+            const Real BAP = lameB(lam, mu, gA, gAc, gP, gPc, dAP, c, d);
+            const Real BAN = lameB(lam, mu, gA, gAc, gN, gNc, dAN, c, d);
+            const Real BBP = lameB(lam, mu, gB, gBc, gP, gPc, dBP, c, d);
+            const Real BBN = lameB(lam, mu, gB, gBc, gN, gNc, dBN, c, d);
+            const Real BAA = -((BAB + BAP) + BAN), BBB = -((BBA + BBP) + BBN);
+            accA[d] += fma(m2, BAA, p6 * BBA);
+            accB[d] += fma(p6, BAB, m2 * BBB);
+            accE[d] += fma(p16, BAA + BBB, p8 * (BAB + BBA));
+            const Real vP = m2 * (BAP + BBP), vN = m2 * (BAN + BBN);
+            const Real vAP = fma(p8, (BAA + BAP) + BBA, p16 * BBP), vAN = fma(p8, (BAA + BAN) + BBA, p16 * BBN);
+            const Real vBP = fma(p8, (BAB + BBB) + BBP, p16 * BAP), vBN = fma(p8, (BAB + BBB) + BBN, p16 * BAN);
+            const Real oP = cP[d] + vP, oAP = cAP[d] + vAP, oBP = cBP[d] + vBP;
+            Real* rowd = myRow + d * L;
+            if (k == 0 && closed) {
+                fP[d] = oP;
+                fAP[d] = oAP;
+                fBP[d] = oBP;
+            } else {
+                rowd[coff & 255u] = oP;
+                rowd[(coff >> 8) & 255u] = oAP;
+                rowd[(coff >> 16) & 255u] = oBP;
+            }
+            rowd[r0.y >> 24] = p8 * ((BAP + BAN) + (BBP + BBN));
+            cP[d] = vN;
+            cAP[d] = vAN;
+            cBP[d] = vBN;
+        }
+        racc += Real(0.2) * bv[11];
+        coff = r0.y;
+#pragma unroll
+        for (int j = 0; j + 1 < KD; ++j) Kq[j] = Kq[j + 1];
+        Kq[KD - 1] = Kn;
+#pragma unroll
+        for (int j = 0; j + 1 < RD; ++j) Rq[j] = Rq[j + 1];
+        Rq[RD - 1] = Rn;
+    }
+    bool bad = false;
+    if (valid) {
+        double F;
+        if (DIR && isdir) {
+            if (deg > 0) myRow[c * L + (int)((hd.x >> 16) & 255u)] = Real(deg);  // diagonal: the edge itself
+            const double bcr = p.bcnz ? p.dir_bc[R] : 0.0;
+            F = 0;
+            for (int q = 0; q < deg; ++q) F += bcr;
+        } else {
+            if (nloop > 0) {
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    Real* rowd = myRow + d * L;
+                    rowd[coff & 255u] = cP[d] + fP[d];
+                    rowd[(coff >> 8) & 255u] = cAP[d] + fAP[d];
+                    rowd[(coff >> 16) & 255u] = cBP[d] + fBP[d];
+                    rowd[hd.x & 255u] = accA[d];
+                    rowd[(hd.x >> 8) & 255u] = accB[d];
+                    rowd[(hd.x >> 16) & 255u] = accE[d];
+                }
+            }
+            F = (double)racc;
+            if (DIR) {
+                // Dirichlet columns: F -= A(i,k) bc_k with the assembled A(i,k), then the column is eliminated
+                const int64_t vb = vrowptr[R];
+                for (int64_t q = p.dir_cptr[R]; q < p.dir_cptr[R + 1]; ++q) {
+                    const int off = p.dir_coff[q];
+                    if (p.bcnz) F -= (double)myRow[off] * p.dir_bc[p.vcol[vb + off]];
+                    myRow[off] = Real(0);
+                }
+            }
+        }
+        bad |= !isfinite(F);
+        rhs[R] = F;
+    }
+    __syncwarp();
+    const Real fin = write_out_range<Real>(sC, shift, clen, cbase, vals, p.vec_ok, lane);
     bad |= !isfinite(fin);
     if (bad) atomicExch(status, ANIGPU_ERR_NONFINITE);
 }
@@ -1871,7 +2042,7 @@ int setup_row_layouts(anigpu_ctx* h) {
     if (h->ring_woff) cudaFree(h->ring_woff);
     h->ring = nullptr;
     h->ring_woff = nullptr;
-    if (h->space != ANIGPU_P2 || h->nt - 1 > (int64_t)kRingTetMask) return ANIGPU_OK;
+    if ((h->space != ANIGPU_P2 && h->space != ANIGPU_VEC3_P2) || h->nt - 1 > (int64_t)kRingTetMask) return ANIGPU_OK;
     const int64_t rb = h->row_range[1], re = h->row_range[2];
     if (re <= rb) return ANIGPU_OK;
     cudaStream_t s = h->stream;
@@ -1976,7 +2147,7 @@ static int run_assemble_vec(anigpu_ctx* h, int kind, const double* D, const doub
     p.dir_bc = h->dir_bc;
     p.edofs = h->edofs;
     p.drop = 0;
-    p.vec_ok = 0;
+    p.vec_ok = ((uintptr_t)vals % 16) == 0 ? 1 : 0;
     p.dir_cptr = h->dir_cptr;
     p.dir_coff = h->dir_coff;
     p.vcol = h->col;
@@ -1997,7 +2168,18 @@ static int run_assemble_vec(anigpu_ctx* h, int kind, const double* D, const doub
         const size_t smem = ((((size_t)32 * 3 * p.cap + 16 / rsz) * rsz + 15) / 16 * 16) * warps;
         const dim3 grid(grid_for(p.nrows - p.row_begin, 32 * warps), 3);
 #define VLAUNCH(R, F, DD)                                                                                          do {                                                                                                               auto kern = vec_row_gather_kernel<R, F, DD>;                                                                   ANI_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));              kern<<<grid, 32 * warps, smem, st>>>(p, h->nds, h->rowptr, (const R*)h->tetdata, (R*)vals, rhs,                                                     h->d_status);                                                         } while (0)
-        if (precision == ANIGPU_F32) {
+        const bool ring = rg == 1 && h->ring_ok && h->ring_enabled;
+#define VRING(R, DD)                                                                                               \
+    do {                                                                                                           \
+        auto kern = vec_edge_ring_kernel<R, DD>;                                                                   \
+        ANI_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));          \
+        kern<<<grid, 32 * warps, smem, st>>>(p, h->nds, h->rowptr, h->ring, h->ring_woff, (const R*)h->tetdata,    \
+                                             (R*)vals, rhs, h->d_status);                                          \
+    } while (0)
+        if (ring) {
+            if (precision == ANIGPU_F32) { if (dir) VRING(float, true); else VRING(float, false); }
+            else { if (dir) VRING(double, true); else VRING(double, false); }
+        } else if (precision == ANIGPU_F32) {
             if (rg == 0) { if (dir) VLAUNCH(float, 1, true); else VLAUNCH(float, 1, false); }
             else { if (dir) VLAUNCH(float, 2, true); else VLAUNCH(float, 2, false); }
         } else {
@@ -2005,6 +2187,7 @@ static int run_assemble_vec(anigpu_ctx* h, int kind, const double* D, const doub
             else { if (dir) VLAUNCH(double, 2, true); else VLAUNCH(double, 2, false); }
         }
 #undef VLAUNCH
+#undef VRING
         ANI_LAUNCHED(h);
     }
     if (side != h->stream) {

@@ -569,7 +569,13 @@ __device__ __forceinline__ float chain_spmv(const ChainArgs& a, int64_t v, const
     return acc;
 }
 
-__global__ void __launch_bounds__(256) coarse_chain_kernel(ChainArgs a) {
+// threads per block of the chain: large blocks, few arrivals per barrier
+#ifndef CHAIN_THREADS
+#define CHAIN_THREADS 1024
+#endif
+constexpr int kChainThreads = CHAIN_THREADS;
+
+__global__ void __launch_bounds__(kChainThreads) coarse_chain_kernel(ChainArgs a) {
     if (a.stop && *a.stop) return;  // the same value for every block: no barrier is entered
     if (((volatile unsigned int*)a.bar)[2]) {  // an earlier launch's wait expired: the barrier is unusable
         for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < a.nc; v += (int64_t)gridDim.x * blockDim.x)
@@ -1334,9 +1340,10 @@ int chain_setup(anigpu_ctx* h, Gnn* g) {
     int coop = 0, nsm = 0, per_sm = 0;
     ANI_CUDA(h, cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, h->device));
     ANI_CUDA(h, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->device));
-    ANI_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, coarse_chain_kernel, 256, 0));
+    ANI_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, coarse_chain_kernel, kChainThreads, 0));
     if (coop && per_sm > 0 && h->chain_enabled && chain_capture_ok())
-        g->chain_grid = (int)std::min<int64_t>((int64_t)per_sm * nsm, std::max<int64_t>(1, (g->nc + 255) / 256));
+        g->chain_grid = (int)std::min<int64_t>((int64_t)per_sm * nsm,
+                                               std::max<int64_t>(1, (g->nc + kChainThreads - 1) / kChainThreads));
     return ANIGPU_OK;
 }
 
@@ -1350,8 +1357,8 @@ int gnn_precond_f32(anigpu_ctx* h, const float* r, float* z, const float* qold, 
         ChainArgs a{g->nc, g->map, r, g->vrow, g->vedge, g->isd_c, g->coef, g->sbase, g->scol, g->sval,
                     g->u, g->t0, g->t1, g->pw, g->cc, g->bar, h->d_status, stop};
         void* args[] = {&a};
-        ANI_CUDA(h, cudaLaunchCooperativeKernel((const void*)coarse_chain_kernel, dim3(g->chain_grid), dim3(256), args,
-                                                0, s));
+        ANI_CUDA(h, cudaLaunchCooperativeKernel((const void*)coarse_chain_kernel, dim3(g->chain_grid), dim3(kChainThreads),
+                                                args, 0, s));
         ANI_LAUNCHED(h);
         prolong_dot_kernel<<<nb, 256, 0, s>>>(g->nf, g->map, r, g->diag_f, g->cc, g->edge_ends, qold, z, part_rz,
                                               part_zq, stop);

@@ -91,3 +91,38 @@ def test_interleaved_vertex_rows_match_oracle(lib, restated, space, kind):
     ref = restated.assemble_problem(xyz, tets, space, kind, D, 1.0, 2, dirichlet=(mask, None))
     assert np.abs(vals.cpu().numpy() - ref["vals"]).max() <= 1e-12 * np.abs(ref["vals"]).max()
     assert np.abs(rhs.cpu().numpy() - ref["rhs"]).max() <= 1e-12 * np.abs(ref["rhs"]).max()
+
+
+@pytest.mark.parametrize("precision", ["F64", "F32"])
+def test_vector_ring_gather_matches_record_gather(lib, restated, precision):
+    """Vector P2 (Lame) edge rows in ring order against the record gather on the same inputs, with
+    clamped and non-zero Dirichlet values, and the FP64 result against the oracle."""
+    import anigpu
+    from anigpu import meshgen
+    prec = getattr(anigpu, precision)
+    xyz, tets = meshgen.kuhn_cube(4, perturb=0.2, seed=13)
+    nt = tets.shape[0]
+    LM = np.stack([1.0 + meshgen.uniform(31, nt), 0.5 + meshgen.uniform(32, nt)], axis=1)
+    lib.mesh_upload(xyz, tets)
+    lib.problem_setup(anigpu.VEC3_P2)
+    coords = lib.dof_coords().cpu().numpy()
+    mask = (np.abs(coords[:, 0]) < 1e-12).astype(np.uint8)
+    bc = np.where(mask == 1, 0.1 * coords[:, 1], 0.0)
+    lib.set_dirichlet(mask, bc)
+    assert lib.gather_layouts() == (True, True)
+    v1, r1, _ = lib.assemble(anigpu.TENSOR_LAME, LM, None, 0.5, 4, prec)
+    v1, r1 = v1.clone(), r1.clone()
+    lib.set_gather_layouts(False)
+    try:
+        v0, r0, _ = lib.assemble(anigpu.TENSOR_LAME, LM, None, 0.5, 4, prec)
+    finally:
+        lib.set_gather_layouts(True)
+    tol = 4e-15 if precision == "F64" else 1e-6
+    a, b = v1.double().cpu().numpy(), v0.double().cpu().numpy()
+    assert np.abs(a - b).max() <= tol * np.abs(b).max()
+    assert np.abs(r1.cpu().numpy() - r0.cpu().numpy()).max() <= tol * np.abs(r0.cpu().numpy()).max()
+    if precision == "F64":
+        ref = restated.assemble_problem(xyz, tets, 5, 4, meshgen.lame9(LM[:, 0], LM[:, 1]), 0.5, 4,
+                                        dirichlet=(mask, bc))
+        assert np.abs(a - ref["vals"]).max() <= 1e-12 * np.abs(ref["vals"]).max()
+        assert np.abs(r1.cpu().numpy() - ref["rhs"]).max() <= 1e-12 * np.abs(ref["rhs"]).max()
