@@ -67,6 +67,7 @@ struct anigpu_ctx {
     cudaStream_t side_stream = nullptr;  // second stream for concurrent launches inside one call
     cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     int row_warps = 2;  // row-gather warps (32 rows each) per block; the batch autotuner sets it
+    bool asm_pdl = false;  // the gathers being launched follow the per-tet kernel on its stream
     bool chain_enabled = true;  // learned preconditioner: coarse products as one cooperative launch
     std::string err;
     int64_t launches = 0;

@@ -39,6 +39,14 @@
 namespace {
 
 
+// Programmatic dependent launch between the phases of one assembly: the per-tet kernel lets the
+// gathers launch once each of its blocks has stored its blocks, and a gather waits for the
+// per-tet kernel's completion (and memory) only before its first per-tet block load, so its
+// set-up (zeroing, row pointers, records) overlaps the per-tet kernel's last wave.  Both are no-ops
+// for launches without a programmatic dependency.
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // ---------------------------------------------------------------- phase 1
 // K = |T| PSI D PSI^T (k00 k11 k22 k01 k02 k12), then f|T| and 0: 8 values per tet.
 // PSI(a,a') = PSI[a + 3a'] (inverse3x3, geometry.h:26-44; core.inl:217-247).
@@ -257,6 +265,7 @@ __global__ void tet_gram_f64_kernel(int64_t nt, const double* __restrict__ xyz, 
     double2* o = reinterpret_cast<double2*>(out + 8 * t);
 #pragma unroll
     for (int q = 0; q < 4; ++q) o[q] = make_double2(G[2 * q], G[2 * q + 1]);
+    pdl_launch_dependents();
 }
 
 // six 256-thread blocks per SM (40 registers): the loads of more tets in flight; the few values
@@ -335,6 +344,7 @@ __global__ void TET_GRAM_BOUNDS tet_gram_f32_kernel(int64_t nt, const double* __
     float4* o = reinterpret_cast<float4*>(out + 8 * t);
     o[0] = make_float4(G[0], G[1], G[2], G[3]);
     o[1] = make_float4(G[4], G[5], G[6], G[7]);
+    pdl_launch_dependents();
 }
 
 // ---------------------------------------------------------------- phase 2
@@ -785,6 +795,12 @@ __global__ void ROW_BOUNDS row_gather_kernel(RowParams p, const Real* __restrict
 constexpr uint32_t kRingTetMask = (1u << 27) - 1;
 constexpr int kRingMax = 32;  // incident tets of an edge that the ring build takes
 
+// the gathers of one assembly on the per-tet kernel's stream with programmatic dependencies (1) or
+// on two streams (0)
+#ifndef ASM_SEQ
+#define ASM_SEQ 1
+#endif
+
 // prefetch depths of the ring gather (per-tet blocks, records) and its unroll, a multiple of both
 #ifndef RING_KD
 #define RING_KD 2
@@ -850,6 +866,7 @@ __global__ void ROW_BOUNDS edge_ring_kernel(RowParams p, const uint2* __restrict
 #pragma unroll
     for (int j = 0; j < RD; ++j)
         if (j <= last) Rq[j] = rr[32 * (j + 1)];
+    pdl_wait();  // the per-tet blocks of this assembly
 #pragma unroll
     for (int j = 0; j < KD; ++j)
         if (j <= last) Kq[j].load(tetK + KS * (int64_t)(Rq[j].x & kRingTetMask));
@@ -951,6 +968,7 @@ __global__ void ROW_BOUNDS edge_ring_kernel(RowParams p, const uint2* __restrict
     const Real fin = write_out_range<Real>(sC, shift, clen, cbase, vals, p.vec_ok, lane);
     bad |= !isfinite(fin);
     if (bad) atomicExch(status, ANIGPU_ERR_NONFINITE);
+    pdl_launch_dependents();
 }
 
 // Vertex rows (Gram form) from lane-interleaved records: record j of lane l of warp w at
@@ -1007,6 +1025,7 @@ __global__ void ROW_BOUNDS vertex_ilv_kernel(RowParams p, const ScatterRec* __re
 #pragma unroll
     for (int j = 0; j < RD; ++j)
         if (j <= last) Rq[j] = rr[32 * j];
+    pdl_wait();  // the per-tet blocks of this assembly
 #pragma unroll
     for (int j = 0; j < KD; ++j)
         if (j <= last) Kq[j].load(tetK + KS * (int64_t)Rq[j].tet);
@@ -1951,8 +1970,20 @@ static int launch_ring_t(anigpu_ctx* h, const RowParams& p, void* vals, double* 
         ANI_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         smem_set[slot] = (int)smem;
     }
-    kern<<<grid_for(p.nrows - p.row_begin, 32 * warps), 32 * warps, smem, st>>>(
-        p, h->ring, h->ring_woff, (const Real*)h->tetdata, (Real*)vals, rhs, h->d_status);
+    // launched right behind the per-tet kernel on the same stream (h->asm_pdl): a programmatic
+    // dependency, so that its blocks start (and set up) while that kernel's last wave runs
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid_for(p.nrows - p.row_begin, 32 * warps));
+    cfg.blockDim = dim3(32 * warps);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = h->asm_pdl ? 1 : 0;
+    ANI_CUDA(h, cudaLaunchKernelEx(&cfg, kern, p, (const uint2*)h->ring, (const int64_t*)h->ring_woff,
+                                   (const Real*)h->tetdata, (Real*)vals, rhs, h->d_status));
     ANI_LAUNCHED(h);
     return ANIGPU_OK;
 }
@@ -1968,8 +1999,18 @@ static int launch_vilv_t(anigpu_ctx* h, const RowParams& p, void* vals, double* 
         ANI_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         smem_set[slot] = (int)smem;
     }
-    kern<<<grid_for(p.nrows - p.row_begin, 32 * warps), 32 * warps, smem, st>>>(
-        p, h->vrec, h->vrec_woff, (const Real*)h->tetdata, (Real*)vals, rhs, h->d_status);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid_for(p.nrows - p.row_begin, 32 * warps));
+    cfg.blockDim = dim3(32 * warps);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = h->asm_pdl ? 1 : 0;
+    ANI_CUDA(h, cudaLaunchKernelEx(&cfg, kern, p, (const ScatterRec*)h->vrec, (const int64_t*)h->vrec_woff,
+                                   (const Real*)h->tetdata, (Real*)vals, rhs, h->d_status));
     ANI_LAUNCHED(h);
     return ANIGPU_OK;
 }
@@ -2260,14 +2301,20 @@ int run_assemble(anigpu_ctx* h, int kind, const double* D, const double* f, doub
     p.dir_cptr = h->dir_cptr;
     p.dir_coff = h->dir_coff;
     // one launch per row range (vertex rows, edge rows) so that the shared-memory row
-    // buffer fits the longest row of that range; the two run concurrently (the vertex
-    // range on a side stream) so that the tail of one overlaps the other
-    cudaStream_t side = h->side_stream ? h->side_stream : h->stream;
+    // buffer fits the longest row of that range.  With the ring and interleaved layouts the
+    // launches follow the per-tet kernel on its stream with programmatic dependencies (edge rows,
+    // then vertex rows); otherwise the two ranges run concurrently (the vertex range on a side
+    // stream) so that the tail of one overlaps the other.
+    const bool seq = ASM_SEQ && gram && h->ring_enabled && !touched && !(h->has_dirichlet && h->bc_nonzero) &&
+                     (h->nloc_s == 4 || h->ring_ok) && h->vrec;
+    cudaStream_t side = h->side_stream && !seq ? h->side_stream : h->stream;
+    h->asm_pdl = seq;
     if (side != h->stream) {
         ANI_CUDA(h, cudaEventRecord(h->fork_ev, h->stream));
         ANI_CUDA(h, cudaStreamWaitEvent(side, h->fork_ev, 0));
     }
-    for (int rg = 0; rg < 2; ++rg) {
+    for (int it = 0; it < 2; ++it) {
+        const int rg = seq ? 1 - it : it;
         p.row_begin = h->row_range[rg];
         p.nrows = h->row_range[rg + 1];
         p.cap = h->row_range_cap[rg];
@@ -2297,8 +2344,12 @@ int run_assemble(anigpu_ctx* h, int kind, const double* D, const double* f, doub
                 rc = f32 ? launch_rows<float, 4, 1>(h, p, tables, vals, rhs, touched, st)
                          : launch_rows<double, 4, 1>(h, p, tables, vals, rhs, touched, st);
         }
-        if (rc) return rc;
+        if (rc) {
+            h->asm_pdl = false;
+            return rc;
+        }
     }
+    h->asm_pdl = false;
     if (side != h->stream) {
         ANI_CUDA(h, cudaEventRecord(h->join_ev, side));
         ANI_CUDA(h, cudaStreamWaitEvent(h->stream, h->join_ev, 0));

@@ -452,6 +452,9 @@ __global__ void __launch_bounds__(256) combine4_kernel(int64_t nc, const int64_t
     }
 }
 
+#ifndef PROLONG_U
+#define PROLONG_U 4
+#endif
 // z = D^-1 r + P c ; block partials of r.z and z.qold (FP32 per thread, FP64 across the block)
 __global__ void __launch_bounds__(256) prolong_dot_kernel(int64_t nf, CMap m, const float* __restrict__ r,
                                                           const float* __restrict__ diag_f,
@@ -463,21 +466,49 @@ __global__ void __launch_bounds__(256) prolong_dot_kernel(int64_t nf, CMap m, co
     __shared__ double sh[32];
     if (stop && *stop) return;
     float arz = 0.f, azq = 0.f;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nf; i += (int64_t)gridDim.x * blockDim.x) {
-        const float d = diag_f[i];
-        const float ri = r[i];
-        float zi = d != 0.f ? ri / d : ri;
-        const int comp = m.comp_fine(i);
-        const int64_t s = i - comp * m.nds;
-        const float* cc = c + comp * m.nv;
-        if (s < m.nv) zi += cc[s];
-        else {
-            const int64_t e = s - m.nv;
-            zi = fmaf(0.5f, cc[ends[2 * e]] + cc[ends[2 * e + 1]], zi);
+    // PROLONG_U DOFs per thread and pass, their loads issued together (the edge DOFs' coarse values
+    // are a two-level gather: end vertices, then their corrections)
+    constexpr int U = PROLONG_U;
+    const int64_t S = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i0 < nf; i0 += U * S) {
+        float ri[U], zi[U], ca[U], cb[U];
+        int64_t ia[U], ib[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int64_t i = i0 + u * S;
+            ia[u] = -1;
+            ib[u] = -1;
+            ri[u] = 0.f;
+            zi[u] = 0.f;
+            if (i < nf) {
+                const float d = diag_f[i];
+                ri[u] = r[i];
+                zi[u] = d != 0.f ? ri[u] / d : ri[u];
+                const int comp = m.comp_fine(i);
+                const int64_t s = i - comp * m.nds;
+                if (s < m.nv) ia[u] = comp * m.nv + s;
+                else {
+                    const int2 e = reinterpret_cast<const int2*>(ends)[s - m.nv];
+                    ia[u] = comp * m.nv + e.x;
+                    ib[u] = comp * m.nv + e.y;
+                }
+            }
         }
-        z[i] = zi;
-        arz = fmaf(ri, zi, arz);
-        if (qold) azq = fmaf(zi, qold[i], azq);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            ca[u] = ia[u] >= 0 ? c[ia[u]] : 0.f;
+            cb[u] = ib[u] >= 0 ? c[ib[u]] : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int64_t i = i0 + u * S;
+            if (i < nf) {
+                const float zz = ib[u] < 0 ? zi[u] + ca[u] : fmaf(0.5f, ca[u] + cb[u], zi[u]);
+                z[i] = zz;
+                arz = fmaf(ri[u], zz, arz);
+                if (qold) azq = fmaf(zz, qold[i], azq);
+            }
+        }
     }
     double a = arz, b = azq;
 #pragma unroll
@@ -569,13 +600,17 @@ __device__ __forceinline__ float chain_spmv(const ChainArgs& a, int64_t v, const
     return acc;
 }
 
-// threads per block of the chain: large blocks, few arrivals per barrier
+// threads per block of the chain: large blocks, few arrivals per barrier; two blocks per SM (32
+// registers) so that every coarse row has its own thread at 64^3
 #ifndef CHAIN_THREADS
 #define CHAIN_THREADS 1024
 #endif
+#ifndef CHAIN_MINB
+#define CHAIN_MINB 2
+#endif
 constexpr int kChainThreads = CHAIN_THREADS;
 
-__global__ void __launch_bounds__(kChainThreads) coarse_chain_kernel(ChainArgs a) {
+__global__ void __launch_bounds__(kChainThreads, CHAIN_MINB) coarse_chain_kernel(ChainArgs a) {
     if (a.stop && *a.stop) return;  // the same value for every block: no barrier is entered
     if (((volatile unsigned int*)a.bar)[2]) {  // an earlier launch's wait expired: the barrier is unusable
         for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < a.nc; v += (int64_t)gridDim.x * blockDim.x)
