@@ -971,12 +971,18 @@ __global__ void ROW_BOUNDS edge_ring_kernel(RowParams p, const uint2* __restrict
     pdl_launch_dependents();
 }
 
+#ifdef VILV_MINB
+#define VILV_BOUNDS __launch_bounds__(64, VILV_MINB)
+#else
+#define VILV_BOUNDS __launch_bounds__(64)
+#endif
+
 // Vertex rows (Gram form) from lane-interleaved records: record j of lane l of warp w at
 // vrec[woff[w] + 32 j + l], so a warp reads one contiguous 512-byte range per step instead of 32
 // scattered records.  The diagonal (every incident tet) is summed in a register and written once;
 // the other columns of an element row are added into the shared-memory row as in row_gather_kernel.
 template <typename Real, int NLOC, bool DIR, bool DROPCHK>
-__global__ void ROW_BOUNDS vertex_ilv_kernel(RowParams p, const ScatterRec* __restrict__ vrec,
+__global__ void VILV_BOUNDS vertex_ilv_kernel(RowParams p, const ScatterRec* __restrict__ vrec,
                                              const int64_t* __restrict__ woff, const Real* __restrict__ tetK,
                                              Real* __restrict__ vals, double* __restrict__ rhs,
                                              int* __restrict__ status) {
