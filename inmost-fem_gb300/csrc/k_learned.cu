@@ -21,12 +21,13 @@
 #include <cmath>
 #include <vector>
 
+#include "coarse_chain.cuh"
 #include "learned.h"
 
 namespace {
 
 constexpr int C = 64;           // hidden channels
-constexpr int K = 4;            // polynomial terms of B (A_hat^0 .. A_hat^3)
+constexpr int K = kChainK;     // polynomial terms of B (A_hat^0 .. A_hat^3)
 constexpr int NF = 2;           // input features
 constexpr int kMaxLayers = 8;
 constexpr int kBlk = 256;
@@ -48,24 +49,6 @@ template <>
 __device__ __forceinline__ __nv_bfloat16 cvt<__nv_bfloat16>(float v) {
     return __float2bfloat16_rn(v);
 }
-
-// coarse nodes are the vertex DOFs of every component: coarse id c*nv + v <-> fine DOF c*nds + v
-// (scalar P2: nds = ndof and the two numberings agree); fine DOF c*nds + nv + e is edge e of
-// component c.  At most 3 components, so the component is found by two compares.
-struct CMap {
-    int64_t nv, nds;
-    __device__ __forceinline__ int comp_fine(int64_t d) const { return d >= nds ? (d >= 2 * nds ? 2 : 1) : 0; }
-    __device__ __forceinline__ int comp_coarse(int64_t cid) const { return cid >= nv ? (cid >= 2 * nv ? 2 : 1) : 0; }
-    __device__ __forceinline__ int64_t fine_of(int64_t cid) const {
-        const int c = comp_coarse(cid);
-        return c * nds + (cid - c * nv);
-    }
-    __device__ __forceinline__ int64_t coarse_of(int64_t d) const {
-        const int c = comp_fine(d);
-        const int64_t s = d - c * nds;
-        return s < nv ? c * nv + s : -1;
-    }
-};
 
 struct Gnn {
     int layers = 4, act = ANIGPU_BF16;  // act: ANIGPU_F32 or ANIGPU_BF16
@@ -452,9 +435,6 @@ __global__ void __launch_bounds__(256) combine4_kernel(int64_t nc, const int64_t
     }
 }
 
-#ifndef PROLONG_U
-#define PROLONG_U 4
-#endif
 // z = D^-1 r + P c ; block partials of r.z and z.qold (FP32 per thread, FP64 across the block)
 __global__ void __launch_bounds__(256) prolong_dot_kernel(int64_t nf, CMap m, const float* __restrict__ r,
                                                           const float* __restrict__ diag_f,
@@ -466,50 +446,9 @@ __global__ void __launch_bounds__(256) prolong_dot_kernel(int64_t nf, CMap m, co
     __shared__ double sh[32];
     if (stop && *stop) return;
     float arz = 0.f, azq = 0.f;
-    // PROLONG_U DOFs per thread and pass, their loads issued together (the edge DOFs' coarse values
-    // are a two-level gather: end vertices, then their corrections)
-    constexpr int U = PROLONG_U;
-    const int64_t S = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i0 < nf; i0 += U * S) {
-        float ri[U], zi[U], ca[U], cb[U];
-        int64_t ia[U], ib[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const int64_t i = i0 + u * S;
-            ia[u] = -1;
-            ib[u] = -1;
-            ri[u] = 0.f;
-            zi[u] = 0.f;
-            if (i < nf) {
-                const float d = diag_f[i];
-                ri[u] = r[i];
-                zi[u] = d != 0.f ? ri[u] / d : ri[u];
-                const int comp = m.comp_fine(i);
-                const int64_t s = i - comp * m.nds;
-                if (s < m.nv) ia[u] = comp * m.nv + s;
-                else {
-                    const int2 e = reinterpret_cast<const int2*>(ends)[s - m.nv];
-                    ia[u] = comp * m.nv + e.x;
-                    ib[u] = comp * m.nv + e.y;
-                }
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            ca[u] = ia[u] >= 0 ? c[ia[u]] : 0.f;
-            cb[u] = ib[u] >= 0 ? c[ib[u]] : 0.f;
-        }
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const int64_t i = i0 + u * S;
-            if (i < nf) {
-                const float zz = ib[u] < 0 ? zi[u] + ca[u] : fmaf(0.5f, ca[u] + cb[u], zi[u]);
-                z[i] = zz;
-                arz = fmaf(ri[u], zz, arz);
-                if (qold) azq = fmaf(zz, qold[i], azq);
-            }
-        }
-    }
+    const ProlongArgs pa{nf, m, diag_f, c, ends};
+    prolong_rows(pa, r, z, qold, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, (int64_t)gridDim.x * blockDim.x, arz,
+                 azq);
     double a = arz, b = azq;
 #pragma unroll
     for (int o = 16; o; o >>= 1) {
@@ -535,71 +474,7 @@ __global__ void __launch_bounds__(256) prolong_dot_kernel(int64_t nf, CMap m, co
 // ------------------------------------------------------------ fused coarse chain (one cooperative launch)
 // The coarse part of M r as one kernel: restriction, the three Horner products, the two powers and
 // the combination (the work of restrict_scale, cspmv4 x 5 and combine4 above), separated by grid
-// barriers instead of kernel boundaries.  One thread per coarse row; the coarse graph is read in
-// 32-row slices (coalesced column and value loads).  The barrier waits are bounded: a wait that
-// expires records ANIGPU_ERR_TIMEOUT in *status and poisons the correction with NaN, which the
-// solver treats as a breakdown (Jacobi for the rest of the solve); no wait can hang.
-struct ChainArgs {
-    int64_t nc;
-    CMap map;
-    const float* r;
-    const int64_t* vrow;
-    const int32_t* vedge;
-    const float* isd;
-    const float* coef;
-    const int64_t* sbase;
-    const int32_t* scol;
-    const float* sval;
-    float *u, *t0, *t1, *pw, *cc;
-    unsigned int* bar;
-    int* status;
-    const int* stop;
-};
-
-constexpr unsigned kBarrierSpins = 1u << 22;  // ~0.3 s of 64-ns sleeps
-
-// all blocks of the (co-resident) grid: returns false when the wait expired
-__device__ __forceinline__ bool chain_barrier(unsigned int* bar, int* status) {
-    __shared__ int ok;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        ok = 1;
-        volatile unsigned int* gen = bar + 1;
-        const unsigned int g0 = *gen;
-        __threadfence();
-        if (atomicAdd(bar, 1u) + 1u == gridDim.x) {
-            bar[0] = 0u;
-            __threadfence();
-            atomicAdd(bar + 1, 1u);
-        } else {
-            unsigned int spins = 0;
-            while (*gen == g0) {
-                if (++spins > kBarrierSpins) {
-                    atomicExch(status, ANIGPU_ERR_TIMEOUT);
-                    atomicExch(bar + 2, 1u);
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(64);
-            }
-        }
-        __threadfence();
-    }
-    __syncthreads();
-    return ok != 0;
-}
-
-// row v of A_hat x from the slices (padding entries: column v, value 0)
-__device__ __forceinline__ float chain_spmv(const ChainArgs& a, int64_t v, const float* __restrict__ x) {
-    const int64_t s = v >> 5;
-    const int64_t b = a.sbase[s], e = a.sbase[s + 1];
-    const int lane = (int)(v & 31);
-    float acc = 0.f;
-#pragma unroll 4
-    for (int64_t q = b + lane; q < e; q += 32) acc = fmaf(a.sval[q], x[a.scol[q]], acc);
-    return acc;
-}
-
+// barriers instead of kernel boundaries (chain_stages, coarse_chain.cuh).
 // threads per block of the chain: large blocks, few arrivals per barrier; two blocks per SM (32
 // registers) so that every coarse row has its own thread at 64^3
 #ifndef CHAIN_THREADS
@@ -612,48 +487,12 @@ constexpr int kChainThreads = CHAIN_THREADS;
 
 __global__ void __launch_bounds__(kChainThreads, CHAIN_MINB) coarse_chain_kernel(ChainArgs a) {
     if (a.stop && *a.stop) return;  // the same value for every block: no barrier is entered
-    if (((volatile unsigned int*)a.bar)[2]) {  // an earlier launch's wait expired: the barrier is unusable
+    if (barrier_expired(a.bar)) {  // an earlier launch's wait expired: the barrier is unusable
         for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < a.nc; v += (int64_t)gridDim.x * blockDim.x)
             a.cc[v] = __int_as_float(0x7fc00000);
         return;
     }
-    const int64_t nthr = (int64_t)gridDim.x * blockDim.x;
-    const int64_t t0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    bool ok = true;
-    // u = Dc^-1/2 P^T r ; t0 = a_3 u
-    for (int64_t v = t0; v < a.nc; v += nthr) {
-        const int c = a.map.comp_coarse(v);
-        const int64_t vs = v - c * a.map.nv;
-        const float* rc = a.r + c * a.map.nds;
-        float sum = 0.f;
-        for (int64_t k = a.vrow[vs]; k < a.vrow[vs + 1]; ++k) sum += rc[a.vedge[k]];
-        const float uu = a.isd[v] * fmaf(0.5f, sum, rc[vs]);
-        a.u[v] = uu;
-        a.t0[v] = a.coef[K * v + K - 1] * uu;
-    }
-    // Horner: t <- A_hat t + a_k u, k = 2, 1, 0 (the last into pw[0])
-    const float* src = a.t0;
-    for (int k = K - 2; k >= 0; --k) {
-        ok &= chain_barrier(a.bar, a.status);
-        float* dst = k == 0 ? a.pw : (src == a.t0 ? a.t1 : a.t0);
-        for (int64_t v = t0; v < a.nc; v += nthr) dst[v] = fmaf(a.coef[K * v + k], a.u[v], chain_spmv(a, v, src));
-        src = dst;
-    }
-    // powers P_k = A_hat P_{k-1}, k = 1, 2
-    for (int k = 1; k <= K - 2; ++k) {
-        ok &= chain_barrier(a.bar, a.status);
-        const float* x = a.pw + (int64_t)(k - 1) * a.nc;
-        float* y = a.pw + (int64_t)k * a.nc;
-        for (int64_t v = t0; v < a.nc; v += nthr) y[v] = chain_spmv(a, v, x);
-    }
-    // P_3 = A_hat P_2 ; c = isd .* sum_k a_k P_k
-    ok &= chain_barrier(a.bar, a.status);
-    for (int64_t v = t0; v < a.nc; v += nthr) {
-        float sum = a.coef[K * v + K - 1] * chain_spmv(a, v, a.pw + (int64_t)(K - 2) * a.nc);
-#pragma unroll
-        for (int k = K - 2; k >= 0; --k) sum = fmaf(a.coef[K * v + k], a.pw[(int64_t)k * a.nc + v], sum);
-        a.cc[v] = ok ? a.isd[v] * sum : __int_as_float(0x7fc00000);
-    }
+    chain_stages(a, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, (int64_t)gridDim.x * blockDim.x);
 }
 
 // slices: 32 x (the longest row of each 32-row slice) entries
