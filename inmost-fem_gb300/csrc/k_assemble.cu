@@ -812,9 +812,15 @@ constexpr int kRingMax = 32;  // incident tets of an edge that the ring build ta
 #define RING_UNROLL 4
 #endif
 constexpr int kRingUnroll = RING_UNROLL;
+// FP32: sixteen 64-thread blocks per SM (64 registers; a few bytes of spill) for more loads in
+// flight; FP64 keeps its registers
+#ifndef RING_MINB
+#define RING_MINB 16
+#endif
+#define RING_BOUNDS __launch_bounds__(64, sizeof(Real) == 4 ? RING_MINB : 1)
 
 template <typename Real, bool DIR, bool DROPCHK>
-__global__ void ROW_BOUNDS edge_ring_kernel(RowParams p, const uint2* __restrict__ ring,
+__global__ void RING_BOUNDS edge_ring_kernel(RowParams p, const uint2* __restrict__ ring,
                                             const int64_t* __restrict__ woff, const Real* __restrict__ tetK,
                                             Real* __restrict__ vals, double* __restrict__ rhs,
                                             int* __restrict__ status) {
