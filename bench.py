@@ -906,7 +906,7 @@ def run_ours(args):
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                      "traffic": traffic, "peak_kind": peak_kind,
-                     "kernel": "assembly = tet_gram + row_gather (vertex rows) + edge-row gather: 3 launches, "
+                     "kernel": "assembly = tet_gram + vertex-row gather + edge-row gather: 3 launches, "
                                "timed back to back in the timed region",
                      "edge_rows": edge_rows,
                      "algorithmic_bytes": b_alg, "ms": {"tet_prepare": prep_ms, "row_gather": rows_ms},
