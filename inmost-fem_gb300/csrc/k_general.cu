@@ -38,7 +38,6 @@
 namespace {
 
 constexpr int kNode = 0, kEdge = 1, kFace = 2, kCell = 3;
-constexpr int kMaxLoc = 20;
 
 // DOFs per entity type (node, edge, face, cell) and local DOFs per tet
 struct SpaceLayout {
@@ -554,7 +553,6 @@ int general_assemble(anigpu_ctx* h, int opA, int opB, int kind, const double* D,
     if (opA / 10 != w->space || opB / 10 != w->space)
         return set_err(h, ANIGPU_ERR_ARG, "operators must act on the problem's space");
     if (!vals) return set_err(h, ANIGPU_ERR_ARG, "NULL values");
-    cudaStream_t s = h->stream;
     const int64_t nt = h->nt, nloc = w->nloc;
     RC_(dev_alloc(h, &w->A, (size_t)nt * nloc * nloc));
     RC_(launch_fem3dtet(h, opA, opB, kind, order, ANIGPU_F64, nt, w->XY, D, w->A));

@@ -968,8 +968,8 @@ __global__ void reduce_parts_kernel(int n, int nb, int64_t stride, const float* 
 }
 
 // ------------------------------------------------------------ loss pieces
-__global__ void sub_kernel(int64_t n, const double* __restrict__ a, const double* __restrict__ b,
-                           double* __restrict__ out) {
+// out = a - b elementwise (out may be a)
+__global__ void sub_kernel(int64_t n, const double* a, const double* __restrict__ b, double* out) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i < n) out[i] = a[i] - b[i];
 }
