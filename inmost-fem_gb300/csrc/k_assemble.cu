@@ -801,17 +801,13 @@ constexpr int kRingMax = 32;  // incident tets of an edge that the ring build ta
 #define ASM_SEQ 1
 #endif
 
-// prefetch depths of the ring gather (per-tet blocks, records) and its unroll, a multiple of both
+// prefetch depths of the ring gather (per-tet blocks, records)
 #ifndef RING_KD
 #define RING_KD 2
 #endif
 #ifndef RING_RD
 #define RING_RD 4
 #endif
-#ifndef RING_UNROLL
-#define RING_UNROLL 4
-#endif
-constexpr int kRingUnroll = RING_UNROLL;
 // FP32: sixteen 64-thread blocks per SM (64 registers; a few bytes of spill) for more loads in
 // flight; FP64 keeps its registers
 #ifndef RING_MINB
@@ -881,16 +877,13 @@ __global__ void RING_BOUNDS edge_ring_kernel(RowParams p, const uint2* __restric
     Real fP = Real(0), fAP = Real(0), fBP = Real(0);  // the first face of a closed ring
     uint32_t coff = hd.y;                             // offsets of the carried face's columns
     Real accA = Real(0), accB = Real(0), accE = Real(0), racc = Real(0);
-#pragma unroll kRingUnroll
-    for (int k = 0; k < nloop; ++k) {
-        KVec<Real, KS> Kn;
-        if (k + KD <= last) Kn.load(tetK + KS * (int64_t)(Rq[KD].x & kRingTetMask));
-        uint2 Rn = make_uint2(0u, 0u);
-        if (k + RD <= last) Rn = rr[32 * (k + RD + 1)];
-        const uint2 r0 = Rq[0];
+    // the walk with its prefetch in fixed slots (records of incidences k..k+3 in Rq[k % 4], blocks
+    // of k, k+1 in Kq[k % 2]), unrolled by four so that no slot is ever moved
+    static_assert(KD == 2 && RD == 4, "slot walk: two blocks and four records ahead");
+    auto blk = [&](const uint2 r) { return tetK + KS * (int64_t)(r.x & kRingTetMask); };
+    auto step = [&](const int k, const uint2 r0, const Real* G) {
         // the Gram entries of the edge (A, B) and of its four neighbours in the tet, in ring roles:
-        // local edge k = (a, b) with the other vertices c < d, then A = b if bit 30, P = d if bit 31
-        const Real* G = Kq[0].v;
+        // local edge le = (a, b) with the other vertices c < d, then A = b if bit 30, P = d if bit 31
         const int le = (int)((r0.x >> 27) & 7u);
         const Real gab = le == 0 ? G[0] : le == 1 ? G[1] : le == 2 ? G[2] : le == 3 ? G[3] : le == 4 ? G[4] : G[5];
         const Real gac = (le == 0 || le == 5) ? G[1] : G[0];
@@ -938,13 +931,31 @@ __global__ void RING_BOUNDS edge_ring_kernel(RowParams p, const uint2* __restric
         cAP = vAN;
         cBP = vBN;
         coff = r0.y;
-#pragma unroll
-        for (int j = 0; j + 1 < KD; ++j) Kq[j] = Kq[j + 1];
-        Kq[KD - 1] = Kn;
-#pragma unroll
-        for (int j = 0; j + 1 < RD; ++j) Rq[j] = Rq[j + 1];
-        Rq[RD - 1] = Rn;
+    };
+    int k = 0;
+    for (; k + 4 <= nloop; k += 4) {
+        step(k, Rq[0], Kq[0].v);
+        if (k + 2 <= last) Kq[0].load(blk(Rq[2]));
+        if (k + 4 <= last) Rq[0] = rr[32 * (k + 5)];
+        step(k + 1, Rq[1], Kq[1].v);
+        if (k + 3 <= last) Kq[1].load(blk(Rq[3]));
+        if (k + 5 <= last) Rq[1] = rr[32 * (k + 6)];
+        step(k + 2, Rq[2], Kq[0].v);
+        if (k + 4 <= last) Kq[0].load(blk(Rq[0]));
+        if (k + 6 <= last) Rq[2] = rr[32 * (k + 7)];
+        step(k + 3, Rq[3], Kq[1].v);
+        if (k + 5 <= last) Kq[1].load(blk(Rq[1]));
+        if (k + 7 <= last) Rq[3] = rr[32 * (k + 8)];
     }
+    if (k < nloop) {
+        step(k, Rq[0], Kq[0].v);
+        if (k + 2 <= last) Kq[0].load(blk(Rq[2]));
+    }
+    if (k + 1 < nloop) {
+        step(k + 1, Rq[1], Kq[1].v);
+        if (k + 3 <= last) Kq[1].load(blk(Rq[3]));
+    }
+    if (k + 2 < nloop) step(k + 2, Rq[2], Kq[0].v);
     bool bad = false;
     if (valid) {
         double F;
