@@ -808,6 +808,9 @@ constexpr int kRingMax = 32;  // incident tets of an edge that the ring build ta
 #ifndef RING_RD
 #define RING_RD 4
 #endif
+#ifndef RING_U
+#define RING_U 4
+#endif
 // FP32: sixteen 64-thread blocks per SM (64 registers; a few bytes of spill) for more loads in
 // flight; FP64 keeps its registers
 #ifndef RING_MINB
@@ -877,10 +880,10 @@ __global__ void RING_BOUNDS edge_ring_kernel(RowParams p, const uint2* __restric
     Real fP = Real(0), fAP = Real(0), fBP = Real(0);  // the first face of a closed ring
     uint32_t coff = hd.y;                             // offsets of the carried face's columns
     Real accA = Real(0), accB = Real(0), accE = Real(0), racc = Real(0);
-    // the walk with its prefetch in fixed slots (records of incidences k..k+3 in Rq[k % 4], blocks
-    // of k, k+1 in Kq[k % 2]), unrolled by four so that no slot is ever moved
-    static_assert(KD == 2 && RD == 4, "slot walk: two blocks and four records ahead");
-    auto blk = [&](const uint2 r) { return tetK + KS * (int64_t)(r.x & kRingTetMask); };
+    // the walk with its prefetch in fixed slots (blocks of incidences k.. in Kq[k % KD], records in
+    // Rq[k % RD]), unrolled by RING_U (a multiple of both) so that no prefetched value is moved
+    constexpr int U = RING_U;
+    static_assert(U % KD == 0 && U % RD == 0, "slot walk");
     auto step = [&](const int k, const uint2 r0, const Real* G) {
         // the Gram entries of the edge (A, B) and of its four neighbours in the tet, in ring roles:
         // local edge le = (a, b) with the other vertices c < d, then A = b if bit 30, P = d if bit 31
@@ -933,29 +936,21 @@ __global__ void RING_BOUNDS edge_ring_kernel(RowParams p, const uint2* __restric
         coff = r0.y;
     };
     int k = 0;
-    for (; k + 4 <= nloop; k += 4) {
-        step(k, Rq[0], Kq[0].v);
-        if (k + 2 <= last) Kq[0].load(blk(Rq[2]));
-        if (k + 4 <= last) Rq[0] = rr[32 * (k + 5)];
-        step(k + 1, Rq[1], Kq[1].v);
-        if (k + 3 <= last) Kq[1].load(blk(Rq[3]));
-        if (k + 5 <= last) Rq[1] = rr[32 * (k + 6)];
-        step(k + 2, Rq[2], Kq[0].v);
-        if (k + 4 <= last) Kq[0].load(blk(Rq[0]));
-        if (k + 6 <= last) Rq[2] = rr[32 * (k + 7)];
-        step(k + 3, Rq[3], Kq[1].v);
-        if (k + 5 <= last) Kq[1].load(blk(Rq[1]));
-        if (k + 7 <= last) Rq[3] = rr[32 * (k + 8)];
+    for (; k + U <= nloop; k += U) {
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            step(k + u, Rq[u % RD], Kq[u % KD].v);
+            if (k + u + KD <= last) Kq[u % KD].load(tetK + KS * (int64_t)(Rq[(u + KD) % RD].x & kRingTetMask));
+            if (k + u + RD <= last) Rq[u % RD] = rr[32 * (k + u + RD + 1)];
+        }
     }
-    if (k < nloop) {
-        step(k, Rq[0], Kq[0].v);
-        if (k + 2 <= last) Kq[0].load(blk(Rq[2]));
+#pragma unroll
+    for (int u = 0; u + 1 < U; ++u) {
+        if (k + u < nloop) {
+            step(k + u, Rq[u % RD], Kq[u % KD].v);
+            if (k + u + KD <= last) Kq[u % KD].load(tetK + KS * (int64_t)(Rq[(u + KD) % RD].x & kRingTetMask));
+        }
     }
-    if (k + 1 < nloop) {
-        step(k + 1, Rq[1], Kq[1].v);
-        if (k + 3 <= last) Kq[1].load(blk(Rq[3]));
-    }
-    if (k + 2 < nloop) step(k + 2, Rq[2], Kq[0].v);
     bool bad = false;
     if (valid) {
         double F;
@@ -988,6 +983,17 @@ __global__ void RING_BOUNDS edge_ring_kernel(RowParams p, const uint2* __restric
     pdl_launch_dependents();
 }
 
+// vertex rows: per-tet blocks four incidences ahead, records eight (127 registers, eight 64-thread
+// blocks per SM: the loads in flight per warp matter more than the warps)
+#ifndef VILV_KD
+#define VILV_KD 4
+#endif
+#ifndef VILV_RD
+#define VILV_RD 8
+#endif
+#ifndef VILV_U
+#define VILV_U 8
+#endif
 #ifdef VILV_MINB
 #define VILV_BOUNDS __launch_bounds__(64, VILV_MINB)
 #else
@@ -1038,7 +1044,10 @@ __global__ void VILV_BOUNDS vertex_ilv_kernel(RowParams p, const ScatterRec* __r
     const Real drop = Real(p.drop);
     const int nloop = isdir ? 0 : deg;
     const int last = nloop - 1;
-    constexpr int KD = ROW_KD, RD = ROW_RD;
+    // the walk with its prefetch in fixed slots (blocks of incidences k.. in Kq[k % KD], records in
+    // Rq[k % RD]), unrolled by U (a multiple of both) so that no prefetched value is moved
+    constexpr int KD = VILV_KD, RD = VILV_RD, U = VILV_U;
+    static_assert(RD > KD && U % KD == 0 && U % RD == 0, "slot walk");
     KVec<Real, KS> Kq[KD];
     ScatterRec Rq[RD];
 #pragma unroll
@@ -1056,15 +1065,9 @@ __global__ void VILV_BOUNDS vertex_ilv_kernel(RowParams p, const ScatterRec* __r
     int odiag = 0;
     if (deg > 0) odiag = (int)((isdir ? rr[0].off03 : Rq[0].off03) & 255u);
     Real accD = Real(0), racc = Real(0);
-#pragma unroll kRowUnroll
-    for (int k = 0; k < nloop; ++k) {
-        KVec<Real, KS> Kn;
-        if (k + KD <= last) Kn.load(tetK + KS * (int64_t)Rq[KD].tet);
-        ScatterRec Rn = ScatterRec{0u, 0u, 0u, 0u};
-        if (k + RD <= last) Rn = rr[32 * (k + RD)];
-        const ScatterRec r0 = Rq[0];
+    auto step = [&](const ScatterRec r0, const Real* G) {
         Real a[NLOC];
-        const Real F = gram_row<Real, NLOC, 1>(Kq[0].v, (int)(r0.meta & 15u), a);
+        const Real F = gram_row<Real, NLOC, 1>(G, (int)(r0.meta & 15u), a);
         if (DROPCHK) {
 #pragma unroll
             for (int j = 0; j < NLOC; ++j) a[j] = fabs(a[j]) > drop ? a[j] : Real(0);
@@ -1081,12 +1084,22 @@ __global__ void VILV_BOUNDS vertex_ilv_kernel(RowParams p, const ScatterRec* __r
         }
 #pragma unroll
         for (int j = 1; j < NLOC; ++j) myRow[o[j]] = cur[j] + a[j];
+    };
+    int k = 0;
+    for (; k + U <= nloop; k += U) {
 #pragma unroll
-        for (int j = 0; j + 1 < KD; ++j) Kq[j] = Kq[j + 1];
-        Kq[KD - 1] = Kn;
+        for (int u = 0; u < U; ++u) {
+            step(Rq[u % RD], Kq[u % KD].v);
+            if (k + u + KD <= last) Kq[u % KD].load(tetK + KS * (int64_t)Rq[(u + KD) % RD].tet);
+            if (k + u + RD <= last) Rq[u % RD] = rr[32 * (k + u + RD)];
+        }
+    }
 #pragma unroll
-        for (int j = 0; j + 1 < RD; ++j) Rq[j] = Rq[j + 1];
-        Rq[RD - 1] = Rn;
+    for (int u = 0; u + 1 < U; ++u) {
+        if (k + u < nloop) {
+            step(Rq[u % RD], Kq[u % KD].v);
+            if (k + u + KD <= last) Kq[u % KD].load(tetK + KS * (int64_t)Rq[(u + KD) % RD].tet);
+        }
     }
     bool bad = false;
     if (valid) {
