@@ -1396,6 +1396,20 @@ __global__ void tet_lame_f32_kernel(int64_t nt, const double* __restrict__ xyz, 
     for (int q = 0; q < 4; ++q) o[q] = make_float4(B[4 * q], B[4 * q + 1], B[4 * q + 2], B[4 * q + 3]);
 }
 
+// prefetch depths of the vector gathers (16-value per-tet blocks, records)
+#ifndef VEC_KD
+#define VEC_KD 2
+#endif
+#ifndef VEC_RD
+#define VEC_RD 4
+#endif
+#ifndef VRING_KD
+#define VRING_KD 2
+#endif
+#ifndef VRING_RD
+#define VRING_RD 4
+#endif
+
 template <typename Real>
 struct VBlock {
     Real v[16];
@@ -1482,7 +1496,7 @@ __global__ void __launch_bounds__(64) vec_row_gather_kernel(RowParams p, int64_t
     Real racc = Real(0);
     const int nloop = isdir ? 0 : deg;
     const int last = nloop - 1;
-    constexpr int KD = 2, RD = 4;
+    constexpr int KD = VEC_KD, RD = VEC_RD;
     VBlock<Real> Kq[KD];
     ScatterRec Rq[RD];
 #pragma unroll
@@ -1687,7 +1701,7 @@ __global__ void __launch_bounds__(64) vec_edge_ring_kernel(RowParams p, int64_t 
     Real* myRow = sC + base;
     const int nloop = isdir ? 0 : deg;
     const int last = nloop - 1;
-    constexpr int KD = 2, RD = 4;
+    constexpr int KD = VRING_KD, RD = VRING_RD;
     VBlock<Real> Kq[KD];
     uint2 Rq[RD];
 #pragma unroll
