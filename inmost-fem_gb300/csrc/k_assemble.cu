@@ -800,6 +800,11 @@ constexpr int kRingMax = 32;  // incident tets of an edge that the ring build ta
 #ifndef ASM_SEQ
 #define ASM_SEQ 1
 #endif
+// with ASM_SEQ and P2: the vertex rows behind the per-tet kernel and the edge rows concurrently on
+// the side stream (1), or edge rows then vertex rows behind the per-tet kernel (0)
+#ifndef ASM_SPLIT
+#define ASM_SPLIT 1
+#endif
 
 // prefetch depths of the ring gather (per-tet blocks, records)
 #ifndef RING_KD
@@ -1122,6 +1127,7 @@ __global__ void VILV_BOUNDS vertex_ilv_kernel(RowParams p, const ScatterRec* __r
     const Real fin = write_out_range<Real>(sC, shift, clen, cbase, vals, p.vec_ok, lane);
     bad |= !isfinite(fin);
     if (bad) atomicExch(status, ANIGPU_ERR_NONFINITE);
+    pdl_launch_dependents();
 }
 
 // slots of each warp of 32 rows in a lane-interleaved layout: 32 x (head + its largest
@@ -2351,25 +2357,28 @@ int run_assemble(anigpu_ctx* h, int kind, const double* D, const double* f, doub
     p.dir_cptr = h->dir_cptr;
     p.dir_coff = h->dir_coff;
     // one launch per row range (vertex rows, edge rows) so that the shared-memory row
-    // buffer fits the longest row of that range.  With the ring and interleaved layouts the
-    // launches follow the per-tet kernel on its stream with programmatic dependencies (edge rows,
-    // then vertex rows); otherwise the two ranges run concurrently (the vertex range on a side
-    // stream) so that the tail of one overlaps the other.
+    // buffer fits the longest row of that range.  With the ring and interleaved layouts the vertex
+    // rows follow the per-tet kernel on its stream with a programmatic dependency and the edge rows
+    // run concurrently on the side stream: the vertex rows' long walks are dispatched first and the
+    // short edge-row blocks fill the SMs as they end (0.197 vs 0.205 ms per 64^3 FP32 assembly
+    // against edge rows then vertex rows on one stream).  Otherwise the two ranges run concurrently
+    // (the vertex range on the side stream) so that the tail of one overlaps the other.
     const bool seq = ASM_SEQ && gram && h->ring_enabled && !touched && !(h->has_dirichlet && h->bc_nonzero) &&
                      (h->nloc_s == 4 || h->ring_ok) && h->vrec;
-    cudaStream_t side = h->side_stream && !seq ? h->side_stream : h->stream;
-    h->asm_pdl = seq;
+    const bool split = seq && ASM_SPLIT && h->nloc_s == 10 && h->side_stream;
+    cudaStream_t side = h->side_stream && (!seq || split) ? h->side_stream : h->stream;
     if (side != h->stream) {
         ANI_CUDA(h, cudaEventRecord(h->fork_ev, h->stream));
         ANI_CUDA(h, cudaStreamWaitEvent(side, h->fork_ev, 0));
     }
     for (int it = 0; it < 2; ++it) {
-        const int rg = seq ? 1 - it : it;
+        const int rg = seq && !split ? 1 - it : it;
         p.row_begin = h->row_range[rg];
         p.nrows = h->row_range[rg + 1];
         p.cap = h->row_range_cap[rg];
         if (p.nrows <= p.row_begin) continue;
-        cudaStream_t st = rg == 0 ? side : h->stream;
+        cudaStream_t st = seq ? (split && rg == 1 ? side : h->stream) : (rg == 0 ? side : h->stream);
+        h->asm_pdl = seq && st == h->stream;
         const bool f32 = precision == ANIGPU_F32;
         if (h->nloc_s == 10) {
             if (!gram)
