@@ -99,11 +99,13 @@ struct anigpu_ctx {
     // per warp of 32 edge rows a header slot, then one 8-byte record per incident tet, lane-interleaved
     uint2* ring = nullptr;
     int64_t* ring_woff = nullptr;  // first slot of each warp (nwarps + 1)
+    int64_t ring_ws = 0;           // slots per warp when every warp has the same (else 0)
     bool ring_ok = false;          // every edge row of the mesh has a ring (else the record gather)
     bool ring_enabled = true;      // anigpu_set_gather_layouts: rings and interleaved vertex records
     // vertex rows' scatter records in the same lane-interleaved layout (no header)
     ScatterRec* vrec = nullptr;
     int64_t* vrec_woff = nullptr;
+    int64_t vrec_ws = 0;
     int max_row_len_s = 0;
     int64_t row_range[3] = {0, 0, 0};  // scalar rows [vertex DOFs | edge DOFs]
     int row_range_cap[2] = {0, 0};     // longest row of each range

@@ -364,6 +364,7 @@ struct RowParams {
     double drop;
     const int32_t* vcol;  // vector template columns (non-zero boundary values of the vector path)
     int bcnz;             // vector path: non-zero boundary values
+    int64_t wstride = 0;  // lane-interleaved records: slots per warp when uniform, else 0 (per-warp offsets)
 };
 
 
@@ -850,7 +851,7 @@ __global__ void RING_BOUNDS edge_ring_kernel(RowParams p, const uint2* __restric
     }
     const int64_t row = row0 + lane;
     const bool valid = row < p.nrows;
-    const uint2* rr = ring + woff[wg] + lane;
+    const uint2* rr = ring + (p.wstride > 0 ? wg * p.wstride : woff[wg]) + lane;
     int deg = 0, base = 0;
     bool isdir = false;
     uint2 hd = make_uint2(0u, 0u);
@@ -1036,7 +1037,7 @@ __global__ void VILV_BOUNDS vertex_ilv_kernel(RowParams p, const ScatterRec* __r
     }
     const int64_t row = row0 + lane;
     const bool valid = row < p.nrows;
-    const ScatterRec* rr = vrec + woff[wg] + lane;
+    const ScatterRec* rr = vrec + (p.wstride > 0 ? wg * p.wstride : woff[wg]) + lane;
     int deg = 0, base = 0;
     bool isdir = false;
     if (valid) {
@@ -1133,12 +1134,21 @@ __global__ void VILV_BOUNDS vertex_ilv_kernel(RowParams p, const ScatterRec* __r
 // slots of each warp of 32 rows in a lane-interleaved layout: 32 x (head + its largest
 // incident-tet count)
 __global__ void warp_slots_kernel(int64_t rb, int64_t re, int head, const int64_t* __restrict__ inc_ptr,
-                                  unsigned long long* __restrict__ cnt) {
+                                  unsigned long long* __restrict__ cnt, unsigned long long* __restrict__ cmax) {
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;  // blockDim: a multiple of 32
     const int64_t r = rb + t;
     const int deg = r < re ? (int)(inc_ptr[r + 1] - inc_ptr[r]) : 0;
     const int m = __reduce_max_sync(0xffffffffu, deg);
-    if ((threadIdx.x & 31) == 0 && rb + t < re) cnt[t >> 5] = 32ull * (unsigned long long)(m + head);
+    if ((threadIdx.x & 31) == 0 && rb + t < re) {
+        const unsigned long long c = 32ull * (unsigned long long)(m + head);
+        cnt[t >> 5] = c;
+        atomicMax(cmax, c);
+    }
+}
+
+__global__ void uniform_offsets_kernel(int64_t nw, int64_t ws, int64_t* __restrict__ woff) {
+    const int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (w <= nw) woff[w] = w * ws;
 }
 
 // vertex rows' records in the lane-interleaved layout: record j of row rb + 32 w + l at
@@ -1692,7 +1702,7 @@ __global__ void __launch_bounds__(64) vec_edge_ring_kernel(RowParams p, int64_t 
     const int64_t r = row0 + lane;
     const int64_t R = c * nds + r;
     const bool valid = r < p.nrows;
-    const uint2* rr = ring + woff[wg] + lane;
+    const uint2* rr = ring + (p.wstride > 0 ? wg * p.wstride : woff[wg]) + lane;
     int deg = 0, base = 0, L = 0;
     bool isdir = false;
     uint2 hd = make_uint2(0u, 0u);
@@ -2038,7 +2048,9 @@ static int launch_ring_t(anigpu_ctx* h, const RowParams& p, void* vals, double* 
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = h->asm_pdl ? 1 : 0;
-    ANI_CUDA(h, cudaLaunchKernelEx(&cfg, kern, p, (const uint2*)h->ring, (const int64_t*)h->ring_woff,
+    RowParams q = p;
+    q.wstride = h->ring_ws;
+    ANI_CUDA(h, cudaLaunchKernelEx(&cfg, kern, q, (const uint2*)h->ring, (const int64_t*)h->ring_woff,
                                    (const Real*)h->tetdata, (Real*)vals, rhs, h->d_status));
     ANI_LAUNCHED(h);
     return ANIGPU_OK;
@@ -2065,7 +2077,9 @@ static int launch_vilv_t(anigpu_ctx* h, const RowParams& p, void* vals, double* 
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = h->asm_pdl ? 1 : 0;
-    ANI_CUDA(h, cudaLaunchKernelEx(&cfg, kern, p, (const ScatterRec*)h->vrec, (const int64_t*)h->vrec_woff,
+    RowParams q = p;
+    q.wstride = h->vrec_ws;
+    ANI_CUDA(h, cudaLaunchKernelEx(&cfg, kern, q, (const ScatterRec*)h->vrec, (const int64_t*)h->vrec_woff,
                                    (const Real*)h->tetdata, (Real*)vals, rhs, h->d_status));
     ANI_LAUNCHED(h);
     return ANIGPU_OK;
@@ -2100,29 +2114,59 @@ static int launch_ring(anigpu_ctx* h, const RowParams& p, void* vals, double* rh
 }
 
 // lane-interleaved records of the vertex rows [0, row_range[1]) (P1: every row)
+#ifndef WS_UNIFORM
+#define WS_UNIFORM 1
+#endif
+
+// slots of the lane-interleaved layout of rows [rb, re) (head + incidences per lane, 32 lanes per
+// warp): per-warp offsets (*woff, nwarps + 1 entries) and the total.  When a uniform stride (every
+// warp the largest warp's slots) costs at most a quarter more slots, the offsets are w * stride and
+// *ws = stride: a warp then finds its records without loading its offset first.
+static int warp_layout(anigpu_ctx* h, int64_t rb, int64_t re, int head, int64_t** woff, int64_t* total,
+                       int64_t* ws) {
+    cudaStream_t s = h->stream;
+    const int64_t n = re - rb, nw = (n + 31) / 32;
+    *ws = 0;
+    unsigned long long* cnt = nullptr;  // nw counts, the scan's zero, the largest count
+    ANI_CUDA(h, cudaMallocAsync((void**)&cnt, sizeof(unsigned long long) * (nw + 2), s));
+    ANI_CUDA(h, cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * (nw + 2), s));
+    warp_slots_kernel<<<grid_for(n, 256), 256, 0, s>>>(rb, re, head, h->inc_ptr, cnt, cnt + nw + 1);
+    ANI_LAUNCHED(h);
+    int rc = dev_alloc(h, woff, (size_t)nw + 1);
+    if (!rc) rc = scan_counts(h, cnt, nw, *woff);
+    int64_t tot = 0;
+    unsigned long long mx = 0;
+    if (!rc) {
+        ANI_CUDA(h, cudaMemcpyAsync(&tot, *woff + nw, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+        ANI_CUDA(h, cudaMemcpyAsync(&mx, cnt + nw + 1, sizeof(mx), cudaMemcpyDeviceToHost, s));
+        ANI_CUDA(h, cudaStreamSynchronize(s));
+    }
+    ANI_CUDA(h, cudaFreeAsync(cnt, s));
+    if (rc) return rc;
+    if (WS_UNIFORM && nw * (int64_t)mx <= tot + tot / 4) {
+        uniform_offsets_kernel<<<grid_for(nw + 1, 256), 256, 0, s>>>(nw, (int64_t)mx, *woff);
+        ANI_LAUNCHED(h);
+        tot = nw * (int64_t)mx;
+        *ws = (int64_t)mx;
+    }
+    *total = tot;
+    return ANIGPU_OK;
+}
+
 static int setup_vertex_ilv(anigpu_ctx* h) {
     if (h->vrec) cudaFree(h->vrec);
     if (h->vrec_woff) cudaFree(h->vrec_woff);
     h->vrec = nullptr;
     h->vrec_woff = nullptr;
+    h->vrec_ws = 0;
     if (h->space != ANIGPU_P1 && h->space != ANIGPU_P2) return ANIGPU_OK;
     const int64_t rb = h->row_range[0], re = h->row_range[1];
     if (re <= rb) return ANIGPU_OK;
     cudaStream_t s = h->stream;
-    const int64_t n = re - rb, nw = (n + 31) / 32;
-    unsigned long long* cnt = nullptr;
-    ANI_CUDA(h, cudaMallocAsync((void**)&cnt, sizeof(unsigned long long) * (nw + 1), s));
-    ANI_CUDA(h, cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * (nw + 1), s));
-    warp_slots_kernel<<<grid_for(n, 256), 256, 0, s>>>(rb, re, 0, h->inc_ptr, cnt);
-    ANI_LAUNCHED(h);
-    int rc = dev_alloc(h, &h->vrec_woff, (size_t)nw + 1);
-    if (rc) return rc;
-    rc = scan_counts(h, cnt, nw, h->vrec_woff);
-    if (rc) return rc;
+    const int64_t n = re - rb;
     int64_t total = 0;
-    ANI_CUDA(h, cudaMemcpyAsync(&total, h->vrec_woff + nw, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-    ANI_CUDA(h, cudaStreamSynchronize(s));
-    ANI_CUDA(h, cudaFreeAsync(cnt, s));
+    int rc = warp_layout(h, rb, re, 0, &h->vrec_woff, &total, &h->vrec_ws);
+    if (rc) return rc;
     rc = dev_alloc(h, &h->vrec, (size_t)total);
     if (rc) return rc;
     ANI_CUDA(h, cudaMemsetAsync(h->vrec, 0, sizeof(ScatterRec) * (size_t)total, s));
@@ -2139,24 +2183,15 @@ int setup_row_layouts(anigpu_ctx* h) {
     if (h->ring_woff) cudaFree(h->ring_woff);
     h->ring = nullptr;
     h->ring_woff = nullptr;
+    h->ring_ws = 0;
     if ((h->space != ANIGPU_P2 && h->space != ANIGPU_VEC3_P2) || h->nt - 1 > (int64_t)kRingTetMask) return ANIGPU_OK;
     const int64_t rb = h->row_range[1], re = h->row_range[2];
     if (re <= rb) return ANIGPU_OK;
     cudaStream_t s = h->stream;
-    const int64_t n = re - rb, nw = (n + 31) / 32;
-    unsigned long long* cnt = nullptr;
-    ANI_CUDA(h, cudaMallocAsync((void**)&cnt, sizeof(unsigned long long) * (nw + 1), s));
-    ANI_CUDA(h, cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * (nw + 1), s));
-    warp_slots_kernel<<<grid_for(n, 256), 256, 0, s>>>(rb, re, 1, h->inc_ptr, cnt);
-    ANI_LAUNCHED(h);
-    rc = dev_alloc(h, &h->ring_woff, (size_t)nw + 1);
-    if (rc) return rc;
-    rc = scan_counts(h, cnt, nw, h->ring_woff);
-    if (rc) return rc;
+    const int64_t n = re - rb;
     int64_t total = 0;
-    ANI_CUDA(h, cudaMemcpyAsync(&total, h->ring_woff + nw, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-    ANI_CUDA(h, cudaStreamSynchronize(s));
-    ANI_CUDA(h, cudaFreeAsync(cnt, s));
+    rc = warp_layout(h, rb, re, 1, &h->ring_woff, &total, &h->ring_ws);
+    if (rc) return rc;
     rc = dev_alloc(h, &h->ring, (size_t)total);
     if (rc) return rc;
     ANI_CUDA(h, cudaMemsetAsync(h->ring, 0, sizeof(uint2) * (size_t)total, s));
@@ -2175,6 +2210,7 @@ int setup_row_layouts(anigpu_ctx* h) {
         cudaFree(h->ring_woff);
         h->ring = nullptr;
         h->ring_woff = nullptr;
+        h->ring_ws = 0;
         return ANIGPU_OK;
     }
     h->ring_ok = true;
@@ -2249,6 +2285,7 @@ static int run_assemble_vec(anigpu_ctx* h, int kind, const double* D, const doub
     p.dir_coff = h->dir_coff;
     p.vcol = h->col;
     p.bcnz = h->bc_nonzero ? 1 : 0;
+    p.wstride = h->ring_ws;
     cudaStream_t side = h->side_stream ? h->side_stream : h->stream;
     if (side != h->stream) {
         ANI_CUDA(h, cudaEventRecord(h->fork_ev, h->stream));
