@@ -2272,7 +2272,7 @@ static int run_assemble_vec(anigpu_ctx* h, int kind, const double* D, const doub
                                                                        (double*)h->tetdata, h->d_status);
     ANI_LAUNCHED(h);
     time_mark(h, 1);
-    RowParams p;
+    RowParams p{};
     p.inc_ptr = h->inc_ptr;
     p.recs = h->recs;
     p.rowptr = h->rowptr_s;
@@ -2382,7 +2382,7 @@ int run_assemble(anigpu_ctx* h, int kind, const double* D, const double* f, doub
     }
     ANI_LAUNCHED(h);
     time_mark(h, 1);
-    RowParams p;
+    RowParams p{};
     p.inc_ptr = h->inc_ptr;
     p.recs = h->recs;
     p.rowptr = h->rowptr_s;
