@@ -801,6 +801,14 @@ constexpr int kRingMax = 32;  // incident tets of an edge that the ring build ta
 #ifndef ASM_SEQ
 #define ASM_SEQ 1
 #endif
+// the lane-interleaved layouts end in kRecPad slots of padding, so that a walk's first records
+// are loaded without waiting for the row's incidence count (1): slots past the lane's own records
+// belong to other lanes or to the padding and are never used; or only the lane's own (0)
+#ifndef REC_AHEAD
+#define REC_AHEAD 1
+#endif
+constexpr int64_t kRecPad = 32 * 16;  // prefetch depths below 16
+
 // with ASM_SEQ and P2: the vertex rows behind the per-tet kernel and the edge rows concurrently on
 // the side stream (1), or edge rows then vertex rows behind the per-tet kernel (0)
 #ifndef ASM_SPLIT
@@ -868,6 +876,7 @@ __global__ void RING_BOUNDS edge_ring_kernel(RowParams p, const uint2* __restric
     const int last = nloop - 1;
     constexpr int KD = RING_KD, RD = RING_RD;
     static_assert(RD > KD, "records must run ahead of the blocks they address");
+    static_assert(RD < 16, "the first records may reach RD slots past the lane's own (kRecPad)");
     KVec<Real, KS> Kq[KD];
     uint2 Rq[RD];
 #pragma unroll
@@ -876,7 +885,7 @@ __global__ void RING_BOUNDS edge_ring_kernel(RowParams p, const uint2* __restric
     for (int j = 0; j < RD; ++j) Rq[j] = make_uint2(0u, 0u);
 #pragma unroll
     for (int j = 0; j < RD; ++j)
-        if (j <= last) Rq[j] = rr[32 * (j + 1)];
+        if (REC_AHEAD || j <= last) Rq[j] = rr[32 * (j + 1)];
     pdl_wait();  // the per-tet blocks of this assembly
 #pragma unroll
     for (int j = 0; j < KD; ++j)
@@ -1054,6 +1063,7 @@ __global__ void VILV_BOUNDS vertex_ilv_kernel(RowParams p, const ScatterRec* __r
     // Rq[k % RD]), unrolled by U (a multiple of both) so that no prefetched value is moved
     constexpr int KD = VILV_KD, RD = VILV_RD, U = VILV_U;
     static_assert(RD > KD && U % KD == 0 && U % RD == 0, "slot walk");
+    static_assert(RD <= 16, "the first records may reach RD - 1 slots past the lane's own (kRecPad)");
     KVec<Real, KS> Kq[KD];
     ScatterRec Rq[RD];
 #pragma unroll
@@ -1062,7 +1072,7 @@ __global__ void VILV_BOUNDS vertex_ilv_kernel(RowParams p, const ScatterRec* __r
     for (int j = 0; j < RD; ++j) Rq[j] = ScatterRec{0u, 0u, 0u, 0u};
 #pragma unroll
     for (int j = 0; j < RD; ++j)
-        if (j <= last) Rq[j] = rr[32 * j];
+        if (REC_AHEAD || j <= last) Rq[j] = rr[32 * j];
     pdl_wait();  // the per-tet blocks of this assembly
 #pragma unroll
     for (int j = 0; j < KD; ++j)
@@ -1718,6 +1728,7 @@ __global__ void __launch_bounds__(64) vec_edge_ring_kernel(RowParams p, int64_t 
     const int nloop = isdir ? 0 : deg;
     const int last = nloop - 1;
     constexpr int KD = VRING_KD, RD = VRING_RD;
+    static_assert(RD < 16, "the first records may reach RD slots past the lane's own (kRecPad)");
     VBlock<Real> Kq[KD];
     uint2 Rq[RD];
 #pragma unroll
@@ -1726,7 +1737,7 @@ __global__ void __launch_bounds__(64) vec_edge_ring_kernel(RowParams p, int64_t 
     for (int j = 0; j < RD; ++j) Rq[j] = make_uint2(0u, 0u);
 #pragma unroll
     for (int j = 0; j < RD; ++j)
-        if (j <= last) Rq[j] = rr[32 * (j + 1)];
+        if (REC_AHEAD || j <= last) Rq[j] = rr[32 * (j + 1)];
 #pragma unroll
     for (int j = 0; j < KD; ++j)
         if (j <= last) Kq[j].load(tetB + 16 * (int64_t)(Rq[j].x & kRingTetMask));
@@ -2167,9 +2178,9 @@ static int setup_vertex_ilv(anigpu_ctx* h) {
     int64_t total = 0;
     int rc = warp_layout(h, rb, re, 0, &h->vrec_woff, &total, &h->vrec_ws);
     if (rc) return rc;
-    rc = dev_alloc(h, &h->vrec, (size_t)total);
+    rc = dev_alloc(h, &h->vrec, (size_t)(total + kRecPad));
     if (rc) return rc;
-    ANI_CUDA(h, cudaMemsetAsync(h->vrec, 0, sizeof(ScatterRec) * (size_t)total, s));
+    ANI_CUDA(h, cudaMemsetAsync(h->vrec, 0, sizeof(ScatterRec) * (size_t)(total + kRecPad), s));
     vertex_ilv_build_kernel<<<grid_for(n, 128), 128, 0, s>>>(rb, re, h->inc_ptr, h->recs, h->vrec_woff, h->vrec);
     ANI_LAUNCHED(h);
     return ANIGPU_OK;
@@ -2192,9 +2203,9 @@ int setup_row_layouts(anigpu_ctx* h) {
     int64_t total = 0;
     rc = warp_layout(h, rb, re, 1, &h->ring_woff, &total, &h->ring_ws);
     if (rc) return rc;
-    rc = dev_alloc(h, &h->ring, (size_t)total);
+    rc = dev_alloc(h, &h->ring, (size_t)(total + kRecPad));
     if (rc) return rc;
-    ANI_CUDA(h, cudaMemsetAsync(h->ring, 0, sizeof(uint2) * (size_t)total, s));
+    ANI_CUDA(h, cudaMemsetAsync(h->ring, 0, sizeof(uint2) * (size_t)(total + kRecPad), s));
     int* fail = nullptr;
     ANI_CUDA(h, cudaMallocAsync((void**)&fail, sizeof(int), s));
     ANI_CUDA(h, cudaMemsetAsync(fail, 0, sizeof(int), s));
