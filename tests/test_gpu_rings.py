@@ -126,3 +126,64 @@ def test_vector_ring_gather_matches_record_gather(lib, restated, precision):
                                         dirichlet=(mask, bc))
         assert np.abs(a - ref["vals"]).max() <= 1e-12 * np.abs(ref["vals"]).max()
         assert np.abs(r1.cpu().numpy() - ref["rhs"]).max() <= 1e-12 * np.abs(ref["rhs"]).max()
+
+
+def _star_mesh():
+    """A vertex at the origin and the 80 tets that join it to a once-subdivided icosahedron: the
+    centre's row has 80 incidences, every other vertex row 5 or 6, so the vertex rows' interleaved
+    layout keeps per-warp offsets (a uniform stride would double it)."""
+    t = (1 + 5 ** 0.5) / 2
+    v = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+         (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    f = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+         (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11),
+         (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    pts = [np.array(p, np.float64) / np.linalg.norm(p) for p in v]
+    mid = {}
+
+    def midpoint(a, b):
+        key = (min(a, b), max(a, b))
+        if key not in mid:
+            m = pts[a] + pts[b]
+            pts.append(m / np.linalg.norm(m))
+            mid[key] = len(pts) - 1
+        return mid[key]
+
+    faces = []
+    for a, b, c in f:
+        ab, bc, ca = midpoint(a, b), midpoint(b, c), midpoint(c, a)
+        faces += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+    xyz = np.vstack([np.zeros((1, 3))] + [p[None] for p in pts])
+    tets = np.array([(0, a + 1, b + 1, c + 1) for a, b, c in faces], np.int32)
+    return xyz, tets
+
+
+@pytest.mark.parametrize("precision", ["F64", "F32"])
+def test_gathers_with_per_warp_offsets(lib, restated, precision):
+    """The star mesh (one vertex row of 80 incidences among rows of 5-6): both gathers against the
+    record gather, FP64 against the oracle, with the walks' first records read past short rows."""
+    import anigpu
+    prec = getattr(anigpu, precision)
+    xyz, tets = _star_mesh()
+    assert tets.shape[0] == 80 and xyz.shape[0] == 43
+    D = np.tile(np.array([2.0, 1.0, 1.5, 0.1, 0.0, 0.2]), (tets.shape[0], 1))
+    lib.mesh_upload(xyz, tets)
+    lib.problem_setup(anigpu.P2)
+    mask = (np.linalg.norm(lib.dof_coords().cpu().numpy(), axis=1) > 0.99).astype(np.uint8)
+    lib.set_dirichlet(mask)
+    assert lib.gather_layouts() == (True, True)
+    v1, r1, _ = lib.assemble(anigpu.TENSOR_TET_SYM, D, None, 1.0, 4, prec)
+    v1, r1 = v1.double().cpu().numpy(), r1.cpu().numpy()
+    lib.set_gather_layouts(False)
+    try:
+        v0, r0, _ = lib.assemble(anigpu.TENSOR_TET_SYM, D, None, 1.0, 4, prec)
+    finally:
+        lib.set_gather_layouts(True)
+    v0, r0 = v0.double().cpu().numpy(), r0.cpu().numpy()
+    tol = 4e-15 if precision == "F64" else 1e-6
+    assert np.abs(v1 - v0).max() <= tol * np.abs(v0).max()
+    assert np.abs(r1 - r0).max() <= tol * np.abs(r0).max()
+    if precision == "F64":
+        ref = restated.assemble_problem(xyz, tets, 2, anigpu.TENSOR_TET_SYM, D, 1.0, 4, dirichlet=(mask, None))
+        assert np.abs(v1 - ref["vals"]).max() <= 1e-12 * np.abs(ref["vals"]).max()
+        assert np.abs(r1 - ref["rhs"]).max() <= 1e-12 * np.abs(ref["rhs"]).max()
