@@ -104,6 +104,16 @@ struct anigpu_ctx {
     bool ring_enabled = true;      // anigpu_set_gather_layouts: rings and interleaved vertex records
     // vertex rows' scatter records in the same lane-interleaved layout (no header)
     ScatterRec* vrec = nullptr;
+    // P2 vertex rows by symmetry: the edge walks store every off-diagonal entry of the vertex rows
+    // at its transposed position (tpos: per edge row the positions of (A,E), (B,E), (A,B), (B,A) and
+    // the first ring vertex's (P,E), then (N,E) of each incidence), and a pass over the vertex rows'
+    // incidences (vrec4: tet | local vertex << 27) adds the diagonal (at vdiag) and the rhs
+    int32_t* tpos = nullptr;
+    int64_t* tpos_woff = nullptr;
+    int64_t tpos_ws = 0;
+    uint32_t* vrec4 = nullptr;
+    int32_t* vdiag = nullptr;
+    bool tr_ok = false;
     int64_t* vrec_woff = nullptr;
     int64_t vrec_ws = 0;
     int max_row_len_s = 0;

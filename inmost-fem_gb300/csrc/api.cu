@@ -70,6 +70,7 @@ int anigpu_destroy(anigpu_handle h) {
     free_general(h);
     void* ptrs[] = {h->xyz, h->xyz2, h->tets, h->tet_edges, h->edofs, h->inc_ptr, h->recs, h->dir_mask, h->dir_bc,
                     h->dir_cptr, h->dir_coff, h->ring, h->ring_woff, h->vrec, h->vrec_woff,
+                    h->tpos, h->tpos_woff, h->vrec4, h->vdiag,
                     h->tetdata, h->d_status, h->d_ref_tables};
     for (void* p : ptrs)
         if (p) cudaFree(p);

@@ -365,6 +365,9 @@ struct RowParams {
     const int32_t* vcol;  // vector template columns (non-zero boundary values of the vector path)
     int bcnz;             // vector path: non-zero boundary values
     int64_t wstride = 0;  // lane-interleaved records: slots per warp when uniform, else 0 (per-warp offsets)
+    const int32_t* tpos = nullptr;   // transposed positions of the edge walks (vertex rows by symmetry)
+    const int64_t* twoff = nullptr;
+    int64_t tstride = 0;
 };
 
 
@@ -832,7 +835,11 @@ constexpr int64_t kRecPad = 32 * 16;  // prefetch depths below 16
 #endif
 #define RING_BOUNDS __launch_bounds__(64, sizeof(Real) == 4 ? RING_MINB : 1)
 
-template <typename Real, bool DIR, bool DROPCHK>
+// TR: the vertex rows by symmetry -- every value of this row that belongs to a vertex column (A,
+// B, the ring vertices) is also stored at its transposed position in that vertex row, together with
+// the vertex-vertex entry (A, B); Dirichlet edge rows walk too (for that entry) but write only
+// their diagonal here.
+template <typename Real, bool DIR, bool DROPCHK, bool TR = false>
 __global__ void RING_BOUNDS edge_ring_kernel(RowParams p, const uint2* __restrict__ ring,
                                             const int64_t* __restrict__ woff, const Real* __restrict__ tetK,
                                             Real* __restrict__ vals, double* __restrict__ rhs,
@@ -872,10 +879,19 @@ __global__ void RING_BOUNDS edge_ring_kernel(RowParams p, const uint2* __restric
     __syncwarp();
     Real* myRow = sC + base;
     const Real drop = Real(p.drop);
-    const int nloop = isdir ? 0 : deg;
+    const int nloop = isdir && !TR ? 0 : deg;
     const int last = nloop - 1;
     constexpr int KD = RING_KD, RD = RING_RD;
     static_assert(RD > KD, "records must run ahead of the blocks they address");
+    // TR: transposed positions, (N,E) of incidence j in slot 5 + j, prefetched like the records
+    const int32_t* tr = TR ? p.tpos + (p.tstride > 0 ? wg * p.tstride : p.twoff[wg]) + lane : nullptr;
+    int32_t Tq[TR ? RD : 1];
+    int32_t tprev = 0;  // (N,E) of the previous incidence: where this step's completed face goes
+    Real tf0 = Real(0), accAB = Real(0);
+    if (TR) {
+#pragma unroll
+        for (int j = 0; j < RD; ++j) Tq[j] = tr[32 * (5 + j)];
+    }
     static_assert(RD < 16, "the first records may reach RD slots past the lane's own (kRecPad)");
     KVec<Real, KS> Kq[KD];
     uint2 Rq[RD];
@@ -935,16 +951,23 @@ __global__ void RING_BOUNDS edge_ring_kernel(RowParams p, const uint2* __restric
         racc += F;
         // face P: the carried tet's part plus this tet's; final except the first face of a closed ring
         const Real oP = cP + vP, oAP = cAP + vAP, oBP = cBP + vBP;
+        if (TR) {
+            // the vertex-vertex entry (A, B) of fem3Dtet's P2 GRAD.GRAD matrix: -0.2 G_AB per tet
+            const Real vAB = Real(-0.2) * gab;
+            accAB += DROPCHK ? (fabs(vAB) > drop ? vAB : Real(0)) : vAB;
+            if (k == 0) tf0 = oP;
+            else if (!isdir) vals[tprev] = oP;  // the completed face's vertex row, column E
+        }
         if (k == 0 && closed) {
             fP = oP;
             fAP = oAP;
             fBP = oBP;
-        } else {
+        } else if (!TR || !isdir) {
             myRow[coff & 255u] = oP;
             myRow[(coff >> 8) & 255u] = oAP;
             myRow[(coff >> 16) & 255u] = oBP;
         }
-        myRow[r0.y >> 24] = vPN;
+        if (!TR || !isdir) myRow[r0.y >> 24] = vPN;
         cP = vN;
         cAP = vAN;
         cBP = vBN;
@@ -955,18 +978,35 @@ __global__ void RING_BOUNDS edge_ring_kernel(RowParams p, const uint2* __restric
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             step(k + u, Rq[u % RD], Kq[u % KD].v);
+            if (TR) tprev = Tq[u % RD];
             if (k + u + KD <= last) Kq[u % KD].load(tetK + KS * (int64_t)(Rq[(u + KD) % RD].x & kRingTetMask));
-            if (k + u + RD <= last) Rq[u % RD] = rr[32 * (k + u + RD + 1)];
+            if (k + u + RD <= last) {
+                Rq[u % RD] = rr[32 * (k + u + RD + 1)];
+                if (TR) Tq[u % RD] = tr[32 * (5 + k + u + RD)];
+            }
         }
     }
 #pragma unroll
     for (int u = 0; u + 1 < U; ++u) {
         if (k + u < nloop) {
             step(k + u, Rq[u % RD], Kq[u % KD].v);
+            if (TR) tprev = Tq[u % RD];
             if (k + u + KD <= last) Kq[u % KD].load(tetK + KS * (int64_t)(Rq[(u + KD) % RD].x & kRingTetMask));
         }
     }
     bool bad = false;
+    if (TR && valid && nloop > 0) {
+        // transposed: the last face, the first face of a path, (A,E), (B,E) and (A,B), (B,A)
+        if (!isdir) {
+            vals[tprev] = cP + fP;
+            if (!closed) vals[tr[128]] = tf0;
+            vals[tr[0]] = accA;
+            vals[tr[32]] = accB;
+        }
+        vals[tr[64]] = accAB;
+        vals[tr[96]] = accAB;
+        bad |= !isfinite(accAB);
+    }
     if (valid) {
         double F;
         if (DIR && isdir) {
@@ -1139,6 +1179,92 @@ __global__ void VILV_BOUNDS vertex_ilv_kernel(RowParams p, const ScatterRec* __r
     bad |= !isfinite(fin);
     if (bad) atomicExch(status, ANIGPU_ERR_NONFINITE);
     pdl_launch_dependents();
+}
+
+// The vertex rows when the edge walks have stored their off-diagonal entries (TR): per row the
+// diagonal (the sum of 0.6 G_ii over the incident tets, fem3Dtet's P2 GRAD.GRAD diagonal) and the
+// right-hand side (-0.05 f|T| per tet), from the incidence words in the interleaved layout; a
+// Dirichlet row is rewritten as its diagonal (the number of incident tets), a row with Dirichlet
+// columns has them zeroed.  Runs after the edge walks (their stores into these rows come first).
+#ifndef VTR_KD
+#define VTR_KD 4
+#endif
+#ifndef VTR_RD
+#define VTR_RD 8
+#endif
+template <typename Real, bool DIR, bool DROPCHK>
+__global__ void __launch_bounds__(128) vertex_tr_kernel(RowParams p, const uint32_t* __restrict__ vrec4,
+                                                        const int64_t* __restrict__ woff,
+                                                        const int32_t* __restrict__ vdiag,
+                                                        const Real* __restrict__ tetK, Real* __restrict__ vals,
+                                                        double* __restrict__ rhs, int* __restrict__ status) {
+    constexpr int KS = 8, KD = VTR_KD, RD = VTR_RD;
+    static_assert(RD > KD && RD <= 16, "prefetch depths (kRecPad)");
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t wg = t >> 5;
+    const int lane = (int)(t & 31);
+    const int64_t row = p.row_begin + t;
+    if (row >= p.nrows) return;  // no warp-wide operation follows
+    const uint32_t* rr = vrec4 + (p.wstride > 0 ? wg * p.wstride : woff[wg]) + lane;
+    const int deg = (int)(p.inc_ptr[row + 1] - p.inc_ptr[row]);
+    const bool isdir = DIR && p.dir_mask[row] != 0;
+    const int nloop = isdir ? 0 : deg;
+    const int last = nloop - 1;
+    const Real drop = Real(p.drop);
+    uint32_t Rq[RD];
+#pragma unroll
+    for (int j = 0; j < RD; ++j) Rq[j] = rr[32 * j];
+    pdl_wait();  // the per-tet blocks and the edge walks' stores
+    KVec<Real, KS> Kq[KD];
+#pragma unroll
+    for (int j = 0; j < KD; ++j) {
+        Kq[j].zero();
+        if (j <= last) Kq[j].load(tetK + KS * (int64_t)(Rq[j] & kRingTetMask));
+    }
+    Real accD = Real(0), racc = Real(0);
+    auto step = [&](const uint32_t r0, const Real* G) {
+        Real a[10];
+        const Real F = gram_row<Real, 10, 1>(G, (int)(r0 >> 27), a);
+        accD += DROPCHK ? (fabs(a[0]) > drop ? a[0] : Real(0)) : a[0];
+        racc += F;
+    };
+    // prefetch in fixed slots (blocks of incidence k in Kq[k % KD], words in Rq[k % RD]), unrolled
+    // by RD so that no prefetched value is moved
+    constexpr int U = RD;
+    static_assert(U % KD == 0, "slot walk");
+    int k = 0;
+    for (; k + U <= nloop; k += U) {
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            step(Rq[u % RD], Kq[u % KD].v);
+            if (k + u + KD <= last) Kq[u % KD].load(tetK + KS * (int64_t)(Rq[(u + KD) % RD] & kRingTetMask));
+            if (k + u + RD <= last) Rq[u % RD] = rr[32 * (k + u + RD)];
+        }
+    }
+#pragma unroll
+    for (int u = 0; u + 1 < U; ++u) {
+        if (k + u < nloop) {
+            step(Rq[u % RD], Kq[u % KD].v);
+            if (k + u + KD <= last) Kq[u % KD].load(tetK + KS * (int64_t)(Rq[(u + KD) % RD] & kRingTetMask));
+        }
+    }
+    const int64_t rb = p.rowptr[row];
+    double F;
+    if (DIR && isdir) {
+        const int64_t re = p.rowptr[row + 1];
+        for (int64_t q = rb; q < re; ++q) vals[q] = Real(0);
+        if (deg > 0) vals[vdiag[row]] = Real(deg);
+        const double bcr = p.dir_bc[row];
+        F = 0;
+        for (int q = 0; q < deg; ++q) F += bcr;
+    } else {
+        vals[vdiag[row]] = accD;
+        F = (double)racc;
+        if (DIR)
+            for (int64_t q = p.dir_cptr[row]; q < p.dir_cptr[row + 1]; ++q) vals[rb + p.dir_coff[q]] = Real(0);
+    }
+    rhs[row] = F;
+    if (!isfinite(F) || !isfinite((double)accD)) atomicExch(status, ANIGPU_ERR_NONFINITE);
 }
 
 // slots of each warp of 32 rows in a lane-interleaved layout: 32 x (head + its largest
@@ -1320,6 +1446,99 @@ __global__ void ring_build_kernel(int64_t rb, int64_t re, const int64_t* __restr
         return;
     }
     out[0] = make_uint2(hx, hy);
+}
+
+// ---------------------------------------------------------------- P2 vertex rows by symmetry
+// position of column c in row x of the template (-1 when absent)
+__device__ __forceinline__ int32_t col_pos(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                                           int64_t x, int32_t c) {
+    int64_t lo = rowptr[x], hi = rowptr[x + 1];
+    const int64_t end = hi;
+    while (lo < hi) {
+        const int64_t m = (lo + hi) >> 1;
+        if (col[m] < c) lo = m + 1;
+        else hi = m;
+    }
+    return lo < end && col[lo] == c ? (int32_t)lo : -1;
+}
+
+// transposed positions of edge row r = E in the lane-interleaved layout (head 5): (A,E), (B,E),
+// (A,B), (B,A), the first ring vertex's (P0,E) for a path, then (N,E) of each incidence of the ring
+__global__ void tpos_build_kernel(int64_t rb, int64_t re, const int64_t* __restrict__ inc_ptr,
+                                  const uint2* __restrict__ ring, const int64_t* __restrict__ ring_woff,
+                                  const int32_t* __restrict__ tets, const int64_t* __restrict__ rowptr,
+                                  const int32_t* __restrict__ col, const int64_t* __restrict__ twoff,
+                                  int32_t* __restrict__ tpos, int* __restrict__ fail) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t r = rb + t;
+    if (r >= re) return;
+    const uint2* rr = ring + ring_woff[t >> 5] + (t & 31);
+    int32_t* out = tpos + twoff[t >> 5] + (t & 31);
+    const int deg = (int)(inc_ptr[r + 1] - inc_ptr[r]);
+    const bool closed = (rr[0].x >> 24) & 1u;
+    const int32_t E = (int32_t)r;
+    const int EI[6] = {0, 0, 0, 1, 1, 2}, EJ[6] = {1, 2, 3, 2, 3, 3};
+    int32_t vA = -1, vB = -1, P0 = -1;
+    bool bad = deg < 1;
+    for (int s = 0; s < deg && !bad; ++s) {
+        const uint2 rec = rr[32 * (s + 1)];
+        const int32_t* tv = tets + 4 * (int64_t)(rec.x & kRingTetMask);
+        const int k = (int)((rec.x >> 27) & 7u), la = EI[k], lb = EJ[k];
+        int lc = -1, ld = -1;
+        for (int l = 0; l < 4; ++l)
+            if (l != la && l != lb) {
+                if (lc < 0) lc = l;
+                else ld = l;
+            }
+        const bool sab = (rec.x >> 30) & 1u, scd = (rec.x >> 31) & 1u;
+        const int32_t A = sab ? tv[lb] : tv[la], B = sab ? tv[la] : tv[lb];
+        const int32_t P = scd ? tv[ld] : tv[lc], N = scd ? tv[lc] : tv[ld];
+        if (s == 0) {
+            vA = A;
+            vB = B;
+            P0 = P;
+        }
+        const int32_t q = col_pos(rowptr, col, N, E);
+        bad |= q < 0 || A != vA || B != vB;
+        out[32 * (5 + s)] = q;
+    }
+    if (!bad) {
+        const int32_t h0 = col_pos(rowptr, col, vA, E), h1 = col_pos(rowptr, col, vB, E);
+        const int32_t h2 = col_pos(rowptr, col, vA, vB), h3 = col_pos(rowptr, col, vB, vA);
+        const int32_t h4 = closed ? 0 : col_pos(rowptr, col, P0, E);
+        bad = h0 < 0 || h1 < 0 || h2 < 0 || h3 < 0 || h4 < 0;
+        out[0] = h0;
+        out[32] = h1;
+        out[64] = h2;
+        out[96] = h3;
+        out[128] = h4;
+    }
+    if (bad) atomicOr(fail, 1);
+}
+
+// the vertex rows' incidences (tet | local vertex << 27) in the interleaved layout of vrec, and the
+// position of each vertex row's diagonal
+__global__ void vertex4_build_kernel(int64_t rb, int64_t re, const int64_t* __restrict__ inc_ptr,
+                                     const ScatterRec* __restrict__ recs, const int64_t* __restrict__ rowptr,
+                                     const int32_t* __restrict__ col, const int64_t* __restrict__ woff,
+                                     uint32_t* __restrict__ vrec4, int32_t* __restrict__ vdiag,
+                                     int* __restrict__ fail) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t r = rb + t;
+    if (r >= re) return;
+    uint32_t* out = vrec4 + woff[t >> 5] + (t & 31);
+    const int64_t ib = inc_ptr[r];
+    const int deg = (int)(inc_ptr[r + 1] - ib);
+    bool bad = false;
+    for (int j = 0; j < deg; ++j) {
+        const ScatterRec rec = recs[ib + j];
+        const uint32_t i = rec.meta & 15u;
+        bad |= i > 3u || rec.tet > kRingTetMask;
+        out[32 * j] = rec.tet | (i << 27);
+    }
+    const int32_t d = col_pos(rowptr, col, r, (int32_t)r);
+    vdiag[r] = d;
+    if (bad || d < 0) atomicOr(fail, 1);
 }
 
 // ---------------------------------------------------------------- vector P2 (linear elasticity)
@@ -2036,11 +2255,11 @@ static int launch_rows_t(anigpu_ctx* h, const RowParams& p, const void* tables, 
     return ANIGPU_OK;
 }
 
-template <typename Real, bool DIR, bool DROPCHK>
+template <typename Real, bool DIR, bool DROPCHK, bool TR = false>
 static int launch_ring_t(anigpu_ctx* h, const RowParams& p, void* vals, double* rhs, cudaStream_t st) {
     const int warps = h->row_warps == 1 ? 1 : 2;
     const size_t smem = RowSmem<Real, 10, 2, false>::total(p.cap, warps);
-    auto kern = edge_ring_kernel<Real, DIR, DROPCHK>;
+    auto kern = edge_ring_kernel<Real, DIR, DROPCHK, TR>;
     static int smem_set[64] = {};
     const int slot = h->device >= 0 && h->device < 64 ? h->device : 0;
     if ((int)smem > smem_set[slot]) {
@@ -2061,10 +2280,61 @@ static int launch_ring_t(anigpu_ctx* h, const RowParams& p, void* vals, double* 
     cfg.numAttrs = h->asm_pdl ? 1 : 0;
     RowParams q = p;
     q.wstride = h->ring_ws;
+    if (TR) {
+        q.tpos = h->tpos;
+        q.twoff = h->tpos_woff;
+        q.tstride = h->tpos_ws;
+    }
     ANI_CUDA(h, cudaLaunchKernelEx(&cfg, kern, q, (const uint2*)h->ring, (const int64_t*)h->ring_woff,
                                    (const Real*)h->tetdata, (Real*)vals, rhs, h->d_status));
     ANI_LAUNCHED(h);
     return ANIGPU_OK;
+}
+
+// the vertex pass behind the edge walks that stored the vertex rows' off-diagonal entries
+template <typename Real, bool DIR, bool DROPCHK>
+static int launch_vtr_t(anigpu_ctx* h, const RowParams& p, void* vals, double* rhs, cudaStream_t st) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid_for(p.nrows - p.row_begin, 128));
+    cfg.blockDim = dim3(128);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = h->asm_pdl ? 1 : 0;
+    RowParams q = p;
+    q.wstride = h->vrec_ws;
+    ANI_CUDA(h, cudaLaunchKernelEx(&cfg, vertex_tr_kernel<Real, DIR, DROPCHK>, q, (const uint32_t*)h->vrec4,
+                                   (const int64_t*)h->vrec_woff, (const int32_t*)h->vdiag, (const Real*)h->tetdata,
+                                   (Real*)vals, rhs, h->d_status));
+    ANI_LAUNCHED(h);
+    return ANIGPU_OK;
+}
+
+// P2 vertex rows by symmetry: the edge walks with their transposed stores, then the vertex pass,
+// both behind the per-tet kernel on its stream
+template <typename Real>
+static int launch_tr(anigpu_ctx* h, const RowParams& p0, void* vals, double* rhs) {
+    const bool dir = h->has_dirichlet;
+    const bool dchk = sizeof(Real) == 8 || (float)p0.drop != 0.0f;
+    RowParams p = p0;
+    p.row_begin = h->row_range[1];
+    p.nrows = h->row_range[2];
+    p.cap = h->row_range_cap[1];
+    int rc;
+    if (dchk) rc = dir ? launch_ring_t<Real, true, true, true>(h, p, vals, rhs, h->stream)
+                       : launch_ring_t<Real, false, true, true>(h, p, vals, rhs, h->stream);
+    else rc = dir ? launch_ring_t<Real, true, false, true>(h, p, vals, rhs, h->stream)
+                  : launch_ring_t<Real, false, false, true>(h, p, vals, rhs, h->stream);
+    if (rc) return rc;
+    p.row_begin = h->row_range[0];
+    p.nrows = h->row_range[1];
+    p.cap = h->row_range_cap[0];
+    if (dchk) return dir ? launch_vtr_t<Real, true, true>(h, p, vals, rhs, h->stream)
+                         : launch_vtr_t<Real, false, true>(h, p, vals, rhs, h->stream);
+    return dir ? launch_vtr_t<Real, true, false>(h, p, vals, rhs, h->stream)
+               : launch_vtr_t<Real, false, false>(h, p, vals, rhs, h->stream);
 }
 
 template <typename Real, int NLOC, bool DIR, bool DROPCHK>
@@ -2186,10 +2456,73 @@ static int setup_vertex_ilv(anigpu_ctx* h) {
     return ANIGPU_OK;
 }
 
+#ifndef VERTEX_TR
+#define VERTEX_TR 1
+#endif
+
+// the transposed positions and the vertex rows' incidence words (P2 with rings); left out (and the
+// vertex rows gathered by their own walk) when a position is missing or the values do not fit
+static int setup_vertex_tr(anigpu_ctx* h) {
+    void* ptrs[] = {h->tpos, h->tpos_woff, h->vrec4, h->vdiag};
+    for (void* q : ptrs)
+        if (q) cudaFree(q);
+    h->tpos = nullptr;
+    h->tpos_woff = nullptr;
+    h->vrec4 = nullptr;
+    h->vdiag = nullptr;
+    h->tpos_ws = 0;
+    h->tr_ok = false;
+    if (!VERTEX_TR || h->space != ANIGPU_P2 || !h->ring_ok || !h->vrec || h->nnz_s >= (int64_t)INT32_MAX) return ANIGPU_OK;
+    const int64_t vb = h->row_range[0], ve = h->row_range[1], rb = h->row_range[1], re = h->row_range[2];
+    if (ve <= vb || re <= rb) return ANIGPU_OK;
+    cudaStream_t s = h->stream;
+    int64_t total = 0;
+    int rc = warp_layout(h, rb, re, 5, &h->tpos_woff, &total, &h->tpos_ws);
+    if (rc) return rc;
+    rc = dev_alloc(h, &h->tpos, (size_t)(total + kRecPad));
+    if (rc) return rc;
+    ANI_CUDA(h, cudaMemsetAsync(h->tpos, 0, sizeof(int32_t) * (size_t)(total + kRecPad), s));
+    const int64_t nwv = (ve - vb + 31) / 32;
+    int64_t vtotal = 0;
+    ANI_CUDA(h, cudaMemcpyAsync(&vtotal, h->vrec_woff + nwv, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    ANI_CUDA(h, cudaStreamSynchronize(s));
+    rc = dev_alloc(h, &h->vrec4, (size_t)(vtotal + kRecPad));
+    if (rc) return rc;
+    ANI_CUDA(h, cudaMemsetAsync(h->vrec4, 0, sizeof(uint32_t) * (size_t)(vtotal + kRecPad), s));
+    rc = dev_alloc(h, &h->vdiag, (size_t)(ve - vb));
+    if (rc) return rc;
+    int* fail = nullptr;
+    ANI_CUDA(h, cudaMallocAsync((void**)&fail, sizeof(int), s));
+    ANI_CUDA(h, cudaMemsetAsync(fail, 0, sizeof(int), s));
+    tpos_build_kernel<<<grid_for(re - rb, 128), 128, 0, s>>>(rb, re, h->inc_ptr, h->ring, h->ring_woff, h->tets,
+                                                             h->rowptr_s, h->col_s, h->tpos_woff, h->tpos, fail);
+    ANI_LAUNCHED(h);
+    vertex4_build_kernel<<<grid_for(ve - vb, 128), 128, 0, s>>>(vb, ve, h->inc_ptr, h->recs, h->rowptr_s, h->col_s,
+                                                                h->vrec_woff, h->vrec4, h->vdiag, fail);
+    ANI_LAUNCHED(h);
+    int hf = 0;
+    ANI_CUDA(h, cudaMemcpyAsync(&hf, fail, sizeof(int), cudaMemcpyDeviceToHost, s));
+    ANI_CUDA(h, cudaStreamSynchronize(s));
+    ANI_CUDA(h, cudaFreeAsync(fail, s));
+    if (hf) {
+        void* q2[] = {h->tpos, h->tpos_woff, h->vrec4, h->vdiag};
+        for (void* q : q2) cudaFree(q);
+        h->tpos = nullptr;
+        h->tpos_woff = nullptr;
+        h->vrec4 = nullptr;
+        h->vdiag = nullptr;
+        h->tpos_ws = 0;
+        return ANIGPU_OK;
+    }
+    h->tr_ok = true;
+    return ANIGPU_OK;
+}
+
 int setup_row_layouts(anigpu_ctx* h) {
     int rc = setup_vertex_ilv(h);
     if (rc) return rc;
     h->ring_ok = false;
+    h->tr_ok = false;
     if (h->ring) cudaFree(h->ring);
     if (h->ring_woff) cudaFree(h->ring_woff);
     h->ring = nullptr;
@@ -2225,7 +2558,7 @@ int setup_row_layouts(anigpu_ctx* h) {
         return ANIGPU_OK;
     }
     h->ring_ok = true;
-    return ANIGPU_OK;
+    return setup_vertex_tr(h);
 }
 
 template <typename Real, int NLOC, int FORM>
@@ -2413,6 +2746,16 @@ int run_assemble(anigpu_ctx* h, int kind, const double* D, const double* f, doub
     // (the vertex range on the side stream) so that the tail of one overlaps the other.
     const bool seq = ASM_SEQ && gram && h->ring_enabled && !touched && !(h->has_dirichlet && h->bc_nonzero) &&
                      (h->nloc_s == 4 || h->ring_ok) && h->vrec;
+    // FP64: the vertex rows by symmetry (their own walk is FP64-bound: 1.53 vs 1.78 ms per 64^3
+    // assembly); FP32 keeps the vertex walk (the transposed stores cost more: 0.248 vs 0.195 ms)
+    if (seq && h->tr_ok && precision == ANIGPU_F64 && h->nloc_s == 10 && h->row_range[1] > h->row_range[0] &&
+        h->row_range[2] > h->row_range[1]) {
+        h->asm_pdl = true;
+        rc = launch_tr<double>(h, p, vals, rhs);
+        h->asm_pdl = false;
+        time_mark(h, 2);
+        return rc;
+    }
     const bool split = seq && ASM_SPLIT && h->nloc_s == 10 && h->side_stream;
     cudaStream_t side = h->side_stream && (!seq || split) ? h->side_stream : h->stream;
     if (side != h->stream) {
