@@ -365,9 +365,6 @@ struct RowParams {
     const int32_t* vcol;  // vector template columns (non-zero boundary values of the vector path)
     int bcnz;             // vector path: non-zero boundary values
     int64_t wstride = 0;  // lane-interleaved records: slots per warp when uniform, else 0 (per-warp offsets)
-    const int32_t* tpos = nullptr;   // transposed positions of the edge walks (vertex rows by symmetry)
-    const int64_t* twoff = nullptr;
-    int64_t tstride = 0;
 };
 
 
@@ -835,15 +832,183 @@ constexpr int64_t kRecPad = 32 * 16;  // prefetch depths below 16
 #endif
 #define RING_BOUNDS __launch_bounds__(64, sizeof(Real) == 4 ? RING_MINB : 1)
 
-// TR: the vertex rows by symmetry -- every value of this row that belongs to a vertex column (A,
-// B, the ring vertices) is also stored at its transposed position in that vertex row, together with
-// the vertex-vertex entry (A, B); Dirichlet edge rows walk too (for that entry) but write only
-// their diagonal here.
-template <typename Real, bool DIR, bool DROPCHK, bool TR = false>
+template <typename Real, bool DIR, bool DROPCHK>
 __global__ void RING_BOUNDS edge_ring_kernel(RowParams p, const uint2* __restrict__ ring,
                                             const int64_t* __restrict__ woff, const Real* __restrict__ tetK,
                                             Real* __restrict__ vals, double* __restrict__ rhs,
                                             int* __restrict__ status) {
+    using Sm = RowSmem<Real, 10, 2, false>;
+    constexpr int KS = 8;
+    constexpr int VEC = Sm::VEC;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarps = blockDim.x >> 5;
+    const int64_t wg = (int64_t)blockIdx.x * nwarps + warp;
+    const int64_t row0 = p.row_begin + wg * 32;
+    if (row0 >= p.nrows) return;  // warp-uniform; no block-wide barrier follows
+    const int64_t rend = row0 + 32 < p.nrows ? row0 + 32 : p.nrows;
+    const int64_t cbase = p.rowptr[row0];
+    const int clen = (int)(p.rowptr[rend] - cbase);
+    const int shift = (int)(cbase & (VEC - 1));
+    unsigned char* wbase = smem_raw + Sm::warp_bytes(p.cap) * warp;
+    Real* sC = reinterpret_cast<Real*>(wbase) + shift;
+    {
+        const int nvec = (shift + clen + VEC - 1) / VEC;
+        int4* z = reinterpret_cast<int4*>(wbase);
+        for (int k = lane; k < nvec; k += 32) z[k] = make_int4(0, 0, 0, 0);
+    }
+    const int64_t row = row0 + lane;
+    const bool valid = row < p.nrows;
+    const uint2* rr = ring + (p.wstride > 0 ? wg * p.wstride : woff[wg]) + lane;
+    int deg = 0, base = 0;
+    bool isdir = false;
+    uint2 hd = make_uint2(0u, 0u);
+    if (valid) {
+        deg = (int)(p.inc_ptr[row + 1] - p.inc_ptr[row]);
+        base = (int)(p.rowptr[row] - cbase);
+        if (DIR) isdir = p.dir_mask[row] != 0;
+        hd = rr[0];
+    }
+    __syncwarp();
+    Real* myRow = sC + base;
+    const Real drop = Real(p.drop);
+    const int nloop = isdir ? 0 : deg;
+    const int last = nloop - 1;
+    constexpr int KD = RING_KD, RD = RING_RD;
+    static_assert(RD > KD, "records must run ahead of the blocks they address");
+    static_assert(RD < 16, "the first records may reach RD slots past the lane's own (kRecPad)");
+    KVec<Real, KS> Kq[KD];
+    uint2 Rq[RD];
+#pragma unroll
+    for (int j = 0; j < KD; ++j) Kq[j].zero();
+#pragma unroll
+    for (int j = 0; j < RD; ++j) Rq[j] = make_uint2(0u, 0u);
+#pragma unroll
+    for (int j = 0; j < RD; ++j)
+        if (REC_AHEAD || j <= last) Rq[j] = rr[32 * (j + 1)];
+    pdl_wait();  // the per-tet blocks of this assembly
+#pragma unroll
+    for (int j = 0; j < KD; ++j)
+        if (j <= last) Kq[j].load(tetK + KS * (int64_t)(Rq[j].x & kRingTetMask));
+    const bool closed = (hd.x >> 24) & 1u;
+    Real cP = Real(0), cAP = Real(0), cBP = Real(0);  // the face carried to the next tet
+    Real fP = Real(0), fAP = Real(0), fBP = Real(0);  // the first face of a closed ring
+    uint32_t coff = hd.y;                             // offsets of the carried face's columns
+    Real accA = Real(0), accB = Real(0), accE = Real(0), racc = Real(0);
+    // the walk with its prefetch in fixed slots (blocks of incidences k.. in Kq[k % KD], records in
+    // Rq[k % RD]), unrolled by RING_U (a multiple of both) so that no prefetched value is moved
+    constexpr int U = RING_U;
+    static_assert(U % KD == 0 && U % RD == 0, "slot walk");
+    auto step = [&](const int k, const uint2 r0, const Real* G) {
+        // the Gram entries of the edge (A, B) and of its four neighbours in the tet, in ring roles:
+        // local edge le = (a, b) with the other vertices c < d, then A = b if bit 30, P = d if bit 31
+        const int le = (int)((r0.x >> 27) & 7u);
+        const Real gab = le == 0 ? G[0] : le == 1 ? G[1] : le == 2 ? G[2] : le == 3 ? G[3] : le == 4 ? G[4] : G[5];
+        const Real gac = (le == 0 || le == 5) ? G[1] : G[0];
+        const Real gad = le <= 1 ? G[2] : le == 2 ? G[1] : le == 3 ? G[4] : G[3];
+        const Real gbc = le <= 1 ? G[3] : le == 2 ? G[4] : le == 3 ? G[1] : G[2];
+        const Real gbd = (le == 0 || le == 5) ? G[4] : G[5];
+        const bool sab = (r0.x >> 30) & 1u, scd = (r0.x >> 31) & 1u;
+        const Real x1 = scd ? gad : gac, x2 = scd ? gac : gad;  // a with P, a with N
+        const Real y1 = scd ? gbd : gbc, y2 = scd ? gbc : gbd;  // b with P, b with N
+        const Real gAP = sab ? y1 : x1, gAN = sab ? y2 : x2;
+        const Real gBP = sab ? x1 : y1, gBN = sab ? x2 : y2;
+        // the element row of the edge (the Gram form of fem3Dtet's P2 GRAD.GRAD row, with
+        // G_AA = -(G_AB + G_AP + G_AN) and G_BB likewise eliminated)
+        const Real sA = gAP + gAN, sB = gBP + gBN;
+        const Real c2 = Real(0.2), c8 = Real(0.8), c16 = Real(1.6);
+        Real vA = fma(c2, sA, c8 * gab), vB = fma(c2, sB, c8 * gab);
+        Real vE = -c16 * ((gab + sA) + sB);
+        Real vP = -c2 * (gAP + gBP), vN = -c2 * (gAN + gBN);
+        Real vAP = fma(c16, gBP, -c8 * gAN), vAN = fma(c16, gBN, -c8 * gAP);
+        Real vBP = fma(c16, gAP, -c8 * gBN), vBN = fma(c16, gAN, -c8 * gBP);
+        Real vPN = c8 * (sA + sB);
+        const Real F = c2 * G[6];
+        if (DROPCHK) {
+            auto keep = [&](Real v) { return fabs(v) > drop ? v : Real(0); };
+            vA = keep(vA); vB = keep(vB); vE = keep(vE); vP = keep(vP); vN = keep(vN);
+            vAP = keep(vAP); vAN = keep(vAN); vBP = keep(vBP); vBN = keep(vBN); vPN = keep(vPN);
+        }
+        accA += vA;
+        accB += vB;
+        accE += vE;
+        racc += F;
+        // face P: the carried tet's part plus this tet's; final except the first face of a closed ring
+        const Real oP = cP + vP, oAP = cAP + vAP, oBP = cBP + vBP;
+        if (k == 0 && closed) {
+            fP = oP;
+            fAP = oAP;
+            fBP = oBP;
+        } else {
+            myRow[coff & 255u] = oP;
+            myRow[(coff >> 8) & 255u] = oAP;
+            myRow[(coff >> 16) & 255u] = oBP;
+        }
+        myRow[r0.y >> 24] = vPN;
+        cP = vN;
+        cAP = vAN;
+        cBP = vBN;
+        coff = r0.y;
+    };
+    int k = 0;
+    for (; k + U <= nloop; k += U) {
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            step(k + u, Rq[u % RD], Kq[u % KD].v);
+            if (k + u + KD <= last) Kq[u % KD].load(tetK + KS * (int64_t)(Rq[(u + KD) % RD].x & kRingTetMask));
+            if (k + u + RD <= last) Rq[u % RD] = rr[32 * (k + u + RD + 1)];
+        }
+    }
+#pragma unroll
+    for (int u = 0; u + 1 < U; ++u) {
+        if (k + u < nloop) {
+            step(k + u, Rq[u % RD], Kq[u % KD].v);
+            if (k + u + KD <= last) Kq[u % KD].load(tetK + KS * (int64_t)(Rq[(u + KD) % RD].x & kRingTetMask));
+        }
+    }
+    bool bad = false;
+    if (valid) {
+        double F;
+        if (DIR && isdir) {
+            if (deg > 0) myRow[(hd.x >> 16) & 255u] = Real(deg);
+            const double bcr = p.dir_bc[row];
+            F = 0;
+            for (int q = 0; q < deg; ++q) F += bcr;
+        } else {
+            if (nloop > 0) {
+                // the last face: a closed ring ends on its first face
+                myRow[coff & 255u] = cP + fP;
+                myRow[(coff >> 8) & 255u] = cAP + fAP;
+                myRow[(coff >> 16) & 255u] = cBP + fBP;
+                myRow[hd.x & 255u] = accA;
+                myRow[(hd.x >> 8) & 255u] = accB;
+                myRow[(hd.x >> 16) & 255u] = accE;
+            }
+            F = (double)racc;
+            if (DIR)
+                for (int64_t q = p.dir_cptr[row]; q < p.dir_cptr[row + 1]; ++q) myRow[p.dir_coff[q]] = Real(0);
+        }
+        bad |= !isfinite(F);
+        rhs[row] = F;
+    }
+    __syncwarp();
+    const Real fin = write_out_range<Real>(sC, shift, clen, cbase, vals, p.vec_ok, lane);
+    bad |= !isfinite(fin);
+    if (bad) atomicExch(status, ANIGPU_ERR_NONFINITE);
+    pdl_launch_dependents();
+}
+
+// The edge walk that also builds the vertex rows by symmetry (used for FP64): every value of this
+// row that belongs to a vertex column (A, B, the ring vertices) is also stored at its transposed
+// position in that vertex row, together with the vertex-vertex entry (A, B); Dirichlet edge rows
+// walk too (for that entry) but write only their diagonal here.  A separate function so that the
+// plain walk above keeps its own code.
+template <typename Real, bool DIR, bool DROPCHK, bool TR = true>
+__global__ void RING_BOUNDS edge_ring_tr_kernel(RowParams p, const uint2* __restrict__ ring,
+                                            const int64_t* __restrict__ woff, const Real* __restrict__ tetK,
+                                            Real* __restrict__ vals, double* __restrict__ rhs,
+                                            int* __restrict__ status, const int32_t* __restrict__ tpos,
+                                               const int64_t* __restrict__ twoff, int64_t tstride) {
     using Sm = RowSmem<Real, 10, 2, false>;
     constexpr int KS = 8;
     constexpr int VEC = Sm::VEC;
@@ -884,7 +1049,7 @@ __global__ void RING_BOUNDS edge_ring_kernel(RowParams p, const uint2* __restric
     constexpr int KD = RING_KD, RD = RING_RD;
     static_assert(RD > KD, "records must run ahead of the blocks they address");
     // TR: transposed positions, (N,E) of incidence j in slot 5 + j, prefetched like the records
-    const int32_t* tr = TR ? p.tpos + (p.tstride > 0 ? wg * p.tstride : p.twoff[wg]) + lane : nullptr;
+    const int32_t* tr = TR ? tpos + (tstride > 0 ? wg * tstride : twoff[wg]) + lane : nullptr;
     int32_t Tq[TR ? RD : 1];
     int32_t tprev = 0;  // (N,E) of the previous incidence: where this step's completed face goes
     Real tf0 = Real(0), accAB = Real(0);
@@ -2259,11 +2424,15 @@ template <typename Real, bool DIR, bool DROPCHK, bool TR = false>
 static int launch_ring_t(anigpu_ctx* h, const RowParams& p, void* vals, double* rhs, cudaStream_t st) {
     const int warps = h->row_warps == 1 ? 1 : 2;
     const size_t smem = RowSmem<Real, 10, 2, false>::total(p.cap, warps);
-    auto kern = edge_ring_kernel<Real, DIR, DROPCHK, TR>;
+    auto kern = edge_ring_kernel<Real, DIR, DROPCHK>;
     static int smem_set[64] = {};
     const int slot = h->device >= 0 && h->device < 64 ? h->device : 0;
     if ((int)smem > smem_set[slot]) {
-        ANI_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        if constexpr (TR)
+            ANI_CUDA(h, cudaFuncSetAttribute(edge_ring_tr_kernel<Real, DIR, DROPCHK>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        else
+            ANI_CUDA(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         smem_set[slot] = (int)smem;
     }
     // launched right behind the per-tet kernel on the same stream (h->asm_pdl): a programmatic
@@ -2280,13 +2449,14 @@ static int launch_ring_t(anigpu_ctx* h, const RowParams& p, void* vals, double* 
     cfg.numAttrs = h->asm_pdl ? 1 : 0;
     RowParams q = p;
     q.wstride = h->ring_ws;
-    if (TR) {
-        q.tpos = h->tpos;
-        q.twoff = h->tpos_woff;
-        q.tstride = h->tpos_ws;
-    }
-    ANI_CUDA(h, cudaLaunchKernelEx(&cfg, kern, q, (const uint2*)h->ring, (const int64_t*)h->ring_woff,
-                                   (const Real*)h->tetdata, (Real*)vals, rhs, h->d_status));
+    if constexpr (TR)
+        ANI_CUDA(h, cudaLaunchKernelEx(&cfg, edge_ring_tr_kernel<Real, DIR, DROPCHK>, q, (const uint2*)h->ring,
+                                       (const int64_t*)h->ring_woff, (const Real*)h->tetdata, (Real*)vals, rhs,
+                                       h->d_status, (const int32_t*)h->tpos, (const int64_t*)h->tpos_woff,
+                                       h->tpos_ws));
+    else
+        ANI_CUDA(h, cudaLaunchKernelEx(&cfg, kern, q, (const uint2*)h->ring, (const int64_t*)h->ring_woff,
+                                       (const Real*)h->tetdata, (Real*)vals, rhs, h->d_status));
     ANI_LAUNCHED(h);
     return ANIGPU_OK;
 }
