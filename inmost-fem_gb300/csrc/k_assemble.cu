@@ -801,6 +801,11 @@ constexpr int kRingMax = 32;  // incident tets of an edge that the ring build ta
 #ifndef ASM_SEQ
 #define ASM_SEQ 1
 #endif
+// the plain edge walk writes every column of its row (checked when the rings are built), so its
+// row buffer is not zeroed first; Dirichlet rows (no walk) zero their own row (1)
+#ifndef RING_NOZERO
+#define RING_NOZERO 1
+#endif
 // the lane-interleaved layouts end in kRecPad slots of padding, so that a walk's first records
 // are loaded without waiting for the row's incidence count (1): slots past the lane's own records
 // belong to other lanes or to the padding and are never used; or only the lane's own (0)
@@ -852,7 +857,7 @@ __global__ void RING_BOUNDS edge_ring_kernel(RowParams p, const uint2* __restric
     const int shift = (int)(cbase & (VEC - 1));
     unsigned char* wbase = smem_raw + Sm::warp_bytes(p.cap) * warp;
     Real* sC = reinterpret_cast<Real*>(wbase) + shift;
-    {
+    if (!RING_NOZERO) {
         const int nvec = (shift + clen + VEC - 1) / VEC;
         int4* z = reinterpret_cast<int4*>(wbase);
         for (int k = lane; k < nvec; k += 32) z[k] = make_int4(0, 0, 0, 0);
@@ -970,6 +975,10 @@ __global__ void RING_BOUNDS edge_ring_kernel(RowParams p, const uint2* __restric
     if (valid) {
         double F;
         if (DIR && isdir) {
+            if (RING_NOZERO) {  // the walk did not run: the row is its diagonal alone
+                const int len = (int)(p.rowptr[row + 1] - p.rowptr[row]);
+                for (int q = 0; q < len; ++q) myRow[q] = Real(0);
+            }
             if (deg > 0) myRow[(hd.x >> 16) & 255u] = Real(deg);
             const double bcr = p.dir_bc[row];
             F = 0;
@@ -1477,7 +1486,8 @@ __device__ __forceinline__ uint32_t rec_off(const ScatterRec& r, int c) {
 // more than kRingMax tets, an inconsistent record) sets *fail, and the mesh keeps the record gather
 __global__ void ring_build_kernel(int64_t rb, int64_t re, const int64_t* __restrict__ inc_ptr,
                                   const ScatterRec* __restrict__ recs, const int32_t* __restrict__ tets,
-                                  const int64_t* __restrict__ woff, uint2* __restrict__ ring, int* __restrict__ fail) {
+                                  const int64_t* __restrict__ rowptr, const int64_t* __restrict__ woff,
+                                  uint2* __restrict__ ring, int* __restrict__ fail) {
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t r = rb + t;
     if (r >= re) return;
@@ -1536,6 +1546,13 @@ __global__ void ring_build_kernel(int64_t rb, int64_t re, const int64_t* __restr
         }
     const bool closed = ones == 0;
     if (!(ones == 0 || ones == 2) || (closed && deg < 3)) {
+        atomicOr(fail, 1);
+        return;
+    }
+    // the walk writes every column of the row: A, B, the edge, three per ring vertex (the vertex and
+    // its edges to A and B) and one per tet (the opposite edge)
+    const int nverts = closed ? deg : deg + 1;
+    if (rowptr[r + 1] - rowptr[r] != 3 + 3 * nverts + deg) {
         atomicOr(fail, 1);
         return;
     }
@@ -2712,8 +2729,8 @@ int setup_row_layouts(anigpu_ctx* h) {
     int* fail = nullptr;
     ANI_CUDA(h, cudaMallocAsync((void**)&fail, sizeof(int), s));
     ANI_CUDA(h, cudaMemsetAsync(fail, 0, sizeof(int), s));
-    ring_build_kernel<<<grid_for(n, 128), 128, 0, s>>>(rb, re, h->inc_ptr, h->recs, h->tets, h->ring_woff, h->ring,
-                                                       fail);
+    ring_build_kernel<<<grid_for(n, 128), 128, 0, s>>>(rb, re, h->inc_ptr, h->recs, h->tets, h->rowptr_s,
+                                                       h->ring_woff, h->ring, fail);
     ANI_LAUNCHED(h);
     int hf = 0;
     ANI_CUDA(h, cudaMemcpyAsync(&hf, fail, sizeof(int), cudaMemcpyDeviceToHost, s));
