@@ -2105,7 +2105,7 @@ __global__ void __launch_bounds__(64) vec_edge_ring_kernel(RowParams p, int64_t 
     const size_t chunk_bytes = (((size_t)32 * 3 * p.cap + VEC) * sizeof(Real) + 15) / 16 * 16;
     unsigned char* wbase = smem_raw + chunk_bytes * warp;
     Real* sC = reinterpret_cast<Real*>(wbase) + shift;
-    {
+    if (!RING_NOZERO) {  // every column is written by the walk (or, in a Dirichlet row, cleared below)
         const int nvec = (shift + clen + VEC - 1) / VEC;
         int4* z = reinterpret_cast<int4*>(wbase);
         for (int k = lane; k < nvec; k += 32) z[k] = make_int4(0, 0, 0, 0);
@@ -2219,6 +2219,8 @@ __global__ void __launch_bounds__(64) vec_edge_ring_kernel(RowParams p, int64_t 
     if (valid) {
         double F;
         if (DIR && isdir) {
+            if (RING_NOZERO)
+                for (int q = 0; q < 3 * L; ++q) myRow[q] = Real(0);
             if (deg > 0) myRow[c * L + (int)((hd.x >> 16) & 255u)] = Real(deg);  // diagonal: the edge itself
             const double bcr = p.bcnz ? p.dir_bc[R] : 0.0;
             F = 0;
