@@ -271,3 +271,30 @@ def test_general_enumeration_perm_closed_form():
         per, off = general_blocks(xyz, t, space)
         for etype in range(6):
             assert np.array_equal(general_enumeration_perm(per, off, etype), np.arange(off[4]))
+
+
+@pytest.mark.parametrize("n,perturb", [(3, 0.0), (4, 0.2)])
+def test_p2_edge_row_length_matches_its_ring(restated, n, perturb):
+    """The invariant the GPU's ring walk relies on to skip clearing its row buffer: in the
+    topological P2 template an edge row (A, B) holds exactly A, B, the edge itself, three columns
+    per ring vertex (the vertex and its edges to A and B) and one per incident tet (the opposite
+    edge) -- 3 + 3 V + n entries for V ring vertices and n tets."""
+    from anigpu import meshgen
+    xyz, tets = meshgen.kuhn_cube(n, perturb=perturb, seed=9)
+    t = restated.orient(xyz, tets)
+    nv = xyz.shape[0]
+    ne, te = restated.edges(nv, t)
+    ndof, edofs = restated.element_dofs(2, nv, ne, t, te)
+    rp, col = restated.csr_template(ndof, edofs)
+    EI, EJ = (0, 0, 0, 1, 1, 2), (1, 2, 3, 2, 3, 3)
+    tets_of, ring = {}, {}
+    for k in range(t.shape[0]):
+        for le in range(6):
+            e = int(te[k, le])
+            a, b = t[k, EI[le]], t[k, EJ[le]]
+            others = [int(v) for v in t[k] if v != a and v != b]
+            tets_of[e] = tets_of.get(e, 0) + 1
+            ring.setdefault(e, set()).update(others)
+    for e, ntet in tets_of.items():
+        r = nv + e
+        assert rp[r + 1] - rp[r] == 3 + 3 * len(ring[e]) + ntet, e
